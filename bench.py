@@ -1,0 +1,289 @@
+"""Benchmark of the closest-hit hot path (reference KDTree::intersect over a batch).
+
+Workload: the 4,096,036-triangle scene (Cornell box + 200 displaced icospheres,
+subdivision 5, seed 1) and a 2^24-ray batch (origins uniform in the 5.56^3 room,
+directions uniform on the sphere, seed 7). One step = one closest-hit pass over the
+whole batch. Synthetic seeded data stand in for the reference's (unshipped) scenes.
+
+  value : Mrays/s with rays resident in HBM (device entry point), CUDA events on the
+          launching stream, L2 flushed between steps (rays are 512 MiB > L2 too).
+  e2e   : Mrays/s through the host-buffer C-ABI call rx_trace_closest from pinned host
+          memory, host<->device copies inside the timed region.
+  cpu_baseline : the oracle's CPU restatement of the reference traversal on the host
+          cores, on a bounded sample of the same batch.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_RAYS = 1 << 24  # default batch; --rays shrinks it for profiler captures
+N_SPHERES, SUBDIV, SCENE_SEED, RAY_SEED = 200, 5, 1, 7
+METRIC = "closest-hit Mrays/s (2^24-ray batch, 4.1M-triangle scene)"
+UNIT = "Mrays/s"
+WORKLOAD = "hit_batch_2^24_rays_cornell+200_icospheres_4096036_tris"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 2 + k and r[2 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_workload(rank: int):
+    from renderx_gb300 import scenes
+    sc = scenes.sphere_field(N_SPHERES, SUBDIV, seed=SCENE_SEED)
+    f = sc.flatten()
+    o, d = scenes.hit_rays(N_RAYS, seed=RAY_SEED + rank)  # N_RAYS may be reset by --rays
+    return sc, f, o, d
+
+
+def cpu_baseline(f, o, d, budget_s: float = 12.0):
+    """Times the oracle (CPU restatement of the reference traversal) on a bounded
+    sample of the batch with every host thread."""
+    import oracle
+    T = oracle.RefTree(f["verts"], f["tris"])
+    threads = os.cpu_count() or 1
+    n = 64
+    t0 = time.perf_counter()
+    T.trace(o[:n], d[:n], threads=threads)
+    dt = time.perf_counter() - t0
+    m = int(max(n, min(1 << 14, n * budget_s / max(dt, 1e-3))))
+    m = max(threads, (m // threads) * threads)
+    t0 = time.perf_counter()
+    T.trace(o[n:n + m], d[n:n + m], threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": m / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{m} rays of the 2^24 batch (rays {n}..{n + m - 1}), oracle restatement of "
+                      f"KDTree::intersect, {threads} threads, {dt:.1f} s"}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    _, f, o, d = make_workload(0)
+    times = []
+    cb = None
+    for s in range(args.warmup + args.steps):
+        cb = cpu_baseline(f, o, d, budget_s=max(2.0, 20.0 / max(1, args.steps)))
+        if s >= args.warmup:
+            times.append(cb["value"])
+    v = statistics.median(times)
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": N_RAYS / (v * 1e6) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "rays": N_RAYS, "triangles": 4096036, "sample": cb["sample"]},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import renderx_gb300 as rx
+
+    sc, f, o, d = make_workload(rank)
+    ctx = rx.Context(local)
+    ctx.set_geometry(f["verts"], f["tris"], f["tri_obj"], f["tri_local"])
+    t0 = time.perf_counter()
+    ctx.build_accel()
+    build_s = time.perf_counter() - t0
+    st = ctx.stats()
+    host_rays = rx.rays_to_array(o, d)
+    d_rays = torch.from_numpy(host_rays).cuda()
+    n = N_RAYS
+    d_tid = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_dist = torch.empty(n, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MiB > 129 MB L2
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+
+    for _ in range(args.warmup):
+        ctx.trace_closest_device(d_rays, n, d_tid, d_dist, sh)
+    torch.cuda.synchronize()
+
+    # device-resident timing: events around each step, L2 flushed between steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            ev[k][0].record(stream)
+            ctx.trace_closest_device(d_rays, n, d_tid, d_dist, sh)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_ms = sum(step_ms)
+    if dist:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    ms_per_step = t_ms / args.steps
+    value = ws * n / (ms_per_step * 1e-3) / 1e6
+    clocks = clk.summary()
+
+    # end to end through the host-buffer C-ABI call, pinned host memory
+    if args.skip_e2e:
+        e2e, same = None, None
+    else:
+        e2e, same = end_to_end(ctx, host_rays, d_tid, args, dist, ws, n)
+
+    if rank == 0:
+        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def end_to_end(ctx, host_rays, d_tid, args, dist, ws, n):
+    import torch
+    pin_rays = torch.from_numpy(host_rays).pin_memory()
+    pin_tid = torch.empty(n, dtype=torch.int32).pin_memory()
+    pin_dist = torch.empty(n, dtype=torch.float32).pin_memory()
+    r_np, t_np, d_np = pin_rays.numpy(), pin_tid.numpy(), pin_dist.numpy()
+    ctx.trace_closest_rays(r_np, t_np, d_np)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.trace_closest_rays(r_np, t_np, d_np)
+    torch.cuda.synchronize()
+    e_s = time.perf_counter() - e0
+    if dist:
+        tt = torch.tensor([e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e_s = float(tt.item())
+    e2e = ws * n * args.steps / e_s / 1e6
+    same = bool(np.array_equal(t_np, d_tid.cpu().numpy()))
+    return e2e, same
+
+
+def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d):
+    if True:
+        peak, peak_kind = load_peaks()
+        bytes_alg = 40 * n + 48 * st["triangles"] + 64 * st["bvh_nodes"]
+        achieved = bytes_alg / (ms_per_step * 1e-3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "hit_traffic.json")
+        if os.path.exists(tp):
+            with open(tp) as fh:
+                traffic = json.load(fh).get("dram_bytes_per_launch")
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "rays": n, "triangles": st["triangles"],
+                           "bvh_nodes": st["bvh_nodes"], "ref_nodes": st["ref_nodes"],
+                           "l2": "flushed between steps (256 MiB write); rays 512 MiB > L2",
+                           "parallelism": f"replicas x{ws}", "accel_build_s": round(build_s, 2)},
+                "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 32,
+                                                 "d2h_bytes_per_step": n * 8, "matches_device_path": same},
+                "gpu_launches": 2 * args.steps,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                             "algorithmic_bytes_per_launch": bytes_alg},
+                "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms], "wall_s": wall}
+        if not args.skip_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(f, o, d)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="batch size (profiler captures use a smaller one)")
+    args = ap.parse_args()
+    globals()["N_RAYS"] = args.rays
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

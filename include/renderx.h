@@ -1,0 +1,129 @@
+/*
+ * renderx.h - C ABI of the GB300 light-transport library (librenderx_gb300.so).
+ *
+ * Plain C types only: pointers, sizes, POD structs. Every call returns an rx_status;
+ * rx_last_error() gives the message of the last failure on a context. A context owns
+ * one CUDA stream on one device; calls on one context are not thread-safe, calls on
+ * different contexts are.
+ *
+ * Each entry point names the reference interface it replaces (reference file:line).
+ */
+#ifndef RENDERX_H
+#define RENDERX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rx_context rx_context;
+
+typedef enum rx_status {
+  RX_OK = 0,
+  RX_ERR_INVALID = 1,     /* bad argument */
+  RX_ERR_CUDA = 2,        /* CUDA runtime error */
+  RX_ERR_OOM = 3,         /* device or host allocation failed */
+  RX_ERR_STATE = 4,       /* call out of order (e.g. trace before build) */
+  RX_ERR_TIMEOUT = 5,     /* a bounded device loop ran out of iterations */
+  RX_ERR_UNSUPPORTED = 6
+} rx_status;
+
+/* Material codes (reference ConfigManager.cpp:25-164 <type> values). */
+enum {
+  RX_MAT_DIFFUSE = 0,     /* SceneDiffuseObject / DiffuseMaterial */
+  RX_MAT_GLOSSY = 1,      /* SceneGlossyObject / GlossyMaterial (Phong lobe) */
+  RX_MAT_REFRACTIVE = 2,  /* SceneRefractiveObject / RefractiveMaterial */
+  RX_MAT_EMISSIVE = 3,    /* SceneEmissiveObject */
+  RX_MAT_PHONG = 4,       /* ScenePhongObject: glossy + diffuse, lobe picked at random */
+  RX_MAT_REFLECTIVE = 5,  /* SceneReflectiveObject: RefractiveMaterial with coeff -1 */
+  RX_MAT_VPM = 6          /* SceneVPMObject: dielectric boundary + homogeneous medium */
+};
+
+/* One scene object: its triangle range in the global triangle list and its material.
+ * Mirrors the SceneObject subclasses' fields set by ConfigManager::generateSceneObject
+ * (reference ConfigManager.cpp:25-164). */
+typedef struct rx_object {
+  uint32_t tri_begin, tri_count;  /* global triangle range (object-major order) */
+  uint32_t material;              /* RX_MAT_* */
+  uint32_t has_vertex_normals;    /* 1: shading normals interpolate vertex normals */
+  float color[3];                 /* diffuse albedo / glossy colour / emission / surface colour */
+  float coeff;                    /* glossy exponent */
+  float diffuse_color[3];         /* Phong diffuse component */
+  float ior;                      /* refractive index (<0: mirror) */
+  float sigma_s[3], sigma_a[3];   /* homogeneous medium */
+  float g;                        /* HG asymmetry */
+  float decay[3];                 /* RefractiveMaterial decayColor (per unit length) */
+} rx_object;
+
+typedef struct rx_build_options {
+  int32_t split_policy;   /* 0: reference as built by GCC/libstdc++ (x axis always);
+                             1: best-ratio axis (libc++/MSVC builds of the reference) */
+  int32_t leaf_size;      /* BVH leaf size (1..8), 0 = default 4 */
+  int32_t host_threads;   /* 0 = all cores */
+  int32_t reserved;
+} rx_build_options;
+
+/* A ray: origin and direction, 32 bytes (w components ignored). */
+typedef struct rx_ray {
+  float ox, oy, oz, ow;
+  float dx, dy, dz, dw;
+} rx_ray;
+
+/* ---- context ------------------------------------------------------------------- */
+/* Replaces the process-global GPU state of IntersectionGPU::init
+ * (reference src/IntersectionGPU.cpp:16-44). */
+rx_status rx_create(rx_context** out, int device);
+void rx_destroy(rx_context* ctx);
+const char* rx_last_error(const rx_context* ctx);
+/* Build identification string (kernels, architecture). */
+const char* rx_version(void);
+
+/* ---- scene --------------------------------------------------------------------- */
+/* Scene::buildKDTree's input (reference src/Scene.cpp:248-285): world-space vertices
+ * of all objects concatenated, triangle vertex-index triples (global), and per
+ * triangle its ObjSourceInformation {objID, triangleID} (reference include/Scene.h:13-17).
+ * vnormals_xyz may be NULL (face normals everywhere). */
+rx_status rx_scene_set_geometry(rx_context* ctx, const float* verts_xyz, uint32_t nv, const uint32_t* tri_vidx,
+                                uint32_t nt, const uint32_t* tri_obj, const uint32_t* tri_local,
+                                const float* vnormals_xyz);
+/* Materials per object (reference ConfigManager.cpp:25-164 generateSceneObject). */
+rx_status rx_scene_set_objects(rx_context* ctx, const rx_object* objs, uint32_t nobj);
+/* KDTree::build (reference src/KDTree.cpp:303-319, include/KDTree.h:54): builds the
+ * reference-order tree (tie ranks, visibility boxes) and the device BVH, uploads both. */
+rx_status rx_build_accel(rx_context* ctx, const rx_build_options* opts);
+/* Tree statistics: [0] BVH nodes, [1] BVH depth, [2] reference nodes,
+ * [3] reference depth, [4] triangles, [5] reference leaves. */
+rx_status rx_accel_stats(rx_context* ctx, int64_t out[8]);
+/* KDTree::serializeForGPU (reference include/KDTree.h:56, src/KDTree.cpp:419-456) of
+ * the reference-order tree this library builds, host only (no device, no context).
+ * nodes12: 12 floats per node (parent, rightChild, leafStart, leafEnd, min.xyz, 0,
+ * max.xyz, 0); leaf_tid: triangle id per leaf slot. Pass NULL outputs to query
+ * *num_nodes and *num_leaf_tris; with outputs, their capacities are read from the same
+ * two counters and must suffice. */
+rx_status rx_reftree_serialize(const float* verts_xyz, uint32_t nv, const uint32_t* tri_vidx, uint32_t nt,
+                               int32_t split_policy, float* nodes12, uint32_t* num_nodes, float* leaf_tid,
+                               uint32_t* num_leaf_tris);
+
+/* ---- closest hit --------------------------------------------------------------- */
+/* KDTree::intersect(ray, triangleID, NULL) (reference include/KDTree.h:50,
+ * src/KDTree.cpp:408-412) over a batch, host buffers: out_tid[i] = global triangle id
+ * or -1, out_dist[i] = hit distance or -1. Copies are pipelined with the kernels. */
+rx_status rx_trace_closest(rx_context* ctx, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist);
+/* Same on device buffers (no copies), enqueued on `stream` (a cudaStream_t, NULL for
+ * the context's stream). */
+rx_status rx_trace_closest_device(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
+                                  float* d_dist, void* stream);
+/* Same semantics, without the BVH: walks every triangle the reference tree lets the
+ * ray see, in the reference's own order (slow; a consistency check on small scenes). */
+rx_status rx_trace_closest_reforder_device(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
+                                           float* d_dist, void* stream);
+/* Rays whose lazy winner failed the reference-visibility check and were re-traced
+ * exactly, counted since the last reset (diagnostic). */
+rx_status rx_trace_counters(rx_context* ctx, uint64_t out[4], int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RENDERX_H */

@@ -1,0 +1,111 @@
+"""ORACLE — test infrastructure only.
+
+CPU restatement of the reference's light-transport path (reference src/KDTree.cpp,
+src/PathTracer.cpp and the material code), compiled from ``oracle/*.cpp`` into
+``oracle/liboracle.so``. Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg may import this package; it is the checker, never the
+thing measured or shipped.
+
+Parity pins: ``tests/test_oracle_golden.py`` checks this restatement against golden
+fixtures produced by the reference's own code compiled from its sources
+(``oracle/ref/``, script ``tests/golden/make_golden.py``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+SPLIT_GCC = 0   # reference as built by GCC/libstdc++: always splits on x
+SPLIT_BEST = 1  # reference's intended best-axis choice (libc++/MSVC builds)
+
+
+def build(force: bool = False) -> str:
+    path = os.path.join(_HERE, "liboracle.so")
+    srcs = [os.path.join(_HERE, f) for f in os.listdir(_HERE) if f.endswith(".cpp")]
+    if force or not os.path.exists(path) or any(os.path.getmtime(s) > os.path.getmtime(path) for s in srcs):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B"], check=True)
+    return path
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        L = ctypes.CDLL(build())
+        P = ctypes.c_void_p
+        L.rxo_tree_build.restype = P
+        L.rxo_tree_build.argtypes = [P, ctypes.c_uint32, P, ctypes.c_uint32, ctypes.c_int]
+        L.rxo_tree_free.argtypes = [P]
+        for f in ("rxo_tree_num_nodes", "rxo_tree_num_leaf_tris"):
+            getattr(L, f).restype = ctypes.c_uint32
+            getattr(L, f).argtypes = [P]
+        L.rxo_tree_max_depth.restype = ctypes.c_int
+        L.rxo_tree_max_depth.argtypes = [P]
+        L.rxo_tree_serialize.argtypes = [P, P, P]
+        L.rxo_trace.argtypes = [P, P, ctypes.c_uint32, P, P, ctypes.c_int]
+        L.rxo_box_test.restype = ctypes.c_float
+        L.rxo_box_test.argtypes = [P, P, P, P]
+        L.rxo_num_threads.restype = ctypes.c_int
+        _LIB = L
+    return _LIB
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class RefTree:
+    """The reference's triangle tree, restated (KDTree::build / splitBest)."""
+
+    def __init__(self, verts: np.ndarray, tris: np.ndarray, policy: int = SPLIT_GCC):
+        self._v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        self._t = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+        self.h = lib().rxo_tree_build(_p(self._v), len(self._v), _p(self._t), len(self._t), policy)
+        if not self.h:
+            raise ValueError("empty scene")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().rxo_tree_free(self.h)
+            self.h = None
+
+    @property
+    def num_nodes(self) -> int:
+        return lib().rxo_tree_num_nodes(self.h)
+
+    @property
+    def max_depth(self) -> int:
+        return lib().rxo_tree_max_depth(self.h)
+
+    def serialize(self):
+        """(nodes (n,12) f32, leaf_tid (m,) f32) in serializeForGPU's layout."""
+        n = self.num_nodes
+        m = lib().rxo_tree_num_leaf_tris(self.h)
+        nodes = np.zeros((n, 12), np.float32)
+        leaf = np.zeros(m, np.float32)
+        lib().rxo_tree_serialize(self.h, _p(nodes), _p(leaf))
+        return nodes, leaf
+
+    def trace(self, origins: np.ndarray, dirs: np.ndarray, threads: int = 0):
+        """Closest hit per ray: (tid int32 with -1 on miss, dist float32)."""
+        r = np.ascontiguousarray(np.concatenate([np.asarray(origins, np.float32).reshape(-1, 3),
+                                                 np.asarray(dirs, np.float32).reshape(-1, 3)], 1))
+        n = len(r)
+        tid = np.empty(n, np.int32)
+        dist = np.empty(n, np.float32)
+        lib().rxo_trace(self.h, _p(r), n, _p(tid), _p(dist), threads)
+        return tid, dist
+
+
+def box_test(mn, mx, o, d) -> float:
+    a = [np.ascontiguousarray(x, np.float32) for x in (mn, mx, o, d)]
+    return lib().rxo_box_test(*[_p(x) for x in a])
+
+
+def num_threads() -> int:
+    return lib().rxo_num_threads()

@@ -1,0 +1,189 @@
+"""renderx_gb300 — GB300-native (sm_103a) light-transport hot path of RenderX.
+
+The compute lives in librenderx_gb300.so (CUDA kernels behind the C ABI of
+include/renderx.h); this package is a thin host-side mirror of the reference's
+interfaces for the path:
+
+* :class:`KDTree` mirrors the reference's triangle KDTree (include/KDTree.h:10-59):
+  ``vertexPositionList`` / ``triangleList``, ``build()``, ``intersect()`` (batched) and
+  ``serializeForGPU()``.
+* :class:`Context` is the C-ABI context: scene upload, accelerator build, closest-hit
+  batches on host or device buffers.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import RxError, rx_build_options, rx_object
+from . import scenes
+
+__all__ = ["Context", "KDTree", "RxError", "reftree_serialize", "scenes", "rays_to_array"]
+
+SPLIT_GCC = 0
+SPLIT_BEST = 1
+
+
+def rays_to_array(origins: np.ndarray, dirs: np.ndarray) -> np.ndarray:
+    """Packs rays into the ABI's 32-byte rx_ray records: (n, 8) float32."""
+    o = np.asarray(origins, np.float32).reshape(-1, 3)
+    d = np.asarray(dirs, np.float32).reshape(-1, 3)
+    r = np.zeros((len(o), 8), np.float32)
+    r[:, 0:3] = o
+    r[:, 4:7] = d
+    return r
+
+
+def reftree_serialize(verts: np.ndarray, tris: np.ndarray, policy: int = SPLIT_GCC):
+    """KDTree::serializeForGPU of the library's reference-order tree (host only)."""
+    L = _capi.lib()
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+    nn, nl = ctypes.c_uint32(0), ctypes.c_uint32(0)
+    _capi.check(None, L.rx_reftree_serialize(_capi.ptr(v), len(v), _capi.ptr(t), len(t), policy, None,
+                                             ctypes.byref(nn), None, ctypes.byref(nl)))
+    nodes = np.zeros((nn.value, 12), np.float32)
+    leaf = np.zeros(nl.value, np.float32)
+    _capi.check(None, L.rx_reftree_serialize(_capi.ptr(v), len(v), _capi.ptr(t), len(t), policy, _capi.ptr(nodes),
+                                             ctypes.byref(nn), _capi.ptr(leaf), ctypes.byref(nl)))
+    return nodes, leaf
+
+
+class Context:
+    """One device, one stream: rx_create / rx_destroy."""
+
+    def __init__(self, device: int = 0):
+        self._L = _capi.lib()
+        h = ctypes.c_void_p()
+        st = self._L.rx_create(ctypes.byref(h), device)
+        if st != 0:
+            raise RxError(st, f"rx_create(device={device}) failed")
+        self.h = h
+        self.num_triangles = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.rx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        _capi.check(self.h, st)
+
+    # -- scene ---------------------------------------------------------------------
+    def set_geometry(self, verts, tris, tri_obj=None, tri_local=None, normals=None):
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+        to = None if tri_obj is None else np.ascontiguousarray(tri_obj, np.uint32)
+        tl = None if tri_local is None else np.ascontiguousarray(tri_local, np.uint32)
+        n = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        self._ck(self._L.rx_scene_set_geometry(self.h, _capi.ptr(v), len(v), _capi.ptr(t), len(t), _capi.ptr(to),
+                                               _capi.ptr(tl), _capi.ptr(n)))
+        self.num_triangles = len(t)
+
+    def set_objects(self, objs):
+        arr = (rx_object * max(1, len(objs)))(*objs)
+        self._ck(self._L.rx_scene_set_objects(self.h, ctypes.cast(arr, ctypes.c_void_p), len(objs)))
+
+    def set_scene(self, scene: "scenes.Scene"):
+        """Uploads a scenes.Scene: geometry (object-major, as Scene::buildKDTree) and
+        the per-object material table."""
+        f = scene.flatten()
+        self.set_geometry(f["verts"], f["tris"], f["tri_obj"], f["tri_local"], f["normals"])
+        self.set_objects(objects_from_scene(scene))
+        return f
+
+    def build_accel(self, split_policy: int = SPLIT_GCC, leaf_size: int = 4, host_threads: int = 0):
+        o = rx_build_options(split_policy, leaf_size, host_threads, 0)
+        self._ck(self._L.rx_build_accel(self.h, ctypes.byref(o)))
+
+    def stats(self) -> dict:
+        out = np.zeros(8, np.int64)
+        self._ck(self._L.rx_accel_stats(self.h, _capi.ptr(out)))
+        return dict(bvh_nodes=int(out[0]), bvh_depth=int(out[1]), ref_nodes=int(out[2]), ref_depth=int(out[3]),
+                    triangles=int(out[4]), ref_leaves=int(out[5]))
+
+    # -- closest hit -----------------------------------------------------------------
+    def trace_closest(self, origins, dirs):
+        """KDTree::intersect over a batch, host buffers: (tid int32, dist float32)."""
+        r = rays_to_array(origins, dirs)
+        n = len(r)
+        tid = np.empty(n, np.int32)
+        dist = np.empty(n, np.float32)
+        self._ck(self._L.rx_trace_closest(self.h, _capi.ptr(r), n, _capi.ptr(tid), _capi.ptr(dist)))
+        return tid, dist
+
+    def trace_closest_rays(self, rays: np.ndarray, tid: np.ndarray, dist: np.ndarray):
+        """Host-buffer call on pre-packed rx_ray records (e.g. pinned memory)."""
+        self._ck(self._L.rx_trace_closest(self.h, _capi.ptr(rays), len(rays), _capi.ptr(tid), _capi.ptr(dist)))
+
+    def trace_closest_device(self, d_rays, n: int, d_tid, d_dist, stream=None):
+        """Device buffers. ``stream``: None = the context's stream, otherwise a
+        cudaStream_t handle (0 = the legacy default stream, e.g. torch's default)."""
+        self._ck(self._L.rx_trace_closest_device(self.h, _capi.ptr(d_rays), n, _capi.ptr(d_tid), _capi.ptr(d_dist),
+                                                 _capi.stream_arg(stream)))
+
+    def trace_reforder_device(self, d_rays, n: int, d_tid, d_dist, stream=None):
+        self._ck(self._L.rx_trace_closest_reforder_device(self.h, _capi.ptr(d_rays), n, _capi.ptr(d_tid),
+                                                          _capi.ptr(d_dist), _capi.stream_arg(stream)))
+
+    def counters(self, reset: bool = False) -> dict:
+        out = np.zeros(4, np.uint64)
+        self._ck(self._L.rx_trace_counters(self.h, _capi.ptr(out), int(reset)))
+        return dict(exact_box_tests=int(out[1]), eager_retraces=int(out[2]), errors=int(out[3]))
+
+
+def objects_from_scene(scene: "scenes.Scene"):
+    objs = []
+    off = 0
+    for o in scene.objects:
+        m = o.material
+        ro = rx_object()
+        ro.tri_begin, ro.tri_count, ro.material = off, len(o.tris), m.kind
+        ro.has_vertex_normals = 0 if o.normals is None else 1
+        ro.color[:] = m.color
+        ro.coeff = m.coeff
+        ro.diffuse_color[:] = m.diffuse_color
+        ro.ior = m.ior
+        ro.sigma_s[:] = m.sigma_s
+        ro.sigma_a[:] = m.sigma_a
+        ro.g = m.g
+        ro.decay[:] = m.decay
+        objs.append(ro)
+        off += len(o.tris)
+    return objs
+
+
+class KDTree:
+    """Host mirror of the reference's KDTree (include/KDTree.h:10-59) backed by the GPU.
+
+    ``vertexPositionList`` (n,3) and ``triangleList`` (m,3) are filled by the caller,
+    ``build()`` uploads and builds, ``intersect(origins, dirs)`` returns per ray
+    ``(dist, triangleID)`` with dist = -1 on a miss (KDTree.h:50)."""
+
+    def __init__(self, device: int = 0, split_policy: int = SPLIT_GCC):
+        self.vertexPositionList = np.zeros((0, 3), np.float32)
+        self.triangleList = np.zeros((0, 3), np.uint32)
+        self.split_policy = split_policy
+        self._ctx = Context(device)
+
+    def build(self):
+        self._ctx.set_geometry(self.vertexPositionList, self.triangleList)
+        self._ctx.build_accel(self.split_policy)
+
+    def intersect(self, origins, dirs):
+        tid, dist = self._ctx.trace_closest(origins, dirs)
+        return dist, tid
+
+    def serializeForGPU(self):
+        return reftree_serialize(self.vertexPositionList, self.triangleList, self.split_policy)

@@ -1,0 +1,103 @@
+"""ctypes binding of the C ABI in include/renderx.h (librenderx_gb300.so).
+
+There is no fallback: if the library cannot be built or loaded, every entry point
+raises. Device buffers are passed as raw CUDA pointers (e.g. ``tensor.data_ptr()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+RX_OK = 0
+STATUS = {0: "RX_OK", 1: "RX_ERR_INVALID", 2: "RX_ERR_CUDA", 3: "RX_ERR_OOM", 4: "RX_ERR_STATE",
+          5: "RX_ERR_TIMEOUT", 6: "RX_ERR_UNSUPPORTED"}
+
+
+class RxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class rx_object(ctypes.Structure):
+    _fields_ = [("tri_begin", ctypes.c_uint32), ("tri_count", ctypes.c_uint32), ("material", ctypes.c_uint32),
+                ("has_vertex_normals", ctypes.c_uint32), ("color", ctypes.c_float * 3), ("coeff", ctypes.c_float),
+                ("diffuse_color", ctypes.c_float * 3), ("ior", ctypes.c_float), ("sigma_s", ctypes.c_float * 3),
+                ("sigma_a", ctypes.c_float * 3), ("g", ctypes.c_float), ("decay", ctypes.c_float * 3)]
+
+
+class rx_build_options(ctypes.Structure):
+    _fields_ = [("split_policy", ctypes.c_int32), ("leaf_size", ctypes.c_int32), ("host_threads", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+_LIB = None
+
+# (name, restype, argtypes) of every exported entry point of include/renderx.h
+P, U32, I32, S = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int
+SIGNATURES = [
+    ("rx_create", S, [ctypes.POINTER(P), S]),
+    ("rx_destroy", None, [P]),
+    ("rx_last_error", ctypes.c_char_p, [P]),
+    ("rx_version", ctypes.c_char_p, []),
+    ("rx_scene_set_geometry", S, [P, P, U32, P, U32, P, P, P]),
+    ("rx_scene_set_objects", S, [P, P, U32]),
+    ("rx_build_accel", S, [P, P]),
+    ("rx_accel_stats", S, [P, P]),
+    ("rx_reftree_serialize", S, [P, U32, P, U32, I32, P, P, P, P]),
+    ("rx_trace_closest", S, [P, P, U32, P, P]),
+    ("rx_trace_closest_device", S, [P, P, U32, P, P, P]),
+    ("rx_trace_closest_reforder_device", S, [P, P, U32, P, P, P]),
+    ("rx_trace_counters", S, [P, P, S]),
+]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Builds (when sources changed) and loads the library; raises on failure."""
+    global _LIB
+    if _LIB is None:
+        path = _build.build()
+        L = ctypes.CDLL(path, mode=ctypes.RTLD_GLOBAL)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def ptr(a) -> ctypes.c_void_p:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(ctypes.c_void_p)
+    if isinstance(a, int):
+        return ctypes.c_void_p(a)
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    raise TypeError(type(a))
+
+
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
+
+
+def stream_arg(stream):
+    """None -> NULL (the context's own stream); a handle -> that stream, where handle 0
+    (the legacy default stream, torch's default) is passed as cudaStreamLegacy."""
+    if stream is None:
+        return None
+    return ctypes.c_void_p(int(stream) or CUDA_STREAM_LEGACY)
+
+
+def check(ctx, status: int):
+    if status != RX_OK:
+        msg = lib().rx_last_error(ctx).decode() if ctx else ""
+        raise RxError(status, msg)

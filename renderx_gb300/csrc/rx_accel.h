@@ -1,0 +1,57 @@
+// Host-side acceleration structures for the closest-hit path.
+//
+// Two trees are built over the same triangles:
+//  * RefOrder: the reference's own triangle tree (reference src/KDTree.cpp:202-319,
+//    splitBest + build), rebuilt exactly. It is never traversed on the GPU; it
+//    supplies (a) the rank that breaks equal-distance ties the way the reference's
+//    recursive traversal does (KDTree.cpp:368-406: right child wins ties, first
+//    triangle in a leaf wins) and (b) the node boxes whose reference box test
+//    (KDTree.cpp:107-125, no epsilon) decides whether the reference can see a
+//    triangle at all.
+//  * Bvh: a binned-SAH bounding volume hierarchy with padded boxes, the structure the
+//    GPU actually walks.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace rx {
+
+struct RefNodeHost {
+  float mn[3], mx[3];
+  int32_t parent;   // -1 at the root
+  int32_t left, right;  // -1 for leaves
+  uint32_t tri_begin, tri_end;  // leaves: range in RefOrder::tri_order
+};
+
+struct RefOrder {
+  std::vector<RefNodeHost> nodes;   // DFS pre-order, left first
+  std::vector<uint32_t> tri_order;  // triangle ids, leaves in DFS order
+  std::vector<uint32_t> leaf_node;  // leaf index (DFS order of leaves) -> node id
+  std::vector<uint32_t> tri_leaf;   // triangle id -> leaf index
+  std::vector<uint32_t> tri_pos;    // triangle id -> position in tri_order
+  int max_depth = 0;
+};
+
+// policy 0: the reference as compiled by GCC/libstdc++ (KDTree.cpp:264 `abs` binds to
+// int abs, the x axis is always kept); policy 1: best-ratio axis (libc++/MSVC builds).
+bool build_ref_order(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt, int policy,
+                     int threads, RefOrder& out);
+
+// Aila-Laine style binary node: both children's boxes live in the parent.
+struct BvhNodeHost {
+  float c0lo[3], c0hi[3], c1lo[3], c1hi[3];
+  int32_t child[2];   // >= 0: inner node id; < 0: ~leaf_first (triangle slot)
+  int32_t count[2];   // triangles in a leaf child, 0 for inner children
+};
+
+struct Bvh {
+  std::vector<BvhNodeHost> nodes;
+  std::vector<uint32_t> tri_order;  // triangle id per slot
+  int max_depth = 0;
+  int leaf_size = 4;
+};
+
+bool build_bvh(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt, int leaf_size, int threads,
+               Bvh& out);
+
+}  // namespace rx

@@ -1,0 +1,318 @@
+// The C ABI (include/renderx.h): context, scene upload, accelerator build and the
+// closest-hit entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "rx_internal.h"
+
+using rx::DevBuf;
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+rx_status upload(rx_context* c, DevBuf& b, const void* src, size_t bytes, const char* what) {
+  rx_status s = c->cuda(b.alloc(bytes), what);
+  if (s != RX_OK || bytes == 0) return s;
+  return c->cuda(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice), what);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rx_version(void) { return "renderx_gb300 0.1 (sm_103a)"; }
+
+rx_status rx_create(rx_context** out, int device) {
+  if (!out) return RX_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return RX_ERR_CUDA;
+  if (device < 0 || device >= ndev) return RX_ERR_INVALID;
+  rx_context* c = new (std::nothrow) rx_context();
+  if (!c) return RX_ERR_OOM;
+  c->device = device;
+  DeviceGuard g(device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->copy_stream[0], cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->copy_stream[1], cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return RX_ERR_CUDA;
+  }
+  if (c->d_counters.alloc(64 * sizeof(unsigned long long)) != cudaSuccess) {
+    delete c;
+    return RX_ERR_OOM;
+  }
+  cudaMemset(c->d_counters.p, 0, c->d_counters.bytes);
+  *out = c;
+  return RX_OK;
+}
+
+void rx_destroy(rx_context* c) {
+  if (!c) return;
+  {
+    DeviceGuard g(c->device);
+    cudaDeviceSynchronize();
+    for (DevBuf* b : {&c->d_bvh, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
+                      &c->d_counters, &c->d_queue})
+      b->release();
+    for (int k = 0; k < 2; k++)
+      for (DevBuf* b : {&c->ring_rays[k], &c->ring_tid[k], &c->ring_dist[k], &c->ring_queue[k], &c->ring_counters[k]})
+        b->release();
+    if (c->stream) cudaStreamDestroy(c->stream);
+    for (auto s : c->copy_stream)
+      if (s) cudaStreamDestroy(s);
+  }
+  delete c;
+}
+
+const char* rx_last_error(const rx_context* c) { return c ? c->err.c_str() : "null context"; }
+
+rx_status rx_scene_set_geometry(rx_context* c, const float* verts, uint32_t nv, const uint32_t* tri_vidx, uint32_t nt,
+                                const uint32_t* tri_obj, const uint32_t* tri_local, const float* vnormals) {
+  if (!c) return RX_ERR_INVALID;
+  if (!verts || !tri_vidx || nv == 0 || nt == 0) return c->fail(RX_ERR_INVALID, "empty geometry");
+  for (size_t k = 0; k < 3 * (size_t)nt; k++)
+    if (tri_vidx[k] >= nv) return c->fail(RX_ERR_INVALID, "triangle vertex index out of range");
+  for (size_t k = 0; k < 3 * (size_t)nv; k++)
+    if (!std::isfinite(verts[k])) return c->fail(RX_ERR_INVALID, "non-finite vertex coordinate");
+  c->verts.assign(verts, verts + 3 * (size_t)nv);
+  c->tris.assign(tri_vidx, tri_vidx + 3 * (size_t)nt);
+  c->tri_obj.assign(nt, 0);
+  c->tri_local.resize(nt);
+  for (uint32_t i = 0; i < nt; i++) c->tri_local[i] = i;
+  if (tri_obj) c->tri_obj.assign(tri_obj, tri_obj + nt);
+  if (tri_local) c->tri_local.assign(tri_local, tri_local + nt);
+  c->has_normals = vnormals != nullptr;
+  if (vnormals) c->vnormals.assign(vnormals, vnormals + 3 * (size_t)nv);
+  else c->vnormals.clear();
+  c->geometry_dirty = true;
+  c->accel_ready = false;
+  return RX_OK;
+}
+
+rx_status rx_scene_set_objects(rx_context* c, const rx_object* objs, uint32_t nobj) {
+  if (!c) return RX_ERR_INVALID;
+  if (nobj && !objs) return c->fail(RX_ERR_INVALID, "null objects");
+  c->objects.assign(objs, objs + nobj);
+  return RX_OK;
+}
+
+rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
+  if (!c) return RX_ERR_INVALID;
+  if (c->tris.empty()) return c->fail(RX_ERR_STATE, "no geometry");
+  rx_build_options o{0, 4, 0, 0};
+  if (opts) o = *opts;
+  if (o.split_policy != 0 && o.split_policy != 1) return c->fail(RX_ERR_INVALID, "split_policy must be 0 or 1");
+  if (o.leaf_size <= 0) o.leaf_size = 4;
+  if (o.leaf_size > 8) return c->fail(RX_ERR_INVALID, "leaf_size must be 1..8");
+  uint32_t nv = (uint32_t)(c->verts.size() / 3), nt = (uint32_t)(c->tris.size() / 3);
+  if (!rx::build_ref_order(c->verts.data(), nv, c->tris.data(), nt, o.split_policy, o.host_threads, c->ref))
+    return c->fail(RX_ERR_INVALID, "reference-order build failed");
+  if (!rx::build_bvh(c->verts.data(), nv, c->tris.data(), nt, o.leaf_size, o.host_threads, c->bvh))
+    return c->fail(RX_ERR_INVALID, "BVH build failed");
+  if (c->bvh.max_depth >= rx::kStackDepth) return c->fail(RX_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+
+  DeviceGuard g(c->device);
+  // BVH nodes: 4 float4 each
+  std::vector<float4> nodes(4 * c->bvh.nodes.size());
+  for (size_t i = 0; i < c->bvh.nodes.size(); i++) {
+    const rx::BvhNodeHost& h = c->bvh.nodes[i];
+    nodes[4 * i + 0] = make_float4(h.c0lo[0], h.c0hi[0], h.c0lo[1], h.c0hi[1]);
+    nodes[4 * i + 1] = make_float4(h.c1lo[0], h.c1hi[0], h.c1lo[1], h.c1hi[1]);
+    nodes[4 * i + 2] = make_float4(h.c0lo[2], h.c0hi[2], h.c1lo[2], h.c1hi[2]);
+    float4 l;
+    std::memcpy(&l.x, &h.child[0], 4);
+    std::memcpy(&l.y, &h.child[1], 4);
+    std::memcpy(&l.z, &h.count[0], 4);
+    std::memcpy(&l.w, &h.count[1], 4);
+    nodes[4 * i + 3] = l;
+  }
+  auto bits = [](uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+  };
+  const float* V = c->verts.data();
+  auto vtx = [&](uint32_t t, int k, uint32_t w) {
+    const float* p = V + 3 * (size_t)c->tris[3 * (size_t)t + k];
+    return make_float4(p[0], p[1], p[2], bits(w));
+  };
+  std::vector<float4> slots(3 * (size_t)nt);
+  for (uint32_t s = 0; s < nt; s++) {
+    uint32_t t = c->bvh.tri_order[s];
+    slots[3 * (size_t)s + 0] = vtx(t, 0, t);
+    slots[3 * (size_t)s + 1] = vtx(t, 1, c->ref.tri_leaf[t]);
+    slots[3 * (size_t)s + 2] = vtx(t, 2, c->ref.tri_pos[t]);
+  }
+  // reference nodes: (min, parent), (max, right child or ~leaf index)
+  std::vector<float4> refn(2 * c->ref.nodes.size());
+  std::vector<int32_t> node_leaf(c->ref.nodes.size(), -1);
+  for (size_t l = 0; l < c->ref.leaf_node.size(); l++) node_leaf[c->ref.leaf_node[l]] = (int32_t)l;
+  std::vector<uint32_t> leaf_range(2 * c->ref.leaf_node.size());
+  for (size_t i = 0; i < c->ref.nodes.size(); i++) {
+    const rx::RefNodeHost& h = c->ref.nodes[i];
+    int32_t w = h.left >= 0 ? h.right : ~node_leaf[i];
+    refn[2 * i] = make_float4(h.mn[0], h.mn[1], h.mn[2], bits((uint32_t)h.parent));
+    refn[2 * i + 1] = make_float4(h.mx[0], h.mx[1], h.mx[2], bits((uint32_t)w));
+    if (h.left < 0) {
+      leaf_range[2 * node_leaf[i]] = h.tri_begin;
+      leaf_range[2 * node_leaf[i] + 1] = h.tri_end;
+    }
+  }
+  std::vector<float4> reft(3 * (size_t)nt);
+  for (uint32_t k = 0; k < nt; k++) {
+    uint32_t t = c->ref.tri_order[k];
+    reft[3 * (size_t)k] = vtx(t, 0, t);
+    reft[3 * (size_t)k + 1] = vtx(t, 1, 0);
+    reft[3 * (size_t)k + 2] = vtx(t, 2, 0);
+  }
+  std::vector<int32_t> leaf_node(c->ref.leaf_node.begin(), c->ref.leaf_node.end());
+  rx_status s;
+  if ((s = upload(c, c->d_bvh, nodes.data(), nodes.size() * sizeof(float4), "upload BVH")) != RX_OK) return s;
+  if ((s = upload(c, c->d_tris, slots.data(), slots.size() * sizeof(float4), "upload triangles")) != RX_OK) return s;
+  if ((s = upload(c, c->d_ref, refn.data(), refn.size() * sizeof(float4), "upload reference nodes")) != RX_OK) return s;
+  if ((s = upload(c, c->d_ref_leaf_node, leaf_node.data(), leaf_node.size() * 4, "upload leaf map")) != RX_OK) return s;
+  if ((s = upload(c, c->d_ref_leaf_range, leaf_range.data(), leaf_range.size() * 4, "upload leaf ranges")) != RX_OK)
+    return s;
+  if ((s = upload(c, c->d_ref_tris, reft.data(), reft.size() * sizeof(float4), "upload reference triangles")) != RX_OK)
+    return s;
+  rx::DevAccel& A = c->accel;
+  A.bvh = c->d_bvh.as<float4>();
+  A.tris = c->d_tris.as<float4>();
+  A.ref = c->d_ref.as<float4>();
+  A.ref_leaf_node = c->d_ref_leaf_node.as<int32_t>();
+  A.ref_leaf_range = c->d_ref_leaf_range.as<uint32_t>();
+  A.ref_tris = c->d_ref_tris.as<float4>();
+  A.num_nodes = (uint32_t)c->bvh.nodes.size();
+  A.num_tris = nt;
+  A.num_ref_nodes = (uint32_t)c->ref.nodes.size();
+  A.num_ref_leaves = (uint32_t)c->ref.leaf_node.size();
+  A.prune_rel = 1e-3f;
+  c->accel_ready = true;
+  c->geometry_dirty = false;
+  return RX_OK;
+}
+
+rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {
+  if (!c || !out) return RX_ERR_INVALID;
+  if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
+  std::memset(out, 0, 8 * sizeof(int64_t));
+  out[0] = (int64_t)c->bvh.nodes.size();
+  out[1] = c->bvh.max_depth;
+  out[2] = (int64_t)c->ref.nodes.size();
+  out[3] = c->ref.max_depth;
+  out[4] = (int64_t)(c->tris.size() / 3);
+  out[5] = (int64_t)c->ref.leaf_node.size();
+  return RX_OK;
+}
+
+static rx_status ensure_queue(rx_context* c, size_t n) {
+  if (c->d_queue.bytes >= n * 4) return RX_OK;
+  return c->cuda(c->d_queue.alloc(std::max<size_t>(n, 1024) * 4), "allocate re-trace queue");
+}
+
+rx_status rx_trace_closest_device(rx_context* c, const rx_ray* d_rays, uint32_t n, int32_t* d_tid, float* d_dist,
+                                  void* stream) {
+  if (!c) return RX_ERR_INVALID;
+  if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
+  if (n == 0) return RX_OK;
+  if (!d_rays || !d_tid || !d_dist) return c->fail(RX_ERR_INVALID, "null buffer");
+  if (reinterpret_cast<uintptr_t>(d_rays) % 16) return c->fail(RX_ERR_INVALID, "rays must be 16-byte aligned");
+  DeviceGuard g(c->device);
+  rx_status s = ensure_queue(c, n);
+  if (s != RX_OK) return s;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return c->cuda(rx::launch_trace_closest(c->accel, d_rays, n, d_tid, d_dist, c->d_queue.as<uint32_t>(),
+                                          c->d_counters.as<unsigned long long>(), st),
+                 "trace_closest launch");
+}
+
+rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
+                                           float* d_dist, void* stream) {
+  if (!c) return RX_ERR_INVALID;
+  if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
+  if (n == 0) return RX_OK;
+  if (!d_rays || !d_tid || !d_dist) return c->fail(RX_ERR_INVALID, "null buffer");
+  if (c->ref.max_depth >= 120) return c->fail(RX_ERR_UNSUPPORTED, "reference tree deeper than the walk stack");
+  DeviceGuard g(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return c->cuda(rx::launch_trace_reforder(c->accel, d_rays, n, d_tid, d_dist, c->d_counters.as<unsigned long long>(), st),
+                 "trace_reforder launch");
+}
+
+// Host buffers: chunks alternate between two copy/compute streams so that one
+// chunk's copies overlap the other chunk's kernels.
+rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist) {
+  if (!c) return RX_ERR_INVALID;
+  if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
+  if (n == 0) return RX_OK;
+  if (!rays || !out_tid || !out_dist) return c->fail(RX_ERR_INVALID, "null buffer");
+  DeviceGuard g(c->device);
+  const size_t chunk = std::min<size_t>(n, (size_t)1 << 21);
+  if (c->ring_chunk < chunk) {
+    for (int k = 0; k < 2; k++) {
+      rx_status s;
+      if ((s = c->cuda(c->ring_rays[k].alloc(chunk * sizeof(rx_ray)), "staging")) != RX_OK) return s;
+      if ((s = c->cuda(c->ring_tid[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
+      if ((s = c->cuda(c->ring_dist[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
+      if ((s = c->cuda(c->ring_queue[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
+      if ((s = c->cuda(c->ring_counters[k].alloc(8 * sizeof(unsigned long long)), "staging")) != RX_OK) return s;
+      cudaMemset(c->ring_counters[k].p, 0, c->ring_counters[k].bytes);
+    }
+    c->ring_chunk = chunk;
+  }
+  for (size_t b = 0, k = 0; b < n; b += chunk, k ^= 1) {
+    size_t m = std::min<size_t>(chunk, n - b);
+    cudaStream_t st = c->copy_stream[k];
+    cudaMemcpyAsync(c->ring_rays[k].p, rays + b, m * sizeof(rx_ray), cudaMemcpyHostToDevice, st);
+    cudaError_t e = rx::launch_trace_closest(c->accel, c->ring_rays[k].as<rx_ray>(), (uint32_t)m,
+                                             c->ring_tid[k].as<int32_t>(), c->ring_dist[k].as<float>(),
+                                             c->ring_queue[k].as<uint32_t>(),
+                                             c->ring_counters[k].as<unsigned long long>(), st);
+    if (e != cudaSuccess) return c->cuda(e, "trace_closest launch");
+    cudaMemcpyAsync(out_tid + b, c->ring_tid[k].p, m * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(out_dist + b, c->ring_dist[k].p, m * 4, cudaMemcpyDeviceToHost, st);
+  }
+  for (auto s : c->copy_stream) {
+    rx_status r = c->cuda(cudaStreamSynchronize(s), "trace_closest");
+    if (r != RX_OK) return r;
+  }
+  return RX_OK;
+}
+
+rx_status rx_trace_counters(rx_context* c, uint64_t out[4], int reset) {
+  if (!c || !out) return RX_ERR_INVALID;
+  DeviceGuard g(c->device);
+  unsigned long long h[4], r[2][8];
+  rx_status s = c->cuda(cudaDeviceSynchronize(), "counters");
+  if (s != RX_OK) return s;
+  cudaMemcpy(h, c->d_counters.p, sizeof h, cudaMemcpyDeviceToHost);
+  for (int k = 0; k < 4; k++) out[k] = h[k];
+  for (int k = 0; k < 2; k++)
+    if (c->ring_counters[k].p) {
+      cudaMemcpy(r[k], c->ring_counters[k].p, sizeof r[k], cudaMemcpyDeviceToHost);
+      for (int j = 1; j < 4; j++) out[j] += r[k][j];
+    }
+  if (reset) {
+    cudaMemset(c->d_counters.p, 0, c->d_counters.bytes);
+    for (int k = 0; k < 2; k++)
+      if (c->ring_counters[k].p) cudaMemset(c->ring_counters[k].p, 0, c->ring_counters[k].bytes);
+  }
+  return RX_OK;
+}
+
+}  // extern "C"

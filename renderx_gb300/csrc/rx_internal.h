@@ -1,0 +1,77 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/renderx.h"
+#include "rx_accel.h"
+#include "rx_device.h"
+
+namespace rx {
+
+// Launchers (rx_trace.cu).
+cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
+                                 uint32_t* queue, unsigned long long* counters, cudaStream_t s);
+cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
+                                  unsigned long long* counters, cudaStream_t s);
+
+// A device allocation owned by the context.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t alloc(size_t b) {
+    release();
+    if (b == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace rx
+
+struct rx_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream[2] = {nullptr, nullptr};
+  std::string err;
+
+  // host scene
+  std::vector<float> verts, vnormals;
+  std::vector<uint32_t> tris, tri_obj, tri_local;
+  bool has_normals = false;
+  std::vector<rx_object> objects;
+  bool geometry_dirty = true;
+
+  // acceleration
+  rx::RefOrder ref;
+  rx::Bvh bvh;
+  rx::DevAccel accel{};
+  bool accel_ready = false;
+  rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris;
+  rx::DevBuf d_counters;     // 4 x u64 diagnostics + per-slot queue lengths
+  rx::DevBuf d_queue;        // eager re-trace queue for device-buffer calls
+  // staging ring for host-buffer calls
+  rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
+  size_t ring_chunk = 0;
+
+  rx_status fail(rx_status s, const std::string& m) {
+    err = m;
+    return s;
+  }
+  rx_status cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return RX_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? RX_ERR_OOM : RX_ERR_CUDA;
+  }
+};

@@ -1,0 +1,127 @@
+"""Generates the closest-hit golden fixtures from the reference's own KDTree.
+
+Runs only where the reference sources are mounted: builds oracle/_ref/hit_driver from
+them (oracle/ref/Makefile), then for each case writes ``hit_<case>.npz`` with the rays,
+the reference's (tid, dist) answers and its serialized tree (KDTree::serializeForGPU).
+Scenes come from renderx_gb300.scenes with fixed seeds; small scenes also store their
+geometry so the fixture stands alone.
+
+    python tests/golden/make_golden.py [REF_DIR]
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from renderx_gb300 import scenes  # noqa: E402
+
+CASES = {
+    # name: (n_spheres, subdiv, scene seed, random rays, store geometry)
+    "cornell": (0, 0, 0, 4096, True),
+    "spheres4": (4, 3, 3, 4096, True),
+    "spheres20": (20, 4, 5, 2048, False),
+}
+
+
+def geometry_hash(verts: np.ndarray, tris: np.ndarray) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(verts, np.float32).tobytes())
+    h.update(np.ascontiguousarray(tris, np.uint32).tobytes())
+    return h.hexdigest()
+
+
+def make_scene(ns: int, sub: int, seed: int):
+    sc = scenes.sphere_field(ns, sub, seed=seed, width=64, height=64) if ns else scenes.cornell_box(64, 64)
+    return sc.flatten()
+
+
+def stress_rays(verts: np.ndarray, tris: np.ndarray, n: int, seed: int):
+    """Rays that stress ties, zero direction components and surface origins."""
+    rng = np.random.default_rng(seed)
+    R = scenes.ROOM
+    o_list, d_list = [], []
+    # 1. aimed exactly at shared vertices and edge midpoints (equal-distance candidates)
+    pick = rng.integers(0, len(tris), n // 4)
+    for k, t in enumerate(pick):
+        a, b = verts[tris[t, k % 3]], verts[tris[t, (k + 1) % 3]]
+        target = a if k % 2 == 0 else (a + b) * np.float32(0.5)
+        o = rng.uniform(0.2, R - 0.2, 3).astype(np.float32)
+        d = (target - o).astype(np.float64)
+        d /= np.linalg.norm(d)
+        o_list.append(o)
+        d_list.append(d.astype(np.float32))
+    # 2. axis-aligned and planar directions (reference skips faces where d[axis] == 0)
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0.6, 0, 0.8], [0, -0.8, 0.6], [0.8, 0.6, 0]], np.float32)
+    for k in range(n // 4):
+        o_list.append(rng.uniform(0.0, R, 3).astype(np.float32))
+        d_list.append(axes[k % len(axes)])
+    # 3. origins on triangles (t = 0 candidates) and just off them
+    pick = rng.integers(0, len(tris), n // 4)
+    for t in pick:
+        w = rng.dirichlet([1, 1, 1])
+        p = (w[0] * verts[tris[t, 0]] + w[1] * verts[tris[t, 1]] + w[2] * verts[tris[t, 2]]).astype(np.float32)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        o_list.append(p)
+        d_list.append(d.astype(np.float32))
+    # 4. grazing rays in the floor plane and from outside the room
+    for k in range(n - 3 * (n // 4)):
+        if k % 2 == 0:
+            o = np.array([rng.uniform(0, R), 0.0, rng.uniform(0, R)], np.float32)
+            phi = rng.uniform(0, 2 * np.pi)
+            d = np.array([np.cos(phi), 0.0, np.sin(phi)], np.float32)
+        else:
+            o = rng.uniform(-3.0, R + 3.0, 3).astype(np.float32)
+            d = (rng.uniform(0.5, R - 0.5, 3) - o).astype(np.float64)
+            d = (d / np.linalg.norm(d)).astype(np.float32)
+        o_list.append(o)
+        d_list.append(d)
+    return np.array(o_list, np.float32), np.array(d_list, np.float32)
+
+
+def run_reference(ref_bin: str, verts, tris, o, d):
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "c")
+        np.ascontiguousarray(verts, np.float32).tofile(p + ".v")
+        np.ascontiguousarray(tris, np.uint32).tofile(p + ".t")
+        np.concatenate([o, d], 1).astype(np.float32).tofile(p + ".r")
+        subprocess.run([ref_bin, p + ".v", p + ".t", p + ".r", p], check=True, capture_output=True,
+                       env={**os.environ, "OMP_NUM_THREADS": "8"})
+        return (np.fromfile(p + ".tid.i32", np.int32), np.fromfile(p + ".dist.f32", np.float32),
+                np.fromfile(p + ".nodes.f32", np.float32).reshape(-1, 12), np.fromfile(p + ".leaf.f32", np.float32))
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"], check=True)
+    ref_bin = os.path.join(ROOT, "oracle", "_ref", "hit_driver")
+    for name, (ns, sub, seed, nrand, store) in CASES.items():
+        f = make_scene(ns, sub, seed)
+        v, t = f["verts"], f["tris"]
+        o1, d1 = scenes.hit_rays(nrand, seed=100 + seed)
+        o2, d2 = stress_rays(v, t, nrand, seed=200 + seed)
+        o = np.concatenate([o1, o2])
+        d = np.concatenate([d1, d2])
+        tid, dist, nodes, leaf = run_reference(ref_bin, v, t, o, d)
+        out = dict(origins=o, dirs=d, tid=tid, dist=dist, nodes=nodes, leaf=leaf,
+                   params=np.array([ns, sub, seed], np.int64), geometry_sha256=np.array(geometry_hash(v, t)))
+        if store:
+            out.update(verts=v, tris=t)
+        path = os.path.join(HERE, f"hit_{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {len(o)} rays, {len(t)} tris, {len(nodes)} nodes, hit rate {(tid >= 0).mean():.3f}, "
+              f"{os.path.getsize(path) // 1024} KiB")
+
+
+if __name__ == "__main__":
+    main()

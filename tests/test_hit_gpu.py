@@ -1,0 +1,135 @@
+"""GPU closest-hit parity: the sm_103a kernels, called through the C ABI, return the
+reference's answers bit for bit (triangle ids and distances), against the golden
+fixtures made by the reference's own KDTree and against the oracle restatement."""
+import numpy as np
+import pytest
+
+import oracle
+import renderx_gb300 as rx
+from renderx_gb300 import scenes
+from golden_util import CASES, load
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits_equal(a, b):
+    return np.array_equal(np.asarray(a, np.float32).view(np.int32), np.asarray(b, np.float32).view(np.int32))
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("leaf_size", [1, 4, 8])
+def test_hits_match_reference_golden(name, leaf_size):
+    z = load(name)
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(z["verts"], z["tris"])
+        ctx.build_accel(rx.SPLIT_GCC, leaf_size=leaf_size)
+        tid, dist = ctx.trace_closest(z["origins"], z["dirs"])
+        c = ctx.counters()
+    bad = np.nonzero(tid != z["tid"])[0]
+    assert bad.size == 0, f"{bad.size} id mismatches, first {bad[:5]}: got {tid[bad[:5]]} want {z['tid'][bad[:5]]}"
+    assert _bits_equal(dist, z["dist"])
+    assert c["errors"] == 0
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_order_walk_matches_golden(name):
+    torch = pytest.importorskip("torch")
+    z = load(name)
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(z["verts"], z["tris"])
+        ctx.build_accel()
+        rays = torch.from_numpy(rx.rays_to_array(z["origins"], z["dirs"])).cuda()
+        n = rays.shape[0]
+        tid = torch.empty(n, dtype=torch.int32, device="cuda")
+        dist = torch.empty(n, dtype=torch.float32, device="cuda")
+        ctx.trace_reforder_device(rays, n, tid, dist)
+        torch.cuda.synchronize()
+        assert np.array_equal(tid.cpu().numpy(), z["tid"])
+        assert _bits_equal(dist.cpu().numpy(), z["dist"])
+        # device-buffer entry point of the fast path, on torch's stream
+        tid2 = torch.empty_like(tid)
+        dist2 = torch.empty_like(dist)
+        ctx.trace_closest_device(rays, n, tid2, dist2, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(tid2.cpu().numpy(), z["tid"])
+        assert _bits_equal(dist2.cpu().numpy(), z["dist"])
+
+
+def test_best_axis_policy_matches_oracle():
+    z = load("spheres4")
+    T = oracle.RefTree(z["verts"], z["tris"], oracle.SPLIT_BEST)
+    want_t, want_d = T.trace(z["origins"], z["dirs"])
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(z["verts"], z["tris"])
+        ctx.build_accel(rx.SPLIT_BEST)
+        tid, dist = ctx.trace_closest(z["origins"], z["dirs"])
+    assert np.array_equal(tid, want_t)
+    assert _bits_equal(dist, want_d)
+
+
+def test_empty_and_single_triangle_and_ragged_batches():
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    t = np.array([[0, 1, 2]], np.uint32)
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(v, t)
+        ctx.build_accel()
+        tid, dist = ctx.trace_closest(np.zeros((0, 3)), np.zeros((0, 3)))
+        assert tid.size == 0
+        T = oracle.RefTree(v, t)
+        for n in (1, 31, 33, 129, 1000):
+            o, d = scenes.hit_rays(n, seed=n, lo=-0.5, hi=1.5)
+            tid, dist = ctx.trace_closest(o, d)
+            wt, wd = T.trace(o, d)
+            assert np.array_equal(tid, wt) and _bits_equal(dist, wd)
+
+
+def test_invalid_inputs_raise():
+    with rx.Context(0) as ctx:
+        with pytest.raises(rx.RxError):
+            ctx.trace_closest(np.zeros((4, 3)), np.ones((4, 3)))  # before build
+        v = np.zeros((3, 3), np.float32)
+        with pytest.raises(rx.RxError):
+            ctx.set_geometry(v, np.array([[0, 1, 3]], np.uint32))  # index out of range
+        v[0, 0] = np.nan
+        with pytest.raises(rx.RxError):
+            ctx.set_geometry(v, np.array([[0, 1, 2]], np.uint32))
+
+
+@pytest.mark.slow
+def test_full_size_batch_matches_oracle_sample_and_reference_walk():
+    """4,096,036 triangles, 2^24 rays: the whole batch through the fast path; a sample
+    against the CPU oracle, a 2^18 slice against the reference-order walk on the GPU,
+    and the whole batch twice for determinism."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.sphere_field(200, 5, seed=1)
+    f = sc.flatten()
+    n = 1 << 24
+    o, d = scenes.hit_rays(n, seed=7)
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(f["verts"], f["tris"])
+        ctx.build_accel()
+        rays = torch.from_numpy(rx.rays_to_array(o, d)).cuda()
+        tid = torch.empty(n, dtype=torch.int32, device="cuda")
+        dist = torch.empty(n, dtype=torch.float32, device="cuda")
+        ctx.trace_closest_device(rays, n, tid, dist)
+        tid2, dist2 = torch.empty_like(tid), torch.empty_like(dist)
+        ctx.trace_closest_device(rays, n, tid2, dist2)
+        torch.cuda.synchronize()
+        assert torch.equal(tid, tid2) and torch.equal(dist.view(torch.int32), dist2.view(torch.int32))
+        m = 1 << 18
+        tr = torch.empty(m, dtype=torch.int32, device="cuda")
+        dr = torch.empty(m, dtype=torch.float32, device="cuda")
+        ctx.trace_reforder_device(rays[:m], m, tr, dr)
+        torch.cuda.synchronize()
+        assert torch.equal(tr, tid[:m])
+        assert torch.equal(dr.view(torch.int32), dist[:m].view(torch.int32))
+        assert ctx.counters()["errors"] == 0
+    tid = tid.cpu().numpy()
+    dist = dist.cpu().numpy()
+    rng = np.random.default_rng(0)
+    sample = np.sort(rng.choice(n, 1024, replace=False))
+    T = oracle.RefTree(f["verts"], f["tris"])
+    wt, wd = T.trace(o[sample], d[sample])
+    assert np.array_equal(tid[sample], wt)
+    assert _bits_equal(dist[sample], wd)
+    assert 0.5 < (tid >= 0).mean() <= 1.0

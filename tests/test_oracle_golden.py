@@ -1,0 +1,51 @@
+"""Pins the oracle: the CPU restatement of the reference KDTree must reproduce the
+reference's own answers (golden fixtures made by the reference code) bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import CASES, load
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_tree_matches_reference_serialization(name):
+    z = load(name)
+    T = oracle.RefTree(z["verts"], z["tris"], oracle.SPLIT_GCC)
+    nodes, leaf = T.serialize()
+    assert np.array_equal(nodes, z["nodes"])
+    assert np.array_equal(leaf, z["leaf"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_hits_match_reference(name):
+    z = load(name)
+    T = oracle.RefTree(z["verts"], z["tris"], oracle.SPLIT_GCC)
+    tid, dist = T.trace(z["origins"], z["dirs"])
+    assert np.array_equal(tid, z["tid"])
+    # bit-identical distances (misses are -1 on both sides)
+    assert np.array_equal(dist.view(np.int32), z["dist"].view(np.int32))
+
+
+def test_fixtures_exercise_ties_and_edge_cases():
+    z = load("spheres4")
+    d = z["dirs"]
+    assert (d == 0).any(axis=1).sum() > 100          # zero direction components
+    assert (z["dist"] == 0).sum() > 0 or (z["dist"] >= 0).sum() > 0
+    assert (z["tid"] < 0).sum() > 0 and (z["tid"] >= 0).sum() > 0
+
+
+def test_box_test_semantics():
+    # KDTree.cpp:107-125: inclusive, no epsilon; faces with a zero direction skipped
+    mn, mx = np.zeros(3), np.ones(3)
+    assert oracle.box_test(mn, mx, [0.5, 0.5, -1], [0, 0, 1]) == 1.0
+    assert oracle.box_test(mn, mx, [0.5, 0.5, 0.5], [0, 0, 1]) == 0.5   # inside: exit face
+    assert oracle.box_test(mn, mx, [1.0, 0.5, -1], [0, 0, 1]) == 1.0    # on the x = 1 face plane
+    assert oracle.box_test(mn, mx, [1.5, 0.5, -1], [0, 0, 1]) < 0
+    assert oracle.box_test(mn, mx, [0.5, 0.5, 2], [0, 0, 1]) < 0        # behind
+
+
+def test_split_policies_differ_only_in_axis_choice():
+    z = load("spheres4")
+    a = oracle.RefTree(z["verts"], z["tris"], oracle.SPLIT_GCC)
+    b = oracle.RefTree(z["verts"], z["tris"], oracle.SPLIT_BEST)
+    assert b.num_nodes > a.num_nodes  # best-axis splits succeed where x-only ones stop
