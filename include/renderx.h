@@ -119,6 +119,11 @@ rx_status rx_trace_closest_device(rx_context* ctx, const rx_ray* d_rays, uint32_
  * ray see, in the reference's own order (slow; a consistency check on small scenes). */
 rx_status rx_trace_closest_reforder_device(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
                                            float* d_dist, void* stream);
+/* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
+ * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative
+ * leaf postponing; blocks of 128 threads, blocks_per_sm per SM. No reference
+ * counterpart (launch tuning). */
+rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_per_sm);
 /* Rays whose lazy winner failed the reference-visibility check and were re-traced
  * exactly, counted since the last reset (diagnostic). */
 rx_status rx_trace_counters(rx_context* ctx, uint64_t out[4], int reset);

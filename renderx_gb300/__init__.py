@@ -137,6 +137,9 @@ class Context:
         self._ck(self._L.rx_trace_closest_reforder_device(self.h, _capi.ptr(d_rays), n, _capi.ptr(d_tid),
                                                           _capi.ptr(d_dist), _capi.stream_arg(stream)))
 
+    def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
+        self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
+
     def counters(self, reset: bool = False) -> dict:
         out = np.zeros(4, np.uint64)
         self._ck(self._L.rx_trace_counters(self.h, _capi.ptr(out), int(reset)))

@@ -53,6 +53,7 @@ SIGNATURES = [
     ("rx_trace_closest_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_closest_reforder_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_counters", S, [P, P, S]),
+    ("rx_trace_set_config", S, [P, I32, I32]),
 ]
 
 

@@ -57,6 +57,7 @@ rx_status rx_create(rx_context** out, int device) {
     return RX_ERR_OOM;
   }
   cudaMemset(c->d_counters.p, 0, c->d_counters.bytes);
+  cudaDeviceGetAttribute(&c->trace_cfg.sms, cudaDevAttrMultiProcessorCount, device);
   *out = c;
   return RX_OK;
 }
@@ -67,6 +68,7 @@ void rx_destroy(rx_context* c) {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
     for (DevBuf* b : {&c->d_bvh, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
+                      &c->d_anc_range, &c->d_anc_nodes,
                       &c->d_counters, &c->d_queue})
       b->release();
     for (int k = 0; k < 2; k++)
@@ -181,6 +183,16 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
     reft[3 * (size_t)k + 2] = vtx(t, 2, 0);
   }
   std::vector<int32_t> leaf_node(c->ref.leaf_node.begin(), c->ref.leaf_node.end());
+  // per reference leaf, the node ids of its root path (leaf first): the boxes the
+  // reference tests before it reaches the leaf's triangles
+  std::vector<uint32_t> anc_range(2 * leaf_node.size());
+  std::vector<int32_t> anc_nodes;
+  anc_nodes.reserve(leaf_node.size() * (size_t)(c->ref.max_depth + 1));
+  for (size_t l = 0; l < leaf_node.size(); l++) {
+    anc_range[2 * l] = (uint32_t)anc_nodes.size();
+    for (int32_t nd = leaf_node[l]; nd >= 0; nd = c->ref.nodes[nd].parent) anc_nodes.push_back(nd);
+    anc_range[2 * l + 1] = (uint32_t)anc_nodes.size();
+  }
   rx_status s;
   if ((s = upload(c, c->d_bvh, nodes.data(), nodes.size() * sizeof(float4), "upload BVH")) != RX_OK) return s;
   if ((s = upload(c, c->d_tris, slots.data(), slots.size() * sizeof(float4), "upload triangles")) != RX_OK) return s;
@@ -190,6 +202,10 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
     return s;
   if ((s = upload(c, c->d_ref_tris, reft.data(), reft.size() * sizeof(float4), "upload reference triangles")) != RX_OK)
     return s;
+  if ((s = upload(c, c->d_anc_range, anc_range.data(), anc_range.size() * 4, "upload ancestor ranges")) != RX_OK)
+    return s;
+  if ((s = upload(c, c->d_anc_nodes, anc_nodes.data(), anc_nodes.size() * 4, "upload ancestor lists")) != RX_OK)
+    return s;
   rx::DevAccel& A = c->accel;
   A.bvh = c->d_bvh.as<float4>();
   A.tris = c->d_tris.as<float4>();
@@ -197,6 +213,8 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.ref_leaf_node = c->d_ref_leaf_node.as<int32_t>();
   A.ref_leaf_range = c->d_ref_leaf_range.as<uint32_t>();
   A.ref_tris = c->d_ref_tris.as<float4>();
+  A.anc_range = c->d_anc_range.as<uint32_t>();
+  A.anc_nodes = c->d_anc_nodes.as<int32_t>();
   A.num_nodes = (uint32_t)c->bvh.nodes.size();
   A.num_tris = nt;
   A.num_ref_nodes = (uint32_t)c->ref.nodes.size();
@@ -220,9 +238,10 @@ rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {
   return RX_OK;
 }
 
+// Scratch of a closest-hit launch over n rays: n winner leaves + up to n queued rays.
 static rx_status ensure_queue(rx_context* c, size_t n) {
-  if (c->d_queue.bytes >= n * 4) return RX_OK;
-  return c->cuda(c->d_queue.alloc(std::max<size_t>(n, 1024) * 4), "allocate re-trace queue");
+  if (c->d_queue.bytes >= n * 8) return RX_OK;
+  return c->cuda(c->d_queue.alloc(std::max<size_t>(n, 1024) * 8), "allocate closest-hit scratch");
 }
 
 rx_status rx_trace_closest_device(rx_context* c, const rx_ray* d_rays, uint32_t n, int32_t* d_tid, float* d_dist,
@@ -237,7 +256,7 @@ rx_status rx_trace_closest_device(rx_context* c, const rx_ray* d_rays, uint32_t 
   if (s != RX_OK) return s;
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   return c->cuda(rx::launch_trace_closest(c->accel, d_rays, n, d_tid, d_dist, c->d_queue.as<uint32_t>(),
-                                          c->d_counters.as<unsigned long long>(), st),
+                                          c->d_counters.as<unsigned long long>(), c->trace_cfg, st),
                  "trace_closest launch");
 }
 
@@ -269,7 +288,7 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
       if ((s = c->cuda(c->ring_rays[k].alloc(chunk * sizeof(rx_ray)), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_tid[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_dist[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
-      if ((s = c->cuda(c->ring_queue[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
+      if ((s = c->cuda(c->ring_queue[k].alloc(chunk * 8), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_counters[k].alloc(8 * sizeof(unsigned long long)), "staging")) != RX_OK) return s;
       cudaMemset(c->ring_counters[k].p, 0, c->ring_counters[k].bytes);
     }
@@ -282,7 +301,7 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
     cudaError_t e = rx::launch_trace_closest(c->accel, c->ring_rays[k].as<rx_ray>(), (uint32_t)m,
                                              c->ring_tid[k].as<int32_t>(), c->ring_dist[k].as<float>(),
                                              c->ring_queue[k].as<uint32_t>(),
-                                             c->ring_counters[k].as<unsigned long long>(), st);
+                                             c->ring_counters[k].as<unsigned long long>(), c->trace_cfg, st);
     if (e != cudaSuccess) return c->cuda(e, "trace_closest launch");
     cudaMemcpyAsync(out_tid + b, c->ring_tid[k].p, m * 4, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(out_dist + b, c->ring_dist[k].p, m * 4, cudaMemcpyDeviceToHost, st);
@@ -291,6 +310,15 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
     rx_status r = c->cuda(cudaStreamSynchronize(s), "trace_closest");
     if (r != RX_OK) return r;
   }
+  return RX_OK;
+}
+
+rx_status rx_trace_set_config(rx_context* c, int32_t variant, int32_t blocks_per_sm) {
+  if (!c) return RX_ERR_INVALID;
+  if (variant < 0 || variant > 2 || blocks_per_sm < 1 || blocks_per_sm > 32)
+    return c->fail(RX_ERR_INVALID, "variant must be 0..2 and blocks_per_sm 1..32");
+  c->trace_cfg.variant = variant;
+  c->trace_cfg.blocks_per_sm = blocks_per_sm;
   return RX_OK;
 }
 

@@ -24,6 +24,8 @@ struct DevAccel {
   const int32_t* ref_leaf_node;
   const uint32_t* ref_leaf_range;  // 2 per leaf: [begin, end) in reference DFS order
   const float4* ref_tris;          // 3 float4 per triangle in reference DFS order (v*.w unused but v0.w = id)
+  const uint32_t* anc_range;       // 2 per leaf: [begin, end) into anc_nodes
+  const int32_t* anc_nodes;        // per leaf, its root path (leaf first) as node ids
   uint32_t num_nodes, num_tris, num_ref_nodes, num_ref_leaves;
   float prune_rel;                 // pruning margin: t_limit = best + prune_rel*(1+best)
 };

@@ -11,9 +11,18 @@
 
 namespace rx {
 
+// Closest-hit launch shape: variant 0 = one thread per ray, 1 = persistent warps
+// refilling finished lanes; blocks_per_sm x sms blocks of 128 threads.
+struct TraceConfig {
+  int variant = 1;
+  int blocks_per_sm = 12;
+  int sms = 152;
+};
+
 // Launchers (rx_trace.cu).
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
-                                 uint32_t* queue, unsigned long long* counters, cudaStream_t s);
+                                 uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
+                                 cudaStream_t s);
 cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                   unsigned long long* counters, cudaStream_t s);
 
@@ -57,10 +66,11 @@ struct rx_context {
   rx::RefOrder ref;
   rx::Bvh bvh;
   rx::DevAccel accel{};
+  rx::TraceConfig trace_cfg;
   bool accel_ready = false;
-  rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris;
+  rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes;
   rx::DevBuf d_counters;     // 4 x u64 diagnostics + per-slot queue lengths
-  rx::DevBuf d_queue;        // eager re-trace queue for device-buffer calls
+  rx::DevBuf d_queue;        // closest-hit scratch (winner leaves + eager queue)
   // staging ring for host-buffer calls
   rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
   size_t ring_chunk = 0;

@@ -6,35 +6,231 @@ namespace rx {
 
 // counters[0]: rays queued for the eager re-walk by the current launch, [1]: box
 // tests decided by the exact test, [2]: rays re-walked (cumulative), [3]: errors
-__global__ void __launch_bounds__(128) k_trace_closest(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
-                                                       int32_t* __restrict__ out_tid, float* __restrict__ out_dist,
+constexpr uint32_t kNoLeaf = 0xffffffffu;
+
+// Reference visibility of each ray's winner (KDTree.cpp:107-125 on every box of the
+// winner's root path), one warp per ray and one root-path box per lane; the boxes of
+// the reference tree are few and stay in cache. Rays whose winner the reference cannot
+// see go to the eager queue.
+__global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                       const uint32_t* __restrict__ hit_leaf,
                                                        uint32_t* __restrict__ eager_queue,
                                                        unsigned long long* __restrict__ counters) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   unsigned n_exact = 0;
-  bool lazy_fail = false;
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    uint32_t leaf = __ldg(&hit_leaf[i]);
+    if (leaf == kNoLeaf) continue;
+    const float4* rp = reinterpret_cast<const float4*>(rays + i);
+    F3 o = f3(__ldg(rp)), d = f3(__ldg(rp + 1));
+    F3 inv = safe_inv(d);
+    bool zd = (d.x == 0.0f) | (d.y == 0.0f) | (d.z == 0.0f);
+    uint32_t b = __ldg(&A.anc_range[2 * leaf]), e = __ldg(&A.anc_range[2 * leaf + 1]);
+    bool ok = true;
+    for (uint32_t base = b; base < e; base += 32) {
+      uint32_t k = base + lane;
+      bool pass = true;
+      if (k < e) {
+        int node = __ldg(&A.anc_nodes[k]);
+        float4 lo = __ldg(&A.ref[2 * node]), hi = __ldg(&A.ref[2 * node + 1]);
+        if (zd || !box_clear_pass(f3(lo), f3(hi), o, d, inv)) {
+          n_exact++;
+          pass = box_exact(f3(lo), f3(hi), o, d);
+        }
+      }
+      ok = __all_sync(FULL, pass) && ok;
+    }
+    if (!ok && lane == 0) {
+      unsigned long long slot = atomicAdd(&counters[0], 1ull);
+      eager_queue[slot] = i;  // the queue holds n entries: never overflows
+    }
+  }
+  unsigned sum = n_exact;
+  for (int s2 = 16; s2 > 0; s2 >>= 1) sum += __shfl_xor_sync(FULL, sum, s2);
+  if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
+}
+
+// One thread per ray. Writes the winner and its reference leaf; k_check_visible then
+// confirms the winner is visible to the reference.
+__global__ void __launch_bounds__(128) k_trace_closest(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                       int32_t* __restrict__ out_tid, float* __restrict__ out_dist,
+                                                       uint32_t* __restrict__ hit_leaf,
+                                                       unsigned long long* __restrict__ counters) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  unsigned n_exact = 0;
+  F3 o{0, 0, 0}, d{0, 0, 1};
+  HitResult h{-1, -1.0f, 0u, 0u, false};
   if (i < n) {
     const float4* rp = reinterpret_cast<const float4*>(rays + i);
     float4 ro = __ldg(rp), rd = __ldg(rp + 1);
-    F3 o = f3(ro), d = f3(rd);
-    HitResult h = trace_ref_exact<false>(A, o, d, &n_exact);
-    if (h.hit) {
-      F3 inv = safe_inv(d);
-      bool zd = (d.x == 0.0f) | (d.y == 0.0f) | (d.z == 0.0f);
-      lazy_fail = !ref_visible(A, h.leaf, o, d, inv, zd, &n_exact);
-    }
-    if (lazy_fail) {
-      unsigned long long slot = atomicAdd(&counters[0], 1ull);
-      eager_queue[slot] = i;  // queue holds n entries: never overflows
-    } else {
-      out_tid[i] = h.hit ? h.tid : -1;
-      out_dist[i] = h.hit ? h.t : -1.0f;
-    }
+    o = f3(ro);
+    d = f3(rd);
+    h = trace_ref_exact<false>(A, o, d, &n_exact);
+  }
+  if (i < n) {
+    out_tid[i] = h.hit ? h.tid : -1;
+    out_dist[i] = h.hit ? h.t : -1.0f;
+    hit_leaf[i] = h.hit ? h.leaf : kNoLeaf;
   }
   // one atomic per warp for the diagnostics
   unsigned sum = n_exact;
   for (int s = 16; s > 0; s >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, s);
-  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
+  if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
+}
+
+// Persistent variant: warps stay resident and refill lanes whose ray has finished with
+// the next rays of the batch (one atomic per warp and refill), so a warp never idles
+// behind its longest ray. Each round walks inner nodes until the lane holds a leaf
+// (SPEC: keeps walking with the leaf postponed until every lane of the warp holds one),
+// then tests that leaf's triangles; finished lanes are checked for reference
+// visibility together. counters[4] is the batch cursor.
+template <bool SPEC>
+__global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                          int32_t* __restrict__ out_tid,
+                                                          float* __restrict__ out_dist,
+                                                          uint32_t* __restrict__ hit_leaf,
+                                                          unsigned long long* __restrict__ counters) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int DONE = INT_MIN;
+  const int lane = threadIdx.x & 31;
+  unsigned long long* cursor = counters + 4;
+  bool active = false, exhausted = false;
+  uint32_t ray = 0;
+  F3 o{}, d{}, inv{}, ood{};
+  float tlimit = INFINITY;
+  HitResult best{-1, -1.0f, 0u, 0u, false};
+  int stack_ref[kStack];
+  float stack_tn[kStack];
+  int sp = 0, cur = DONE, cnt = 0;
+  unsigned n_exact = 0;
+
+  auto pop = [&]() {
+    while (sp > 0) {
+      sp--;
+      if (stack_tn[sp] <= tlimit) {
+        int r = stack_ref[sp];
+        if (r < 0) {
+          int packed = ~r;
+          cnt = (packed & 7) + 1;
+          return ~(packed >> 3);
+        }
+        return r;
+      }
+    }
+    return DONE;
+  };
+
+  while (true) {
+    unsigned want = __ballot_sync(FULL, !active && !exhausted);
+    if (want) {
+      int leader = __ffs(want) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(cursor, (unsigned long long)__popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if (!active && !exhausted) {
+        unsigned long long r = base + __popc(want & ((1u << lane) - 1));
+        if (r < n) {
+          ray = (uint32_t)r;
+          const float4* rp = reinterpret_cast<const float4*>(rays + ray);
+          float4 ro = __ldg(rp), rd = __ldg(rp + 1);
+          o = f3(ro);
+          d = f3(rd);
+          inv = safe_inv(d);
+          ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
+          tlimit = INFINITY;
+          best = {-1, -1.0f, 0u, 0u, false};
+          sp = 0;
+          cur = 0;
+          cnt = 0;
+          active = true;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) break;
+
+    if (active) {
+      int pl = DONE, pcnt = 0;  // postponed leaf
+      while (true) {
+        if (cur >= 0) {
+          const float4* np = A.bvh + 4 * (size_t)cur;
+          float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+          int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+          float a0 = fmaf(n0.x, inv.x, -ood.x), b0 = fmaf(n0.y, inv.x, -ood.x);
+          float a1 = fmaf(n0.z, inv.y, -ood.y), b1 = fmaf(n0.w, inv.y, -ood.y);
+          float a2 = fmaf(n2.x, inv.z, -ood.z), b2 = fmaf(n2.y, inv.z, -ood.z);
+          float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
+          float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tlimit));
+          float c0 = fmaf(n1.x, inv.x, -ood.x), d0 = fmaf(n1.y, inv.x, -ood.x);
+          float c1 = fmaf(n1.z, inv.y, -ood.y), d1 = fmaf(n1.w, inv.y, -ood.y);
+          float c2 = fmaf(n2.z, inv.z, -ood.z), d2 = fmaf(n2.w, inv.z, -ood.z);
+          float tn1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), 0.0f));
+          float tf1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), tlimit));
+          bool h0 = tn0 <= tf0 * 1.0000005f, h1 = tn1 <= tf1 * 1.0000005f;
+          if (h0 && h1) {
+            bool first0 = tn0 <= tn1;
+            int near_ref = first0 ? n3.x : n3.y, far_ref = first0 ? n3.y : n3.x;
+            int near_cnt = first0 ? n3.z : n3.w, far_cnt = first0 ? n3.w : n3.z;
+            if (sp < kStack) {
+              stack_ref[sp] = far_ref < 0 ? ~((~far_ref) << 3 | (far_cnt - 1)) : far_ref;
+              stack_tn[sp] = first0 ? tn1 : tn0;
+              sp++;
+            }
+            cur = near_ref;
+            cnt = near_cnt;
+          } else if (h0) {
+            cur = n3.x;
+            cnt = n3.z;
+          } else if (h1) {
+            cur = n3.y;
+            cnt = n3.w;
+          } else {
+            cur = pop();
+          }
+        } else if (cur != DONE) {
+          if (pl != DONE) break;  // a second leaf waits for the next round
+          pl = cur;
+          pcnt = cnt;
+          cur = pop();
+        }
+        if (cur == DONE) break;
+        if (pl != DONE) {
+          if (!SPEC) break;
+          if (!__any_sync(__activemask(), pl == DONE)) break;
+        }
+      }
+      if (pl != DONE) {
+        int first = ~pl;
+        for (int k = 0; k < pcnt; k++) {
+          const float4* tp = A.tris + 3 * (size_t)(first + k);
+          float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+          float t;
+          if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
+            uint32_t leaf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
+            if (!best.hit || t < best.t ||
+                (t == best.t && (leaf > best.leaf || (leaf == best.leaf && pos < best.pos)))) {
+              best = {__float_as_int(v0.w), t, leaf, pos, true};
+              tlimit = t + A.prune_rel * (1.0f + t);
+            }
+          }
+        }
+      }
+    }
+
+    if (active && cur == DONE) {
+      out_tid[ray] = best.hit ? best.tid : -1;
+      out_dist[ray] = best.hit ? best.t : -1.0f;
+      hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+      active = false;
+    }
+  }
+  unsigned sum = n_exact;
+  for (int s2 = 16; s2 > 0; s2 >>= 1) sum += __shfl_xor_sync(FULL, sum, s2);
+  if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
 }
 
 // Re-traces the queued rays checking visibility at every improvement.
@@ -108,11 +304,26 @@ __global__ void __launch_bounds__(128) k_trace_reforder(DevAccel A, const rx_ray
 }
 
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
-                                 uint32_t* queue, unsigned long long* counters, cudaStream_t s) {
+                                 uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
+                                 cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  cudaMemsetAsync(counters, 0, sizeof(unsigned long long), s);  // queue length
-  k_trace_closest<<<(n + 127) / 128, 128, 0, s>>>(A, rays, n, tid, dist, queue, counters);
-  k_trace_eager<<<152, 128, 0, s>>>(A, rays, tid, dist, queue, counters);
+  cudaMemsetAsync(counters, 0, sizeof(unsigned long long), s);  // eager queue length
+  uint32_t* hit_leaf = queue;  // scratch: n entries of winners' reference leaves
+  uint32_t* eager = queue + n;  // then up to n queued rays
+  if (cfg.variant == 0) {
+    k_trace_closest<<<(n + 127) / 128, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
+  } else {
+    cudaMemsetAsync(counters + 4, 0, sizeof(unsigned long long), s);  // batch cursor
+    unsigned blocks = (unsigned)cfg.sms * (unsigned)cfg.blocks_per_sm;
+    unsigned need = (n + 127) / 128;
+    blocks = blocks < need ? blocks : need;
+    if (cfg.variant == 1)
+      k_trace_persistent<false><<<blocks, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
+    else
+      k_trace_persistent<true><<<blocks, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
+  }
+  k_check_visible<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, hit_leaf, eager, counters);
+  k_trace_eager<<<cfg.sms, 128, 0, s>>>(A, rays, tid, dist, eager, counters);
   return cudaGetLastError();
 }
 

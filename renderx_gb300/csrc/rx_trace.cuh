@@ -27,19 +27,30 @@ __device__ __forceinline__ F3 safe_inv(F3 d) {
 }
 
 // Reference visibility of a triangle in reference leaf `leaf`: every box on the root
-// path passes KDTree.cpp:107-125.
+// path passes KDTree.cpp:107-125. The root path comes from the per-leaf ancestor list,
+// read four boxes at a time so the loads are independent.
 __device__ __forceinline__ bool ref_visible(const DevAccel& A, uint32_t leaf, F3 o, F3 d, F3 inv, bool zero_dir,
                                             unsigned* n_exact) {
-  int node = A.ref_leaf_node[leaf];
-  for (int guard = 0; node >= 0 && guard < 1 << 20; guard++) {
-    float4 a = __ldg(&A.ref[2 * node]);
-    float4 b = __ldg(&A.ref[2 * node + 1]);
-    F3 mn = f3(a), mx = f3(b);
-    if (zero_dir || !box_clear_pass(mn, mx, o, d, inv)) {
-      (*n_exact)++;
-      if (!box_exact(mn, mx, o, d)) return false;
+  uint32_t b = __ldg(&A.anc_range[2 * leaf]), e = __ldg(&A.anc_range[2 * leaf + 1]);
+  for (uint32_t k = b; k < e; k += 4) {
+    int nd[4];
+    float4 lo[4], hi[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) nd[j] = (k + j < e) ? __ldg(&A.anc_nodes[k + j]) : -1;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int q = nd[j] < 0 ? 0 : nd[j];
+      lo[j] = __ldg(&A.ref[2 * q]);
+      hi[j] = __ldg(&A.ref[2 * q + 1]);
     }
-    node = __float_as_int(a.w);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (nd[j] < 0) continue;
+      if (zero_dir || !box_clear_pass(f3(lo[j]), f3(hi[j]), o, d, inv)) {
+        (*n_exact)++;
+        if (!box_exact(f3(lo[j]), f3(hi[j]), o, d)) return false;
+      }
+    }
   }
   return true;
 }

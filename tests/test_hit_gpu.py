@@ -18,9 +18,11 @@ def _bits_equal(a, b):
 
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("leaf_size", [1, 4, 8])
-def test_hits_match_reference_golden(name, leaf_size):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_hits_match_reference_golden(name, leaf_size, variant):
     z = load(name)
     with rx.Context(0) as ctx:
+        ctx.set_trace_config(variant, 4)
         ctx.set_geometry(z["verts"], z["tris"])
         ctx.build_accel(rx.SPLIT_GCC, leaf_size=leaf_size)
         tid, dist = ctx.trace_closest(z["origins"], z["dirs"])
