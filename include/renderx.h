@@ -71,6 +71,38 @@ typedef struct rx_ray {
   float dx, dy, dz, dw;
 } rx_ray;
 
+/* Pinhole camera with the reference's integer sightDist in pixels (reference
+ * include/Camera.h:10-31, ConfigManager.cpp:263-269). */
+typedef struct rx_camera {
+  uint32_t width, height;
+  uint32_t sight_dist;
+  uint32_t reserved;
+  float position[3];
+  float focus[3];
+  float up[3];
+} rx_camera;
+
+/* Path-tracing options. */
+typedef struct rx_pt_options {
+  uint32_t spp;            /* samples per pixel */
+  uint32_t max_depth;      /* MCRenderer::maxDepth (bounce rays per path) */
+  uint32_t rr_mode;        /* 0: the reference's Russian roulette at every bounce
+                              (p = max albedo); 1: roulette only from depth 3 on */
+  uint32_t nee;            /* 0: PathTracer (BSDF sampling only); 1: PathTracerTest
+                              (light sampling + balance-heuristic MIS) */
+  uint64_t seed;
+  uint32_t paths_per_pass; /* wavefront size, 0 = 2^21 */
+  uint32_t flags;          /* reserved, 0 */
+} rx_pt_options;
+
+typedef struct rx_render_stats {
+  uint64_t extension_rays; /* closest-hit rays traced (camera + bounce) */
+  uint64_t shadow_rays;    /* next-event-estimation visibility rays */
+  uint64_t paths;          /* pixel samples */
+  float ms;                /* device time of the render (CUDA events) */
+  float reserved;
+} rx_render_stats;
+
 /* ---- context ------------------------------------------------------------------- */
 /* Replaces the process-global GPU state of IntersectionGPU::init
  * (reference src/IntersectionGPU.cpp:16-44). */
@@ -119,6 +151,16 @@ rx_status rx_trace_closest_device(rx_context* ctx, const rx_ray* d_rays, uint32_
  * ray see, in the reference's own order (slow; a consistency check on small scenes). */
 rx_status rx_trace_closest_reforder_device(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
                                            float* d_dist, void* stream);
+/* ---- rendering ------------------------------------------------------------------ */
+/* MCRenderer::renderPixels(const Camera&) of PathTracer (reference
+ * src/PathTracer.cpp:6-89) or PathTracerTest (src/PathTracerTest.cpp:7-86) for a fixed
+ * sample count: film_rgb receives width*height*3 doubles, the per-pixel mean radiance,
+ * rows from the top (the order of renderPixels' vector<vec3f>). film_sq (optional)
+ * receives the per-pixel mean of squared sample values, for standard errors. Needs
+ * rx_scene_set_objects before rx_build_accel. */
+rx_status rx_render_pt(rx_context* ctx, const rx_camera* cam, const rx_pt_options* opts, double* film_rgb,
+                       double* film_sq, rx_render_stats* stats);
+
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
  * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative
  * leaf postponing; blocks of 128 threads, blocks_per_sm per SM. No reference

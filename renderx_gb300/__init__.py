@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 
 from . import _capi
-from ._capi import RxError, rx_build_options, rx_object
+from ._capi import RxError, rx_build_options, rx_camera, rx_object, rx_pt_options, rx_render_stats
 from . import scenes
 
 __all__ = ["Context", "KDTree", "RxError", "reftree_serialize", "scenes", "rays_to_array"]
@@ -137,6 +137,21 @@ class Context:
         self._ck(self._L.rx_trace_closest_reforder_device(self.h, _capi.ptr(d_rays), n, _capi.ptr(d_tid),
                                                           _capi.ptr(d_dist), _capi.stream_arg(stream)))
 
+    # -- rendering -------------------------------------------------------------------
+    def render_pt(self, camera: "scenes.Camera", spp: int, max_depth: int = 8, nee: bool = False, rr_mode: int = 0,
+                  seed: int = 1, paths_per_pass: int = 0, want_sq: bool = False):
+        """PathTracer (nee=False) or PathTracerTest (nee=True) renderPixels for ``spp``
+        samples: returns (mean (H,W,3) float64, mean of squares or None, stats dict)."""
+        cam = camera_struct(camera)
+        o = rx_pt_options(spp, max_depth, rr_mode, int(bool(nee)), seed, paths_per_pass, 0)
+        h, w = camera.height, camera.width
+        film = np.zeros((h, w, 3), np.float64)
+        sq = np.zeros((h, w, 3), np.float64) if want_sq else None
+        st = rx_render_stats()
+        self._ck(self._L.rx_render_pt(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), _capi.ptr(sq),
+                                      ctypes.byref(st)))
+        return film, sq, dict(extension_rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms)
+
     def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
@@ -144,6 +159,15 @@ class Context:
         out = np.zeros(4, np.uint64)
         self._ck(self._L.rx_trace_counters(self.h, _capi.ptr(out), int(reset)))
         return dict(exact_box_tests=int(out[1]), eager_retraces=int(out[2]), errors=int(out[3]))
+
+
+def camera_struct(c: "scenes.Camera") -> rx_camera:
+    r = rx_camera()
+    r.width, r.height, r.sight_dist = c.width, c.height, c.sight_dist
+    r.position[:] = c.position
+    r.focus[:] = c.focus
+    r.up[:] = c.up
+    return r
 
 
 def objects_from_scene(scene: "scenes.Scene"):

@@ -30,6 +30,23 @@ class rx_object(ctypes.Structure):
                 ("sigma_a", ctypes.c_float * 3), ("g", ctypes.c_float), ("decay", ctypes.c_float * 3)]
 
 
+class rx_camera(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("sight_dist", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("position", ctypes.c_float * 3), ("focus", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3)]
+
+
+class rx_pt_options(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("rr_mode", ctypes.c_uint32),
+                ("nee", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("paths_per_pass", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32)]
+
+
+class rx_render_stats(ctypes.Structure):
+    _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64), ("paths", ctypes.c_uint64),
+                ("ms", ctypes.c_float), ("reserved", ctypes.c_float)]
+
+
 class rx_build_options(ctypes.Structure):
     _fields_ = [("split_policy", ctypes.c_int32), ("leaf_size", ctypes.c_int32), ("host_threads", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]
@@ -54,6 +71,7 @@ SIGNATURES = [
     ("rx_trace_closest_reforder_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_counters", S, [P, P, S]),
     ("rx_trace_set_config", S, [P, I32, I32]),
+    ("rx_render_pt", S, [P, P, P, P, P, P]),
 ]
 
 

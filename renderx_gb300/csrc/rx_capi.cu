@@ -68,7 +68,8 @@ void rx_destroy(rx_context* c) {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
     for (DevBuf* b : {&c->d_bvh, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
-                      &c->d_anc_range, &c->d_anc_nodes,
+                      &c->d_anc_range, &c->d_anc_nodes, &c->d_slot_n, &c->d_tri_v, &c->d_tri_n, &c->d_tri_obj,
+                      &c->d_objects, &c->d_light_cdf, &c->d_light_tri,
                       &c->d_counters, &c->d_queue})
       b->release();
     for (int k = 0; k < 2; k++)
@@ -222,6 +223,144 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.prune_rel = 1e-3f;
   c->accel_ready = true;
   c->geometry_dirty = false;
+  if (!c->objects.empty()) return c->build_scene();
+  return RX_OK;
+}
+
+}  // extern "C"
+
+// Shading data for the light-transport kernels: objects, per-triangle vertices and
+// normals (vertex normals where the object has them, else the face normal), the same
+// normals in BVH slot order for the traversal's self-intersection condition, and the
+// emitter sampler (cumulative triangle areas over the emissive objects, the product of
+// Scene::SurfaceSampler's object choice and SceneObject::emit's triangle choice).
+rx_status rx_context::build_scene() {
+  rx_context* c = this;
+  uint32_t nt = (uint32_t)(c->tris.size() / 3), nobj = (uint32_t)c->objects.size();
+  for (uint32_t i = 0; i < nt; i++)
+    if (c->tri_obj[i] >= nobj) return c->fail(RX_ERR_INVALID, "triangle object id out of range");
+  for (uint32_t o = 0; o < nobj; o++)
+    if (c->objects[o].material > RX_MAT_VPM) return c->fail(RX_ERR_INVALID, "unknown material");
+  const float* V = c->verts.data();
+  auto vtx = [&](uint32_t t, int k) {
+    const float* p = V + 3 * (size_t)c->tris[3 * (size_t)t + k];
+    return make_float4(p[0], p[1], p[2], 0.0f);
+  };
+  std::vector<float4> tv(3 * (size_t)nt), tn(3 * (size_t)nt), sn(3 * (size_t)nt);
+  for (uint32_t t = 0; t < nt; t++) {
+    float4 a = vtx(t, 0), b = vtx(t, 1), d = vtx(t, 2);
+    tv[3 * (size_t)t] = a;
+    tv[3 * (size_t)t + 1] = b;
+    tv[3 * (size_t)t + 2] = d;
+    bool vn = c->has_normals && c->objects[c->tri_obj[t]].has_vertex_normals;
+    float e1[3] = {b.x - a.x, b.y - a.y, b.z - a.z}, e2[3] = {d.x - a.x, d.y - a.y, d.z - a.z};
+    float fn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    float l = std::sqrt(fn[0] * fn[0] + fn[1] * fn[1] + fn[2] * fn[2]);
+    if (l > 0) for (float& x : fn) x /= l;
+    for (int k = 0; k < 3; k++) {
+      if (vn) {
+        const float* q = c->vnormals.data() + 3 * (size_t)c->tris[3 * (size_t)t + k];
+        tn[3 * (size_t)t + k] = make_float4(q[0], q[1], q[2], 0.0f);
+      } else {
+        tn[3 * (size_t)t + k] = make_float4(fn[0], fn[1], fn[2], 0.0f);
+      }
+    }
+  }
+  for (uint32_t s = 0; s < nt; s++) {
+    uint32_t t = c->bvh.tri_order[s];
+    for (int k = 0; k < 3; k++) sn[3 * (size_t)s + k] = tn[3 * (size_t)t + k];
+    uint32_t ob = c->tri_obj[t];
+    std::memcpy(&sn[3 * (size_t)s].w, &ob, 4);
+  }
+  std::vector<rx::DevObject> objs(nobj);
+  std::vector<float> cdf;
+  std::vector<uint32_t> ltri;
+  double acc = 0;
+  for (uint32_t o = 0; o < nobj; o++) {
+    const rx_object& r = c->objects[o];
+    rx::DevObject& d = objs[o];
+    d.material = r.material;
+    d.has_normals = (c->has_normals && r.has_vertex_normals) ? 1 : 0;
+    d.tri_begin = r.tri_begin;
+    d.tri_count = r.tri_count;
+    std::memcpy(d.color, r.color, sizeof d.color);
+    d.coeff = r.coeff;
+    std::memcpy(d.diffuse_color, r.diffuse_color, sizeof d.diffuse_color);
+    d.ior = r.ior;
+    std::memcpy(d.sigma_s, r.sigma_s, sizeof d.sigma_s);
+    std::memcpy(d.sigma_a, r.sigma_a, sizeof d.sigma_a);
+    d.g = r.g;
+    std::memcpy(d.decay, r.decay, sizeof d.decay);
+  }
+  for (uint32_t t = 0; t < nt; t++) {
+    if (c->objects[c->tri_obj[t]].material != RX_MAT_EMISSIVE) continue;
+    float4 a = tv[3 * (size_t)t], b = tv[3 * (size_t)t + 1], d = tv[3 * (size_t)t + 2];
+    // SimpleShape::getTriangleArea: |(v1-v0) x (v2-v1)| / 2
+    double l0[3] = {b.x - a.x, b.y - a.y, b.z - a.z}, l1[3] = {d.x - b.x, d.y - b.y, d.z - b.z};
+    double cx = l0[1] * l1[2] - l0[2] * l1[1], cy = l0[2] * l1[0] - l0[0] * l1[2], cz = l0[0] * l1[1] - l0[1] * l1[0];
+    acc += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+    cdf.push_back((float)acc);
+    ltri.push_back(t);
+  }
+  DeviceGuard g(c->device);
+  rx_status st;
+  if ((st = upload(c, c->d_tri_v, tv.data(), tv.size() * sizeof(float4), "upload triangle vertices")) != RX_OK) return st;
+  if ((st = upload(c, c->d_tri_n, tn.data(), tn.size() * sizeof(float4), "upload triangle normals")) != RX_OK) return st;
+  if ((st = upload(c, c->d_slot_n, sn.data(), sn.size() * sizeof(float4), "upload slot normals")) != RX_OK) return st;
+  if ((st = upload(c, c->d_tri_obj, c->tri_obj.data(), nt * 4, "upload triangle objects")) != RX_OK) return st;
+  if ((st = upload(c, c->d_objects, objs.data(), objs.size() * sizeof(rx::DevObject), "upload objects")) != RX_OK)
+    return st;
+  if (!cdf.empty()) {
+    if ((st = upload(c, c->d_light_cdf, cdf.data(), cdf.size() * 4, "upload light cdf")) != RX_OK) return st;
+    if ((st = upload(c, c->d_light_tri, ltri.data(), ltri.size() * 4, "upload light triangles")) != RX_OK) return st;
+  }
+  rx::DevScene& S = c->scene;
+  S.accel = c->accel;
+  S.slot_n = c->d_slot_n.as<float4>();
+  S.tri_v = c->d_tri_v.as<float4>();
+  S.tri_n = c->d_tri_n.as<float4>();
+  S.tri_obj = c->d_tri_obj.as<uint32_t>();
+  S.objects = c->d_objects.as<rx::DevObject>();
+  S.num_objects = nobj;
+  S.light_cdf = c->d_light_cdf.as<float>();
+  S.light_tri = c->d_light_tri.as<uint32_t>();
+  S.num_lights = (uint32_t)cdf.size();
+  S.light_area = (float)acc;
+  c->scene_ready = true;
+  return RX_OK;
+}
+
+extern "C" {
+
+rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options* opts, double* film_rgb,
+                       double* film_sq, rx_render_stats* stats) {
+  if (!c) return RX_ERR_INVALID;
+  if (!cam || !opts || !film_rgb) return c->fail(RX_ERR_INVALID, "null argument");
+  if (!c->scene_ready) return c->fail(RX_ERR_STATE, "scene objects not built (rx_scene_set_objects, rx_build_accel)");
+  if (cam->width == 0 || cam->height == 0 || cam->sight_dist == 0) return c->fail(RX_ERR_INVALID, "bad camera");
+  if (opts->spp == 0) return c->fail(RX_ERR_INVALID, "spp must be positive");
+  if (opts->max_depth > 1000) return c->fail(RX_ERR_INVALID, "max_depth too large");
+  if (opts->nee && c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
+  DeviceGuard g(c->device);
+  size_t np = (size_t)cam->width * cam->height;
+  DevBuf sum, sq;
+  rx_status s;
+  if ((s = c->cuda(sum.alloc(np * 3 * sizeof(double)), "film")) != RX_OK) return s;
+  if (film_sq && (s = c->cuda(sq.alloc(np * 3 * sizeof(double)), "film")) != RX_OK) return s;
+  cudaMemsetAsync(sum.p, 0, sum.bytes, c->stream);
+  if (film_sq) cudaMemsetAsync(sq.p, 0, sq.bytes, c->stream);
+  rx_render_stats st{};
+  if ((s = c->cuda(rx::render_pt(c, *cam, *opts, sum.as<double>(), film_sq ? sq.as<double>() : nullptr, &st, c->stream),
+                   "render_pt")) != RX_OK)
+    return s;
+  std::vector<double> h(np * 3);
+  if ((s = c->cuda(cudaMemcpy(h.data(), sum.p, sum.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
+  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->spp;
+  if (film_sq) {
+    if ((s = c->cuda(cudaMemcpy(h.data(), sq.p, sq.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
+    for (size_t k = 0; k < h.size(); k++) film_sq[k] = h[k] / opts->spp;
+  }
+  if (stats) *stats = st;
   return RX_OK;
 }
 

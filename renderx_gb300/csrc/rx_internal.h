@@ -8,6 +8,7 @@
 #include "../../include/renderx.h"
 #include "rx_accel.h"
 #include "rx_device.h"
+#include "rx_scene.h"
 
 namespace rx {
 
@@ -26,6 +27,7 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
 cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                   unsigned long long* counters, cudaStream_t s);
 
+struct rx_context_fwd;
 // A device allocation owned by the context.
 struct DevBuf {
   void* p = nullptr;
@@ -69,12 +71,16 @@ struct rx_context {
   rx::TraceConfig trace_cfg;
   bool accel_ready = false;
   rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes;
+  rx::DevScene scene{};
+  bool scene_ready = false;
+  rx::DevBuf d_slot_n, d_tri_v, d_tri_n, d_tri_obj, d_objects, d_light_cdf, d_light_tri;
   rx::DevBuf d_counters;     // 4 x u64 diagnostics + per-slot queue lengths
   rx::DevBuf d_queue;        // closest-hit scratch (winner leaves + eager queue)
   // staging ring for host-buffer calls
   rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
   size_t ring_chunk = 0;
 
+  rx_status build_scene();
   rx_status fail(rx_status s, const std::string& m) {
     err = m;
     return s;
@@ -85,3 +91,9 @@ struct rx_context {
     return e == cudaErrorMemoryAllocation ? RX_ERR_OOM : RX_ERR_CUDA;
   }
 };
+
+namespace rx {
+// Path tracing (rx_pt.cu): renders into device films (sum, optional sum of squares).
+cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& opt, double* film_sum,
+                      double* film_sq, rx_render_stats* stats, cudaStream_t s);
+}  // namespace rx

@@ -1,0 +1,227 @@
+// Device building blocks of the light-transport kernels: vector math, the counter-based
+// random numbers, shading normals, the reference's materials and the condition-aware
+// closest-hit / occlusion queries.
+//
+// Sampling semantics follow the reference (cited per function); arithmetic here is
+// ordinary fast FP32 with FMA (statistical parity, not bit parity).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rx_exact.cuh"
+#include "rx_scene.h"
+
+namespace rx {
+
+#define RX_PI 3.14159265358979323846f
+
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ F3 operator*(float s, F3 a) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ F3 operator*(F3 a, F3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 cross(F3 l, F3 r) {
+  return {l.y * r.z - l.z * r.y, l.z * r.x - l.x * r.z, l.x * r.y - l.y * r.x};
+}
+__device__ __forceinline__ float length(F3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ F3 normalize(F3 a) {
+  float l = length(a);
+  return l > 0.0f ? a * (1.0f / l) : a;
+}
+__device__ __forceinline__ float maxc(F3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+// luminance weights of smallFuncs.h y()/intensity()
+__device__ __forceinline__ float lum(F3 a) { return 0.212671f * a.x + 0.715160f * a.y + 0.072169f * a.z; }
+__device__ __forceinline__ F3 f3v(const float* p) { return {p[0], p[1], p[2]}; }
+
+// ---- random numbers ------------------------------------------------------------------
+// Counter-based: value k of path `path` under `seed` is a 64-bit mix (splitmix64
+// finaliser) of (seed, path, k), 24-bit floats in [0,1) like RNG::randFloat
+// (reference src/RandGenerator.cpp:21-25). Paths are independent and reproducible,
+// with no shared state (the reference's single global MT19937 is raced by all its
+// OpenMP threads, RandGenerator.cpp:9).
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+struct Rng {
+  uint64_t key;
+  uint32_t k;
+  __device__ __forceinline__ Rng(uint64_t seed, uint64_t path, uint32_t start)
+      : key(mix64(seed ^ mix64(path + 0x9e3779b97f4a7c15ull))), k(start) {}
+  __device__ __forceinline__ float next() {
+    uint64_t h = mix64(key + 0x9e3779b97f4a7c15ull * (uint64_t)(++k));
+    return (float)(uint32_t)(h >> 40) * (1.0f / 16777216.0f);
+  }
+};
+
+// ---- local frames and samplers ---------------------------------------------------------
+// LocalFrame::buildFromNormal / toWorld, reference include/LocalFrame.h:13-33.
+struct Frame {
+  F3 s, t, n;
+};
+__device__ __forceinline__ Frame frame_from(F3 n) {
+  F3 tmp = fabsf(n.z) > 0.99f ? F3{1, 0, 0} : F3{0, 0, 1};
+  Frame f;
+  f.n = n;
+  f.s = normalize(cross(n, tmp));
+  f.t = normalize(cross(f.s, f.n));
+  return f;
+}
+__device__ __forceinline__ F3 to_world(const Frame& f, F3 a) { return f.s * a.x + f.n * a.y + f.t * a.z; }
+// RandGenerator::genHemiCosDirection, src/RandGenerator.cpp:152-167 (cos^exp lobe
+// around the frame's n; exp = 1 is cosine sampling).
+__device__ __forceinline__ F3 hemi_cos(float e, float r1, float r2) {
+  float u1 = 2.0f * RX_PI * r1;
+  float u2 = e == 1.0f ? sqrtf(r2) : powf(r2, 1.0f / (e + 1.0f));
+  float u3 = sqrtf(fmaxf(0.0f, 1.0f - u2 * u2));
+  float s, c;
+  sincosf(u1, &s, &c);
+  return normalize(F3{c * u3, u2, s * u3});
+}
+// CosineSphericalSampler::getProbDensity, include/CosineSphericalSampler.h:292-303
+__device__ __forceinline__ float cos_lobe_pdf(F3 n, F3 dir, float e) {
+  float ct = fmaxf(dot(n, dir), 0.0f);
+  float p = e == 1.0f ? ct : powf(ct, e);
+  return p * (e + 1.0f) / (2.0f * RX_PI);
+}
+
+// ---- normals -------------------------------------------------------------------------
+struct TriGeom {
+  F3 v0, v1, v2, n0, n1, n2;
+  int obj;
+};
+__device__ __forceinline__ TriGeom tri_geom(const DevScene& S, int tid) {
+  TriGeom g;
+  const float4* v = S.tri_v + 3 * (size_t)tid;
+  const float4* n = S.tri_n + 3 * (size_t)tid;
+  g.v0 = f3(__ldg(v));
+  g.v1 = f3(__ldg(v + 1));
+  g.v2 = f3(__ldg(v + 2));
+  g.n0 = f3(__ldg(n));
+  g.n1 = f3(__ldg(n + 1));
+  g.n2 = f3(__ldg(n + 2));
+  g.obj = (int)__ldg(&S.tri_obj[tid]);
+  return g;
+}
+// SimpleShape::getWorldNormal (src/SimpleShape.cpp:393-441): face normal without vertex
+// normals, else the vertex normals interpolated with the barycentric coordinates of
+// `p` (same u1, u2 formula); flat = face normal turned toward the interpolated one.
+__device__ __forceinline__ F3 world_normal(const TriGeom& g, bool has_normals, F3 p, bool flat = false) {
+  F3 b1 = g.v1 - g.v0, b2 = g.v2 - g.v0;
+  F3 fn = normalize(cross(b1, b2));
+  if (!has_normals) return fn;
+  F3 v = p - g.v0;
+  float d12 = dot(b1, b2), l1s = dot(b1, b1), l2s = dot(b2, b2);
+  float u2 = (dot(v, b1) * d12 - dot(v, b2) * l1s) / (d12 * d12 - l1s * l2s);
+  float u1 = (dot(v, b1) - u2 * d12) / l1s;
+  F3 n = normalize(g.n0 * (1.0f - u1 - u2) + g.n1 * u1 + g.n2 * u2);
+  if (flat) return dot(n, fn) < 0.0f ? -fn : fn;
+  return n;
+}
+
+// ---- self-intersection condition + closest hit ---------------------------------------
+// NoSelfIntersectionCondition::legal (src/NoSelfIntersectionCondition.cpp:12-27),
+// evaluated on every candidate before the closest one is chosen (KDTree.cpp:363):
+// the sign of the direction against the candidate's shading normal decides.
+__device__ __forceinline__ bool legal_hit(int contact, int inside, int obj, float dn) {
+  bool in = dn <= 0.0f, out = dn >= 0.0f;
+  if (inside == contact) return !(in && contact == obj);
+  return !(out && inside != obj);
+}
+
+struct PHit {
+  int tid;
+  float t;
+};
+
+// Closest legal hit with t < tmax (ANY: stop at the first legal one). contact, inside:
+// object ids, -1 for none (camera rays use -1/-1: no condition).
+template <bool ANY>
+__device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
+  const DevAccel& A = S.accel;
+  F3 inv = {fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(1e30f, d.x),
+            fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(1e30f, d.y),
+            fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(1e30f, d.z)};
+  F3 ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
+  PHit best{-1, tmax};
+  int stack[kStackDepth];
+  int sp = 0, cur = 0, cnt = 0;
+  const bool cond = !(contact < 0 && inside < 0);
+  while (true) {
+    if (cur >= 0) {
+      const float4* np = A.bvh + 4 * (size_t)cur;
+      float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+      int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+      float a0 = fmaf(n0.x, inv.x, -ood.x), b0 = fmaf(n0.y, inv.x, -ood.x);
+      float a1 = fmaf(n0.z, inv.y, -ood.y), b1 = fmaf(n0.w, inv.y, -ood.y);
+      float a2 = fmaf(n2.x, inv.z, -ood.z), b2 = fmaf(n2.y, inv.z, -ood.z);
+      float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
+      float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), best.t));
+      float c0 = fmaf(n1.x, inv.x, -ood.x), d0 = fmaf(n1.y, inv.x, -ood.x);
+      float c1 = fmaf(n1.z, inv.y, -ood.y), d1 = fmaf(n1.w, inv.y, -ood.y);
+      float c2 = fmaf(n2.z, inv.z, -ood.z), d2 = fmaf(n2.w, inv.z, -ood.z);
+      float tn1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), 0.0f));
+      float tf1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), best.t));
+      bool h0 = tn0 <= tf0 * 1.0000005f, h1 = tn1 <= tf1 * 1.0000005f;
+      if (h0 && h1) {
+        bool first0 = tn0 <= tn1;
+        int far_ref = first0 ? n3.y : n3.x, far_cnt = first0 ? n3.w : n3.z;
+        if (sp < kStackDepth) stack[sp++] = far_ref < 0 ? ~((~far_ref) << 3 | (far_cnt - 1)) : far_ref;
+        cur = first0 ? n3.x : n3.y;
+        cnt = first0 ? n3.z : n3.w;
+        continue;
+      } else if (h0) {
+        cur = n3.x;
+        cnt = n3.z;
+        continue;
+      } else if (h1) {
+        cur = n3.y;
+        cnt = n3.w;
+        continue;
+      }
+    } else {
+      int first = ~cur;
+      for (int k = 0; k < cnt; k++) {
+        const float4* tp = A.tris + 3 * (size_t)(first + k);
+        float4 w0 = __ldg(tp), w1 = __ldg(tp + 1), w2 = __ldg(tp + 2);
+        F3 v0 = f3(w0), e1 = f3(w1) - v0, e2 = f3(w2) - v0;
+        F3 pv = cross(d, e2);
+        float det = dot(e1, pv);
+        if (fabsf(det) < 1e-30f) continue;
+        float idet = 1.0f / det;
+        F3 sv = o - v0;
+        float u = dot(sv, pv) * idet;
+        if (u < -1e-7f || u > 1.0000001f) continue;
+        F3 qv = cross(sv, e1);
+        float v = dot(d, qv) * idet;
+        if (v < -1e-7f || u + v > 1.0000001f) continue;
+        float t = dot(e2, qv) * idet;
+        if (!(t >= 0.0f) || !(t < best.t)) continue;
+        if (cond) {
+          const float4* nn = S.slot_n + 3 * (size_t)(first + k);
+          float4 q0 = __ldg(nn), q1 = __ldg(nn + 1), q2 = __ldg(nn + 2);
+          int obj = __float_as_int(q0.w);
+          F3 n = normalize(f3(q0) * (1.0f - u - v) + f3(q1) * u + f3(q2) * v);
+          if (!legal_hit(contact, inside, obj, dot(d, n))) continue;
+        }
+        best = {__float_as_int(w0.w), t};
+        if (ANY) return best;
+      }
+    }
+    if (sp == 0) break;
+    int r = stack[--sp];
+    if (r < 0) {
+      int packed = ~r;
+      cur = ~(packed >> 3);
+      cnt = (packed & 7) + 1;
+    } else {
+      cur = r;
+    }
+  }
+  return best;
+}
+
+}  // namespace rx

@@ -302,12 +302,29 @@ def hit_rays(n: int, seed: int = 7, lo: float = 0.0, hi: float = ROOM):
     return o, d
 
 
+def material_spheres(width: int = 64, height: int = 64, subdiv: int = 2) -> Scene:
+    """The Cornell room with five smooth-shaded icospheres (vertex normals), one per
+    material: diffuse, Phong-lobe glossy, dielectric (IOR 1.5), Phong (glossy +
+    diffuse) and mirror."""
+    sc = cornell_box(width, height)
+    uv, uf = icosphere(subdiv)
+    specs = [((0.8, 0.5, 3.5), 0.5, Material(DIFFUSE, (0.7, 0.35, 0.2))),
+             ((1.85, 2.2, 1.69), 0.5, Material(GLOSSY, (0.8, 0.8, 0.6), coeff=60.0)),
+             ((4.3, 0.8, 1.4), 0.8, Material(REFRACTIVE, (1.0, 1.0, 1.0), ior=1.5)),
+             ((3.1, 0.4, 0.45), 0.4, Material(PHONG, (0.5, 0.5, 0.5), coeff=30.0, diffuse_color=(0.2, 0.4, 0.6))),
+             ((4.0, 4.0, 1.2), 0.5, Material(REFLECTIVE, (0.9, 0.9, 0.9), ior=-1.0))]
+    for k, (c, r, m) in enumerate(specs):
+        p = np.asarray(c)[None, :] + r * uv
+        sc.objects.append(Obj(f"ball{k}", p.astype(np.float32), uf.astype(np.uint32), m, uv.astype(np.float32)))
+    return sc
+
+
 def medium_scene(width: int = 512, height: int = 512) -> Scene:
     """The Cornell room plus a dielectric sphere (r=1.0, IOR 1.5) filled with a
     homogeneous medium sigma_s=0.5, sigma_a=0.05 per unit, HG g=0.7."""
     sc = cornell_box(width, height)
     uv, uf = icosphere(4)
-    c = np.array([2.78, 1.9, 2.2])
+    c = np.array([2.78, 3.0, 1.5])
     p = c[None, :] + 1.0 * uv
     mat = Material(VPM, (1.0, 1.0, 1.0), ior=1.5, sigma_s=(0.5, 0.5, 0.5), sigma_a=(0.05, 0.05, 0.05), g=0.7)
     sc.objects.append(Obj("medium", p.astype(np.float32), uf.astype(np.uint32), mat, uv.astype(np.float32)))

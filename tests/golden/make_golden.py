@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
 sys.path.insert(0, ROOT)
 
-from renderx_gb300 import scenes  # noqa: E402
+from renderx_gb300 import scenes, sceneio  # noqa: E402
 
 CASES = {
     # name: (n_spheres, subdiv, scene seed, random rays, store geometry)
@@ -101,9 +101,48 @@ def run_reference(ref_bin: str, verts, tris, o, d):
                 np.fromfile(p + ".nodes.f32", np.float32).reshape(-1, 12), np.fromfile(p + ".leaf.f32", np.float32))
 
 
+# Path-tracing goldens: (scene function, renderer mode, max depth, spp). The reference
+# renders through its own ConfigManager from the XML/OBJ files sceneio writes.
+RENDER_CASES = {
+    "cornell_pt": ("cornell_box", "pt", 8, 4096),
+    "cornell_nee": ("cornell_box", "ptnee", 8, 4096),
+    "spheres_pt": ("material_spheres", "pt", 8, 4096),
+    "spheres_nee": ("material_spheres", "ptnee", 8, 4096),
+}
+
+
+def render_scene(name: str, w: int = 64, h: int = 64) -> scenes.Scene:
+    return getattr(scenes, name)(w, h)
+
+
+def make_render_goldens(ref_pt: str):
+    for case, (scene_fn, mode, depth, spp) in RENDER_CASES.items():
+        sc = render_scene(scene_fn)
+        f = sc.flatten()
+        with tempfile.TemporaryDirectory() as td:
+            cfg = sceneio.write_config(sc, td, "PTtest" if mode == "ptnee" else "PT", depth)
+            pre = os.path.join(td, "out")
+            out = subprocess.run([ref_pt, cfg, mode, str(spp), pre, "8"], check=True, capture_output=True,
+                                 text=True, cwd=td).stdout.split()
+            s1 = np.fromfile(pre + ".sum.f64").reshape(sc.camera.height, sc.camera.width, 3)
+            s2 = np.fromfile(pre + ".sq.f64").reshape(sc.camera.height, sc.camera.width, 3)
+        mean = s1 / spp
+        var = np.maximum(s2 / spp - mean * mean, 0.0) * spp / (spp - 1)
+        path = os.path.join(HERE, f"render_{case}.npz")
+        np.savez_compressed(path, mean=mean.astype(np.float32), stderr=np.sqrt(var / spp).astype(np.float32),
+                            spp=np.int64(spp), max_depth=np.int64(depth), mode=np.array(mode),
+                            scene=np.array(scene_fn), segments=np.int64(out[3]), seconds=np.float64(out[4]),
+                            geometry_sha256=np.array(geometry_hash(f["verts"], f["tris"])))
+        print(f"{path}: {spp} spp, mean {mean.mean(axis=(0, 1))}, {out[4]} s")
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else "/root/reference"
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"], check=True)
+    make_render_goldens(os.path.join(ROOT, "oracle", "_ref", "pt_driver"))
+    if "--render-only" in sys.argv:
+        return
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "hit_driver")
     for name, (ns, sub, seed, nrand, store) in CASES.items():
         f = make_scene(ns, sub, seed)

@@ -1,0 +1,118 @@
+"""GPU path-tracing parity: the wavefront PathTracer / PathTracerTest estimators agree
+per pixel with the reference's own renders (golden images made by the reference code
+through its ConfigManager, tests/golden/render_*.npz) within 3 sigma of the combined
+Monte Carlo standard error.
+
+Tolerance: a pixel channel fails when |gpu - ref| > 3 * sqrt(se_gpu^2 + se_ref^2) +
+1e-4. An unbiased match fails ~0.3% of channels; the test allows 1% per pixel and
+none beyond 8 sigma. The GPU renders 8192 samples against the reference's 4096: both
+sides must carry comparable noise, because the estimators are heavy-tailed (rare light
+hits) and a pixel's sample variance underestimates its error exactly where its mean
+falls short; when one side's error is made negligible the test would rest on the other
+side's biased error estimate alone. On 4x4 pixel blocks at most 1% of block channels
+may fail 3 sigma and none 6 sigma, and the image means per channel must agree within
+4 standard errors of the image mean."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import renderx_gb300 as rx
+from renderx_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+CASES = ["cornell_pt", "cornell_nee", "spheres_pt", "spheres_nee"]
+
+
+def load_case(name):
+    z = dict(np.load(os.path.join(GOLDEN, f"render_{name}.npz")))
+    sc = getattr(scenes, str(z["scene"]))(64, 64)
+    f = sc.flatten()
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(f["verts"], np.float32).tobytes())
+    h.update(np.ascontiguousarray(f["tris"], np.uint32).tobytes())
+    assert h.hexdigest() == str(z["geometry_sha256"])
+    return z, sc
+
+
+def compare(mean, se, ref_mean, ref_se):
+    sig = np.sqrt(se ** 2 + ref_se ** 2)
+    z = np.abs(mean - ref_mean) / (sig + 1e-12)
+    bad3 = (np.abs(mean - ref_mean) > 3 * sig + 1e-4)
+    return z, bad3
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_render_matches_reference_within_3_sigma(name):
+    z, sc = load_case(name)
+    spp = 8192
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        mean, sq, st = ctx.render_pt(sc.camera, spp, max_depth=int(z["max_depth"]), nee=str(z["mode"]) == "ptnee",
+                                     rr_mode=0, seed=12345, want_sq=True)
+    var = np.maximum(sq - mean * mean, 0.0) * spp / (spp - 1)
+    se = np.sqrt(var / spp)
+    zz, bad = compare(mean, se, z["mean"].astype(np.float64), z["stderr"].astype(np.float64))
+    frac = bad.mean()
+    assert frac <= 0.01, f"{frac:.4f} of channels beyond 3 sigma (max z {zz.max():.1f})"
+    assert (zz > 8).sum() == 0, f"channels beyond 8 sigma: {(zz > 8).sum()}"
+    # 4x4 blocks: means of 16 pixels, standard errors combined in quadrature
+    def blocks(a, e):
+        h, w, _ = a.shape
+        m = a.reshape(h // 4, 4, w // 4, 4, 3).mean(axis=(1, 3))
+        v = (e.reshape(h // 4, 4, w // 4, 4, 3) ** 2).sum(axis=(1, 3)) / 256.0
+        return m, np.sqrt(v)
+    bm, bs = blocks(mean, se)
+    rm, rs = blocks(z["mean"].astype(np.float64), z["stderr"].astype(np.float64))
+    bz, bbad = compare(bm, bs, rm, rs)
+    assert bbad.mean() <= 0.01, f"{bbad.mean():.4f} of block channels beyond 3 sigma"
+    assert (bz > 6).sum() == 0, f"block channels beyond 6 sigma: {(bz > 6).sum()} (max {bz.max():.1f})"
+    n = mean.shape[0] * mean.shape[1]
+    for c in range(3):
+        dm = mean[..., c].mean() - z["mean"][..., c].astype(np.float64).mean()
+        s_img = np.sqrt((se[..., c] ** 2).sum() + (z["stderr"][..., c].astype(np.float64) ** 2).sum()) / n
+        assert abs(dm) < 4 * s_img, (c, dm, s_img)
+    assert st["extension_rays"] >= 64 * 64 * spp
+
+
+def test_render_is_deterministic_for_a_seed():
+    sc = scenes.cornell_box(32, 32)
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        a, _, _ = ctx.render_pt(sc.camera, 64, max_depth=8, seed=7)
+        b, _, _ = ctx.render_pt(sc.camera, 64, max_depth=8, seed=7)
+        c, _, _ = ctx.render_pt(sc.camera, 64, max_depth=8, seed=8)
+    # FP64 film atomics sum in varying order: equal to rounding, different seeds differ
+    assert np.allclose(a, b, rtol=1e-12, atol=1e-12)
+    assert not np.allclose(a, c)
+
+
+def test_render_rejects_bad_arguments():
+    sc = scenes.cornell_box(8, 8)
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(sc.flatten()["verts"], sc.flatten()["tris"])
+        ctx.build_accel()
+        with pytest.raises(rx.RxError):  # no objects uploaded
+            ctx.render_pt(sc.camera, 4)
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        with pytest.raises(rx.RxError):
+            ctx.render_pt(sc.camera, 0)
+
+
+def test_baseline_roulette_mode_converges_to_the_same_image():
+    """RR only from depth 3 on (rr_mode 1) changes variance, not the expectation."""
+    sc = scenes.cornell_box(32, 32)
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        a, sa, _ = ctx.render_pt(sc.camera, 4096, max_depth=8, rr_mode=0, seed=1, want_sq=True)
+        b, sb, _ = ctx.render_pt(sc.camera, 4096, max_depth=8, rr_mode=1, seed=2, want_sq=True)
+    sea = np.sqrt(np.maximum(sa - a * a, 0) / 4096)
+    seb = np.sqrt(np.maximum(sb - b * b, 0) / 4096)
+    _, bad = compare(a, sea, b, seb)
+    assert bad.mean() < 0.02
