@@ -147,6 +147,19 @@ rx_status rx_trace_closest(rx_context* ctx, const rx_ray* rays, uint32_t n, int3
  * the context's stream). */
 rx_status rx_trace_closest_device(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
                                   float* d_dist, void* stream);
+/* Same answers as rx_trace_closest_device, for callers that cannot allocate device
+ * memory while they trace (a host whose device memory belongs to its own pool
+ * allocator, or a latency-sensitive loop that must not pay cudaMalloc's implicit
+ * synchronisation). No counterpart in the reference. It calls no cudaMalloc/cudaFree:
+ * its scratch (winner leaves, re-walk queue, counters) is one fixed device array of
+ * 8 MiB that every GPU loading the library holds until exit. At most 1048576 rays
+ * per call; larger batches are rejected with RX_ERR_INVALID. The first call on a
+ * device looks up the array's device address with that device current; make that
+ * first call before any stream capture. All calls share the one array: calls whose
+ * work overlaps on the GPU (other streams, other contexts on the device) race on it
+ * and must be serialised by the caller. Requires a built accelerator. */
+rx_status rx_trace_closest_noalloc(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
+                                   float* d_dist, void* stream);
 /* Same semantics, without the BVH: walks every triangle the reference tree lets the
  * ray see, in the reference's own order (slow; a consistency check on small scenes). */
 rx_status rx_trace_closest_reforder_device(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,

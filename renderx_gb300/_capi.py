@@ -68,6 +68,7 @@ SIGNATURES = [
     ("rx_reftree_serialize", S, [P, U32, P, U32, I32, P, P, P, P]),
     ("rx_trace_closest", S, [P, P, U32, P, P]),
     ("rx_trace_closest_device", S, [P, P, U32, P, P, P]),
+    ("rx_trace_closest_noalloc", S, [P, P, U32, P, P, P]),
     ("rx_trace_closest_reforder_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_counters", S, [P, P, S]),
     ("rx_trace_set_config", S, [P, I32, I32]),
