@@ -95,6 +95,17 @@ typedef struct rx_pt_options {
   uint32_t flags;          /* reserved, 0 */
 } rx_pt_options;
 
+/* Vertex connection and merging options (VCMTracer, reference include/VCMTracer.h). */
+typedef struct rx_vcm_options {
+  uint32_t iterations;     /* progressive iterations (the reference loops until its time budget) */
+  uint32_t max_depth;      /* MCRenderer::maxDepth, at most 21 */
+  uint32_t light_paths;    /* light subpaths per iteration, 0 = width*height (the reference) */
+  uint32_t flags;          /* reserved, 0 */
+  float radius;            /* initial merge radius (VCMTracer::mergeRadius, <radius> in XML) */
+  float alpha;             /* radius shrink: r *= ((s+alpha)/(s+1))^(1/3) (reference default 0.6667) */
+  uint64_t seed;
+} rx_vcm_options;
+
 typedef struct rx_render_stats {
   uint64_t extension_rays; /* closest-hit rays traced (camera + bounce) */
   uint64_t shadow_rays;    /* next-event-estimation visibility rays */
@@ -173,6 +184,13 @@ rx_status rx_trace_closest_reforder_device(rx_context* ctx, const rx_ray* d_rays
  * rx_scene_set_objects before rx_build_accel. */
 rx_status rx_render_pt(rx_context* ctx, const rx_camera* cam, const rx_pt_options* opts, double* film_rgb,
                        double* film_sq, rx_render_stats* stats);
+
+/* VCMTracer::renderPixels (reference src/VCMTracer.cpp:6-143) for a fixed number of
+ * iterations: film_rgb receives the running mean of the vignetting-corrected
+ * iteration images (width*height*3 doubles, rows from the top). Light-path and
+ * merge normalisation use light_paths (width*height in the reference). */
+rx_status rx_render_vcm(rx_context* ctx, const rx_camera* cam, const rx_vcm_options* opts, double* film_rgb,
+                        rx_render_stats* stats);
 
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
  * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative

@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 
 from . import _capi
-from ._capi import RxError, rx_build_options, rx_camera, rx_object, rx_pt_options, rx_render_stats
+from ._capi import RxError, rx_build_options, rx_camera, rx_object, rx_pt_options, rx_render_stats, rx_vcm_options
 from . import scenes
 
 __all__ = ["Context", "KDTree", "RxError", "reftree_serialize", "scenes", "rays_to_array"]
@@ -151,6 +151,16 @@ class Context:
         self._ck(self._L.rx_render_pt(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), _capi.ptr(sq),
                                       ctypes.byref(st)))
         return film, sq, dict(extension_rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms)
+
+    def render_vcm(self, camera: "scenes.Camera", iterations: int, radius: float, alpha: float = 0.6667,
+                   max_depth: int = 8, light_paths: int = 0, seed: int = 1):
+        """VCMTracer renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats)."""
+        cam = camera_struct(camera)
+        o = rx_vcm_options(iterations, max_depth, light_paths, 0, radius, alpha, seed)
+        film = np.zeros((camera.height, camera.width, 3), np.float64)
+        st = rx_render_stats()
+        self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
+        return film, dict(rays=st.extension_rays, paths=st.paths, ms=st.ms)
 
     def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))

@@ -42,6 +42,12 @@ class rx_pt_options(ctypes.Structure):
                 ("flags", ctypes.c_uint32)]
 
 
+class rx_vcm_options(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("light_paths", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("radius", ctypes.c_float), ("alpha", ctypes.c_float),
+                ("seed", ctypes.c_uint64)]
+
+
 class rx_render_stats(ctypes.Structure):
     _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64), ("paths", ctypes.c_uint64),
                 ("ms", ctypes.c_float), ("reserved", ctypes.c_float)]
@@ -73,6 +79,7 @@ SIGNATURES = [
     ("rx_trace_counters", S, [P, P, S]),
     ("rx_trace_set_config", S, [P, I32, I32]),
     ("rx_render_pt", S, [P, P, P, P, P, P]),
+    ("rx_render_vcm", S, [P, P, P, P, P]),
 ]
 
 

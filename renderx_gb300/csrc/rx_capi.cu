@@ -364,6 +364,31 @@ rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options*
   return RX_OK;
 }
 
+rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_options* opts, double* film_rgb,
+                        rx_render_stats* stats) {
+  if (!c) return RX_ERR_INVALID;
+  if (!cam || !opts || !film_rgb) return c->fail(RX_ERR_INVALID, "null argument");
+  if (!c->scene_ready) return c->fail(RX_ERR_STATE, "scene objects not built (rx_scene_set_objects, rx_build_accel)");
+  if (cam->width == 0 || cam->height == 0 || cam->sight_dist == 0) return c->fail(RX_ERR_INVALID, "bad camera");
+  if (opts->iterations == 0) return c->fail(RX_ERR_INVALID, "iterations must be positive");
+  if (opts->max_depth > 21) return c->fail(RX_ERR_INVALID, "max_depth must be at most 21");
+  if (!(opts->radius > 0.0f) || !(opts->alpha > 0.0f)) return c->fail(RX_ERR_INVALID, "radius and alpha must be positive");
+  if (c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "vertex connection and merging needs an emitter");
+  DeviceGuard g(c->device);
+  size_t np = (size_t)cam->width * cam->height;
+  DevBuf film;
+  rx_status s;
+  if ((s = c->cuda(film.alloc(np * 3 * sizeof(double)), "film")) != RX_OK) return s;
+  cudaMemsetAsync(film.p, 0, film.bytes, c->stream);
+  rx_render_stats st{};
+  if ((s = c->cuda(rx::render_vcm(c, *cam, *opts, film.as<double>(), &st, c->stream), "render_vcm")) != RX_OK) return s;
+  std::vector<double> h(np * 3);
+  if ((s = c->cuda(cudaMemcpy(h.data(), film.p, film.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
+  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->iterations;
+  if (stats) *stats = st;
+  return RX_OK;
+}
+
 rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {
   if (!c || !out) return RX_ERR_INVALID;
   if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");

@@ -27,11 +27,28 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
 cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                   unsigned long long* counters, cudaStream_t s);
 
-struct rx_context_fwd;
-// A device allocation owned by the context.
+// A device allocation, released when its owner goes away (move-only).
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
   cudaError_t alloc(size_t b) {
     release();
     if (b == 0) return cudaSuccess;
@@ -96,4 +113,7 @@ namespace rx {
 // Path tracing (rx_pt.cu): renders into device films (sum, optional sum of squares).
 cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& opt, double* film_sum,
                       double* film_sq, rx_render_stats* stats, cudaStream_t s);
+// Vertex connection and merging (rx_vcm.cu): adds iteration images to `film` (sum).
+cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
+                       rx_render_stats* stats, cudaStream_t s);
 }  // namespace rx

@@ -138,9 +138,12 @@ struct PHit {
 };
 
 // Closest legal hit with t < tmax (ANY: stop at the first legal one). contact, inside:
-// object ids, -1 for none (camera rays use -1/-1: no condition).
+// object ids, -1 for none (-1/-1: no condition, as the camera ray's first query),
+// -2 for the camera as contact object. only_obj >= 0: closest hit among that object's
+// triangles only, no condition (the per-object trees of Scene::findInsideObject).
 template <bool ANY>
-__device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
+__device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside,
+                                           int only_obj = -1) {
   const DevAccel& A = S.accel;
   F3 inv = {fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(1e30f, d.x),
             fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(1e30f, d.y),
@@ -149,7 +152,7 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
   PHit best{-1, tmax};
   int stack[kStackDepth];
   int sp = 0, cur = 0, cnt = 0;
-  const bool cond = !(contact < 0 && inside < 0);
+  const bool cond = only_obj < 0 && !(contact == -1 && inside == -1);
   while (true) {
     if (cur >= 0) {
       const float4* np = A.bvh + 4 * (size_t)cur;
@@ -200,7 +203,9 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
         if (v < -1e-7f || u + v > 1.0000001f) continue;
         float t = dot(e2, qv) * idet;
         if (!(t >= 0.0f) || !(t < best.t)) continue;
-        if (cond) {
+        if (only_obj >= 0) {
+          if (__float_as_int(__ldg(&S.slot_n[3 * (size_t)(first + k)]).w) != only_obj) continue;
+        } else if (cond) {
           const float4* nn = S.slot_n + 3 * (size_t)(first + k);
           float4 q0 = __ldg(nn), q1 = __ldg(nn + 1), q2 = __ldg(nn + 2);
           int obj = __float_as_int(q0.w);

@@ -1,0 +1,595 @@
+// Vertex connection and merging: the reference's VCMTracer (src/VCMTracer.cpp:6-639).
+//
+// Per iteration (VCMTracer.cpp:25-142):
+//  1. k_vcm_light: one light subpath per light path (emission sample + the bounce loop
+//     of MCRenderer::samplePathIter, with light-path scattering), its vertices stored;
+//     every non-specular vertex after the first that is not on an emitter becomes a
+//     photon (VCMTracer.cpp:64-95).
+//  2. A sort-by-cell hash grid over the photons (cell = 2 r, SmallVCM's spatial hash
+//     (x*73856093)^(y*19349663)^(z*83492791)): count per bucket, exclusive scan,
+//     scatter (the counting-sort build of include/Hashgrid.h:21-91); it replaces the
+//     per-iteration PointKDTree (include/PointKDTree.h), queried with the same strict
+//     |p-x| < r test over the (up to) 8 cells the sphere touches.
+//  3. k_vcm_eye: per pixel, the eye subpath (sampled with light-path scattering, as
+//     VCMTracer.cpp:107 does), then colorByMergingPaths (:566-636) and
+//     colorByConnectingPaths (:430-562) with the full-path MIS of connectMergeWeight
+//     (:321-428, double precision) and light-tracing splats through
+//     Camera::transToPixel.
+//  4. Vignetting correction of the iteration image and the running mean (FP64 film).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "rx_internal.h"
+#include "rx_material.cuh"
+
+namespace rx {
+
+constexpr int kMaxV = 24;  // vertices per stored subpath (max_depth <= kMaxV - 3)
+
+struct VcmParams {
+  CamDev cam;
+  F3 focus;
+  uint64_t seed;
+  uint32_t iter;
+  uint32_t max_depth;
+  uint32_t maxv;       // vertices per stored subpath: max_depth + 3
+  uint32_t n_light;    // light paths per iteration
+  uint32_t n_pixels;
+  float radius;
+  float norm;          // light-path count normaliser (W*H in the reference)
+};
+
+// ---- camera ----------------------------------------------------------------------------
+__device__ __forceinline__ F3 cam_dir(const CamDev& c, float xp, float yp) {
+  float x = xp - c.width * 0.5f, y = c.height * 0.5f - yp;
+  return normalize(c.front * c.sight + c.right * x + c.up * y);
+}
+
+// Camera::generateRay + generateRayBase (src/Camera.cpp:4-47)
+__device__ PV camera_ray(const DevScene& S, const CamDev& c, uint32_t pixel, Rng& rng, Hit3& hit) {
+  int x = pixel % c.width, y = pixel / c.width;
+  float jx = rng.next(), jy = rng.next();
+  PV r = pv_term(c.pos);
+  r.d = cam_dir(c, x + jx, y + jy);
+  r.c = {1, 1, 1};
+  r.contact = kCameraObj;
+  r.flags = kDirRandom;
+  r.pixel = (int)pixel;
+  PHit h = trace_cond<false>(S, r.o, r.d, INFINITY, kNone, kNone);
+  hit = h.tid >= 0 ? Hit3{(int)__ldg(&S.tri_obj[h.tid]), h.tid, h.t} : Hit3{kNone, -1, -1.0f};
+  r.inside = find_inside(S, r.o, r.d, kNone);
+  return r;
+}
+
+// MCRenderer::samplePath / samplePathIter (src/MCRenderer.cpp:151-273): the path's rays
+// in order, ending with the ray that stopped it or a terminating ray.
+__device__ int sample_path(const DevScene& S, const CamDev& cam, PV start, Hit3 h, uint32_t max_depth, Rng& rng,
+                           PV* out) {
+  int n = 0;
+  PV prev = start;
+  for (uint32_t depth = 0;; depth++) {
+    out[n++] = prev;
+    if (prev.inside == kNone && h.obj == kNone) {
+      out[n++] = pv_term(prev.o);
+      return n;
+    }
+    PV next = scatter_step(S, cam, prev, h, true, true, rng);
+    if (length(next.d) < 0.5f) {
+      out[n++] = next;
+      return n;
+    }
+    if (depth + 1 > max_depth) {
+      out[n++] = pv_term(prev.o);
+      return n;
+    }
+    PHit hh = trace_cond<false>(S, next.o, next.d, INFINITY, next.contact, next.inside);
+    if (hh.tid < 0) {
+      out[n++] = next;
+      out[n++] = pv_term(prev.o);
+      return n;
+    }
+    h = Hit3{(int)__ldg(&S.tri_obj[hh.tid]), hh.tid, hh.t};
+    prev = next;
+  }
+}
+
+// ---- packed vertex storage (4 float4 per vertex) ---------------------------------------
+__device__ __forceinline__ void store_pv(float4* p, const PV& v) {
+  p[0] = make_float4(v.o.x, v.o.y, v.o.z, v.dprob);
+  p[1] = make_float4(v.d.x, v.d.y, v.d.z, v.oprob);
+  p[2] = make_float4(v.c.x, v.c.y, v.c.z, __int_as_float(v.pixel));
+  p[3] = make_float4(__int_as_float(v.contact), __int_as_float(v.ctri), __int_as_float(v.inside),
+                     __uint_as_float(v.flags));
+}
+__device__ __forceinline__ PV load_pv(const float4* p) {
+  float4 a = p[0], b = p[1], c = p[2], e = p[3];
+  PV v;
+  v.o = f3(a);
+  v.dprob = a.w;
+  v.d = f3(b);
+  v.oprob = b.w;
+  v.c = f3(c);
+  v.pixel = __float_as_int(c.w);
+  v.contact = __float_as_int(e.x);
+  v.ctri = __float_as_int(e.y);
+  v.inside = __float_as_int(e.z);
+  v.flags = __float_as_uint(e.w);
+  return v;
+}
+
+// ---- light subpaths + photons ----------------------------------------------------------
+__global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, float4* photon_pos, int* photon_ref,
+                            unsigned* n_photons, unsigned photon_cap, unsigned long long* rays) {
+  uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long nr = 0;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += stride) {
+    Rng rng(P.seed, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+    PV path[kMaxV];
+    Hit3 h;
+    PV start = emit_ray(S, P.cam, rng, h);
+    int n = sample_path(S, P.cam, start, h, P.max_depth, rng, path);
+    nr += (unsigned long long)n;
+    llen[p] = n;
+    for (int i = 0; i < n; i++) store_pv(lv + 4 * ((size_t)p * P.maxv + i), path[i]);
+    for (int i = 1; i < n; i++) {
+      if (is_emissive(S, path[i].contact)) break;
+      if (!(path[i].flags & kDirRandom)) continue;
+      unsigned slot = atomicAdd(n_photons, 1u);
+      if (slot < photon_cap) {
+        photon_pos[slot] = make_float4(path[i].o.x, path[i].o.y, path[i].o.z, 0.0f);
+        photon_ref[slot] = (int)(p * P.maxv + i);
+      }
+    }
+  }
+  if (nr) atomicAdd(rays, nr);
+}
+
+// ---- hash grid ---------------------------------------------------------------------------
+struct Grid {
+  float cell;          // 2 * radius
+  unsigned mask;       // buckets - 1
+  const unsigned* start;  // bucket -> first sorted photon (exclusive scan), buckets + 1 entries
+  const int* sorted;   // sorted photon ids
+};
+__device__ __forceinline__ unsigned cell_hash(int x, int y, int z, unsigned mask) {
+  return ((unsigned)(x * 73856093) ^ (unsigned)(y * 19349663) ^ (unsigned)(z * 83492791)) & mask;
+}
+__global__ void k_grid_count(const float4* pos, const unsigned* n_photons, unsigned cap, float cell, unsigned mask,
+                             unsigned* count, unsigned* key) {
+  unsigned n = min(*n_photons, cap);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 p = pos[i];
+    unsigned k = cell_hash((int)floorf(p.x / cell), (int)floorf(p.y / cell), (int)floorf(p.z / cell), mask);
+    key[i] = k;
+    atomicAdd(&count[k], 1u);
+  }
+}
+// exclusive scan of `count` (n entries) into `start`, block-wise then over block sums
+__global__ void k_scan_blocks(const unsigned* count, unsigned* start, unsigned* block_sum, unsigned n) {
+  __shared__ unsigned s[1024];
+  unsigned i = blockIdx.x * 1024 + threadIdx.x;
+  unsigned v = i < n ? count[i] : 0u;
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (unsigned off = 1; off < 1024; off <<= 1) {
+    unsigned t = threadIdx.x >= off ? s[threadIdx.x - off] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) start[i] = s[threadIdx.x] - v;
+  if (threadIdx.x == 1023) block_sum[blockIdx.x] = s[1023];
+}
+__global__ void k_scan_sums(unsigned* block_sum, unsigned nb) {
+  // single block, sequential carry over chunks of 1024
+  __shared__ unsigned s[1024];
+  unsigned carry = 0;
+  for (unsigned base = 0; base < nb; base += 1024) {
+    unsigned i = base + threadIdx.x;
+    unsigned v = i < nb ? block_sum[i] : 0u;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (unsigned off = 1; off < 1024; off <<= 1) {
+      unsigned t = threadIdx.x >= off ? s[threadIdx.x - off] : 0u;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nb) block_sum[i] = carry + s[threadIdx.x] - v;
+    __syncthreads();
+    carry += s[1023];
+    __syncthreads();
+  }
+}
+__global__ void k_scan_add(unsigned* start, const unsigned* block_sum, unsigned n, unsigned* cursor) {
+  unsigned i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) {
+    start[i] += block_sum[blockIdx.x];
+    cursor[i] = start[i];
+  }
+}
+__global__ void k_grid_scatter(const unsigned* key, const unsigned* n_photons, unsigned cap, unsigned* cursor,
+                               int* sorted) {
+  unsigned n = min(*n_photons, cap);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned slot = atomicAdd(&cursor[key[i]], 1u);
+    sorted[slot] = (int)i;
+  }
+}
+
+// ---- the reference's bidirectional machinery over a whole path ----------------------
+// VCMTracer::link (src/VCMTracer.cpp:308-319)
+__device__ __forceinline__ PV link(const PV* w, int n, int ci, int i, int j) {
+  const PV& src = w[min(max(i, 0), n - 1)];
+  const PV& dst = w[min(max(j, 0), n - 1)];
+  PV r = src;
+  if ((j > i && i <= ci) || (j < i && i > ci)) return r;
+  r.d = normalize(dst.o - src.o);
+  r.inside = dst.inside;
+  return r;
+}
+
+// MCRenderer::connectRays (src/MCRenderer.cpp:50-106)
+__device__ bool connect_rays(const DevScene& S, const CamDev& cam, PV* w, int n, int ci, bool merged) {
+  PV& L = w[ci];
+  PV& E = w[ci + 1];
+  if (!merged && (!(L.flags & kDirRandom) || !(E.flags & kDirRandom))) return false;
+  if (merged && !(E.flags & kDirRandom)) return false;
+  const PV& pl = w[ci - 1 > 0 ? ci - 1 : 0];
+  const PV& pe = w[ci + 2 < n - 1 ? ci + 2 : n - 1];
+  L.d = normalize(E.o - L.o);
+  E.d = -L.d;
+  if (!merged) {
+    L.dprob = 1.0f;
+    L.c = bsdf_of(S, cam, pl, L);
+    L.flags |= kDirRandom;
+    if (L.contact != kNone && ci > 0) {
+      F3 n0 = contact_normal(S, cam, L);
+      if (dot(n0, L.d) <= 0.0f) L.inside = L.contact;
+      else if (dot(n0, pl.d) <= 0.0f) L.inside = pl.inside;
+      else L.inside = find_inside(S, L.o, L.d, L.contact);
+    }
+  }
+  E.dprob = 1.0f;
+  E.c = bsdf_of(S, cam, pe, E);
+  E.flags |= kDirRandom;
+  if (E.contact != kNone && ci < n - 2) {
+    F3 n0 = contact_normal(S, cam, E);
+    if (dot(n0, E.d) <= 0.0f) E.inside = E.contact;
+    else if (dot(n0, pe.d) <= 0.0f) E.inside = pe.inside;
+    else E.inside = find_inside(S, E.o, E.d, E.contact);
+  }
+  return true;
+}
+
+// VCMTracer::connectColorProb (src/VCMTracer.cpp:248-306)
+__device__ void connect_color_prob(const DevScene& S, const CamDev& cam, const PV* w, int n, int ci, bool merged,
+                                   float r, F3& color, float& prob) {
+  color = {1, 1, 1};
+  prob = 1.0f;
+  for (int i = 0; i < n; i++) {
+    color = color * w[i].c;
+    float dist = 1e-5f;
+    if (i <= ci) {
+      dist = fmaxf(length(w[i + 1].o - w[i].o), 1e-5f);
+      color = color * decay_of(S, w[i].inside, dist);
+    } else if (i > ci + 1) {
+      dist = fmaxf(length(w[i - 1].o - w[i].o), 1e-5f);
+      color = color * decay_of(S, w[i].inside, dist);
+    }
+    if (i == ci && i < n - 1) color = color * (cos_term(S, cam, w[i]) * cos_term(S, cam, w[i + 1]) / (dist * dist));
+    if (i != ci && i != ci + 1) color = color * cos_term(S, cam, w[i]);
+    prob *= w[i].dprob * w[i].oprob;
+    if (merged && i == ci) {
+      prob *= RX_PI * r * r;
+      prob *= cos_term(S, cam, link(w, n, ci, i + 1, i));
+      prob /= dist * dist;
+      prob *= origin_pdf(S, link(w, n, ci, i, i + 1), link(w, n, ci, i + 1, i + 2));
+      if (w[i + 1].inside != kNone && w[i + 1].contact == kNone) prob *= 4.0f / 3.0f * r;
+    }
+  }
+}
+
+__device__ __forceinline__ bool must_use_pt(const PV* w, int n) {
+  for (int i = 1; i < n - 1; i++)
+    if (w[i].flags & kDirRandom) return false;
+  return true;
+}
+
+// VCMTracer::connectMergeWeight (src/VCMTracer.cpp:321-428), power 1, double precision
+__device__ float connect_merge_weight(const DevScene& S, const CamDev& cam, const PV* w, int n, int ci, bool merged,
+                                      float r, float norm) {
+  double pf[2 * kMaxV], pb[2 * kMaxV];
+  float dist[2 * kMaxV];
+  pf[0] = w[0].oprob;
+  for (int i = 0; i < n - 1; i++) {
+    pf[i + 1] = pf[i] * cos_term(S, cam, link(w, n, ci, i + 1, i));
+    dist[i] = fmaxf(length(w[i + 1].o - w[i].o), 1e-5f);
+    pf[i + 1] /= (double)dist[i] * dist[i];
+    if (w[i].flags & kDirRandom) {
+      if (i > 0) {
+        pf[i + 1] *= dir_pdf(S, cam, link(w, n, ci, i - 1, i), link(w, n, ci, i, i + 1), false);
+      } else {
+        PV ray = link(w, n, ci, i, i + 1);
+        pf[i + 1] *= dir_pdf(S, cam, ray, ray, true);
+      }
+      pf[i + 1] *= origin_pdf(S, link(w, n, ci, i, i + 1), link(w, n, ci, i + 1, i + 2));
+    }
+  }
+  pb[n - 1] = w[n - 1].oprob;
+  for (int i = n - 1; i > 0; i--) {
+    pb[i - 1] = pb[i] * cos_term(S, cam, link(w, n, ci, i - 1, i));
+    pb[i - 1] /= (double)dist[i - 1] * dist[i - 1];
+    if (w[i].flags & kDirRandom) {
+      if (i < n - 1) {
+        pb[i - 1] *= dir_pdf(S, cam, link(w, n, ci, i + 1, i), link(w, n, ci, i, i - 1), false);
+      } else {
+        PV ray = link(w, n, ci, i, i - 1);
+        pb[i - 1] *= dir_pdf(S, cam, ray, ray, true);
+      }
+      pb[i - 1] *= origin_pdf(S, link(w, n, ci, i, i - 1), link(w, n, ci, i - 1, i - 2));
+    }
+  }
+  double self = ci == -1 ? pb[0] : pf[ci] * pb[ci + 1];
+  double sum = 0.0;
+  for (int i = 0; i < n - 1; i++) {
+    if ((w[i].flags & kDirRandom) && (w[i + 1].flags & kDirRandom)) sum += pf[i] * pb[i + 1];
+    if (i < n - 2 && (w[i + 1].flags & kDirRandom)) {
+      double p = pf[i] * pb[i + 1];
+      if (w[i].flags & kDirRandom) {
+        if (i > 0) {
+          p *= dir_pdf(S, cam, link(w, n, ci, i - 1, i), link(w, n, ci, i, i + 1), false);
+        } else {
+          PV ray = link(w, n, ci, i, i + 1);
+          p *= dir_pdf(S, cam, ray, ray, true);
+        }
+      }
+      p *= origin_pdf(S, link(w, n, ci, i, i + 1), link(w, n, ci, i + 1, i + 2));
+      p *= RX_PI * r * r;
+      p *= cos_term(S, cam, link(w, n, ci, i + 1, i));
+      p /= (double)dist[i] * dist[i];
+      if (w[i + 1].inside != kNone && w[i + 1].contact == kNone) p *= 4.0 / 3.0 * r;
+      p *= norm;
+      sum += p;
+      if (merged && ci == i) self = p;
+    }
+  }
+  if (must_use_pt(w, n)) sum += pb[0];
+  double res = self / sum;
+  if (!(res >= 0.0)) return 0.0f;
+  return (float)res;
+}
+
+// Camera::transToPixel (src/Camera.cpp:136-152)
+__device__ __forceinline__ void trans_to_pixel(const CamDev& c, F3 point, float& px, float& py) {
+  F3 v = point - c.pos;
+  float fd = dot(v, c.front);
+  float ratio = c.sight / fd;
+  px = dot(v, c.right) * ratio + c.width / 2.0f - 0.5f;
+  py = c.height / 2.0f - dot(v, c.up) * ratio - 0.5f;
+}
+
+__device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
+  atomicAdd(img + 3 * pixel, c.x);
+  atomicAdd(img + 3 * pixel + 1, c.y);
+  atomicAdd(img + 3 * pixel + 2, c.z);
+}
+
+// ---- eye subpaths: merging and connecting ---------------------------------------------
+__global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const float4* lv, const int* llen,
+                                                 const float4* photon_pos, const int* photon_ref, Grid G,
+                                                 float* img, unsigned long long* rays) {
+  uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long nrays = 0;
+  const float r = P.radius;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += stride) {
+    Rng rng(P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+    PV eye[kMaxV];
+    PV w[2 * kMaxV];
+    Hit3 h;
+    PV start = camera_ray(S, P.cam, p, rng, h);
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, eye);
+    nrays += (unsigned long long)ne;
+    F3 acc = {0, 0, 0};
+    // colorByMergingPaths (VCMTracer.cpp:566-636)
+    for (int ei = 1; ei < ne; ei++) {
+      if (is_emissive(S, eye[ei].contact)) break;
+      if (!(eye[ei].flags & kDirRandom)) continue;
+      F3 q = eye[ei].o;
+      F3 sum = {0, 0, 0};
+      // cells the sphere touches: two per axis in exact arithmetic (cell = 2r), up to
+      // three after rounding of the two divisions
+      int x0 = (int)floorf((q.x - r) / G.cell), y0 = (int)floorf((q.y - r) / G.cell), z0 = (int)floorf((q.z - r) / G.cell);
+      int x1 = min((int)floorf((q.x + r) / G.cell), x0 + 2), y1 = min((int)floorf((q.y + r) / G.cell), y0 + 2);
+      int z1 = min((int)floorf((q.z + r) / G.cell), z0 + 2);
+      unsigned seen[27];
+      int nseen = 0;
+      for (int cx = x0; cx <= x1; cx++)
+        for (int cy = y0; cy <= y1; cy++)
+          for (int cz = z0; cz <= z1; cz++) {
+            unsigned b = cell_hash(cx, cy, cz, G.mask);
+            bool dup = false;
+            for (int k = 0; k < nseen; k++) dup |= seen[k] == b;
+            if (dup || nseen >= 27) continue;
+            seen[nseen++] = b;
+            for (unsigned s = G.start[b]; s < G.start[b + 1]; s++) {
+              int ph = G.sorted[s];
+              F3 pp = f3(photon_pos[ph]);
+              if (!(length(q - pp) < r)) continue;
+              int ref = photon_ref[ph];
+              int lp = ref / (int)P.maxv, li = ref % (int)P.maxv;
+              // wholePath = light[0 .. li-1] + eye[ei .. 0]
+              int n = 0;
+              for (int k = 0; k < li; k++) w[n++] = load_pv(lv + 4 * ((size_t)lp * P.maxv + k));
+              for (int k = ei; k >= 0; k--) w[n++] = eye[k];
+              int ci = li - 1;
+              if (!connect_rays(S, P.cam, w, n, ci, true)) continue;
+              F3 col;
+              float prob;
+              connect_color_prob(S, P.cam, w, n, ci, true, r, col, prob);
+              if (length(col) == 0.0f || prob == 0.0f) continue;
+              float wt = connect_merge_weight(S, P.cam, w, n, ci, true, r, P.norm);
+              sum = sum + col * (wt / prob);
+            }
+          }
+      acc = acc + sum * (1.0f / P.norm);
+    }
+    // colorByConnectingPaths (VCMTracer.cpp:430-562) with this pixel's light path
+    uint32_t lp = p % P.n_light;
+    int nl = llen[lp];
+    for (int whole = 2; whole <= ne + nl; whole++) {
+      int s0 = whole - ne > 0 ? whole - ne : 0;
+      int s1 = whole - 1 < nl ? whole - 1 : nl;
+      for (int s = s0; s <= s1; s++) {
+        int t = whole - s;
+        int n = 0;
+        for (int k = 0; k < s; k++) w[n++] = load_pv(lv + 4 * ((size_t)lp * P.maxv + k));
+        for (int k = t - 1; k >= 0; k--) w[n++] = eye[k];
+        int ci = s - 1;
+        if (s == 0 && !is_emissive(S, w[0].contact)) continue;
+        if (s == 0 && !must_use_pt(w, n)) continue;
+        if (s > 0) {
+          if (s > 1 && is_emissive(S, w[ci].contact)) continue;
+          if (is_emissive(S, w[ci + 1].contact)) continue;
+          if (!connect_rays(S, P.cam, w, n, ci, false)) continue;
+          const PV& E = w[ci + 1];
+          const PV& L = w[ci];
+          float len = length(E.o - L.o);
+          nrays++;
+          PHit sh = trace_cond<true>(S, E.o, E.d, len - 1e-5f, E.contact, E.inside);  // testVisibility
+          if (sh.tid >= 0) continue;
+        }
+        F3 col;
+        float prob;
+        connect_color_prob(S, P.cam, w, n, ci, false, r, col, prob);
+        if (!(prob > 0.0f)) continue;
+        if (!(length(col) > 0.0f)) continue;
+        float wt = connect_merge_weight(S, P.cam, w, n, ci, false, r, P.norm);
+        F3 c = col * (wt / prob);
+        if (!(length(c) > 0.0f)) continue;
+        if (t == 1) {  // light tracing: splat onto the pixel the light vertex projects to
+          F3 dir = normalize(w[ci].o - w[ci + 1].o);
+          float ca = fabsf(dot(P.cam.front, dir));
+          float to_solid = P.cam.sight * P.cam.sight / (ca * ca * ca);
+          float to_surface = to_solid / ca;
+          c = c * (to_surface / (float)P.n_pixels) * ca;
+          float px, py;
+          trans_to_pixel(P.cam, w[n - 2].o, px, py);
+          int ix = (int)px, iy = (int)py;
+          if (ix >= 0 && ix < P.cam.width && iy >= 0 && iy < P.cam.height) img_add(img, iy * P.cam.width + ix, c);
+        } else {
+          acc = acc + c;
+        }
+      }
+    }
+    img_add(img, (int)p, acc);
+  }
+  if (nrays) atomicAdd(rays, nrays);
+}
+
+// MCRenderer::eliminateVignetting on the iteration image, then the running mean's sum.
+__global__ void k_vcm_accumulate(VcmParams P, const float* img, double* film) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += gridDim.x * blockDim.x) {
+    int x = p % P.cam.width, y = p / P.cam.width;
+    F3 dc = cam_dir(P.cam, x + 0.5f, y + 0.5f);
+    float v = fabsf(dot(dc, P.cam.front));
+    for (int c = 0; c < 3; c++) film[3 * p + c] += (double)(img[3 * p + c] / v);
+  }
+}
+
+// ---- host driver -----------------------------------------------------------------------
+cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
+                       rx_render_stats* stats, cudaStream_t s) {
+  const DevScene& S = c->scene;
+  VcmParams P{};
+  auto v3 = [](const float* p) { return F3{p[0], p[1], p[2]}; };
+  auto hn = [](F3 a) {
+    float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    return l > 0 ? F3{a.x / l, a.y / l, a.z / l} : a;
+  };
+  auto hc = [](F3 l, F3 r) { return F3{l.y * r.z - l.z * r.y, l.z * r.x - l.x * r.z, l.x * r.y - l.y * r.x}; };
+  F3 pos = v3(cam.position), foc = v3(cam.focus), up = v3(cam.up);
+  P.cam.pos = pos;
+  P.cam.front = hn(F3{foc.x - pos.x, foc.y - pos.y, foc.z - pos.z});
+  P.cam.right = hn(hc(P.cam.front, up));
+  P.cam.up = hc(P.cam.right, P.cam.front);
+  P.cam.sight = (float)cam.sight_dist;
+  P.cam.width = (int)cam.width;
+  P.cam.height = (int)cam.height;
+  P.focus = foc;
+  P.seed = opt.seed;
+  P.max_depth = opt.max_depth;
+  P.maxv = opt.max_depth + 3;
+  P.n_pixels = cam.width * cam.height;
+  P.n_light = opt.light_paths ? opt.light_paths : P.n_pixels;
+  P.norm = (float)P.n_light;
+  const unsigned cap = P.n_light * P.maxv;
+  unsigned buckets = 1u << 16;
+  while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
+  std::vector<DevBuf> bufs(12);
+  cudaError_t e;
+  auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
+  if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
+  if ((e = al(1, (size_t)P.n_light * sizeof(int))) != cudaSuccess) return e;
+  if ((e = al(2, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;                      // photon positions
+  if ((e = al(3, (size_t)cap * sizeof(int))) != cudaSuccess) return e;
+  if ((e = al(4, (size_t)cap * sizeof(unsigned))) != cudaSuccess) return e;                     // photon keys
+  if ((e = al(5, (size_t)cap * sizeof(int))) != cudaSuccess) return e;                          // sorted ids
+  if ((e = al(6, (size_t)(buckets + 1) * sizeof(unsigned))) != cudaSuccess) return e;           // counts
+  if ((e = al(7, (size_t)(buckets + 1) * sizeof(unsigned))) != cudaSuccess) return e;           // start
+  if ((e = al(8, (size_t)(buckets + 1) * sizeof(unsigned))) != cudaSuccess) return e;           // cursor
+  if ((e = al(9, ((buckets + 1) / 1024 + 2) * sizeof(unsigned))) != cudaSuccess) return e;      // block sums
+  if ((e = al(10, (size_t)P.n_pixels * 3 * sizeof(float))) != cudaSuccess) return e;            // iteration image
+  if ((e = al(11, 64 * sizeof(unsigned long long))) != cudaSuccess) return e;                   // counters
+  unsigned long long* ctr = bufs[11].as<unsigned long long>();
+  unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
+  cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
+  int grid = c->trace_cfg.sms * 4;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  float radius = opt.radius;
+  unsigned nscan = buckets + 1;
+  unsigned nblk = (nscan + 1023) / 1024;
+  for (uint32_t it = 0; it < opt.iterations; it++) {
+    radius *= powf(((float)it + opt.alpha) / ((float)it + 1.0f), 1.0f / 3.0f);  // VCMTracer.cpp:29-30
+    P.radius = radius;
+    P.iter = it;
+    cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
+    k_vcm_light<<<grid, 64, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
+                                     bufs[3].as<int>(), nph, cap, ctr);
+    cudaMemsetAsync(bufs[6].p, 0, bufs[6].bytes, s);
+    float cell = 2.0f * radius;
+    k_grid_count<<<grid, 256, 0, s>>>(bufs[2].as<float4>(), nph, cap, cell, buckets - 1, bufs[6].as<unsigned>(),
+                                      bufs[4].as<unsigned>());
+    k_scan_blocks<<<nblk, 1024, 0, s>>>(bufs[6].as<unsigned>(), bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan);
+    k_scan_sums<<<1, 1024, 0, s>>>(bufs[9].as<unsigned>(), nblk);
+    k_scan_add<<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan, bufs[8].as<unsigned>());
+    k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), nph, cap, bufs[8].as<unsigned>(), bufs[5].as<int>());
+    Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[5].as<int>()};
+    cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
+    k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
+                                   bufs[3].as<int>(), G, bufs[10].as<float>(), ctr + 1);
+    k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
+  }
+  cudaEventRecord(e1, s);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (stats) {
+    unsigned long long h[2];
+    cudaMemcpy(h, ctr, sizeof h, cudaMemcpyDeviceToHost);
+    stats->extension_rays = h[0] + h[1];
+    stats->shadow_rays = 0;
+    stats->paths = (uint64_t)P.n_pixels * opt.iterations;
+    stats->ms = ms;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace rx

@@ -136,12 +136,47 @@ def make_render_goldens(ref_pt: str):
         print(f"{path}: {spp} spp, mean {mean.mean(axis=(0, 1))}, {out[4]} s")
 
 
+# VCM goldens: (scene function, max depth, iterations per estimate, independent
+# estimates, initial radius, alpha). One reference process per estimate.
+VCM_CASES = {
+    "cornell_vcm": ("cornell_box", 8, 8, 64, 0.0963, 0.75),
+    "spheres_vcm": ("material_spheres", 8, 8, 48, 0.0963, 0.75),
+}
+
+
+def make_vcm_goldens(ref_vcm: str):
+    for case, (scene_fn, depth, iters, runs, r0, alpha) in VCM_CASES.items():
+        sc = render_scene(scene_fn)
+        f = sc.flatten()
+        imgs = []
+        secs = 0.0
+        with tempfile.TemporaryDirectory() as td:
+            cfg = sceneio.write_config(sc, td, "VCM", depth, radius=r0)
+            for run in range(runs):
+                pre = os.path.join(td, f"out{run}")
+                out = subprocess.run([ref_vcm, cfg, str(iters), str(run), str(r0), str(alpha), pre, "8"], check=True,
+                                     capture_output=True, text=True, cwd=td).stdout.split()
+                secs += float(out[-1])
+                imgs.append(np.fromfile(pre + ".img.f64").reshape(sc.camera.height, sc.camera.width, 3))
+        imgs = np.array(imgs)
+        mean = imgs.mean(axis=0)
+        stderr = imgs.std(axis=0, ddof=1) / np.sqrt(runs)
+        path = os.path.join(HERE, f"render_{case}.npz")
+        np.savez_compressed(path, mean=mean.astype(np.float32), stderr=stderr.astype(np.float32),
+                            runs=np.int64(runs), iterations=np.int64(iters), max_depth=np.int64(depth),
+                            radius=np.float64(r0), alpha=np.float64(alpha), scene=np.array(scene_fn),
+                            seconds=np.float64(secs), geometry_sha256=np.array(geometry_hash(f["verts"], f["tris"])))
+        print(f"{path}: {runs} x {iters} iterations, mean {mean.mean(axis=(0, 1))}, {secs:.1f} s", flush=True)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref = args[0] if args else "/root/reference"
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"], check=True)
-    make_render_goldens(os.path.join(ROOT, "oracle", "_ref", "pt_driver"))
-    if "--render-only" in sys.argv:
+    if "--vcm-only" not in sys.argv:
+        make_render_goldens(os.path.join(ROOT, "oracle", "_ref", "pt_driver"))
+    make_vcm_goldens(os.path.join(ROOT, "oracle", "_ref", "vcm_driver"))
+    if "--render-only" in sys.argv or "--vcm-only" in sys.argv:
         return
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "hit_driver")
     for name, (ns, sub, seed, nrand, store) in CASES.items():
