@@ -181,6 +181,7 @@ def run_ours(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    ctx.set_trace_timing(args.steps)  # per-kernel events inside each timed call
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
         for k in range(args.steps):
@@ -193,6 +194,8 @@ def run_ours(args):
     if dist:
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
+    kern_ms = ctx.read_trace_timing()  # (steps, 3): walk, visibility check, re-walk
+    ctx.set_trace_timing(0)
     t_ms = sum(step_ms)
     if dist:
         tt = torch.tensor([t_ms], device="cuda")
@@ -209,7 +212,7 @@ def run_ours(args):
         e2e, same = end_to_end(ctx, host_rays, d_tid, args, dist, ws, n)
 
     if rank == 0:
-        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d)
+        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms)
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -239,11 +242,12 @@ def end_to_end(ctx, host_rays, d_tid, args, dist, ws, n):
     return e2e, same
 
 
-def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d):
+def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms):
     if True:
         peak, peak_kind = load_peaks()
         bytes_alg = 40 * n + 48 * st["triangles"] + 64 * st["bvh_nodes"]
-        achieved = bytes_alg / (ms_per_step * 1e-3) / 1e9
+        walk_ms = float(kern_ms[:, 0].mean()) if len(kern_ms) else ms_per_step
+        achieved = bytes_alg / (walk_ms * 1e-3) / 1e9
         traffic = None
         tp = os.path.join(ROOT, "profiles", "hit_traffic.json")
         if os.path.exists(tp):
@@ -258,10 +262,14 @@ def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_m
                            "parallelism": f"replicas x{ws}", "accel_build_s": round(build_s, 2)},
                 "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                                                  "d2h_bytes_per_step": n * 8, "matches_device_path": same},
-                "gpu_launches": 2 * args.steps,
+                "gpu_launches": 3 * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                             "kernel": "k_trace_persistent (closest-hit walk)", "kernel_ms": walk_ms,
                              "algorithmic_bytes_per_launch": bytes_alg},
+                "kernel_ms_mean": {"walk": walk_ms,
+                                   "visibility_check": float(kern_ms[:, 1].mean()) if len(kern_ms) else None,
+                                   "rewalk": float(kern_ms[:, 2].mean()) if len(kern_ms) else None},
                 "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms], "wall_s": wall}
         if not args.skip_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(f, o, d)

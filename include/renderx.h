@@ -92,8 +92,26 @@ typedef struct rx_pt_options {
                               (light sampling + balance-heuristic MIS) */
   uint64_t seed;
   uint32_t paths_per_pass; /* wavefront size, 0 = 2^21 */
-  uint32_t flags;          /* reserved, 0 */
+  uint32_t flags;          /* RX_PT_GUIDED or 0 */
 } rx_pt_options;
+
+/* rx_pt_options.flags: sample directions at diffuse / glossy / Phong vertices by
+ * one-sample MIS between the BSDF and the context's guiding network (rx_guide_init),
+ * training the network on the render's own samples during the first train_passes
+ * passes. PathTracer (nee = 0) only. */
+#define RX_PT_GUIDED 1u
+
+/* Learned path guiding (no reference counterpart): a BF16 MLP on the tensor cores,
+ * 80 encoded inputs -> 4 x 64 ReLU -> 8 von Mises-Fisher lobes, trained online with Adam. */
+typedef struct rx_guide_options {
+  float learning_rate;     /* Adam step size (5e-3) */
+  float bsdf_fraction;     /* one-sample MIS: probability of sampling the BSDF (0.5) */
+  uint32_t batch;          /* training records per Adam step (2^18) */
+  uint32_t train_passes;   /* rendering passes whose samples train the network */
+  uint32_t steps_per_pass; /* Adam steps after each training pass */
+  uint32_t flags;          /* reserved, 0 */
+  uint64_t seed;           /* weight initialisation */
+} rx_guide_options;
 
 /* Vertex connection and merging options (VCMTracer, reference include/VCMTracer.h). */
 typedef struct rx_vcm_options {
@@ -197,9 +215,50 @@ rx_status rx_render_vcm(rx_context* ctx, const rx_camera* cam, const rx_vcm_opti
  * leaf postponing; blocks of 128 threads, blocks_per_sm per SM. No reference
  * counterpart (launch tuning). */
 rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_per_sm);
+/* Per-kernel device timing of rx_trace_closest_device calls: the next max_calls calls
+ * record CUDA events around their three kernels (walk, reference-visibility check,
+ * re-walk of rejected winners); 0 turns timing off. No reference counterpart
+ * (measurement). */
+rx_status rx_trace_set_timing(rx_context* ctx, int32_t max_calls);
+/* ms3[3*i + j]: device milliseconds of kernel j in recorded call i (waits for the
+ * events); *calls = number of recorded calls. ms3 may be NULL to query the count. */
+rx_status rx_trace_read_timing(rx_context* ctx, float* ms3, int32_t* calls);
 /* Rays whose lazy winner failed the reference-visibility check and were re-traced
  * exactly, counted since the last reset (diagnostic). */
 rx_status rx_trace_counters(rx_context* ctx, uint64_t out[4], int reset);
+
+/* ---- learned guiding ------------------------------------------------------------- */
+/* Creates (or re-creates) the context's guiding network with seeded weights. box6 = the
+ * position-encoding box {min xyz, max xyz}; NULL takes the bounds of the scene geometry.
+ * Records everywhere below are 16 floats: position, shading normal, outgoing direction,
+ * incident direction, weight (integrand / sampling density), 3 unused. */
+rx_status rx_guide_init(rx_context* ctx, const rx_guide_options* opts, const float* box6);
+/* FP32 master parameters, 21504 floats: layer l's [out][in] row-major block at
+ * {0, 5120, 9216, 13312, 17408}, widths in = {80, 64, 64, 64, 64}, 64 rows each (the last
+ * layer's rows 40..63 are zero). set_params also resets the Adam moments. */
+rx_status rx_guide_get_params(rx_context* ctx, float* params);
+rx_status rx_guide_set_params(rx_context* ctx, const float* params);
+/* Forward pass (inference kernel) on n host records: raw40 (n x 40, optional) = the
+ * network outputs; pdf (n, optional) = the mixture density of each record's incident
+ * direction. */
+rx_status rx_guide_eval(rx_context* ctx, const float* recs, uint32_t n, float* raw40, float* pdf);
+/* Gradient (training kernel, no update) of the batch loss
+ * -sum_s w_s log q(wi_s) / sum_s w_s (weights clipped at 32 x their mean) over n host
+ * records: grad receives 21504 floats, *loss the loss. */
+rx_status rx_guide_gradient(rx_context* ctx, const float* recs, uint32_t n, float* grad, float* loss);
+/* One Adam step on n device records (16-byte aligned), enqueued on `stream`; with loss
+ * non-NULL waits and returns the batch loss. */
+rx_status rx_guide_train_step(rx_context* ctx, const float* d_recs, uint32_t n, float* loss, void* stream);
+
+/* ---- diagnostics ---------------------------------------------------------------- */
+/* Tensor-core operand-layout self-test (no reference counterpart): D = A * B^T with A
+ * M x K and B N x K row-major BF16 host arrays, through one CTA's tcgen05 MMAs with FP32
+ * accumulation in tensor memory. a_mn / b_mn stage A / B in the MN-major instead of the
+ * K-major shared-memory view. d_out (host) receives all 128 tensor-memory lanes x N
+ * columns, zero where the accumulator does not reach. M is 64 or 128, N 16..128 and K
+ * 16..128, both in steps of 16. */
+rx_status rx_diag_umma_gemm(rx_context* ctx, uint32_t M, uint32_t N, uint32_t K, int32_t a_mn, int32_t b_mn,
+                            const uint16_t* a_bf16, const uint16_t* b_bf16, float* d_out);
 
 #ifdef __cplusplus
 }

@@ -139,11 +139,12 @@ class Context:
 
     # -- rendering -------------------------------------------------------------------
     def render_pt(self, camera: "scenes.Camera", spp: int, max_depth: int = 8, nee: bool = False, rr_mode: int = 0,
-                  seed: int = 1, paths_per_pass: int = 0, want_sq: bool = False):
+                  seed: int = 1, paths_per_pass: int = 0, want_sq: bool = False, guided: bool = False):
         """PathTracer (nee=False) or PathTracerTest (nee=True) renderPixels for ``spp``
-        samples: returns (mean (H,W,3) float64, mean of squares or None, stats dict)."""
+        samples: returns (mean (H,W,3) float64, mean of squares or None, stats dict).
+        guided: one-sample MIS with the guiding network (guide_init first; PathTracer only)."""
         cam = camera_struct(camera)
-        o = rx_pt_options(spp, max_depth, rr_mode, int(bool(nee)), seed, paths_per_pass, 0)
+        o = rx_pt_options(spp, max_depth, rr_mode, int(bool(nee)), seed, paths_per_pass, 1 if guided else 0)
         h, w = camera.height, camera.width
         film = np.zeros((h, w, 3), np.float64)
         sq = np.zeros((h, w, 3), np.float64) if want_sq else None
@@ -164,6 +165,74 @@ class Context:
 
     def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
+
+    def set_trace_timing(self, max_calls: int):
+        """Record per-kernel CUDA events for the next ``max_calls`` device trace calls."""
+        self._ck(self._L.rx_trace_set_timing(self.h, int(max_calls)))
+
+    def read_trace_timing(self) -> np.ndarray:
+        """(calls, 3) device milliseconds: walk, visibility check, re-walk."""
+        n = ctypes.c_int32(0)
+        self._ck(self._L.rx_trace_read_timing(self.h, None, ctypes.byref(n)))
+        out = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            self._ck(self._L.rx_trace_read_timing(self.h, _capi.ptr(out), ctypes.byref(n)))
+        return out
+
+    def diag_umma_gemm(self, a: np.ndarray, b: np.ndarray, a_mn: bool = False, b_mn: bool = False) -> np.ndarray:
+        """Tensor-core layout self-test: A (M x K) and B (N x K) as bf16 bit patterns
+        (uint16); returns all 128 tensor-memory lanes x N columns of A @ B.T (float32)."""
+        a = np.ascontiguousarray(a, np.uint16)
+        b = np.ascontiguousarray(b, np.uint16)
+        (m, k), n = a.shape, b.shape[0]
+        assert b.shape[1] == k
+        out = np.zeros((128, n), np.float32)
+        self._ck(self._L.rx_diag_umma_gemm(self.h, m, n, k, int(a_mn), int(b_mn), _capi.ptr(a), _capi.ptr(b),
+                                           _capi.ptr(out)))
+        return out
+
+    # ---- learned guiding ---------------------------------------------------------
+    def guide_init(self, learning_rate: float = 5e-3, bsdf_fraction: float = 0.5, batch: int = 1 << 18,
+                   train_passes: int = 4, steps_per_pass: int = 4, seed: int = 1, box=None):
+        """Creates the guiding network (seeded weights). box = (min xyz, max xyz) of the
+        position encoding, default the scene bounds."""
+        o = _capi.rx_guide_options(learning_rate, bsdf_fraction, batch, train_passes, steps_per_pass, 0, seed)
+        b = None if box is None else np.ascontiguousarray(np.concatenate([box[0], box[1]]), np.float32)
+        self._ck(self._L.rx_guide_init(self.h, ctypes.byref(o), _capi.ptr(b)))
+
+    def guide_params(self) -> np.ndarray:
+        out = np.zeros(21504, np.float32)
+        self._ck(self._L.rx_guide_get_params(self.h, _capi.ptr(out)))
+        return out
+
+    def guide_set_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.shape == (21504,)
+        self._ck(self._L.rx_guide_set_params(self.h, _capi.ptr(p)))
+
+    def guide_eval(self, recs: np.ndarray):
+        """Forward pass on (n, 16) records: (raw outputs (n, 40), mixture pdf of wi (n,))."""
+        r = np.ascontiguousarray(recs, np.float32)
+        n = len(r)
+        raw = np.zeros((n, 40), np.float32)
+        pdf = np.zeros(n, np.float32)
+        self._ck(self._L.rx_guide_eval(self.h, _capi.ptr(r), n, _capi.ptr(raw), _capi.ptr(pdf)))
+        return raw, pdf
+
+    def guide_gradient(self, recs: np.ndarray):
+        """(loss, gradient (21504,)) of the batch loss on (n, 16) records, no update."""
+        r = np.ascontiguousarray(recs, np.float32)
+        g = np.zeros(21504, np.float32)
+        loss = ctypes.c_float(0)
+        self._ck(self._L.rx_guide_gradient(self.h, _capi.ptr(r), len(r), _capi.ptr(g), ctypes.byref(loss)))
+        return float(loss.value), g
+
+    def guide_train_step(self, d_recs, n: int, stream=None, want_loss: bool = True):
+        """One Adam step on n device records (a pointer or tensor)."""
+        loss = ctypes.c_float(0)
+        self._ck(self._L.rx_guide_train_step(self.h, _capi.ptr(d_recs), n,
+                                             ctypes.byref(loss) if want_loss else None, _capi.stream_arg(stream)))
+        return float(loss.value) if want_loss else None
 
     def counters(self, reset: bool = False) -> dict:
         out = np.zeros(4, np.uint64)

@@ -53,6 +53,12 @@ class rx_render_stats(ctypes.Structure):
                 ("ms", ctypes.c_float), ("reserved", ctypes.c_float)]
 
 
+class rx_guide_options(ctypes.Structure):
+    _fields_ = [("learning_rate", ctypes.c_float), ("bsdf_fraction", ctypes.c_float), ("batch", ctypes.c_uint32),
+                ("train_passes", ctypes.c_uint32), ("steps_per_pass", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64)]
+
+
 class rx_build_options(ctypes.Structure):
     _fields_ = [("split_policy", ctypes.c_int32), ("leaf_size", ctypes.c_int32), ("host_threads", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]
@@ -78,6 +84,15 @@ SIGNATURES = [
     ("rx_trace_closest_reforder_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_counters", S, [P, P, S]),
     ("rx_trace_set_config", S, [P, I32, I32]),
+    ("rx_trace_set_timing", S, [P, I32]),
+    ("rx_diag_umma_gemm", S, [P, U32, U32, U32, I32, I32, P, P, P]),
+    ("rx_guide_init", S, [P, P, P]),
+    ("rx_guide_get_params", S, [P, P]),
+    ("rx_guide_set_params", S, [P, P]),
+    ("rx_guide_eval", S, [P, P, U32, P, P]),
+    ("rx_guide_gradient", S, [P, P, U32, P, P]),
+    ("rx_guide_train_step", S, [P, P, U32, P, P]),
+    ("rx_trace_read_timing", S, [P, P, P]),
     ("rx_render_pt", S, [P, P, P, P, P, P]),
     ("rx_render_vcm", S, [P, P, P, P, P]),
 ]

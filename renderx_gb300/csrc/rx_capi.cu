@@ -5,24 +5,13 @@
 #include <cstring>
 #include <new>
 
+#include "rx_guide.h"
 #include "rx_internal.h"
 
 using rx::DevBuf;
+using rx::DeviceGuard;
 
 namespace {
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    cudaGetDevice(&prev);
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    cudaGetDevice(&cur);
-    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-  }
-};
 
 rx_status upload(rx_context* c, DevBuf& b, const void* src, size_t bytes, const char* what) {
   rx_status s = c->cuda(b.alloc(bytes), what);
@@ -75,6 +64,9 @@ void rx_destroy(rx_context* c) {
     for (int k = 0; k < 2; k++)
       for (DevBuf* b : {&c->ring_rays[k], &c->ring_tid[k], &c->ring_dist[k], &c->ring_queue[k], &c->ring_counters[k]})
         b->release();
+    for (cudaEvent_t e : c->timing_ev) cudaEventDestroy(e);
+    rx::guide_free(c->guide);
+    c->guide = nullptr;
     if (c->stream) cudaStreamDestroy(c->stream);
     for (auto s : c->copy_stream)
       if (s) cudaStreamDestroy(s);
@@ -341,6 +333,11 @@ rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options*
   if (opts->spp == 0) return c->fail(RX_ERR_INVALID, "spp must be positive");
   if (opts->max_depth > 1000) return c->fail(RX_ERR_INVALID, "max_depth too large");
   if (opts->nee && c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
+  if (opts->flags & ~RX_PT_GUIDED) return c->fail(RX_ERR_INVALID, "unknown flags");
+  if (opts->flags & RX_PT_GUIDED) {
+    if (opts->nee) return c->fail(RX_ERR_INVALID, "guiding applies to PathTracer (nee = 0)");
+    if (!rx::guide_ready(c->guide)) return c->fail(RX_ERR_STATE, "guided rendering needs rx_guide_init");
+  }
   DeviceGuard g(c->device);
   size_t np = (size_t)cam->width * cam->height;
   DevBuf sum, sq;
@@ -419,9 +416,46 @@ rx_status rx_trace_closest_device(rx_context* c, const rx_ray* d_rays, uint32_t 
   rx_status s = ensure_queue(c, n);
   if (s != RX_OK) return s;
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const cudaEvent_t* ev = nullptr;
+  if (c->timing_on && c->timing_used + 4 <= c->timing_ev.size()) {
+    ev = &c->timing_ev[c->timing_used];
+    c->timing_used += 4;
+  }
   return c->cuda(rx::launch_trace_closest(c->accel, d_rays, n, d_tid, d_dist, c->d_queue.as<uint32_t>(),
-                                          c->d_counters.as<unsigned long long>(), c->trace_cfg, st),
+                                          c->d_counters.as<unsigned long long>(), c->trace_cfg, st, ev),
                  "trace_closest launch");
+}
+
+rx_status rx_trace_set_timing(rx_context* c, int32_t max_calls) {
+  if (!c || max_calls < 0 || max_calls > 4096) return c ? c->fail(RX_ERR_INVALID, "max_calls must be 0..4096") : RX_ERR_INVALID;
+  DeviceGuard g(c->device);
+  for (cudaEvent_t e : c->timing_ev) cudaEventDestroy(e);
+  c->timing_ev.clear();
+  c->timing_used = 0;
+  c->timing_on = max_calls > 0;
+  for (int32_t k = 0; k < 4 * max_calls; k++) {
+    cudaEvent_t e;
+    rx_status s = c->cuda(cudaEventCreate(&e), "create timing event");
+    if (s != RX_OK) return s;
+    c->timing_ev.push_back(e);
+  }
+  return RX_OK;
+}
+
+rx_status rx_trace_read_timing(rx_context* c, float* ms3, int32_t* calls) {
+  if (!c || !calls) return RX_ERR_INVALID;
+  DeviceGuard g(c->device);
+  int32_t k = (int32_t)(c->timing_used / 4);
+  if (ms3) {
+    for (int32_t i = 0; i < k; i++) {
+      const cudaEvent_t* e = &c->timing_ev[4 * (size_t)i];
+      rx_status s = c->cuda(cudaEventSynchronize(e[3]), "timing events");
+      if (s != RX_OK) return s;
+      for (int j = 0; j < 3; j++) cudaEventElapsedTime(&ms3[3 * i + j], e[j], e[j + 1]);
+    }
+  }
+  *calls = k;
+  return RX_OK;
 }
 
 rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,

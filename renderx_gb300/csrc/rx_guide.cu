@@ -1,0 +1,933 @@
+// Learned path guiding on the fifth-generation tensor cores: a BF16 MLP (FP32
+// accumulation in tensor memory) mapping a surface point, its normal and the outgoing
+// direction to a mixture of von Mises-Fisher lobes over incident directions, trained
+// online by the renderer's own radiance samples. No counterpart in the reference: it is
+// the learned proposal that the path tracer combines with BSDF sampling by one-sample MIS.
+//
+// Network: 80 inputs (12-frequency sin/cos encoding of the position normalised to the
+// scene box, the shading normal, the outgoing direction, a constant 1) -> 4 hidden
+// layers of 64 ReLU units -> 64 outputs of which 40 are used: 8 lobes x (weight logit,
+// log-concentration, 3 mean coordinates). Weights and activations BF16, accumulation
+// FP32 in tensor memory. One CTA of 128 threads owns a tile of 128 samples; thread s owns
+// sample s (tensor-memory lane s of the M = 128 accumulators).
+//
+// Training minimises the cross entropy of the mixture against the renderer's integrand
+// samples, -sum_s w_s log q(wi_s) / sum_s w_s, with w_s = (BSDF x cosine x incident
+// radiance) / (sampling density) of sample s. The training kernel runs forward and
+// backward per tile and accumulates every layer's weight gradient in tensor memory
+// across all tiles a CTA processes; one flush per CTA adds them to the FP32 gradient.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "rx_guide.h"
+#include "rx_internal.h"
+#include "rx_tc.cuh"
+
+namespace rx {
+
+constexpr uint32_t kDiagARegion = 96u << 10;   // A operand region (bytes)
+constexpr uint32_t kDiagBRegion = 100u << 10;  // B operand region
+constexpr uint32_t kDiagSmem = kDiagARegion + kDiagBRegion + 64;
+
+// D = A * B^T on one CTA of 128 threads. A: M x K, B: N x K (row-major bf16 in global
+// memory), placed in shared memory in the K-major or MN-major core-matrix view. Every
+// TMEM lane (128) x N columns is zeroed first and written out, so rows >= M show where an
+// M = 64 accumulator lands.
+__global__ void __launch_bounds__(128) k_diag_umma(const uint16_t* A, const uint16_t* B, float* D, uint32_t M,
+                                                   uint32_t N, uint32_t K, int a_mn, int b_mn, int* status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  unsigned char* sa = smem;
+  unsigned char* sb = smem + kDiagARegion;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // stage operands
+  for (uint32_t i = tid; i < M * K; i += blockDim.x) {
+    uint32_t m = i / K, k = i % K;
+    uint32_t off = a_mn ? tc::core_off(k, m, M) : tc::core_off(m, k, K);
+    *reinterpret_cast<uint16_t*>(sa + off) = A[i];
+  }
+  for (uint32_t i = tid; i < N * K; i += blockDim.x) {
+    uint32_t n = i / K, k = i % K;
+    uint32_t off = b_mn ? tc::core_off(k, n, N) : tc::core_off(n, k, K);
+    *reinterpret_cast<uint16_t*>(sb + off) = B[i];
+  }
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
+  tc::fence_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tbase = tmem_base;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  float z[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) z[i] = 0.0f;
+  for (uint32_t c = 0; c < N; c += 16) tc::tmem_st16(tbase + lane_base + c, z);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (tid == 0) {
+    uint32_t idesc = tc::idesc_bf16(M, N, a_mn != 0, b_mn != 0);
+    uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
+    for (uint32_t k0 = 0; k0 < K; k0 += 16) {
+      uint64_t ad = a_mn ? tc::sdesc(a0 + tc::core_off(k0, 0, M), (M >> 3) * 128u, 128u)
+                         : tc::sdesc(a0 + tc::core_off(0, k0, K), 128u, (K >> 3) * 128u);
+      uint64_t bd = b_mn ? tc::sdesc(b0 + tc::core_off(k0, 0, N), (N >> 3) * 128u, 128u)
+                         : tc::sdesc(b0 + tc::core_off(0, k0, K), 128u, (K >> 3) * 128u);
+      tc::mma_bf16(tbase, ad, bd, idesc, k0 > 0);
+    }
+    tc::mma_commit(&bar);
+  }
+  bool ok = tc::mbar_wait(&bar, 0);
+  tc::tc_fence_after();
+  if (!ok) {
+    if ((tid & 31) == 0) atomicExch(status, 1);
+  } else {
+    for (uint32_t c = 0; c < N; c += 16) {
+      float v[16];
+      tc::tmem_ld16(tbase + lane_base + c, v);
+#pragma unroll
+      for (int i = 0; i < 16; i++) D[(size_t)tid * N + c + i] = v[i];
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, 128);
+}
+
+// =======================================================================================
+// Network kernels
+// =======================================================================================
+using namespace guide;
+
+// Tensor-memory placement of an M = 64 accumulator (cta_group::1): row r in lane
+// 32 (r / 16) + r % 16 (lanes 0..15 of each 32-lane quarter) when set, else lane r.
+#ifndef RX_M64_SPLIT
+#define RX_M64_SPLIT 1
+#endif
+// Row of an M = 64 accumulator that tensor-memory lane `lane` (0..127) holds, or -1.
+__device__ __forceinline__ int m64_row(int lane) {
+#if RX_M64_SPLIT
+  return (lane & 31) < 16 ? (lane >> 5) * 16 + (lane & 15) : -1;
+#else
+  return lane < 64 ? lane : -1;
+#endif
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // a in the low half (lower address)
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xFFFF0000u); }
+
+__device__ __forceinline__ void store_chunk(unsigned char* base, uint32_t off, const float (&f)[8]) {
+  uint4 u;
+  u.x = pack_bf16(f[0], f[1]);
+  u.y = pack_bf16(f[2], f[3]);
+  u.z = pack_bf16(f[4], f[5]);
+  u.w = pack_bf16(f[6], f[7]);
+  *reinterpret_cast<uint4*>(base + off) = u;
+}
+
+// Encodes one query (position, normal, outgoing direction) into row s of the 128 x 80
+// input tile. Feature j < 72: coordinate c = j / 24, frequency f = (j % 24) / 2,
+// sin (j even) or cos (j odd) of pi 2^f p_c with p_c = (x_c - min_c) / extent_c;
+// 72..74 normal, 75..77 outgoing direction, 78 = 1, 79 = 0.
+__device__ void encode_row(const float (&q)[9], bool valid, const Box& box, unsigned char* A0, int s) {
+  float p[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) p[c] = valid ? __fdiv_rn(__fsub_rn(q[c], box.mn[c]), box.ext[c]) : 0.0f;
+#pragma unroll
+  for (int ch = 0; ch < 9; ch++) {
+    float f[8];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      int j = ch * 8 + t;
+      int c = j / 24, fr = (j % 24) / 2;
+      float sn = 0.0f, cs = 0.0f;
+      if (valid) sincospif(ldexpf(p[c], fr), &sn, &cs);
+      f[t] = sn;
+      f[t + 1] = cs;
+    }
+    store_chunk(A0, tc::core_off(s, ch * 8, kIn), f);
+  }
+  float f[8] = {q[3], q[4], q[5], q[6], q[7], q[8], 1.0f, 0.0f};
+  if (!valid)
+#pragma unroll
+    for (int t = 0; t < 8; t++) f[t] = 0.0f;
+  store_chunk(A0, tc::core_off(s, 72, kIn), f);
+}
+
+// Hidden-layer epilogue: the thread's accumulator row (64 columns) -> ReLU -> BF16 row s.
+__device__ __forceinline__ void epi_relu(uint32_t tacc, unsigned char* out, int s) {
+#pragma unroll
+  for (int c0 = 0; c0 < kHid; c0 += 16) {
+    float v[16];
+    tc::tmem_ld16(tacc + c0, v);
+    float a[8], b[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      a[i] = fmaxf(v[i], 0.0f);
+      b[i] = fmaxf(v[8 + i], 0.0f);
+    }
+    store_chunk(out, tc::core_off(s, c0, kHid), a);
+    store_chunk(out, tc::core_off(s, c0 + 8, kHid), b);
+  }
+}
+
+__device__ __forceinline__ void load_raw(uint32_t tacc, float (&raw)[48]) {
+#pragma unroll
+  for (int c0 = 0; c0 < 48; c0 += 16) {
+    float v[16];
+    tc::tmem_ld16(tacc + c0, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) raw[c0 + i] = v[i];
+  }
+}
+
+constexpr float kLogKMin = -4.0f, kLogKMax = 8.0f;
+
+// Lobe j of the raw outputs: log weight (log-softmax), concentration, mean, and the log
+// of the vMF normaliser kappa / (2 pi (1 - e^{-2 kappa})).
+struct Lobe {
+  float logpi, kappa, mu[3], len, lognorm;
+  bool kin;  // log-concentration inside its clamp range (gradient flows)
+};
+__device__ __forceinline__ void decode(const float (&raw)[48], Lobe (&L)[kLobes]) {
+  float amax = raw[0];
+#pragma unroll
+  for (int j = 1; j < kLobes; j++) amax = fmaxf(amax, raw[5 * j]);
+  float z = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) z += expf(raw[5 * j] - amax);
+  float logz = amax + logf(z);
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) {
+    Lobe& l = L[j];
+    l.logpi = raw[5 * j] - logz;
+    float b = raw[5 * j + 1];
+    l.kin = b > kLogKMin && b < kLogKMax;
+    l.kappa = expf(fminf(fmaxf(b, kLogKMin), kLogKMax));
+    float m0 = raw[5 * j + 2], m1 = raw[5 * j + 3], m2 = raw[5 * j + 4];
+    l.len = fmaxf(sqrtf(m0 * m0 + m1 * m1 + m2 * m2), 1e-6f);
+    l.mu[0] = m0 / l.len;
+    l.mu[1] = m1 / l.len;
+    l.mu[2] = m2 / l.len;
+    l.lognorm = logf(l.kappa) - logf(2.0f * RX_PI) - logf(-expm1f(-2.0f * l.kappa));
+  }
+}
+
+// -scale * log q(wi) and its gradient with respect to the 40 raw outputs.
+__device__ float mix_loss_grad(const float (&raw)[48], const float (&wi)[3], float scale, float (&dz)[48]) {
+  Lobe L[kLobes];
+  decode(raw, L);
+  float lv[kLobes], t[kLobes];
+  float mx = -INFINITY;
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) {
+    t[j] = L[j].mu[0] * wi[0] + L[j].mu[1] * wi[1] + L[j].mu[2] * wi[2];
+    lv[j] = L[j].logpi + L[j].lognorm + L[j].kappa * (t[j] - 1.0f);
+    mx = fmaxf(mx, lv[j]);
+  }
+  float sum = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) sum += expf(lv[j] - mx);
+  float lq = mx + logf(sum);
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) {
+    float g = expf(lv[j] - lq);  // responsibility
+    float pi = expf(L[j].logpi);
+    float k = L[j].kappa;
+    dz[5 * j] = scale * (pi - g);
+    float dk = 1.0f - 2.0f * k / expm1f(2.0f * k) + k * (t[j] - 1.0f);  // kappa * d log v / d kappa
+    dz[5 * j + 1] = L[j].kin ? -scale * g * dk : 0.0f;
+    float c = -scale * g * k / L[j].len;
+#pragma unroll
+    for (int a = 0; a < 3; a++) dz[5 * j + 2 + a] = c * (wi[a] - t[j] * L[j].mu[a]);
+  }
+#pragma unroll
+  for (int i = kOutUsed; i < 48; i++) dz[i] = 0.0f;
+  return -lq;
+}
+
+// Mixture for sampling / evaluation: per lobe weight, kappa, mean, weight x normaliser.
+__device__ void mix_store(const float (&raw)[48], float* out) {
+  Lobe L[kLobes];
+  decode(raw, L);
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) {
+    float* o = out + j * kLobeFloats;
+    o[0] = expf(L[j].logpi);
+    o[1] = L[j].kappa;
+    o[2] = L[j].mu[0];
+    o[3] = L[j].mu[1];
+    o[4] = L[j].mu[2];
+    o[5] = expf(L[j].logpi + L[j].lognorm);
+  }
+}
+
+__device__ float mix_pdf_raw(const float (&raw)[48], const float (&wi)[3]) {
+  Lobe L[kLobes];
+  decode(raw, L);
+  float q = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kLobes; j++) {
+    float t = L[j].mu[0] * wi[0] + L[j].mu[1] * wi[1] + L[j].mu[2] * wi[2];
+    q += expf(L[j].logpi + L[j].lognorm + L[j].kappa * (t - 1.0f));
+  }
+  return q;
+}
+
+// Issues the forward MMAs of layer l (A: 128 x K K-major, W: 64 x K K-major) into `tacc`.
+__device__ __forceinline__ void issue_fwd(uint32_t tacc, const unsigned char* A, const unsigned char* W, int K) {
+  const uint32_t id = tc::idesc_bf16(128, 64, false, false);
+  const uint32_t a0 = tc::smem_u32(A), w0 = tc::smem_u32(W);
+  const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    uint64_t ad = tc::sdesc(a0 + tc::core_off(0, k0, K), 128u, sbo);
+    uint64_t wd = tc::sdesc(w0 + tc::core_off(0, k0, K), 128u, sbo);
+    tc::mma_bf16(tacc, ad, wd, id, k0 > 0);
+  }
+}
+
+// Block-wide barrier that also orders tensor-core work and generic shared-memory writes.
+__device__ __forceinline__ void tc_sync() {
+  tc::fence_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+}
+
+// Shared-memory plan of the network kernels (bytes from the dynamic base).
+constexpr uint32_t kSmW = 0;                         // weight image
+constexpr uint32_t kSmA0 = kImgBytes;                // 128 x 80 input tile
+constexpr uint32_t kSmA1 = kSmA0 + 128 * kIn * 2;    // hidden activations, 128 x 64 each
+constexpr uint32_t kActBytes = 128 * kHid * 2;
+constexpr uint32_t kSmInfer = kSmA1 + 2 * kActBytes;                 // inference: 2 ping-pong buffers
+constexpr uint32_t kSmTrain = kSmA1 + 4 * kActBytes + kActBytes;     // training: A1..A4 + dZ
+
+// Loads the weight image into shared memory with bulk copies (one per layer).
+__device__ __forceinline__ void load_weights(unsigned char* sm, const unsigned char* img, uint64_t* bar) {
+  tc::mbar_expect_tx(bar, kImgBytes);
+#pragma unroll
+  for (int l = 0; l < 5; l++) {
+    uint32_t bytes = (l == 4 ? kImgBytes : layer_img(l + 1)) - layer_img(l);
+    tc::bulk_g2s(sm + kSmW + layer_img(l), img + layer_img(l), bytes, bar);
+  }
+}
+
+// ---- inference -------------------------------------------------------------------------
+// Queries from records (x, n, wo, wi, ...): raw outputs and the mixture pdf at wi.
+struct RecordIO {
+  const float* recs;
+  float* raw_out;  // n x 40 (optional)
+  float* pdf_out;  // n (optional)
+  __device__ bool load(uint32_t i, float (&q)[9], float (&wi)[3]) const {
+    const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
+    float4 a = r[0], b = r[1], c = r[2];
+    q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w; q[8] = c.x;
+    wi[0] = c.y; wi[1] = c.z; wi[2] = c.w;
+    return true;
+  }
+  __device__ void store(uint32_t i, const float (&raw)[48], const float (&wi)[3]) const {
+    if (raw_out)
+      for (int k = 0; k < kOutUsed; k++) raw_out[(size_t)i * kOutUsed + k] = raw[k];
+    if (pdf_out) pdf_out[i] = mix_pdf_raw(raw, wi);
+  }
+};
+
+// Queries from the wavefront: the hit point of each live path, if its surface is guided
+// (diffuse, glossy or Phong, seen from the front, the path not inside an object).
+struct PathIO {
+  DevScene S;
+  PathSoA P;
+  const int2* hit;
+  float* lobes;
+  __device__ bool load(uint32_t i, float (&q)[9], float (&wi)[3]) const {
+    wi[0] = wi[1] = wi[2] = 0.0f;
+    int2 h = hit[i];
+    int4 inf = P.info[i];
+    bool ok = h.x >= 0 && inf.z < 0;
+    int obj = ok ? (int)__ldg(&S.tri_obj[h.x]) : -1;
+    if (ok) {
+      uint32_t m = S.objects[obj].material;
+      ok = m == kDiffuse || m == kGlossy || m == kPhong;
+    }
+    if (!ok) {
+      lobes[(size_t)i * kLobeStride] = -1.0f;  // not guided
+      return false;
+    }
+    float4 o = P.o[i], d = P.d[i];
+    float t = __int_as_float(h.y);
+    F3 x = F3{o.x, o.y, o.z} + F3{d.x, d.y, d.z} * t;
+    TriGeom g = tri_geom(S, h.x);
+    F3 n = world_normal(g, S.objects[obj].has_normals, x);
+    if (n.x * d.x + n.y * d.y + n.z * d.z > 0.0f) {
+      lobes[(size_t)i * kLobeStride] = -1.0f;
+      return false;
+    }
+    q[0] = x.x; q[1] = x.y; q[2] = x.z; q[3] = n.x; q[4] = n.y; q[5] = n.z; q[6] = -d.x; q[7] = -d.y; q[8] = -d.z;
+    return true;
+  }
+  __device__ void store(uint32_t i, const float (&raw)[48], const float (&)[3]) const {
+    mix_store(raw, lobes + (size_t)i * kLobeStride);
+  }
+};
+
+// Persistent inference: 128-sample tiles, five layers each (MMA, then the epilogue).
+template <class IO>
+__global__ void __launch_bounds__(128) k_guide_infer(IO io, const unsigned* count, uint32_t n_host,
+                                                     const unsigned char* img, Box box, int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar_mma, bar_w;
+  __shared__ uint32_t tmem_base;
+  const int s = threadIdx.x, warp = s >> 5;
+  const uint32_t n = count ? *count : n_host;
+  const uint32_t ntiles = (n + kTile - 1) / kTile;
+  if (blockIdx.x >= ntiles) return;
+  if (s == 0) {
+    tc::mbar_init(&bar_mma, 1);
+    tc::mbar_init(&bar_w, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (s == 0) load_weights(sm, img, &bar_w);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+  tc_sync();
+  const uint32_t tacc = tmem_base + ((uint32_t)(warp * 32) << 16);
+  bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0));
+  uint32_t ph = 0;
+  unsigned char* A0 = sm + kSmA0;
+  unsigned char* Ab[2] = {sm + kSmA1, sm + kSmA1 + kActBytes};
+  for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    uint32_t i = tile * kTile + s;
+    float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0};
+    bool valid = i < n && io.load(i, q, wi);
+    encode_row(q, valid, box, A0, s);
+    tc_sync();
+    float raw[48];
+    for (int l = 0; l < 5; l++) {
+      const unsigned char* A = l == 0 ? A0 : Ab[(l - 1) & 1];
+      if (s == 0) {
+        issue_fwd(tmem_base, A, sm + kSmW + layer_img(l), layer_k(l));
+        tc::mma_commit(&bar_mma);
+      }
+      ok = __syncthreads_and(tc::mbar_wait(&bar_mma, ph));
+      ph ^= 1;
+      tc::tc_fence_after();
+      if (!ok) break;
+      if (l < 4) epi_relu(tacc, Ab[l & 1], s);
+      else load_raw(tacc, raw);
+      tc_sync();
+    }
+    if (ok && valid) io.store(i, raw, wi);
+  }
+  if (!ok && s == 0) atomicExch(status, 1);
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem_base, 64);
+}
+
+// ---- training --------------------------------------------------------------------------
+// Sum of record weights and number of records (for the loss normalisation).
+__global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t n_host, uint32_t first,
+                             uint32_t len, float* out) {
+  uint32_t n = count ? *count : n_host;
+  uint32_t end = min(first + len, n);
+  float acc = 0.0f;
+  unsigned c = 0;
+  for (uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+    acc += recs[(size_t)i * kRec + 12];
+    c++;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0 && c) {
+    atomicAdd(out, acc);
+    atomicAdd(out + 1, (float)c);
+  }
+}
+
+// Gradient of the batch loss over records [first, first + len) (clipped to the live
+// count): forward and backward per tile, weight gradients accumulated in tensor memory,
+// flushed once per CTA into `grad` (FP32, row-major per layer). wsum = {sum w, count}.
+// Weights are clipped at 32 x their batch mean before normalisation by the sum.
+__global__ void __launch_bounds__(128, 1) k_guide_train(const float* recs, const unsigned* count, uint32_t n_host,
+                                                        uint32_t first, uint32_t len, const unsigned char* img, Box box,
+                                                        const float* wsum, float* grad, float* loss_sum, int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar_mma, bar_w;
+  __shared__ uint32_t tmem_base;
+  __shared__ float red[4];
+  const int s = threadIdx.x, warp = s >> 5;
+  const uint32_t n_all = count ? *count : n_host;
+  const uint32_t end = min(first + len, n_all);
+  const uint32_t n = end > first ? end - first : 0;
+  const uint32_t ntiles = (n + kTile - 1) / kTile;
+  if (blockIdx.x >= ntiles) return;
+  if (s == 0) {
+    tc::mbar_init(&bar_mma, 1);
+    tc::mbar_init(&bar_w, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (s == 0) load_weights(sm, img, &bar_w);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
+  tc_sync();
+  const uint32_t T0 = tmem_base;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t t_fwd = T0, t_da = T0 + 64;
+  const uint32_t t_dw[5] = {T0 + 128, T0 + 208, T0 + 272, T0 + 336, T0 + 400};
+  unsigned char* A[5] = {sm + kSmA0, sm + kSmA1, sm + kSmA1 + kActBytes, sm + kSmA1 + 2 * kActBytes,
+                         sm + kSmA1 + 3 * kActBytes};
+  unsigned char* dZ = sm + kSmA1 + 4 * kActBytes;
+  const float total = wsum[0], cnt = fmaxf(wsum[1], 1.0f);
+  const float wclip = 32.0f * total / cnt;
+  const float inv_total = total > 0.0f ? 1.0f / total : 0.0f;
+  bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0));
+  uint32_t ph = 0;
+  bool first_tile = true;
+  float loss = 0.0f;
+  for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    uint32_t i = first + tile * kTile + s;
+    bool valid = i < end;
+    float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0}, w = 0.0f;
+    if (valid) {
+      const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
+      float4 a = r[0], b = r[1], c = r[2], e = r[3];
+      q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w; q[8] = c.x;
+      wi[0] = c.y; wi[1] = c.z; wi[2] = c.w;
+      w = fminf(e.x, wclip) * inv_total;
+    }
+    encode_row(q, valid, box, A[0], s);
+    tc_sync();
+    // forward
+    for (int l = 0; l < 5 && ok; l++) {
+      if (s == 0) {
+        issue_fwd(T0, A[l], sm + kSmW + layer_img(l), layer_k(l));
+        tc::mma_commit(&bar_mma);
+      }
+      ok = __syncthreads_and(tc::mbar_wait(&bar_mma, ph));
+      ph ^= 1;
+      tc::tc_fence_after();
+      if (!ok) break;
+      if (l < 4) {
+        epi_relu(t_fwd + lane_off, A[l + 1], s);
+      } else {
+        float raw[48], dz[48];
+        load_raw(t_fwd + lane_off, raw);
+        if (valid && w > 0.0f) {
+          loss += mix_loss_grad(raw, wi, w, dz);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 48; k++) dz[k] = 0.0f;
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 8) {
+          float f[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) f[k] = c0 + k < 48 ? dz[c0 + k] : 0.0f;
+          store_chunk(dZ, tc::core_off(s, c0, kOut), f);
+        }
+      }
+      tc_sync();
+    }
+    // backward: dZ holds dZ_{l+1}; dW_l += dZ^T A_l; dA_l = dZ W_l; dZ_l = dA_l * [A_l > 0]
+    for (int l = 4; l >= 0 && ok; l--) {
+      const int K = layer_k(l);
+      if (s == 0) {
+        const uint32_t dz0 = tc::smem_u32(dZ), a0 = tc::smem_u32(A[l]), w0 = tc::smem_u32(sm + kSmW + layer_img(l));
+        const uint32_t id_w = tc::idesc_bf16(64, (uint32_t)K, true, true);
+        for (int s0 = 0; s0 < kTile; s0 += 16) {
+          uint64_t ad = tc::sdesc(dz0 + tc::core_off(s0, 0, kOut), (kOut >> 3) * 128u, 128u);
+          uint64_t bd = tc::sdesc(a0 + tc::core_off(s0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
+          tc::mma_bf16(t_dw[l], ad, bd, id_w, (first_tile && s0 == 0) ? 0u : 1u);
+        }
+        if (l > 0) {
+          const uint32_t id_a = tc::idesc_bf16(128, (uint32_t)K, false, true);
+          for (int n0 = 0; n0 < kOut; n0 += 16) {
+            uint64_t ad = tc::sdesc(dz0 + tc::core_off(0, n0, kOut), 128u, (kOut >> 3) * 128u);
+            uint64_t bd = tc::sdesc(w0 + tc::core_off(n0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
+            tc::mma_bf16(t_da, ad, bd, id_a, n0 > 0);
+          }
+        }
+        tc::mma_commit(&bar_mma);
+      }
+      ok = __syncthreads_and(tc::mbar_wait(&bar_mma, ph));
+      ph ^= 1;
+      tc::tc_fence_after();
+      if (!ok) break;
+      if (l > 0) {
+#pragma unroll
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(t_da + lane_off + c0, v);
+          uint4 m0 = *reinterpret_cast<const uint4*>(A[l] + tc::core_off(s, c0, kHid));
+          uint4 m1 = *reinterpret_cast<const uint4*>(A[l] + tc::core_off(s, c0 + 8, kHid));
+          uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+          float a[8], b[8];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            a[2 * k] = bf16_lo(mw[k]) > 0.0f ? v[2 * k] : 0.0f;
+            a[2 * k + 1] = bf16_hi(mw[k]) > 0.0f ? v[2 * k + 1] : 0.0f;
+            b[2 * k] = bf16_lo(mw[4 + k]) > 0.0f ? v[8 + 2 * k] : 0.0f;
+            b[2 * k + 1] = bf16_hi(mw[4 + k]) > 0.0f ? v[8 + 2 * k + 1] : 0.0f;
+          }
+          store_chunk(dZ, tc::core_off(s, c0, kHid), a);
+          store_chunk(dZ, tc::core_off(s, c0 + 8, kHid), b);
+        }
+      }
+      tc_sync();
+    }
+    first_tile = false;
+  }
+  // flush the weight-gradient accumulators
+  if (ok && !first_tile) {
+    const int row = m64_row(s);
+    for (int l = 0; l < 5; l++) {
+      const int K = layer_k(l);
+      for (int c0 = 0; c0 < K; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(t_dw[l] + lane_off + c0, v);
+        if (row >= 0)
+#pragma unroll
+          for (int k = 0; k < 16; k++) atomicAdd(&grad[layer_w(l) + row * K + c0 + k], v[k]);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+  if ((s & 31) == 0) red[warp] = loss;
+  if (!ok && s == 0) atomicExch(status, 1);
+  tc::tc_fence_before();
+  __syncthreads();
+  if (s == 0) atomicAdd(loss_sum, red[0] + red[1] + red[2] + red[3]);
+  if (warp == 0) tc::tmem_dealloc(T0, 512);
+}
+
+// Writes the BF16 image of FP32 parameters (core-matrix layout per layer).
+__device__ __forceinline__ void image_store(unsigned char* img, int i, float w) {
+  int l = 4;
+  while (l > 0 && i < layer_w(l)) l--;
+  int K = layer_k(l), r = (i - layer_w(l)) / K, c = (i - layer_w(l)) % K;
+  *reinterpret_cast<__nv_bfloat16*>(img + layer_img(l) + tc::core_off(r, c, K)) = __float2bfloat16_rn(w);
+}
+
+__global__ void k_make_image(const float* w, unsigned char* img) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kParams) image_store(img, i, w[i]);
+}
+
+// Adam (bias-corrected), then the BF16 image; clears the gradient.
+__global__ void k_adam(float* w, float* m, float* v, float* g, unsigned char* img, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  float gi = g[i];
+  g[i] = 0.0f;
+  float mi = b1 * m[i] + (1.0f - b1) * gi;
+  float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  w[i] = wi;
+  image_store(img, i, wi);
+}
+
+}  // namespace rx
+
+using rx::DevBuf;
+using rx::DeviceGuard;
+
+extern "C" rx_status rx_diag_umma_gemm(rx_context* c, uint32_t M, uint32_t N, uint32_t K, int32_t a_mn,
+                                       int32_t b_mn, const uint16_t* a, const uint16_t* b, float* d_out) {
+  if (!c) return RX_ERR_INVALID;
+  if (!a || !b || !d_out) return c->fail(RX_ERR_INVALID, "null buffer");
+  if ((M != 64 && M != 128) || N < 16 || N > 128 || N % 16 || K < 16 || K > 128 || K % 16)
+    return c->fail(RX_ERR_INVALID, "M must be 64 or 128, N 16..128 and K 16..128 in steps of 16");
+  DeviceGuard g(c->device);
+  DevBuf da, db, dd, ds;
+  rx_status s;
+  if ((s = c->cuda(da.alloc((size_t)M * K * 2), "alloc")) != RX_OK) return s;
+  if ((s = c->cuda(db.alloc((size_t)N * K * 2), "alloc")) != RX_OK) return s;
+  if ((s = c->cuda(dd.alloc((size_t)128 * N * 4), "alloc")) != RX_OK) return s;
+  if ((s = c->cuda(ds.alloc(4), "alloc")) != RX_OK) return s;
+  cudaMemcpy(da.p, a, (size_t)M * K * 2, cudaMemcpyHostToDevice);
+  cudaMemcpy(db.p, b, (size_t)N * K * 2, cudaMemcpyHostToDevice);
+  cudaMemset(ds.p, 0, 4);
+  cudaFuncSetAttribute(rx::k_diag_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rx::kDiagSmem);
+  rx::k_diag_umma<<<1, 128, rx::kDiagSmem, c->stream>>>(da.as<uint16_t>(), db.as<uint16_t>(), dd.as<float>(), M, N,
+                                                         K, a_mn, b_mn, ds.as<int>());
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "umma self-test")) != RX_OK) return s;
+  int st = 0;
+  cudaMemcpy(&st, ds.p, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(d_out, dd.p, (size_t)128 * N * 4, cudaMemcpyDeviceToHost);
+  if (st) return c->fail(RX_ERR_TIMEOUT, "tensor-core MMA did not complete");
+  return RX_OK;
+}
+
+// =======================================================================================
+// Host state and entry points
+// =======================================================================================
+namespace rx {
+
+struct GuideState {
+  rx_guide_options opt{};
+  guide::Box box{};
+  DevBuf params, m, v, grad, img, scratch, status;  // scratch: {sum w, count, loss}
+  uint32_t step = 0;
+  int sms = 152;
+  bool ready = false;
+};
+
+void guide_free(GuideState* g) { delete g; }
+bool guide_ready(const GuideState* g) { return g && g->ready; }
+float guide_bsdf_fraction(const GuideState* g) { return g->opt.bsdf_fraction; }
+uint32_t guide_train_passes(const GuideState* g) { return g->opt.train_passes; }
+uint32_t guide_steps_per_pass(const GuideState* g) { return g->opt.steps_per_pass; }
+
+// Opts the network kernels into their shared-memory sizes, once per device.
+static void set_kernel_smem() {
+  static uint64_t done_mask = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && (done_mask >> dev) & 1) return;
+  cudaFuncSetAttribute(k_guide_infer<RecordIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
+  cudaFuncSetAttribute(k_guide_infer<PathIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
+  cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTrain);
+  if (dev < 64) done_mask |= 1ull << dev;
+}
+
+cudaError_t guide_infer_paths(GuideState* g, const DevScene& S, const PathSoA& P, const unsigned* count,
+                              const int2* hit, float* lobes, int grid, cudaStream_t s) {
+  set_kernel_smem();
+  PathIO io{S, P, hit, lobes};
+  k_guide_infer<PathIO><<<grid, 128, kSmInfer, s>>>(io, count, 0, g->img.as<unsigned char>(), g->box,
+                                                     g->status.as<int>());
+  return cudaGetLastError();
+}
+
+// One Adam step on records [first, first + len) of `recs` (live count on the device or n).
+static cudaError_t train_step(GuideState* g, const float* recs, const unsigned* count, uint32_t n, uint32_t first,
+                              uint32_t len, cudaStream_t s, bool update) {
+  set_kernel_smem();
+  float* sc = g->scratch.as<float>();
+  cudaMemsetAsync(sc, 0, 3 * sizeof(float), s);
+  k_weight_sum<<<g->sms * 4, 256, 0, s>>>(recs, count, n, first, len, sc);
+  uint32_t tiles = (len + kTile - 1) / kTile;
+  uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)g->sms);
+  if (grid == 0) return cudaGetLastError();
+  k_guide_train<<<grid, 128, kSmTrain, s>>>(recs, count, n, first, len, g->img.as<unsigned char>(), g->box, sc,
+                                            g->grad.as<float>(), sc + 2, g->status.as<int>());
+  if (update) {
+    g->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    float c1 = 1.0f / (1.0f - powf(b1, (float)g->step)), c2 = 1.0f / (1.0f - powf(b2, (float)g->step));
+    k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(g->params.as<float>(), g->m.as<float>(), g->v.as<float>(),
+                                                 g->grad.as<float>(), g->img.as<unsigned char>(),
+                                                 g->opt.learning_rate, b1, b2, 1e-8f, c1, c2);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t guide_train_records(GuideState* g, const float* recs, const unsigned* count, uint32_t n_max, int steps,
+                                cudaStream_t s) {
+  unsigned n = 0;
+  cudaError_t e = cudaMemcpyAsync(&n, count, sizeof n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  n = std::min(n, n_max);
+  uint32_t B = g->opt.batch;
+  if (n < 1024) return cudaSuccess;  // too few samples to learn from
+  for (int k = 0; k < steps && e == cudaSuccess; k++) {
+    uint32_t first = n > B ? (uint32_t)(((uint64_t)k * B) % (n - B + 1)) : 0;
+    e = train_step(g, recs, nullptr, n, first, std::min(B, n), s, true);
+  }
+  return e;
+}
+
+}  // namespace rx
+
+namespace {
+// Seeded uniform in [-1, 1) from (seed, index): splitmix64.
+float init_uniform(uint64_t seed, uint64_t i) {
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (float)((z >> 40) * (1.0 / 16777216.0)) * 2.0f - 1.0f;
+}
+
+rx_status need_guide(rx_context* c) {
+  if (!c) return RX_ERR_INVALID;
+  if (!rx::guide_ready(c->guide)) return c->fail(RX_ERR_STATE, "guiding network not initialised (rx_guide_init)");
+  return RX_OK;
+}
+}  // namespace
+
+extern "C" rx_status rx_guide_init(rx_context* c, const rx_guide_options* opt, const float* box6) {
+  if (!c || !opt) return RX_ERR_INVALID;
+  if (!(opt->learning_rate > 0.0f) || !(opt->bsdf_fraction > 0.0f) || opt->bsdf_fraction > 1.0f || opt->batch == 0)
+    return c->fail(RX_ERR_INVALID, "learning_rate > 0, 0 < bsdf_fraction <= 1 and batch > 0 required");
+  float bmin[3], bmax[3];
+  if (box6) {
+    for (int k = 0; k < 3; k++) bmin[k] = box6[k], bmax[k] = box6[3 + k];
+  } else {
+    if (c->verts.empty()) return c->fail(RX_ERR_STATE, "no geometry for the encoding box (pass box6)");
+    for (int k = 0; k < 3; k++) bmin[k] = INFINITY, bmax[k] = -INFINITY;
+    for (size_t i = 0; i < c->verts.size(); i += 3)
+      for (int k = 0; k < 3; k++) bmin[k] = std::min(bmin[k], c->verts[i + k]), bmax[k] = std::max(bmax[k], c->verts[i + k]);
+  }
+  for (int k = 0; k < 3; k++)
+    if (!(bmax[k] > bmin[k])) return c->fail(RX_ERR_INVALID, "degenerate encoding box");
+  DeviceGuard dg(c->device);
+  auto* g = new rx::GuideState();
+  g->opt = *opt;
+  cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, c->device);
+  for (int k = 0; k < 3; k++) g->box.mn[k] = bmin[k], g->box.ext[k] = bmax[k] - bmin[k];
+  const size_t pb = rx::guide::kParams * sizeof(float);
+  rx_status s = RX_OK;
+  for (DevBuf* b : {&g->params, &g->m, &g->v, &g->grad})
+    if (s == RX_OK) s = c->cuda(b->alloc(pb), "allocate guide parameters");
+  if (s == RX_OK) s = c->cuda(g->img.alloc(rx::guide::kImgBytes), "allocate guide image");
+  if (s == RX_OK) s = c->cuda(g->scratch.alloc(64), "allocate guide scratch");
+  if (s == RX_OK) s = c->cuda(g->status.alloc(16), "allocate guide status");
+  if (s != RX_OK) {
+    delete g;
+    return s;
+  }
+  // He-uniform hidden layers; the output layer scaled by 0.1 (near-uniform start); the
+  // unused output rows 40..63 are zero.
+  std::vector<float> w(rx::guide::kParams, 0.0f);
+  for (int l = 0; l < 5; l++) {
+    int K = rx::guide::layer_k(l);
+    float a = std::sqrt(6.0f / (float)K) * (l == 4 ? 0.1f : 1.0f);
+    int rows = l == 4 ? rx::guide::kOutUsed : 64;
+    for (int r = 0; r < rows; r++)
+      for (int k = 0; k < K; k++) {
+        size_t i = (size_t)rx::guide::layer_w(l) + (size_t)r * K + k;
+        w[i] = a * init_uniform(opt->seed, i);
+      }
+  }
+  cudaMemcpy(g->params.p, w.data(), pb, cudaMemcpyHostToDevice);
+  for (DevBuf* b : {&g->m, &g->v, &g->grad}) cudaMemset(b->p, 0, pb);
+  cudaMemset(g->img.p, 0, rx::guide::kImgBytes);
+  cudaMemset(g->status.p, 0, 16);
+  rx::k_make_image<<<(rx::guide::kParams + 255) / 256, 256, 0, c->stream>>>(g->params.as<float>(),
+                                                                             g->img.as<unsigned char>());
+  s = c->cuda(cudaStreamSynchronize(c->stream), "guide init");
+  if (s != RX_OK) {
+    delete g;
+    return s;
+  }
+  g->ready = true;
+  rx::guide_free(c->guide);
+  c->guide = g;
+  return RX_OK;
+}
+
+extern "C" rx_status rx_guide_get_params(rx_context* c, float* params) {
+  rx_status s = need_guide(c);
+  if (s != RX_OK) return s;
+  if (!params) return c->fail(RX_ERR_INVALID, "null buffer");
+  DeviceGuard dg(c->device);
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide sync")) != RX_OK) return s;
+  return c->cuda(cudaMemcpy(params, c->guide->params.p, rx::guide::kParams * sizeof(float), cudaMemcpyDeviceToHost),
+                 "read guide parameters");
+}
+
+extern "C" rx_status rx_guide_set_params(rx_context* c, const float* params) {
+  rx_status s = need_guide(c);
+  if (s != RX_OK) return s;
+  if (!params) return c->fail(RX_ERR_INVALID, "null buffer");
+  DeviceGuard dg(c->device);
+  rx::GuideState* g = c->guide;
+  const size_t pb = rx::guide::kParams * sizeof(float);
+  cudaMemcpy(g->params.p, params, pb, cudaMemcpyHostToDevice);
+  for (DevBuf* b : {&g->m, &g->v, &g->grad}) cudaMemset(b->p, 0, pb);
+  g->step = 0;
+  rx::k_make_image<<<(rx::guide::kParams + 255) / 256, 256, 0, c->stream>>>(g->params.as<float>(),
+                                                                             g->img.as<unsigned char>());
+  return c->cuda(cudaStreamSynchronize(c->stream), "set guide parameters");
+}
+
+static rx_status guide_status(rx_context* c) {
+  int st = 0;
+  cudaMemcpy(&st, c->guide->status.p, sizeof st, cudaMemcpyDeviceToHost);
+  if (st) {
+    cudaMemset(c->guide->status.p, 0, sizeof st);
+    return c->fail(RX_ERR_TIMEOUT, "tensor-core work did not complete in the network kernel");
+  }
+  return RX_OK;
+}
+
+extern "C" rx_status rx_guide_eval(rx_context* c, const float* recs, uint32_t n, float* raw40, float* pdf) {
+  rx_status s = need_guide(c);
+  if (s != RX_OK) return s;
+  if (n == 0) return RX_OK;
+  if (!recs || (!raw40 && !pdf)) return c->fail(RX_ERR_INVALID, "null buffer");
+  DeviceGuard dg(c->device);
+  rx::GuideState* g = c->guide;
+  DevBuf dr, draw, dp;
+  if ((s = c->cuda(dr.alloc((size_t)n * rx::guide::kRec * 4), "alloc")) != RX_OK) return s;
+  if ((s = c->cuda(draw.alloc((size_t)n * rx::guide::kOutUsed * 4), "alloc")) != RX_OK) return s;
+  if ((s = c->cuda(dp.alloc((size_t)n * 4), "alloc")) != RX_OK) return s;
+  cudaMemcpy(dr.p, recs, (size_t)n * rx::guide::kRec * 4, cudaMemcpyHostToDevice);
+  rx::set_kernel_smem();
+  rx::RecordIO io{dr.as<float>(), draw.as<float>(), dp.as<float>()};
+  uint32_t tiles = (n + rx::guide::kTile - 1) / rx::guide::kTile;
+  uint32_t grid = std::min<uint32_t>(tiles, 2u * (uint32_t)g->sms);
+  rx::k_guide_infer<rx::RecordIO><<<grid, 128, rx::kSmInfer, c->stream>>>(io, nullptr, n, g->img.as<unsigned char>(),
+                                                                           g->box, g->status.as<int>());
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide eval")) != RX_OK) return s;
+  if ((s = guide_status(c)) != RX_OK) return s;
+  if (raw40) cudaMemcpy(raw40, draw.p, (size_t)n * rx::guide::kOutUsed * 4, cudaMemcpyDeviceToHost);
+  if (pdf) cudaMemcpy(pdf, dp.p, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  return RX_OK;
+}
+
+extern "C" rx_status rx_guide_gradient(rx_context* c, const float* recs, uint32_t n, float* grad, float* loss) {
+  rx_status s = need_guide(c);
+  if (s != RX_OK) return s;
+  if (!recs || !grad || n == 0) return c->fail(RX_ERR_INVALID, "null buffer or empty batch");
+  DeviceGuard dg(c->device);
+  rx::GuideState* g = c->guide;
+  DevBuf dr;
+  if ((s = c->cuda(dr.alloc((size_t)n * rx::guide::kRec * 4), "alloc")) != RX_OK) return s;
+  cudaMemcpy(dr.p, recs, (size_t)n * rx::guide::kRec * 4, cudaMemcpyHostToDevice);
+  cudaMemsetAsync(g->grad.p, 0, rx::guide::kParams * 4, c->stream);
+  cudaError_t e = rx::train_step(g, dr.as<float>(), nullptr, n, 0, n, c->stream, false);
+  if ((s = c->cuda(e, "guide gradient")) != RX_OK) return s;
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide gradient")) != RX_OK) return s;
+  if ((s = guide_status(c)) != RX_OK) return s;
+  cudaMemcpy(grad, g->grad.p, rx::guide::kParams * 4, cudaMemcpyDeviceToHost);
+  cudaMemset(g->grad.p, 0, rx::guide::kParams * 4);
+  if (loss) cudaMemcpy(loss, g->scratch.as<float>() + 2, 4, cudaMemcpyDeviceToHost);
+  return RX_OK;
+}
+
+extern "C" rx_status rx_guide_train_step(rx_context* c, const float* d_recs, uint32_t n, float* loss, void* stream) {
+  rx_status s = need_guide(c);
+  if (s != RX_OK) return s;
+  if (!d_recs || n == 0) return c->fail(RX_ERR_INVALID, "null buffer or empty batch");
+  if (reinterpret_cast<uintptr_t>(d_recs) % 16) return c->fail(RX_ERR_INVALID, "records must be 16-byte aligned");
+  DeviceGuard dg(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  cudaError_t e = rx::train_step(c->guide, d_recs, nullptr, n, 0, n, st, true);
+  if ((s = c->cuda(e, "guide train step")) != RX_OK) return s;
+  if (loss) {
+    if ((s = c->cuda(cudaStreamSynchronize(st), "guide train step")) != RX_OK) return s;
+    if ((s = guide_status(c)) != RX_OK) return s;
+    cudaMemcpy(loss, c->guide->scratch.as<float>() + 2, 4, cudaMemcpyDeviceToHost);
+  }
+  return RX_OK;
+}

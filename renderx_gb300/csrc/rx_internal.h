@@ -12,6 +12,9 @@
 
 namespace rx {
 
+struct GuideState;
+void guide_free(GuideState* g);
+
 // Closest-hit launch shape: variant 0 = one thread per ray, 1 = persistent warps
 // refilling finished lanes; blocks_per_sm x sms blocks of 128 threads.
 struct TraceConfig {
@@ -20,12 +23,27 @@ struct TraceConfig {
   int sms = 152;
 };
 
-// Launchers (rx_trace.cu).
+// Launchers (rx_trace.cu). `ev` (optional): four events recorded before the walk
+// kernel, after it, after the visibility check and after the re-walk.
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                  uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
-                                 cudaStream_t s);
+                                 cudaStream_t s, const cudaEvent_t* ev = nullptr);
 cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                   unsigned long long* counters, cudaStream_t s);
+
+// Makes `dev` current for a scope and restores the caller's device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
 
 // A device allocation, released when its owner goes away (move-only).
 struct DevBuf {
@@ -96,6 +114,12 @@ struct rx_context {
   // staging ring for host-buffer calls
   rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
   size_t ring_chunk = 0;
+  // per-kernel timing of device-buffer closest-hit calls (rx_trace_set_timing)
+  std::vector<cudaEvent_t> timing_ev;  // 4 per recorded call
+  size_t timing_used = 0;
+  bool timing_on = false;
+  // learned guiding (rx_guide.cu)
+  rx::GuideState* guide = nullptr;
 
   rx_status build_scene();
   rx_status fail(rx_status s, const std::string& m) {

@@ -145,7 +145,7 @@ __device__ __forceinline__ int find_inside(const DevScene& S, F3 o, F3 d, int ex
 // BSDF and pdf queries
 // ---------------------------------------------------------------------------------------
 // The getBSDF of a non-medium object `obj` (camera, emitter, surface materials).
-__device__ F3 bsdf_surface(const DevScene& S, const CamDev& cam, int obj, const PV& in, const PV& out) {
+static __device__ F3 bsdf_surface(const DevScene& S, const CamDev& cam, int obj, const PV& in, const PV& out) {
   if (obj == kCameraObj) return {1, 1, 1};  // Camera::getBSDF
   const DevObject& ob = S.objects[obj];
   if (ob.material == kEmissive) {  // SceneEmissiveObject::getBSDF
@@ -174,7 +174,7 @@ __device__ F3 bsdf_surface(const DevScene& S, const CamDev& cam, int obj, const 
 // in.getBSDF(out): Ray::getBSDF (src/Ray.cpp:14-25) -> the out ray's contact (or inside)
 // object's getBSDF(in, out); a medium delegates to a contact surface
 // (SceneVPMObject::getBSDF).
-__device__ F3 bsdf_of(const DevScene& S, const CamDev& cam, const PV& in, const PV& out) {
+static __device__ F3 bsdf_of(const DevScene& S, const CamDev& cam, const PV& in, const PV& out) {
   int obj = out.contact != kNone ? out.contact : out.inside;
   if (obj == kNone) return {0, 0, 0};
   if (obj >= 0 && S.objects[obj].material == kVPM) {
@@ -188,7 +188,7 @@ __device__ F3 bsdf_of(const DevScene& S, const CamDev& cam, const PV& in, const 
 
 // The getDirectionSampleProbDensity of a non-medium object `obj`. `emitted`: the
 // reference's &inRay == &outRay case (a ray asked about itself: its emission pdf).
-__device__ float dir_pdf_surface(const DevScene& S, const CamDev& cam, int obj, const PV& in, const PV& out,
+static __device__ float dir_pdf_surface(const DevScene& S, const CamDev& cam, int obj, const PV& in, const PV& out,
                                  bool emitted) {
   if (obj == kCameraObj) return 1.0f;  // Camera::getDirectionSampleProbDensity
   const DevObject& ob = S.objects[obj];
@@ -216,7 +216,7 @@ __device__ float dir_pdf_surface(const DevScene& S, const CamDev& cam, int obj, 
 // in.getDirectionSampleProbDensity(out) (src/Ray.cpp:27-38) with the medium's
 // SceneVPMObject::getDirectionSampleProbDensity (delegation to a contact surface, else
 // albedo times the HG density).
-__device__ float dir_pdf(const DevScene& S, const CamDev& cam, const PV& in, const PV& out, bool emitted) {
+static __device__ float dir_pdf(const DevScene& S, const CamDev& cam, const PV& in, const PV& out, bool emitted) {
   int obj = out.contact != kNone ? out.contact : out.inside;
   if (obj == kNone) return 0.0f;
   if (obj >= 0 && S.objects[obj].material == kVPM) {
@@ -254,11 +254,11 @@ __device__ __forceinline__ float fresnel_er(float cur_n, float next_n, float ct,
   return (a * a + b * b) * 0.5f;
 }
 
-__device__ PV scatter_material(const DevScene& S, const CamDev& cam, int obj, const PV& in, Hit3 h,
+static __device__ PV scatter_material(const DevScene& S, const CamDev& cam, int obj, const PV& in, Hit3 h,
                                bool fix_is_light, bool russian, Rng& rng);
 
 // SceneVPMObject::scatter (src/SceneVPMObject.cpp:4-251)
-__device__ PV scatter_vpm(const DevScene& S, const CamDev& cam, int self, const PV& in, Hit3 h, bool fix_is_light,
+static __device__ PV scatter_vpm(const DevScene& S, const CamDev& cam, int self, const PV& in, Hit3 h, bool fix_is_light,
                           bool russian, Rng& rng) {
   const DevObject& ob = S.objects[self];
   if (h.obj < 0 || h.tri < 0) {  // nothing hit: the path ends (the reference reports an error)
@@ -405,7 +405,7 @@ __device__ PV scatter_vpm(const DevScene& S, const CamDev& cam, int self, const 
 // SceneObject::scatter with the object's material(s): Diffuse, Glossy, Phong (one lobe
 // picked uniformly, SceneObject.cpp:373-380), Refractive / Reflective, Emissive. A
 // medium object is not handled here (scatter_vpm).
-__device__ PV scatter_material(const DevScene& S, const CamDev& cam, int obj, const PV& in, Hit3 h,
+static __device__ PV scatter_material(const DevScene& S, const CamDev& cam, int obj, const PV& in, Hit3 h,
                                bool fix_is_light, bool russian, Rng& rng) {
   const DevObject& ob = S.objects[obj];
   F3 x = in.o + in.d * h.dist;
@@ -540,7 +540,7 @@ __device__ PV scatter_material(const DevScene& S, const CamDev& cam, int obj, co
 // The object's scatter: a medium's (SceneVPMObject::scatter); a dielectric the ray is
 // inside that hits another object hands the ray to that object
 // (RefractiveMaterial.cpp:183-187); else the object's material.
-__device__ PV scatter_object(const DevScene& S, const CamDev& cam, int obj, const PV& in, Hit3 h, bool fix_is_light,
+static __device__ PV scatter_object(const DevScene& S, const CamDev& cam, int obj, const PV& in, Hit3 h, bool fix_is_light,
                              bool russian, Rng& rng) {
   const DevObject& ob = S.objects[obj];
   if (ob.material == kVPM) return scatter_vpm(S, cam, obj, in, h, fix_is_light, russian, rng);
@@ -553,10 +553,8 @@ __device__ PV scatter_object(const DevScene& S, const CamDev& cam, int obj, cons
 // One scatter of MCRenderer::samplePathIter (src/MCRenderer.cpp:169-217): the inside
 // object scatters when there is one, else the intersected object; then the
 // shading-normal light-leak kill.
-__device__ PV scatter_step(const DevScene& S, const CamDev& cam, const PV& in, Hit3 h, bool fix_is_light, bool russian,
-                           Rng& rng) {
-  int obj = in.inside != kNone ? in.inside : h.obj;
-  PV o = scatter_object(S, cam, obj, in, h, fix_is_light, russian, rng);
+// The bounce loop's shading-normal light-leak kill (src/MCRenderer.cpp:183-217).
+__device__ __forceinline__ void leak_kill(const DevScene& S, const CamDev& cam, const PV& in, PV& o) {
   if (length(o.d) > 0.5f && o.inside == kNone && o.contact >= 0) {
     F3 ns = contact_normal(S, cam, o, false), nf = contact_normal(S, cam, o, true);
     F3 wi = -in.d;
@@ -565,13 +563,20 @@ __device__ PV scatter_step(const DevScene& S, const CamDev& cam, const PV& in, H
       o.c = {0, 0, 0};
     }
   }
+}
+
+static __device__ PV scatter_step(const DevScene& S, const CamDev& cam, const PV& in, Hit3 h, bool fix_is_light, bool russian,
+                           Rng& rng) {
+  int obj = in.inside != kNone ? in.inside : h.obj;
+  PV o = scatter_object(S, cam, obj, in, h, fix_is_light, russian, rng);
+  leak_kill(S, cam, in, o);
   return o;
 }
 
 // SceneObject::emit(isUniformOrigin = true, isUniformDir = false) through
 // Scene::SurfaceSampler (src/SceneObject.cpp:233-314, src/Scene.cpp:91-98): an emitter
 // triangle by area, a uniform point, a cosine direction; then its first hit.
-__device__ PV emit_ray(const DevScene& S, const CamDev& cam, Rng& rng, Hit3& hit) {
+static __device__ PV emit_ray(const DevScene& S, const CamDev& cam, Rng& rng, Hit3& hit) {
   float ru = rng.next() * S.light_area;
   int lo = 0, hi = (int)S.num_lights - 1;
   while (lo < hi) {

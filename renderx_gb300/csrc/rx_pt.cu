@@ -4,24 +4,20 @@
 // of MCRenderer::samplePathIter (src/MCRenderer.cpp:151-267).
 //
 // Stages per bounce, each a grid-stride kernel whose work count lives in device memory
-// (no host round trip inside a pass): extend (closest legal hit), shade (emission,
-// material scatter, next-event estimation with an inline shadow ray, Russian
-// roulette) with queue compaction by warp ballot + one atomic per warp. Film
-// accumulation is FP64.
+// (no host round trip inside a pass): extend (closest legal hit), shade (one scatter of
+// the reference's bounce loop through rx_material.cuh, emission, next-event estimation
+// with an inline shadow ray, Russian roulette) with queue compaction by warp ballot +
+// one atomic per warp. Film accumulation is FP64.
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
+#include "rx_guide.h"
 #include "rx_internal.h"
-#include "rx_pt.cuh"
+#include "rx_material.cuh"
+#include "rx_wavefront.h"
 
 namespace rx {
-
-struct CamDev {
-  F3 pos, front, right, up;
-  float sight;
-  int width, height;
-};
 
 struct PtParams {
   CamDev cam;
@@ -32,16 +28,7 @@ struct PtParams {
   uint32_t pixels;
   uint64_t path_base;
   uint32_t npaths;
-};
-
-// Path state, structure of arrays (one slot per live path).
-struct PathSoA {
-  float4* o;     // origin, w = pdf of the sampled direction (MIS)
-  float4* d;     // direction, w = unused
-  float4* T;     // throughput, w = unused
-  float4* L;     // accumulated radiance, w = unused
-  int4* info;    // pixel, contact object, inside object, depth | last-specular << 8
-  uint64_t* id;  // path id (random-number key)
+  uint32_t has_media;  // any medium object: camera rays look up their inside object
 };
 
 // -------------------------------------------------------------------------------------
@@ -52,7 +39,7 @@ __device__ __forceinline__ F3 camera_dir(const CamDev& c, float xp, float yp) {
   return normalize(c.front * c.sight + c.right * x + c.up * y);
 }
 
-__global__ void k_generate(PtParams P, PathSoA S, unsigned* count) {
+__global__ void k_generate(DevScene SC, PtParams P, PathSoA S, unsigned* count) {
   uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npaths; i += stride) {
     uint64_t pid = P.path_base + i;
@@ -68,11 +55,12 @@ __global__ void k_generate(PtParams P, PathSoA S, unsigned* count) {
       F3 dc = camera_dir(P.cam, x + 0.5f, y + 0.5f);
       w = fmaxf(fabsf(dot(P.cam.front, d)), 1e-6f) / fabsf(dot(dc, P.cam.front));
     }
+    int inside = P.has_media ? find_inside(SC, P.cam.pos, d, kNone) : kNone;
     S.o[i] = make_float4(P.cam.pos.x, P.cam.pos.y, P.cam.pos.z, 1.0f);
     S.d[i] = make_float4(d.x, d.y, d.z, 0.0f);
     S.T[i] = make_float4(w, w, w, 0.0f);
     S.L[i] = make_float4(0, 0, 0, 0);
-    S.info[i] = make_int4((int)pixel, -1, -1, 1 << 8);
+    S.info[i] = make_int4((int)pixel, kCameraObj, inside, 1 << 8);
     S.id[i] = pid;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = P.npaths;
@@ -85,212 +73,150 @@ __global__ void __launch_bounds__(128) k_extend(DevScene SC, PathSoA S, const un
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     float4 o = S.o[i], d = S.d[i];
     int4 inf = S.info[i];
-    bool camera = (inf.w & 255) == 0;
-    PHit h = trace_cond<false>(SC, f3(o), f3(d), INFINITY, camera ? -1 : inf.y, camera ? -1 : inf.z);
+    bool camera = (inf.w & 255) == 0;  // the camera ray's first query has no condition
+    PHit h = trace_cond<false>(SC, f3(o), f3(d), INFINITY, camera ? kNone : inf.y, camera ? kNone : inf.z);
     hit[i] = make_int2(h.tid, __float_as_int(h.t));
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
 }
 
-// -------------------------------------------------------------------------------------
-// Materials
-// -------------------------------------------------------------------------------------
-struct Scatter {
-  F3 dir, color;
-  float prob;
-  bool definite;  // Ray::DEFINITE (specular / pass-through)
-  bool killed;    // direction of length 0: the path ends here
-  int inside, contact;
-};
-
-__device__ __forceinline__ F3 refl(F3 n, F3 d) { return n * (-dot(n, d) * 2.0f) + d; }
-
-// DiffuseMaterial::scatter, src/DiffuseMaterial.cpp:4-77
-__device__ Scatter scatter_diffuse(F3 color, F3 n, F3 din, int obj, int inside, bool russian, Rng& rng) {
-  Scatter s;
-  s.inside = inside;
-  s.contact = obj;
-  s.killed = false;
-  if (dot(din, n) > 0.0f) {  // leaving: pass through
-    s.dir = din;
-    s.color = {1, 1, 1};
-    s.prob = 1.0f;
-    s.definite = true;
-    return s;
-  }
-  Frame f = frame_from(n);
-  float r1 = rng.next(), r2 = rng.next();
-  s.dir = to_world(f, hemi_cos(1.0f, r1, r2));
-  float p = maxc(color);
-  s.definite = false;
-  if (!russian || rng.next() < p) {
-    bool ok = dot(n, din) <= 0.0f && dot(n, s.dir) >= 0.0f;  // DiffuseBSDF::evaluate
-    s.color = ok ? color * (1.0f / RX_PI) : F3{0, 0, 0};
-    float pdf = cos_lobe_pdf(n, s.dir, 1.0f);
-    s.prob = russian ? p * pdf : pdf;
-  } else {
-    s.dir = {0, 0, 0};
-    s.color = {0, 0, 0};
-    s.prob = 1.0f - p;
-    s.killed = true;
-  }
-  return s;
-}
-
-// GlossyMaterial::scatter, src/GlossyMaterial.cpp:4-57 (Phong lobe, no (n+2)/2pi
-// normalisation, GlossyBSDF.h:24-33)
-__device__ Scatter scatter_glossy(F3 color, float coeff, F3 n, F3 din, int obj, int inside, bool russian, Rng& rng) {
-  Scatter s;
-  s.inside = inside;
-  s.contact = obj;
-  s.definite = false;
-  s.killed = false;
-  F3 r = refl(n, din);
-  Frame f = frame_from(r);
-  float r1 = rng.next(), r2 = rng.next();
-  s.dir = to_world(f, hemi_cos(coeff, r1, r2));
-  F3 c = {0, 0, 0};
-  if (dot(n, din) <= 0.0f && dot(n, s.dir) >= 0.0f) {
-    float rw = dot(r, s.dir);
-    if (rw > 0.0f) c = color * powf(rw, coeff);
-  }
-  s.color = c;
-  s.prob = cos_lobe_pdf(r, s.dir, coeff);
-  float p = maxc(color);
-  if (c.x == 0.0f && c.y == 0.0f && c.z == 0.0f) {
-    s.dir = {0, 0, 0};
-    s.prob = 1.0f;
-    s.killed = true;
-    return s;
-  }
-  if (!russian) return s;
-  if (rng.next() < p) {
-    s.prob *= p;
-  } else {
-    s.dir = {0, 0, 0};
-    s.color = {0, 0, 0};
-    s.prob = 1.0f - p;
-    s.killed = true;
-  }
-  return s;
-}
-
-// RefractiveMaterial::scatter, src/RefractiveMaterial.cpp:132-269: unpolarised Fresnel
-// choice between mirror reflection and Snell refraction (rotMat(n x d, phi) * n is the
-// rotation of n toward d by phi), total internal reflection ends the path, the
-// (n_i/n_t)^2 radiance scaling on eye paths. cos_out: |n . dir| as
-// Ray::getCosineTerm, clamped at 1e-6.
-__device__ Scatter scatter_refractive(F3 surf, float ior, F3 n, F3 din, int obj, int inside, float cur_n, float next_n,
-                                      int outside, bool light_path, Rng& rng) {
-  Scatter s;
-  s.contact = obj;
-  s.definite = true;
-  s.killed = false;
-  s.inside = inside;
-  F3 r = refl(n, din);
-  if (ior < 0.0f) {  // mirror (SceneReflectiveObject)
-    s.dir = r;
-    s.prob = 1.0f;
-    s.color = surf * (1.0f / fmaxf(fabsf(dot(n, r)), 1e-6f));
-    return s;
-  }
-  float cd = fminf(fmaxf(dot(din, n), -1.0f), 1.0f);
-  float theta = acosf(cd);
-  float sin_phi = cur_n / next_n * sinf(theta);
-  if (sin_phi >= 1.0f) {  // total internal reflection kills the path
-    s.dir = {0, 0, 0};
-    s.color = {0, 0, 0};
-    s.prob = 1.0f;
-    s.killed = true;
-    s.contact = -1;
-    return s;
-  }
-  float phi = asinf(sin_phi);
-  if (theta > RX_PI * 0.5f) phi = RX_PI - phi;
-  F3 tp = normalize(din - n * cd);
-  float sp, cp;
-  sincosf(phi, &sp, &cp);
-  F3 wt = normalize(n * cp + tp * sp);
-  float ct = fabsf(cosf(theta)), cph = fabsf(cp);
-  float a = fabsf(cur_n * ct - next_n * cph) / (cur_n * ct + next_n * cph);
-  float b = fabsf(next_n * ct - cur_n * cph) / (next_n * ct + cur_n * cph);
-  float er = (a * a + b * b) * 0.5f;
-  float p = fminf(fmaxf(er, 0.0f), 1.0f);
-  if (rng.next() < p) {
-    s.dir = normalize(r);
-    s.color = surf * (er / fmaxf(fabsf(dot(n, r)), 1e-6f));
-    s.prob = p;
-  } else {
-    F3 c = surf;
-    if (!light_path) c = c * ((cur_n * cur_n) / (next_n * next_n));
-    s.color = c * ((1.0f - er) / fmaxf(fabsf(dot(n, wt)), 1e-6f));
-    s.prob = 1.0f - p;
-    s.inside = outside;
-    s.dir = wt;
-  }
-  return s;
-}
-
-// BSDF value and sampling pdf for a connection (SceneObject::getBSDF sums the
-// materials, getDirectionSampleProbDensity averages them; SceneObject.cpp:323-359).
-// Glossy's getBSDF carries an extra factor max(colour) (GlossyMaterial.cpp:207-217);
-// diffuse's pdf includes its roulette factor (DiffuseMaterial.cpp:79-87).
-__device__ void bsdf_eval(const DevObject& ob, F3 n, F3 din, F3 wo, F3& f, float& pdf) {
-  f = {0, 0, 0};
-  pdf = 0.0f;
-  bool front = dot(n, din) <= 0.0f && dot(n, wo) >= 0.0f;
-  int nm = 0;
-  if (ob.material == kDiffuse || ob.material == kPhong) {
-    F3 c = ob.material == kPhong ? f3v(ob.diffuse_color) : f3v(ob.color);
-    if (front) f = f + c * (1.0f / RX_PI);
-    pdf += maxc(c) * cos_lobe_pdf(n, wo, 1.0f);
-    nm++;
-  }
-  if (ob.material == kGlossy || ob.material == kPhong) {
-    F3 c = f3v(ob.color);
-    F3 r = refl(n, din);
-    if (front) {
-      float rw = dot(r, wo);
-      if (rw > 0.0f) f = f + c * (maxc(c) * powf(rw, ob.coeff));
-    }
-    pdf += cos_lobe_pdf(r, wo, ob.coeff);
-    nm++;
-  }
-  if (nm > 1) pdf /= (float)nm;
-}
-
-// -------------------------------------------------------------------------------------
-// Shade: one bounce of MCRenderer::samplePathIter plus the estimator's bookkeeping.
-// -------------------------------------------------------------------------------------
 __device__ __forceinline__ void film_add(double* sum, double* sq, int pixel, F3 L) {
   double* s = sum + 3 * (size_t)pixel;
-  double* q = sq + 3 * (size_t)pixel;
   atomicAdd(s, (double)L.x);
   atomicAdd(s + 1, (double)L.y);
   atomicAdd(s + 2, (double)L.z);
-  if (q) {
+  if (sq) {
+    double* q = sq + 3 * (size_t)pixel;
     atomicAdd(q, (double)L.x * L.x);
     atomicAdd(q + 1, (double)L.y * L.y);
     atomicAdd(q + 2, (double)L.z * L.z);
   }
 }
 
-__device__ __forceinline__ F3 decay_of(const DevScene& SC, int inside, float t) {
-  if (inside < 0) return {1, 1, 1};
-  const DevObject& ob = SC.objects[inside];
-  if (ob.material == kRefractive) {  // RefractiveMaterial::getRadianceDecay: decay^dist
-    return {powf(ob.decay[0], t), powf(ob.decay[1], t), powf(ob.decay[2], t)};
+// PathTracerTest::colorByConnectingLights (src/PathTracerTest.cpp:88-136) at vertex `v`
+// (the ray leaving it), reached by `in`: a light point by area, two-sided emission,
+// balance-heuristic weight against the BSDF's sampling pdf.
+__device__ F3 connect_light(const DevScene& SC, const CamDev& cam, const PV& in, const PV& v, Rng& rng,
+                            unsigned& shadows) {
+  float ru = rng.next() * SC.light_area;
+  int lo = 0, hi = (int)SC.num_lights - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(&SC.light_cdf[mid]) < ru) lo = mid + 1;
+    else hi = mid;
   }
-  if (ob.material == kVPM) {  // SceneVPMObject: exp(-sigma_t d) per channel
-    return {expf(-(ob.sigma_s[0] + ob.sigma_a[0]) * t), expf(-(ob.sigma_s[1] + ob.sigma_a[1]) * t),
-            expf(-(ob.sigma_s[2] + ob.sigma_a[2]) * t)};
-  }
-  return {1, 1, 1};
+  int lt = (int)__ldg(&SC.light_tri[lo]);
+  TriGeom lg = tri_geom(SC, lt);
+  float u1 = rng.next(), u2 = rng.next();
+  float su1 = sqrtf(u1);
+  float bu = 1.0f - su1, bv = u2 * su1;
+  F3 xl = lg.v0 * bu + lg.v1 * bv + lg.v2 * (1.0f - bu - bv);
+  F3 ld = v.o - xl;
+  float dist = length(ld);
+  ld = ld * (1.0f / dist);
+  PV out = v;
+  out.d = -ld;
+  F3 f = bsdf_of(SC, cam, in, out);
+  if (lum(f) < 1e-7f) return {0, 0, 0};
+  F3 nl = world_normal(lg, SC.objects[lg.obj].has_normals, xl);
+  float cos_l = fminf(fabsf(dot(nl, ld)), 1.0f);
+  if (cos_l < 1e-6f) return {0, 0, 0};
+  float cos_s = 1.0f;
+  if (v.contact != kNone) cos_s = fminf(fabsf(dot(contact_normal(SC, cam, v), out.d)), 1.0f);
+  float bpdf = dir_pdf(SC, cam, in, out, false);
+  shadows++;
+  PHit sh = trace_cond<true>(SC, v.o, out.d, dist - 1e-5f, v.contact, v.inside);  // testVisibility
+  if (sh.tid >= 0) return {0, 0, 0};
+  float pdfa = 1.0f / SC.light_area;
+  float pdfw = pdfa * dist * dist / cos_l;
+  float mis = pdfw / (pdfw + bpdf);
+  return f3v(SC.objects[lg.obj].color) * f * (cos_l * cos_s / (pdfa * dist * dist) * mis);
 }
 
+// Guided sampling state of a wavefront (all null / zero when guiding is off).
+struct GuideIO {
+  float* lobes;        // per live path: guide::kLobeStride floats, lobes[0] < 0 = not guided
+  float frac;          // one-sample MIS: probability of sampling the BSDF
+  float* recs;         // training records (guide::kRec floats) or null
+  unsigned* rec_count;
+  uint32_t rec_cap;
+  float4* lpath;       // radiance of each pass-local path at its end (training) or null
+};
+
+// The diffuse / glossy / Phong scatter of the eye path with its direction drawn by
+// one-sample MIS: from the material's own lobe with probability `frac`, else from the
+// guiding mixture G; the sampling density is the mixture of both. Russian roulette,
+// the Phong lobe choice and the BSDF values are the plain scatter's, so the estimator's
+// expectation is unchanged.
+static __device__ PV scatter_guided(const DevScene& S, const PV& in, Hit3 h, bool russian, Rng& rng, const float* G,
+                                    float frac) {
+  const DevObject& ob = S.objects[h.obj];
+  F3 x = in.o + in.d * h.dist;
+  PV o = pv_term(x);
+  o.pixel = in.pixel;
+  o.contact = h.obj;
+  o.ctri = h.tri;
+  o.inside = in.inside;
+  TriGeom g = tri_geom(S, h.tri);
+  F3 n = world_normal(g, S.objects[g.obj].has_normals, x);
+  uint32_t kind = ob.material;
+  if (kind == kPhong) kind = rng.next() < 0.5f ? kGlossy : kDiffuse;
+  bool from_bsdf = rng.next() < frac;
+  float u0 = rng.next(), u1 = rng.next(), u2 = rng.next();
+  o.flags = kDirRandom;
+  if (kind == kDiffuse) {
+    F3 c = ob.material == kPhong ? f3v(ob.diffuse_color) : f3v(ob.color);
+    if (dot(in.d, n) > 0.0f) {  // leaving: pass through (not guided)
+      o.d = in.d;
+      o.c = {1, 1, 1};
+      o.dprob = 1.0f;
+      o.flags = 0;
+      return o;
+    }
+    F3 w = from_bsdf ? to_world(frame_from(n), hemi_cos(1.0f, u1, u2)) : guide::mix_sample(G, u0, u1, u2);
+    float p = maxc(c);
+    if (russian && rng.next() >= p) {
+      o.dprob = 1.0f - p;
+      return o;  // d = 0, c = 0: the path ends
+    }
+    float pdf = frac * cos_lobe_pdf(n, w, 1.0f) + (1.0f - frac) * guide::mix_pdf(G, w);
+    bool front = dot(n, in.d) <= 0.0f && dot(n, w) >= 0.0f;
+    if (!front || !(pdf > 0.0f)) return o;  // no contribution: end
+    o.d = w;
+    o.c = c * (1.0f / RX_PI);
+    o.dprob = (russian ? p : 1.0f) * pdf;
+    return o;
+  }
+  F3 c = f3v(ob.color);
+  F3 r = n * (-dot(n, in.d) * 2.0f) + in.d;
+  F3 w = from_bsdf ? to_world(frame_from(r), hemi_cos(ob.coeff, u1, u2)) : guide::mix_sample(G, u0, u1, u2);
+  F3 val = {0, 0, 0};
+  if (dot(n, in.d) <= 0.0f && dot(n, w) >= 0.0f) {
+    float rw = dot(r, w);
+    if (rw > 0.0f) val = c * powf(rw, ob.coeff);
+  }
+  float pdf = frac * cos_lobe_pdf(r, w, ob.coeff) + (1.0f - frac) * guide::mix_pdf(G, w);
+  if ((val.x == 0.0f && val.y == 0.0f && val.z == 0.0f) || !(pdf > 0.0f)) return o;
+  o.d = w;
+  o.c = val;
+  o.dprob = pdf;
+  if (russian) {
+    float p = maxc(c);
+    if (rng.next() < p) {
+      o.dprob *= p;
+    } else {
+      o.d = {0, 0, 0};
+      o.c = {0, 0, 0};
+      o.dprob = 1.0f - p;
+    }
+  }
+  return o;
+}
+
+// One bounce of MCRenderer::samplePathIter plus the estimator's bookkeeping.
 __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA S, const unsigned* count,
                                                const int2* hit, PathSoA N, unsigned* next_count, double* film_sum,
-                                               double* film_sq, unsigned long long* shadow_rays) {
+                                               double* film_sq, unsigned long long* shadow_rays, GuideIO G) {
   uint32_t n = *count;
   uint32_t stride = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
@@ -299,144 +225,97 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
   uint32_t nwarp_iter = (n + stride - 1) / stride;
   for (uint32_t it = 0; it < nwarp_iter; it++) {
     uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = i < n, cont = false;
-    float4 o4, d4, T4, L4;
-    int4 inf;
-    F3 xo{}, wo{}, T{}, L{};
-    float pdf_out = 1.0f;
-    int contact_out = -1, inside_out = -1, depth = 0;
-    bool spec_out = true;
+    bool cont = false;
+    PV nx;
+    F3 T{}, L{}, Tb{};
+    int4 inf{};
     uint64_t pid = 0;
-    if (live) {
-      o4 = S.o[i];
-      d4 = S.d[i];
-      T4 = S.T[i];
-      L4 = S.L[i];
+    int depth = 0;
+    bool rec = false;  // a guided vertex whose path continues: a training record
+    if (i < n) {
+      float4 o4 = S.o[i], d4 = S.d[i], T4 = S.T[i], L4 = S.L[i];
       inf = S.info[i];
       pid = S.id[i];
       depth = inf.w & 255;
       bool last_spec = (inf.w >> 8) & 1;
-      int inside = inf.z;
       T = f3(T4);
       L = f3(L4);
-      F3 o = f3(o4), d = f3(d4);
+      PV cur = pv_term(f3(o4));
+      cur.d = f3(d4);
+      cur.contact = inf.y;
+      cur.inside = inf.z;
+      cur.pixel = inf.x;
+      cur.flags = (depth == 0 || !last_spec) ? kDirRandom : 0u;  // the camera ray is RANDOM
       int2 h = hit[i];
       Rng rng(P.seed, pid, 16u + 32u * (uint32_t)depth);
       bool done = true;
-      if (h.x >= 0) {
-        float t = __int_as_float(h.y);
-        F3 x = o + d * t;
-        TriGeom g = tri_geom(SC, h.x);
-        int hit_obj = g.obj;
-        F3 dec = decay_of(SC, inside, t);
-        if (!P.nee) T = T * dec;
-        int sobj = inside >= 0 ? inside : hit_obj;  // samplePathIter: the inside object scatters
-        const DevObject& ob = SC.objects[sobj];
-        const DevObject& hob = SC.objects[hit_obj];
-        if (ob.material == kEmissive) {
-          F3 fn = world_normal(g, ob.has_normals, x);
-          F3 Le = f3v(ob.color);
-          if (!P.nee) {
-            // SceneEmissiveObject::scatter: emitted only toward the front
-            if (dot(d, fn) <= 0.0f) L = L + T * Le;
-          } else {
-            // PathTracerTest.cpp:37-56: two-sided, MIS against light sampling
-            float mis = 1.0f;
-            if (depth > 0 && !last_spec) {
-              float cosine = dot(fn, -d);
-              float pdfw = (1.0f / SC.light_area) * t * t / fabsf(cosine);
-              mis = o4.w / (o4.w + pdfw);
-            }
-            L = L + T * Le * mis;
-          }
+      if (h.x >= 0) {  // a ray that hits nothing ends the path (samplePathIter's termRay)
+        Hit3 hh{(int)__ldg(&SC.tri_obj[h.x]), h.x, __int_as_float(h.y)};
+        bool russian = P.rr_mode == 0 || depth >= 3;
+        bool guided = G.lobes && !P.nee && __ldg(&G.lobes[(size_t)i * guide::kLobeStride]) >= 0.0f;
+        if (guided) {
+          nx = scatter_guided(SC, cur, hh, russian, rng, G.lobes + (size_t)i * guide::kLobeStride, G.frac);
+          leak_kill(SC, P.cam, cur, nx);
         } else {
-          F3 ns = world_normal(g, hob.has_normals, x);  // shading normal at the hit
-          bool russian = P.rr_mode == 0 || depth >= 3;
-          Scatter sc;
-          uint32_t kind = ob.material;
-          if (kind == kPhong) kind = rng.next() < 0.5f ? kGlossy : kDiffuse;  // rand()%2, SceneObject.cpp:373-380
-          if (kind == kDiffuse) {
-            F3 c = ob.material == kPhong ? f3v(ob.diffuse_color) : f3v(ob.color);
-            sc = scatter_diffuse(c, ns, d, sobj, inside, russian, rng);
-          } else if (kind == kGlossy) {
-            sc = scatter_glossy(f3v(ob.color), ob.coeff, ns, d, sobj, inside, russian, rng);
-          } else {
-            // refractive / reflective / medium boundary
-            bool going_out = inside == sobj;
-            int outside = going_out ? -1 : sobj;  // findInsideObject: no enclosing volume
-            float cur_n = inside >= 0 ? fabsf(SC.objects[inside].ior) : 1.0f;
-            if (inside >= 0 && SC.objects[inside].material != kRefractive && SC.objects[inside].material != kVPM)
-              cur_n = 1.0f;
-            float next_n = outside >= 0 ? fabsf(SC.objects[outside].ior) : 1.0f;
-            sc = scatter_refractive(f3v(ob.color), ob.material == kReflective ? -1.0f : ob.ior, ns, d, sobj, inside,
-                                    cur_n, next_n, outside, false, rng);
+          nx = scatter_step(SC, P.cam, cur, hh, false, russian, rng);
+        }
+        float dist = length(nx.o - cur.o);
+        bool killed = length(nx.d) < 0.5f;
+        bool capped = !killed && depth + 1 > (int)P.max_depth;
+        if (!P.nee) {
+          // PathTracer.cpp:48-60: colour/directionProb/originProb of every ray, cosine
+          // and transmittance of every ray but the last
+          T = T * decay_of(SC, cur.inside, dist);
+          Tb = T;
+          T = T * (nx.c * (1.0f / (nx.dprob * nx.oprob)));
+          if (killed && is_emissive(SC, nx.contact)) L = L + T;
+          if (!killed && !capped) {
+            T = T * cos_term(SC, P.cam, nx);
+            done = false;
+            rec = guided && G.recs;
           }
-          // shading-normal light-leak kill, MCRenderer.cpp:183-217
-          if (!sc.killed && sc.inside < 0 && sc.contact >= 0) {
-            F3 fl = world_normal(g, hob.has_normals, x, true);
-            F3 wi = -d;
-            if (dot(ns, wi) * dot(fl, wi) <= 0.0f || dot(ns, sc.dir) * dot(fl, sc.dir) <= 0.0f) {
-              sc.dir = {0, 0, 0};
-              sc.color = {0, 0, 0};
-              sc.killed = true;
-            }
+        } else if (is_emissive(SC, nx.contact)) {
+          // PathTracerTest.cpp:37-56: two-sided emission, MIS against light sampling
+          float mis = 1.0f;
+          if (depth > 0 && !last_spec) {
+            float cosine = dot(contact_normal(SC, P.cam, nx), -cur.d);
+            float pdfw = (1.0f / SC.light_area) * dist * dist / fabsf(cosine);
+            mis = o4.w / (o4.w + pdfw);
           }
-          bool capped = !sc.killed && depth + 1 > (int)P.max_depth;
-          if (P.nee && !sc.definite && !capped && SC.num_lights > 0) {
-            // PathTracerTest::colorByConnectingLights, PathTracerTest.cpp:88-136
-            float ru = rng.next() * SC.light_area;
-            int lo = 0, hi = (int)SC.num_lights - 1;
-            while (lo < hi) {
-              int mid = (lo + hi) >> 1;
-              if (__ldg(&SC.light_cdf[mid]) < ru) lo = mid + 1;
-              else hi = mid;
-            }
-            int lt = (int)__ldg(&SC.light_tri[lo]);
-            TriGeom lg = tri_geom(SC, lt);
-            float u1 = rng.next(), u2 = rng.next();
-            float su1 = sqrtf(u1);
-            float bu = 1.0f - su1, bv = u2 * su1;
-            F3 xl = lg.v0 * bu + lg.v1 * bv + lg.v2 * (1.0f - bu - bv);
-            F3 ld = x - xl;
-            float dist = length(ld);
-            ld = ld * (1.0f / dist);
-            F3 wl = -ld;
-            F3 f;
-            float bpdf;
-            bsdf_eval(ob, ns, d, wl, f, bpdf);
-            F3 nl = world_normal(lg, SC.objects[lg.obj].has_normals, xl);
-            float cos_l = fminf(fabsf(dot(nl, ld)), 1.0f);
-            if (lum(f) >= 1e-7f && cos_l >= 1e-6f) {
-              shadows++;
-              PHit sh = trace_cond<true>(SC, x, wl, dist - 1e-5f, sc.contact, sc.inside);
-              if (sh.tid < 0) {
-                float cos_s = fminf(fabsf(dot(ns, wl)), 1.0f);
-                float pdfa = 1.0f / SC.light_area;
-                float pdfw = pdfa * dist * dist / cos_l;
-                float mis = pdfw / (pdfw + bpdf);
-                F3 Le = f3v(SC.objects[lg.obj].color);
-                L = L + T * Le * f * (cos_l * cos_s / (pdfa * dist * dist) * mis);
-              }
-            }
-          }
-          if (!sc.killed && !capped) {
-            float cos_o = fmaxf(fabsf(dot(ns, sc.dir)), 1e-6f);  // Ray::getCosineTerm
-            T = T * sc.color * (cos_o / sc.prob);
-            if (P.nee) T = T * dec;  // PathTracerTest applies the previous segment's decay here
-            xo = x;
-            wo = sc.dir;
-            pdf_out = sc.prob;
-            spec_out = sc.definite;
-            contact_out = sc.contact;
-            inside_out = sc.inside;
+          L = L + T * f3v(SC.objects[nx.contact].color) * mis;
+        } else if (!capped) {
+          if ((nx.flags & kDirRandom) && SC.num_lights > 0) L = L + T * connect_light(SC, P.cam, cur, nx, rng, shadows);
+          if (!killed) {
+            T = T * (nx.c * (cos_term(SC, P.cam, nx) / nx.dprob));
+            T = T * decay_of(SC, cur.inside, fmaxf(dist, 1e-5f));
             done = false;
           }
         }
       }
       if (done) {
         if (L.x != 0.0f || L.y != 0.0f || L.z != 0.0f) film_add(film_sum, film_sq, inf.x, L);
+        if (G.lpath) G.lpath[pid - P.path_base] = make_float4(L.x, L.y, L.z, 0.0f);
       } else {
         cont = true;
+      }
+    }
+    // training record: position, shading normal, outgoing and incident directions,
+    // throughput before this vertex, pass-local path index (weights follow the pass)
+    unsigned rm = __ballot_sync(0xffffffffu, rec);
+    if (rm) {
+      unsigned rb = 0;
+      int leader = __ffs(rm) - 1;
+      if (lane == leader) rb = atomicAdd(G.rec_count, (unsigned)__popc(rm));
+      rb = __shfl_sync(0xffffffffu, rb, leader);
+      uint32_t j = rb + __popc(rm & ((1u << lane) - 1));
+      if (rec && j < G.rec_cap) {
+        F3 ns = contact_normal(SC, P.cam, nx);
+        float4* r = reinterpret_cast<float4*>(G.recs + (size_t)j * guide::kRec);
+        float4 d4 = S.d[i];
+        r[0] = make_float4(nx.o.x, nx.o.y, nx.o.z, ns.x);
+        r[1] = make_float4(ns.y, ns.z, -d4.x, -d4.y);
+        r[2] = make_float4(-d4.z, nx.d.x, nx.d.y, nx.d.z);
+        r[3] = make_float4(Tb.x, Tb.y, Tb.z, __uint_as_float((uint32_t)(pid - P.path_base)));
       }
     }
     // compaction: warp ballot, one atomic per warp
@@ -448,11 +327,12 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
       base = __shfl_sync(0xffffffffu, base, leader);
       if (cont) {
         uint32_t j = base + __popc(m & ((1u << lane) - 1));
-        N.o[j] = make_float4(xo.x, xo.y, xo.z, pdf_out);
-        N.d[j] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+        N.o[j] = make_float4(nx.o.x, nx.o.y, nx.o.z, nx.dprob);
+        N.d[j] = make_float4(nx.d.x, nx.d.y, nx.d.z, 0.0f);
         N.T[j] = make_float4(T.x, T.y, T.z, 0.0f);
         N.L[j] = make_float4(L.x, L.y, L.z, 0.0f);
-        N.info[j] = make_int4(inf.x, contact_out, inside_out, (depth + 1) | ((spec_out ? 1 : 0) << 8));
+        N.info[j] = make_int4(inf.x, nx.contact, nx.inside,
+                              (depth + 1) | (((nx.flags & kDirRandom) ? 0 : 1) << 8));
         N.id[j] = pid;
       }
     }
@@ -462,6 +342,48 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
 }
 
 __global__ void k_zero(unsigned* p) { *p = 0; }
+
+// Training samples of a finished pass: each record's weight is the luminance of its
+// path's final radiance over the throughput before the vertex, i.e. (BSDF x cosine x
+// incident radiance) / (sampling density) at the vertex. Records with a positive weight
+// are compacted into `out` (x, n, wo, wi, weight, 0, 0, 0).
+__global__ void k_record_weights(const float* recs, const unsigned* count, uint32_t cap, const float4* lpath,
+                                 float* out, unsigned* out_count) {
+  uint32_t n = min(*count, cap);
+  const int lane = threadIdx.x & 31;
+  uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t iters = (n + stride - 1) / stride;
+  for (uint32_t it = 0; it < iters; it++) {
+    uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    float4 a{}, b{}, c{}, d{};
+    float w = 0.0f;
+    if (i < n) {
+      const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * guide::kRec);
+      a = r[0];
+      b = r[1];
+      c = r[2];
+      d = r[3];
+      float4 L = lpath[__float_as_uint(d.w)];
+      F3 q{d.x > 0.0f ? L.x / d.x : 0.0f, d.y > 0.0f ? L.y / d.y : 0.0f, d.z > 0.0f ? L.z / d.z : 0.0f};
+      w = lum(q);
+      if (!(w < 1e30f)) w = 0.0f;
+    }
+    bool keep = w > 0.0f;
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) continue;
+    unsigned base = 0;
+    int leader = __ffs(m) - 1;
+    if (lane == leader) base = atomicAdd(out_count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (keep) {
+      float4* o = reinterpret_cast<float4*>(out + (size_t)(base + __popc(m & ((1u << lane) - 1))) * guide::kRec);
+      o[0] = a;
+      o[1] = b;
+      o[2] = c;
+      o[3] = make_float4(w, 0.0f, 0.0f, 0.0f);
+    }
+  }
+}
 
 // -------------------------------------------------------------------------------------
 // Host driver
@@ -501,6 +423,7 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
   P.rr_mode = opt.rr_mode;
   P.nee = opt.nee;
   P.pixels = cam.width * cam.height;
+  for (uint32_t o = 0; o < (uint32_t)c->objects.size(); o++) P.has_media |= c->objects[o].material == RX_MAT_VPM;
   uint64_t total = (uint64_t)P.pixels * opt.spp;
   uint32_t per_pass = opt.paths_per_pass ? opt.paths_per_pass : (1u << 21);
   per_pass = (uint32_t)std::min<uint64_t>(per_pass, total);
@@ -520,25 +443,71 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
   unsigned* cnt = reinterpret_cast<unsigned*>(ctr + 8);            // two queue counts
   cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
 
+  // guiding: mixture per live path, training records, per-path final radiance
+  const bool guided = (opt.flags & RX_PT_GUIDED) && guide_ready(c->guide) && !opt.nee;
+  GuideIO G{};
+  float* train = nullptr;
+  unsigned* rcnt = nullptr;
+  uint32_t cap = 0;
+  if (guided) {
+    cap = (uint32_t)std::min<uint64_t>((uint64_t)per_pass * 4, 1u << 22);
+    bufs.emplace_back();
+    if ((e = bufs.back().alloc((size_t)per_pass * guide::kLobeStride * sizeof(float))) != cudaSuccess) return e;
+    G.lobes = bufs.back().as<float>();
+    G.frac = guide_bsdf_fraction(c->guide);
+    if (guide_train_passes(c->guide) > 0) {
+      bufs.emplace_back();
+      if ((e = bufs.back().alloc((size_t)cap * guide::kRec * sizeof(float))) != cudaSuccess) return e;
+      G.recs = bufs.back().as<float>();
+      bufs.emplace_back();
+      if ((e = bufs.back().alloc((size_t)cap * guide::kRec * sizeof(float))) != cudaSuccess) return e;
+      train = bufs.back().as<float>();
+      bufs.emplace_back();
+      if ((e = bufs.back().alloc((size_t)per_pass * sizeof(float4))) != cudaSuccess) return e;
+      G.lpath = bufs.back().as<float4>();
+      rcnt = cnt + 2;  // [2] records, [3] weighted records
+      G.rec_count = rcnt;
+      G.rec_cap = cap;
+    }
+  }
+
   int grid = c->trace_cfg.sms * 8;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  for (uint64_t base = 0; base < total; base += per_pass) {
+  uint32_t pass = 0;
+  for (uint64_t base = 0; base < total; base += per_pass, pass++) {
     P.path_base = base;
     P.npaths = (uint32_t)std::min<uint64_t>(per_pass, total - base);
     PathSoA* cur = &A;
     PathSoA* nxt = &B;
     unsigned* ccur = cnt;
     unsigned* cnxt = cnt + 1;
-    k_generate<<<grid, 256, 0, s>>>(P, *cur, ccur);
+    GuideIO Gp = G;
+    const bool training = guided && G.recs && pass < guide_train_passes(c->guide);
+    if (!training) {
+      Gp.recs = nullptr;
+      Gp.lpath = nullptr;
+    } else {
+      cudaMemsetAsync(rcnt, 0, 2 * sizeof(unsigned), s);
+      cudaMemsetAsync(G.lpath, 0, (size_t)P.npaths * sizeof(float4), s);
+    }
+    k_generate<<<grid, 256, 0, s>>>(SC, P, *cur, ccur);
     for (uint32_t depth = 0; depth <= opt.max_depth; depth++) {
       k_extend<<<grid, 128, 0, s>>>(SC, *cur, ccur, hit, ctr);
+      if (guided && (e = guide_infer_paths(c->guide, SC, *cur, ccur, hit, G.lobes, 2 * c->trace_cfg.sms, s)) !=
+                        cudaSuccess)
+        return e;
       k_zero<<<1, 1, 0, s>>>(cnxt);
-      k_shade<<<grid, 128, 0, s>>>(SC, P, *cur, ccur, hit, *nxt, cnxt, film_sum, film_sq, ctr + 1);
+      k_shade<<<grid, 128, 0, s>>>(SC, P, *cur, ccur, hit, *nxt, cnxt, film_sum, film_sq, ctr + 1, Gp);
       std::swap(cur, nxt);
       std::swap(ccur, cnxt);
+    }
+    if (training) {
+      k_record_weights<<<grid, 128, 0, s>>>(G.recs, rcnt, cap, G.lpath, train, rcnt + 1);
+      if ((e = guide_train_records(c->guide, train, rcnt + 1, cap, (int)guide_steps_per_pass(c->guide), s)) != cudaSuccess)
+        return e;
     }
   }
   cudaEventRecord(e1, s);

@@ -305,15 +305,16 @@ __global__ void __launch_bounds__(128) k_trace_reforder(DevAccel A, const rx_ray
 
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                  uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, const cudaEvent_t* ev) {
   if (n == 0) return cudaSuccess;
   cudaMemsetAsync(counters, 0, sizeof(unsigned long long), s);  // eager queue length
   uint32_t* hit_leaf = queue;  // scratch: n entries of winners' reference leaves
   uint32_t* eager = queue + n;  // then up to n queued rays
+  if (cfg.variant != 0) cudaMemsetAsync(counters + 4, 0, sizeof(unsigned long long), s);  // batch cursor
+  if (ev) cudaEventRecord(ev[0], s);
   if (cfg.variant == 0) {
     k_trace_closest<<<(n + 127) / 128, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
   } else {
-    cudaMemsetAsync(counters + 4, 0, sizeof(unsigned long long), s);  // batch cursor
     unsigned blocks = (unsigned)cfg.sms * (unsigned)cfg.blocks_per_sm;
     unsigned need = (n + 127) / 128;
     blocks = blocks < need ? blocks : need;
@@ -322,8 +323,11 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     else
       k_trace_persistent<true><<<blocks, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
   }
+  if (ev) cudaEventRecord(ev[1], s);
   k_check_visible<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, hit_leaf, eager, counters);
+  if (ev) cudaEventRecord(ev[2], s);
   k_trace_eager<<<cfg.sms, 128, 0, s>>>(A, rays, tid, dist, eager, counters);
+  if (ev) cudaEventRecord(ev[3], s);
   return cudaGetLastError();
 }
 

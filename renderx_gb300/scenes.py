@@ -290,6 +290,18 @@ def sphere_field(n_spheres: int = 200, subdiv: int = 5, seed: int = 1, width: in
     return sc
 
 
+GUIDING_LIGHT_SCALE = math.sqrt(0.01 * ROOM * ROOM / (1.3 * 1.05))  # light = 1% of the ceiling
+
+
+def guiding_scene(width: int = 1024, height: int = 1024, n_spheres: int = 200, subdiv: int = 5,
+                  seed: int = 1) -> Scene:
+    """The glossy workload of the learned-guiding comparison: the sphere field with 60%
+    Phong-lobe glossy spheres (exponent log-U[100,1000]), 30% diffuse, 10% dielectric,
+    and the ceiling light shrunk to 1% of the ceiling area."""
+    return sphere_field(n_spheres, subdiv, seed, width, height, glossy_frac=0.6, diffuse_frac=0.3,
+                        glossy_exp=(100.0, 1000.0), light_scale=GUIDING_LIGHT_SCALE)
+
+
 def hit_rays(n: int, seed: int = 7, lo: float = 0.0, hi: float = ROOM):
     """Closest-hit batch: origins U[lo,hi]^3, directions uniform on S^2 with
     z = 1-2u, phi = 2 pi u. Returns (origins (n,3) f32, dirs (n,3) f32)."""

@@ -108,6 +108,8 @@ RENDER_CASES = {
     "cornell_nee": ("cornell_box", "ptnee", 8, 4096),
     "spheres_pt": ("material_spheres", "pt", 8, 4096),
     "spheres_nee": ("material_spheres", "ptnee", 8, 4096),
+    "medium_pt": ("medium_scene", "pt", 8, 4096),
+    "medium_nee": ("medium_scene", "ptnee", 8, 4096),
 }
 
 
@@ -115,15 +117,22 @@ def render_scene(name: str, w: int = 64, h: int = 64) -> scenes.Scene:
     return getattr(scenes, name)(w, h)
 
 
+def _selected(case: str) -> bool:
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
+    return not only or case in only[0].split(",")
+
+
 def make_render_goldens(ref_pt: str):
     for case, (scene_fn, mode, depth, spp) in RENDER_CASES.items():
+        if not _selected(case):
+            continue
         sc = render_scene(scene_fn)
         f = sc.flatten()
         with tempfile.TemporaryDirectory() as td:
             cfg = sceneio.write_config(sc, td, "PTtest" if mode == "ptnee" else "PT", depth)
             pre = os.path.join(td, "out")
             out = subprocess.run([ref_pt, cfg, mode, str(spp), pre, "8"], check=True, capture_output=True,
-                                 text=True, cwd=td).stdout.split()
+                                 text=True, cwd=td).stdout.strip().splitlines()[-1].split()
             s1 = np.fromfile(pre + ".sum.f64").reshape(sc.camera.height, sc.camera.width, 3)
             s2 = np.fromfile(pre + ".sq.f64").reshape(sc.camera.height, sc.camera.width, 3)
         mean = s1 / spp
@@ -141,11 +150,14 @@ def make_render_goldens(ref_pt: str):
 VCM_CASES = {
     "cornell_vcm": ("cornell_box", 8, 8, 64, 0.0963, 0.75),
     "spheres_vcm": ("material_spheres", 8, 8, 48, 0.0963, 0.75),
+    "medium_vcm": ("medium_scene", 8, 8, 48, 0.0963, 0.75),
 }
 
 
 def make_vcm_goldens(ref_vcm: str):
     for case, (scene_fn, depth, iters, runs, r0, alpha) in VCM_CASES.items():
+        if not _selected(case):
+            continue
         sc = render_scene(scene_fn)
         f = sc.flatten()
         imgs = []
@@ -155,7 +167,7 @@ def make_vcm_goldens(ref_vcm: str):
             for run in range(runs):
                 pre = os.path.join(td, f"out{run}")
                 out = subprocess.run([ref_vcm, cfg, str(iters), str(run), str(r0), str(alpha), pre, "8"], check=True,
-                                     capture_output=True, text=True, cwd=td).stdout.split()
+                                     capture_output=True, text=True, cwd=td).stdout.strip().splitlines()[-1].split()
                 secs += float(out[-1])
                 imgs.append(np.fromfile(pre + ".img.f64").reshape(sc.camera.height, sc.camera.width, 3))
         imgs = np.array(imgs)

@@ -1,0 +1,166 @@
+"""GPU checks of the guiding network's tensor-core kernels against the FP64 oracle
+(oracle/guide_mlp.py): the tcgen05 operand layouts, the forward pass, the training
+kernel's gradient, and that Adam steps on the GPU reduce the loss."""
+import itertools
+
+import numpy as np
+import pytest
+
+import renderx_gb300 as rx
+from oracle import guide_mlp as gm
+
+pytestmark = pytest.mark.gpu
+BOX = ((0.0, 0.0, 0.0), (5.56, 5.56, 5.56))
+
+
+def bf16_bits(x):
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def random_records(n, seed):
+    rng = np.random.default_rng(seed)
+    r = np.zeros((n, 16), np.float32)
+    r[:, 0:3] = rng.random((n, 3)) * 5.56
+    for k in (3, 6, 9):
+        v = rng.normal(size=(n, 3))
+        r[:, k:k + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    r[:, 12] = rng.exponential(1.0, n)
+    return r
+
+
+@pytest.mark.parametrize("a_mn,b_mn", list(itertools.product([0, 1], [0, 1])))
+@pytest.mark.parametrize("N,K", [(16, 16), (64, 64), (80, 128), (128, 80)])
+def test_umma_m128_layouts_exact(a_mn, b_mn, N, K):
+    rng = np.random.default_rng(N * 1000 + K + 10 * a_mn + b_mn)
+    a = rng.integers(-2, 3, (128, K)).astype(np.float32)
+    b = rng.integers(-2, 3, (N, K)).astype(np.float32)
+    with rx.Context(0) as ctx:
+        d = ctx.diag_umma_gemm(bf16_bits(a), bf16_bits(b), a_mn, b_mn)
+    assert np.array_equal(d, a @ b.T)
+
+
+@pytest.mark.parametrize("a_mn,b_mn", [(0, 0), (1, 1)])
+@pytest.mark.parametrize("N", [64, 80])
+def test_umma_m64_lane_placement(a_mn, b_mn, N):
+    """An M = 64 accumulator occupies lanes 0..15 of each 32-lane quarter (row r in
+    lane 32 (r // 16) + r % 16), the placement the training kernel's flush assumes."""
+    rng = np.random.default_rng(N + 7 * a_mn)
+    a = rng.integers(-2, 3, (64, 128)).astype(np.float32)
+    b = rng.integers(-2, 3, (N, 128)).astype(np.float32)
+    with rx.Context(0) as ctx:
+        d = ctx.diag_umma_gemm(bf16_bits(a), bf16_bits(b), a_mn, b_mn)
+    lanes = np.array([32 * (r // 16) + r % 16 for r in range(64)])
+    assert np.array_equal(d[lanes], a @ b.T)
+
+
+def test_forward_matches_oracle():
+    recs = random_records(1000, 1)
+    with rx.Context(0) as ctx:
+        ctx.guide_init(seed=5, box=BOX)
+        params = ctx.guide_params()
+        raw, pdf = ctx.guide_eval(recs)
+    assert np.array_equal(params, gm.init_params(5))
+    _, ref = gm.forward(params, recs, *BOX)
+    scale = np.abs(ref).max()
+    err = np.abs(raw - ref).max() / scale
+    assert err < 2e-2, err
+    ref_pdf = gm.mixture_pdf(raw.astype(np.float64), recs[:, 9:12])
+    assert np.allclose(pdf, ref_pdf, rtol=1e-3, atol=1e-6)
+
+
+def test_gradient_matches_oracle():
+    rng = np.random.default_rng(2)
+    recs = random_records(4096 + 77, 3)  # ragged last tile
+    with rx.Context(0) as ctx:
+        ctx.guide_init(seed=9, box=BOX)
+        p = gm.init_params(9)
+        p = (p + rng.normal(scale=0.03, size=p.shape).astype(np.float32) * (p != 0)).astype(np.float32)
+        ctx.guide_set_params(p)
+        loss, g = ctx.guide_gradient(recs)
+    ref_loss, ref = gm.gradient(p, recs, *BOX)
+    assert abs(loss - ref_loss) <= 2e-3 * abs(ref_loss) + 1e-6
+    for l in range(5):
+        a, b = gm.W_OFF[l], gm.W_OFF[l] + 64 * gm.K_IN[l]
+        rel = np.linalg.norm(g[a:b] - ref[a:b]) / max(np.linalg.norm(ref[a:b]), 1e-30)
+        assert rel < 2e-2, (l, rel)
+    last = g[gm.W_OFF[4]:].reshape(64, 64)
+    assert np.all(last[40:] == 0)
+
+
+def test_adam_steps_reduce_loss():
+    """Records whose incident directions cluster about a position-dependent mean: a
+    few hundred Adam steps on the GPU must lower the loss well below its start."""
+    import torch
+    rng = np.random.default_rng(4)
+    n = 1 << 16
+    recs = random_records(n, 8)
+    mean = np.stack([np.cos(recs[:, 0]), np.sin(recs[:, 0]), 0.3 * np.ones(n)], 1)
+    mean /= np.linalg.norm(mean, axis=1, keepdims=True)
+    wi = mean + 0.15 * rng.normal(size=(n, 3))
+    recs[:, 9:12] = wi / np.linalg.norm(wi, axis=1, keepdims=True)
+    recs[:, 12] = 1.0
+    d = torch.from_numpy(recs).cuda()
+    with rx.Context(0) as ctx:
+        ctx.guide_init(seed=1, box=BOX, learning_rate=5e-3, batch=n)
+        first = ctx.guide_train_step(d.data_ptr(), n)
+        for _ in range(300):
+            last = ctx.guide_train_step(d.data_ptr(), n, want_loss=False)
+        last = ctx.guide_train_step(d.data_ptr(), n)
+    # uniform density on the sphere: -log(1/4pi) = 2.53; a concentrated fit is far lower
+    assert first > 1.5 and last < first - 1.5, (first, last)
+
+
+def _relmse(img, ref):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def test_guided_render_matches_reference_pathtracer():
+    """Guided sampling (network trained during the first passes of the same render) is
+    unbiased: it agrees with the reference's own PathTracer render of the Cornell box
+    under the per-pixel 3-sigma criteria of the plain path-tracing parity test."""
+    from renderx_gb300 import scenes
+    from test_render_gpu import compare, load_case
+    z, sc = load_case("cornell_pt")
+    spp = 8192
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ctx.guide_init(seed=3, batch=1 << 16, train_passes=6, steps_per_pass=8)
+        mean, sq, st = ctx.render_pt(sc.camera, spp, max_depth=int(z["max_depth"]), rr_mode=0, seed=777,
+                                     want_sq=True, guided=True, paths_per_pass=1 << 18)
+    var = np.maximum(sq - mean * mean, 0.0) * spp / (spp - 1)
+    se = np.sqrt(var / spp)
+    ref, rse = z["mean"].astype(np.float64), z["stderr"].astype(np.float64)
+    zz, bad = compare(mean, se, ref, rse)
+    assert bad.mean() <= 0.01, f"{bad.mean():.4f} of channels beyond 3 sigma (max z {zz.max():.1f})"
+    assert (zz > 8).sum() == 0
+    n = mean.shape[0] * mean.shape[1]
+    for c in range(3):
+        dm = mean[..., c].mean() - ref[..., c].mean()
+        s_img = np.sqrt((se[..., c] ** 2).sum() + (rse[..., c] ** 2).sum()) / n
+        assert abs(dm) < 4 * s_img, (c, dm, s_img)
+
+
+def test_guiding_gain_on_glossy_workload():
+    """Equal-work comparison on the glossy workload (60% glossy spheres, 1%-area light):
+    the guided path tracer, training time included, reaches a lower relMSE per unit of
+    render time than plain BSDF sampling, against a high-sample FP64 reference."""
+    from renderx_gb300 import scenes
+    sc = scenes.guiding_scene(128, 128, n_spheres=40, subdiv=3, seed=2)
+    depth = 8
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ctx.guide_init(seed=1, batch=1 << 16, train_passes=8, steps_per_pass=8)
+        ref, _, _ = ctx.render_pt(sc.camera, 8192, max_depth=depth, rr_mode=1, seed=99, guided=True,
+                                  paths_per_pass=1 << 20)
+        ctx.guide_init(seed=1, batch=1 << 16, train_passes=8, steps_per_pass=8)
+        spp = 256
+        plain, _, sp = ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=5, paths_per_pass=1 << 18)
+        guided, _, sg = ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=6, guided=True,
+                                      paths_per_pass=1 << 18)
+    e_plain = _relmse(plain, ref) * sp["ms"]
+    e_guided = _relmse(guided, ref) * sg["ms"]
+    print(f"relMSE x ms: plain {e_plain:.4g} ({sp['ms']:.1f} ms), guided {e_guided:.4g} ({sg['ms']:.1f} ms)")
+    assert e_guided < e_plain, (e_guided, e_plain)
