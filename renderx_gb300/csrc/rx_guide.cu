@@ -225,7 +225,7 @@ __device__ __forceinline__ void decode(const float (&raw)[48], Lobe (&L)[kLobes]
   }
 }
 
-// -scale * log q(wi) and its gradient with respect to the 40 raw outputs.
+// -scale * log q(wi) and its gradient with respect to the 40 raw outputs (returns the former).
 __device__ float mix_loss_grad(const float (&raw)[48], const float (&wi)[3], float scale, float (&dz)[48]) {
   Lobe L[kLobes];
   decode(raw, L);
@@ -255,7 +255,7 @@ __device__ float mix_loss_grad(const float (&raw)[48], const float (&wi)[3], flo
   }
 #pragma unroll
   for (int i = kOutUsed; i < 48; i++) dz[i] = 0.0f;
-  return -lq;
+  return -scale * lq;
 }
 
 // Mixture for sampling / evaluation: per lobe weight, kappa, mean, weight x normaliser.

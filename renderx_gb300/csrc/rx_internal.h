@@ -21,6 +21,14 @@ struct TraceConfig {
   int variant = 1;
   int blocks_per_sm = 12;
   int sms = 152;
+  int pt_blocks_per_sm = 8;  // wavefront extend / shade kernels
+};
+
+// Launch shape of the wavefront's extend / shade kernels: blocks of 128 threads per SM
+// and the traversal stack depth (32 or 64 entries; must exceed the BVH depth).
+struct PtShape {
+  int blocks_per_sm = 8;
+  int stack = 64;
 };
 
 // Launchers (rx_trace.cu). `ev` (optional): four events recorded before the walk
@@ -134,6 +142,23 @@ struct rx_context {
 };
 
 namespace rx {
+// One scene of a path-traced render: a context with a built scene, its camera and options,
+// and the offset (pixels) of its image in the shared film.
+struct PtJob {
+  const rx_context* ctx;
+  rx_camera cam;
+  rx_pt_options opt;
+  uint64_t film_base;
+};
+struct PtRun {
+  uint32_t paths_per_pass = 0;  // 0 = 2^21
+  bool guided = false;          // one scene only
+  bool use_graph = true;        // replay a captured pass
+  bool autotune = false;        // time launch shapes on the first passes
+};
+// Renders all jobs in one wavefront into device films (sum, optional sum of squares).
+cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun& run, double* film_sum,
+                           double* film_sq, rx_render_stats* stats, PtShape* chosen, cudaStream_t s);
 // Path tracing (rx_pt.cu): renders into device films (sum, optional sum of squares).
 cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& opt, double* film_sum,
                       double* film_sq, rx_render_stats* stats, cudaStream_t s);

@@ -26,10 +26,34 @@ struct PtParams {
   uint32_t rr_mode;  // 0: reference RR at every bounce, 1: RR from depth 3 on
   uint32_t nee;      // 0: PathTracer, 1: PathTracerTest
   uint32_t pixels;
-  uint64_t path_base;
-  uint32_t npaths;
   uint32_t has_media;  // any medium object: camera rays look up their inside object
 };
+
+// One scene of a render: its geometry, estimator settings, and where its paths and film
+// sit. A render of several scenes runs one wavefront over all their paths; a path
+// carries its scene index (info.w >> 16).
+struct SceneRec {
+  DevScene S;
+  PtParams P;
+  uint64_t path_begin;  // first global path index of the scene
+  uint64_t film_base;   // first pixel of the scene in the shared film
+};
+
+// Pass cursor in device memory, so that one captured pass replays unchanged.
+struct PassState {
+  uint64_t base, total;
+  uint32_t per_pass, npaths;
+};
+
+__device__ __forceinline__ int scene_of(const SceneRec* R, int nr, uint64_t g) {
+  int lo = 0, hi = nr - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (R[mid].path_begin <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
 
 // -------------------------------------------------------------------------------------
 // Camera (reference src/Camera.cpp:4-47, 78-96)
@@ -39,10 +63,16 @@ __device__ __forceinline__ F3 camera_dir(const CamDev& c, float xp, float yp) {
   return normalize(c.front * c.sight + c.right * x + c.up * y);
 }
 
-__global__ void k_generate(DevScene SC, PtParams P, PathSoA S, unsigned* count) {
+__global__ void k_generate(const SceneRec* R, int nr, PassState* ps, PathSoA S, unsigned* count) {
+  const uint64_t base = ps->base;
+  const uint64_t left = base < ps->total ? ps->total - base : 0;
+  const uint32_t np = (uint32_t)(left < ps->per_pass ? left : ps->per_pass);
   uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npaths; i += stride) {
-    uint64_t pid = P.path_base + i;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
+    uint64_t g = base + i;
+    int sc = scene_of(R, nr, g);
+    const PtParams& P = R[sc].P;
+    uint64_t pid = g - R[sc].path_begin;  // path index within its scene (random-number key)
     uint32_t pixel = (uint32_t)(pid % P.pixels);
     int x = pixel % P.cam.width, y = pixel / P.cam.width;
     Rng rng(P.seed, pid, 0);
@@ -55,18 +85,22 @@ __global__ void k_generate(DevScene SC, PtParams P, PathSoA S, unsigned* count) 
       F3 dc = camera_dir(P.cam, x + 0.5f, y + 0.5f);
       w = fmaxf(fabsf(dot(P.cam.front, d)), 1e-6f) / fabsf(dot(dc, P.cam.front));
     }
-    int inside = P.has_media ? find_inside(SC, P.cam.pos, d, kNone) : kNone;
+    int inside = P.has_media ? find_inside(R[sc].S, P.cam.pos, d, kNone) : kNone;
     S.o[i] = make_float4(P.cam.pos.x, P.cam.pos.y, P.cam.pos.z, 1.0f);
     S.d[i] = make_float4(d.x, d.y, d.z, 0.0f);
     S.T[i] = make_float4(w, w, w, 0.0f);
     S.L[i] = make_float4(0, 0, 0, 0);
-    S.info[i] = make_int4((int)pixel, kCameraObj, inside, 1 << 8);
-    S.id[i] = pid;
+    S.info[i] = make_int4((int)pixel, kCameraObj, inside, (sc << 16) | (1 << 8));
+    S.id[i] = g;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *count = P.npaths;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *count = np;
+    ps->npaths = np;
+  }
 }
 
-__global__ void __launch_bounds__(128) k_extend(DevScene SC, PathSoA S, const unsigned* count, int2* hit,
+template <int STACK>
+__global__ void __launch_bounds__(128) k_extend(const SceneRec* R, PathSoA S, const unsigned* count, int2* hit,
                                                 unsigned long long* rays) {
   uint32_t n = *count;
   uint32_t stride = gridDim.x * blockDim.x;
@@ -74,7 +108,8 @@ __global__ void __launch_bounds__(128) k_extend(DevScene SC, PathSoA S, const un
     float4 o = S.o[i], d = S.d[i];
     int4 inf = S.info[i];
     bool camera = (inf.w & 255) == 0;  // the camera ray's first query has no condition
-    PHit h = trace_cond<false>(SC, f3(o), f3(d), INFINITY, camera ? kNone : inf.y, camera ? kNone : inf.z);
+    const DevScene& SC = R[(uint32_t)inf.w >> 16].S;
+    PHit h = trace_cond<false, STACK>(SC, f3(o), f3(d), INFINITY, camera ? kNone : inf.y, camera ? kNone : inf.z);
     hit[i] = make_int2(h.tid, __float_as_int(h.t));
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
@@ -96,6 +131,7 @@ __device__ __forceinline__ void film_add(double* sum, double* sq, int pixel, F3 
 // PathTracerTest::colorByConnectingLights (src/PathTracerTest.cpp:88-136) at vertex `v`
 // (the ray leaving it), reached by `in`: a light point by area, two-sided emission,
 // balance-heuristic weight against the BSDF's sampling pdf.
+template <int STACK>
 __device__ F3 connect_light(const DevScene& SC, const CamDev& cam, const PV& in, const PV& v, Rng& rng,
                             unsigned& shadows) {
   float ru = rng.next() * SC.light_area;
@@ -125,7 +161,7 @@ __device__ F3 connect_light(const DevScene& SC, const CamDev& cam, const PV& in,
   if (v.contact != kNone) cos_s = fminf(fabsf(dot(contact_normal(SC, cam, v), out.d)), 1.0f);
   float bpdf = dir_pdf(SC, cam, in, out, false);
   shadows++;
-  PHit sh = trace_cond<true>(SC, v.o, out.d, dist - 1e-5f, v.contact, v.inside);  // testVisibility
+  PHit sh = trace_cond<true, STACK>(SC, v.o, out.d, dist - 1e-5f, v.contact, v.inside);  // testVisibility
   if (sh.tid >= 0) return {0, 0, 0};
   float pdfa = 1.0f / SC.light_area;
   float pdfw = pdfa * dist * dist / cos_l;
@@ -214,9 +250,11 @@ static __device__ PV scatter_guided(const DevScene& S, const PV& in, Hit3 h, boo
 }
 
 // One bounce of MCRenderer::samplePathIter plus the estimator's bookkeeping.
-__global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA S, const unsigned* count,
-                                               const int2* hit, PathSoA N, unsigned* next_count, double* film_sum,
-                                               double* film_sq, unsigned long long* shadow_rays, GuideIO G) {
+template <int STACK>
+__global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassState* ps, PathSoA S,
+                                               const unsigned* count, const int2* hit, PathSoA N, unsigned* next_count,
+                                               double* film_sum, double* film_sq, unsigned long long* shadow_rays,
+                                               GuideIO G) {
   uint32_t n = *count;
   uint32_t stride = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
@@ -232,12 +270,16 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
     uint64_t pid = 0;
     int depth = 0;
     bool rec = false;  // a guided vertex whose path continues: a training record
+    uint32_t sc = 0;
     if (i < n) {
       float4 o4 = S.o[i], d4 = S.d[i], T4 = S.T[i], L4 = S.L[i];
       inf = S.info[i];
       pid = S.id[i];
       depth = inf.w & 255;
       bool last_spec = (inf.w >> 8) & 1;
+      sc = (uint32_t)inf.w >> 16;
+      const DevScene& SC = R[sc].S;
+      const PtParams& P = R[sc].P;
       T = f3(T4);
       L = f3(L4);
       PV cur = pv_term(f3(o4));
@@ -247,7 +289,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
       cur.pixel = inf.x;
       cur.flags = (depth == 0 || !last_spec) ? kDirRandom : 0u;  // the camera ray is RANDOM
       int2 h = hit[i];
-      Rng rng(P.seed, pid, 16u + 32u * (uint32_t)depth);
+      Rng rng(P.seed, pid - R[sc].path_begin, 16u + 32u * (uint32_t)depth);
       bool done = true;
       if (h.x >= 0) {  // a ray that hits nothing ends the path (samplePathIter's termRay)
         Hit3 hh{(int)__ldg(&SC.tri_obj[h.x]), h.x, __int_as_float(h.y)};
@@ -284,7 +326,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
           }
           L = L + T * f3v(SC.objects[nx.contact].color) * mis;
         } else if (!capped) {
-          if ((nx.flags & kDirRandom) && SC.num_lights > 0) L = L + T * connect_light(SC, P.cam, cur, nx, rng, shadows);
+          if ((nx.flags & kDirRandom) && SC.num_lights > 0) L = L + T * connect_light<STACK>(SC, P.cam, cur, nx, rng, shadows);
           if (!killed) {
             T = T * (nx.c * (cos_term(SC, P.cam, nx) / nx.dprob));
             T = T * decay_of(SC, cur.inside, fmaxf(dist, 1e-5f));
@@ -293,8 +335,9 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
         }
       }
       if (done) {
-        if (L.x != 0.0f || L.y != 0.0f || L.z != 0.0f) film_add(film_sum, film_sq, inf.x, L);
-        if (G.lpath) G.lpath[pid - P.path_base] = make_float4(L.x, L.y, L.z, 0.0f);
+        if (L.x != 0.0f || L.y != 0.0f || L.z != 0.0f)
+          film_add(film_sum, film_sq, (int)(R[sc].film_base + (uint32_t)inf.x), L);
+        if (G.lpath) G.lpath[pid - ps->base] = make_float4(L.x, L.y, L.z, 0.0f);
       } else {
         cont = true;
       }
@@ -309,13 +352,13 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
       rb = __shfl_sync(0xffffffffu, rb, leader);
       uint32_t j = rb + __popc(rm & ((1u << lane) - 1));
       if (rec && j < G.rec_cap) {
-        F3 ns = contact_normal(SC, P.cam, nx);
+        F3 ns = contact_normal(R[sc].S, R[sc].P.cam, nx);
         float4* r = reinterpret_cast<float4*>(G.recs + (size_t)j * guide::kRec);
         float4 d4 = S.d[i];
         r[0] = make_float4(nx.o.x, nx.o.y, nx.o.z, ns.x);
         r[1] = make_float4(ns.y, ns.z, -d4.x, -d4.y);
         r[2] = make_float4(-d4.z, nx.d.x, nx.d.y, nx.d.z);
-        r[3] = make_float4(Tb.x, Tb.y, Tb.z, __uint_as_float((uint32_t)(pid - P.path_base)));
+        r[3] = make_float4(Tb.x, Tb.y, Tb.z, __uint_as_float((uint32_t)(pid - ps->base)));
       }
     }
     // compaction: warp ballot, one atomic per warp
@@ -332,7 +375,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
         N.T[j] = make_float4(T.x, T.y, T.z, 0.0f);
         N.L[j] = make_float4(L.x, L.y, L.z, 0.0f);
         N.info[j] = make_int4(inf.x, nx.contact, nx.inside,
-                              (depth + 1) | (((nx.flags & kDirRandom) ? 0 : 1) << 8));
+                              (int)(sc << 16) | (depth + 1) | (((nx.flags & kDirRandom) ? 0 : 1) << 8));
         N.id[j] = pid;
       }
     }
@@ -342,6 +385,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene SC, PtParams P, PathSoA 
 }
 
 __global__ void k_zero(unsigned* p) { *p = 0; }
+__global__ void k_advance(PassState* ps) { ps->base += ps->per_pass; }
 
 // Training samples of a finished pass: each record's weight is the luminance of its
 // path's final radiance over the throughput before the vertex, i.e. (BSDF x cosine x
@@ -400,9 +444,7 @@ static cudaError_t alloc_soa(PathSoA& s, std::vector<DevBuf>& bufs, size_t n) {
   return cudaSuccess;
 }
 
-cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& opt, double* film_sum,
-                      double* film_sq, rx_render_stats* stats, cudaStream_t s) {
-  const DevScene& SC = c->scene;
+PtParams make_pt_params(const rx_context* c, const rx_camera& cam, const rx_pt_options& opt) {
   PtParams P{};
   auto v3 = [](const float* p) { return F3{p[0], p[1], p[2]}; };
   auto hn = [](F3 a) {
@@ -423,91 +465,199 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
   P.rr_mode = opt.rr_mode;
   P.nee = opt.nee;
   P.pixels = cam.width * cam.height;
-  for (uint32_t o = 0; o < (uint32_t)c->objects.size(); o++) P.has_media |= c->objects[o].material == RX_MAT_VPM;
-  uint64_t total = (uint64_t)P.pixels * opt.spp;
-  uint32_t per_pass = opt.paths_per_pass ? opt.paths_per_pass : (1u << 21);
+  for (const rx_object& o : c->objects) P.has_media |= o.material == RX_MAT_VPM;
+  return P;
+}
+
+namespace {
+
+// Device buffers of one wavefront render.
+struct Wave {
+  const SceneRec* R;
+  int nr;
+  PassState* ps;
+  PathSoA A, B;
+  int2* hit;
+  unsigned long long* ctr;  // [0] extension rays, [1] shadow rays
+  unsigned* cnt;            // [0], [1] queue lengths, [2] records, [3] weighted records
+  double *film, *sq;
+  uint32_t loops;           // bounce stages per pass (max depth cap + 1)
+};
+
+// One pass: generate, `loops` x (extend, clear the next queue, shade), advance the cursor.
+// Everything is a kernel on `s` with device-resident counts, so the pass can be captured
+// into a CUDA graph once and replayed.
+template <int STACK>
+void enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
+  k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.A, W.cnt);
+  PathSoA cur = W.A, nxt = W.B;
+  unsigned *cc = W.cnt, *cn = W.cnt + 1;
+  for (uint32_t d = 0; d < W.loops; d++) {
+    k_extend<STACK><<<grid, 128, 0, s>>>(W.R, cur, cc, W.hit, W.ctr);
+    k_zero<<<1, 1, 0, s>>>(cn);
+    k_shade<STACK><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, GuideIO{});
+    std::swap(cur, nxt);
+    std::swap(cc, cn);
+  }
+  k_advance<<<1, 1, 0, s>>>(W.ps);
+}
+
+void enqueue_pass_shape(const Wave& W, const PtShape& sh, int sms, cudaStream_t s) {
+  int grid = sms * sh.blocks_per_sm;
+  if (sh.stack == 32) enqueue_pass<32>(W, grid, s);
+  else enqueue_pass<kStackDepth>(W, grid, s);
+}
+
+}  // namespace
+
+cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun& run, double* film_sum,
+                           double* film_sq, rx_render_stats* stats, PtShape* chosen, cudaStream_t s) {
+  std::vector<SceneRec> recs(nj);
+  uint64_t total = 0;
+  uint32_t max_depth = 0, max_bvh_depth = 0;
+  for (int k = 0; k < nj; k++) {
+    recs[k].S = jobs[k].ctx->scene;
+    recs[k].P = make_pt_params(jobs[k].ctx, jobs[k].cam, jobs[k].opt);
+    recs[k].path_begin = total;
+    recs[k].film_base = jobs[k].film_base;
+    total += (uint64_t)recs[k].P.pixels * jobs[k].opt.spp;
+    max_depth = std::max(max_depth, jobs[k].opt.max_depth);
+    max_bvh_depth = std::max<uint32_t>(max_bvh_depth, (uint32_t)jobs[k].ctx->bvh.max_depth);
+  }
+  uint32_t per_pass = run.paths_per_pass ? run.paths_per_pass : (1u << 21);
   per_pass = (uint32_t)std::min<uint64_t>(per_pass, total);
   if (per_pass == 0) return cudaSuccess;
+  const uint64_t npasses = (total + per_pass - 1) / per_pass;
+  const int sms = c->trace_cfg.sms;
 
   std::vector<DevBuf> bufs;
-  PathSoA A{}, B{};
   cudaError_t e;
-  if ((e = alloc_soa(A, bufs, per_pass)) != cudaSuccess) return e;
-  if ((e = alloc_soa(B, bufs, per_pass)) != cudaSuccess) return e;
-  bufs.emplace_back();
-  if ((e = bufs.back().alloc(per_pass * sizeof(int2))) != cudaSuccess) return e;
-  int2* hit = bufs.back().as<int2>();
-  bufs.emplace_back();
-  if ((e = bufs.back().alloc(64 * sizeof(unsigned long long))) != cudaSuccess) return e;
-  unsigned long long* ctr = bufs.back().as<unsigned long long>();  // [0] ext rays, [1] shadow rays
-  unsigned* cnt = reinterpret_cast<unsigned*>(ctr + 8);            // two queue counts
-  cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
+  auto alloc = [&](size_t bytes) -> void* {
+    bufs.emplace_back();
+    if ((e = bufs.back().alloc(bytes)) != cudaSuccess) return nullptr;
+    return bufs.back().p;
+  };
+  Wave W{};
+  W.nr = nj;
+  W.loops = max_depth + 1;
+  W.film = film_sum;
+  W.sq = film_sq;
+  void* pR = alloc(sizeof(SceneRec) * nj);
+  if (!pR) return e;
+  W.R = static_cast<const SceneRec*>(pR);
+  cudaMemcpyAsync(pR, recs.data(), sizeof(SceneRec) * nj, cudaMemcpyHostToDevice, s);
+  if (!(W.ps = static_cast<PassState*>(alloc(sizeof(PassState))))) return e;
+  PassState ps0{0, total, per_pass, 0};
+  cudaMemcpyAsync(W.ps, &ps0, sizeof ps0, cudaMemcpyHostToDevice, s);
+  if ((e = alloc_soa(W.A, bufs, per_pass)) != cudaSuccess) return e;
+  if ((e = alloc_soa(W.B, bufs, per_pass)) != cudaSuccess) return e;
+  if (!(W.hit = static_cast<int2*>(alloc(per_pass * sizeof(int2))))) return e;
+  if (!(W.ctr = static_cast<unsigned long long*>(alloc(64 * sizeof(unsigned long long))))) return e;
+  W.cnt = reinterpret_cast<unsigned*>(W.ctr + 8);
+  cudaMemsetAsync(W.ctr, 0, 64 * sizeof(unsigned long long), s);
 
-  // guiding: mixture per live path, training records, per-path final radiance
-  const bool guided = (opt.flags & RX_PT_GUIDED) && guide_ready(c->guide) && !opt.nee;
+  // guiding (one scene): mixture per live path, training records, per-path radiance
+  const bool guided = run.guided && nj == 1 && guide_ready(c->guide) && !jobs[0].opt.nee;
   GuideIO G{};
   float* train = nullptr;
-  unsigned* rcnt = nullptr;
+  unsigned* rcnt = W.cnt + 2;
   uint32_t cap = 0;
   if (guided) {
     cap = (uint32_t)std::min<uint64_t>((uint64_t)per_pass * 4, 1u << 22);
-    bufs.emplace_back();
-    if ((e = bufs.back().alloc((size_t)per_pass * guide::kLobeStride * sizeof(float))) != cudaSuccess) return e;
-    G.lobes = bufs.back().as<float>();
+    if (!(G.lobes = static_cast<float*>(alloc((size_t)per_pass * guide::kLobeStride * sizeof(float))))) return e;
     G.frac = guide_bsdf_fraction(c->guide);
     if (guide_train_passes(c->guide) > 0) {
-      bufs.emplace_back();
-      if ((e = bufs.back().alloc((size_t)cap * guide::kRec * sizeof(float))) != cudaSuccess) return e;
-      G.recs = bufs.back().as<float>();
-      bufs.emplace_back();
-      if ((e = bufs.back().alloc((size_t)cap * guide::kRec * sizeof(float))) != cudaSuccess) return e;
-      train = bufs.back().as<float>();
-      bufs.emplace_back();
-      if ((e = bufs.back().alloc((size_t)per_pass * sizeof(float4))) != cudaSuccess) return e;
-      G.lpath = bufs.back().as<float4>();
-      rcnt = cnt + 2;  // [2] records, [3] weighted records
+      if (!(G.recs = static_cast<float*>(alloc((size_t)cap * guide::kRec * sizeof(float))))) return e;
+      if (!(train = static_cast<float*>(alloc((size_t)cap * guide::kRec * sizeof(float))))) return e;
+      if (!(G.lpath = static_cast<float4*>(alloc((size_t)per_pass * sizeof(float4))))) return e;
       G.rec_count = rcnt;
       G.rec_cap = cap;
     }
   }
 
-  int grid = c->trace_cfg.sms * 8;
+  // launch shapes: the context's default, or candidates timed on the first passes
+  PtShape best{c->trace_cfg.pt_blocks_per_sm, max_bvh_depth < 32 ? 32 : kStackDepth};
+  std::vector<PtShape> cands;
+  if (run.autotune && !guided) {
+    for (int bps : {4, 8, 16})
+      for (int st : {32, kStackDepth})
+        if (st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
+    if (npasses < cands.size() + 2) cands.clear();
+  }
+
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  uint32_t pass = 0;
-  for (uint64_t base = 0; base < total; base += per_pass, pass++) {
-    P.path_base = base;
-    P.npaths = (uint32_t)std::min<uint64_t>(per_pass, total - base);
-    PathSoA* cur = &A;
-    PathSoA* nxt = &B;
-    unsigned* ccur = cnt;
-    unsigned* cnxt = cnt + 1;
-    GuideIO Gp = G;
-    const bool training = guided && G.recs && pass < guide_train_passes(c->guide);
-    if (!training) {
-      Gp.recs = nullptr;
-      Gp.lpath = nullptr;
+  uint64_t pass = 0;
+  if (!cands.empty()) {
+    float best_t = INFINITY;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    for (const PtShape& sh : cands) {
+      cudaEventRecord(t0, s);
+      enqueue_pass_shape(W, sh, sms, s);
+      cudaEventRecord(t1, s);
+      if ((e = cudaEventSynchronize(t1)) != cudaSuccess) return e;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (ms < best_t) best_t = ms, best = sh;
+      pass++;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+  }
+  if (chosen) *chosen = best;
+
+  if (!guided) {
+    if (run.use_graph && npasses - pass >= 2) {
+      cudaGraph_t graph;
+      cudaGraphExec_t exec;
+      if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+      enqueue_pass_shape(W, best, sms, s);
+      if ((e = cudaStreamEndCapture(s, &graph)) != cudaSuccess) return e;
+      if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return e;
+      }
+      for (; pass < npasses && e == cudaSuccess; pass++) e = cudaGraphLaunch(exec, s);
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return e;
     } else {
-      cudaMemsetAsync(rcnt, 0, 2 * sizeof(unsigned), s);
-      cudaMemsetAsync(G.lpath, 0, (size_t)P.npaths * sizeof(float4), s);
+      for (; pass < npasses; pass++) enqueue_pass_shape(W, best, sms, s);
     }
-    k_generate<<<grid, 256, 0, s>>>(SC, P, *cur, ccur);
-    for (uint32_t depth = 0; depth <= opt.max_depth; depth++) {
-      k_extend<<<grid, 128, 0, s>>>(SC, *cur, ccur, hit, ctr);
-      if (guided && (e = guide_infer_paths(c->guide, SC, *cur, ccur, hit, G.lobes, 2 * c->trace_cfg.sms, s)) !=
-                        cudaSuccess)
-        return e;
-      k_zero<<<1, 1, 0, s>>>(cnxt);
-      k_shade<<<grid, 128, 0, s>>>(SC, P, *cur, ccur, hit, *nxt, cnxt, film_sum, film_sq, ctr + 1, Gp);
-      std::swap(cur, nxt);
-      std::swap(ccur, cnxt);
-    }
-    if (training) {
-      k_record_weights<<<grid, 128, 0, s>>>(G.recs, rcnt, cap, G.lpath, train, rcnt + 1);
-      if ((e = guide_train_records(c->guide, train, rcnt + 1, cap, (int)guide_steps_per_pass(c->guide), s)) != cudaSuccess)
-        return e;
+  } else {
+    const int grid = sms * best.blocks_per_sm;
+    for (; pass < npasses; pass++) {
+      const bool training = G.recs && pass < guide_train_passes(c->guide);
+      GuideIO Gp = G;
+      if (!training) {
+        Gp.recs = nullptr;
+        Gp.lpath = nullptr;
+      } else {
+        cudaMemsetAsync(rcnt, 0, 2 * sizeof(unsigned), s);
+        cudaMemsetAsync(G.lpath, 0, (size_t)per_pass * sizeof(float4), s);
+      }
+      k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.A, W.cnt);
+      PathSoA cur = W.A, nxt = W.B;
+      unsigned *cc = W.cnt, *cn = W.cnt + 1;
+      for (uint32_t d = 0; d < W.loops; d++) {
+        k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, W.hit, W.ctr);
+        if ((e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, 2 * sms, s)) != cudaSuccess) return e;
+        k_zero<<<1, 1, 0, s>>>(cn);
+        k_shade<kStackDepth><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
+        std::swap(cur, nxt);
+        std::swap(cc, cn);
+      }
+      if (training) {
+        k_record_weights<<<grid, 128, 0, s>>>(G.recs, rcnt, cap, G.lpath, train, rcnt + 1);
+        if ((e = guide_train_records(c->guide, train, rcnt + 1, cap, (int)guide_steps_per_pass(c->guide), s)) !=
+            cudaSuccess)
+          return e;
+      }
+      k_advance<<<1, 1, 0, s>>>(W.ps);
     }
   }
   cudaEventRecord(e1, s);
@@ -520,13 +670,23 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
   cudaEventDestroy(e1);
   if (stats) {
     unsigned long long h[2];
-    cudaMemcpy(h, ctr, sizeof h, cudaMemcpyDeviceToHost);
+    cudaMemcpy(h, W.ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0];
     stats->shadow_rays = h[1];
     stats->paths = total;
     stats->ms = ms;
   }
   return cudaSuccess;
+}
+
+cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& opt, double* film_sum,
+                      double* film_sq, rx_render_stats* stats, cudaStream_t s) {
+  PtJob job{c, cam, opt, 0};
+  PtRun run{};
+  run.paths_per_pass = opt.paths_per_pass;
+  run.guided = (opt.flags & RX_PT_GUIDED) != 0;
+  run.use_graph = true;
+  return render_pt_jobs(c, &job, 1, run, film_sum, film_sq, stats, nullptr, s);
 }
 
 }  // namespace rx

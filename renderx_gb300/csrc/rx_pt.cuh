@@ -141,7 +141,7 @@ struct PHit {
 // object ids, -1 for none (-1/-1: no condition, as the camera ray's first query),
 // -2 for the camera as contact object. only_obj >= 0: closest hit among that object's
 // triangles only, no condition (the per-object trees of Scene::findInsideObject).
-template <bool ANY>
+template <bool ANY, int STACK = kStackDepth>
 __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside,
                                            int only_obj = -1) {
   const DevAccel& A = S.accel;
@@ -150,7 +150,7 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
             fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(1e30f, d.z)};
   F3 ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
   PHit best{-1, tmax};
-  int stack[kStackDepth];
+  int stack[STACK];
   int sp = 0, cur = 0, cnt = 0;
   const bool cond = only_obj < 0 && !(contact == -1 && inside == -1);
   while (true) {
@@ -172,7 +172,7 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
       if (h0 && h1) {
         bool first0 = tn0 <= tn1;
         int far_ref = first0 ? n3.y : n3.x, far_cnt = first0 ? n3.w : n3.z;
-        if (sp < kStackDepth) stack[sp++] = far_ref < 0 ? ~((~far_ref) << 3 | (far_cnt - 1)) : far_ref;
+        if (sp < STACK) stack[sp++] = far_ref < 0 ? ~((~far_ref) << 3 | (far_cnt - 1)) : far_ref;
         cur = first0 ? n3.x : n3.y;
         cnt = first0 ? n3.z : n3.w;
         continue;

@@ -107,8 +107,9 @@ def test_adam_steps_reduce_loss():
         for _ in range(300):
             last = ctx.guide_train_step(d.data_ptr(), n, want_loss=False)
         last = ctx.guide_train_step(d.data_ptr(), n)
-    # uniform density on the sphere: -log(1/4pi) = 2.53; a concentrated fit is far lower
-    assert first > 1.5 and last < first - 1.5, (first, last)
+    # uniform density on the sphere: -log(1/4pi) = 2.53; the fit to a lobe of spread
+    # 0.15 rad (about 1.9 nats when matched exactly) is far lower
+    assert 1.5 < first < 4.0 and last < first - 1.5, (first, last)
 
 
 def _relmse(img, ref):

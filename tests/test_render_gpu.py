@@ -23,7 +23,7 @@ from renderx_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-CASES = ["cornell_pt", "cornell_nee", "spheres_pt", "spheres_nee"]
+CASES = ["cornell_pt", "cornell_nee", "spheres_pt", "spheres_nee", "medium_pt", "medium_nee"]
 
 
 def load_case(name):

@@ -38,7 +38,7 @@ def _blocks(a, e):
     return m, np.sqrt(v)
 
 
-@pytest.mark.parametrize("name", ["cornell_vcm", "spheres_vcm"])
+@pytest.mark.parametrize("name", ["cornell_vcm", "spheres_vcm", "medium_vcm"])
 def test_vcm_matches_reference(name):
     z, sc = _load(name)
     runs = 256
