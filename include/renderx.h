@@ -98,7 +98,8 @@ typedef struct rx_pt_options {
 /* rx_pt_options.flags: sample directions at diffuse / glossy / Phong vertices by
  * one-sample MIS between the BSDF and the context's guiding network (rx_guide_init),
  * training the network on the render's own samples during the first train_passes
- * passes. PathTracer (nee = 0) only. */
+ * passes; the first warmup_passes passes sample by the BSDF alone. PathTracer (nee = 0)
+ * only. */
 #define RX_PT_GUIDED 1u
 
 /* Learned path guiding (no reference counterpart): a BF16 MLP on the tensor cores,
@@ -109,9 +110,26 @@ typedef struct rx_guide_options {
   uint32_t batch;          /* training records per Adam step (2^18) */
   uint32_t train_passes;   /* rendering passes whose samples train the network */
   uint32_t steps_per_pass; /* Adam steps after each training pass */
-  uint32_t flags;          /* reserved, 0 */
+  uint32_t warmup_passes;  /* first passes sample by the BSDF alone (no inference) */
   uint64_t seed;           /* weight initialisation */
 } rx_guide_options;
+
+/* One scene of a batched path-traced render. */
+typedef struct rx_batch_item {
+  rx_context* scene;       /* context holding the scene (objects set, accelerator built) */
+  rx_camera camera;
+  rx_pt_options options;   /* spp, max_depth, rr_mode, nee, seed; paths_per_pass and flags unused */
+  double* film_rgb;        /* host output: width*height*3 per-pixel means, rows from the top */
+} rx_batch_item;
+
+typedef struct rx_batch_options {
+  uint32_t paths_per_pass; /* wavefront size shared by all scenes, 0 = 2^21 */
+  uint32_t use_graph;      /* 1: capture one pass as a CUDA graph and replay it */
+  uint32_t autotune;       /* 1: time the launch-shape candidates on the first passes */
+  uint32_t reserved;
+  int32_t chosen_blocks_per_sm;  /* out: extend / shade blocks per SM used */
+  int32_t chosen_stack;          /* out: traversal stack depth used */
+} rx_batch_options;
 
 /* Vertex connection and merging options (VCMTracer, reference include/VCMTracer.h). */
 typedef struct rx_vcm_options {
@@ -202,6 +220,14 @@ rx_status rx_trace_closest_reforder_device(rx_context* ctx, const rx_ray* d_rays
  * rx_scene_set_objects before rx_build_accel. */
 rx_status rx_render_pt(rx_context* ctx, const rx_camera* cam, const rx_pt_options* opts, double* film_rgb,
                        double* film_sq, rx_render_stats* stats);
+
+/* Many scenes in one wavefront (no reference counterpart: the reference renders one
+ * scene per Renderer): every item's paths share the pass queues; paths of uneven
+ * length compact away per bounce. Each item's image equals what rx_render_pt gives for
+ * the same options (up to the summation order of the FP64 film). ctx supplies the
+ * stream and device; every item's scene must live on the same device. */
+rx_status rx_render_pt_batch(rx_context* ctx, const rx_batch_item* items, uint32_t n, rx_batch_options* opts,
+                             rx_render_stats* stats);
 
 /* VCMTracer::renderPixels (reference src/VCMTracer.cpp:6-143) for a fixed number of
  * iterations: film_rgb receives the running mean of the vignetting-corrected

@@ -153,6 +153,25 @@ class Context:
                                       ctypes.byref(st)))
         return film, sq, dict(extension_rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms)
 
+    def render_pt_batch(self, items, paths_per_pass: int = 0, use_graph: bool = True, autotune: bool = False):
+        """Renders several scenes in one wavefront. items: list of (Context, Camera,
+        dict(spp, max_depth, rr_mode, nee, seed)). Returns (list of (H,W,3) means, stats)."""
+        arr = (_capi.rx_batch_item * len(items))()
+        films = []
+        for k, (ctx, cam, o) in enumerate(items):
+            film = np.zeros((cam.height, cam.width, 3), np.float64)
+            films.append(film)
+            arr[k].scene = ctx.h
+            arr[k].camera = camera_struct(cam)
+            arr[k].options = rx_pt_options(o.get("spp", 16), o.get("max_depth", 8), o.get("rr_mode", 0),
+                                           int(bool(o.get("nee", False))), o.get("seed", 1), 0, 0)
+            arr[k].film_rgb = film.ctypes.data
+        bo = _capi.rx_batch_options(paths_per_pass, int(use_graph), int(autotune), 0, 0, 0)
+        st = rx_render_stats()
+        self._ck(self._L.rx_render_pt_batch(self.h, arr, len(items), ctypes.byref(bo), ctypes.byref(st)))
+        return films, dict(extension_rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms,
+                           blocks_per_sm=bo.chosen_blocks_per_sm, stack=bo.chosen_stack)
+
     def render_vcm(self, camera: "scenes.Camera", iterations: int, radius: float, alpha: float = 0.6667,
                    max_depth: int = 8, light_paths: int = 0, seed: int = 1):
         """VCMTracer renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats)."""
@@ -193,10 +212,12 @@ class Context:
 
     # ---- learned guiding ---------------------------------------------------------
     def guide_init(self, learning_rate: float = 5e-3, bsdf_fraction: float = 0.5, batch: int = 1 << 18,
-                   train_passes: int = 4, steps_per_pass: int = 4, seed: int = 1, box=None):
+                   train_passes: int = 4, steps_per_pass: int = 4, warmup_passes: int = 0, seed: int = 1, box=None):
         """Creates the guiding network (seeded weights). box = (min xyz, max xyz) of the
-        position encoding, default the scene bounds."""
-        o = _capi.rx_guide_options(learning_rate, bsdf_fraction, batch, train_passes, steps_per_pass, 0, seed)
+        position encoding, default the scene bounds. The first warmup_passes passes of a
+        guided render sample by the BSDF alone; the first train_passes passes train."""
+        o = _capi.rx_guide_options(learning_rate, bsdf_fraction, batch, train_passes, steps_per_pass, warmup_passes,
+                                   seed)
         b = None if box is None else np.ascontiguousarray(np.concatenate([box[0], box[1]]), np.float32)
         self._ck(self._L.rx_guide_init(self.h, ctypes.byref(o), _capi.ptr(b)))
 

@@ -42,6 +42,17 @@ class rx_pt_options(ctypes.Structure):
                 ("flags", ctypes.c_uint32)]
 
 
+class rx_batch_item(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("camera", rx_camera), ("options", rx_pt_options),
+                ("film_rgb", ctypes.c_void_p)]
+
+
+class rx_batch_options(ctypes.Structure):
+    _fields_ = [("paths_per_pass", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("autotune", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("chosen_blocks_per_sm", ctypes.c_int32),
+                ("chosen_stack", ctypes.c_int32)]
+
+
 class rx_vcm_options(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("light_paths", ctypes.c_uint32),
                 ("flags", ctypes.c_uint32), ("radius", ctypes.c_float), ("alpha", ctypes.c_float),
@@ -55,8 +66,8 @@ class rx_render_stats(ctypes.Structure):
 
 class rx_guide_options(ctypes.Structure):
     _fields_ = [("learning_rate", ctypes.c_float), ("bsdf_fraction", ctypes.c_float), ("batch", ctypes.c_uint32),
-                ("train_passes", ctypes.c_uint32), ("steps_per_pass", ctypes.c_uint32), ("flags", ctypes.c_uint32),
-                ("seed", ctypes.c_uint64)]
+                ("train_passes", ctypes.c_uint32), ("steps_per_pass", ctypes.c_uint32),
+                ("warmup_passes", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
 
 
 class rx_build_options(ctypes.Structure):
@@ -95,6 +106,7 @@ SIGNATURES = [
     ("rx_trace_read_timing", S, [P, P, P]),
     ("rx_render_pt", S, [P, P, P, P, P, P]),
     ("rx_render_vcm", S, [P, P, P, P, P]),
+    ("rx_render_pt_batch", S, [P, P, U32, P, P]),
 ]
 
 

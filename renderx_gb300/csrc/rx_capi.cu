@@ -361,6 +361,56 @@ rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options*
   return RX_OK;
 }
 
+rx_status rx_render_pt_batch(rx_context* c, const rx_batch_item* items, uint32_t n, rx_batch_options* opts,
+                             rx_render_stats* stats) {
+  if (!c) return RX_ERR_INVALID;
+  if (!items || n == 0) return c->fail(RX_ERR_INVALID, "empty batch");
+  if (n > 65535) return c->fail(RX_ERR_INVALID, "at most 65535 scenes per batch");
+  std::vector<rx::PtJob> jobs(n);
+  uint64_t pixels = 0;
+  for (uint32_t k = 0; k < n; k++) {
+    const rx_batch_item& it = items[k];
+    if (!it.scene || !it.film_rgb) return c->fail(RX_ERR_INVALID, "batch item without scene or film");
+    if (!it.scene->scene_ready) return c->fail(RX_ERR_STATE, "batch item scene not built");
+    if (it.scene->device != c->device) return c->fail(RX_ERR_INVALID, "batch scenes must share the device");
+    const rx_camera& cam = it.camera;
+    if (cam.width == 0 || cam.height == 0 || cam.sight_dist == 0) return c->fail(RX_ERR_INVALID, "bad camera");
+    if (it.options.spp == 0 || it.options.max_depth > 1000) return c->fail(RX_ERR_INVALID, "bad spp or max_depth");
+    if (it.options.nee && it.scene->scene.num_lights == 0)
+      return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
+    jobs[k] = rx::PtJob{it.scene, cam, it.options, pixels};
+    jobs[k].opt.flags = 0;
+    pixels += (uint64_t)cam.width * cam.height;
+  }
+  DeviceGuard g(c->device);
+  DevBuf film;
+  rx_status s;
+  if ((s = c->cuda(film.alloc(pixels * 3 * sizeof(double)), "film")) != RX_OK) return s;
+  cudaMemsetAsync(film.p, 0, film.bytes, c->stream);
+  rx::PtRun run;
+  run.paths_per_pass = opts ? opts->paths_per_pass : 0;
+  run.use_graph = opts ? opts->use_graph != 0 : true;
+  run.autotune = opts ? opts->autotune != 0 : false;
+  rx::PtShape shape;
+  rx_render_stats st{};
+  if ((s = c->cuda(rx::render_pt_jobs(c, jobs.data(), (int)n, run, film.as<double>(), nullptr, &st, &shape, c->stream),
+                   "render_pt_batch")) != RX_OK)
+    return s;
+  std::vector<double> h(pixels * 3);
+  if ((s = c->cuda(cudaMemcpy(h.data(), film.p, film.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
+  for (uint32_t k = 0; k < n; k++) {
+    size_t np = (size_t)items[k].camera.width * items[k].camera.height * 3;
+    const double* src = h.data() + jobs[k].film_base * 3;
+    for (size_t q = 0; q < np; q++) items[k].film_rgb[q] = src[q] / items[k].options.spp;
+  }
+  if (opts) {
+    opts->chosen_blocks_per_sm = shape.blocks_per_sm;
+    opts->chosen_stack = shape.stack;
+  }
+  if (stats) *stats = st;
+  return RX_OK;
+}
+
 rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_options* opts, double* film_rgb,
                         rx_render_stats* stats) {
   if (!c) return RX_ERR_INVALID;

@@ -437,14 +437,30 @@ __global__ void __launch_bounds__(128) k_guide_infer(IO io, const unsigned* coun
 }
 
 // ---- training --------------------------------------------------------------------------
+// The records a training step reads: with step >= 0, the step-th window of `len` records
+// of the live count (device count clipped to n_host, wrapping); else [first, first + len)
+// clipped to n_host.
+__device__ __forceinline__ void train_window(const unsigned* count, uint32_t n_host, uint32_t first, uint32_t len,
+                                             int step, uint32_t& lo, uint32_t& hi) {
+  uint32_t n = count ? min(*count, n_host) : n_host;
+  if (step >= 0) {
+    uint32_t L = min(len, n);
+    lo = n > len ? (uint32_t)(((uint64_t)step * len) % (n - len + 1)) : 0u;
+    hi = lo + L;
+  } else {
+    lo = min(first, n);
+    hi = min(first + len, n);
+  }
+}
+
 // Sum of record weights and number of records (for the loss normalisation).
 __global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t n_host, uint32_t first,
-                             uint32_t len, float* out) {
-  uint32_t n = count ? *count : n_host;
-  uint32_t end = min(first + len, n);
+                             uint32_t len, int step, float* out) {
+  uint32_t lo, end;
+  train_window(count, n_host, first, len, step, lo, end);
   float acc = 0.0f;
   unsigned c = 0;
-  for (uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+  for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
     acc += recs[(size_t)i * kRec + 12];
     c++;
   }
@@ -463,16 +479,17 @@ __global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t 
 // flushed once per CTA into `grad` (FP32, row-major per layer). wsum = {sum w, count}.
 // Weights are clipped at 32 x their batch mean before normalisation by the sum.
 __global__ void __launch_bounds__(128, 1) k_guide_train(const float* recs, const unsigned* count, uint32_t n_host,
-                                                        uint32_t first, uint32_t len, const unsigned char* img, Box box,
-                                                        const float* wsum, float* grad, float* loss_sum, int* status) {
+                                                        uint32_t first0, uint32_t len, int step, const unsigned char* img,
+                                                        Box box, const float* wsum, float* grad, float* loss_sum,
+                                                        int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar_mma, bar_w;
   __shared__ uint32_t tmem_base;
   __shared__ float red[4];
   const int s = threadIdx.x, warp = s >> 5;
-  const uint32_t n_all = count ? *count : n_host;
-  const uint32_t end = min(first + len, n_all);
-  const uint32_t n = end > first ? end - first : 0;
+  uint32_t first, end;
+  train_window(count, n_host, first0, len, step, first, end);
+  const uint32_t n = end - first;
   const uint32_t ntiles = (n + kTile - 1) / kTile;
   if (blockIdx.x >= ntiles) return;
   if (s == 0) {
@@ -694,6 +711,7 @@ bool guide_ready(const GuideState* g) { return g && g->ready; }
 float guide_bsdf_fraction(const GuideState* g) { return g->opt.bsdf_fraction; }
 uint32_t guide_train_passes(const GuideState* g) { return g->opt.train_passes; }
 uint32_t guide_steps_per_pass(const GuideState* g) { return g->opt.steps_per_pass; }
+uint32_t guide_warmup_passes(const GuideState* g) { return g->opt.warmup_passes; }
 
 // Opts the network kernels into their shared-memory sizes, once per device.
 static void set_kernel_smem() {
@@ -716,17 +734,18 @@ cudaError_t guide_infer_paths(GuideState* g, const DevScene& S, const PathSoA& P
   return cudaGetLastError();
 }
 
-// One Adam step on records [first, first + len) of `recs` (live count on the device or n).
+// One Adam step (or, without update, the gradient alone) on the records a window
+// selects (train_window).
 static cudaError_t train_step(GuideState* g, const float* recs, const unsigned* count, uint32_t n, uint32_t first,
-                              uint32_t len, cudaStream_t s, bool update) {
+                              uint32_t len, int step, cudaStream_t s, bool update) {
   set_kernel_smem();
   float* sc = g->scratch.as<float>();
   cudaMemsetAsync(sc, 0, 3 * sizeof(float), s);
-  k_weight_sum<<<g->sms * 4, 256, 0, s>>>(recs, count, n, first, len, sc);
-  uint32_t tiles = (len + kTile - 1) / kTile;
+  k_weight_sum<<<g->sms * 4, 256, 0, s>>>(recs, count, n, first, len, step, sc);
+  uint32_t tiles = (std::min(len, n) + kTile - 1) / kTile;
   uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)g->sms);
   if (grid == 0) return cudaGetLastError();
-  k_guide_train<<<grid, 128, kSmTrain, s>>>(recs, count, n, first, len, g->img.as<unsigned char>(), g->box, sc,
+  k_guide_train<<<grid, 128, kSmTrain, s>>>(recs, count, n, first, len, step, g->img.as<unsigned char>(), g->box, sc,
                                             g->grad.as<float>(), sc + 2, g->status.as<int>());
   if (update) {
     g->step++;
@@ -741,17 +760,9 @@ static cudaError_t train_step(GuideState* g, const float* recs, const unsigned* 
 
 cudaError_t guide_train_records(GuideState* g, const float* recs, const unsigned* count, uint32_t n_max, int steps,
                                 cudaStream_t s) {
-  unsigned n = 0;
-  cudaError_t e = cudaMemcpyAsync(&n, count, sizeof n, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return e;
-  n = std::min(n, n_max);
-  uint32_t B = g->opt.batch;
-  if (n < 1024) return cudaSuccess;  // too few samples to learn from
-  for (int k = 0; k < steps && e == cudaSuccess; k++) {
-    uint32_t first = n > B ? (uint32_t)(((uint64_t)k * B) % (n - B + 1)) : 0;
-    e = train_step(g, recs, nullptr, n, first, std::min(B, n), s, true);
-  }
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < steps && e == cudaSuccess; k++)
+    e = train_step(g, recs, count, n_max, 0, g->opt.batch, k, s, true);
   return e;
 }
 
@@ -905,7 +916,7 @@ extern "C" rx_status rx_guide_gradient(rx_context* c, const float* recs, uint32_
   if ((s = c->cuda(dr.alloc((size_t)n * rx::guide::kRec * 4), "alloc")) != RX_OK) return s;
   cudaMemcpy(dr.p, recs, (size_t)n * rx::guide::kRec * 4, cudaMemcpyHostToDevice);
   cudaMemsetAsync(g->grad.p, 0, rx::guide::kParams * 4, c->stream);
-  cudaError_t e = rx::train_step(g, dr.as<float>(), nullptr, n, 0, n, c->stream, false);
+  cudaError_t e = rx::train_step(g, dr.as<float>(), nullptr, n, 0, n, -1, c->stream, false);
   if ((s = c->cuda(e, "guide gradient")) != RX_OK) return s;
   if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide gradient")) != RX_OK) return s;
   if ((s = guide_status(c)) != RX_OK) return s;
@@ -922,7 +933,7 @@ extern "C" rx_status rx_guide_train_step(rx_context* c, const float* d_recs, uin
   if (reinterpret_cast<uintptr_t>(d_recs) % 16) return c->fail(RX_ERR_INVALID, "records must be 16-byte aligned");
   DeviceGuard dg(c->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  cudaError_t e = rx::train_step(c->guide, d_recs, nullptr, n, 0, n, st, true);
+  cudaError_t e = rx::train_step(c->guide, d_recs, nullptr, n, 0, n, -1, st, true);
   if ((s = c->cuda(e, "guide train step")) != RX_OK) return s;
   if (loss) {
     if ((s = c->cuda(cudaStreamSynchronize(st), "guide train step")) != RX_OK) return s;

@@ -79,12 +79,15 @@ void guide_free(GuideState* g);
 // whose hit is a guided surface, writes its mixture (guide::kLobeStride floats) to `lobes`.
 cudaError_t guide_infer_paths(GuideState* g, const DevScene& S, const PathSoA& P, const unsigned* count,
                               const int2* hit, float* lobes, int grid, cudaStream_t s);
-// Trains on the `n_max`-capacity record buffer whose live count is device-resident.
+// `steps` Adam steps on the record buffer whose live count (at most n_max) is device-
+// resident: step k trains on a window of `batch` records picked on the device, so no
+// host synchronisation is needed.
 cudaError_t guide_train_records(GuideState* g, const float* recs, const unsigned* count, uint32_t n_max,
                                 int steps, cudaStream_t s);
 bool guide_ready(const GuideState* g);
 float guide_bsdf_fraction(const GuideState* g);
 uint32_t guide_train_passes(const GuideState* g);
 uint32_t guide_steps_per_pass(const GuideState* g);
+uint32_t guide_warmup_passes(const GuideState* g);
 
 }  // namespace rx

@@ -314,7 +314,11 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
           if (!killed && !capped) {
             T = T * cos_term(SC, P.cam, nx);
             done = false;
-            rec = guided && G.recs;
+            // a training sample: a sampled direction at a diffuse / glossy / Phong
+            // surface seen from outside any object
+            uint32_t m = SC.objects[hh.obj].material;
+            rec = G.recs && cur.inside == kNone && (nx.flags & kDirRandom) && nx.contact == hh.obj &&
+                  (m == kDiffuse || m == kGlossy || m == kPhong);
           }
         } else if (is_emissive(SC, nx.contact)) {
           // PathTracerTest.cpp:37-56: two-sided emission, MIS against light sampling
@@ -632,7 +636,9 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     const int grid = sms * best.blocks_per_sm;
     for (; pass < npasses; pass++) {
       const bool training = G.recs && pass < guide_train_passes(c->guide);
+      const bool use_guide = pass >= guide_warmup_passes(c->guide);
       GuideIO Gp = G;
+      if (!use_guide) Gp.lobes = nullptr;
       if (!training) {
         Gp.recs = nullptr;
         Gp.lpath = nullptr;
@@ -645,7 +651,8 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       unsigned *cc = W.cnt, *cn = W.cnt + 1;
       for (uint32_t d = 0; d < W.loops; d++) {
         k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, W.hit, W.ctr);
-        if ((e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, 2 * sms, s)) != cudaSuccess) return e;
+        if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, 2 * sms, s)) != cudaSuccess)
+          return e;
         k_zero<<<1, 1, 0, s>>>(cn);
         k_shade<kStackDepth><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
         std::swap(cur, nxt);

@@ -116,52 +116,53 @@ def _relmse(img, ref):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-def test_guided_render_matches_reference_pathtracer():
-    """Guided sampling (network trained during the first passes of the same render) is
-    unbiased: it agrees with the reference's own PathTracer render of the Cornell box
-    under the per-pixel 3-sigma criteria of the plain path-tracing parity test."""
-    from renderx_gb300 import scenes
-    from test_render_gpu import compare, load_case
+def test_guided_render_is_unbiased():
+    """Guided sampling (network trained during the first passes of the same render, after
+    BSDF-only warm-up passes) keeps the estimator's expectation: per pixel it agrees
+    with a high-sample plain render within 3 sigma (at most 1% of channels, none beyond
+    8), and its image mean agrees with the reference's own PathTracer render of the
+    Cornell box within 4 standard errors."""
+    from test_render_gpu import load_case
     z, sc = load_case("cornell_pt")
     spp = 8192
     with rx.Context(0) as ctx:
         ctx.set_scene(sc)
         ctx.build_accel()
-        ctx.guide_init(seed=3, batch=1 << 16, train_passes=6, steps_per_pass=8)
-        mean, sq, st = ctx.render_pt(sc.camera, spp, max_depth=int(z["max_depth"]), rr_mode=0, seed=777,
-                                     want_sq=True, guided=True, paths_per_pass=1 << 18)
-    var = np.maximum(sq - mean * mean, 0.0) * spp / (spp - 1)
-    se = np.sqrt(var / spp)
-    ref, rse = z["mean"].astype(np.float64), z["stderr"].astype(np.float64)
-    zz, bad = compare(mean, se, ref, rse)
-    assert bad.mean() <= 0.01, f"{bad.mean():.4f} of channels beyond 3 sigma (max z {zz.max():.1f})"
+        ref, ref_sq, _ = ctx.render_pt(sc.camera, 131072, max_depth=8, rr_mode=0, seed=1, want_sq=True)
+        ctx.guide_init(seed=3, batch=1 << 16, warmup_passes=4, train_passes=8, steps_per_pass=8)
+        mean, sq, st = ctx.render_pt(sc.camera, spp, max_depth=8, rr_mode=0, seed=777, want_sq=True, guided=True,
+                                     paths_per_pass=1 << 18)
+    se = np.sqrt(np.maximum(sq - mean * mean, 0.0) / (spp - 1))
+    rse = np.sqrt(np.maximum(ref_sq - ref * ref, 0.0) / (131072 - 1))
+    zz = np.abs(mean - ref) / (np.sqrt(se ** 2 + rse ** 2) + 1e-12)
+    assert (zz > 3).mean() <= 0.01, f"{(zz > 3).mean():.4f} of channels beyond 3 sigma (max z {zz.max():.1f})"
     assert (zz > 8).sum() == 0
+    gold, gse = z["mean"].astype(np.float64), z["stderr"].astype(np.float64)
     n = mean.shape[0] * mean.shape[1]
     for c in range(3):
-        dm = mean[..., c].mean() - ref[..., c].mean()
-        s_img = np.sqrt((se[..., c] ** 2).sum() + (rse[..., c] ** 2).sum()) / n
+        dm = mean[..., c].mean() - gold[..., c].mean()
+        s_img = np.sqrt((se[..., c] ** 2).sum() + (gse[..., c] ** 2).sum()) / n
         assert abs(dm) < 4 * s_img, (c, dm, s_img)
 
 
 def test_guiding_gain_on_glossy_workload():
-    """Equal-work comparison on the glossy workload (60% glossy spheres, 1%-area light):
-    the guided path tracer, training time included, reaches a lower relMSE per unit of
-    render time than plain BSDF sampling, against a high-sample FP64 reference."""
+    """Equal-sample comparison on the glossy workload (60% glossy spheres, light of 1% of
+    the ceiling): the guided path tracer, training and inference time included, needs
+    well under the render time of plain BSDF sampling for the same relMSE against a
+    high-sample FP64 reference (relMSE x time, which is constant for an unbiased
+    estimator at a fixed sampler, below 0.6 of plain's)."""
     from renderx_gb300 import scenes
     sc = scenes.guiding_scene(128, 128, n_spheres=40, subdiv=3, seed=2)
-    depth = 8
     with rx.Context(0) as ctx:
         ctx.set_scene(sc)
         ctx.build_accel()
-        ctx.guide_init(seed=1, batch=1 << 16, train_passes=8, steps_per_pass=8)
-        ref, _, _ = ctx.render_pt(sc.camera, 8192, max_depth=depth, rr_mode=1, seed=99, guided=True,
-                                  paths_per_pass=1 << 20)
-        ctx.guide_init(seed=1, batch=1 << 16, train_passes=8, steps_per_pass=8)
-        spp = 256
-        plain, _, sp = ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=5, paths_per_pass=1 << 18)
-        guided, _, sg = ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=6, guided=True,
+        ref, _, _ = ctx.render_pt(sc.camera, 32768, max_depth=8, rr_mode=1, seed=1)
+        spp = 1024
+        plain, _, sp = ctx.render_pt(sc.camera, spp, max_depth=8, rr_mode=1, seed=5, paths_per_pass=1 << 18)
+        ctx.guide_init(seed=1, batch=1 << 16, warmup_passes=4, train_passes=12, steps_per_pass=8)
+        guided, _, sg = ctx.render_pt(sc.camera, spp, max_depth=8, rr_mode=1, seed=6, guided=True,
                                       paths_per_pass=1 << 18)
     e_plain = _relmse(plain, ref) * sp["ms"]
     e_guided = _relmse(guided, ref) * sg["ms"]
     print(f"relMSE x ms: plain {e_plain:.4g} ({sp['ms']:.1f} ms), guided {e_guided:.4g} ({sg['ms']:.1f} ms)")
-    assert e_guided < e_plain, (e_guided, e_plain)
+    assert e_guided < 0.6 * e_plain, (e_guided, e_plain)
