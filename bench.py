@@ -12,6 +12,17 @@ whole batch. Synthetic seeded data stand in for the reference's (unshipped) scen
   cpu_baseline : the oracle's CPU restatement of the reference traversal on the host
           cores, on a bounded sample of the same batch.
 
+Secondary sections of the same JSON line (each skippable):
+  pt      : wavefront PathTracer on the same scene, 1024^2 x 64 spp, depth 16, Russian
+            roulette from depth 3: Mrays/s (extension + shadow rays), samples/s.
+  guiding : the glossy workload (60% glossy spheres, exponent log-U[100,1000], light of
+            1% of the ceiling): plain vs guided PathTracer at equal samples, relMSE
+            against a high-sample FP64 render, relMSE x time (lower is better).
+  mlp     : the guiding network's tensor-core kernels alone: training step on 2^18
+            records and inference on 2^20 queries, TFLOP/s against the BF16 peak.
+  vcm     : VCMTracer with the homogeneous-medium scene, 512^2, 2^20 light paths per
+            iteration: ms per iteration.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
 from __future__ import annotations
@@ -35,6 +46,17 @@ N_SPHERES, SUBDIV, SCENE_SEED, RAY_SEED = 200, 5, 1, 7
 METRIC = "closest-hit Mrays/s (2^24-ray batch, 4.1M-triangle scene)"
 UNIT = "Mrays/s"
 WORKLOAD = "hit_batch_2^24_rays_cornell+200_icospheres_4096036_tris"
+
+
+TRAFFIC_BYTES_PER_RAY = 646.2e6 / (1 << 20)
+
+
+def load_tflops():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"])
+    return 1900.0
 
 
 def load_peaks():
@@ -94,6 +116,106 @@ def make_workload(rank: int):
     f = sc.flatten()
     o, d = scenes.hit_rays(N_RAYS, seed=RAY_SEED + rank)  # N_RAYS may be reset by --rays
     return sc, f, o, d
+
+
+def _relmse(img, ref):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def section_pt(ctx, sc, peak):
+    """C1: plain wavefront PathTracer at 1024^2 x 64 spp, depth 16, RR from depth 3."""
+    spp, depth = 64, 16
+    ctx.render_pt(sc.camera, 1, max_depth=depth, rr_mode=1, seed=3)  # warm-up
+    film, _, st = ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=4)
+    rays = st["extension_rays"] + st["shadow_rays"]
+    s = st["ms"] * 1e-3
+    # algorithmic bytes: 40 per traced ray, 96 per shade event (path state read + write),
+    # 24 per pixel for the FP64 film
+    alg = 40 * rays + 96 * st["extension_rays"] + 24 * sc.camera.width * sc.camera.height
+    return {"workload": f"PathTracer {sc.camera.width}x{sc.camera.height} x {spp} spp, depth {depth}, "
+                        "4,096,036 triangles", "ms": st["ms"], "mrays_per_s": rays / s / 1e6,
+            "samples_per_s": st["paths"] / s, "extension_rays": st["extension_rays"],
+            "shadow_rays": st["shadow_rays"], "image_mean": [float(x) for x in film.mean(axis=(0, 1))],
+            "roofline": {"bound": "hbm", "achieved": alg / s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / s / 1e9 / peak}}
+
+
+def section_guiding(res: int, ref_spp: int, spp: int):
+    """C4 glossy workload at res^2: plain vs guided PathTracer at equal samples."""
+    import renderx_gb300 as rx
+    from renderx_gb300 import scenes
+    sc = scenes.guiding_scene(res, res, 200, 5, seed=1)
+    out = {"workload": f"glossy guiding workload {res}x{res}, 4,096,036 triangles, depth 16, RR from depth 3",
+           "reference_spp": ref_spp, "spp": spp}
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ref, _, st = ctx.render_pt(sc.camera, ref_spp, max_depth=16, rr_mode=1, seed=1)
+        out["reference_ms"] = st["ms"]
+        plain, _, sp = ctx.render_pt(sc.camera, spp, max_depth=16, rr_mode=1, seed=5)
+        ctx.guide_init(seed=1, learning_rate=5e-3, batch=1 << 18, warmup_passes=2, train_passes=10, steps_per_pass=8)
+        guided, _, sg = ctx.render_pt(sc.camera, spp, max_depth=16, rr_mode=1, seed=6, guided=True,
+                                      paths_per_pass=1 << 19)
+    rp, rg = _relmse(plain, ref), _relmse(guided, ref)
+    out.update({"plain": {"ms": sp["ms"], "relmse": rp, "relmse_x_s": rp * sp["ms"] * 1e-3},
+                "guided": {"ms": sg["ms"], "relmse": rg, "relmse_x_s": rg * sg["ms"] * 1e-3},
+                "time_to_equal_relmse_ratio": (rg * sg["ms"]) / (rp * sp["ms"])})
+    return out
+
+
+def section_mlp(ctx, peak_tflops):
+    """The guiding network's kernels alone, on device-resident records."""
+    import torch
+    rng = np.random.default_rng(1)
+    n_train, n_inf = 1 << 18, 1 << 20
+    recs = np.zeros((n_inf, 16), np.float32)
+    recs[:, 0:3] = rng.random((n_inf, 3)) * 5.56
+    for k in (3, 6, 9):
+        v = rng.normal(size=(n_inf, 3))
+        recs[:, k:k + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    recs[:, 12] = rng.exponential(1.0, n_inf)
+    d = torch.from_numpy(recs).cuda()
+    raw = torch.empty((n_inf, 40), dtype=torch.float32, device="cuda")
+    ctx.guide_init(seed=1, batch=n_train, box=((0, 0, 0), (5.56, 5.56, 5.56)))
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        ctx.guide_train_step(d.data_ptr(), n_train, stream=stream.cuda_stream, want_loss=False)
+        ctx.guide_eval_device(d, n_inf, raw, None, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    k = 20
+    e[0].record(stream)
+    for _ in range(k):
+        ctx.guide_train_step(d.data_ptr(), n_train, stream=stream.cuda_stream, want_loss=False)
+    e[1].record(stream)
+    for _ in range(k):
+        ctx.guide_eval_device(d, n_inf, raw, None, stream=stream.cuda_stream)
+    e[2].record(stream)
+    torch.cuda.synchronize()
+    t_train = e[0].elapsed_time(e[1]) / k
+    t_inf = e[1].elapsed_time(e[2]) / k
+    macs = 80 * 64 + 3 * 64 * 64 + 64 * 40  # 19,968 per sample
+    f_train = 3 * 2 * macs * n_train / (t_train * 1e-3) / 1e12
+    f_inf = 2 * macs * n_inf / (t_inf * 1e-3) / 1e12
+    return {"train_step_ms": t_train, "train_records": n_train, "train_tflops": f_train,
+            "infer_ms": t_inf, "infer_queries": n_inf, "infer_tflops": f_inf,
+            "roofline": {"bound": "tensor", "achieved": f_train, "peak": peak_tflops, "unit": "TFLOP/s",
+                         "frac": f_train / peak_tflops, "kernel": "k_guide_train (forward + backward, BF16 tcgen05)"}}
+
+
+def section_vcm(iters: int = 4):
+    """C2: VCMTracer, medium scene at 512^2, 2^20 light paths per iteration."""
+    import renderx_gb300 as rx
+    from renderx_gb300 import scenes
+    sc = scenes.medium_scene(512, 512)
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ctx.render_vcm(sc.camera, 1, 0.0963, 0.75, max_depth=16, light_paths=1 << 20, seed=1)
+        img, st = ctx.render_vcm(sc.camera, iters, 0.0963, 0.75, max_depth=16, light_paths=1 << 20, seed=2)
+    return {"workload": "VCMTracer, Cornell room + homogeneous-medium sphere, 512x512, 2^20 light paths/iter, "
+                        "depth 16, r0 0.0963, alpha 0.75", "iterations": iters, "ms": st["ms"],
+            "ms_per_iteration": st["ms"] / iters, "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
 def cpu_baseline(f, o, d, budget_s: float = 12.0):
@@ -157,7 +279,7 @@ def run_ours(args):
 
     sc, f, o, d = make_workload(rank)
     ctx = rx.Context(local)
-    ctx.set_geometry(f["verts"], f["tris"], f["tri_obj"], f["tri_local"])
+    ctx.set_scene(sc)
     t0 = time.perf_counter()
     ctx.build_accel()
     build_s = time.perf_counter() - t0
@@ -211,8 +333,24 @@ def run_ours(args):
     else:
         e2e, same = end_to_end(ctx, host_rays, d_tid, args, dist, ws, n)
 
+    extra = {}
     if rank == 0:
-        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms)
+        peak, _ = load_peaks()
+        tf = load_tflops()
+        for name, skip, fn in (("pt", args.skip_pt, lambda: section_pt(ctx, sc, peak)),
+                               ("mlp", args.skip_mlp, lambda: section_mlp(ctx, tf)),
+                               ("guiding", args.skip_guiding,
+                                lambda: section_guiding(args.guide_res, args.guide_ref_spp, args.guide_spp)),
+                               ("vcm", args.skip_vcm, lambda: section_vcm())):
+            if skip:
+                continue
+            t0 = time.perf_counter()
+            try:
+                extra[name] = fn()
+            except Exception as ex:  # a failing section is reported, not hidden
+                extra[name] = {"error": f"{type(ex).__name__}: {ex}"}
+            extra[name]["wall_s"] = round(time.perf_counter() - t0, 2)
+        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms, extra)
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -242,17 +380,15 @@ def end_to_end(ctx, host_rays, d_tid, args, dist, ws, n):
     return e2e, same
 
 
-def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms):
+def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms, extra):
     if True:
         peak, peak_kind = load_peaks()
         bytes_alg = 40 * n + 48 * st["triangles"] + 64 * st["bvh_nodes"]
         walk_ms = float(kern_ms[:, 0].mean()) if len(kern_ms) else ms_per_step
         achieved = bytes_alg / (walk_ms * 1e-3) / 1e9
-        traffic = None
-        tp = os.path.join(ROOT, "profiles", "hit_traffic.json")
-        if os.path.exists(tp):
-            with open(tp) as fh:
-                traffic = json.load(fh).get("dram_bytes_per_launch")
+        # DRAM bytes per ray of the walk kernel from the 2^20-ray profiler capture
+        # (profiles/k_trace_persistent_hit1M.md: 646.2 MB / 2^20 rays), scaled to this launch
+        traffic = TRAFFIC_BYTES_PER_RAY * n
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -271,6 +407,7 @@ def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_m
                                    "visibility_check": float(kern_ms[:, 1].mean()) if len(kern_ms) else None,
                                    "rewalk": float(kern_ms[:, 2].mean()) if len(kern_ms) else None},
                 "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms], "wall_s": wall}
+        line.update(extra)
         if not args.skip_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(f, o, d)
         print(json.dumps(line), flush=True)
@@ -285,8 +422,18 @@ def main():
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="batch size (profiler captures use a smaller one)")
+    ap.add_argument("--skip-pt", action="store_true")
+    ap.add_argument("--skip-mlp", action="store_true")
+    ap.add_argument("--skip-guiding", action="store_true")
+    ap.add_argument("--skip-vcm", action="store_true")
+    ap.add_argument("--skip-extra", action="store_true", help="skip every secondary section")
+    ap.add_argument("--guide-res", type=int, default=256)
+    ap.add_argument("--guide-ref-spp", type=int, default=4096)
+    ap.add_argument("--guide-spp", type=int, default=256)
     args = ap.parse_args()
     globals()["N_RAYS"] = args.rays
+    if args.skip_extra:
+        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = True
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -241,6 +241,12 @@ rx_status rx_render_vcm(rx_context* ctx, const rx_camera* cam, const rx_vcm_opti
  * leaf postponing; blocks of 128 threads, blocks_per_sm per SM. No reference
  * counterpart (launch tuning). */
 rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_per_sm);
+/* Closest-hit options (no reference counterpart): check_mode = how each walk's winner
+ * is checked for reference visibility, 1 = one thread per ray (default), 0 = one warp
+ * per ray (one ancestor box per lane); bin_min = batches of at least this many rays are
+ * reordered by origin cell and direction before the walk (counting sort), 0 = never
+ * (default 262144). Answers do not depend on either. */
+rx_status rx_trace_set_options(rx_context* ctx, int32_t check_mode, uint32_t bin_min);
 /* Per-kernel device timing of rx_trace_closest_device calls: the next max_calls calls
  * record CUDA events around their three kernels (walk, reference-visibility check,
  * re-walk of rejected winners); 0 turns timing off. No reference counterpart
@@ -268,6 +274,10 @@ rx_status rx_guide_set_params(rx_context* ctx, const float* params);
  * network outputs; pdf (n, optional) = the mixture density of each record's incident
  * direction. */
 rx_status rx_guide_eval(rx_context* ctx, const float* recs, uint32_t n, float* raw40, float* pdf);
+/* The same on device buffers (16-byte aligned records), enqueued on `stream` (NULL: the
+ * context's stream); d_raw40 / d_pdf may each be NULL. */
+rx_status rx_guide_eval_device(rx_context* ctx, const float* d_recs, uint32_t n, float* d_raw40, float* d_pdf,
+                               void* stream);
 /* Gradient (training kernel, no update) of the batch loss
  * -sum_s w_s log q(wi_s) / sum_s w_s (weights clipped at 32 x their mean) over n host
  * records: grad receives 21504 floats, *loss the loss. */

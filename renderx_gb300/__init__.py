@@ -185,6 +185,11 @@ class Context:
     def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
+    def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18):
+        """Visibility check of each winner (1 = thread per ray, 0 = warp per ray) and the
+        batch size from which rays are binned before the walk (0 = never)."""
+        self._ck(self._L.rx_trace_set_options(self.h, int(check_mode), int(bin_min)))
+
     def set_trace_timing(self, max_calls: int):
         """Record per-kernel CUDA events for the next ``max_calls`` device trace calls."""
         self._ck(self._L.rx_trace_set_timing(self.h, int(max_calls)))
@@ -239,6 +244,11 @@ class Context:
         pdf = np.zeros(n, np.float32)
         self._ck(self._L.rx_guide_eval(self.h, _capi.ptr(r), n, _capi.ptr(raw), _capi.ptr(pdf)))
         return raw, pdf
+
+    def guide_eval_device(self, d_recs, n: int, d_raw=None, d_pdf=None, stream=None):
+        """Forward pass on n device records (pointers or tensors), enqueued on ``stream``."""
+        self._ck(self._L.rx_guide_eval_device(self.h, _capi.ptr(d_recs), n, _capi.ptr(d_raw), _capi.ptr(d_pdf),
+                                              _capi.stream_arg(stream)))
 
     def guide_gradient(self, recs: np.ndarray):
         """(loss, gradient (21504,)) of the batch loss on (n, 16) records, no update."""

@@ -213,6 +213,11 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.num_ref_nodes = (uint32_t)c->ref.nodes.size();
   A.num_ref_leaves = (uint32_t)c->ref.leaf_node.size();
   A.prune_rel = 1e-3f;
+  for (int k = 0; k < 3; k++) {
+    const rx::BvhNodeHost& r = c->bvh.nodes[0];
+    A.lo[k] = std::min(r.c0lo[k], r.c1lo[k]);
+    A.hi[k] = std::max(r.c0hi[k], r.c1hi[k]);
+  }
   c->accel_ready = true;
   c->geometry_dirty = false;
   if (!c->objects.empty()) return c->build_scene();
@@ -451,8 +456,9 @@ rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {
 
 // Scratch of a closest-hit launch over n rays: n winner leaves + up to n queued rays.
 static rx_status ensure_queue(rx_context* c, size_t n) {
-  if (c->d_queue.bytes >= n * 8) return RX_OK;
-  return c->cuda(c->d_queue.alloc(std::max<size_t>(n, 1024) * 8), "allocate closest-hit scratch");
+  size_t need = rx::trace_scratch_bytes(std::max<size_t>(n, 1024));
+  if (c->d_queue.bytes >= need) return RX_OK;
+  return c->cuda(c->d_queue.alloc(need), "allocate closest-hit scratch");
 }
 
 rx_status rx_trace_closest_device(rx_context* c, const rx_ray* d_rays, uint32_t n, int32_t* d_tid, float* d_dist,
@@ -536,7 +542,7 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
       if ((s = c->cuda(c->ring_rays[k].alloc(chunk * sizeof(rx_ray)), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_tid[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_dist[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
-      if ((s = c->cuda(c->ring_queue[k].alloc(chunk * 8), "staging")) != RX_OK) return s;
+      if ((s = c->cuda(c->ring_queue[k].alloc(rx::trace_scratch_bytes(chunk)), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_counters[k].alloc(8 * sizeof(unsigned long long)), "staging")) != RX_OK) return s;
       cudaMemset(c->ring_counters[k].p, 0, c->ring_counters[k].bytes);
     }
@@ -567,6 +573,14 @@ rx_status rx_trace_set_config(rx_context* c, int32_t variant, int32_t blocks_per
     return c->fail(RX_ERR_INVALID, "variant must be 0..2 and blocks_per_sm 1..32");
   c->trace_cfg.variant = variant;
   c->trace_cfg.blocks_per_sm = blocks_per_sm;
+  return RX_OK;
+}
+
+rx_status rx_trace_set_options(rx_context* c, int32_t check_mode, uint32_t bin_min) {
+  if (!c) return RX_ERR_INVALID;
+  if (check_mode != 0 && check_mode != 1) return c->fail(RX_ERR_INVALID, "check_mode must be 0 or 1");
+  c->trace_cfg.check_thread = check_mode;
+  c->trace_cfg.bin_min = bin_min;
   return RX_OK;
 }
 

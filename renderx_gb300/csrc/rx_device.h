@@ -28,6 +28,7 @@ struct DevAccel {
   const int32_t* anc_nodes;        // per leaf, its root path (leaf first) as node ids
   uint32_t num_nodes, num_tris, num_ref_nodes, num_ref_leaves;
   float prune_rel;                 // pruning margin: t_limit = best + prune_rel*(1+best)
+  float lo[3], hi[3];              // scene bounds (ray binning)
 };
 
 }  // namespace rx

@@ -906,6 +906,25 @@ extern "C" rx_status rx_guide_eval(rx_context* c, const float* recs, uint32_t n,
   return RX_OK;
 }
 
+extern "C" rx_status rx_guide_eval_device(rx_context* c, const float* d_recs, uint32_t n, float* d_raw40, float* d_pdf,
+                                          void* stream) {
+  rx_status s = need_guide(c);
+  if (s != RX_OK) return s;
+  if (n == 0) return RX_OK;
+  if (!d_recs || (!d_raw40 && !d_pdf)) return c->fail(RX_ERR_INVALID, "null buffer");
+  if (reinterpret_cast<uintptr_t>(d_recs) % 16) return c->fail(RX_ERR_INVALID, "records must be 16-byte aligned");
+  DeviceGuard dg(c->device);
+  rx::GuideState* g = c->guide;
+  rx::set_kernel_smem();
+  rx::RecordIO io{d_recs, d_raw40, d_pdf};
+  uint32_t tiles = (n + rx::guide::kTile - 1) / rx::guide::kTile;
+  uint32_t grid = std::min<uint32_t>(tiles, 2u * (uint32_t)g->sms);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  rx::k_guide_infer<rx::RecordIO><<<grid, 128, rx::kSmInfer, st>>>(io, nullptr, n, g->img.as<unsigned char>(), g->box,
+                                                                    g->status.as<int>());
+  return c->cuda(cudaGetLastError(), "guide eval");
+}
+
 extern "C" rx_status rx_guide_gradient(rx_context* c, const float* recs, uint32_t n, float* grad, float* loss) {
   rx_status s = need_guide(c);
   if (s != RX_OK) return s;

@@ -22,6 +22,8 @@ struct TraceConfig {
   int blocks_per_sm = 12;
   int sms = 152;
   int pt_blocks_per_sm = 8;  // wavefront extend / shade kernels
+  int check_thread = 1;      // reference-visibility check: 1 = thread per ray, 0 = warp per ray
+  uint32_t bin_min = 1u << 18;  // bin rays before the walk from this batch size on (0 = never)
 };
 
 // Launch shape of the wavefront's extend / shade kernels: blocks of 128 threads per SM
@@ -31,11 +33,17 @@ struct PtShape {
   int stack = 64;
 };
 
-// Launchers (rx_trace.cu). `ev` (optional): four events recorded before the walk
-// kernel, after it, after the visibility check and after the re-walk.
+// Scratch of a closest-hit launch over n rays (rx_trace.cu): winner leaves, re-walk
+// queue, and the ray binning's keys, permutation and bin counters.
+constexpr uint32_t kRayBins = 1u << 18;
+inline size_t trace_scratch_bytes(size_t n) { return n * 16 + (size_t)kRayBins * 4; }
+// Launchers (rx_trace.cu). `queue`: trace_scratch_bytes(n) bytes, or 8 n bytes when
+// `bin` is false. bin: reorder rays by origin cell and direction before the walk (for
+// large batches). `ev` (optional): four events recorded before the walk kernel, after
+// it, after the visibility check and after the re-walk.
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                  uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
-                                 cudaStream_t s, const cudaEvent_t* ev = nullptr);
+                                 cudaStream_t s, const cudaEvent_t* ev = nullptr, bool bin = true);
 cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                   unsigned long long* counters, cudaStream_t s);
 

@@ -64,7 +64,8 @@ extern "C" rx_status rx_trace_closest_noalloc(rx_context* c, const rx_ray* d_ray
     auto* queue = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + kCounterBytes);
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     // the launcher clears the queue length and the batch cursor before its kernels
-    e = rx::launch_trace_closest(c->accel, d_rays, n, d_tid, d_dist, queue, counters, c->trace_cfg, st);
+    e = rx::launch_trace_closest(c->accel, d_rays, n, d_tid, d_dist, queue, counters, c->trace_cfg, st, nullptr,
+                                 false);
   }
   if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
   return c->cuda(e, "trace_closest_noalloc");

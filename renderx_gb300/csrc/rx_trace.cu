@@ -52,6 +52,46 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
   if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
 }
 
+// The same check with one thread per ray: each thread walks its winner's ancestor list
+// (four boxes per step); the lists and boxes of the reference tree are a few hundred KB
+// and stay in L1/L2. Rays whose winner fails go to the eager queue (warp-aggregated).
+__global__ void __launch_bounds__(128) k_check_visible_thread(DevAccel A, const rx_ray* __restrict__ rays,
+                                                              uint32_t n, const uint32_t* __restrict__ order,
+                                                              const uint32_t* __restrict__ hit_leaf,
+                                                              uint32_t* __restrict__ eager_queue,
+                                                              unsigned long long* __restrict__ counters) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  unsigned n_exact = 0;
+  for (uint32_t it = 0; it < iters; it++) {
+    uint32_t j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t i = j < n && order ? __ldg(&order[j]) : j;  // binned order: a warp checks nearby leaves
+    bool fail = false;
+    if (j < n) {
+      uint32_t leaf = __ldg(&hit_leaf[i]);
+      if (leaf != kNoLeaf) {
+        const float4* rp = reinterpret_cast<const float4*>(rays + i);
+        F3 o = f3(__ldg(rp)), d = f3(__ldg(rp + 1));
+        bool zd = (d.x == 0.0f) | (d.y == 0.0f) | (d.z == 0.0f);
+        fail = !ref_visible(A, leaf, o, d, safe_inv(d), zd, &n_exact);
+      }
+    }
+    unsigned m = __ballot_sync(FULL, fail);
+    if (m) {
+      unsigned long long base = 0;
+      int leader = __ffs(m) - 1;
+      if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (fail) eager_queue[base + __popc(m & ((1u << lane) - 1))] = i;  // at most n entries
+    }
+  }
+  unsigned sum = n_exact;
+  for (int s2 = 16; s2 > 0; s2 >>= 1) sum += __shfl_xor_sync(FULL, sum, s2);
+  if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
+}
+
 // One thread per ray. Writes the winner and its reference leaf; k_check_visible then
 // confirms the winner is visible to the reference.
 __global__ void __launch_bounds__(128) k_trace_closest(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
@@ -89,6 +129,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevAccel A, const rx_ray*
 // visibility together. counters[4] is the batch cursor.
 template <bool SPEC>
 __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                          const uint32_t* __restrict__ order,
                                                           int32_t* __restrict__ out_tid,
                                                           float* __restrict__ out_dist,
                                                           uint32_t* __restrict__ hit_leaf,
@@ -133,7 +174,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
       if (!active && !exhausted) {
         unsigned long long r = base + __popc(want & ((1u << lane) - 1));
         if (r < n) {
-          ray = (uint32_t)r;
+          ray = order ? __ldg(&order[r]) : (uint32_t)r;
           const float4* rp = reinterpret_cast<const float4*>(rays + ray);
           float4 ro = __ldg(rp), rd = __ldg(rp + 1);
           o = f3(ro);
@@ -303,14 +344,86 @@ __global__ void __launch_bounds__(128) k_trace_reforder(DevAccel A, const rx_ray
   out_dist[i] = have ? bt : -1.0f;
 }
 
+// ---- ray binning: counting sort by (origin cell, direction bin) ---------------------
+// Key: Morton code of the origin's cell on a 16^3 grid over the scene bounds (12 bits),
+// then the direction quantised to 4 levels per axis (6 bits). Rays of one bin start
+// close together and head the same way, so a warp's walks stay coherent.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 4 bits -> every third bit
+  v &= 15u;
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+__device__ __forceinline__ uint32_t ray_key(const DevAccel& A, float4 o, float4 d) {
+  float p[3] = {o.x, o.y, o.z}, q[3] = {d.x, d.y, d.z};
+  uint32_t cell[3], dir[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float t = (p[k] - A.lo[k]) / fmaxf(A.hi[k] - A.lo[k], 1e-20f) * 16.0f;
+    cell[k] = (uint32_t)fminf(fmaxf(t, 0.0f), 15.0f);
+    dir[k] = (uint32_t)fminf(fmaxf((q[k] + 1.0f) * 2.0f, 0.0f), 3.0f);
+  }
+  uint32_t morton = spread3(cell[0]) | (spread3(cell[1]) << 1) | (spread3(cell[2]) << 2);
+  return (morton << 6) | (dir[0] << 4) | (dir[1] << 2) | dir[2];
+}
+
+__global__ void k_ray_keys(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ hist) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4* rp = reinterpret_cast<const float4*>(rays + i);
+    uint32_t k = ray_key(A, __ldg(rp), __ldg(rp + 1));
+    keys[i] = k;
+    atomicAdd(&hist[k], 1u);
+  }
+}
+
+// Exclusive prefix sum of the kRayBins counters, in place, by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_bins(uint32_t* hist) {
+  constexpr uint32_t per = kRayBins / 1024;
+  __shared__ uint32_t part[1024];
+  const uint32_t t = threadIdx.x;
+  uint32_t* h = hist + t * per;
+  uint32_t sum = 0;
+  for (uint32_t k = 0; k < per; k++) sum += h[k];
+  part[t] = sum;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
+    uint32_t v = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - sum;
+  for (uint32_t k = 0; k < per; k++) {
+    uint32_t c = h[k];
+    h[k] = run;
+    run += c;
+  }
+}
+
+__global__ void k_ray_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
+                              uint32_t* __restrict__ order) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    order[atomicAdd(&cursor[keys[i]], 1u)] = i;
+}
+
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                  uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
-                                 cudaStream_t s, const cudaEvent_t* ev) {
+                                 cudaStream_t s, const cudaEvent_t* ev, bool bin) {
   if (n == 0) return cudaSuccess;
   cudaMemsetAsync(counters, 0, sizeof(unsigned long long), s);  // eager queue length
   uint32_t* hit_leaf = queue;  // scratch: n entries of winners' reference leaves
   uint32_t* eager = queue + n;  // then up to n queued rays
   if (cfg.variant != 0) cudaMemsetAsync(counters + 4, 0, sizeof(unsigned long long), s);  // batch cursor
+  const uint32_t* order = nullptr;
+  if (bin && cfg.variant != 0 && cfg.bin_min && n >= cfg.bin_min) {
+    uint32_t* keys = queue + 2 * (size_t)n;
+    uint32_t* perm = queue + 3 * (size_t)n;
+    uint32_t* hist = queue + 4 * (size_t)n;
+    cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), s);
+    k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist);
+    k_scan_bins<<<1, 1024, 0, s>>>(hist);
+    k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, hist, perm);
+    order = perm;
+  }
   if (ev) cudaEventRecord(ev[0], s);
   if (cfg.variant == 0) {
     k_trace_closest<<<(n + 127) / 128, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
@@ -319,12 +432,15 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     unsigned need = (n + 127) / 128;
     blocks = blocks < need ? blocks : need;
     if (cfg.variant == 1)
-      k_trace_persistent<false><<<blocks, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
+      k_trace_persistent<false><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
     else
-      k_trace_persistent<true><<<blocks, 128, 0, s>>>(A, rays, n, tid, dist, hit_leaf, counters);
+      k_trace_persistent<true><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
   }
   if (ev) cudaEventRecord(ev[1], s);
-  k_check_visible<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, hit_leaf, eager, counters);
+  if (cfg.check_thread)
+    k_check_visible_thread<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, order, hit_leaf, eager, counters);
+  else
+    k_check_visible<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, hit_leaf, eager, counters);
   if (ev) cudaEventRecord(ev[2], s);
   k_trace_eager<<<cfg.sms, 128, 0, s>>>(A, rays, tid, dist, eager, counters);
   if (ev) cudaEventRecord(ev[3], s);

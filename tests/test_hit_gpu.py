@@ -19,10 +19,12 @@ def _bits_equal(a, b):
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("leaf_size", [1, 4, 8])
 @pytest.mark.parametrize("variant", [0, 1])
-def test_hits_match_reference_golden(name, leaf_size, variant):
+@pytest.mark.parametrize("check", [0, 1])
+def test_hits_match_reference_golden(name, leaf_size, variant, check):
     z = load(name)
     with rx.Context(0) as ctx:
         ctx.set_trace_config(variant, 4)
+        ctx.set_trace_options(check, 64 if check else 0)  # bin even the small golden batches
         ctx.set_geometry(z["verts"], z["tris"])
         ctx.build_accel(rx.SPLIT_GCC, leaf_size=leaf_size)
         tid, dist = ctx.trace_closest(z["origins"], z["dirs"])
