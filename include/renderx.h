@@ -91,7 +91,7 @@ typedef struct rx_pt_options {
   uint32_t nee;            /* 0: PathTracer (BSDF sampling only); 1: PathTracerTest
                               (light sampling + balance-heuristic MIS) */
   uint64_t seed;
-  uint32_t paths_per_pass; /* wavefront size, 0 = 2^21 */
+  uint32_t paths_per_pass; /* wavefront size, 0 = 2^22 */
   uint32_t flags;          /* RX_PT_GUIDED or 0 */
 } rx_pt_options;
 
@@ -123,7 +123,7 @@ typedef struct rx_batch_item {
 } rx_batch_item;
 
 typedef struct rx_batch_options {
-  uint32_t paths_per_pass; /* wavefront size shared by all scenes, 0 = 2^21 */
+  uint32_t paths_per_pass; /* wavefront size shared by all scenes, 0 = 2^22 */
   uint32_t use_graph;      /* 1: capture one pass as a CUDA graph and replay it */
   uint32_t autotune;       /* 1: time the launch-shape candidates on the first passes */
   uint32_t reserved;

@@ -159,10 +159,12 @@ struct PtJob {
   uint64_t film_base;
 };
 struct PtRun {
-  uint32_t paths_per_pass = 0;  // 0 = 2^21
+  uint32_t paths_per_pass = 0;  // 0 = 2^22
   bool guided = false;          // one scene only
   bool use_graph = true;        // replay a captured pass
   bool autotune = false;        // time launch shapes on the first passes
+  bool bin = false;             // bin bounce rays by origin cell and direction before each extend
+                                // (measured slower for path tracing: off)
 };
 // Renders all jobs in one wavefront into device films (sum, optional sum of squares).
 cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun& run, double* film_sum,

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <vector>
 
+#include "rx_bin.cuh"
 #include "rx_guide.h"
 #include "rx_internal.h"
 #include "rx_material.cuh"
@@ -99,12 +100,27 @@ __global__ void k_generate(const SceneRec* R, int nr, PassState* ps, PathSoA S, 
   }
 }
 
+// Bin keys of the live paths' next rays (counting sort input; rx_bin.cuh).
+__global__ void k_path_keys(const SceneRec* R, PathSoA S, const unsigned* count, uint32_t* keys, uint32_t* hist) {
+  uint32_t n = *count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const DevAccel& A = R[(uint32_t)S.info[i].w >> 16].S.accel;
+    uint32_t k = ray_key(A.lo, A.hi, S.o[i], S.d[i]);
+    keys[i] = k;
+    atomicAdd(&hist[k], 1u);
+  }
+}
+
+// Closest legal hit of each live path's ray; `order` (optional) visits the paths in
+// binned order.
 template <int STACK>
-__global__ void __launch_bounds__(128) k_extend(const SceneRec* R, PathSoA S, const unsigned* count, int2* hit,
+__global__ void __launch_bounds__(128) k_extend(const SceneRec* R, PathSoA S, const unsigned* count,
+                                                const uint32_t* __restrict__ order, int2* hit,
                                                 unsigned long long* rays) {
   uint32_t n = *count;
   uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    uint32_t i = order ? __ldg(&order[j]) : j;
     float4 o = S.o[i], d = S.d[i];
     int4 inf = S.info[i];
     bool camera = (inf.w & 255) == 0;  // the camera ray's first query has no condition
@@ -486,7 +502,18 @@ struct Wave {
   unsigned* cnt;            // [0], [1] queue lengths, [2] records, [3] weighted records
   double *film, *sq;
   uint32_t loops;           // bounce stages per pass (max depth cap + 1)
+  uint32_t *keys, *order, *hist;  // ray binning of bounce rays (null: off)
 };
+
+// Bins the queue's rays (bounces after the camera rays) and returns the visiting order.
+const uint32_t* enqueue_binning(const Wave& W, PathSoA cur, const unsigned* cc, int grid, cudaStream_t s) {
+  if (!W.order) return nullptr;
+  cudaMemsetAsync(W.hist, 0, kRayBins * sizeof(uint32_t), s);
+  k_path_keys<<<grid, 256, 0, s>>>(W.R, cur, cc, W.keys, W.hist);
+  k_scan_bins<<<1, 1024, 0, s>>>(W.hist);
+  k_ray_scatter<<<grid, 256, 0, s>>>(W.keys, 0, cc, W.hist, W.order);
+  return W.order;
+}
 
 // One pass: generate, `loops` x (extend, clear the next queue, shade), advance the cursor.
 // Everything is a kernel on `s` with device-resident counts, so the pass can be captured
@@ -497,7 +524,8 @@ void enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
   PathSoA cur = W.A, nxt = W.B;
   unsigned *cc = W.cnt, *cn = W.cnt + 1;
   for (uint32_t d = 0; d < W.loops; d++) {
-    k_extend<STACK><<<grid, 128, 0, s>>>(W.R, cur, cc, W.hit, W.ctr);
+    const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
+    k_extend<STACK><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
     k_zero<<<1, 1, 0, s>>>(cn);
     k_shade<STACK><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, GuideIO{});
     std::swap(cur, nxt);
@@ -528,7 +556,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     max_depth = std::max(max_depth, jobs[k].opt.max_depth);
     max_bvh_depth = std::max<uint32_t>(max_bvh_depth, (uint32_t)jobs[k].ctx->bvh.max_depth);
   }
-  uint32_t per_pass = run.paths_per_pass ? run.paths_per_pass : (1u << 21);
+  uint32_t per_pass = run.paths_per_pass ? run.paths_per_pass : (1u << 22);
   per_pass = (uint32_t)std::min<uint64_t>(per_pass, total);
   if (per_pass == 0) return cudaSuccess;
   const uint64_t npasses = (total + per_pass - 1) / per_pass;
@@ -559,6 +587,11 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   if (!(W.ctr = static_cast<unsigned long long*>(alloc(64 * sizeof(unsigned long long))))) return e;
   W.cnt = reinterpret_cast<unsigned*>(W.ctr + 8);
   cudaMemsetAsync(W.ctr, 0, 64 * sizeof(unsigned long long), s);
+  if (run.bin && per_pass >= c->trace_cfg.bin_min && c->trace_cfg.bin_min) {
+    if (!(W.keys = static_cast<uint32_t*>(alloc((size_t)per_pass * 4)))) return e;
+    if (!(W.order = static_cast<uint32_t*>(alloc((size_t)per_pass * 4)))) return e;
+    if (!(W.hist = static_cast<uint32_t*>(alloc((size_t)kRayBins * 4)))) return e;
+  }
 
   // guiding (one scene): mixture per live path, training records, per-path radiance
   const bool guided = run.guided && nj == 1 && guide_ready(c->guide) && !jobs[0].opt.nee;
@@ -650,11 +683,18 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       PathSoA cur = W.A, nxt = W.B;
       unsigned *cc = W.cnt, *cn = W.cnt + 1;
       for (uint32_t d = 0; d < W.loops; d++) {
-        k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, W.hit, W.ctr);
+        const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
+        if (best.stack == 32)
+          k_extend<32><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
+        else
+          k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
         if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, 2 * sms, s)) != cudaSuccess)
           return e;
         k_zero<<<1, 1, 0, s>>>(cn);
-        k_shade<kStackDepth><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
+        if (best.stack == 32)
+          k_shade<32><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
+        else
+          k_shade<kStackDepth><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
         std::swap(cur, nxt);
         std::swap(cc, cn);
       }

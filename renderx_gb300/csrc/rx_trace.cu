@@ -1,5 +1,6 @@
 // Closest-hit kernels (reference KDTree::intersect over a ray batch).
 #include "rx_internal.h"
+#include "rx_bin.cuh"
 #include "rx_trace.cuh"
 
 namespace rx {
@@ -344,32 +345,12 @@ __global__ void __launch_bounds__(128) k_trace_reforder(DevAccel A, const rx_ray
   out_dist[i] = have ? bt : -1.0f;
 }
 
-// ---- ray binning: counting sort by (origin cell, direction bin) ---------------------
-// Key: Morton code of the origin's cell on a 16^3 grid over the scene bounds (12 bits),
-// then the direction quantised to 4 levels per axis (6 bits). Rays of one bin start
-// close together and head the same way, so a warp's walks stay coherent.
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 4 bits -> every third bit
-  v &= 15u;
-  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
-}
-__device__ __forceinline__ uint32_t ray_key(const DevAccel& A, float4 o, float4 d) {
-  float p[3] = {o.x, o.y, o.z}, q[3] = {d.x, d.y, d.z};
-  uint32_t cell[3], dir[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    float t = (p[k] - A.lo[k]) / fmaxf(A.hi[k] - A.lo[k], 1e-20f) * 16.0f;
-    cell[k] = (uint32_t)fminf(fmaxf(t, 0.0f), 15.0f);
-    dir[k] = (uint32_t)fminf(fmaxf((q[k] + 1.0f) * 2.0f, 0.0f), 3.0f);
-  }
-  uint32_t morton = spread3(cell[0]) | (spread3(cell[1]) << 1) | (spread3(cell[2]) << 2);
-  return (morton << 6) | (dir[0] << 4) | (dir[1] << 2) | dir[2];
-}
-
+// ---- ray binning (rx_bin.cuh): counting sort by (origin cell, direction bin) --------
 __global__ void k_ray_keys(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n, uint32_t* __restrict__ keys,
                            uint32_t* __restrict__ hist) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    uint32_t k = ray_key(A, __ldg(rp), __ldg(rp + 1));
+    uint32_t k = ray_key(A.lo, A.hi, __ldg(rp), __ldg(rp + 1));
     keys[i] = k;
     atomicAdd(&hist[k], 1u);
   }
@@ -399,8 +380,9 @@ __global__ void __launch_bounds__(1024) k_scan_bins(uint32_t* hist) {
   }
 }
 
-__global__ void k_ray_scatter(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cursor,
-                              uint32_t* __restrict__ order) {
+__global__ void k_ray_scatter(const uint32_t* __restrict__ keys, uint32_t n_host, const unsigned* count,
+                              uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
+  const uint32_t n = count ? *count : n_host;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     order[atomicAdd(&cursor[keys[i]], 1u)] = i;
 }
@@ -421,7 +403,7 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), s);
     k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist);
     k_scan_bins<<<1, 1024, 0, s>>>(hist);
-    k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, hist, perm);
+    k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, nullptr, hist, perm);
     order = perm;
   }
   if (ev) cudaEventRecord(ev[0], s);
