@@ -185,6 +185,41 @@ rx_status rx_reftree_serialize(const float* verts_xyz, uint32_t nv, const uint32
                                int32_t split_policy, float* nodes12, uint32_t* num_nodes, float* leaf_tid,
                                uint32_t* num_leaf_tris);
 
+/* ---- scene files ------------------------------------------------------------------ */
+/* What a config file asks for (ConfigManager::load, reference src/ConfigManager.cpp:166-405). */
+typedef struct rx_config_info {
+  char renderer[32];       /* <Renderer><type> as written ("PT", "PTtest", "VCM", ...) */
+  int32_t estimator;       /* 0 PathTracer, 1 PathTracerTest, 2 VCMTracer, -1 other */
+  uint32_t max_depth;      /* <maxDepth>, default 20 (MCRenderer) */
+  uint32_t spp;            /* <spp>, 0 if absent */
+  float radius;            /* <radius> (VCM merge radius), 0 if absent */
+  double runtime_s;        /* <time> hours and minutes, in seconds */
+  uint32_t num_objects, num_triangles;
+  rx_camera camera;        /* the <Camera> the config names */
+  char save_path[256];     /* <savePath>, empty if absent */
+} rx_config_info;
+
+typedef struct rx_host_scene rx_host_scene;
+/* Reads a config file, its scene file(s) and meshes (OBJ / .shp) into host arrays, the
+ * geometry Scene::buildKDTree would see (objects concatenated, world space) and the
+ * object table of ConfigManager::generateSceneObject. No device, no context. err
+ * (optional) receives a message on failure. */
+rx_status rx_config_read(const char* config_path, rx_host_scene** out, rx_config_info* info, char* err,
+                         size_t err_len);
+void rx_host_scene_free(rx_host_scene* scene);
+/* Views of a host scene's arrays (valid until rx_host_scene_free); *vnormals is NULL when
+ * no mesh has vertex normals. Any output pointer may be NULL. */
+rx_status rx_host_scene_arrays(const rx_host_scene* scene, const float** verts_xyz, uint32_t* nv,
+                               const uint32_t** tri_vidx, uint32_t* nt, const uint32_t** tri_obj,
+                               const uint32_t** tri_local, const float** vnormals_xyz, const rx_object** objs,
+                               uint32_t* nobj);
+/* rx_config_read, then rx_scene_set_geometry and rx_scene_set_objects on ctx (call
+ * rx_build_accel next). */
+rx_status rx_scene_load_config(rx_context* ctx, const char* config_path, rx_config_info* info);
+/* MCRenderer::saveImagePFM (reference src/MCRenderer.cpp:556-574): width*height*3 RGB
+ * values, rows from the top, written as a little-endian PFM with rows from the bottom. */
+rx_status rx_write_pfm(const char* path, uint32_t width, uint32_t height, const double* rgb);
+
 /* ---- closest hit --------------------------------------------------------------- */
 /* KDTree::intersect(ray, triangleID, NULL) (reference include/KDTree.h:50,
  * src/KDTree.cpp:408-412) over a batch, host buffers: out_tid[i] = global triangle id

@@ -51,6 +51,53 @@ def reftree_serialize(verts: np.ndarray, tris: np.ndarray, policy: int = SPLIT_G
     return nodes, leaf
 
 
+def config_read(path: str) -> tuple[dict, dict]:
+    """rx_config_read: the library's C++ reader of the reference's config / scene XML and
+    meshes (host only). Returns (arrays: verts, tris, tri_obj, tri_local, normals or None,
+    objects (list of rx_object), info dict)."""
+    L = _capi.lib()
+    h = ctypes.c_void_p()
+    info = _capi.rx_config_info()
+    err = ctypes.create_string_buffer(512)
+    st = L.rx_config_read(path.encode(), ctypes.byref(h), ctypes.byref(info), err, len(err))
+    if st != 0:
+        raise RxError(st, err.value.decode())
+    try:
+        pv, pt, po, pl, pn, pob = (ctypes.c_void_p() for _ in range(6))
+        nv, nt, nobj = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _capi.check(None, L.rx_host_scene_arrays(h, ctypes.byref(pv), ctypes.byref(nv), ctypes.byref(pt),
+                                                 ctypes.byref(nt), ctypes.byref(po), ctypes.byref(pl),
+                                                 ctypes.byref(pn), ctypes.byref(pob), ctypes.byref(nobj)))
+
+        def arr(p, n, ct, shape):
+            if not p.value or n == 0:
+                return np.zeros(shape, np.dtype(ct))
+            buf = (ct * n).from_address(p.value)
+            return np.ctypeslib.as_array(buf).reshape(shape).copy()
+        out = dict(verts=arr(pv, 3 * nv.value, ctypes.c_float, (nv.value, 3)),
+                   tris=arr(pt, 3 * nt.value, ctypes.c_uint32, (nt.value, 3)),
+                   tri_obj=arr(po, nt.value, ctypes.c_uint32, (nt.value,)),
+                   tri_local=arr(pl, nt.value, ctypes.c_uint32, (nt.value,)),
+                   normals=arr(pn, 3 * nv.value, ctypes.c_float, (nv.value, 3)) if pn.value else None,
+                   objects=[rx_object.from_buffer_copy((rx_object * nobj.value).from_address(pob.value)[k])
+                            for k in range(nobj.value)])
+    finally:
+        L.rx_host_scene_free(h)
+    c = info.camera
+    meta = dict(renderer=info.renderer.decode(), estimator=info.estimator, max_depth=info.max_depth, spp=info.spp,
+                radius=info.radius, runtime_s=info.runtime_s, num_objects=info.num_objects,
+                num_triangles=info.num_triangles, save_path=info.save_path.decode(),
+                camera=scenes.Camera(c.width, c.height, c.sight_dist, tuple(c.position), tuple(c.focus), tuple(c.up)))
+    return out, meta
+
+
+def write_pfm(path: str, rgb: np.ndarray):
+    """rx_write_pfm: MCRenderer::saveImagePFM of an (H, W, 3) image (rows from the top)."""
+    a = np.ascontiguousarray(rgb, np.float64)
+    h, w, _ = a.shape
+    _capi.check(None, _capi.lib().rx_write_pfm(path.encode(), w, h, _capi.ptr(a)))
+
+
 class Context:
     """One device, one stream: rx_create / rx_destroy."""
 
@@ -94,6 +141,17 @@ class Context:
     def set_objects(self, objs):
         arr = (rx_object * max(1, len(objs)))(*objs)
         self._ck(self._L.rx_scene_set_objects(self.h, ctypes.cast(arr, ctypes.c_void_p), len(objs)))
+
+    def load_config(self, path: str) -> dict:
+        """rx_scene_load_config: the reference's config / scene XML and meshes straight
+        into this context (then build_accel). Returns the config's renderer settings."""
+        info = _capi.rx_config_info()
+        self._ck(self._L.rx_scene_load_config(self.h, path.encode(), ctypes.byref(info)))
+        c = info.camera
+        return dict(renderer=info.renderer.decode(), estimator=info.estimator, max_depth=info.max_depth,
+                    spp=info.spp, radius=info.radius, runtime_s=info.runtime_s,
+                    camera=scenes.Camera(c.width, c.height, c.sight_dist, tuple(c.position), tuple(c.focus),
+                                         tuple(c.up)))
 
     def set_scene(self, scene: "scenes.Scene"):
         """Uploads a scenes.Scene: geometry (object-major, as Scene::buildKDTree) and

@@ -42,6 +42,13 @@ class rx_pt_options(ctypes.Structure):
                 ("flags", ctypes.c_uint32)]
 
 
+class rx_config_info(ctypes.Structure):
+    _fields_ = [("renderer", ctypes.c_char * 32), ("estimator", ctypes.c_int32), ("max_depth", ctypes.c_uint32),
+                ("spp", ctypes.c_uint32), ("radius", ctypes.c_float), ("runtime_s", ctypes.c_double),
+                ("num_objects", ctypes.c_uint32), ("num_triangles", ctypes.c_uint32), ("camera", rx_camera),
+                ("save_path", ctypes.c_char * 256)]
+
+
 class rx_batch_item(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("camera", rx_camera), ("options", rx_pt_options),
                 ("film_rgb", ctypes.c_void_p)]
@@ -89,6 +96,11 @@ SIGNATURES = [
     ("rx_build_accel", S, [P, P]),
     ("rx_accel_stats", S, [P, P]),
     ("rx_reftree_serialize", S, [P, U32, P, U32, I32, P, P, P, P]),
+    ("rx_config_read", S, [ctypes.c_char_p, ctypes.POINTER(P), P, P, ctypes.c_size_t]),
+    ("rx_host_scene_free", None, [P]),
+    ("rx_host_scene_arrays", S, [P, P, P, P, P, P, P, P, P, P]),
+    ("rx_scene_load_config", S, [P, ctypes.c_char_p, P]),
+    ("rx_write_pfm", S, [ctypes.c_char_p, U32, U32, P]),
     ("rx_trace_closest", S, [P, P, U32, P, P]),
     ("rx_trace_closest_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_closest_noalloc", S, [P, P, U32, P, P, P]),

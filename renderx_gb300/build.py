@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librenderx_gb300.so")
+CLI = os.path.join(HERE, "rx_render")  # command-line renderer over the library (cli/rx_render.cpp)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -51,7 +52,8 @@ def _stale() -> bool:
         return True
     t = os.path.getmtime(LIB)
     deps = glob.glob(os.path.join(CSRC, "*")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
-    return any(os.path.getmtime(d) > t for d in deps)
+    deps += glob.glob(os.path.join(HERE, "cli", "*"))
+    return not os.path.exists(CLI) or any(os.path.getmtime(d) > t for d in deps)
 
 
 def build(force: bool = False, ptxas_verbose: bool = False, quiet: bool = True) -> str:
@@ -72,6 +74,12 @@ def build(force: bool = False, ptxas_verbose: bool = False, quiet: bool = True) 
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(HERE, "..", "include"), os.path.join(HERE, "cli", "rx_render.cpp"),
+           "-o", CLI + ".tmp", "-L", HERE, "-lrenderx_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cli build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

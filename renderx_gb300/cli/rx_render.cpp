@@ -1,0 +1,95 @@
+// rx_render: render a scene described by the reference's config file, as the reference's
+// Renderer::loadConfig + MCRenderer::renderPixels + saveImagePFM do (reference
+// src/Renderer.cpp:47-126, src/ConfigManager.cpp:166-405), through the C ABI.
+//
+//   rx_render config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N]
+//             [--alpha A] [--seed S] [--guided] [--device D]
+//
+// The renderer type comes from the config (PathTracer / PT, PTtest, VCMTracer / VCM).
+// The reference renders until its <time> budget runs out; here a fixed sample count
+// (--spp, else <spp>, else 16) or VCM iteration count (--iterations, default 8) is used.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "renderx.h"
+
+static int fail(rx_context* c, const char* what) {
+  fprintf(stderr, "rx_render: %s: %s\n", what, c ? rx_last_error(c) : "");
+  if (c) rx_destroy(c);
+  return 1;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 2 || !strcmp(argv[1], "-h") || !strcmp(argv[1], "--help")) {
+    fprintf(stderr,
+            "usage: %s config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N] [--alpha A]\n"
+            "       [--seed S] [--guided] [--device D]\n",
+            argv[0]);
+    return 2;
+  }
+  std::string cfg = argv[1], out;
+  uint32_t spp = 0, iters = 8, light_paths = 0;
+  float alpha = 0.6667f;
+  uint64_t seed = 1;
+  int device = 0;
+  bool guided = false;
+  for (int i = 2; i < argc; i++) {
+    std::string a = argv[i];
+    auto next = [&]() -> const char* { return i + 1 < argc ? argv[++i] : ""; };
+    if (a == "--out") out = next();
+    else if (a == "--spp") spp = (uint32_t)atoi(next());
+    else if (a == "--iterations") iters = (uint32_t)atoi(next());
+    else if (a == "--light-paths") light_paths = (uint32_t)atoi(next());
+    else if (a == "--alpha") alpha = (float)atof(next());
+    else if (a == "--seed") seed = strtoull(next(), nullptr, 10);
+    else if (a == "--device") device = atoi(next());
+    else if (a == "--guided") guided = true;
+    else {
+      fprintf(stderr, "rx_render: unknown option %s\n", a.c_str());
+      return 2;
+    }
+  }
+  rx_context* c = nullptr;
+  if (rx_create(&c, device) != RX_OK) return fail(nullptr, "no CUDA device");
+  rx_config_info info;
+  auto t0 = std::chrono::steady_clock::now();
+  if (rx_scene_load_config(c, cfg.c_str(), &info) != RX_OK) return fail(c, "loading the config");
+  rx_build_options bo = {0, 4, 0, 0};
+  if (rx_build_accel(c, &bo) != RX_OK) return fail(c, "building the accelerator");
+  double load_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (out.empty()) out = info.save_path[0] ? info.save_path : "result.pfm";
+  const uint32_t w = info.camera.width, h = info.camera.height;
+  std::vector<double> film(3 * (size_t)w * h);
+  rx_render_stats st{};
+  if (info.estimator == 0 || info.estimator == 1) {
+    rx_pt_options po = {spp ? spp : (info.spp ? info.spp : 16u), info.max_depth, 0, (uint32_t)info.estimator, seed,
+                        0, 0};
+    if (guided) {
+      if (info.estimator != 0) return fail(c, "--guided applies to PathTracer");
+      rx_guide_options go = {5e-3f, 0.5f, 1u << 18, 4, 16, 1, seed};
+      if (rx_guide_init(c, &go, nullptr) != RX_OK) return fail(c, "guiding network");
+      po.flags = RX_PT_GUIDED;
+    }
+    if (rx_render_pt(c, &info.camera, &po, film.data(), nullptr, &st) != RX_OK) return fail(c, "rendering");
+    printf("%s: %u x %u, %u spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h, po.spp,
+           po.max_depth, st.ms, (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
+  } else if (info.estimator == 2) {
+    float r = info.radius > 0 ? info.radius : 0.01f;
+    rx_vcm_options vo = {iters, info.max_depth > 21 ? 21u : info.max_depth, light_paths, 0, r, alpha, seed};
+    if (rx_render_vcm(c, &info.camera, &vo, film.data(), &st) != RX_OK) return fail(c, "rendering");
+    printf("%s: %u x %u, %u iterations, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
+           iters, vo.max_depth, st.ms, (unsigned long long)st.extension_rays, load_s);
+  } else {
+    fprintf(stderr, "rx_render: renderer type '%s' is not on this library's path\n", info.renderer);
+    rx_destroy(c);
+    return 3;
+  }
+  if (rx_write_pfm(out.c_str(), w, h, film.data()) != RX_OK) return fail(c, "writing the image");
+  printf("wrote %s\n", out.c_str());
+  rx_destroy(c);
+  return 0;
+}
