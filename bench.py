@@ -122,17 +122,20 @@ def _relmse(img, ref):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-def section_pt(ctx, sc, peak):
+def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64):
     """C1: plain wavefront PathTracer at 1024^2 x 64 spp, depth 16, RR from depth 3."""
-    spp, depth = 64, 16
-    ctx.render_pt(sc.camera, 1, max_depth=depth, rr_mode=1, seed=3)  # warm-up
-    film, _, st = ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=4)
+    from dataclasses import replace
+    depth = 16
+    cam = sc.camera if res == sc.camera.width else replace(sc.camera, width=res, height=res,
+                                                            sight_dist=round(sc.camera.sight_dist * res / sc.camera.width))
+    ctx.render_pt(cam, 1, max_depth=depth, rr_mode=1, seed=3)  # warm-up
+    film, _, st = ctx.render_pt(cam, spp, max_depth=depth, rr_mode=1, seed=4)
     rays = st["extension_rays"] + st["shadow_rays"]
     s = st["ms"] * 1e-3
     # algorithmic bytes: 40 per traced ray, 96 per shade event (path state read + write),
     # 24 per pixel for the FP64 film
-    alg = 40 * rays + 96 * st["extension_rays"] + 24 * sc.camera.width * sc.camera.height
-    return {"workload": f"PathTracer {sc.camera.width}x{sc.camera.height} x {spp} spp, depth {depth}, "
+    alg = 40 * rays + 96 * st["extension_rays"] + 24 * cam.width * cam.height
+    return {"workload": f"PathTracer {cam.width}x{cam.height} x {spp} spp, depth {depth}, "
                         "4,096,036 triangles", "ms": st["ms"], "mrays_per_s": rays / s / 1e6,
             "samples_per_s": st["paths"] / s, "extension_rays": st["extension_rays"],
             "shadow_rays": st["shadow_rays"], "image_mean": [float(x) for x in film.mean(axis=(0, 1))],
@@ -213,18 +216,18 @@ def section_mlp(ctx, peak_tflops):
                          "frac": f_train / peak_tflops, "kernel": "k_guide_train (forward + backward, BF16 tcgen05)"}}
 
 
-def section_vcm(iters: int = 2):
+def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
     """C2: VCMTracer, medium scene at 512^2, 2^20 light paths per iteration."""
     import renderx_gb300 as rx
     from renderx_gb300 import scenes
-    sc = scenes.medium_scene(512, 512)
+    sc = scenes.medium_scene(res, res)
     with rx.Context(0) as ctx:
         ctx.set_scene(sc)
         ctx.build_accel()
-        ctx.render_vcm(sc.camera, 1, 0.0963, 0.75, max_depth=16, light_paths=1 << 20, seed=1)
-        img, st = ctx.render_vcm(sc.camera, iters, 0.0963, 0.75, max_depth=16, light_paths=1 << 20, seed=2)
-    return {"workload": "VCMTracer, Cornell room + homogeneous-medium sphere, 512x512, 2^20 light paths/iter, "
-                        "depth 16, r0 0.0963, alpha 0.75", "iterations": iters, "ms": st["ms"],
+        ctx.render_vcm(sc.camera, 1, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=1)
+        img, st = ctx.render_vcm(sc.camera, iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=2)
+    return {"workload": f"VCMTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, {light_paths} light "
+                        "paths/iter, depth 16, r0 0.0963, alpha 0.75", "iterations": iters, "ms": st["ms"],
             "ms_per_iteration": st["ms"] / iters, "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
@@ -347,11 +350,12 @@ def run_ours(args):
     if rank == 0:
         peak, _ = load_peaks()
         tf = load_tflops()
-        for name, skip, fn in (("pt", args.skip_pt, lambda: section_pt(ctx, sc, peak)),
+        for name, skip, fn in (("pt", args.skip_pt, lambda: section_pt(ctx, sc, peak, args.pt_res, args.pt_spp)),
                                ("mlp", args.skip_mlp, lambda: section_mlp(ctx, tf)),
                                ("guiding", args.skip_guiding,
                                 lambda: section_guiding(args.guide_res, args.guide_ref_spp, args.guide_spp)),
-                               ("vcm", args.skip_vcm, lambda: section_vcm())):
+                               ("vcm", args.skip_vcm,
+                                lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths))):
             if skip:
                 continue
             t0 = time.perf_counter()
@@ -440,6 +444,11 @@ def main():
     ap.add_argument("--guide-res", type=int, default=256)
     ap.add_argument("--guide-ref-spp", type=int, default=4096)
     ap.add_argument("--guide-spp", type=int, default=512)
+    ap.add_argument("--pt-res", type=int, default=1024, help="path-tracing section resolution (profiling: smaller)")
+    ap.add_argument("--pt-spp", type=int, default=64)
+    ap.add_argument("--vcm-res", type=int, default=512)
+    ap.add_argument("--vcm-light-paths", type=int, default=1 << 20)
+    ap.add_argument("--vcm-iters", type=int, default=2)
     args = ap.parse_args()
     globals()["N_RAYS"] = args.rays
     if args.skip_extra:
