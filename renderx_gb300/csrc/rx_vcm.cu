@@ -166,14 +166,15 @@ __global__ void k_grid_count(const float4* pos, const unsigned* n_photons, unsig
   }
 }
 // exclusive scan of `count` (n entries) into `start`, block-wise then over block sums
-__global__ void k_scan_blocks(const unsigned* count, unsigned* start, unsigned* block_sum, unsigned n) {
-  __shared__ unsigned s[1024];
+template <class T>
+__global__ void k_scan_blocks(const T* count, T* start, T* block_sum, unsigned n) {
+  __shared__ T s[1024];
   unsigned i = blockIdx.x * 1024 + threadIdx.x;
-  unsigned v = i < n ? count[i] : 0u;
+  T v = i < n ? count[i] : T(0);
   s[threadIdx.x] = v;
   __syncthreads();
   for (unsigned off = 1; off < 1024; off <<= 1) {
-    unsigned t = threadIdx.x >= off ? s[threadIdx.x - off] : 0u;
+    T t = threadIdx.x >= off ? s[threadIdx.x - off] : T(0);
     __syncthreads();
     s[threadIdx.x] += t;
     __syncthreads();
@@ -181,17 +182,18 @@ __global__ void k_scan_blocks(const unsigned* count, unsigned* start, unsigned* 
   if (i < n) start[i] = s[threadIdx.x] - v;
   if (threadIdx.x == 1023) block_sum[blockIdx.x] = s[1023];
 }
-__global__ void k_scan_sums(unsigned* block_sum, unsigned nb) {
+template <class T>
+__global__ void k_scan_sums(T* block_sum, unsigned nb) {
   // single block, sequential carry over chunks of 1024
-  __shared__ unsigned s[1024];
-  unsigned carry = 0;
+  __shared__ T s[1024];
+  T carry = 0;
   for (unsigned base = 0; base < nb; base += 1024) {
     unsigned i = base + threadIdx.x;
-    unsigned v = i < nb ? block_sum[i] : 0u;
+    T v = i < nb ? block_sum[i] : T(0);
     s[threadIdx.x] = v;
     __syncthreads();
     for (unsigned off = 1; off < 1024; off <<= 1) {
-      unsigned t = threadIdx.x >= off ? s[threadIdx.x - off] : 0u;
+      T t = threadIdx.x >= off ? s[threadIdx.x - off] : T(0);
       __syncthreads();
       s[threadIdx.x] += t;
       __syncthreads();
@@ -202,11 +204,12 @@ __global__ void k_scan_sums(unsigned* block_sum, unsigned nb) {
     __syncthreads();
   }
 }
-__global__ void k_scan_add(unsigned* start, const unsigned* block_sum, unsigned n, unsigned* cursor) {
+template <class T>
+__global__ void k_scan_add(T* start, const T* block_sum, unsigned n, T* cursor) {
   unsigned i = blockIdx.x * 1024 + threadIdx.x;
   if (i < n) {
     start[i] += block_sum[blockIdx.x];
-    cursor[i] = start[i];
+    if (cursor) cursor[i] = start[i];
   }
 }
 __global__ void k_grid_scatter(const unsigned* key, const unsigned* n_photons, unsigned cap, unsigned* cursor,
@@ -376,10 +379,11 @@ __device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
   atomicAdd(img + 3 * pixel + 2, c.z);
 }
 
-// ---- eye subpaths: merging and connecting ---------------------------------------------
+// ---- eye subpaths and connections ------------------------------------------------------
+// Per pixel: the eye subpath (stored for the merging stage) and colorByConnectingPaths
+// (VCMTracer.cpp:430-562) with this pixel's light path.
 __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const float4* lv, const int* llen,
-                                                 const float4* photon_pos, const int* photon_ref, Grid G,
-                                                 float* img, unsigned long long* rays) {
+                                                 float4* ev, int* elen, float* img, unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nrays = 0;
   const float r = P.radius;
@@ -391,51 +395,9 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
     PV start = camera_ray(S, P.cam, p, rng, h);
     int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, eye);
     nrays += (unsigned long long)ne;
+    for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
+    elen[p] = ne;
     F3 acc = {0, 0, 0};
-    // colorByMergingPaths (VCMTracer.cpp:566-636)
-    for (int ei = 1; ei < ne; ei++) {
-      if (is_emissive(S, eye[ei].contact)) break;
-      if (!(eye[ei].flags & kDirRandom)) continue;
-      F3 q = eye[ei].o;
-      F3 sum = {0, 0, 0};
-      // cells the sphere touches: two per axis in exact arithmetic (cell = 2r), up to
-      // three after rounding of the two divisions
-      int x0 = (int)floorf((q.x - r) / G.cell), y0 = (int)floorf((q.y - r) / G.cell), z0 = (int)floorf((q.z - r) / G.cell);
-      int x1 = min((int)floorf((q.x + r) / G.cell), x0 + 2), y1 = min((int)floorf((q.y + r) / G.cell), y0 + 2);
-      int z1 = min((int)floorf((q.z + r) / G.cell), z0 + 2);
-      unsigned seen[27];
-      int nseen = 0;
-      for (int cx = x0; cx <= x1; cx++)
-        for (int cy = y0; cy <= y1; cy++)
-          for (int cz = z0; cz <= z1; cz++) {
-            unsigned b = cell_hash(cx, cy, cz, G.mask);
-            bool dup = false;
-            for (int k = 0; k < nseen; k++) dup |= seen[k] == b;
-            if (dup || nseen >= 27) continue;
-            seen[nseen++] = b;
-            for (unsigned s = G.start[b]; s < G.start[b + 1]; s++) {
-              int ph = G.sorted[s];
-              F3 pp = f3(photon_pos[ph]);
-              if (!(length(q - pp) < r)) continue;
-              int ref = photon_ref[ph];
-              int lp = ref / (int)P.maxv, li = ref % (int)P.maxv;
-              // wholePath = light[0 .. li-1] + eye[ei .. 0]
-              int n = 0;
-              for (int k = 0; k < li; k++) w[n++] = load_pv(lv + 4 * ((size_t)lp * P.maxv + k));
-              for (int k = ei; k >= 0; k--) w[n++] = eye[k];
-              int ci = li - 1;
-              if (!connect_rays(S, P.cam, w, n, ci, true)) continue;
-              F3 col;
-              float prob;
-              connect_color_prob(S, P.cam, w, n, ci, true, r, col, prob);
-              if (length(col) == 0.0f || prob == 0.0f) continue;
-              float wt = connect_merge_weight(S, P.cam, w, n, ci, true, r, P.norm);
-              sum = sum + col * (wt / prob);
-            }
-          }
-      acc = acc + sum * (1.0f / P.norm);
-    }
-    // colorByConnectingPaths (VCMTracer.cpp:430-562) with this pixel's light path
     uint32_t lp = p % P.n_light;
     int nl = llen[lp];
     for (int whole = 2; whole <= ne + nl; whole++) {
@@ -488,6 +450,118 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
   if (nrays) atomicAdd(rays, nrays);
 }
 
+// ---- merging as a wavefront: queries, (query, photon) pairs, one pair per lane -------
+// colorByMergingPaths (VCMTracer.cpp:566-636): eye vertex ei of pixel p (query
+// q = p * maxv + ei) merges with every photon closer than r, for ei >= 1 up to the first
+// emitter, at vertices sampled at random. The grid walk visits every cell the sphere
+// touches (two per axis in exact arithmetic, up to three after rounding of the cell
+// divisions), each bucket once.
+template <class F>
+__device__ __forceinline__ void merge_walk(const Grid& G, const float4* photon_pos, F3 q, float r, F&& visit) {
+  int x0 = (int)floorf((q.x - r) / G.cell), y0 = (int)floorf((q.y - r) / G.cell), z0 = (int)floorf((q.z - r) / G.cell);
+  int x1 = min((int)floorf((q.x + r) / G.cell), x0 + 2), y1 = min((int)floorf((q.y + r) / G.cell), y0 + 2);
+  int z1 = min((int)floorf((q.z + r) / G.cell), z0 + 2);
+  unsigned seen[27];
+  int nseen = 0;
+  for (int cx = x0; cx <= x1; cx++)
+    for (int cy = y0; cy <= y1; cy++)
+      for (int cz = z0; cz <= z1; cz++) {
+        unsigned b = cell_hash(cx, cy, cz, G.mask);
+        bool dup = false;
+        for (int k = 0; k < nseen; k++) dup |= seen[k] == b;
+        if (dup || nseen >= 27) continue;
+        seen[nseen++] = b;
+        for (unsigned s = G.start[b]; s < G.start[b + 1]; s++) {
+          int ph = G.sorted[s];
+          if (length(q - f3(photon_pos[ph])) < r) visit(ph);
+        }
+      }
+}
+
+// The merge position of query q, or false if the eye vertex does not merge.
+__device__ __forceinline__ bool merge_query(const DevScene& S, const VcmParams& P, const float4* ev, const int* elen,
+                                            uint32_t q, F3& pos) {
+  uint32_t p = q / P.maxv;
+  int ei = (int)(q % P.maxv);
+  if (p >= P.n_pixels || ei < 1 || ei >= elen[p]) return false;
+  for (int k = 1; k <= ei; k++) {
+    PV v = load_pv(ev + 4 * ((size_t)p * P.maxv + k));
+    if (is_emissive(S, v.contact)) return false;  // the loop stops at the first emitter
+    if (k == ei) {
+      if (!(v.flags & kDirRandom)) return false;
+      pos = v.o;
+    }
+  }
+  return true;
+}
+
+__global__ void k_merge_count(DevScene S, VcmParams P, const float4* ev, const int* elen, const float4* photon_pos,
+                              Grid G, unsigned long long* qcount, uint32_t nq) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    F3 pos;
+    unsigned long long c = 0;
+    if (merge_query(S, P, ev, elen, q, pos)) merge_walk(G, photon_pos, pos, P.radius, [&](int) { c++; });
+    qcount[q] = c;
+  }
+}
+
+// Pairs [win0, win0 + cap) of the scanned order: query and photon of each.
+__global__ void k_merge_fill(DevScene S, VcmParams P, const float4* ev, const int* elen, const float4* photon_pos,
+                             Grid G, const unsigned long long* qoff, uint32_t nq, unsigned long long win0, uint32_t cap,
+                             uint32_t* pair_q, int* pair_ph) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    F3 pos;
+    if (!merge_query(S, P, ev, elen, q, pos)) continue;
+    unsigned long long idx = qoff[q];
+    merge_walk(G, photon_pos, pos, P.radius, [&](int ph) {
+      if (idx >= win0 && idx - win0 < cap) {
+        pair_q[idx - win0] = q;
+        pair_ph[idx - win0] = ph;
+      }
+      idx++;
+    });
+  }
+}
+
+// One (query, photon) pair per lane, a run of kRun consecutive pairs per thread so that
+// pairs of one pixel add up in registers before the image atomics.
+constexpr int kRun = 8;
+__global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
+                                                    const int* photon_ref, const uint32_t* pair_q,
+                                                    const int* pair_ph, uint32_t npairs, float* img) {
+  const float r = P.radius;
+  uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kRun; base < npairs; base += stride * kRun) {
+    F3 acc = {0, 0, 0};
+    int acc_pixel = -1;
+    for (uint32_t j = base; j < base + kRun && j < npairs; j++) {
+      uint32_t q = pair_q[j];
+      int ref = photon_ref[pair_ph[j]];
+      int p = (int)(q / P.maxv), ei = (int)(q % P.maxv);
+      int lp = ref / (int)P.maxv, li = ref % (int)P.maxv;
+      PV w[2 * kMaxV];
+      int n = 0;
+      for (int k = 0; k < li; k++) w[n++] = load_pv(lv + 4 * ((size_t)lp * P.maxv + k));
+      for (int k = ei; k >= 0; k--) w[n++] = load_pv(ev + 4 * ((size_t)p * P.maxv + k));
+      int ci = li - 1;
+      if (!connect_rays(S, P.cam, w, n, ci, true)) continue;
+      F3 col;
+      float prob;
+      connect_color_prob(S, P.cam, w, n, ci, true, r, col, prob);
+      if (length(col) == 0.0f || prob == 0.0f) continue;
+      float wt = connect_merge_weight(S, P.cam, w, n, ci, true, r, P.norm);
+      F3 c = col * (wt / prob) * (1.0f / P.norm);
+      if (p != acc_pixel) {
+        if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
+        acc = {0, 0, 0};
+        acc_pixel = p;
+      }
+      acc = acc + c;
+    }
+    if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
+  }
+}
+
 // MCRenderer::eliminateVignetting on the iteration image, then the running mean's sum.
 __global__ void k_vcm_accumulate(VcmParams P, const float* img, double* film) {
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += gridDim.x * blockDim.x) {
@@ -527,7 +601,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.n_light * P.maxv;
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(12);
+  std::vector<DevBuf> bufs(20);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
   if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
@@ -542,6 +616,17 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = al(9, ((buckets + 1) / 1024 + 2) * sizeof(unsigned))) != cudaSuccess) return e;      // block sums
   if ((e = al(10, (size_t)P.n_pixels * 3 * sizeof(float))) != cudaSuccess) return e;            // iteration image
   if ((e = al(11, 64 * sizeof(unsigned long long))) != cudaSuccess) return e;                   // counters
+  const uint32_t nq = P.n_pixels * P.maxv;                                                       // merge queries
+  const unsigned nqblk = (nq + 1023) / 1024;
+  if ((e = al(12, (size_t)P.n_pixels * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // eye vertices
+  if ((e = al(13, (size_t)P.n_pixels * sizeof(int))) != cudaSuccess) return e;                   // eye lengths
+  if ((e = al(14, (size_t)nq * sizeof(unsigned long long))) != cudaSuccess) return e;            // query counts
+  if ((e = al(15, (size_t)nq * sizeof(unsigned long long))) != cudaSuccess) return e;            // query offsets
+  if ((e = al(16, ((size_t)nqblk + 2) * sizeof(unsigned long long))) != cudaSuccess) return e;  // block sums
+  const uint32_t pair_cap = 1u << 27;  // pairs per evaluation window
+  uint32_t pair_alloc = 1u << 20;      // grows with demand up to pair_cap
+  if ((e = al(17, (size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
+  if ((e = al(18, (size_t)pair_alloc * sizeof(int))) != cudaSuccess) return e;
   unsigned long long* ctr = bufs[11].as<unsigned long long>();
   unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
   cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
@@ -551,6 +636,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   float radius = opt.radius;
+  unsigned long long merges = 0;
   unsigned nscan = buckets + 1;
   unsigned nblk = (nscan + 1023) / 1024;
   for (uint32_t it = 0; it < opt.iterations; it++) {
@@ -564,14 +650,42 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     float cell = 2.0f * radius;
     k_grid_count<<<grid, 256, 0, s>>>(bufs[2].as<float4>(), nph, cap, cell, buckets - 1, bufs[6].as<unsigned>(),
                                       bufs[4].as<unsigned>());
-    k_scan_blocks<<<nblk, 1024, 0, s>>>(bufs[6].as<unsigned>(), bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan);
-    k_scan_sums<<<1, 1024, 0, s>>>(bufs[9].as<unsigned>(), nblk);
-    k_scan_add<<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan, bufs[8].as<unsigned>());
+    k_scan_blocks<unsigned><<<nblk, 1024, 0, s>>>(bufs[6].as<unsigned>(), bufs[7].as<unsigned>(),
+                                                    bufs[9].as<unsigned>(), nscan);
+    k_scan_sums<unsigned><<<1, 1024, 0, s>>>(bufs[9].as<unsigned>(), nblk);
+    k_scan_add<unsigned><<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan,
+                                                bufs[8].as<unsigned>());
     k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), nph, cap, bufs[8].as<unsigned>(), bufs[5].as<int>());
     Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[5].as<int>()};
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
-    k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
-                                   bufs[3].as<int>(), G, bufs[10].as<float>(), ctr + 1);
+    k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
+                                   bufs[13].as<int>(), bufs[10].as<float>(), ctr + 1);
+    // merging: count per query, scan, then windows of (query, photon) pairs
+    unsigned long long* qc = bufs[14].as<unsigned long long>();
+    unsigned long long* qo = bufs[15].as<unsigned long long>();
+    k_merge_count<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,
+                                           qc, nq);
+    k_scan_blocks<unsigned long long><<<nqblk, 1024, 0, s>>>(qc, qo, bufs[16].as<unsigned long long>(), nq);
+    k_scan_sums<unsigned long long><<<1, 1024, 0, s>>>(bufs[16].as<unsigned long long>(), nqblk);
+    k_scan_add<unsigned long long><<<nqblk, 1024, 0, s>>>(qo, bufs[16].as<unsigned long long>(), nq, nullptr);
+    unsigned long long tail[2] = {0, 0};
+    cudaMemcpyAsync(&tail[0], qo + (nq - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&tail[1], qc + (nq - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    const unsigned long long total = tail[0] + tail[1];
+    merges += total;
+    if (total > pair_alloc && pair_alloc < pair_cap) {
+      pair_alloc = (uint32_t)std::min<unsigned long long>(pair_cap, std::max<unsigned long long>(total, 2ull * pair_alloc));
+      if ((e = bufs[17].alloc((size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
+      if ((e = bufs[18].alloc((size_t)pair_alloc * sizeof(int))) != cudaSuccess) return e;
+    }
+    for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
+      uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
+      k_merge_fill<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,
+                                            qo, nq, w0, pair_alloc, bufs[17].as<uint32_t>(), bufs[18].as<int>());
+      k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[3].as<int>(),
+                                            bufs[17].as<uint32_t>(), bufs[18].as<int>(), np, bufs[10].as<float>());
+    }
     k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
   }
   cudaEventRecord(e1, s);
