@@ -22,6 +22,9 @@ Secondary sections of the same JSON line (each skippable):
             records and inference on 2^20 queries, TFLOP/s against the BF16 peak.
   vcm     : VCMTracer with the homogeneous-medium scene, 512^2, 2^20 light paths per
             iteration: ms per iteration.
+  batch   : 64 seeded sphere-field variants (1k-2M triangles, 128^2-1024^2, 4-64 spp,
+            8 with the medium) in one wavefront with graph replay and autotuning, and
+            the same scenes rendered one after another.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -216,6 +219,46 @@ def section_mlp(ctx, peak_tflops):
                          "frac": f_train / peak_tflops, "kernel": "k_guide_train (forward + backward, BF16 tcgen05)"}}
 
 
+def section_batch(n: int = 64):
+    """C3: n seeded sphere-field variants in one wavefront (graph replay, autotuned launch
+    shape) against rendering them one after another."""
+    import renderx_gb300 as rx
+    from renderx_gb300 import scenes
+    t0 = time.perf_counter()
+    variants = scenes.batch_variants(n)
+    gen_s = time.perf_counter() - t0
+    ctxs = []
+    try:
+        t0 = time.perf_counter()
+        tris = 0
+        for sc, _ in variants:
+            c = rx.Context(0)
+            ctxs.append(c)
+            f = c.set_scene(sc)
+            tris += len(f["tris"])
+            c.build_accel()
+        build_s = time.perf_counter() - t0
+        items = [(c, sc.camera, o) for c, (sc, o) in zip(ctxs, variants)]
+        ctxs[0].render_pt_batch(items[:2], autotune=False)  # warm-up
+        films, st = ctxs[0].render_pt_batch(items, use_graph=True, autotune=True)
+        seq_ms, seq_rays = 0.0, 0
+        for c, (sc, o) in zip(ctxs, variants):
+            _, _, s1 = c.render_pt(sc.camera, o["spp"], max_depth=o["max_depth"], rr_mode=o["rr_mode"], seed=o["seed"])
+            seq_ms += s1["ms"]
+            seq_rays += s1["extension_rays"]
+    finally:
+        for c in ctxs:
+            c.close()
+    rays = st["extension_rays"] + st["shadow_rays"]
+    return {"workload": f"{n} sphere-field variants, {tris} triangles in all (1k-2M each), 128^2-1024^2, "
+                        "4-64 spp, depth 16, 8 with the homogeneous medium",
+            "paths": st["paths"], "ms": st["ms"], "mrays_per_s": rays / st["ms"] / 1e3,
+            "samples_per_s": st["paths"] / st["ms"] * 1e3, "chosen_blocks_per_sm": st["blocks_per_sm"],
+            "chosen_stack": st["stack"], "one_by_one_ms": seq_ms,
+            "one_by_one_mrays_per_s": seq_rays / seq_ms / 1e3, "speedup_vs_one_by_one": seq_ms / st["ms"],
+            "scene_generation_s": round(gen_s, 1), "accel_build_s": round(build_s, 1)}
+
+
 def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
     """C2: VCMTracer, medium scene at 512^2, 2^20 light paths per iteration."""
     import renderx_gb300 as rx
@@ -355,7 +398,8 @@ def run_ours(args):
                                ("guiding", args.skip_guiding,
                                 lambda: section_guiding(args.guide_res, args.guide_ref_spp, args.guide_spp)),
                                ("vcm", args.skip_vcm,
-                                lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths))):
+                                lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths)),
+                               ("batch", args.skip_batch, lambda: section_batch(args.batch_scenes))):
             if skip:
                 continue
             t0 = time.perf_counter()
@@ -440,6 +484,8 @@ def main():
     ap.add_argument("--skip-mlp", action="store_true")
     ap.add_argument("--skip-guiding", action="store_true")
     ap.add_argument("--skip-vcm", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--skip-extra", action="store_true", help="skip every secondary section")
     ap.add_argument("--guide-res", type=int, default=256)
     ap.add_argument("--guide-ref-spp", type=int, default=4096)
@@ -452,7 +498,7 @@ def main():
     args = ap.parse_args()
     globals()["N_RAYS"] = args.rays
     if args.skip_extra:
-        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = True
+        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = True
     if args.impl == "reference":
         run_reference(args)
     else:

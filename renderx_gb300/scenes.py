@@ -302,6 +302,30 @@ def guiding_scene(width: int = 1024, height: int = 1024, n_spheres: int = 200, s
                         glossy_exp=(100.0, 1000.0), light_scale=GUIDING_LIGHT_SCALE)
 
 
+def batch_variants(n: int = 64, seed: int = 1, n_medium: int = 8):
+    """The batching workload: ``n`` seeded variants of the sphere field. Triangle counts
+    log-U[1k, 2M] (sphere subdivision 2..5 and sphere count chosen to match),
+    resolution drawn from {128, 256, 512, 1024}^2, spp U{4..64}, depth cap 16, Russian
+    roulette from depth 3; the first ``n_medium`` carry the homogeneous-medium sphere of
+    ``medium_scene``. Returns a list of (Scene, options dict)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        target = math.exp(rng.uniform(math.log(1e3), math.log(2e6)))
+        d = 5
+        while d > 2 and 20 * 4 ** d * 4 > target:
+            d -= 1
+        ns = int(max(1, min(400, round((target - 36) / (20 * 4 ** d)))))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = int(rng.integers(4, 65))
+        sc = sphere_field(ns, d, seed=1000 + k, width=res, height=res)
+        if k < n_medium:
+            med = medium_scene(res, res).objects[-1]
+            sc.objects.append(med)
+        out.append((sc, dict(spp=spp, max_depth=16, rr_mode=1, nee=False, seed=k + 1)))
+    return out
+
+
 def hit_rays(n: int, seed: int = 7, lo: float = 0.0, hi: float = ROOM):
     """Closest-hit batch: origins U[lo,hi]^3, directions uniform on S^2 with
     z = 1-2u, phi = 2 pi u. Returns (origins (n,3) f32, dirs (n,3) f32)."""
