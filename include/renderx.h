@@ -280,8 +280,10 @@ rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_p
  * is checked for reference visibility, 1 = one thread per ray (default), 0 = one warp
  * per ray (one ancestor box per lane); bin_min = batches of at least this many rays are
  * reordered by origin cell and direction before the walk (counting sort), 0 = never
- * (default 262144). Answers do not depend on either. */
-rx_status rx_trace_set_options(rx_context* ctx, int32_t check_mode, uint32_t bin_min);
+ * (default 262144); walk_stack = entries of the walk's stack: 0 or 32 = 32 when the
+ * BVH is shallower than 32 levels, else 64 (default 0); 64 = always 64. Answers depend
+ * on none of them. */
+rx_status rx_trace_set_options(rx_context* ctx, int32_t check_mode, uint32_t bin_min, int32_t walk_stack);
 /* Per-kernel device timing of rx_trace_closest_device calls: the next max_calls calls
  * record CUDA events around their three kernels (walk, reference-visibility check,
  * re-walk of rejected winners); 0 turns timing off. No reference counterpart

@@ -243,10 +243,11 @@ class Context:
     def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
-    def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18):
-        """Visibility check of each winner (1 = thread per ray, 0 = warp per ray) and the
-        batch size from which rays are binned before the walk (0 = never)."""
-        self._ck(self._L.rx_trace_set_options(self.h, int(check_mode), int(bin_min)))
+    def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18, walk_stack: int = 0):
+        """Visibility check of each winner (1 = thread per ray, 0 = warp per ray), the
+        batch size from which rays are binned before the walk (0 = never) and the walk
+        stack depth (0 = automatic, 32 or 64)."""
+        self._ck(self._L.rx_trace_set_options(self.h, int(check_mode), int(bin_min), int(walk_stack)))
 
     def set_trace_timing(self, max_calls: int):
         """Record per-kernel CUDA events for the next ``max_calls`` device trace calls."""

@@ -213,6 +213,7 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.num_ref_nodes = (uint32_t)c->ref.nodes.size();
   A.num_ref_leaves = (uint32_t)c->ref.leaf_node.size();
   A.prune_rel = 1e-3f;
+  A.bvh_depth = (uint32_t)c->bvh.max_depth;
   for (int k = 0; k < 3; k++) {
     const rx::BvhNodeHost& r = c->bvh.nodes[0];
     A.lo[k] = std::min(r.c0lo[k], r.c1lo[k]);
@@ -576,11 +577,13 @@ rx_status rx_trace_set_config(rx_context* c, int32_t variant, int32_t blocks_per
   return RX_OK;
 }
 
-rx_status rx_trace_set_options(rx_context* c, int32_t check_mode, uint32_t bin_min) {
+rx_status rx_trace_set_options(rx_context* c, int32_t check_mode, uint32_t bin_min, int32_t walk_stack) {
   if (!c) return RX_ERR_INVALID;
   if (check_mode != 0 && check_mode != 1) return c->fail(RX_ERR_INVALID, "check_mode must be 0 or 1");
+  if (walk_stack != 0 && walk_stack != 32 && walk_stack != 64) return c->fail(RX_ERR_INVALID, "walk_stack: 0, 32 or 64");
   c->trace_cfg.check_thread = check_mode;
   c->trace_cfg.bin_min = bin_min;
+  c->trace_cfg.walk_stack = walk_stack;
   return RX_OK;
 }
 

@@ -29,6 +29,7 @@ struct DevAccel {
   uint32_t num_nodes, num_tris, num_ref_nodes, num_ref_leaves;
   float prune_rel;                 // pruning margin: t_limit = best + prune_rel*(1+best)
   float lo[3], hi[3];              // scene bounds (ray binning)
+  uint32_t bvh_depth;              // deepest BVH level (the walk's stack must exceed it)
 };
 
 }  // namespace rx

@@ -24,6 +24,7 @@ struct TraceConfig {
   int pt_blocks_per_sm = 8;  // wavefront extend / shade kernels
   int check_thread = 1;      // reference-visibility check: 1 = thread per ray, 0 = warp per ray
   uint32_t bin_min = 1u << 18;  // bin rays before the walk from this batch size on (0 = never)
+  int walk_stack = 0;           // walk stack entries: 0 = 32 when the BVH is shallower, else 64
 };
 
 // Launch shape of the wavefront's extend / shade kernels: blocks of 128 threads per SM

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevAccel A, const rx_ray*
 // (SPEC: keeps walking with the leaf postponed until every lane of the warp holds one),
 // then tests that leaf's triangles; finished lanes are checked for reference
 // visibility together. counters[4] is the batch cursor.
-template <bool SPEC>
+template <bool SPEC, int kStack>
 __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
                                                           const uint32_t* __restrict__ order,
                                                           int32_t* __restrict__ out_tid,
@@ -413,10 +413,16 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     unsigned blocks = (unsigned)cfg.sms * (unsigned)cfg.blocks_per_sm;
     unsigned need = (n + 127) / 128;
     blocks = blocks < need ? blocks : need;
-    if (cfg.variant == 1)
-      k_trace_persistent<false><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+    // the walk's stack lives in local memory: the shallower one when the BVH allows
+    const bool shallow = cfg.walk_stack != 64 && A.bvh_depth < 32;
+    if (cfg.variant == 1 && shallow)
+      k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+    else if (cfg.variant == 1)
+      k_trace_persistent<false, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+    else if (shallow)
+      k_trace_persistent<true, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
     else
-      k_trace_persistent<true><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent<true, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
   }
   if (ev) cudaEventRecord(ev[1], s);
   if (cfg.check_thread)

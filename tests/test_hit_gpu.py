@@ -24,7 +24,8 @@ def test_hits_match_reference_golden(name, leaf_size, variant, check):
     z = load(name)
     with rx.Context(0) as ctx:
         ctx.set_trace_config(variant, 4)
-        ctx.set_trace_options(check, 64 if check else 0)  # bin even the small golden batches
+        # bin even the small golden batches; both walk stack depths
+        ctx.set_trace_options(check, 64 if check else 0, 32 if check else 64)
         ctx.set_geometry(z["verts"], z["tris"])
         ctx.build_accel(rx.SPLIT_GCC, leaf_size=leaf_size)
         tid, dist = ctx.trace_closest(z["origins"], z["dirs"])
