@@ -51,7 +51,9 @@ UNIT = "Mrays/s"
 WORKLOAD = "hit_batch_2^24_rays_cornell+200_icospheres_4096036_tris"
 
 
-TRAFFIC_BYTES_PER_RAY = 646.2e6 / (1 << 20)
+# DRAM bytes (read + write) of one walk-kernel launch over the 2^24-ray batch, from a
+# one-pass ncu capture of this workload (profiles/k_trace_persistent_hit1M.md)
+TRAFFIC_BYTES_PER_RAY = (8393696768 + 1892597760) / (1 << 24)
 
 
 def load_tflops():
@@ -444,9 +446,7 @@ def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_m
         bytes_alg = 40 * n + 48 * st["triangles"] + 64 * st["bvh_nodes"]
         walk_ms = float(kern_ms[:, 0].mean()) if len(kern_ms) else ms_per_step
         achieved = bytes_alg / (walk_ms * 1e-3) / 1e9
-        # DRAM bytes per ray of the walk kernel from the 2^20-ray profiler capture
-        # (profiles/k_trace_persistent_hit1M.md: 646.2 MB / 2^20 rays), scaled to this launch
-        traffic = TRAFFIC_BYTES_PER_RAY * n
+        traffic = TRAFFIC_BYTES_PER_RAY * n  # measured at 2^24 rays; scaled by rays for other sizes
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
