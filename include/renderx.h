@@ -223,7 +223,8 @@ rx_status rx_write_pfm(const char* path, uint32_t width, uint32_t height, const 
 /* ---- closest hit --------------------------------------------------------------- */
 /* KDTree::intersect(ray, triangleID, NULL) (reference include/KDTree.h:50,
  * src/KDTree.cpp:408-412) over a batch, host buffers: out_tid[i] = global triangle id
- * or -1, out_dist[i] = hit distance or -1. Copies are pipelined with the kernels. */
+ * or -1, out_dist[i] = hit distance or -1. Up to 2^24 rays are copied and traced as one
+ * batch; larger inputs are pipelined in chunks of 2^24 over two streams. */
 rx_status rx_trace_closest(rx_context* ctx, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist);
 /* Same on device buffers (no copies), enqueued on `stream` (a cudaStream_t, NULL for
  * the context's stream). */
@@ -273,8 +274,9 @@ rx_status rx_render_vcm(rx_context* ctx, const rx_camera* cam, const rx_vcm_opti
 
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
  * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative
- * leaf postponing; blocks of 128 threads, blocks_per_sm per SM. No reference
- * counterpart (launch tuning). */
+ * leaf postponing, 3 = persistent over the 4-wide BVH (the default; falls back to 1
+ * when that tree is too deep for its stack); blocks of 128 threads, blocks_per_sm per
+ * SM. No reference counterpart (launch tuning). */
 rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_per_sm);
 /* Closest-hit options (no reference counterpart): check_mode = how each walk's winner
  * is checked for reference visibility, 1 = one thread per ray (default), 0 = one warp

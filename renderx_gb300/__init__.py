@@ -240,7 +240,7 @@ class Context:
         self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
         return film, dict(rays=st.extension_rays, paths=st.paths, ms=st.ms)
 
-    def set_trace_config(self, variant: int = 1, blocks_per_sm: int = 12):
+    def set_trace_config(self, variant: int = 3, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
     def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18, walk_stack: int = 0):

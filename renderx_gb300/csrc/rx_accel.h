@@ -54,4 +54,17 @@ struct Bvh {
 bool build_bvh(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt, int leaf_size, int threads,
                Bvh& out);
 
+// 4-wide BVH collapsed from the binary one: each node holds up to four children (inner
+// nodes or leaves of the binary tree), found by repeatedly opening the child with the
+// largest surface area. Node layout on the device: 8 float4 = 128 B (lo.x, hi.x, lo.y,
+// hi.y, lo.z, hi.z of the four children, then child refs and leaf counts; an empty
+// child slot has ref kBvh4Empty).
+constexpr int32_t kBvh4Empty = 0x7fffffff;
+struct Bvh4 {
+  std::vector<float> data;  // 32 floats per node
+  int max_depth = 0;
+  size_t num_nodes() const { return data.size() / 32; }
+};
+void collapse_bvh4(const Bvh& b2, Bvh4& out);
+
 }  // namespace rx

@@ -510,3 +510,75 @@ extern "C" rx_status rx_reftree_serialize(const float* verts, uint32_t nv, const
   for (size_t k = 0; k < ro.tri_order.size(); k++) leaf_tid[k] = (float)ro.tri_order[k];
   return RX_OK;
 }
+
+namespace rx {
+
+namespace {
+struct Child4 {
+  int32_t ref, count;
+  float lo[3], hi[3];
+};
+float half_area(const Child4& c) {
+  float ex = c.hi[0] - c.lo[0], ey = c.hi[1] - c.lo[1], ez = c.hi[2] - c.lo[2];
+  return ex * ey + ey * ez + ez * ex;
+}
+void children_of(const BvhNodeHost& n, Child4 (&c)[2]) {
+  for (int k = 0; k < 3; k++) {
+    c[0].lo[k] = n.c0lo[k];
+    c[0].hi[k] = n.c0hi[k];
+    c[1].lo[k] = n.c1lo[k];
+    c[1].hi[k] = n.c1hi[k];
+  }
+  c[0].ref = n.child[0];
+  c[0].count = n.count[0];
+  c[1].ref = n.child[1];
+  c[1].count = n.count[1];
+}
+int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
+  Child4 two[2];
+  children_of(b2.nodes[n2], two);
+  std::vector<Child4> kids = {two[0], two[1]};
+  while (kids.size() < 4) {
+    int best = -1;
+    float area = -1.0f;
+    for (size_t i = 0; i < kids.size(); i++)
+      if (kids[i].ref >= 0 && half_area(kids[i]) > area) area = half_area(kids[i]), best = (int)i;
+    if (best < 0) break;
+    Child4 sub[2];
+    children_of(b2.nodes[kids[best].ref], sub);
+    kids[best] = sub[0];
+    kids.push_back(sub[1]);
+  }
+  const int32_t me = (int32_t)out.num_nodes();
+  out.data.resize(out.data.size() + 32, 0.0f);
+  out.max_depth = std::max(out.max_depth, depth);
+  int32_t refs[4], counts[4];
+  for (int j = 0; j < 4; j++) {
+    refs[j] = kBvh4Empty;
+    counts[j] = 0;
+  }
+  for (size_t j = 0; j < kids.size(); j++) {
+    refs[j] = kids[j].ref >= 0 ? collapse(b2, kids[j].ref, depth + 1, out) : kids[j].ref;
+    counts[j] = kids[j].count;
+  }
+  float* f = out.data.data() + 32 * (size_t)me;  // after the recursion: data may have moved
+  for (int j = 0; j < 4; j++) {
+    bool has = j < (int)kids.size();
+    for (int k = 0; k < 3; k++) {
+      f[8 * k + j] = has ? kids[j].lo[k] : 0.0f;
+      f[8 * k + 4 + j] = has ? kids[j].hi[k] : 0.0f;
+    }
+    std::memcpy(&f[24 + j], &refs[j], 4);
+    std::memcpy(&f[28 + j], &counts[j], 4);
+  }
+  return me;
+}
+}  // namespace
+
+void collapse_bvh4(const Bvh& b2, Bvh4& out) {
+  out.data.clear();
+  out.max_depth = 0;
+  if (!b2.nodes.empty()) collapse(b2, 0, 0, out);
+}
+
+}  // namespace rx

@@ -56,7 +56,7 @@ void rx_destroy(rx_context* c) {
   {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf* b : {&c->d_bvh, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
+    for (DevBuf* b : {&c->d_bvh, &c->d_bvh4, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
                       &c->d_anc_range, &c->d_anc_nodes, &c->d_slot_n, &c->d_tri_v, &c->d_tri_n, &c->d_tri_obj,
                       &c->d_objects, &c->d_light_cdf, &c->d_light_tri,
                       &c->d_counters, &c->d_queue})
@@ -188,6 +188,9 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   }
   rx_status s;
   if ((s = upload(c, c->d_bvh, nodes.data(), nodes.size() * sizeof(float4), "upload BVH")) != RX_OK) return s;
+  rx::collapse_bvh4(c->bvh, c->bvh4);
+  if ((s = upload(c, c->d_bvh4, c->bvh4.data.data(), c->bvh4.data.size() * sizeof(float), "upload BVH4")) != RX_OK)
+    return s;
   if ((s = upload(c, c->d_tris, slots.data(), slots.size() * sizeof(float4), "upload triangles")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref, refn.data(), refn.size() * sizeof(float4), "upload reference nodes")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref_leaf_node, leaf_node.data(), leaf_node.size() * 4, "upload leaf map")) != RX_OK) return s;
@@ -214,6 +217,8 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.num_ref_leaves = (uint32_t)c->ref.leaf_node.size();
   A.prune_rel = 1e-3f;
   A.bvh_depth = (uint32_t)c->bvh.max_depth;
+  A.bvh4 = c->d_bvh4.as<float4>();
+  A.bvh4_depth = (uint32_t)c->bvh4.max_depth;
   for (int k = 0; k < 3; k++) {
     const rx::BvhNodeHost& r = c->bvh.nodes[0];
     A.lo[k] = std::min(r.c0lo[k], r.c1lo[k]);
@@ -528,17 +533,22 @@ rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, 
                  "trace_reforder launch");
 }
 
-// Host buffers: chunks alternate between two copy/compute streams so that one
-// chunk's copies overlap the other chunk's kernels.
+// Host buffers. Up to kWholeBatch rays go to the device in one copy and are traced as
+// one batch (binning and the persistent walk work best on whole batches; the copies run
+// at the host link's full rate); larger inputs go in chunks of kWholeBatch that
+// alternate between two copy/compute streams, so one chunk's copies overlap the other
+// chunk's kernels.
+static constexpr size_t kWholeBatch = (size_t)1 << 24;
 rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist) {
   if (!c) return RX_ERR_INVALID;
   if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
   if (n == 0) return RX_OK;
   if (!rays || !out_tid || !out_dist) return c->fail(RX_ERR_INVALID, "null buffer");
   DeviceGuard g(c->device);
-  const size_t chunk = std::min<size_t>(n, (size_t)1 << 21);
-  if (c->ring_chunk < chunk) {
-    for (int k = 0; k < 2; k++) {
+  const size_t chunk = std::min<size_t>(n, kWholeBatch);
+  const int nring = n > kWholeBatch ? 2 : 1;
+  if (c->ring_chunk < chunk || (nring == 2 && !c->ring_rays[1].p)) {
+    for (int k = 0; k < nring; k++) {
       rx_status s;
       if ((s = c->cuda(c->ring_rays[k].alloc(chunk * sizeof(rx_ray)), "staging")) != RX_OK) return s;
       if ((s = c->cuda(c->ring_tid[k].alloc(chunk * 4), "staging")) != RX_OK) return s;
@@ -549,7 +559,7 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
     }
     c->ring_chunk = chunk;
   }
-  for (size_t b = 0, k = 0; b < n; b += chunk, k ^= 1) {
+  for (size_t b = 0, k = 0; b < n; b += chunk, k = (k + 1) % nring) {
     size_t m = std::min<size_t>(chunk, n - b);
     cudaStream_t st = c->copy_stream[k];
     cudaMemcpyAsync(c->ring_rays[k].p, rays + b, m * sizeof(rx_ray), cudaMemcpyHostToDevice, st);
@@ -570,8 +580,8 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
 
 rx_status rx_trace_set_config(rx_context* c, int32_t variant, int32_t blocks_per_sm) {
   if (!c) return RX_ERR_INVALID;
-  if (variant < 0 || variant > 2 || blocks_per_sm < 1 || blocks_per_sm > 32)
-    return c->fail(RX_ERR_INVALID, "variant must be 0..2 and blocks_per_sm 1..32");
+  if (variant < 0 || variant > 3 || blocks_per_sm < 1 || blocks_per_sm > 32)
+    return c->fail(RX_ERR_INVALID, "variant must be 0..3 and blocks_per_sm 1..32");
   c->trace_cfg.variant = variant;
   c->trace_cfg.blocks_per_sm = blocks_per_sm;
   return RX_OK;

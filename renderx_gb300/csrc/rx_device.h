@@ -30,6 +30,8 @@ struct DevAccel {
   float prune_rel;                 // pruning margin: t_limit = best + prune_rel*(1+best)
   float lo[3], hi[3];              // scene bounds (ray binning)
   uint32_t bvh_depth;              // deepest BVH level (the walk's stack must exceed it)
+  const float4* bvh4;              // 4-wide BVH, 8 float4 per node (rx_accel.h), or null
+  uint32_t bvh4_depth;
 };
 
 }  // namespace rx

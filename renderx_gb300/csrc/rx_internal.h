@@ -18,7 +18,7 @@ void guide_free(GuideState* g);
 // Closest-hit launch shape: variant 0 = one thread per ray, 1 = persistent warps
 // refilling finished lanes; blocks_per_sm x sms blocks of 128 threads.
 struct TraceConfig {
-  int variant = 1;
+  int variant = 3;
   int blocks_per_sm = 12;
   int sms = 152;
   int pt_blocks_per_sm = 8;  // wavefront extend / shade kernels
@@ -122,6 +122,8 @@ struct rx_context {
   rx::DevAccel accel{};
   rx::TraceConfig trace_cfg;
   bool accel_ready = false;
+  rx::Bvh4 bvh4;
+  rx::DevBuf d_bvh4;
   rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes;
   rx::DevScene scene{};
   bool scene_ready = false;

@@ -2,6 +2,7 @@
 #include "rx_internal.h"
 #include "rx_bin.cuh"
 #include "rx_trace.cuh"
+#include "rx_accel.h"
 
 namespace rx {
 
@@ -51,6 +52,171 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
   unsigned sum = n_exact;
   for (int s2 = 16; s2 > 0; s2 >>= 1) sum += __shfl_xor_sync(FULL, sum, s2);
   if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
+}
+
+// The persistent walk over the 4-wide BVH: one node visit tests four child boxes
+// (128-byte node, one cache line), visits the nearest hit child next and stacks the
+// others far to near; pruning, leaf tests and refills as k_trace_persistent.
+__global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                           const uint32_t* __restrict__ order,
+                                                           int32_t* __restrict__ out_tid,
+                                                           float* __restrict__ out_dist,
+                                                           uint32_t* __restrict__ hit_leaf,
+                                                           unsigned long long* __restrict__ counters) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int DONE = INT_MIN;
+  constexpr int kStack4 = 64;  // at most 3 entries per level of a BVH4 shallower than 21 levels
+  const int lane = threadIdx.x & 31;
+  unsigned long long* cursor = counters + 4;
+  bool active = false, exhausted = false;
+  uint32_t ray = 0;
+  F3 o{}, d{}, inv{}, ood{};
+  float tlimit = INFINITY;
+  HitResult best{-1, -1.0f, 0u, 0u, false};
+  int stack_ref[kStack4];
+  float stack_tn[kStack4];
+  int sp = 0, cur = DONE, cnt = 0;
+
+  auto pop = [&]() {
+    while (sp > 0) {
+      sp--;
+      if (stack_tn[sp] <= tlimit) {
+        int r = stack_ref[sp];
+        if (r < 0) {
+          int packed = ~r;
+          cnt = (packed & 7) + 1;
+          return ~(packed >> 3);
+        }
+        return r;
+      }
+    }
+    return DONE;
+  };
+  auto pack = [](int ref, int count) { return ref < 0 ? ~((~ref) << 3 | (count - 1)) : ref; };
+
+  while (true) {
+    unsigned want = __ballot_sync(FULL, !active && !exhausted);
+    if (want) {
+      int leader = __ffs(want) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(cursor, (unsigned long long)__popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if (!active && !exhausted) {
+        unsigned long long r = base + __popc(want & ((1u << lane) - 1));
+        if (r < n) {
+          ray = order ? __ldg(&order[r]) : (uint32_t)r;
+          const float4* rp = reinterpret_cast<const float4*>(rays + ray);
+          float4 ro = __ldg(rp), rd = __ldg(rp + 1);
+          o = f3(ro);
+          d = f3(rd);
+          inv = safe_inv(d);
+          ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
+          tlimit = INFINITY;
+          best = {-1, -1.0f, 0u, 0u, false};
+          sp = 0;
+          cur = 0;
+          cnt = 0;
+          active = true;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) break;
+
+    if (active) {
+      int pl = DONE, pcnt = 0;  // the next leaf to test
+      while (true) {
+        if (cur >= 0) {
+          const float4* np = A.bvh4 + 8 * (size_t)cur;
+          float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+          float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+          int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
+          const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+          const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+          const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+          int r[4] = {cr.x, cr.y, cr.z, cr.w}, c[4] = {cc.x, cc.y, cc.z, cc.w};
+          float tn[4];
+          int nh = 0;
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            float a0 = fmaf(lxa[j], inv.x, -ood.x), b0 = fmaf(hxa[j], inv.x, -ood.x);
+            float a1 = fmaf(lya[j], inv.y, -ood.y), b1 = fmaf(hya[j], inv.y, -ood.y);
+            float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
+            float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
+            float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tlimit));
+            bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
+            tn[j] = h ? t0 : INFINITY;
+            nh += h ? 1 : 0;
+          }
+          // sorting network on registers (ties keep child order): near to far
+          auto cs = [&](int a, int b) {
+            if (tn[b] < tn[a]) {
+              float t = tn[a];
+              tn[a] = tn[b];
+              tn[b] = t;
+              int q = r[a];
+              r[a] = r[b];
+              r[b] = q;
+              q = c[a];
+              c[a] = c[b];
+              c[b] = q;
+            }
+          };
+          cs(0, 1);
+          cs(2, 3);
+          cs(0, 2);
+          cs(1, 3);
+          cs(1, 2);
+          if (nh == 0) {
+            cur = pop();
+          } else {
+#pragma unroll
+            for (int k = 3; k >= 1; k--) {  // farthest first, so the nearer pop earlier
+              if (k < nh && sp < kStack4) {
+                stack_ref[sp] = pack(r[k], c[k]);
+                stack_tn[sp] = tn[k];
+                sp++;
+              }
+            }
+            cur = r[0];
+            cnt = c[0];
+          }
+        } else if (cur != DONE) {
+          pl = cur;
+          pcnt = cnt;
+          cur = pop();
+          break;
+        }
+        if (cur == DONE) break;
+      }
+      if (pl != DONE) {
+        int first = ~pl;
+        for (int k = 0; k < pcnt; k++) {
+          const float4* tp = A.tris + 3 * (size_t)(first + k);
+          float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+          float t;
+          if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
+            uint32_t leaf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
+            if (!best.hit || t < best.t ||
+                (t == best.t && (leaf > best.leaf || (leaf == best.leaf && pos < best.pos)))) {
+              best = {__float_as_int(v0.w), t, leaf, pos, true};
+              tlimit = t + A.prune_rel * (1.0f + t);
+            }
+          }
+        }
+        // (the next node was popped under the limit before this leaf's test: a looser
+        // limit only visits more candidates, never fewer)
+      }
+    }
+
+    if (active && cur == DONE) {
+      out_tid[ray] = best.hit ? best.tid : -1;
+      out_dist[ray] = best.hit ? best.t : -1.0f;
+      hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+      active = false;
+    }
+  }
 }
 
 // The same check with one thread per ray: each thread walks its winner's ancestor list
@@ -415,7 +581,9 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     blocks = blocks < need ? blocks : need;
     // the walk's stack lives in local memory: the shallower one when the BVH allows
     const bool shallow = cfg.walk_stack != 64 && A.bvh_depth < 32;
-    if (cfg.variant == 1 && shallow)
+    if (cfg.variant == 3 && A.bvh4 && 3 * A.bvh4_depth + 1 <= 64)  // the 4-wide walk's stack bound
+      k_trace_persistent4<<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+    else if (cfg.variant == 1 && shallow)
       k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
     else if (cfg.variant == 1)
       k_trace_persistent<false, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
