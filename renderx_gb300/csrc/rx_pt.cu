@@ -510,7 +510,7 @@ const uint32_t* enqueue_binning(const Wave& W, PathSoA cur, const unsigned* cc, 
   if (!W.order) return nullptr;
   cudaMemsetAsync(W.hist, 0, kRayBins * sizeof(uint32_t), s);
   k_path_keys<<<grid, 256, 0, s>>>(W.R, cur, cc, W.keys, W.hist);
-  k_scan_bins<<<1, 1024, 0, s>>>(W.hist);
+  scan_bins(W.hist, W.hist + kRayBins, s);
   k_ray_scatter<<<grid, 256, 0, s>>>(W.keys, 0, cc, W.hist, W.order);
   return W.order;
 }
@@ -590,7 +590,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   if (run.bin && per_pass >= c->trace_cfg.bin_min && c->trace_cfg.bin_min) {
     if (!(W.keys = static_cast<uint32_t*>(alloc((size_t)per_pass * 4)))) return e;
     if (!(W.order = static_cast<uint32_t*>(alloc((size_t)per_pass * 4)))) return e;
-    if (!(W.hist = static_cast<uint32_t*>(alloc((size_t)kRayBins * 4)))) return e;
+    if (!(W.hist = static_cast<uint32_t*>(alloc((size_t)kRayBins * 4 + 4096)))) return e;
   }
 
   // guiding (one scene): mixture per live path, training records, per-path radiance

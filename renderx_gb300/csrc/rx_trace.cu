@@ -522,30 +522,6 @@ __global__ void k_ray_keys(DevAccel A, const rx_ray* __restrict__ rays, uint32_t
   }
 }
 
-// Exclusive prefix sum of the kRayBins counters, in place, by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_bins(uint32_t* hist) {
-  constexpr uint32_t per = kRayBins / 1024;
-  __shared__ uint32_t part[1024];
-  const uint32_t t = threadIdx.x;
-  uint32_t* h = hist + t * per;
-  uint32_t sum = 0;
-  for (uint32_t k = 0; k < per; k++) sum += h[k];
-  part[t] = sum;
-  __syncthreads();
-  for (uint32_t off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
-    uint32_t v = t >= off ? part[t - off] : 0u;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
-  }
-  uint32_t run = part[t] - sum;
-  for (uint32_t k = 0; k < per; k++) {
-    uint32_t c = h[k];
-    h[k] = run;
-    run += c;
-  }
-}
-
 __global__ void k_ray_scatter(const uint32_t* __restrict__ keys, uint32_t n_host, const unsigned* count,
                               uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
   const uint32_t n = count ? *count : n_host;
@@ -568,7 +544,7 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     uint32_t* hist = queue + 4 * (size_t)n;
     cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), s);
     k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist);
-    k_scan_bins<<<1, 1024, 0, s>>>(hist);
+    scan_bins(hist, hist + kRayBins, s);
     k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, nullptr, hist, perm);
     order = perm;
   }

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <vector>
 
+#include "rx_bin.cuh"
 #include "rx_internal.h"
 #include "rx_material.cuh"
 
@@ -163,53 +164,6 @@ __global__ void k_grid_count(const float4* pos, const unsigned* n_photons, unsig
     unsigned k = cell_hash((int)floorf(p.x / cell), (int)floorf(p.y / cell), (int)floorf(p.z / cell), mask);
     key[i] = k;
     atomicAdd(&count[k], 1u);
-  }
-}
-// exclusive scan of `count` (n entries) into `start`, block-wise then over block sums
-template <class T>
-__global__ void k_scan_blocks(const T* count, T* start, T* block_sum, unsigned n) {
-  __shared__ T s[1024];
-  unsigned i = blockIdx.x * 1024 + threadIdx.x;
-  T v = i < n ? count[i] : T(0);
-  s[threadIdx.x] = v;
-  __syncthreads();
-  for (unsigned off = 1; off < 1024; off <<= 1) {
-    T t = threadIdx.x >= off ? s[threadIdx.x - off] : T(0);
-    __syncthreads();
-    s[threadIdx.x] += t;
-    __syncthreads();
-  }
-  if (i < n) start[i] = s[threadIdx.x] - v;
-  if (threadIdx.x == 1023) block_sum[blockIdx.x] = s[1023];
-}
-template <class T>
-__global__ void k_scan_sums(T* block_sum, unsigned nb) {
-  // single block, sequential carry over chunks of 1024
-  __shared__ T s[1024];
-  T carry = 0;
-  for (unsigned base = 0; base < nb; base += 1024) {
-    unsigned i = base + threadIdx.x;
-    T v = i < nb ? block_sum[i] : T(0);
-    s[threadIdx.x] = v;
-    __syncthreads();
-    for (unsigned off = 1; off < 1024; off <<= 1) {
-      T t = threadIdx.x >= off ? s[threadIdx.x - off] : T(0);
-      __syncthreads();
-      s[threadIdx.x] += t;
-      __syncthreads();
-    }
-    if (i < nb) block_sum[i] = carry + s[threadIdx.x] - v;
-    __syncthreads();
-    carry += s[1023];
-    __syncthreads();
-  }
-}
-template <class T>
-__global__ void k_scan_add(T* start, const T* block_sum, unsigned n, T* cursor) {
-  unsigned i = blockIdx.x * 1024 + threadIdx.x;
-  if (i < n) {
-    start[i] += block_sum[blockIdx.x];
-    if (cursor) cursor[i] = start[i];
   }
 }
 __global__ void k_grid_scatter(const unsigned* key, const unsigned* n_photons, unsigned cap, unsigned* cursor,
