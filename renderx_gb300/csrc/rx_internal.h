@@ -28,7 +28,8 @@ struct TraceConfig {
 };
 
 // Launch shape of the wavefront's extend / shade kernels: blocks of 128 threads per SM
-// and the traversal stack depth (32 or 64 entries; must exceed the BVH depth).
+// and the walk: 4 = the 4-wide BVH, 32 or 64 = the binary BVH with that many stack
+// entries (must exceed the BVH depth).
 struct PtShape {
   int blocks_per_sm = 8;
   int stack = 64;

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(128) k_extend(const SceneRec* R, PathSoA S, co
     int4 inf = S.info[i];
     bool camera = (inf.w & 255) == 0;  // the camera ray's first query has no condition
     const DevScene& SC = R[(uint32_t)inf.w >> 16].S;
-    PHit h = trace_cond<false, STACK>(SC, f3(o), f3(d), INFINITY, camera ? kNone : inf.y, camera ? kNone : inf.z);
+    PHit h = trace_walk<false, STACK>(SC, f3(o), f3(d), INFINITY, camera ? kNone : inf.y, camera ? kNone : inf.z);
     hit[i] = make_int2(h.tid, __float_as_int(h.t));
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
@@ -177,7 +177,7 @@ __device__ F3 connect_light(const DevScene& SC, const CamDev& cam, const PV& in,
   if (v.contact != kNone) cos_s = fminf(fabsf(dot(contact_normal(SC, cam, v), out.d)), 1.0f);
   float bpdf = dir_pdf(SC, cam, in, out, false);
   shadows++;
-  PHit sh = trace_cond<true, STACK>(SC, v.o, out.d, dist - 1e-5f, v.contact, v.inside);  // testVisibility
+  PHit sh = trace_walk<true, STACK>(SC, v.o, out.d, dist - 1e-5f, v.contact, v.inside);  // testVisibility
   if (sh.tid >= 0) return {0, 0, 0};
   float pdfa = 1.0f / SC.light_area;
   float pdfw = pdfa * dist * dist / cos_l;
@@ -536,7 +536,8 @@ void enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
 
 void enqueue_pass_shape(const Wave& W, const PtShape& sh, int sms, cudaStream_t s) {
   int grid = sms * sh.blocks_per_sm;
-  if (sh.stack == 32) enqueue_pass<32>(W, grid, s);
+  if (sh.stack == kWalk4) enqueue_pass<kWalk4>(W, grid, s);
+  else if (sh.stack == 32) enqueue_pass<32>(W, grid, s);
   else enqueue_pass<kStackDepth>(W, grid, s);
 }
 
@@ -547,6 +548,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   std::vector<SceneRec> recs(nj);
   uint64_t total = 0;
   uint32_t max_depth = 0, max_bvh_depth = 0;
+  bool wide_ok = true;  // every scene's 4-wide BVH fits the 4-wide walk's stack
   for (int k = 0; k < nj; k++) {
     recs[k].S = jobs[k].ctx->scene;
     recs[k].P = make_pt_params(jobs[k].ctx, jobs[k].cam, jobs[k].opt);
@@ -555,6 +557,8 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     total += (uint64_t)recs[k].P.pixels * jobs[k].opt.spp;
     max_depth = std::max(max_depth, jobs[k].opt.max_depth);
     max_bvh_depth = std::max<uint32_t>(max_bvh_depth, (uint32_t)jobs[k].ctx->bvh.max_depth);
+    const DevAccel& A = jobs[k].ctx->scene.accel;
+    wide_ok = wide_ok && A.bvh4 && 3 * A.bvh4_depth + 1 <= 64;
   }
   uint32_t per_pass = run.paths_per_pass ? run.paths_per_pass : (1u << 22);
   per_pass = (uint32_t)std::min<uint64_t>(per_pass, total);
@@ -613,12 +617,12 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   }
 
   // launch shapes: the context's default, or candidates timed on the first passes
-  PtShape best{c->trace_cfg.pt_blocks_per_sm, max_bvh_depth < 32 ? 32 : kStackDepth};
+  PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4 : (max_bvh_depth < 32 ? 32 : kStackDepth)};
   std::vector<PtShape> cands;
   if (run.autotune && !guided) {
     for (int bps : {4, 8, 16})
-      for (int st : {32, kStackDepth})
-        if (st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
+      for (int st : {kWalk4, 32, kStackDepth})
+        if (st == kWalk4 ? wide_ok : st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
     if (npasses < cands.size() + 2) cands.clear();
   }
 
@@ -684,14 +688,18 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       unsigned *cc = W.cnt, *cn = W.cnt + 1;
       for (uint32_t d = 0; d < W.loops; d++) {
         const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
-        if (best.stack == 32)
+        if (best.stack == kWalk4)
+          k_extend<kWalk4><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
+        else if (best.stack == 32)
           k_extend<32><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
         else
           k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
         if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, 2 * sms, s)) != cudaSuccess)
           return e;
         k_zero<<<1, 1, 0, s>>>(cn);
-        if (best.stack == 32)
+        if (best.stack == kWalk4)
+          k_shade<kWalk4><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
+        else if (best.stack == 32)
           k_shade<32><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
         else
           k_shade<kStackDepth><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);

@@ -229,4 +229,133 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
   return best;
 }
 
+// The same query over the 4-wide BVH (rx_accel.h layout): four child boxes per
+// 128-byte node, nearest hit child next, the others stacked far to near with their entry
+// distance so that popped subtrees beyond the current best are skipped. The stack holds
+// at most 3 entries per level: callers use it only when 3 * bvh4_depth + 1 <= 64.
+constexpr int kWalk4 = 4;  // walk selector: the 4-wide BVH
+template <bool ANY>
+__device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
+  const DevAccel& A = S.accel;
+  F3 inv = {fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(1e30f, d.x),
+            fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(1e30f, d.y),
+            fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(1e30f, d.z)};
+  F3 ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
+  PHit best{-1, tmax};
+  constexpr int kS = 64;
+  int stack_ref[kS];
+  float stack_tn[kS];
+  int sp = 0, cur = 0, cnt = 0;
+  const bool cond = !(contact == -1 && inside == -1);
+  while (true) {
+    if (cur >= 0) {
+      const float4* np = A.bvh4 + 8 * (size_t)cur;
+      float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+      float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+      int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
+      const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+      const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+      const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+      int r[4] = {cr.x, cr.y, cr.z, cr.w}, c[4] = {cc.x, cc.y, cc.z, cc.w};
+      float tn[4];
+      int nh = 0;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        float a0 = fmaf(lxa[j], inv.x, -ood.x), b0 = fmaf(hxa[j], inv.x, -ood.x);
+        float a1 = fmaf(lya[j], inv.y, -ood.y), b1 = fmaf(hya[j], inv.y, -ood.y);
+        float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
+        float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
+        float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), best.t));
+        bool h = r[j] != 0x7fffffff && t0 <= t1 * 1.0000005f;
+        tn[j] = h ? t0 : INFINITY;
+        nh += h ? 1 : 0;
+      }
+      auto cs = [&](int a, int b) {
+        if (tn[b] < tn[a]) {
+          float t = tn[a];
+          tn[a] = tn[b];
+          tn[b] = t;
+          int q = r[a];
+          r[a] = r[b];
+          r[b] = q;
+          q = c[a];
+          c[a] = c[b];
+          c[b] = q;
+        }
+      };
+      cs(0, 1);
+      cs(2, 3);
+      cs(0, 2);
+      cs(1, 3);
+      cs(1, 2);
+      if (nh > 0) {
+#pragma unroll
+        for (int k = 3; k >= 1; k--)
+          if (k < nh && sp < kS) {
+            stack_ref[sp] = r[k] < 0 ? ~((~r[k]) << 3 | (c[k] - 1)) : r[k];
+            stack_tn[sp] = tn[k];
+            sp++;
+          }
+        cur = r[0];
+        cnt = c[0];
+        continue;
+      }
+    } else {
+      int first = ~cur;
+      for (int k = 0; k < cnt; k++) {
+        const float4* tp = A.tris + 3 * (size_t)(first + k);
+        float4 w0 = __ldg(tp), w1 = __ldg(tp + 1), w2 = __ldg(tp + 2);
+        F3 v0 = f3(w0), e1 = f3(w1) - v0, e2 = f3(w2) - v0;
+        F3 pv = cross(d, e2);
+        float det = dot(e1, pv);
+        if (fabsf(det) < 1e-30f) continue;
+        float idet = 1.0f / det;
+        F3 sv = o - v0;
+        float u = dot(sv, pv) * idet;
+        if (u < -1e-7f || u > 1.0000001f) continue;
+        F3 qv = cross(sv, e1);
+        float v = dot(d, qv) * idet;
+        if (v < -1e-7f || u + v > 1.0000001f) continue;
+        float t = dot(e2, qv) * idet;
+        if (!(t >= 0.0f) || !(t < best.t)) continue;
+        if (cond) {
+          const float4* nn = S.slot_n + 3 * (size_t)(first + k);
+          float4 q0 = __ldg(nn), q1 = __ldg(nn + 1), q2 = __ldg(nn + 2);
+          int obj = __float_as_int(q0.w);
+          F3 n = normalize(f3(q0) * (1.0f - u - v) + f3(q1) * u + f3(q2) * v);
+          if (!legal_hit(contact, inside, obj, dot(d, n))) continue;
+        }
+        best = {__float_as_int(w0.w), t};
+        if (ANY) return best;
+      }
+    }
+    bool found = false;
+    while (sp > 0) {
+      sp--;
+      if (stack_tn[sp] <= best.t) {
+        int rr = stack_ref[sp];
+        if (rr < 0) {
+          int packed = ~rr;
+          cur = ~(packed >> 3);
+          cnt = (packed & 7) + 1;
+        } else {
+          cur = rr;
+        }
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+  }
+  return best;
+}
+
+// Closest / any legal hit with the walk WALK selects: kWalk4 = the 4-wide BVH, else the
+// binary BVH with a stack of WALK entries.
+template <bool ANY, int WALK>
+__device__ __forceinline__ PHit trace_walk(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
+  if constexpr (WALK == kWalk4) return trace_cond4<ANY>(S, o, d, tmax, contact, inside);
+  else return trace_cond<ANY, WALK>(S, o, d, tmax, contact, inside);
+}
+
 }  // namespace rx
