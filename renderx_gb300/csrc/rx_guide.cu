@@ -140,24 +140,29 @@ __device__ __forceinline__ void store_chunk(unsigned char* base, uint32_t off, c
 // Encodes one query (position, normal, outgoing direction) into row s of the 128 x 80
 // input tile. Feature j < 72: coordinate c = j / 24, frequency f = (j % 24) / 2,
 // sin (j even) or cos (j odd) of pi 2^f p_c with p_c = (x_c - min_c) / extent_c;
-// 72..74 normal, 75..77 outgoing direction, 78 = 1, 79 = 0.
+// 72..74 normal, 75..77 outgoing direction, 78 = 1, 79 = 0. Frequency 0 comes from
+// sincospif, each next one from the double-angle identities (sin 2a = 2 sin a cos a,
+// cos 2a = (cos a - sin a)(cos a + sin a)): the angle error doubles per step, about
+// 1e-4 at f = 11, far below the BF16 rounding of the features (4e-3).
 __device__ void encode_row(const float (&q)[9], bool valid, const Box& box, unsigned char* A0, int s) {
-  float p[3];
 #pragma unroll
-  for (int c = 0; c < 3; c++) p[c] = valid ? __fdiv_rn(__fsub_rn(q[c], box.mn[c]), box.ext[c]) : 0.0f;
+  for (int c = 0; c < 3; c++) {
+    float p = valid ? __fdiv_rn(__fsub_rn(q[c], box.mn[c]), box.ext[c]) : 0.0f;
+    float sn = 0.0f, cs = 0.0f;
+    if (valid) sincospif(p, &sn, &cs);
 #pragma unroll
-  for (int ch = 0; ch < 9; ch++) {
-    float f[8];
+    for (int part = 0; part < 3; part++) {  // 4 frequencies = 8 features = one 16-byte row chunk
+      float f[8];
 #pragma unroll
-    for (int t = 0; t < 8; t += 2) {
-      int j = ch * 8 + t;
-      int c = j / 24, fr = (j % 24) / 2;
-      float sn = 0.0f, cs = 0.0f;
-      if (valid) sincospif(ldexpf(p[c], fr), &sn, &cs);
-      f[t] = sn;
-      f[t + 1] = cs;
+      for (int t = 0; t < 4; t++) {
+        f[2 * t] = sn;
+        f[2 * t + 1] = cs;
+        float s2 = 2.0f * sn * cs, c2 = (cs - sn) * (cs + sn);
+        sn = s2;
+        cs = c2;
+      }
+      store_chunk(A0, tc::core_off(s, c * 24 + part * 8, kIn), f);
     }
-    store_chunk(A0, tc::core_off(s, ch * 8, kIn), f);
   }
   float f[8] = {q[3], q[4], q[5], q[6], q[7], q[8], 1.0f, 0.0f};
   if (!valid)
@@ -474,123 +479,164 @@ __global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t 
   }
 }
 
-// Gradient of the batch loss over records [first, first + len) (clipped to the live
-// count): forward and backward per tile, weight gradients accumulated in tensor memory,
-// flushed once per CTA into `grad` (FP32, row-major per layer). wsum = {sum w, count}.
-// Weights are clipped at 32 x their batch mean before normalisation by the sum.
-__global__ void __launch_bounds__(128, 1) k_guide_train(const float* recs, const unsigned* count, uint32_t n_host,
-                                                        uint32_t first0, uint32_t len, int step, const unsigned char* img,
-                                                        Box box, const float* wsum, float* grad, float* loss_sum,
-                                                        int* status) {
+// Gradient of the batch loss over the records a window selects (train_window): forward
+// and backward per tile, weight gradients accumulated in tensor memory across all tiles
+// a CTA processes, flushed once per CTA into `grad` (FP32, row-major per layer).
+// wsum = {sum w, count}; weights are clipped at 32 x their batch mean before
+// normalisation by the sum.
+//
+// A CTA carries kTrainTiles tiles of 128 samples at once, one warpgroup per tile (thread
+// s of warpgroup g owns sample s of tile g, TMEM lane s of that tile's accumulator).
+// One thread issues every MMA, so the shared weight-gradient accumulators see each
+// tile's contribution in order, and one warpgroup's epilogue overlaps the other tile's
+// MMAs. The 128 x 80 input tile is not kept: it lives in the region of activations 3-4
+// during the forward pass and is encoded again from the records for the last weight
+// gradient.
+constexpr int kTrainTiles = 2;
+constexpr uint32_t kTrainTileBytes = 5 * kActBytes;  // A1, A2, A3|A4 (A0 alias), dZ
+constexpr uint32_t kSmTrain2 = kImgBytes + kTrainTiles * kTrainTileBytes;
+
+__device__ __forceinline__ void load_record(const float* recs, uint32_t i, float (&q)[9], float (&wi)[3], float& w) {
+  const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
+  float4 a = r[0], b = r[1], c = r[2], e = r[3];
+  q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w; q[8] = c.x;
+  wi[0] = c.y; wi[1] = c.z; wi[2] = c.w;
+  w = e.x;
+}
+
+__global__ void __launch_bounds__(128 * kTrainTiles, 1)
+    k_guide_train(const float* recs, const unsigned* count, uint32_t n_host, uint32_t first0, uint32_t len, int step,
+                  const unsigned char* img, Box box, const float* wsum, float* grad, float* loss_sum, int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) uint64_t bar_mma, bar_w;
+  __shared__ __align__(8) uint64_t bar_mma[kTrainTiles], bar_w;
   __shared__ uint32_t tmem_base;
-  __shared__ float red[4];
-  const int s = threadIdx.x, warp = s >> 5;
+  __shared__ float red[4 * kTrainTiles];
+  const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, s = tid & 127;
   uint32_t first, end;
   train_window(count, n_host, first0, len, step, first, end);
   const uint32_t n = end - first;
-  const uint32_t ntiles = (n + kTile - 1) / kTile;
-  if (blockIdx.x >= ntiles) return;
-  if (s == 0) {
-    tc::mbar_init(&bar_mma, 1);
+  const uint32_t ngroups = (n + kTile * kTrainTiles - 1) / (kTile * kTrainTiles);
+  if (blockIdx.x >= ngroups) return;
+  if (tid == 0) {
+    for (int k = 0; k < kTrainTiles; k++) tc::mbar_init(&bar_mma[k], 1);
     tc::mbar_init(&bar_w, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
-  if (s == 0) load_weights(sm, img, &bar_w);
+  if (tid == 0) load_weights(sm, img, &bar_w);
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   tc_sync();
   const uint32_t T0 = tmem_base;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-  const uint32_t t_fwd = T0, t_da = T0 + 64;
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+  // TMEM columns: per tile one 64-column accumulator (forward, then dA); the shared dW
   const uint32_t t_dw[5] = {T0 + 128, T0 + 208, T0 + 272, T0 + 336, T0 + 400};
-  unsigned char* A[5] = {sm + kSmA0, sm + kSmA1, sm + kSmA1 + kActBytes, sm + kSmA1 + 2 * kActBytes,
-                         sm + kSmA1 + 3 * kActBytes};
-  unsigned char* dZ = sm + kSmA1 + 4 * kActBytes;
+  unsigned char* tile_base[kTrainTiles];
+  for (int k = 0; k < kTrainTiles; k++) tile_base[k] = sm + kImgBytes + k * kTrainTileBytes;
+  // this warpgroup's buffers
+  unsigned char* A1 = tile_base[g];
+  unsigned char* A2 = A1 + kActBytes;
+  unsigned char* A34 = A1 + 2 * kActBytes;  // A3, A4; A0 (20 KB) aliases it
+  unsigned char* dZ = A1 + 4 * kActBytes;
+  unsigned char* Al[5] = {A34, A1, A2, A34, A34 + kActBytes};
+  const uint32_t t_acc = T0 + 64u * (uint32_t)g + lane_off;
   const float total = wsum[0], cnt = fmaxf(wsum[1], 1.0f);
   const float wclip = 32.0f * total / cnt;
   const float inv_total = total > 0.0f ? 1.0f / total : 0.0f;
   bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0));
   uint32_t ph = 0;
-  bool first_tile = true;
+  bool first_group = true;
   float loss = 0.0f;
-  for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    uint32_t i = first + tile * kTile + s;
-    bool valid = i < end;
+  // operand pointers of tile k's layer l (for the issuing thread)
+  auto act = [&](int k, int l) -> unsigned char* {
+    unsigned char* b = tile_base[k];
+    return l == 0 ? b + 2 * kActBytes : l == 1 ? b : l == 2 ? b + kActBytes : l == 3 ? b + 2 * kActBytes
+                                                                                      : b + 3 * kActBytes;
+  };
+  for (uint32_t grp = blockIdx.x; ok && grp < ngroups; grp += gridDim.x) {
+    const uint32_t i = first + (grp * kTrainTiles + g) * kTile + s;
+    const bool valid = i < end;
     float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0}, w = 0.0f;
     if (valid) {
-      const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
-      float4 a = r[0], b = r[1], c = r[2], e = r[3];
-      q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w; q[8] = c.x;
-      wi[0] = c.y; wi[1] = c.z; wi[2] = c.w;
-      w = fminf(e.x, wclip) * inv_total;
+      load_record(recs, i, q, wi, w);
+      w = fminf(w, wclip) * inv_total;
     }
-    encode_row(q, valid, box, A[0], s);
+    encode_row(q, valid, box, Al[0], s);
     tc_sync();
-    // forward
+    // forward: layer l of every tile, then every warpgroup's epilogue
     for (int l = 0; l < 5 && ok; l++) {
-      if (s == 0) {
-        issue_fwd(T0, A[l], sm + kSmW + layer_img(l), layer_k(l));
-        tc::mma_commit(&bar_mma);
+      if (tid == 0) {
+        for (int k = 0; k < kTrainTiles; k++) {
+          issue_fwd(T0 + 64u * k, act(k, l), sm + kSmW + layer_img(l), layer_k(l));
+          tc::mma_commit(&bar_mma[k]);
+        }
       }
-      ok = __syncthreads_and(tc::mbar_wait(&bar_mma, ph));
-      ph ^= 1;
+      ok = tc::mbar_wait(&bar_mma[g], ph);
       tc::tc_fence_after();
-      if (!ok) break;
-      if (l < 4) {
-        epi_relu(t_fwd + lane_off, A[l + 1], s);
-      } else {
-        float raw[48], dz[48];
-        load_raw(t_fwd + lane_off, raw);
-        if (valid && w > 0.0f) {
-          loss += mix_loss_grad(raw, wi, w, dz);
+      if (ok) {
+        if (l < 4) {
+          epi_relu(t_acc, Al[l + 1], s);
         } else {
+          float raw[48], dz[48];
+          load_raw(t_acc, raw);
+          if (valid && w > 0.0f) {
+            loss += mix_loss_grad(raw, wi, w, dz);
+          } else {
 #pragma unroll
-          for (int k = 0; k < 48; k++) dz[k] = 0.0f;
-        }
+            for (int k = 0; k < 48; k++) dz[k] = 0.0f;
+          }
 #pragma unroll
-        for (int c0 = 0; c0 < 64; c0 += 8) {
-          float f[8];
+          for (int c0 = 0; c0 < 64; c0 += 8) {
+            float f[8];
 #pragma unroll
-          for (int k = 0; k < 8; k++) f[k] = c0 + k < 48 ? dz[c0 + k] : 0.0f;
-          store_chunk(dZ, tc::core_off(s, c0, kOut), f);
-        }
-      }
-      tc_sync();
-    }
-    // backward: dZ holds dZ_{l+1}; dW_l += dZ^T A_l; dA_l = dZ W_l; dZ_l = dA_l * [A_l > 0]
-    for (int l = 4; l >= 0 && ok; l--) {
-      const int K = layer_k(l);
-      if (s == 0) {
-        const uint32_t dz0 = tc::smem_u32(dZ), a0 = tc::smem_u32(A[l]), w0 = tc::smem_u32(sm + kSmW + layer_img(l));
-        const uint32_t id_w = tc::idesc_bf16(64, (uint32_t)K, true, true);
-        for (int s0 = 0; s0 < kTile; s0 += 16) {
-          uint64_t ad = tc::sdesc(dz0 + tc::core_off(s0, 0, kOut), (kOut >> 3) * 128u, 128u);
-          uint64_t bd = tc::sdesc(a0 + tc::core_off(s0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
-          tc::mma_bf16(t_dw[l], ad, bd, id_w, (first_tile && s0 == 0) ? 0u : 1u);
-        }
-        if (l > 0) {
-          const uint32_t id_a = tc::idesc_bf16(128, (uint32_t)K, false, true);
-          for (int n0 = 0; n0 < kOut; n0 += 16) {
-            uint64_t ad = tc::sdesc(dz0 + tc::core_off(0, n0, kOut), 128u, (kOut >> 3) * 128u);
-            uint64_t bd = tc::sdesc(w0 + tc::core_off(n0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
-            tc::mma_bf16(t_da, ad, bd, id_a, n0 > 0);
+            for (int k = 0; k < 8; k++) f[k] = c0 + k < 48 ? dz[c0 + k] : 0.0f;
+            store_chunk(dZ, tc::core_off(s, c0, kOut), f);
           }
         }
-        tc::mma_commit(&bar_mma);
       }
-      ok = __syncthreads_and(tc::mbar_wait(&bar_mma, ph));
+      ok = __syncthreads_and(ok);
       ph ^= 1;
+      tc::fence_async_smem();
+      tc::tc_fence_before();
+      __syncthreads();
       tc::tc_fence_after();
-      if (!ok) break;
-      if (l > 0) {
+    }
+    // backward: dZ holds dZ_{l+1}; dW_l += dZ^T A_l over both tiles; dA_l = dZ W_l
+    for (int l = 4; l >= 0 && ok; l--) {
+      const int K = layer_k(l);
+      if (l == 0) {  // the input tile again, into the (now free) activation 3-4 region
+        encode_row(q, valid, box, Al[0], s);
+        tc_sync();
+      }
+      if (tid == 0) {
+        const uint32_t w0 = tc::smem_u32(sm + kSmW + layer_img(l));
+        const uint32_t id_w = tc::idesc_bf16(64, (uint32_t)K, true, true);
+        const uint32_t id_a = tc::idesc_bf16(128, (uint32_t)K, false, true);
+        for (int k = 0; k < kTrainTiles; k++) {
+          const uint32_t dz0 = tc::smem_u32(tile_base[k] + 4 * kActBytes), a0 = tc::smem_u32(act(k, l));
+          for (int s0 = 0; s0 < kTile; s0 += 16) {
+            uint64_t ad = tc::sdesc(dz0 + tc::core_off(s0, 0, kOut), (kOut >> 3) * 128u, 128u);
+            uint64_t bd = tc::sdesc(a0 + tc::core_off(s0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
+            tc::mma_bf16(t_dw[l], ad, bd, id_w, (first_group && k == 0 && s0 == 0) ? 0u : 1u);
+          }
+          if (l > 0) {
+            for (int n0 = 0; n0 < kOut; n0 += 16) {
+              uint64_t ad = tc::sdesc(dz0 + tc::core_off(0, n0, kOut), 128u, (kOut >> 3) * 128u);
+              uint64_t bd = tc::sdesc(w0 + tc::core_off(n0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
+              tc::mma_bf16(T0 + 64u * k, ad, bd, id_a, n0 > 0);
+            }
+          }
+          tc::mma_commit(&bar_mma[k]);
+        }
+      }
+      ok = tc::mbar_wait(&bar_mma[g], ph);
+      tc::tc_fence_after();
+      if (ok && l > 0) {
 #pragma unroll
         for (int c0 = 0; c0 < kHid; c0 += 16) {
           float v[16];
-          tc::tmem_ld16(t_da + lane_off + c0, v);
-          uint4 m0 = *reinterpret_cast<const uint4*>(A[l] + tc::core_off(s, c0, kHid));
-          uint4 m1 = *reinterpret_cast<const uint4*>(A[l] + tc::core_off(s, c0 + 8, kHid));
+          tc::tmem_ld16(t_acc + c0, v);
+          uint4 m0 = *reinterpret_cast<const uint4*>(Al[l] + tc::core_off(s, c0, kHid));
+          uint4 m1 = *reinterpret_cast<const uint4*>(Al[l] + tc::core_off(s, c0 + 8, kHid));
           uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
           float a[8], b[8];
 #pragma unroll
@@ -604,12 +650,17 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const float* recs, const
           store_chunk(dZ, tc::core_off(s, c0 + 8, kHid), b);
         }
       }
-      tc_sync();
+      ok = __syncthreads_and(ok);
+      ph ^= 1;
+      tc::fence_async_smem();
+      tc::tc_fence_before();
+      __syncthreads();
+      tc::tc_fence_after();
     }
-    first_tile = false;
+    first_group = false;
   }
-  // flush the weight-gradient accumulators
-  if (ok && !first_tile) {
+  // flush the weight-gradient accumulators (warpgroup 0 reads them)
+  if (ok && !first_group && g == 0) {
     const int row = m64_row(s);
     for (int l = 0; l < 5; l++) {
       const int K = layer_k(l);
@@ -623,11 +674,15 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const float* recs, const
     }
   }
   for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-  if ((s & 31) == 0) red[warp] = loss;
-  if (!ok && s == 0) atomicExch(status, 1);
+  if ((tid & 31) == 0) red[warp] = loss;
+  if (!ok && tid == 0) atomicExch(status, 1);
   tc::tc_fence_before();
   __syncthreads();
-  if (s == 0) atomicAdd(loss_sum, red[0] + red[1] + red[2] + red[3]);
+  if (tid == 0) {
+    float t = 0.0f;
+    for (int k = 0; k < 4 * kTrainTiles; k++) t += red[k];
+    atomicAdd(loss_sum, t);
+  }
   if (warp == 0) tc::tmem_dealloc(T0, 512);
 }
 
@@ -721,7 +776,7 @@ static void set_kernel_smem() {
   if (dev < 64 && (done_mask >> dev) & 1) return;
   cudaFuncSetAttribute(k_guide_infer<RecordIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
   cudaFuncSetAttribute(k_guide_infer<PathIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
-  cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTrain);
+  cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTrain2);
   if (dev < 64) done_mask |= 1ull << dev;
 }
 
@@ -742,10 +797,10 @@ static cudaError_t train_step(GuideState* g, const float* recs, const unsigned* 
   float* sc = g->scratch.as<float>();
   cudaMemsetAsync(sc, 0, 3 * sizeof(float), s);
   k_weight_sum<<<g->sms * 4, 256, 0, s>>>(recs, count, n, first, len, step, sc);
-  uint32_t tiles = (std::min(len, n) + kTile - 1) / kTile;
-  uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)g->sms);
+  uint32_t groups = (std::min(len, n) + kTile * kTrainTiles - 1) / (kTile * kTrainTiles);
+  uint32_t grid = std::min<uint32_t>(groups, (uint32_t)g->sms);
   if (grid == 0) return cudaGetLastError();
-  k_guide_train<<<grid, 128, kSmTrain, s>>>(recs, count, n, first, len, step, g->img.as<unsigned char>(), g->box, sc,
+  k_guide_train<<<grid, 128 * kTrainTiles, kSmTrain2, s>>>(recs, count, n, first, len, step, g->img.as<unsigned char>(), g->box, sc,
                                             g->grad.as<float>(), sc + 2, g->status.as<int>());
   if (update) {
     g->step++;

@@ -36,15 +36,17 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-// Waits for the phase with parity `phase` to complete, at most `limit` polls.
+// Waits for the phase with parity `phase` to complete, at most `limit` polls. The poll
+// is the non-blocking test_wait: try_wait may suspend the thread for a system-dependent
+// time, which adds that latency to every dependent MMA -> epilogue step.
 // Returns false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit = 1u << 24) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit = 1u << 26) {
   uint32_t a = smem_u32(bar);
   for (uint32_t it = 0; it < limit; it++) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
         : "r"(a), "r"(phase)
