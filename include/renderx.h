@@ -136,11 +136,15 @@ typedef struct rx_vcm_options {
   uint32_t iterations;     /* progressive iterations (the reference loops until its time budget) */
   uint32_t max_depth;      /* MCRenderer::maxDepth, at most 21 */
   uint32_t light_paths;    /* light subpaths per iteration, 0 = width*height (the reference) */
-  uint32_t flags;          /* reserved, 0 */
+  uint32_t flags;          /* RX_VCM_FULL_PATH_MIS or 0 */
   float radius;            /* initial merge radius (VCMTracer::mergeRadius, <radius> in XML) */
   float alpha;             /* radius shrink: r *= ((s+alpha)/(s+1))^(1/3) (reference default 0.6667) */
   uint64_t seed;
 } rx_vcm_options;
+/* Evaluate each merge's colour and MIS weight with the reference's loops over the whole
+ * joined path (VCMTracer::connectColorProb / connectMergeWeight, O(path length) per
+ * pair) instead of the per-subpath records (O(1) per pair). Same estimator; slower. */
+#define RX_VCM_FULL_PATH_MIS 1u
 
 typedef struct rx_render_stats {
   uint64_t extension_rays; /* closest-hit rays traced (camera + bounce) */

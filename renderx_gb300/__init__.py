@@ -231,10 +231,12 @@ class Context:
                            blocks_per_sm=bo.chosen_blocks_per_sm, stack=bo.chosen_stack)
 
     def render_vcm(self, camera: "scenes.Camera", iterations: int, radius: float, alpha: float = 0.6667,
-                   max_depth: int = 8, light_paths: int = 0, seed: int = 1):
-        """VCMTracer renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats)."""
+                   max_depth: int = 8, light_paths: int = 0, seed: int = 1, full_path_mis: bool = False):
+        """VCMTracer renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats).
+        ``full_path_mis`` evaluates merges with the reference's whole-path loops
+        (RX_VCM_FULL_PATH_MIS) instead of the per-subpath records."""
         cam = camera_struct(camera)
-        o = rx_vcm_options(iterations, max_depth, light_paths, 0, radius, alpha, seed)
+        o = rx_vcm_options(iterations, max_depth, light_paths, 1 if full_path_mis else 0, radius, alpha, seed)
         film = np.zeros((camera.height, camera.width, 3), np.float64)
         st = rx_render_stats()
         self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))

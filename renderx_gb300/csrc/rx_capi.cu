@@ -432,6 +432,7 @@ rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_option
   if (opts->max_depth > 21) return c->fail(RX_ERR_INVALID, "max_depth must be at most 21");
   if (!(opts->radius > 0.0f) || !(opts->alpha > 0.0f)) return c->fail(RX_ERR_INVALID, "radius and alpha must be positive");
   if (c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "vertex connection and merging needs an emitter");
+  if (opts->flags & ~RX_VCM_FULL_PATH_MIS) return c->fail(RX_ERR_INVALID, "unknown VCM flags");
   DeviceGuard g(c->device);
   size_t np = (size_t)cam->width * cam->height;
   DevBuf film;

@@ -317,7 +317,6 @@ constexpr uint32_t kSmA0 = kImgBytes;                // 128 x 80 input tile
 constexpr uint32_t kSmA1 = kSmA0 + 128 * kIn * 2;    // hidden activations, 128 x 64 each
 constexpr uint32_t kActBytes = 128 * kHid * 2;
 constexpr uint32_t kSmInfer = kSmA1 + 2 * kActBytes;                 // inference: 2 ping-pong buffers
-constexpr uint32_t kSmTrain = kSmA1 + 4 * kActBytes + kActBytes;     // training: A1..A4 + dZ
 
 // Loads the weight image into shared memory with bulk copies (one per layer).
 __device__ __forceinline__ void load_weights(unsigned char* sm, const unsigned char* img, uint64_t* bar) {

@@ -119,9 +119,179 @@ __device__ __forceinline__ PV load_pv(const float4* p) {
   return v;
 }
 
+// ---- the MIS weight of a merge in O(1) ---------------------------------------------------
+// connectMergeWeight sums, over every technique that could have made the joined path
+// w[0..n-1] (light vertices 0..ci, eye vertices after), products pf[i] pb[i+1] of
+// forward and backward pdf chains. For a merge at light vertex ci with eye vertex E
+// (w[ci+1]), connectRays changes only the directions at ci and ci+1 (and E's colour,
+// direction pdf, sampling flag and inside object), and VCMTracer::link reverses a
+// vertex only by its neighbours' positions, so:
+//  - pf[0..ci] and the ratios pb[i] / pb[ci-1] (i <= ci-1) depend on the light subpath
+//    alone, pb[ci+1..n-1] and the ratios pf[i] / pf[ci+2] (i >= ci+2) on the eye
+//    subpath alone;
+//  - the techniques at i <= ci-2 add up to pb[ci-1] * MisL::sl and those at
+//    i >= ci+1 (but the connection at ci+1) to pf[ci+2] * MisE::se, both built once
+//    per subpath by a recursion over its vertices;
+//  - what is left (connection and merge at ci-1 and ci, connection at ci+1, and the
+//    pdfs through the two changed directions) is evaluated per pair.
+// The throughput of connectColorProb splits the same way (MisL::thr, MisE::thr).
+struct alignas(16) MisL {  // per light vertex c, for a merge at ci = c
+  double pf;       // pf[c]
+  double pf_prev;  // pf[c-1]
+  double sl;       // (C_i + M_i, i <= c-2) / pb[c-1]
+  double tl;       // (C_{c-1} + M_{c-1}) / pb[c]
+  double al;       // pb[c-1] / pb[c] without the direction pdf at c
+  double pad;
+  F3 thr;          // prod_{i<c} colour x transmittance x cosine
+  float prob;      // prod_{i<=c} directionProb x originProb
+};
+struct alignas(16) MisE {  // per eye vertex k, for a merge with E = eye vertex k
+  double pb;       // pb at eye vertex k (pb[ci+1])
+  double pb_prev;  // pb at eye vertex k-1 (pb[ci+2])
+  double se;       // (M_{ci+1} + C_i + M_i, i >= ci+2) / pf[ci+2]
+  double fe;       // pf[ci+2] / pf[ci+1] without the direction pdf at E
+  F3 thr;          // prod_{m<k} colour x transmittance x cosine of the eye vertices
+  float prob;      // prod_{m<k} directionProb x originProb
+};
+
+// link(w, n, ci, i, j) for a link against the subpath's own direction: vertex v aimed
+// at u, with u's inside object.
+__device__ __forceinline__ PV rev_to(const PV& v, const PV& u) {
+  PV r = v;
+  r.d = normalize(u.o - v.o);
+  r.inside = u.inside;
+  return r;
+}
+__device__ __forceinline__ float seg_len(const PV& a, const PV& b) { return fmaxf(length(b.o - a.o), 1e-5f); }
+__device__ __forceinline__ bool rnd(const PV& v) { return (v.flags & kDirRandom) != 0u; }
+// the merge technique's pdf factors of connectMergeWeight (VCMTracer.cpp:400-409) past pf, pb
+__device__ __forceinline__ double merge_area(double p, const PV& v, float r, float norm) {
+  p *= RX_PI * r * r;
+  if (v.inside != kNone && v.contact == kNone) p *= 4.0 / 3.0 * r;
+  return p * norm;
+}
+
+// Light-subpath records for c = 0 .. n-2 (the vertices a photon's predecessor can be).
+__device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int n, float r, float norm, MisL* out) {
+  double pf = l[0].oprob, pf_prev = 0.0, sl = 0.0;
+  F3 thr = {1, 1, 1};
+  float prob = 1.0f;
+  for (int c = 0; c + 1 < n; c++) {
+    const PV& v = l[c];
+    prob *= v.dprob * v.oprob;
+    MisL m;
+    m.pf = pf;
+    m.pf_prev = pf_prev;
+    m.sl = sl;
+    m.tl = 0.0;
+    m.al = 0.0;
+    m.pad = 0.0;
+    if (c >= 1) {
+      const PV& a = l[c - 1];
+      float d = seg_len(a, v);
+      PV rv = rev_to(v, a);
+      double al = cos_term(S, cam, a);
+      al /= (double)d * d;
+      if (rnd(v)) al *= origin_pdf(S, rv, a);
+      m.al = al;
+      double tl = rnd(a) && rnd(v) ? pf_prev : 0.0;
+      if (rnd(v)) {
+        double p = pf_prev;
+        if (rnd(a)) p *= c - 1 > 0 ? dir_pdf(S, cam, l[c - 2], a, false) : dir_pdf(S, cam, a, a, true);
+        p *= origin_pdf(S, a, v);
+        p *= cos_term(S, cam, rv);
+        p /= (double)d * d;
+        tl += merge_area(p, v, r, norm);
+      }
+      m.tl = tl;
+    }
+    m.thr = thr;
+    m.prob = prob;
+    out[c] = m;
+    // advance to c + 1
+    const PV& nx = l[c + 1];
+    float d = seg_len(v, nx);
+    thr = thr * v.c;
+    thr = thr * decay_of(S, v.inside, d);
+    thr = thr * cos_term(S, cam, v);
+    double pfn = pf * cos_term(S, cam, rev_to(nx, v));
+    pfn /= (double)d * d;
+    if (rnd(v)) {
+      pfn *= c > 0 ? dir_pdf(S, cam, l[c - 1], v, false) : dir_pdf(S, cam, v, v, true);
+      pfn *= origin_pdf(S, v, nx);
+    }
+    if (c >= 1) {
+      double g = m.al;
+      if (rnd(v)) g *= dir_pdf(S, cam, rev_to(nx, v), rev_to(v, l[c - 1]), false);
+      sl = sl * g + m.tl;
+    }
+    pf_prev = pf;
+    pf = pfn;
+  }
+}
+
+// Eye-subpath records for k = 0 .. n-1 (k >= 1 are merge vertices).
+__device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n, float r, float norm, MisE* out) {
+  double pb = e[0].oprob, pb_prev = 0.0, u = 0.0;
+  F3 thr = {1, 1, 1};
+  float prob = 1.0f;
+  for (int k = 0; k < n; k++) {
+    const PV& v = e[k];
+    MisE m;
+    m.pb = pb;
+    m.pb_prev = pb_prev;
+    m.se = 0.0;
+    m.fe = 0.0;
+    if (k >= 1) {
+      const PV& pe = e[k - 1];
+      float d = seg_len(v, pe);
+      double fe = cos_term(S, cam, pe);
+      fe /= (double)d * d;
+      fe *= origin_pdf(S, rev_to(v, pe), pe);
+      m.fe = fe;
+      m.se = u + (k >= 2 && rnd(pe) ? merge_area(pb_prev, pe, r, norm) : 0.0);
+    }
+    m.thr = thr;
+    m.prob = prob;
+    out[k] = m;
+    if (k + 1 >= n) break;
+    // advance to k + 1
+    const PV& up = e[k + 1];
+    float d = seg_len(v, up);
+    thr = thr * v.c;
+    thr = thr * decay_of(S, v.inside, d);
+    thr = thr * cos_term(S, cam, v);
+    prob *= v.dprob * v.oprob;
+    double pbn = pb * cos_term(S, cam, rev_to(up, v));
+    pbn /= (double)d * d;
+    if (rnd(v)) {
+      pbn *= k > 0 ? dir_pdf(S, cam, e[k - 1], v, false) : dir_pdf(S, cam, v, v, true);
+      pbn *= origin_pdf(S, v, up);
+    }
+    if (k >= 1) {
+      const PV& pe = e[k - 1];
+      float dd = seg_len(v, pe);
+      PV rv = rev_to(v, pe);
+      double g = cos_term(S, cam, pe);
+      g /= (double)dd * dd;
+      double opf = origin_pdf(S, rv, pe);
+      if (rnd(v)) {
+        g *= dir_pdf(S, cam, rev_to(up, v), rv, false);
+        g *= opf;
+      }
+      double un = u * g;
+      if (rnd(v) && rnd(pe)) un += pb_prev;
+      if (k >= 2 && rnd(pe)) un += merge_area(g * pb_prev * (rnd(v) ? 1.0 : opf), pe, r, norm);
+      u = un;
+    }
+    pb_prev = pb;
+    pb = pbn;
+  }
+}
+
 // ---- light subpaths + photons ----------------------------------------------------------
-__global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, float4* photon_pos, int* photon_ref,
-                            unsigned* n_photons, unsigned photon_cap, unsigned long long* rays) {
+__global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, MisL* lmis, float4* photon_pos,
+                            int* photon_ref, unsigned* n_photons, unsigned photon_cap, unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nr = 0;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += stride) {
@@ -133,6 +303,7 @@ __global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, floa
     nr += (unsigned long long)n;
     llen[p] = n;
     for (int i = 0; i < n; i++) store_pv(lv + 4 * ((size_t)p * P.maxv + i), path[i]);
+    light_mis(S, P.cam, path, n, P.radius, P.norm, lmis + (size_t)p * P.maxv);
     for (int i = 1; i < n; i++) {
       if (is_emissive(S, path[i].contact)) break;
       if (!(path[i].flags & kDirRandom)) continue;
@@ -337,7 +508,8 @@ __device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
 // Per pixel: the eye subpath (stored for the merging stage) and colorByConnectingPaths
 // (VCMTracer.cpp:430-562) with this pixel's light path.
 __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const float4* lv, const int* llen,
-                                                 float4* ev, int* elen, float* img, unsigned long long* rays) {
+                                                 float4* ev, int* elen, MisE* emis, float* img,
+                                                 unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nrays = 0;
   const float r = P.radius;
@@ -351,6 +523,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
     nrays += (unsigned long long)ne;
     for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
+    eye_mis(S, P.cam, eye, ne, r, P.norm, emis + (size_t)p * P.maxv);
     F3 acc = {0, 0, 0};
     uint32_t lp = p % P.n_light;
     int nl = llen[lp];
@@ -478,9 +651,118 @@ __global__ void k_merge_fill(DevScene S, VcmParams P, const float4* ev, const in
 }
 
 // One (query, photon) pair per lane, a run of kRun consecutive pairs per thread so that
-// pairs of one pixel add up in registers before the image atomics.
+// pairs of one pixel add up in registers before the image atomics. The pair's light
+// vertex ci (the photon's predecessor, w[ci]) and eye vertex E (w[ci+1]) are joined as
+// connectRays does for a merge; colour, probability and MIS weight come from the two
+// subpaths' records and the pdfs through the two new directions.
 constexpr int kRun = 8;
 __global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
+                                                    const MisL* lmis, const MisE* emis, const int* photon_ref,
+                                                    const uint32_t* pair_q, const int* pair_ph, uint32_t npairs,
+                                                    float* img) {
+  const float r = P.radius;
+  uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kRun; base < npairs; base += stride * kRun) {
+    F3 acc = {0, 0, 0};
+    int acc_pixel = -1;
+    for (uint32_t j = base; j < base + kRun && j < npairs; j++) {
+      uint32_t q = pair_q[j];
+      int ref = photon_ref[pair_ph[j]];
+      int p = (int)(q / P.maxv), k = (int)(q % P.maxv);
+      int lp = ref / (int)P.maxv, ci = ref % (int)P.maxv - 1;
+      const float4* lb = lv + 4 * ((size_t)lp * P.maxv);
+      const float4* eb = ev + 4 * ((size_t)p * P.maxv);
+      const PV L = load_pv(lb + 4 * ci);
+      const PV E = load_pv(eb + 4 * k);
+      const PV pe = load_pv(eb + 4 * (k - 1));
+      const MisL ml = lmis[(size_t)lp * P.maxv + ci];
+      const MisE me = emis[(size_t)p * P.maxv + k];
+      // connectRays (MCRenderer.cpp:50-106), merged: E is interior, so its inside object is updated
+      PV Lp = L;
+      Lp.d = normalize(E.o - L.o);
+      PV Ep = E;
+      Ep.d = -Lp.d;
+      Ep.dprob = 1.0f;
+      Ep.c = bsdf_of(S, P.cam, pe, Ep);
+      Ep.flags |= kDirRandom;
+      if (Ep.contact != kNone) {
+        F3 n0 = contact_normal(S, P.cam, Ep);
+        if (dot(n0, Ep.d) <= 0.0f) Ep.inside = Ep.contact;
+        else if (dot(n0, pe.d) <= 0.0f) Ep.inside = pe.inside;
+        else Ep.inside = find_inside(S, Ep.o, Ep.d, Ep.contact);
+      }
+      const float D = fmaxf(length(E.o - L.o), 1e-5f);
+      const float cosL = cos_term(S, P.cam, Lp), cosE = cos_term(S, P.cam, Ep);
+      const PV rE = rev_to(Ep, pe);
+      const bool rl = rnd(L);
+      const float opf = origin_pdf(S, Lp, rE);
+      PV Lm;
+      float dpf = 1.0f;
+      if (ci > 0) {
+        Lm = load_pv(lb + 4 * (ci - 1));
+        if (rl) dpf = dir_pdf(S, P.cam, Lm, Lp, false);
+      } else if (rl) {
+        dpf = dir_pdf(S, P.cam, Lp, Lp, true);
+      }
+      // connectColorProb (VCMTracer.cpp:248-306)
+      F3 col = ml.thr * L.c;
+      col = col * decay_of(S, L.inside, D);
+      col = col * (cosL * cosE / (D * D));
+      col = col * Ep.c;
+      col = col * me.thr;
+      float prob = ml.prob * (Ep.dprob * E.oprob) * me.prob;
+      prob *= RX_PI * r * r;
+      prob *= cosE;
+      prob /= D * D;
+      prob *= opf;
+      if (Ep.inside != kNone && Ep.contact == kNone) prob *= 4.0f / 3.0f * r;
+      if (length(col) == 0.0f || prob == 0.0f) continue;
+      // connectMergeWeight (VCMTracer.cpp:321-428)
+      const double dd = (double)D * D;
+      double self = ml.pf * me.pb;
+      if (rl) self *= dpf;
+      self *= opf;
+      self *= cosE;
+      self /= dd;
+      self = merge_area(self, Ep, r, P.norm);
+      double sum = self;
+      if (rl) sum += ml.pf * me.pb;  // connection at ci
+      double pb0 = me.pb * cosL;      // pb[ci]
+      pb0 /= dd;
+      pb0 *= dir_pdf(S, P.cam, pe, Ep, false);
+      pb0 *= origin_pdf(S, Ep, L);
+      if (ci > 0) {
+        double pbm = pb0 * ml.al;  // pb[ci-1]
+        if (rl) pbm *= dir_pdf(S, P.cam, Ep, rev_to(L, Lm), false);
+        sum += pbm * ml.sl + pb0 * ml.tl;
+      }
+      double pf1 = ml.pf * cosE;  // pf[ci+1]
+      pf1 /= dd;
+      if (rl) {
+        pf1 *= dpf;
+        pf1 *= opf;
+      }
+      if (rnd(pe)) sum += pf1 * me.pb_prev;  // connection at ci+1
+      double pf2 = pf1 * me.fe * dir_pdf(S, P.cam, Lp, rE, false);
+      sum += pf2 * me.se;
+      double res = self / sum;
+      float wt = res >= 0.0 ? (float)res : 0.0f;
+      F3 c = col * (wt / prob) * (1.0f / P.norm);
+      if (p != acc_pixel) {
+        if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
+        acc = {0, 0, 0};
+        acc_pixel = p;
+      }
+      acc = acc + c;
+    }
+    if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
+  }
+}
+
+// The same pairs evaluated by the reference's loops over the whole joined path
+// (connectRays, connectColorProb, connectMergeWeight): O(path length) per pair, with the
+// path in a per-thread array. Kept as the check of k_merge_eval (RX_VCM_FULL_PATH_MIS).
+__global__ void __launch_bounds__(128) k_merge_eval_full(DevScene S, VcmParams P, const float4* lv, const float4* ev,
                                                     const int* photon_ref, const uint32_t* pair_q,
                                                     const int* pair_ph, uint32_t npairs, float* img) {
   const float r = P.radius;
@@ -555,7 +837,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.n_light * P.maxv;
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(20);
+  std::vector<DevBuf> bufs(22);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
   if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
@@ -577,6 +859,9 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = al(14, (size_t)nq * sizeof(unsigned long long))) != cudaSuccess) return e;            // query counts
   if ((e = al(15, (size_t)nq * sizeof(unsigned long long))) != cudaSuccess) return e;            // query offsets
   if ((e = al(16, ((size_t)nqblk + 2) * sizeof(unsigned long long))) != cudaSuccess) return e;  // block sums
+  if ((e = al(19, (size_t)P.n_light * P.maxv * sizeof(MisL))) != cudaSuccess) return e;         // light MIS records
+  if ((e = al(20, (size_t)P.n_pixels * P.maxv * sizeof(MisE))) != cudaSuccess) return e;        // eye MIS records
+  const bool full_mis = (opt.flags & RX_VCM_FULL_PATH_MIS) != 0;
   const uint32_t pair_cap = 1u << 27;  // pairs per evaluation window
   uint32_t pair_alloc = 1u << 20;      // grows with demand up to pair_cap
   if ((e = al(17, (size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
@@ -598,8 +883,8 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     P.radius = radius;
     P.iter = it;
     cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
-    k_vcm_light<<<grid, 64, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
-                                     bufs[3].as<int>(), nph, cap, ctr);
+    k_vcm_light<<<grid, 64, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[19].as<MisL>(),
+                                     bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap, ctr);
     cudaMemsetAsync(bufs[6].p, 0, bufs[6].bytes, s);
     float cell = 2.0f * radius;
     k_grid_count<<<grid, 256, 0, s>>>(bufs[2].as<float4>(), nph, cap, cell, buckets - 1, bufs[6].as<unsigned>(),
@@ -613,7 +898,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[5].as<int>()};
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
     k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
-                                   bufs[13].as<int>(), bufs[10].as<float>(), ctr + 1);
+                                   bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[10].as<float>(), ctr + 1);
     // merging: count per query, scan, then windows of (query, photon) pairs
     unsigned long long* qc = bufs[14].as<unsigned long long>();
     unsigned long long* qo = bufs[15].as<unsigned long long>();
@@ -637,8 +922,14 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
       uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
       k_merge_fill<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,
                                             qo, nq, w0, pair_alloc, bufs[17].as<uint32_t>(), bufs[18].as<int>());
-      k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[3].as<int>(),
-                                            bufs[17].as<uint32_t>(), bufs[18].as<int>(), np, bufs[10].as<float>());
+      if (full_mis)
+        k_merge_eval_full<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[3].as<int>(),
+                                                   bufs[17].as<uint32_t>(), bufs[18].as<int>(), np,
+                                                   bufs[10].as<float>());
+      else
+        k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
+                                              bufs[20].as<MisE>(), bufs[3].as<int>(), bufs[17].as<uint32_t>(),
+                                              bufs[18].as<int>(), np, bufs[10].as<float>());
     }
     k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
   }

@@ -83,3 +83,22 @@ def test_vcm_rejects_bad_arguments():
             ctx.render_vcm(sc.camera, 2, -1.0)
         with pytest.raises(rx.RxError):
             ctx.render_vcm(sc.camera, 2, 0.1, max_depth=40)
+
+
+@pytest.mark.parametrize("name", ["cornell_vcm", "spheres_vcm", "medium_vcm"])
+def test_factored_merge_mis_matches_full_path_loops(name):
+    """The merge evaluation from per-subpath records (O(1) per pair) against the
+    reference's loops over each whole joined path (RX_VCM_FULL_PATH_MIS) on the same
+    seeded iterations: the subpaths, pairs and connections are the same, so the images
+    differ only by FP32 rounding of the regrouped products and the order of the image
+    atomics."""
+    z, sc = _load(name)
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        for seed in (5, 6):
+            args = (sc.camera, 2, float(z["radius"]), float(z["alpha"]))
+            fast, _ = ctx.render_vcm(*args, max_depth=int(z["max_depth"]), seed=seed)
+            full, _ = ctx.render_vcm(*args, max_depth=int(z["max_depth"]), seed=seed, full_path_mis=True)
+            assert full.mean() > 0
+            np.testing.assert_allclose(fast, full, rtol=1e-3, atol=1e-5 * full.max())
