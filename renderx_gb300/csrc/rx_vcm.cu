@@ -143,7 +143,7 @@ struct alignas(16) MisL {  // per light vertex c, for a merge at ci = c
   double al;       // pb[c-1] / pb[c] without the direction pdf at c
   double pad;
   F3 thr;          // prod_{i<c} colour x transmittance x cosine
-  float prob;      // prod_{i<=c} directionProb x originProb
+  float prob;      // prod_{i<c} directionProb x originProb
 };
 struct alignas(16) MisE {  // per eye vertex k, for a merge with E = eye vertex k
   double pb;       // pb at eye vertex k (pb[ci+1])
@@ -171,14 +171,13 @@ __device__ __forceinline__ double merge_area(double p, const PV& v, float r, flo
   return p * norm;
 }
 
-// Light-subpath records for c = 0 .. n-2 (the vertices a photon's predecessor can be).
+// Light-subpath records for c = 0 .. n-1.
 __device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int n, float r, float norm, MisL* out) {
   double pf = l[0].oprob, pf_prev = 0.0, sl = 0.0;
   F3 thr = {1, 1, 1};
   float prob = 1.0f;
-  for (int c = 0; c + 1 < n; c++) {
+  for (int c = 0; c < n; c++) {
     const PV& v = l[c];
-    prob *= v.dprob * v.oprob;
     MisL m;
     m.pf = pf;
     m.pf_prev = pf_prev;
@@ -208,9 +207,11 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int
     m.thr = thr;
     m.prob = prob;
     out[c] = m;
+    if (c + 1 >= n) break;
     // advance to c + 1
     const PV& nx = l[c + 1];
     float d = seg_len(v, nx);
+    prob *= v.dprob * v.oprob;
     thr = thr * v.c;
     thr = thr * decay_of(S, v.inside, d);
     thr = thr * cos_term(S, cam, v);
@@ -287,6 +288,104 @@ __device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n
     pb_prev = pb;
     pb = pbn;
   }
+}
+
+// connectRays (MCRenderer.cpp:50-106) for light vertex L (w[ci]) and eye vertex E
+// (w[ci+1]). Lm: the light vertex before L (null when ci = 0); pe: the eye vertex
+// before E (null when E is the camera vertex, t = 1). Where the reference's neighbour
+// index clamps onto the vertex itself (pl for ci = 0, pe for t = 1), the vertex is its
+// own neighbour, already redirected. A merge changes only the directions and E.
+__device__ __forceinline__ void join(const DevScene& S, const CamDev& cam, const PV& L, const PV* Lm, const PV& E,
+                                     const PV* pe, bool merged, PV& Lp, PV& Ep) {
+  Lp = L;
+  Lp.d = normalize(E.o - L.o);
+  Ep = E;
+  Ep.d = -Lp.d;
+  if (!merged) {
+    Lp.dprob = 1.0f;
+    Lp.c = bsdf_of(S, cam, Lm ? *Lm : Lp, Lp);
+    Lp.flags |= kDirRandom;
+    if (Lp.contact != kNone && Lm) {
+      F3 n0 = contact_normal(S, cam, Lp);
+      if (dot(n0, Lp.d) <= 0.0f) Lp.inside = Lp.contact;
+      else if (dot(n0, Lm->d) <= 0.0f) Lp.inside = Lm->inside;
+      else Lp.inside = find_inside(S, Lp.o, Lp.d, Lp.contact);
+    }
+  }
+  Ep.dprob = 1.0f;
+  Ep.c = bsdf_of(S, cam, pe ? *pe : Ep, Ep);
+  Ep.flags |= kDirRandom;
+  if (Ep.contact != kNone && pe) {
+    F3 n0 = contact_normal(S, cam, Ep);
+    if (dot(n0, Ep.d) <= 0.0f) Ep.inside = Ep.contact;
+    else if (dot(n0, pe->d) <= 0.0f) Ep.inside = pe->inside;
+    else Ep.inside = find_inside(S, Ep.o, Ep.d, Ep.contact);
+  }
+}
+
+// connectColorProb (VCMTracer.cpp:248-306) and connectMergeWeight (:321-428) of the
+// joined path from the two subpaths' records. Returns false where the reference drops
+// the path (zero colour or probability); col / prob / wt as the reference's.
+__device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, const PV* Lm, const PV& Lp, const PV& Ep,
+                          const PV* pe, const MisL& ml, const MisE& me, bool merged, float r, float norm, F3& col,
+                          float& prob, float& wt) {
+  const float D = fmaxf(length(Ep.o - Lp.o), 1e-5f);
+  const float cosL = cos_term(S, cam, Lp), cosE = cos_term(S, cam, Ep);
+  const PV rE = pe ? rev_to(Ep, *pe) : Ep;  // link(ci+1, ci+2); for t = 1 only its origin is read
+  const bool rl = rnd(Lp);
+  const float opf = origin_pdf(S, Lp, rE);
+  col = ml.thr * Lp.c;
+  col = col * decay_of(S, Lp.inside, D);
+  col = col * (cosL * cosE / (D * D));
+  col = col * Ep.c;
+  col = col * me.thr;
+  prob = ml.prob * (Lp.dprob * Lp.oprob) * (Ep.dprob * Ep.oprob) * me.prob;
+  if (merged) {
+    prob *= RX_PI * r * r;
+    prob *= cosE;
+    prob /= D * D;
+    prob *= opf;
+    if (Ep.inside != kNone && Ep.contact == kNone) prob *= 4.0f / 3.0f * r;
+  }
+  if (!(prob > 0.0f) || !(length(col) > 0.0f)) return false;
+  float dpf = 1.0f;
+  if (rl) dpf = Lm ? dir_pdf(S, cam, *Lm, Lp, false) : dir_pdf(S, cam, Lp, Lp, true);
+  const double dd = (double)D * D;
+  const double C = rl ? ml.pf * me.pb : 0.0;  // connection at ci
+  double M = 0.0;                              // merge at ci (needs an eye vertex after E)
+  if (pe) {
+    M = ml.pf * me.pb;
+    if (rl) M *= dpf;
+    M *= opf;
+    M *= cosE;
+    M /= dd;
+    M = merge_area(M, Ep, r, norm);
+  }
+  double sum = C + M;
+  double pb0 = me.pb * cosL;  // pb[ci]
+  pb0 /= dd;
+  pb0 *= pe ? dir_pdf(S, cam, *pe, Ep, false) : dir_pdf(S, cam, Ep, Ep, true);
+  pb0 *= origin_pdf(S, Ep, L);
+  if (Lm) {
+    double pbm = pb0 * ml.al;  // pb[ci-1]
+    if (rl) pbm *= dir_pdf(S, cam, Ep, rev_to(Lp, *Lm), false);
+    sum += pbm * ml.sl + pb0 * ml.tl;
+  }
+  if (pe) {
+    double pf1 = ml.pf * cosE;  // pf[ci+1]
+    pf1 /= dd;
+    if (rl) {
+      pf1 *= dpf;
+      pf1 *= opf;
+    }
+    if (rnd(*pe)) sum += pf1 * me.pb_prev;  // connection at ci+1
+    double pf2 = pf1 * me.fe * dir_pdf(S, cam, Lp, rE, false);
+    sum += pf2 * me.se;
+  }
+  if (!pe && !Lm) sum += pb0;  // two-vertex path: mustUsePT adds pb[0]
+  double res = (merged ? M : C) / sum;
+  wt = res >= 0.0 ? (float)res : 0.0f;
+  return true;
 }
 
 // ---- light subpaths + photons ----------------------------------------------------------
@@ -504,10 +603,161 @@ __device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
   atomicAdd(img + 3 * pixel + 2, c.z);
 }
 
-// ---- eye subpaths and connections ------------------------------------------------------
-// Per pixel: the eye subpath (stored for the merging stage) and colorByConnectingPaths
-// (VCMTracer.cpp:430-562) with this pixel's light path.
+// ---- eye subpaths and connections as a wavefront -----------------------------------------
+// colorByConnectingPaths (VCMTracer.cpp:430-562) joins every light vertex ci of the
+// pixel's light path with every eye vertex k (s = ci + 1, t = k + 1), plus the pure
+// eye path (s = 0). k_vcm_eye samples and stores the eye subpath and its records, adds
+// the s = 0 technique, and lists which vertices can take part in a connection (sampled
+// at random, not on an emitter past the light's own vertex); the (k, ci) pairs are then
+// evaluated one per lane with their shadow rays (k_conn_eval).
 __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const float4* lv, const int* llen,
+                                                 float4* ev, int* elen, MisE* emis, uint2* cmask,
+                                                 unsigned long long* ccount, float* img, unsigned long long* rays) {
+  uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long nrays = 0;
+  const float r = P.radius;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += stride) {
+    Rng rng(P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+    PV eye[kMaxV];
+    Hit3 h;
+    PV start = camera_ray(S, P.cam, p, rng, h);
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, eye);
+    nrays += (unsigned long long)ne;
+    for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
+    elen[p] = ne;
+    MisE* me = emis + (size_t)p * P.maxv;
+    eye_mis(S, P.cam, eye, ne, r, P.norm, me);
+    // s = 0: the eye path ends on an emitter and no interior vertex was sampled at random
+    // (mustUsePT); its weight is pb[0] / (pb[0] + the two-vertex connection).
+    F3 acc = {0, 0, 0};
+    int first_rand = ne;
+    for (int m = 1; m < ne; m++)
+      if (rnd(eye[m])) {
+        first_rand = m;
+        break;
+      }
+    for (int t = 2; t <= ne && first_rand > t - 2; t++) {
+      const PV& v = eye[t - 1];
+      if (!is_emissive(S, v.contact)) continue;
+      const MisE m = me[t - 1];
+      F3 col = v.c * m.thr;
+      float prob = (v.dprob * v.oprob) * m.prob;
+      if (!(prob > 0.0f) || !(length(col) > 0.0f)) continue;
+      double sum = m.pb;
+      if (t == 2 && rnd(v) && rnd(eye[0])) sum += (double)v.oprob * me[0].pb;
+      double res = m.pb / sum;
+      float wt = res >= 0.0 ? (float)res : 0.0f;
+      F3 c = col * (wt / prob);
+      if (length(c) > 0.0f) acc = acc + c;
+    }
+    img_add(img, (int)p, acc);
+    // connection candidates
+    uint32_t em = 0, lm = 0;
+    for (int k = 0; k < ne; k++)
+      if (rnd(eye[k]) && !is_emissive(S, eye[k].contact)) em |= 1u << k;
+    const uint32_t lp = p % P.n_light;
+    const int nl = llen[lp];
+    for (int ci = 0; ci < nl; ci++) {
+      float4 t4 = lv[4 * ((size_t)lp * P.maxv + ci) + 3];
+      int contact = __float_as_int(t4.x);
+      uint32_t flags = __float_as_uint(t4.w);
+      if ((flags & kDirRandom) && (ci == 0 || !is_emissive(S, contact))) lm |= 1u << ci;
+    }
+    cmask[p] = make_uint2(em, lm);
+    ccount[p] = (unsigned long long)(__popc(em) * __popc(lm));
+  }
+  if (nrays) atomicAdd(rays, nrays);
+}
+
+// Pairs [win0, win0 + cap) of the scanned order: pixel and eye vertex (q = p * maxv + k)
+// and light vertex of each.
+__global__ void k_conn_fill(VcmParams P, const uint2* cmask, const unsigned long long* coff, unsigned long long win0,
+                            uint32_t cap, uint32_t* pair_q, int* pair_c) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += gridDim.x * blockDim.x) {
+    uint2 m = cmask[p];
+    unsigned long long idx = coff[p];
+    for (uint32_t em = m.x; em; em &= em - 1) {
+      int k = __ffs(em) - 1;
+      for (uint32_t lm = m.y; lm; lm &= lm - 1) {
+        if (idx >= win0 && idx - win0 < cap) {
+          pair_q[idx - win0] = p * P.maxv + (uint32_t)k;
+          pair_c[idx - win0] = __ffs(lm) - 1;
+        }
+        idx++;
+      }
+    }
+  }
+}
+
+// One connection per lane (runs of kConnRun per thread, accumulated per pixel): the
+// joined path's colour, probability and MIS weight from the records, then the shadow
+// ray (testVisibility) for the contributions that are not zero.
+constexpr int kConnRun = 4;
+__global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
+                                                   const MisL* lmis, const MisE* emis, const uint32_t* pair_q,
+                                                   const int* pair_c, uint32_t npairs, float* img,
+                                                   unsigned long long* rays) {
+  const float r = P.radius;
+  uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long nrays = 0;
+  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kConnRun; base < npairs;
+       base += stride * kConnRun) {
+    F3 acc = {0, 0, 0};
+    int acc_pixel = -1;
+    for (uint32_t j = base; j < base + kConnRun && j < npairs; j++) {
+      uint32_t q = pair_q[j];
+      int ci = pair_c[j];
+      int p = (int)(q / P.maxv), k = (int)(q % P.maxv);
+      uint32_t lp = (uint32_t)p % P.n_light;
+      const float4* lb = lv + 4 * ((size_t)lp * P.maxv);
+      const float4* eb = ev + 4 * ((size_t)p * P.maxv);
+      const PV L = load_pv(lb + 4 * ci);
+      const PV E = load_pv(eb + 4 * k);
+      PV Lm, pe, Lp, Ep;
+      if (ci > 0) Lm = load_pv(lb + 4 * (ci - 1));
+      if (k > 0) pe = load_pv(eb + 4 * (k - 1));
+      const MisL ml = lmis[(size_t)lp * P.maxv + ci];
+      const MisE me = emis[(size_t)p * P.maxv + k];
+      join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, k > 0 ? &pe : nullptr, false, Lp, Ep);
+      F3 col;
+      float prob, wt;
+      if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, k > 0 ? &pe : nullptr, ml, me, false, r, P.norm,
+                     col, prob, wt))
+        continue;
+      F3 c = col * (wt / prob);
+      if (!(length(c) > 0.0f)) continue;
+      float len = length(Ep.o - Lp.o);
+      nrays++;
+      PHit sh = trace_cond<true>(S, Ep.o, Ep.d, len - 1e-5f, Ep.contact, Ep.inside);  // testVisibility
+      if (sh.tid >= 0) continue;
+      if (k == 0) {  // light tracing: splat onto the pixel the light vertex projects to
+        F3 dir = normalize(Lp.o - Ep.o);
+        float ca = fabsf(dot(P.cam.front, dir));
+        float to_solid = P.cam.sight * P.cam.sight / (ca * ca * ca);
+        float to_surface = to_solid / ca;
+        c = c * (to_surface / (float)P.n_pixels) * ca;
+        float px, py;
+        trans_to_pixel(P.cam, Lp.o, px, py);
+        int ix = (int)px, iy = (int)py;
+        if (ix >= 0 && ix < P.cam.width && iy >= 0 && iy < P.cam.height) img_add(img, iy * P.cam.width + ix, c);
+        continue;
+      }
+      if (p != acc_pixel) {
+        if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
+        acc = {0, 0, 0};
+        acc_pixel = p;
+      }
+      acc = acc + c;
+    }
+    if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
+  }
+  if (nrays) atomicAdd(rays, nrays);
+}
+
+// Per pixel: the eye subpath and colorByConnectingPaths by the reference's loops over each
+// whole joined path, a shadow ray per connection in the same thread. Kept as the check of
+// k_vcm_eye + k_conn_eval (RX_VCM_FULL_PATH_MIS).
+__global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, const float4* lv, const int* llen,
                                                  float4* ev, int* elen, MisE* emis, float* img,
                                                  unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
@@ -677,76 +927,13 @@ __global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, con
       const PV pe = load_pv(eb + 4 * (k - 1));
       const MisL ml = lmis[(size_t)lp * P.maxv + ci];
       const MisE me = emis[(size_t)p * P.maxv + k];
-      // connectRays (MCRenderer.cpp:50-106), merged: E is interior, so its inside object is updated
-      PV Lp = L;
-      Lp.d = normalize(E.o - L.o);
-      PV Ep = E;
-      Ep.d = -Lp.d;
-      Ep.dprob = 1.0f;
-      Ep.c = bsdf_of(S, P.cam, pe, Ep);
-      Ep.flags |= kDirRandom;
-      if (Ep.contact != kNone) {
-        F3 n0 = contact_normal(S, P.cam, Ep);
-        if (dot(n0, Ep.d) <= 0.0f) Ep.inside = Ep.contact;
-        else if (dot(n0, pe.d) <= 0.0f) Ep.inside = pe.inside;
-        else Ep.inside = find_inside(S, Ep.o, Ep.d, Ep.contact);
-      }
-      const float D = fmaxf(length(E.o - L.o), 1e-5f);
-      const float cosL = cos_term(S, P.cam, Lp), cosE = cos_term(S, P.cam, Ep);
-      const PV rE = rev_to(Ep, pe);
-      const bool rl = rnd(L);
-      const float opf = origin_pdf(S, Lp, rE);
-      PV Lm;
-      float dpf = 1.0f;
-      if (ci > 0) {
-        Lm = load_pv(lb + 4 * (ci - 1));
-        if (rl) dpf = dir_pdf(S, P.cam, Lm, Lp, false);
-      } else if (rl) {
-        dpf = dir_pdf(S, P.cam, Lp, Lp, true);
-      }
-      // connectColorProb (VCMTracer.cpp:248-306)
-      F3 col = ml.thr * L.c;
-      col = col * decay_of(S, L.inside, D);
-      col = col * (cosL * cosE / (D * D));
-      col = col * Ep.c;
-      col = col * me.thr;
-      float prob = ml.prob * (Ep.dprob * E.oprob) * me.prob;
-      prob *= RX_PI * r * r;
-      prob *= cosE;
-      prob /= D * D;
-      prob *= opf;
-      if (Ep.inside != kNone && Ep.contact == kNone) prob *= 4.0f / 3.0f * r;
-      if (length(col) == 0.0f || prob == 0.0f) continue;
-      // connectMergeWeight (VCMTracer.cpp:321-428)
-      const double dd = (double)D * D;
-      double self = ml.pf * me.pb;
-      if (rl) self *= dpf;
-      self *= opf;
-      self *= cosE;
-      self /= dd;
-      self = merge_area(self, Ep, r, P.norm);
-      double sum = self;
-      if (rl) sum += ml.pf * me.pb;  // connection at ci
-      double pb0 = me.pb * cosL;      // pb[ci]
-      pb0 /= dd;
-      pb0 *= dir_pdf(S, P.cam, pe, Ep, false);
-      pb0 *= origin_pdf(S, Ep, L);
-      if (ci > 0) {
-        double pbm = pb0 * ml.al;  // pb[ci-1]
-        if (rl) pbm *= dir_pdf(S, P.cam, Ep, rev_to(L, Lm), false);
-        sum += pbm * ml.sl + pb0 * ml.tl;
-      }
-      double pf1 = ml.pf * cosE;  // pf[ci+1]
-      pf1 /= dd;
-      if (rl) {
-        pf1 *= dpf;
-        pf1 *= opf;
-      }
-      if (rnd(pe)) sum += pf1 * me.pb_prev;  // connection at ci+1
-      double pf2 = pf1 * me.fe * dir_pdf(S, P.cam, Lp, rE, false);
-      sum += pf2 * me.se;
-      double res = self / sum;
-      float wt = res >= 0.0 ? (float)res : 0.0f;
+      PV Lm, Lp, Ep;
+      if (ci > 0) Lm = load_pv(lb + 4 * (ci - 1));
+      join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, &pe, true, Lp, Ep);
+      F3 col;
+      float prob, wt;
+      if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, &pe, ml, me, true, r, P.norm, col, prob, wt))
+        continue;
       F3 c = col * (wt / prob) * (1.0f / P.norm);
       if (p != acc_pixel) {
         if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
@@ -861,6 +1048,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = al(16, ((size_t)nqblk + 2) * sizeof(unsigned long long))) != cudaSuccess) return e;  // block sums
   if ((e = al(19, (size_t)P.n_light * P.maxv * sizeof(MisL))) != cudaSuccess) return e;         // light MIS records
   if ((e = al(20, (size_t)P.n_pixels * P.maxv * sizeof(MisE))) != cudaSuccess) return e;        // eye MIS records
+  if ((e = al(21, (size_t)P.n_pixels * sizeof(uint2))) != cudaSuccess) return e;                // connection masks
   const bool full_mis = (opt.flags & RX_VCM_FULL_PATH_MIS) != 0;
   const uint32_t pair_cap = 1u << 27;  // pairs per evaluation window
   uint32_t pair_alloc = 1u << 20;      // grows with demand up to pair_cap
@@ -897,27 +1085,49 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), nph, cap, bufs[8].as<unsigned>(), bufs[5].as<int>());
     Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[5].as<int>()};
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
-    k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
-                                   bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[10].as<float>(), ctr + 1);
-    // merging: count per query, scan, then windows of (query, photon) pairs
     unsigned long long* qc = bufs[14].as<unsigned long long>();
     unsigned long long* qo = bufs[15].as<unsigned long long>();
+    // exclusive scan of n 64-bit counts into qo; returns the total (synchronises)
+    auto scan_total = [&](uint32_t n, unsigned long long& total) -> cudaError_t {
+      const unsigned nb = (n + 1023) / 1024;
+      k_scan_blocks<unsigned long long><<<nb, 1024, 0, s>>>(qc, qo, bufs[16].as<unsigned long long>(), n);
+      k_scan_sums<unsigned long long><<<1, 1024, 0, s>>>(bufs[16].as<unsigned long long>(), nb);
+      k_scan_add<unsigned long long><<<nb, 1024, 0, s>>>(qo, bufs[16].as<unsigned long long>(), n, nullptr);
+      unsigned long long tail[2] = {0, 0};
+      cudaMemcpyAsync(&tail[0], qo + (n - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(&tail[1], qc + (n - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+      cudaError_t err = cudaStreamSynchronize(s);
+      total = tail[0] + tail[1];
+      if (err == cudaSuccess && total > pair_alloc && pair_alloc < pair_cap) {
+        pair_alloc = (uint32_t)std::min<unsigned long long>(pair_cap, std::max<unsigned long long>(total, 2ull * pair_alloc));
+        if ((err = bufs[17].alloc((size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return err;
+        err = bufs[18].alloc((size_t)pair_alloc * sizeof(int));
+      }
+      return err;
+    };
+    unsigned long long total = 0;
+    if (full_mis) {
+      k_vcm_eye_full<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
+                                          bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[10].as<float>(), ctr + 1);
+    } else {
+      k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
+                                     bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[21].as<uint2>(), qc,
+                                     bufs[10].as<float>(), ctr + 1);
+      if ((e = scan_total(P.n_pixels, total)) != cudaSuccess) return e;
+      for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
+        uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
+        k_conn_fill<<<grid * 4, 128, 0, s>>>(P, bufs[21].as<uint2>(), qo, w0, pair_alloc, bufs[17].as<uint32_t>(),
+                                             bufs[18].as<int>());
+        k_conn_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
+                                             bufs[20].as<MisE>(), bufs[17].as<uint32_t>(), bufs[18].as<int>(), np,
+                                             bufs[10].as<float>(), ctr + 1);
+      }
+    }
+    // merging: count per query, scan, then windows of (query, photon) pairs
     k_merge_count<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,
                                            qc, nq);
-    k_scan_blocks<unsigned long long><<<nqblk, 1024, 0, s>>>(qc, qo, bufs[16].as<unsigned long long>(), nq);
-    k_scan_sums<unsigned long long><<<1, 1024, 0, s>>>(bufs[16].as<unsigned long long>(), nqblk);
-    k_scan_add<unsigned long long><<<nqblk, 1024, 0, s>>>(qo, bufs[16].as<unsigned long long>(), nq, nullptr);
-    unsigned long long tail[2] = {0, 0};
-    cudaMemcpyAsync(&tail[0], qo + (nq - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&tail[1], qc + (nq - 1), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    const unsigned long long total = tail[0] + tail[1];
+    if ((e = scan_total(nq, total)) != cudaSuccess) return e;
     merges += total;
-    if (total > pair_alloc && pair_alloc < pair_cap) {
-      pair_alloc = (uint32_t)std::min<unsigned long long>(pair_cap, std::max<unsigned long long>(total, 2ull * pair_alloc));
-      if ((e = bufs[17].alloc((size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
-      if ((e = bufs[18].alloc((size_t)pair_alloc * sizeof(int))) != cudaSuccess) return e;
-    }
     for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
       uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
       k_merge_fill<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,

@@ -86,12 +86,12 @@ def test_vcm_rejects_bad_arguments():
 
 
 @pytest.mark.parametrize("name", ["cornell_vcm", "spheres_vcm", "medium_vcm"])
-def test_factored_merge_mis_matches_full_path_loops(name):
-    """The merge evaluation from per-subpath records (O(1) per pair) against the
-    reference's loops over each whole joined path (RX_VCM_FULL_PATH_MIS) on the same
-    seeded iterations: the subpaths, pairs and connections are the same, so the images
-    differ only by FP32 rounding of the regrouped products and the order of the image
-    atomics."""
+def test_factored_mis_matches_full_path_loops(name):
+    """Connections and merges evaluated from per-subpath records (O(1) per pair, one
+    pair per lane) against the reference's loops over each whole joined path, per pixel
+    in one thread (RX_VCM_FULL_PATH_MIS), on the same seeded iterations: the subpaths and
+    pairs are the same, so the images differ only by FP32 rounding of the regrouped
+    products and the order of the image atomics."""
     z, sc = _load(name)
     with rx.Context(0) as ctx:
         ctx.set_scene(sc)
