@@ -273,7 +273,9 @@ def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
         img, st = ctx.render_vcm(sc.camera, iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=2)
     return {"workload": f"VCMTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, {light_paths} light "
                         "paths/iter, depth 16, r0 0.0963, alpha 0.75", "iterations": iters, "ms": st["ms"],
-            "ms_per_iteration": st["ms"] / iters, "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
+            "ms_per_iteration": st["ms"] / iters, "rays_per_iteration": st["rays"] // iters,
+            "shadow_rays_per_iteration": st["shadow_rays"] // iters, "merges_per_iteration": st["merges"] // iters,
+            "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
 def cpu_baseline(f, o, d, budget_s: float = 12.0):

@@ -152,6 +152,7 @@ typedef struct rx_render_stats {
   uint64_t paths;          /* pixel samples */
   float ms;                /* device time of the render (CUDA events) */
   float reserved;
+  uint64_t merges;         /* VCM: (eye vertex, photon) pairs merged */
 } rx_render_stats;
 
 /* ---- context ------------------------------------------------------------------- */

@@ -240,7 +240,8 @@ class Context:
         film = np.zeros((camera.height, camera.width, 3), np.float64)
         st = rx_render_stats()
         self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
-        return film, dict(rays=st.extension_rays, paths=st.paths, ms=st.ms)
+        return film, dict(rays=st.extension_rays, shadow_rays=st.shadow_rays, merges=st.merges, paths=st.paths,
+                          ms=st.ms)
 
     def set_trace_config(self, variant: int = 3, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))

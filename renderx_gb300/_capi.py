@@ -68,7 +68,7 @@ class rx_vcm_options(ctypes.Structure):
 
 class rx_render_stats(ctypes.Structure):
     _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64), ("paths", ctypes.c_uint64),
-                ("ms", ctypes.c_float), ("reserved", ctypes.c_float)]
+                ("ms", ctypes.c_float), ("reserved", ctypes.c_float), ("merges", ctypes.c_uint64)]
 
 
 class rx_guide_options(ctypes.Structure):

@@ -171,13 +171,16 @@ __device__ __forceinline__ double merge_area(double p, const PV& v, float r, flo
   return p * norm;
 }
 
-// Light-subpath records for c = 0 .. n-1.
-__device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int n, float r, float norm, MisL* out) {
-  double pf = l[0].oprob, pf_prev = 0.0, sl = 0.0;
+// Light-subpath records for c = 0 .. n-1, from the stored vertices of one light path
+// (a window of four vertices, c - 2 .. c + 1, in registers).
+__device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb, int n, float r, float norm,
+                          MisL* out) {
+  PV l2, l1, v = load_pv(lb), nx;  // vertices c - 2, c - 1, c, c + 1
+  double pf = v.oprob, pf_prev = 0.0, sl = 0.0;
   F3 thr = {1, 1, 1};
   float prob = 1.0f;
   for (int c = 0; c < n; c++) {
-    const PV& v = l[c];
+    if (c + 1 < n) nx = load_pv(lb + 4 * (c + 1));
     MisL m;
     m.pf = pf;
     m.pf_prev = pf_prev;
@@ -186,7 +189,7 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int
     m.al = 0.0;
     m.pad = 0.0;
     if (c >= 1) {
-      const PV& a = l[c - 1];
+      const PV& a = l1;
       float d = seg_len(a, v);
       PV rv = rev_to(v, a);
       double al = cos_term(S, cam, a);
@@ -196,7 +199,7 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int
       double tl = rnd(a) && rnd(v) ? pf_prev : 0.0;
       if (rnd(v)) {
         double p = pf_prev;
-        if (rnd(a)) p *= c - 1 > 0 ? dir_pdf(S, cam, l[c - 2], a, false) : dir_pdf(S, cam, a, a, true);
+        if (rnd(a)) p *= c - 1 > 0 ? dir_pdf(S, cam, l2, a, false) : dir_pdf(S, cam, a, a, true);
         p *= origin_pdf(S, a, v);
         p *= cos_term(S, cam, rv);
         p /= (double)d * d;
@@ -209,7 +212,6 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int
     out[c] = m;
     if (c + 1 >= n) break;
     // advance to c + 1
-    const PV& nx = l[c + 1];
     float d = seg_len(v, nx);
     prob *= v.dprob * v.oprob;
     thr = thr * v.c;
@@ -218,16 +220,19 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const PV* l, int
     double pfn = pf * cos_term(S, cam, rev_to(nx, v));
     pfn /= (double)d * d;
     if (rnd(v)) {
-      pfn *= c > 0 ? dir_pdf(S, cam, l[c - 1], v, false) : dir_pdf(S, cam, v, v, true);
+      pfn *= c > 0 ? dir_pdf(S, cam, l1, v, false) : dir_pdf(S, cam, v, v, true);
       pfn *= origin_pdf(S, v, nx);
     }
     if (c >= 1) {
       double g = m.al;
-      if (rnd(v)) g *= dir_pdf(S, cam, rev_to(nx, v), rev_to(v, l[c - 1]), false);
+      if (rnd(v)) g *= dir_pdf(S, cam, rev_to(nx, v), rev_to(v, l1), false);
       sl = sl * g + m.tl;
     }
     pf_prev = pf;
     pf = pfn;
+    l2 = l1;
+    l1 = v;
+    v = nx;
   }
 }
 
@@ -389,8 +394,8 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
 }
 
 // ---- light subpaths + photons ----------------------------------------------------------
-__global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, MisL* lmis, float4* photon_pos,
-                            int* photon_ref, unsigned* n_photons, unsigned photon_cap, unsigned long long* rays) {
+__global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, float4* photon_pos, int* photon_ref,
+                            unsigned* n_photons, unsigned photon_cap, unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nr = 0;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += stride) {
@@ -402,7 +407,6 @@ __global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, MisL
     nr += (unsigned long long)n;
     llen[p] = n;
     for (int i = 0; i < n; i++) store_pv(lv + 4 * ((size_t)p * P.maxv + i), path[i]);
-    light_mis(S, P.cam, path, n, P.radius, P.norm, lmis + (size_t)p * P.maxv);
     for (int i = 1; i < n; i++) {
       if (is_emissive(S, path[i].contact)) break;
       if (!(path[i].flags & kDirRandom)) continue;
@@ -416,12 +420,21 @@ __global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, MisL
   if (nr) atomicAdd(rays, nr);
 }
 
+// The light subpaths' records, one thread per path, from the stored vertices (apart from
+// the sampling kernel, whose traversal stack and divergent bounce loop would hold them).
+__global__ void __launch_bounds__(128) k_light_mis(DevScene S, VcmParams P, const float4* lv, const int* llen,
+                                                   MisL* lmis) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += gridDim.x * blockDim.x)
+    light_mis(S, P.cam, lv + 4 * ((size_t)p * P.maxv), llen[p], P.radius, P.norm, lmis + (size_t)p * P.maxv);
+}
+
 // ---- hash grid ---------------------------------------------------------------------------
 struct Grid {
   float cell;          // 2 * radius
   unsigned mask;       // buckets - 1
   const unsigned* start;  // bucket -> first sorted photon (exclusive scan), buckets + 1 entries
-  const int* sorted;   // sorted photon ids
+  const float4* pos;      // photon positions in bucket order
+  const int* ref;         // photon light vertices (path * maxv + index) in bucket order
 };
 __device__ __forceinline__ unsigned cell_hash(int x, int y, int z, unsigned mask) {
   return ((unsigned)(x * 73856093) ^ (unsigned)(y * 19349663) ^ (unsigned)(z * 83492791)) & mask;
@@ -436,12 +449,13 @@ __global__ void k_grid_count(const float4* pos, const unsigned* n_photons, unsig
     atomicAdd(&count[k], 1u);
   }
 }
-__global__ void k_grid_scatter(const unsigned* key, const unsigned* n_photons, unsigned cap, unsigned* cursor,
-                               int* sorted) {
+__global__ void k_grid_scatter(const unsigned* key, const float4* pos, const int* ref, const unsigned* n_photons,
+                               unsigned cap, unsigned* cursor, float4* pos_out, int* ref_out) {
   unsigned n = min(*n_photons, cap);
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     unsigned slot = atomicAdd(&cursor[key[i]], 1u);
-    sorted[slot] = (int)i;
+    pos_out[slot] = pos[i];
+    ref_out[slot] = ref[i];
   }
 }
 
@@ -761,7 +775,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
                                                  float4* ev, int* elen, MisE* emis, float* img,
                                                  unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
-  unsigned long long nrays = 0;
+  unsigned long long nrays = 0, nshadow = 0;
   const float r = P.radius;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += stride) {
     Rng rng(P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
@@ -795,7 +809,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
           const PV& E = w[ci + 1];
           const PV& L = w[ci];
           float len = length(E.o - L.o);
-          nrays++;
+          nshadow++;
           PHit sh = trace_cond<true>(S, E.o, E.d, len - 1e-5f, E.contact, E.inside);  // testVisibility
           if (sh.tid >= 0) continue;
         }
@@ -825,6 +839,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
     img_add(img, (int)p, acc);
   }
   if (nrays) atomicAdd(rays, nrays);
+  if (nshadow) atomicAdd(rays + 1, nshadow);
 }
 
 // ---- merging as a wavefront: queries, (query, photon) pairs, one pair per lane -------
@@ -833,8 +848,9 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
 // emitter, at vertices sampled at random. The grid walk visits every cell the sphere
 // touches (two per axis in exact arithmetic, up to three after rounding of the cell
 // divisions), each bucket once.
+// Calls range(begin, end) for each distinct bucket of the cells around q.
 template <class F>
-__device__ __forceinline__ void merge_walk(const Grid& G, const float4* photon_pos, F3 q, float r, F&& visit) {
+__device__ __forceinline__ void merge_buckets(const Grid& G, F3 q, float r, F&& range) {
   int x0 = (int)floorf((q.x - r) / G.cell), y0 = (int)floorf((q.y - r) / G.cell), z0 = (int)floorf((q.z - r) / G.cell);
   int x1 = min((int)floorf((q.x + r) / G.cell), x0 + 2), y1 = min((int)floorf((q.y + r) / G.cell), y0 + 2);
   int z1 = min((int)floorf((q.z + r) / G.cell), z0 + 2);
@@ -848,11 +864,15 @@ __device__ __forceinline__ void merge_walk(const Grid& G, const float4* photon_p
         for (int k = 0; k < nseen; k++) dup |= seen[k] == b;
         if (dup || nseen >= 27) continue;
         seen[nseen++] = b;
-        for (unsigned s = G.start[b]; s < G.start[b + 1]; s++) {
-          int ph = G.sorted[s];
-          if (length(q - f3(photon_pos[ph])) < r) visit(ph);
-        }
+        range(G.start[b], G.start[b + 1]);
       }
+}
+template <class F>
+__device__ __forceinline__ void merge_walk(const Grid& G, F3 q, float r, F&& visit) {
+  merge_buckets(G, q, r, [&](unsigned b0, unsigned b1) {
+    for (unsigned i = b0; i < b1; i++)
+      if (length(q - f3(G.pos[i])) < r) visit(G.ref[i]);
+  });
 }
 
 // The merge position of query q, or false if the eye vertex does not merge.
@@ -872,86 +892,144 @@ __device__ __forceinline__ bool merge_query(const DevScene& S, const VcmParams& 
   return true;
 }
 
-__global__ void k_merge_count(DevScene S, VcmParams P, const float4* ev, const int* elen, const float4* photon_pos,
-                              Grid G, unsigned long long* qcount, uint32_t nq) {
+__global__ void k_merge_count(DevScene S, VcmParams P, const float4* ev, const int* elen, Grid G,
+                              unsigned long long* qcount, uint32_t nq) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     F3 pos;
     unsigned long long c = 0;
-    if (merge_query(S, P, ev, elen, q, pos)) merge_walk(G, photon_pos, pos, P.radius, [&](int) { c++; });
+    if (merge_query(S, P, ev, elen, q, pos)) merge_walk(G, pos, P.radius, [&](int) { c++; });
     qcount[q] = c;
   }
 }
 
 // Pairs [win0, win0 + cap) of the scanned order: query and photon of each.
-__global__ void k_merge_fill(DevScene S, VcmParams P, const float4* ev, const int* elen, const float4* photon_pos,
-                             Grid G, const unsigned long long* qoff, uint32_t nq, unsigned long long win0, uint32_t cap,
-                             uint32_t* pair_q, int* pair_ph) {
+__global__ void k_merge_fill(DevScene S, VcmParams P, const float4* ev, const int* elen, Grid G,
+                             const unsigned long long* qoff, uint32_t nq, unsigned long long win0, uint32_t cap,
+                             uint32_t* pair_q, int* pair_ref) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     F3 pos;
     if (!merge_query(S, P, ev, elen, q, pos)) continue;
     unsigned long long idx = qoff[q];
-    merge_walk(G, photon_pos, pos, P.radius, [&](int ph) {
+    merge_walk(G, pos, P.radius, [&](int ref) {
       if (idx >= win0 && idx - win0 < cap) {
         pair_q[idx - win0] = q;
-        pair_ph[idx - win0] = ph;
+        pair_ref[idx - win0] = ref;
       }
       idx++;
     });
   }
 }
 
-// One (query, photon) pair per lane, a run of kRun consecutive pairs per thread so that
-// pairs of one pixel add up in registers before the image atomics. The pair's light
-// vertex ci (the photon's predecessor, w[ci]) and eye vertex E (w[ci+1]) are joined as
-// connectRays does for a merge; colour, probability and MIS weight come from the two
-// subpaths' records and the pdfs through the two new directions.
-constexpr int kRun = 8;
-__global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
-                                                    const MisL* lmis, const MisE* emis, const int* photon_ref,
-                                                    const uint32_t* pair_q, const int* pair_ph, uint32_t npairs,
-                                                    float* img) {
+// The contribution of merging eye vertex E (pe before it, records me) with the photon
+// at light vertex `ref`: the photon's predecessor L = w[ci] is joined with E as
+// connectRays does for a merge, then colour, probability and MIS weight from the
+// records (zero where the reference drops the path).
+__device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, const float4* lv, const MisL* lmis,
+                                         const PV& E, const PV& pe, const MisE& me, int ref) {
+  int lp = ref / (int)P.maxv, ci = ref % (int)P.maxv - 1;
+  const float4* lb = lv + 4 * ((size_t)lp * P.maxv);
+  const PV L = load_pv(lb + 4 * ci);
+  PV Lm, Lp, Ep;
+  if (ci > 0) Lm = load_pv(lb + 4 * (ci - 1));
+  const MisL ml = lmis[(size_t)lp * P.maxv + ci];
+  join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, &pe, true, Lp, Ep);
+  F3 col;
+  float prob, wt;
+  if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, &pe, ml, me, true, P.radius, P.norm, col, prob, wt))
+    return F3{0, 0, 0};
+  return col * (wt / prob) * (1.0f / P.norm);
+}
+
+// Merge pairs (colorByMergingPaths, VCMTracer.cpp:566-636), one warp per pixel of
+// [p0, p1): for each merge vertex of the pixel's eye path (ei >= 1, sampled at random,
+// up to the first emitter) the warp walks the grid cells the sphere touches, 64 sorted
+// photons per step (coalesced positions, the strict |p - x| < r test), and appends the
+// photons inside as (query, light vertex) pairs with one atomic per step. Pairs past
+// `cap` are counted, not written (the host then grows the list or splits the range).
+__global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, const float4* ev, const int* elen,
+                                                    Grid G, uint32_t p0, uint32_t p1, unsigned long long cap,
+                                                    uint32_t* pair_q, int* pair_ref, unsigned long long* npairs) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   const float r = P.radius;
-  uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kRun; base < npairs; base += stride * kRun) {
-    F3 acc = {0, 0, 0};
-    int acc_pixel = -1;
-    for (uint32_t j = base; j < base + kRun && j < npairs; j++) {
-      uint32_t q = pair_q[j];
-      int ref = photon_ref[pair_ph[j]];
-      int p = (int)(q / P.maxv), k = (int)(q % P.maxv);
-      int lp = ref / (int)P.maxv, ci = ref % (int)P.maxv - 1;
-      const float4* lb = lv + 4 * ((size_t)lp * P.maxv);
-      const float4* eb = ev + 4 * ((size_t)p * P.maxv);
-      const PV L = load_pv(lb + 4 * ci);
-      const PV E = load_pv(eb + 4 * k);
-      const PV pe = load_pv(eb + 4 * (k - 1));
-      const MisL ml = lmis[(size_t)lp * P.maxv + ci];
-      const MisE me = emis[(size_t)p * P.maxv + k];
-      PV Lm, Lp, Ep;
-      if (ci > 0) Lm = load_pv(lb + 4 * (ci - 1));
-      join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, &pe, true, Lp, Ep);
-      F3 col;
-      float prob, wt;
-      if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, &pe, ml, me, true, r, P.norm, col, prob, wt))
-        continue;
-      F3 c = col * (wt / prob) * (1.0f / P.norm);
-      if (p != acc_pixel) {
-        if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
-        acc = {0, 0, 0};
-        acc_pixel = p;
-      }
-      acc = acc + c;
+  for (uint32_t p = p0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < p1; p += nw) {
+    const float4* eb = ev + 4 * ((size_t)p * P.maxv);
+    const int ne = elen[p];
+    for (int k = 1; k < ne; k++) {
+      const float4 o4 = eb[4 * k], t4 = eb[4 * k + 3];
+      if (is_emissive(S, __float_as_int(t4.x))) break;  // the reference's merge loop stops at the first emitter
+      if (!(__float_as_uint(t4.w) & kDirRandom)) continue;
+      const F3 x = f3(o4);
+      const uint32_t q = p * P.maxv + (uint32_t)k;
+      merge_buckets(G, x, r, [&](unsigned b0, unsigned b1) {
+        for (unsigned i0 = b0; i0 < b1; i0 += 64) {
+          const unsigned ia = i0 + lane, ib = ia + 32;
+          const bool ha = ia < b1 && length(x - f3(G.pos[ia])) < r;
+          const bool hb = ib < b1 && length(x - f3(G.pos[ib])) < r;
+          const unsigned ma = __ballot_sync(0xffffffffu, ha), mb = __ballot_sync(0xffffffffu, hb);
+          const unsigned n = __popc(ma) + __popc(mb);
+          if (n == 0) continue;
+          unsigned long long base = 0;
+          if (lane == 0) base = atomicAdd(npairs, (unsigned long long)n);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (ha) {
+            unsigned long long slot = base + __popc(ma & lt);
+            if (slot < cap) {
+              pair_q[slot] = q;
+              pair_ref[slot] = G.ref[ia];
+            }
+          }
+          if (hb) {
+            unsigned long long slot = base + __popc(ma) + __popc(mb & lt);
+            if (slot < cap) {
+              pair_q[slot] = q;
+              pair_ref[slot] = G.ref[ib];
+            }
+          }
+        }
+      });
     }
-    if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
   }
 }
 
-// The same pairs evaluated by the reference's loops over the whole joined path
+// One merge pair per lane, kRun consecutive pairs per thread (pairs of one query are
+// appended together, so the eye vertex and its records are loaded once per query and
+// contributions summed per pixel before the image atomics).
+constexpr int kRun = 8;
+__global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
+                                                    const MisL* lmis, const MisE* emis, const uint32_t* pair_q,
+                                                    const int* pair_ref, uint32_t npairs, float* img) {
+  uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kRun; base < npairs; base += stride * kRun) {
+    F3 acc = {0, 0, 0};
+    uint32_t cur = 0xffffffffu;
+    PV E, pe;
+    MisE me;
+    for (uint32_t j = base; j < base + kRun && j < npairs; j++) {
+      const uint32_t q = pair_q[j];
+      if (q != cur) {
+        if (cur != 0xffffffffu) img_add(img, (int)(cur / P.maxv), acc);
+        acc = {0, 0, 0};
+        cur = q;
+        const uint32_t p = q / P.maxv, k = q % P.maxv;
+        const float4* eb = ev + 4 * ((size_t)p * P.maxv);
+        E = load_pv(eb + 4 * k);
+        pe = load_pv(eb + 4 * (k - 1));
+        me = emis[q];
+      }
+      acc = acc + merge_pair(S, P, lv, lmis, E, pe, me, pair_ref[j]);
+    }
+    if (cur != 0xffffffffu) img_add(img, (int)(cur / P.maxv), acc);
+  }
+}
+
+// Merge pairs evaluated by the reference's loops over the whole joined path
 // (connectRays, connectColorProb, connectMergeWeight): O(path length) per pair, with the
 // path in a per-thread array. Kept as the check of k_merge_eval (RX_VCM_FULL_PATH_MIS).
 __global__ void __launch_bounds__(128) k_merge_eval_full(DevScene S, VcmParams P, const float4* lv, const float4* ev,
-                                                    const int* photon_ref, const uint32_t* pair_q,
-                                                    const int* pair_ph, uint32_t npairs, float* img) {
+                                                         const uint32_t* pair_q, const int* pair_ref, uint32_t npairs,
+                                                         float* img) {
   const float r = P.radius;
   uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kRun; base < npairs; base += stride * kRun) {
@@ -959,7 +1037,7 @@ __global__ void __launch_bounds__(128) k_merge_eval_full(DevScene S, VcmParams P
     int acc_pixel = -1;
     for (uint32_t j = base; j < base + kRun && j < npairs; j++) {
       uint32_t q = pair_q[j];
-      int ref = photon_ref[pair_ph[j]];
+      int ref = pair_ref[j];
       int p = (int)(q / P.maxv), ei = (int)(q % P.maxv);
       int lp = ref / (int)P.maxv, li = ref % (int)P.maxv;
       PV w[2 * kMaxV];
@@ -1024,7 +1102,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.n_light * P.maxv;
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(22);
+  std::vector<DevBuf> bufs(23);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
   if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
@@ -1049,7 +1127,10 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = al(19, (size_t)P.n_light * P.maxv * sizeof(MisL))) != cudaSuccess) return e;         // light MIS records
   if ((e = al(20, (size_t)P.n_pixels * P.maxv * sizeof(MisE))) != cudaSuccess) return e;        // eye MIS records
   if ((e = al(21, (size_t)P.n_pixels * sizeof(uint2))) != cudaSuccess) return e;                // connection masks
+  if ((e = al(22, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;                      // sorted photon positions
   const bool full_mis = (opt.flags & RX_VCM_FULL_PATH_MIS) != 0;
+  constexpr uint32_t kMergeCap = 1u << 30;  // merge pairs per evaluation (8 GB of pair list)
+  uint32_t pix_chunk = P.n_pixels;           // pixels per merge walk
   const uint32_t pair_cap = 1u << 27;  // pairs per evaluation window
   uint32_t pair_alloc = 1u << 20;      // grows with demand up to pair_cap
   if ((e = al(17, (size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
@@ -1071,8 +1152,9 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     P.radius = radius;
     P.iter = it;
     cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
-    k_vcm_light<<<grid, 64, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[19].as<MisL>(),
-                                     bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap, ctr);
+    k_vcm_light<<<grid, 64, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
+                                     bufs[3].as<int>(), nph, cap, ctr);
+    k_light_mis<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[19].as<MisL>());
     cudaMemsetAsync(bufs[6].p, 0, bufs[6].bytes, s);
     float cell = 2.0f * radius;
     k_grid_count<<<grid, 256, 0, s>>>(bufs[2].as<float4>(), nph, cap, cell, buckets - 1, bufs[6].as<unsigned>(),
@@ -1082,8 +1164,9 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     k_scan_sums<unsigned><<<1, 1024, 0, s>>>(bufs[9].as<unsigned>(), nblk);
     k_scan_add<unsigned><<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan,
                                                 bufs[8].as<unsigned>());
-    k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), nph, cap, bufs[8].as<unsigned>(), bufs[5].as<int>());
-    Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[5].as<int>()};
+    k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap,
+                                        bufs[8].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>());
+    Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>()};
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
     unsigned long long* qc = bufs[14].as<unsigned long long>();
     unsigned long long* qo = bufs[15].as<unsigned long long>();
@@ -1120,26 +1203,51 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
                                              bufs[18].as<int>());
         k_conn_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
                                              bufs[20].as<MisE>(), bufs[17].as<uint32_t>(), bufs[18].as<int>(), np,
-                                             bufs[10].as<float>(), ctr + 1);
+                                             bufs[10].as<float>(), ctr + 2);
       }
     }
-    // merging: count per query, scan, then windows of (query, photon) pairs
-    k_merge_count<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,
-                                           qc, nq);
-    if ((e = scan_total(nq, total)) != cudaSuccess) return e;
-    merges += total;
-    for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
-      uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
-      k_merge_fill<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), bufs[2].as<float4>(), G,
-                                            qo, nq, w0, pair_alloc, bufs[17].as<uint32_t>(), bufs[18].as<int>());
-      if (full_mis)
-        k_merge_eval_full<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[3].as<int>(),
+    if (full_mis) {  // merging as (query, photon) pair lists: count per query, scan, windows
+      k_merge_count<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), G, qc, nq);
+      if ((e = scan_total(nq, total)) != cudaSuccess) return e;
+      merges += total;
+      for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
+        uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
+        k_merge_fill<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), G, qo, nq, w0, pair_alloc,
+                                              bufs[17].as<uint32_t>(), bufs[18].as<int>());
+        k_merge_eval_full<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(),
                                                    bufs[17].as<uint32_t>(), bufs[18].as<int>(), np,
                                                    bufs[10].as<float>());
-      else
-        k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
-                                              bufs[20].as<MisE>(), bufs[3].as<int>(), bufs[17].as<uint32_t>(),
-                                              bufs[18].as<int>(), np, bufs[10].as<float>());
+      }
+    } else {  // one walk appending pairs, then one pair per lane
+      for (uint32_t p0 = 0; p0 < P.n_pixels;) {
+        const uint32_t p1 = (uint32_t)std::min<uint64_t>(P.n_pixels, (uint64_t)p0 + pix_chunk);
+        unsigned long long* np_dev = ctr + 4;
+        cudaMemsetAsync(np_dev, 0, sizeof(unsigned long long), s);
+        k_merge_walk<<<grid * 2, 256, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), G, p0, p1, pair_alloc,
+                                              bufs[17].as<uint32_t>(), bufs[18].as<int>(), np_dev);
+        unsigned long long np = 0;
+        cudaMemcpyAsync(&np, np_dev, sizeof np, cudaMemcpyDeviceToHost, s);
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        if (np > pair_alloc) {  // grow the pair list, or split the pixel range once it is at its cap
+          if (pair_alloc < kMergeCap) {
+            pair_alloc = (uint32_t)std::min<unsigned long long>(kMergeCap, np + np / 4);
+            if ((e = bufs[17].alloc((size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
+            if ((e = bufs[18].alloc((size_t)pair_alloc * sizeof(int))) != cudaSuccess) return e;
+            continue;
+          }
+          if (p1 - p0 > 1) {
+            pix_chunk = (p1 - p0) / 2;
+            continue;
+          }
+          np = pair_alloc;  // one pixel beyond the cap: its first kMergeCap pairs
+        }
+        merges += np;
+        if (np)
+          k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
+                                                bufs[20].as<MisE>(), bufs[17].as<uint32_t>(), bufs[18].as<int>(),
+                                                (uint32_t)np, bufs[10].as<float>());
+        p0 = p1;
+      }
     }
     k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
   }
@@ -1151,10 +1259,11 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (stats) {
-    unsigned long long h[2];
+    unsigned long long h[4];
     cudaMemcpy(h, ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0] + h[1];
-    stats->shadow_rays = 0;
+    stats->shadow_rays = h[2];
+    stats->merges = merges;
     stats->paths = (uint64_t)P.n_pixels * opt.iterations;
     stats->ms = ms;
   }
