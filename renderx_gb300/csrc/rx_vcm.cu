@@ -135,21 +135,21 @@ __device__ __forceinline__ PV load_pv(const float4* p) {
 //  - what is left (connection and merge at ci-1 and ci, connection at ci+1, and the
 //    pdfs through the two changed directions) is evaluated per pair.
 // The throughput of connectColorProb splits the same way (MisL::thr, MisE::thr).
-struct alignas(16) MisL {  // per light vertex c, for a merge at ci = c
-  double pf;       // pf[c]
-  double pf_prev;  // pf[c-1]
-  double sl;       // (C_i + M_i, i <= c-2) / pb[c-1]
-  double tl;       // (C_{c-1} + M_{c-1}) / pb[c]
-  double al;       // pb[c-1] / pb[c] without the direction pdf at c
-  double pad;
-  F3 thr;          // prod_{i<c} colour x transmittance x cosine
+// The sums are kept relative to the product pf[ci] pb[ci+1] that every technique's term
+// shares, so the per-pair arithmetic is FP32 (the recursions that build the records run
+// in FP64, as the reference's weights do).
+struct alignas(16) MisL {  // per light vertex c, for a join at ci = c
+  float sla;       // pb[c-1] / pb[c] x (C_i + M_i, i <= c-2) / pb[c-1] / pf[c], without the direction pdf at c
+  float tla;       // (C_{c-1} + M_{c-1}) / (pb[c] pf[c])
   float prob;      // prod_{i<c} directionProb x originProb
+  float pad;
+  F3 thr;          // prod_{i<c} colour x transmittance x cosine
+  float pad2;
 };
-struct alignas(16) MisE {  // per eye vertex k, for a merge with E = eye vertex k
+struct alignas(16) MisE {  // per eye vertex k, for a join with E = eye vertex k
   double pb;       // pb at eye vertex k (pb[ci+1])
-  double pb_prev;  // pb at eye vertex k-1 (pb[ci+2])
-  double se;       // (M_{ci+1} + C_i + M_i, i >= ci+2) / pf[ci+2]
-  double fe;       // pf[ci+2] / pf[ci+1] without the direction pdf at E
+  float pbr;       // pb at eye vertex k-1 / pb at eye vertex k
+  float sea;       // pf[ci+2] / pf[ci+1] x (M_{ci+1} + C_i + M_i, i >= ci+2) / pf[ci+2] / pb[ci+1], without the direction pdf at E
   F3 thr;          // prod_{m<k} colour x transmittance x cosine of the eye vertices
   float prob;      // prod_{m<k} directionProb x originProb
 };
@@ -182,21 +182,15 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb
   for (int c = 0; c < n; c++) {
     if (c + 1 < n) nx = load_pv(lb + 4 * (c + 1));
     MisL m;
-    m.pf = pf;
-    m.pf_prev = pf_prev;
-    m.sl = sl;
-    m.tl = 0.0;
-    m.al = 0.0;
-    m.pad = 0.0;
+    double al = 0.0, tl = 0.0;
     if (c >= 1) {
       const PV& a = l1;
       float d = seg_len(a, v);
       PV rv = rev_to(v, a);
-      double al = cos_term(S, cam, a);
+      al = cos_term(S, cam, a);
       al /= (double)d * d;
       if (rnd(v)) al *= origin_pdf(S, rv, a);
-      m.al = al;
-      double tl = rnd(a) && rnd(v) ? pf_prev : 0.0;
+      tl = rnd(a) && rnd(v) ? pf_prev : 0.0;
       if (rnd(v)) {
         double p = pf_prev;
         if (rnd(a)) p *= c - 1 > 0 ? dir_pdf(S, cam, l2, a, false) : dir_pdf(S, cam, a, a, true);
@@ -205,10 +199,13 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb
         p /= (double)d * d;
         tl += merge_area(p, v, r, norm);
       }
-      m.tl = tl;
     }
-    m.thr = thr;
+    m.sla = (float)(al * sl / pf);
+    m.tla = (float)(tl / pf);
     m.prob = prob;
+    m.pad = 0.0f;
+    m.thr = thr;
+    m.pad2 = 0.0f;
     out[c] = m;
     if (c + 1 >= n) break;
     // advance to c + 1
@@ -224,9 +221,9 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb
       pfn *= origin_pdf(S, v, nx);
     }
     if (c >= 1) {
-      double g = m.al;
+      double g = al;
       if (rnd(v)) g *= dir_pdf(S, cam, rev_to(nx, v), rev_to(v, l1), false);
-      sl = sl * g + m.tl;
+      sl = sl * g + tl;
     }
     pf_prev = pf;
     pf = pfn;
@@ -245,17 +242,16 @@ __device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n
     const PV& v = e[k];
     MisE m;
     m.pb = pb;
-    m.pb_prev = pb_prev;
-    m.se = 0.0;
-    m.fe = 0.0;
+    m.pbr = (float)(pb_prev / pb);
+    m.sea = 0.0f;
     if (k >= 1) {
       const PV& pe = e[k - 1];
       float d = seg_len(v, pe);
       double fe = cos_term(S, cam, pe);
       fe /= (double)d * d;
       fe *= origin_pdf(S, rev_to(v, pe), pe);
-      m.fe = fe;
-      m.se = u + (k >= 2 && rnd(pe) ? merge_area(pb_prev, pe, r, norm) : 0.0);
+      double se = u + (k >= 2 && rnd(pe) ? merge_area(pb_prev, pe, r, norm) : 0.0);
+      m.sea = (float)(fe * se / pb);
     }
     m.thr = thr;
     m.prob = prob;
@@ -355,41 +351,26 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
   if (!(prob > 0.0f) || !(length(col) > 0.0f)) return false;
   float dpf = 1.0f;
   if (rl) dpf = Lm ? dir_pdf(S, cam, *Lm, Lp, false) : dir_pdf(S, cam, Lp, Lp, true);
-  const double dd = (double)D * D;
-  const double C = rl ? ml.pf * me.pb : 0.0;  // connection at ci
-  double M = 0.0;                              // merge at ci (needs an eye vertex after E)
+  // every term over pf[ci] pb[ci+1]
+  const float g = 1.0f / (D * D);
+  const float C = rl ? 1.0f : 0.0f;  // connection at ci
+  float M = 0.0f;                     // merge at ci (needs an eye vertex after E)
   if (pe) {
-    M = ml.pf * me.pb;
-    if (rl) M *= dpf;
-    M *= opf;
-    M *= cosE;
-    M /= dd;
-    M = merge_area(M, Ep, r, norm);
+    M = (rl ? dpf : 1.0f) * opf * cosE * g * (RX_PI * r * r) * norm;
+    if (Ep.inside != kNone && Ep.contact == kNone) M *= 4.0f / 3.0f * r;
   }
-  double sum = C + M;
-  double pb0 = me.pb * cosL;  // pb[ci]
-  pb0 /= dd;
+  float sum = C + M;
+  float pb0 = cosL * g * origin_pdf(S, Ep, L);  // pb[ci] / pb[ci+1]
   pb0 *= pe ? dir_pdf(S, cam, *pe, Ep, false) : dir_pdf(S, cam, Ep, Ep, true);
-  pb0 *= origin_pdf(S, Ep, L);
-  if (Lm) {
-    double pbm = pb0 * ml.al;  // pb[ci-1]
-    if (rl) pbm *= dir_pdf(S, cam, Ep, rev_to(Lp, *Lm), false);
-    sum += pbm * ml.sl + pb0 * ml.tl;
-  }
+  if (Lm) sum += pb0 * ((rl ? dir_pdf(S, cam, Ep, rev_to(Lp, *Lm), false) : 1.0f) * ml.sla + ml.tla);
   if (pe) {
-    double pf1 = ml.pf * cosE;  // pf[ci+1]
-    pf1 /= dd;
-    if (rl) {
-      pf1 *= dpf;
-      pf1 *= opf;
-    }
-    if (rnd(*pe)) sum += pf1 * me.pb_prev;  // connection at ci+1
-    double pf2 = pf1 * me.fe * dir_pdf(S, cam, Lp, rE, false);
-    sum += pf2 * me.se;
+    const float pf1 = cosE * g * (rl ? dpf * opf : 1.0f);  // pf[ci+1] / pf[ci]
+    if (rnd(*pe)) sum += pf1 * me.pbr;                      // connection at ci+1
+    sum += pf1 * dir_pdf(S, cam, Lp, rE, false) * me.sea;
   }
-  if (!pe && !Lm) sum += pb0;  // two-vertex path: mustUsePT adds pb[0]
-  double res = (merged ? M : C) / sum;
-  wt = res >= 0.0 ? (float)res : 0.0f;
+  if (!pe && !Lm) sum += pb0 / L.oprob;  // two-vertex path: mustUsePT adds pb[0] (pf[0] = originProb of L)
+  const float res = (merged ? M : C) / sum;
+  wt = res >= 0.0f ? res : 0.0f;
   return true;
 }
 
@@ -657,10 +638,11 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
       F3 col = v.c * m.thr;
       float prob = (v.dprob * v.oprob) * m.prob;
       if (!(prob > 0.0f) || !(length(col) > 0.0f)) continue;
-      double sum = m.pb;
-      if (t == 2 && rnd(v) && rnd(eye[0])) sum += (double)v.oprob * me[0].pb;
-      double res = m.pb / sum;
-      float wt = res >= 0.0 ? (float)res : 0.0f;
+      float wt = m.pb > 0.0 && m.pb < INFINITY ? 1.0f : 0.0f;  // pb[0] / pb[0]
+      if (wt > 0.0f && t == 2 && rnd(v) && rnd(eye[0])) {      // pb[0] / (pb[0] + pf[0] pb[1])
+        float res = 1.0f / (1.0f + v.oprob * m.pbr);
+        wt = res >= 0.0f ? res : 0.0f;
+      }
       F3 c = col * (wt / prob);
       if (length(c) > 0.0f) acc = acc + c;
     }
@@ -942,7 +924,7 @@ __device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, 
 
 // Merge pairs (colorByMergingPaths, VCMTracer.cpp:566-636), one warp per pixel of
 // [p0, p1): for each merge vertex of the pixel's eye path (ei >= 1, sampled at random,
-// up to the first emitter) the warp walks the grid cells the sphere touches, 64 sorted
+// up to the first emitter) the warp walks the grid cells the sphere touches, 128 sorted
 // photons per step (coalesced positions, the strict |p - x| < r test), and appends the
 // photons inside as (query, light vertex) pairs with one atomic per step. Pairs past
 // `cap` are counted, not written (the host then grows the list or splits the range).
@@ -962,33 +944,58 @@ __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, con
       if (!(__float_as_uint(t4.w) & kDirRandom)) continue;
       const F3 x = f3(o4);
       const uint32_t q = p * P.maxv + (uint32_t)k;
-      merge_buckets(G, x, r, [&](unsigned b0, unsigned b1) {
-        for (unsigned i0 = b0; i0 < b1; i0 += 64) {
-          const unsigned ia = i0 + lane, ib = ia + 32;
-          const bool ha = ia < b1 && length(x - f3(G.pos[ia])) < r;
-          const bool hb = ib < b1 && length(x - f3(G.pos[ib])) < r;
-          const unsigned ma = __ballot_sync(0xffffffffu, ha), mb = __ballot_sync(0xffffffffu, hb);
-          const unsigned n = __popc(ma) + __popc(mb);
+      // the cells the sphere touches (as merge_buckets), one per lane; equal buckets are
+      // walked once, by the lowest lane that holds them
+      const int x0 = (int)floorf((x.x - r) / G.cell), y0 = (int)floorf((x.y - r) / G.cell);
+      const int z0 = (int)floorf((x.z - r) / G.cell);
+      const int nx = min((int)floorf((x.x + r) / G.cell), x0 + 2) - x0 + 1;
+      const int ny = min((int)floorf((x.y + r) / G.cell), y0 + 2) - y0 + 1;
+      const int nz = min((int)floorf((x.z + r) / G.cell), z0 + 2) - z0 + 1;
+      const bool cell_lane = lane < nx * ny * nz;
+      unsigned bucket = 0xffffffffu, b0 = 0, b1 = 0;
+      if (cell_lane) {
+        const int cz = lane % nz, cy = (lane / nz) % ny, cx = lane / (nz * ny);
+        bucket = cell_hash(x0 + cx, y0 + cy, z0 + cz, G.mask);
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, bucket);
+      const bool leader = cell_lane && (unsigned)(__ffs(peers) - 1) == (unsigned)lane;
+      if (leader) {
+        b0 = G.start[bucket];
+        b1 = G.start[bucket + 1];
+      }
+      for (unsigned lead = __ballot_sync(0xffffffffu, leader && b1 > b0); lead; lead &= lead - 1) {
+        const int src = __ffs(lead) - 1;
+        const unsigned r0 = __shfl_sync(0xffffffffu, b0, src), r1 = __shfl_sync(0xffffffffu, b1, src);
+        for (unsigned i0 = r0; i0 < r1; i0 += 128) {
+          bool h[4];
+          unsigned m[4], n = 0;
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const unsigned i = i0 + 32 * u + lane;
+            h[u] = i < r1 && length(x - f3(G.pos[i])) < r;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            m[u] = __ballot_sync(0xffffffffu, h[u]);
+            n += __popc(m[u]);
+          }
           if (n == 0) continue;
           unsigned long long base = 0;
           if (lane == 0) base = atomicAdd(npairs, (unsigned long long)n);
           base = __shfl_sync(0xffffffffu, base, 0);
-          if (ha) {
-            unsigned long long slot = base + __popc(ma & lt);
-            if (slot < cap) {
-              pair_q[slot] = q;
-              pair_ref[slot] = G.ref[ia];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            if (h[u]) {
+              const unsigned long long slot = base + __popc(m[u] & lt);
+              if (slot < cap) {
+                pair_q[slot] = q;
+                pair_ref[slot] = G.ref[i0 + 32 * u + lane];
+              }
             }
-          }
-          if (hb) {
-            unsigned long long slot = base + __popc(ma) + __popc(mb & lt);
-            if (slot < cap) {
-              pair_q[slot] = q;
-              pair_ref[slot] = G.ref[ib];
-            }
+            base += __popc(m[u]);
           }
         }
-      });
+      }
     }
   }
 }
