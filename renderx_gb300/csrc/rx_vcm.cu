@@ -65,29 +65,31 @@ __device__ PV camera_ray(const DevScene& S, const CamDev& c, uint32_t pixel, Rng
 
 // MCRenderer::samplePath / samplePathIter (src/MCRenderer.cpp:151-273): the path's rays
 // in order, ending with the ray that stopped it or a terminating ray.
+// `put(i, ray)` receives the rays in order; returns their count.
+template <class Put>
 __device__ int sample_path(const DevScene& S, const CamDev& cam, PV start, Hit3 h, uint32_t max_depth, Rng& rng,
-                           PV* out) {
+                           Put&& put) {
   int n = 0;
   PV prev = start;
   for (uint32_t depth = 0;; depth++) {
-    out[n++] = prev;
+    put(n++, prev);
     if (prev.inside == kNone && h.obj == kNone) {
-      out[n++] = pv_term(prev.o);
+      put(n++, pv_term(prev.o));
       return n;
     }
     PV next = scatter_step(S, cam, prev, h, true, true, rng);
     if (length(next.d) < 0.5f) {
-      out[n++] = next;
+      put(n++, next);
       return n;
     }
     if (depth + 1 > max_depth) {
-      out[n++] = pv_term(prev.o);
+      put(n++, pv_term(prev.o));
       return n;
     }
     PHit hh = trace_cond<false>(S, next.o, next.d, INFINITY, next.contact, next.inside);
     if (hh.tid < 0) {
-      out[n++] = next;
-      out[n++] = pv_term(prev.o);
+      put(n++, next);
+      put(n++, pv_term(prev.o));
       return n;
     }
     h = Hit3{(int)__ldg(&S.tri_obj[hh.tid]), hh.tid, hh.t};
@@ -375,28 +377,33 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
 }
 
 // ---- light subpaths + photons ----------------------------------------------------------
-__global__ void k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen, float4* photon_pos, int* photon_ref,
-                            unsigned* n_photons, unsigned photon_cap, unsigned long long* rays) {
+__global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen,
+                                                   float4* photon_pos, int* photon_ref, unsigned* n_photons,
+                                                   unsigned photon_cap, unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nr = 0;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += stride) {
     Rng rng(P.seed, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
-    PV path[kMaxV];
     Hit3 h;
     PV start = emit_ray(S, P.cam, rng, h);
-    int n = sample_path(S, P.cam, start, h, P.max_depth, rng, path);
-    nr += (unsigned long long)n;
-    llen[p] = n;
-    for (int i = 0; i < n; i++) store_pv(lv + 4 * ((size_t)p * P.maxv + i), path[i]);
-    for (int i = 1; i < n; i++) {
-      if (is_emissive(S, path[i].contact)) break;
-      if (!(path[i].flags & kDirRandom)) continue;
+    float4* out = lv + 4 * ((size_t)p * P.maxv);
+    bool emitter_seen = false;  // photons stop at the first emitter after the origin
+    int n = sample_path(S, P.cam, start, h, P.max_depth, rng, [&](int i, const PV& v) {
+      store_pv(out + 4 * i, v);
+      if (i == 0 || emitter_seen) return;
+      if (is_emissive(S, v.contact)) {
+        emitter_seen = true;
+        return;
+      }
+      if (!(v.flags & kDirRandom)) return;
       unsigned slot = atomicAdd(n_photons, 1u);
       if (slot < photon_cap) {
-        photon_pos[slot] = make_float4(path[i].o.x, path[i].o.y, path[i].o.z, 0.0f);
+        photon_pos[slot] = make_float4(v.o.x, v.o.y, v.o.z, 0.0f);
         photon_ref[slot] = (int)(p * P.maxv + i);
       }
-    }
+    });
+    nr += (unsigned long long)n;
+    llen[p] = n;
   }
   if (nr) atomicAdd(rays, nr);
 }
@@ -616,7 +623,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
     PV eye[kMaxV];
     Hit3 h;
     PV start = camera_ray(S, P.cam, p, rng, h);
-    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, eye);
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, [&](int i, const PV& v) { eye[i] = v; });
     nrays += (unsigned long long)ne;
     for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
@@ -765,7 +772,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
     PV w[2 * kMaxV];
     Hit3 h;
     PV start = camera_ray(S, P.cam, p, rng, h);
-    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, eye);
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, [&](int i, const PV& v) { eye[i] = v; });
     nrays += (unsigned long long)ne;
     for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
@@ -1159,7 +1166,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     P.radius = radius;
     P.iter = it;
     cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
-    k_vcm_light<<<grid, 64, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
+    k_vcm_light<<<grid * 4, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
                                      bufs[3].as<int>(), nph, cap, ctr);
     k_light_mis<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[19].as<MisL>());
     cudaMemsetAsync(bufs[6].p, 0, bufs[6].bytes, s);
@@ -1200,7 +1207,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
       k_vcm_eye_full<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
                                           bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[10].as<float>(), ctr + 1);
     } else {
-      k_vcm_eye<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
+      k_vcm_eye<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
                                      bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[21].as<uint2>(), qc,
                                      bufs[10].as<float>(), ctr + 1);
       if ((e = scan_total(P.n_pixels, total)) != cudaSuccess) return e;
