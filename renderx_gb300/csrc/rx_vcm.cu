@@ -121,25 +121,23 @@ __device__ __forceinline__ PV load_pv(const float4* p) {
   return v;
 }
 
-// ---- the MIS weight of a merge in O(1) ---------------------------------------------------
+// ---- the MIS weight of a join in O(1) ---------------------------------------------------
 // connectMergeWeight sums, over every technique that could have made the joined path
 // w[0..n-1] (light vertices 0..ci, eye vertices after), products pf[i] pb[i+1] of
-// forward and backward pdf chains. For a merge at light vertex ci with eye vertex E
-// (w[ci+1]), connectRays changes only the directions at ci and ci+1 (and E's colour,
-// direction pdf, sampling flag and inside object), and VCMTracer::link reverses a
-// vertex only by its neighbours' positions, so:
+// forward and backward pdf chains (C_i: connection at i, M_i: merge at i). For a join
+// (connection or merge) of light vertex ci with eye vertex E = w[ci+1], connectRays
+// changes only the two vertices' directions, colours, direction pdfs, sampling flags and
+// inside objects, and VCMTracer::link reverses a vertex by its neighbours' positions
+// only, so:
 //  - pf[0..ci] and the ratios pb[i] / pb[ci-1] (i <= ci-1) depend on the light subpath
 //    alone, pb[ci+1..n-1] and the ratios pf[i] / pf[ci+2] (i >= ci+2) on the eye
 //    subpath alone;
-//  - the techniques at i <= ci-2 add up to pb[ci-1] * MisL::sl and those at
-//    i >= ci+1 (but the connection at ci+1) to pf[ci+2] * MisE::se, both built once
-//    per subpath by a recursion over its vertices;
-//  - what is left (connection and merge at ci-1 and ci, connection at ci+1, and the
-//    pdfs through the two changed directions) is evaluated per pair.
-// The throughput of connectColorProb splits the same way (MisL::thr, MisE::thr).
-// The sums are kept relative to the product pf[ci] pb[ci+1] that every technique's term
-// shares, so the per-pair arithmetic is FP32 (the recursions that build the records run
-// in FP64, as the reference's weights do).
+//  - the techniques at i <= ci-2 add up to pb[ci-1] x (a light-only sum) and those at
+//    i >= ci+2, with the merge at ci+1, to pf[ci+2] x (an eye-only sum), both built once
+//    per subpath by a recursion over its vertices (light_mis, eye_mis);
+//  - what is left (C and M at ci-1 and ci, C at ci+1, and the pdfs through the two
+//    changed directions) is evaluated per pair (join_eval).
+// The throughput and probability of connectColorProb split the same way.
 struct alignas(16) MisL {  // per light vertex c, for a join at ci = c
   float sla;       // pb[c-1] / pb[c] x (C_i + M_i, i <= c-2) / pb[c-1] / pf[c], without the direction pdf at c
   float tla;       // (C_{c-1} + M_{c-1}) / (pb[c] pf[c])
