@@ -263,20 +263,24 @@ __device__ float mix_loss_grad(const float (&raw)[48], const float (&wi)[3], flo
   return -scale * lq;
 }
 
-// Mixture for sampling / evaluation: per lobe weight, kappa, mean, weight x normaliser.
+// Mixture for sampling / evaluation: per lobe weight, kappa, mean, weight x normaliser
+// (kLobes x kLobeFloats floats, written as 16-byte stores; `out` 16-byte aligned).
 __device__ void mix_store(const float (&raw)[48], float* out) {
   Lobe L[kLobes];
   decode(raw, L);
+  float o[kLobes * kLobeFloats];
 #pragma unroll
   for (int j = 0; j < kLobes; j++) {
-    float* o = out + j * kLobeFloats;
-    o[0] = expf(L[j].logpi);
-    o[1] = L[j].kappa;
-    o[2] = L[j].mu[0];
-    o[3] = L[j].mu[1];
-    o[4] = L[j].mu[2];
-    o[5] = expf(L[j].logpi + L[j].lognorm);
+    o[j * kLobeFloats + 0] = expf(L[j].logpi);
+    o[j * kLobeFloats + 1] = L[j].kappa;
+    o[j * kLobeFloats + 2] = L[j].mu[0];
+    o[j * kLobeFloats + 3] = L[j].mu[1];
+    o[j * kLobeFloats + 4] = L[j].mu[2];
+    o[j * kLobeFloats + 5] = expf(L[j].logpi + L[j].lognorm);
   }
+  float4* o4 = reinterpret_cast<float4*>(out);
+#pragma unroll
+  for (int k = 0; k < kLobes * kLobeFloats / 4; k++) o4[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
 }
 
 __device__ float mix_pdf_raw(const float (&raw)[48], const float (&wi)[3]) {
@@ -312,11 +316,13 @@ __device__ __forceinline__ void tc_sync() {
 }
 
 // Shared-memory plan of the network kernels (bytes from the dynamic base).
-constexpr uint32_t kSmW = 0;                         // weight image
-constexpr uint32_t kSmA0 = kImgBytes;                // 128 x 80 input tile
-constexpr uint32_t kSmA1 = kSmA0 + 128 * kIn * 2;    // hidden activations, 128 x 64 each
-constexpr uint32_t kActBytes = 128 * kHid * 2;
-constexpr uint32_t kSmInfer = kSmA1 + 2 * kActBytes;                 // inference: 2 ping-pong buffers
+constexpr uint32_t kSmW = 0;                         // weight image, then the per-tile buffers
+constexpr uint32_t kActBytes = 128 * kHid * 2;       // one 128 x 64 BF16 activation tile
+constexpr int kInferTiles = 4;  // inference tiles in flight per CTA, one warpgroup each
+// per tile: the 128 x 80 input (its first 16 KB also hold the odd layers' outputs) and one
+// 128 x 64 activation buffer
+constexpr uint32_t kInferTileBytes = 128 * kIn * 2 + kActBytes;
+constexpr uint32_t kSmInfer = kImgBytes + kInferTiles * kInferTileBytes;
 
 // Loads the weight image into shared memory with bulk copies (one per layer).
 __device__ __forceinline__ void load_weights(unsigned char* sm, const unsigned char* img, uint64_t* bar) {
@@ -329,21 +335,39 @@ __device__ __forceinline__ void load_weights(unsigned char* sm, const unsigned c
 }
 
 // ---- inference -------------------------------------------------------------------------
+// Each IO splits its input into prefetch (the first, independent loads, issued one tile
+// ahead) and finish (the rest), and stores a query's result with 16-byte stores.
+
 // Queries from records (x, n, wo, wi, ...): raw outputs and the mixture pdf at wi.
 struct RecordIO {
   const float* recs;
   float* raw_out;  // n x 40 (optional)
   float* pdf_out;  // n (optional)
-  __device__ bool load(uint32_t i, float (&q)[9], float (&wi)[3]) const {
-    const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
-    float4 a = r[0], b = r[1], c = r[2];
-    q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x; q[5] = b.y; q[6] = b.z; q[7] = b.w; q[8] = c.x;
-    wi[0] = c.y; wi[1] = c.z; wi[2] = c.w;
-    return true;
+  struct Pre {
+    float4 a, b, c;
+  };
+  __device__ Pre prefetch(uint32_t i, uint32_t n) const {
+    Pre p{};
+    if (i < n) {
+      const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
+      p.a = r[0];
+      p.b = r[1];
+      p.c = r[2];
+    }
+    return p;
+  }
+  __device__ bool finish(const Pre& p, uint32_t i, uint32_t n, float (&q)[9], float (&wi)[3]) const {
+    q[0] = p.a.x; q[1] = p.a.y; q[2] = p.a.z; q[3] = p.a.w; q[4] = p.b.x; q[5] = p.b.y; q[6] = p.b.z; q[7] = p.b.w;
+    q[8] = p.c.x;
+    wi[0] = p.c.y; wi[1] = p.c.z; wi[2] = p.c.w;
+    return i < n;
   }
   __device__ void store(uint32_t i, const float (&raw)[48], const float (&wi)[3]) const {
-    if (raw_out)
-      for (int k = 0; k < kOutUsed; k++) raw_out[(size_t)i * kOutUsed + k] = raw[k];
+    if (raw_out) {
+      float4* o = reinterpret_cast<float4*>(raw_out + (size_t)i * kOutUsed);
+#pragma unroll
+      for (int k = 0; k < kOutUsed / 4; k++) o[k] = make_float4(raw[4 * k], raw[4 * k + 1], raw[4 * k + 2], raw[4 * k + 3]);
+    }
     if (pdf_out) pdf_out[i] = mix_pdf_raw(raw, wi);
   }
 };
@@ -355,12 +379,27 @@ struct PathIO {
   PathSoA P;
   const int2* hit;
   float* lobes;
-  __device__ bool load(uint32_t i, float (&q)[9], float (&wi)[3]) const {
+  struct Pre {
+    int2 h;
+    int4 inf;
+    float4 o, d;
+  };
+  __device__ Pre prefetch(uint32_t i, uint32_t n) const {
+    Pre p;
+    p.h = make_int2(-1, 0);
+    if (i < n) {
+      p.h = hit[i];
+      p.inf = P.info[i];
+      p.o = P.o[i];
+      p.d = P.d[i];
+    }
+    return p;
+  }
+  __device__ bool finish(const Pre& p, uint32_t i, uint32_t n, float (&q)[9], float (&wi)[3]) const {
     wi[0] = wi[1] = wi[2] = 0.0f;
-    int2 h = hit[i];
-    int4 inf = P.info[i];
-    bool ok = h.x >= 0 && inf.z < 0;
-    int obj = ok ? (int)__ldg(&S.tri_obj[h.x]) : -1;
+    if (i >= n) return false;
+    bool ok = p.h.x >= 0 && p.inf.z < 0;
+    int obj = ok ? (int)__ldg(&S.tri_obj[p.h.x]) : -1;
     if (ok) {
       uint32_t m = S.objects[obj].material;
       ok = m == kDiffuse || m == kGlossy || m == kPhong;
@@ -369,16 +408,16 @@ struct PathIO {
       lobes[(size_t)i * kLobeStride] = -1.0f;  // not guided
       return false;
     }
-    float4 o = P.o[i], d = P.d[i];
-    float t = __int_as_float(h.y);
-    F3 x = F3{o.x, o.y, o.z} + F3{d.x, d.y, d.z} * t;
-    TriGeom g = tri_geom(S, h.x);
-    F3 n = world_normal(g, S.objects[obj].has_normals, x);
-    if (n.x * d.x + n.y * d.y + n.z * d.z > 0.0f) {
+    float t = __int_as_float(p.h.y);
+    F3 x = F3{p.o.x, p.o.y, p.o.z} + F3{p.d.x, p.d.y, p.d.z} * t;
+    TriGeom g = tri_geom(S, p.h.x);
+    F3 nn = world_normal(g, S.objects[obj].has_normals, x);
+    if (nn.x * p.d.x + nn.y * p.d.y + nn.z * p.d.z > 0.0f) {
       lobes[(size_t)i * kLobeStride] = -1.0f;
       return false;
     }
-    q[0] = x.x; q[1] = x.y; q[2] = x.z; q[3] = n.x; q[4] = n.y; q[5] = n.z; q[6] = -d.x; q[7] = -d.y; q[8] = -d.z;
+    q[0] = x.x; q[1] = x.y; q[2] = x.z; q[3] = nn.x; q[4] = nn.y; q[5] = nn.z;
+    q[6] = -p.d.x; q[7] = -p.d.y; q[8] = -p.d.z;
     return true;
   }
   __device__ void store(uint32_t i, const float (&raw)[48], const float (&)[3]) const {
@@ -386,58 +425,90 @@ struct PathIO {
   }
 };
 
-// Persistent inference: 128-sample tiles, five layers each (MMA, then the epilogue).
+// Barrier of warpgroup g (its 128 threads, named barrier g + 1) that also orders
+// tensor-core work and generic shared-memory writes; and its AND-reduction.
+__device__ __forceinline__ void wg_sync(int g) {
+  tc::fence_async_smem();
+  tc::tc_fence_before();
+  asm volatile("bar.sync %0, 128;" ::"r"(g + 1) : "memory");
+  tc::tc_fence_after();
+}
+__device__ __forceinline__ bool wg_and(int g, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(g + 1)
+      : "memory");
+  return r != 0;
+}
+
+// Persistent inference: kInferTiles warpgroups per CTA share the weight image and each
+// runs its own 128-sample tiles through the five layers (its own input / activation
+// buffers, TMEM columns 64 g .. 64 g + 63, mbarrier, and MMA-issuing thread), so several
+// tiles' MMA -> epilogue chains interleave on the SM. The next tile's inputs are loaded
+// while the current one runs.
 template <class IO>
-__global__ void __launch_bounds__(128) k_guide_infer(IO io, const unsigned* count, uint32_t n_host,
-                                                     const unsigned char* img, Box box, int* status) {
+__global__ void __launch_bounds__(128 * kInferTiles, 1)
+    k_guide_infer(IO io, const unsigned* count, uint32_t n_host, const unsigned char* img, Box box, int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) uint64_t bar_mma, bar_w;
+  __shared__ __align__(8) uint64_t bar_mma[kInferTiles], bar_w;
   __shared__ uint32_t tmem_base;
-  const int s = threadIdx.x, warp = s >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, s = tid & 127;
   const uint32_t n = count ? *count : n_host;
   const uint32_t ntiles = (n + kTile - 1) / kTile;
-  if (blockIdx.x >= ntiles) return;
-  if (s == 0) {
-    tc::mbar_init(&bar_mma, 1);
+  if (blockIdx.x * kInferTiles >= ntiles) return;
+  if (tid == 0) {
+    for (int k = 0; k < kInferTiles; k++) tc::mbar_init(&bar_mma[k], 1);
     tc::mbar_init(&bar_w, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
-  if (s == 0) load_weights(sm, img, &bar_w);
-  if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+  if (tid == 0) load_weights(sm, img, &bar_w);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 64 * kInferTiles);
   tc_sync();
-  const uint32_t tacc = tmem_base + ((uint32_t)(warp * 32) << 16);
+  const uint32_t tcol = tmem_base + 64u * (uint32_t)g;
+  const uint32_t tacc = tcol + ((uint32_t)((warp & 3) * 32) << 16);
   bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0));
   uint32_t ph = 0;
-  unsigned char* A0 = sm + kSmA0;
-  unsigned char* Ab[2] = {sm + kSmA1, sm + kSmA1 + kActBytes};
-  for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    uint32_t i = tile * kTile + s;
+  unsigned char* A0 = sm + kImgBytes + (uint32_t)g * kInferTileBytes;
+  unsigned char* A1 = A0 + 128 * kIn * 2;
+  const uint32_t tstride = gridDim.x * kInferTiles;
+  uint32_t tile = blockIdx.x * kInferTiles + (uint32_t)g;
+  typename IO::Pre pre = io.prefetch(tile * kTile + s, tile < ntiles ? n : 0u);
+  for (; ok && tile < ntiles; tile += tstride) {
+    const uint32_t i = tile * kTile + s;
     float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0};
-    bool valid = i < n && io.load(i, q, wi);
+    const bool valid = io.finish(pre, i, n, q, wi);
+    const uint32_t next = tile + tstride;
+    pre = io.prefetch(next * kTile + s, next < ntiles ? n : 0u);
     encode_row(q, valid, box, A0, s);
-    tc_sync();
+    wg_sync(g);
     float raw[48];
     for (int l = 0; l < 5; l++) {
-      const unsigned char* A = l == 0 ? A0 : Ab[(l - 1) & 1];
+      // layer l reads A0 (l = 0, 2, 4) or A1 (l = 1, 3) and writes the other
+      const unsigned char* A = (l & 1) ? A1 : A0;
       if (s == 0) {
-        issue_fwd(tmem_base, A, sm + kSmW + layer_img(l), layer_k(l));
-        tc::mma_commit(&bar_mma);
+        issue_fwd(tcol, A, sm + kSmW + layer_img(l), layer_k(l));
+        tc::mma_commit(&bar_mma[g]);
       }
-      ok = __syncthreads_and(tc::mbar_wait(&bar_mma, ph));
+      ok = wg_and(g, tc::mbar_wait(&bar_mma[g], ph));
       ph ^= 1;
       tc::tc_fence_after();
       if (!ok) break;
-      if (l < 4) epi_relu(tacc, Ab[l & 1], s);
+      if (l < 4) epi_relu(tacc, (l & 1) ? A0 : A1, s);
       else load_raw(tacc, raw);
-      tc_sync();
+      wg_sync(g);
     }
     if (ok && valid) io.store(i, raw, wi);
   }
   if (!ok && s == 0) atomicExch(status, 1);
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem_base, 64);
+  if (warp == 0) tc::tmem_dealloc(tmem_base, 64 * kInferTiles);
 }
 
 // ---- training --------------------------------------------------------------------------
@@ -783,8 +854,8 @@ cudaError_t guide_infer_paths(GuideState* g, const DevScene& S, const PathSoA& P
                               const int2* hit, float* lobes, int grid, cudaStream_t s) {
   set_kernel_smem();
   PathIO io{S, P, hit, lobes};
-  k_guide_infer<PathIO><<<grid, 128, kSmInfer, s>>>(io, count, 0, g->img.as<unsigned char>(), g->box,
-                                                     g->status.as<int>());
+  k_guide_infer<PathIO><<<grid, 128 * kInferTiles, kSmInfer, s>>>(io, count, 0, g->img.as<unsigned char>(), g->box,
+                                                                   g->status.as<int>());
   return cudaGetLastError();
 }
 
@@ -950,9 +1021,9 @@ extern "C" rx_status rx_guide_eval(rx_context* c, const float* recs, uint32_t n,
   rx::set_kernel_smem();
   rx::RecordIO io{dr.as<float>(), draw.as<float>(), dp.as<float>()};
   uint32_t tiles = (n + rx::guide::kTile - 1) / rx::guide::kTile;
-  uint32_t grid = std::min<uint32_t>(tiles, 2u * (uint32_t)g->sms);
-  rx::k_guide_infer<rx::RecordIO><<<grid, 128, rx::kSmInfer, c->stream>>>(io, nullptr, n, g->img.as<unsigned char>(),
-                                                                           g->box, g->status.as<int>());
+  uint32_t grid = std::min<uint32_t>((tiles + rx::kInferTiles - 1) / rx::kInferTiles, (uint32_t)g->sms);
+  rx::k_guide_infer<rx::RecordIO><<<grid, 128 * rx::kInferTiles, rx::kSmInfer, c->stream>>>(
+      io, nullptr, n, g->img.as<unsigned char>(), g->box, g->status.as<int>());
   if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide eval")) != RX_OK) return s;
   if ((s = guide_status(c)) != RX_OK) return s;
   if (raw40) cudaMemcpy(raw40, draw.p, (size_t)n * rx::guide::kOutUsed * 4, cudaMemcpyDeviceToHost);
@@ -972,10 +1043,10 @@ extern "C" rx_status rx_guide_eval_device(rx_context* c, const float* d_recs, ui
   rx::set_kernel_smem();
   rx::RecordIO io{d_recs, d_raw40, d_pdf};
   uint32_t tiles = (n + rx::guide::kTile - 1) / rx::guide::kTile;
-  uint32_t grid = std::min<uint32_t>(tiles, 2u * (uint32_t)g->sms);
+  uint32_t grid = std::min<uint32_t>((tiles + rx::kInferTiles - 1) / rx::kInferTiles, (uint32_t)g->sms);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  rx::k_guide_infer<rx::RecordIO><<<grid, 128, rx::kSmInfer, st>>>(io, nullptr, n, g->img.as<unsigned char>(), g->box,
-                                                                    g->status.as<int>());
+  rx::k_guide_infer<rx::RecordIO><<<grid, 128 * rx::kInferTiles, rx::kSmInfer, st>>>(
+      io, nullptr, n, g->img.as<unsigned char>(), g->box, g->status.as<int>());
   return c->cuda(cudaGetLastError(), "guide eval");
 }
 

@@ -694,7 +694,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
           k_extend<32><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
         else
           k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
-        if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, 2 * sms, s)) != cudaSuccess)
+        if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, sms, s)) != cudaSuccess)
           return e;
         k_zero<<<1, 1, 0, s>>>(cn);
         if (best.stack == kWalk4)
