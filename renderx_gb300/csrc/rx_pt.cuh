@@ -234,6 +234,42 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
 // distance so that popped subtrees beyond the current best are skipped. The stack holds
 // at most 3 entries per level: callers use it only when 3 * bvh4_depth + 1 <= 64.
 constexpr int kWalk4 = 4;  // walk selector: the 4-wide BVH
+// The cnt triangles of the 4-wide tree's leaf at slot `first` (Moller-Trumbore, the
+// NoSelfIntersectionCondition when cond): lowers best to the nearest legal hit; with ANY,
+// returns true at the first one.
+template <bool ANY>
+__device__ __forceinline__ bool leaf_test(const DevScene& S, int first, int cnt, F3 o, F3 d, bool cond, int contact,
+                                          int inside, PHit& best) {
+  const DevAccel& A = S.accel;
+  for (int k = 0; k < cnt; k++) {
+    const float4* tp = A.tris + 3 * (size_t)(first + k);
+    float4 w0 = __ldg(tp), w1 = __ldg(tp + 1), w2 = __ldg(tp + 2);
+    F3 v0 = f3(w0), e1 = f3(w1) - v0, e2 = f3(w2) - v0;
+    F3 pv = cross(d, e2);
+    float det = dot(e1, pv);
+    if (fabsf(det) < 1e-30f) continue;
+    float idet = 1.0f / det;
+    F3 sv = o - v0;
+    float u = dot(sv, pv) * idet;
+    if (u < -1e-7f || u > 1.0000001f) continue;
+    F3 qv = cross(sv, e1);
+    float v = dot(d, qv) * idet;
+    if (v < -1e-7f || u + v > 1.0000001f) continue;
+    float t = dot(e2, qv) * idet;
+    if (!(t >= 0.0f) || !(t < best.t)) continue;
+    if (cond) {
+      const float4* nn = S.slot_n + 3 * (size_t)(first + k);
+      float4 q0 = __ldg(nn), q1 = __ldg(nn + 1), q2 = __ldg(nn + 2);
+      int obj = __float_as_int(q0.w);
+      F3 n = normalize(f3(q0) * (1.0f - u - v) + f3(q1) * u + f3(q2) * v);
+      if (!legal_hit(contact, inside, obj, dot(d, n))) continue;
+    }
+    best = {__float_as_int(w0.w), t};
+    if (ANY) return true;
+  }
+  return false;
+}
+
 template <bool ANY>
 __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
   const DevAccel& A = S.accel;
@@ -300,34 +336,8 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
         cnt = c[0];
         continue;
       }
-    } else {
-      int first = ~cur;
-      for (int k = 0; k < cnt; k++) {
-        const float4* tp = A.tris + 3 * (size_t)(first + k);
-        float4 w0 = __ldg(tp), w1 = __ldg(tp + 1), w2 = __ldg(tp + 2);
-        F3 v0 = f3(w0), e1 = f3(w1) - v0, e2 = f3(w2) - v0;
-        F3 pv = cross(d, e2);
-        float det = dot(e1, pv);
-        if (fabsf(det) < 1e-30f) continue;
-        float idet = 1.0f / det;
-        F3 sv = o - v0;
-        float u = dot(sv, pv) * idet;
-        if (u < -1e-7f || u > 1.0000001f) continue;
-        F3 qv = cross(sv, e1);
-        float v = dot(d, qv) * idet;
-        if (v < -1e-7f || u + v > 1.0000001f) continue;
-        float t = dot(e2, qv) * idet;
-        if (!(t >= 0.0f) || !(t < best.t)) continue;
-        if (cond) {
-          const float4* nn = S.slot_n + 3 * (size_t)(first + k);
-          float4 q0 = __ldg(nn), q1 = __ldg(nn + 1), q2 = __ldg(nn + 2);
-          int obj = __float_as_int(q0.w);
-          F3 n = normalize(f3(q0) * (1.0f - u - v) + f3(q1) * u + f3(q2) * v);
-          if (!legal_hit(contact, inside, obj, dot(d, n))) continue;
-        }
-        best = {__float_as_int(w0.w), t};
-        if (ANY) return best;
-      }
+    } else if (leaf_test<ANY>(S, ~cur, cnt, o, d, cond, contact, inside, best)) {
+      return best;
     }
     bool found = false;
     while (sp > 0) {
