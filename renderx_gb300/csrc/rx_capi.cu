@@ -534,12 +534,12 @@ rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, 
                  "trace_reforder launch");
 }
 
-// Host buffers. Up to kWholeBatch rays go to the device in one copy and are traced as
-// one batch (binning and the persistent walk work best on whole batches; the copies run
-// at the host link's full rate); larger inputs go in chunks of kWholeBatch that
-// alternate between two copy/compute streams, so one chunk's copies overlap the other
-// chunk's kernels.
-static constexpr size_t kWholeBatch = (size_t)1 << 24;
+// Host buffers. The rays go to the device in chunks of up to kWholeBatch that alternate
+// between two copy/compute streams, so one chunk's copies overlap the other chunk's
+// kernels (2^23 rays per chunk: large enough for binning and the persistent walk; for a
+// 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for one whole-batch
+// copy, trace and copy back).
+static constexpr size_t kWholeBatch = (size_t)1 << 23;
 rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist) {
   if (!c) return RX_ERR_INVALID;
   if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
