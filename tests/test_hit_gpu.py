@@ -104,7 +104,8 @@ def test_invalid_inputs_raise():
 def test_full_size_batch_matches_oracle_sample_and_reference_walk():
     """4,096,036 triangles, 2^24 rays: the whole batch through the fast path; a sample
     against the CPU oracle, a 2^18 slice against the reference-order walk on the GPU,
-    and the whole batch twice for determinism."""
+    the whole batch twice for determinism, and once more from host buffers (two chunks
+    over two streams)."""
     torch = pytest.importorskip("torch")
     sc = scenes.sphere_field(200, 5, seed=1)
     f = sc.flatten()
@@ -134,9 +135,11 @@ def test_full_size_batch_matches_oracle_sample_and_reference_walk():
         torch.cuda.synchronize()
         assert torch.equal(tr, tid[:m])
         assert torch.equal(dr.view(torch.int32), dist[:m].view(torch.int32))
+        ht, hd = ctx.trace_closest(o, d)
         assert ctx.counters()["errors"] == 0
     tid = tid.cpu().numpy()
     dist = dist.cpu().numpy()
+    assert np.array_equal(ht, tid) and _bits_equal(hd, dist)
     rng = np.random.default_rng(0)
     sample = np.sort(rng.choice(n, 1024, replace=False))
     T = oracle.RefTree(f["verts"], f["tris"])
