@@ -421,7 +421,12 @@ struct Grid {
   const unsigned* start;  // bucket -> first sorted photon (exclusive scan), buckets + 1 entries
   const float4* pos;      // photon positions in bucket order
   const int* ref;         // photon light vertices (path * maxv + index) in bucket order
+  const float4* join;     // per photon in bucket order, kJoin float4: the light side of a merge
 };
+// The light side of a merge with a photon at light vertex ci + 1, gathered once per
+// photon into bucket order: vertex ci (L, 4 float4), vertex ci - 1 (Lm, 4 float4, zero
+// when ci = 0) and L's record (2 float4; MisL::pad carries ci).
+constexpr int kJoin = 10;
 __device__ __forceinline__ unsigned cell_hash(int x, int y, int z, unsigned mask) {
   return ((unsigned)(x * 73856093) ^ (unsigned)(y * 19349663) ^ (unsigned)(z * 83492791)) & mask;
 }
@@ -436,12 +441,30 @@ __global__ void k_grid_count(const float4* pos, const unsigned* n_photons, unsig
   }
 }
 __global__ void k_grid_scatter(const unsigned* key, const float4* pos, const int* ref, const unsigned* n_photons,
-                               unsigned cap, unsigned* cursor, float4* pos_out, int* ref_out) {
+                               unsigned cap, unsigned* cursor, float4* pos_out, int* ref_out, const float4* lv,
+                               const MisL* lmis, uint32_t maxv, float4* join) {
   unsigned n = min(*n_photons, cap);
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     unsigned slot = atomicAdd(&cursor[key[i]], 1u);
+    const int r = ref[i];
     pos_out[slot] = pos[i];
-    ref_out[slot] = ref[i];
+    ref_out[slot] = r;
+    const uint32_t lp = (uint32_t)r / maxv, ci = (uint32_t)r % maxv - 1;
+    const float4* L = lv + 4 * ((size_t)lp * maxv + ci);
+    float4* out = join + (size_t)kJoin * slot;
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = L[k];
+    if (ci > 0) {
+      const float4* Lm = L - 4;
+#pragma unroll
+      for (int k = 0; k < 4; k++) out[4 + k] = Lm[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) out[4 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    MisL m = lmis[(size_t)lp * maxv + ci];
+    out[8] = make_float4(m.sla, m.tla, m.prob, __int_as_float((int)ci));
+    out[9] = make_float4(m.thr.x, m.thr.y, m.thr.z, 0.0f);
   }
 }
 
@@ -908,17 +931,21 @@ __global__ void k_merge_fill(DevScene S, VcmParams P, const float4* ev, const in
 }
 
 // The contribution of merging eye vertex E (pe before it, records me) with the photon
-// at light vertex `ref`: the photon's predecessor L = w[ci] is joined with E as
-// connectRays does for a merge, then colour, probability and MIS weight from the
-// records (zero where the reference drops the path).
-__device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, const float4* lv, const MisL* lmis,
-                                         const PV& E, const PV& pe, const MisE& me, int ref) {
-  int lp = ref / (int)P.maxv, ci = ref % (int)P.maxv - 1;
-  const float4* lb = lv + 4 * ((size_t)lp * P.maxv);
-  const PV L = load_pv(lb + 4 * ci);
+// whose light side is `jd` (kJoin float4): the photon's predecessor L = w[ci] is joined
+// with E as connectRays does for a merge, then colour, probability and MIS weight from
+// the records (zero where the reference drops the path).
+__device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, const float4* jd, const PV& E,
+                                         const PV& pe, const MisE& me) {
+  const PV L = load_pv(jd);
+  const float4 m0 = jd[8], m1 = jd[9];
+  const int ci = __float_as_int(m0.w);
+  MisL ml;
+  ml.sla = m0.x;
+  ml.tla = m0.y;
+  ml.prob = m0.z;
+  ml.thr = f3(m1);
   PV Lm, Lp, Ep;
-  if (ci > 0) Lm = load_pv(lb + 4 * (ci - 1));
-  const MisL ml = lmis[(size_t)lp * P.maxv + ci];
+  if (ci > 0) Lm = load_pv(jd + 4);
   join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, &pe, true, Lp, Ep);
   F3 col;
   float prob, wt;
@@ -931,7 +958,7 @@ __device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, 
 // [p0, p1): for each merge vertex of the pixel's eye path (ei >= 1, sampled at random,
 // up to the first emitter) the warp walks the grid cells the sphere touches, 128 sorted
 // photons per step (coalesced positions, the strict |p - x| < r test), and appends the
-// photons inside as (query, light vertex) pairs with one atomic per step. Pairs past
+// photons inside as (query, photon slot in bucket order) pairs with one atomic per step. Pairs past
 // `cap` are counted, not written (the host then grows the list or splits the range).
 __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, const float4* ev, const int* elen,
                                                     Grid G, uint32_t p0, uint32_t p1, unsigned long long cap,
@@ -994,7 +1021,7 @@ __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, con
               const unsigned long long slot = base + __popc(m[u] & lt);
               if (slot < cap) {
                 pair_q[slot] = q;
-                pair_ref[slot] = G.ref[i0 + 32 * u + lane];
+                pair_ref[slot] = (int)(i0 + 32 * u + lane);
               }
             }
             base += __popc(m[u]);
@@ -1009,9 +1036,9 @@ __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, con
 // appended together, so the eye vertex and its records are loaded once per query and
 // contributions summed per pixel before the image atomics).
 constexpr int kRun = 8;
-__global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
-                                                    const MisL* lmis, const MisE* emis, const uint32_t* pair_q,
-                                                    const int* pair_ref, uint32_t npairs, float* img) {
+__global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, const float4* ev, const MisE* emis,
+                                                    const float4* join, const uint32_t* pair_q, const int* pair_slot,
+                                                    uint32_t npairs, float* img) {
   uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kRun; base < npairs; base += stride * kRun) {
     F3 acc = {0, 0, 0};
@@ -1030,7 +1057,7 @@ __global__ void __launch_bounds__(128) k_merge_eval(DevScene S, VcmParams P, con
         pe = load_pv(eb + 4 * (k - 1));
         me = emis[q];
       }
-      acc = acc + merge_pair(S, P, lv, lmis, E, pe, me, pair_ref[j]);
+      acc = acc + merge_pair(S, P, join + (size_t)kJoin * pair_slot[j], E, pe, me);
     }
     if (cur != 0xffffffffu) img_add(img, (int)(cur / P.maxv), acc);
   }
@@ -1114,7 +1141,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.n_light * P.maxv;
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(23);
+  std::vector<DevBuf> bufs(24);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
   if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
@@ -1140,6 +1167,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = al(20, (size_t)P.n_pixels * P.maxv * sizeof(MisE))) != cudaSuccess) return e;        // eye MIS records
   if ((e = al(21, (size_t)P.n_pixels * sizeof(uint2))) != cudaSuccess) return e;                // connection masks
   if ((e = al(22, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;                      // sorted photon positions
+  if ((e = al(23, (size_t)cap * kJoin * sizeof(float4))) != cudaSuccess) return e;              // photon join data
   const bool full_mis = (opt.flags & RX_VCM_FULL_PATH_MIS) != 0;
   constexpr uint32_t kMergeCap = 1u << 30;  // merge pairs per evaluation (8 GB of pair list)
   uint32_t pix_chunk = P.n_pixels;           // pixels per merge walk
@@ -1177,8 +1205,9 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     k_scan_add<unsigned><<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan,
                                                 bufs[8].as<unsigned>());
     k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap,
-                                        bufs[8].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>());
-    Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>()};
+                                        bufs[8].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(),
+                                        bufs[0].as<float4>(), bufs[19].as<MisL>(), P.maxv, bufs[23].as<float4>());
+    Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(), bufs[23].as<float4>()};
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
     unsigned long long* qc = bufs[14].as<unsigned long long>();
     unsigned long long* qo = bufs[15].as<unsigned long long>();
@@ -1255,9 +1284,9 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
         }
         merges += np;
         if (np)
-          k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
-                                                bufs[20].as<MisE>(), bufs[17].as<uint32_t>(), bufs[18].as<int>(),
-                                                (uint32_t)np, bufs[10].as<float>());
+          k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[20].as<MisE>(), bufs[23].as<float4>(),
+                                                bufs[17].as<uint32_t>(), bufs[18].as<int>(), (uint32_t)np,
+                                                bufs[10].as<float>());
         p0 = p1;
       }
     }
