@@ -146,6 +146,16 @@ typedef struct rx_vcm_options {
  * pair) instead of the per-subpath records (O(1) per pair). Same estimator; slower. */
 #define RX_VCM_FULL_PATH_MIS 1u
 
+/* BidirectionalPathTracer options (reference include/BidirectionalPathTracer.h): per
+ * iteration one eye and one light subpath per pixel, all their connections. */
+typedef struct rx_bpt_options {
+  uint32_t iterations;     /* samples per pixel (BidirectionalPathTracer::spp) */
+  uint32_t max_depth;      /* MCRenderer::maxDepth, at most 21 */
+  uint32_t flags;          /* RX_VCM_FULL_PATH_MIS or 0 */
+  uint32_t reserved;       /* 0 */
+  uint64_t seed;
+} rx_bpt_options;
+
 typedef struct rx_render_stats {
   uint64_t extension_rays; /* closest-hit rays traced (camera + bounce) */
   uint64_t shadow_rays;    /* next-event-estimation visibility rays */
@@ -275,6 +285,13 @@ rx_status rx_render_pt_batch(rx_context* ctx, const rx_batch_item* items, uint32
  * iteration images (width*height*3 doubles, rows from the top). Light-path and
  * merge normalisation use light_paths (width*height in the reference). */
 rx_status rx_render_vcm(rx_context* ctx, const rx_camera* cam, const rx_vcm_options* opts, double* film_rgb,
+                        rx_render_stats* stats);
+/* Replaces BidirectionalPathTracer::renderPixels (reference
+ * src/BidirectionalPathTracer.cpp:6-112): the running mean of `iterations` images, each
+ * from one eye and one light subpath per pixel joined by every (s, t) connection,
+ * weighted by connectWeight (balance heuristic, no merging), with light-tracing splats
+ * and the vignetting correction. Output as rx_render_vcm. */
+rx_status rx_render_bpt(rx_context* ctx, const rx_camera* cam, const rx_bpt_options* opts, double* film_rgb,
                         rx_render_stats* stats);
 
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per

@@ -17,7 +17,8 @@ import ctypes
 import numpy as np
 
 from . import _capi
-from ._capi import RxError, rx_build_options, rx_camera, rx_object, rx_pt_options, rx_render_stats, rx_vcm_options
+from ._capi import (RxError, rx_bpt_options, rx_build_options, rx_camera, rx_object, rx_pt_options, rx_render_stats,
+                    rx_vcm_options)
 from . import scenes
 
 __all__ = ["Context", "KDTree", "RxError", "reftree_serialize", "scenes", "rays_to_array"]
@@ -242,6 +243,18 @@ class Context:
         self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
         return film, dict(rays=st.extension_rays, shadow_rays=st.shadow_rays, merges=st.merges, paths=st.paths,
                           ms=st.ms)
+
+    def render_bpt(self, camera: "scenes.Camera", iterations: int, max_depth: int = 8, seed: int = 1,
+                   full_path_mis: bool = False):
+        """BidirectionalPathTracer renderPixels for ``iterations`` samples per pixel:
+        returns (mean (H,W,3) float64, stats). ``full_path_mis`` evaluates connections with
+        the reference's whole-path loops (RX_VCM_FULL_PATH_MIS)."""
+        cam = camera_struct(camera)
+        o = rx_bpt_options(iterations, max_depth, 1 if full_path_mis else 0, 0, seed)
+        film = np.zeros((camera.height, camera.width, 3), np.float64)
+        st = rx_render_stats()
+        self._ck(self._L.rx_render_bpt(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
+        return film, dict(rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms)
 
     def set_trace_config(self, variant: int = 3, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))

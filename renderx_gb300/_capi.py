@@ -66,6 +66,11 @@ class rx_vcm_options(ctypes.Structure):
                 ("seed", ctypes.c_uint64)]
 
 
+class rx_bpt_options(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
 class rx_render_stats(ctypes.Structure):
     _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64), ("paths", ctypes.c_uint64),
                 ("ms", ctypes.c_float), ("reserved", ctypes.c_float), ("merges", ctypes.c_uint64)]
@@ -120,6 +125,7 @@ SIGNATURES = [
     ("rx_trace_read_timing", S, [P, P, P]),
     ("rx_render_pt", S, [P, P, P, P, P, P]),
     ("rx_render_vcm", S, [P, P, P, P, P]),
+    ("rx_render_bpt", S, [P, P, P, P, P]),
     ("rx_render_pt_batch", S, [P, P, U32, P, P]),
 ]
 

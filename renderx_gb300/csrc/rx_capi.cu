@@ -422,8 +422,8 @@ rx_status rx_render_pt_batch(rx_context* c, const rx_batch_item* items, uint32_t
   return RX_OK;
 }
 
-rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_options* opts, double* film_rgb,
-                        rx_render_stats* stats) {
+static rx_status render_bidirectional(rx_context* c, const rx_camera* cam, const rx_vcm_options* opts,
+                                      double* film_rgb, rx_render_stats* stats) {
   if (!c) return RX_ERR_INVALID;
   if (!cam || !opts || !film_rgb) return c->fail(RX_ERR_INVALID, "null argument");
   if (!c->scene_ready) return c->fail(RX_ERR_STATE, "scene objects not built (rx_scene_set_objects, rx_build_accel)");
@@ -432,7 +432,6 @@ rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_option
   if (opts->max_depth > 21) return c->fail(RX_ERR_INVALID, "max_depth must be at most 21");
   if (!(opts->radius > 0.0f) || !(opts->alpha > 0.0f)) return c->fail(RX_ERR_INVALID, "radius and alpha must be positive");
   if (c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "vertex connection and merging needs an emitter");
-  if (opts->flags & ~RX_VCM_FULL_PATH_MIS) return c->fail(RX_ERR_INVALID, "unknown VCM flags");
   DeviceGuard g(c->device);
   size_t np = (size_t)cam->width * cam->height;
   DevBuf film;
@@ -446,6 +445,22 @@ rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_option
   for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->iterations;
   if (stats) *stats = st;
   return RX_OK;
+}
+
+rx_status rx_render_vcm(rx_context* c, const rx_camera* cam, const rx_vcm_options* opts, double* film_rgb,
+                        rx_render_stats* stats) {
+  if (!c) return RX_ERR_INVALID;
+  if (opts && (opts->flags & ~RX_VCM_FULL_PATH_MIS)) return c->fail(RX_ERR_INVALID, "unknown VCM flags");
+  return render_bidirectional(c, cam, opts, film_rgb, stats);
+}
+
+rx_status rx_render_bpt(rx_context* c, const rx_camera* cam, const rx_bpt_options* opts, double* film_rgb,
+                        rx_render_stats* stats) {
+  if (!c) return RX_ERR_INVALID;
+  if (!opts) return c->fail(RX_ERR_INVALID, "null argument");
+  if ((opts->flags & ~RX_VCM_FULL_PATH_MIS) || opts->reserved) return c->fail(RX_ERR_INVALID, "unknown BPT flags");
+  rx_vcm_options v{opts->iterations, opts->max_depth, 0u, opts->flags | rx::kVcmBidirectional, 1.0f, 1.0f, opts->seed};
+  return render_bidirectional(c, cam, &v, film_rgb, stats);
 }
 
 rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {

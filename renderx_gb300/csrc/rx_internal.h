@@ -177,6 +177,9 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
 cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& opt, double* film_sum,
                       double* film_sq, rx_render_stats* stats, cudaStream_t s);
 // Vertex connection and merging (rx_vcm.cu): adds iteration images to `film` (sum).
+// With kVcmBidirectional in opt.flags, the BidirectionalPathTracer instead (no merging,
+// one light path per pixel; radius and alpha unused).
+constexpr uint32_t kVcmBidirectional = 1u << 31;
 cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
                        rx_render_stats* stats, cudaStream_t s);
 }  // namespace rx

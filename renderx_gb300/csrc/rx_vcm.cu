@@ -16,6 +16,11 @@
 //     (:321-428, double precision) and light-tracing splats through
 //     Camera::transToPixel.
 //  4. Vignetting correction of the iteration image and the running mean (FP64 film).
+//
+// The same pipeline without photons and merging is the reference's
+// BidirectionalPathTracer (src/BidirectionalPathTracer.cpp:6-398): eye subpaths sampled
+// as eye paths, the connection weight without merge techniques, and its own rule for
+// the pure path-tracing technique (VcmParams::bpt).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -39,6 +44,7 @@ struct VcmParams {
   uint32_t n_pixels;
   float radius;
   float norm;          // light-path count normaliser (W*H in the reference)
+  uint32_t bpt;        // 1: BidirectionalPathTracer (no merging), 0: VCMTracer
 };
 
 // ---- camera ----------------------------------------------------------------------------
@@ -64,11 +70,12 @@ __device__ PV camera_ray(const DevScene& S, const CamDev& c, uint32_t pixel, Rng
 }
 
 // MCRenderer::samplePath / samplePathIter (src/MCRenderer.cpp:151-273): the path's rays
-// in order, ending with the ray that stopped it or a terminating ray.
+// in order, ending with the ray that stopped it or a terminating ray. `light`: the
+// isLightPath argument (light-path scattering).
 // `put(i, ray)` receives the rays in order; returns their count.
 template <class Put>
-__device__ int sample_path(const DevScene& S, const CamDev& cam, PV start, Hit3 h, uint32_t max_depth, Rng& rng,
-                           Put&& put) {
+__device__ int sample_path(const DevScene& S, const CamDev& cam, PV start, Hit3 h, uint32_t max_depth, bool light,
+                           Rng& rng, Put&& put) {
   int n = 0;
   PV prev = start;
   for (uint32_t depth = 0;; depth++) {
@@ -77,7 +84,7 @@ __device__ int sample_path(const DevScene& S, const CamDev& cam, PV start, Hit3 
       put(n++, pv_term(prev.o));
       return n;
     }
-    PV next = scatter_step(S, cam, prev, h, true, true, rng);
+    PV next = scatter_step(S, cam, prev, h, light, true, rng);
     if (length(next.d) < 0.5f) {
       put(n++, next);
       return n;
@@ -174,7 +181,7 @@ __device__ __forceinline__ double merge_area(double p, const PV& v, float r, flo
 // Light-subpath records for c = 0 .. n-1, from the stored vertices of one light path
 // (a window of four vertices, c - 2 .. c + 1, in registers).
 __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb, int n, float r, float norm,
-                          MisL* out) {
+                          bool merges, MisL* out) {
   PV l2, l1, v = load_pv(lb), nx;  // vertices c - 2, c - 1, c, c + 1
   double pf = v.oprob, pf_prev = 0.0, sl = 0.0;
   F3 thr = {1, 1, 1};
@@ -191,7 +198,7 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb
       al /= (double)d * d;
       if (rnd(v)) al *= origin_pdf(S, rv, a);
       tl = rnd(a) && rnd(v) ? pf_prev : 0.0;
-      if (rnd(v)) {
+      if (merges && rnd(v)) {
         double p = pf_prev;
         if (rnd(a)) p *= c - 1 > 0 ? dir_pdf(S, cam, l2, a, false) : dir_pdf(S, cam, a, a, true);
         p *= origin_pdf(S, a, v);
@@ -234,7 +241,8 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb
 }
 
 // Eye-subpath records for k = 0 .. n-1 (k >= 1 are merge vertices).
-__device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n, float r, float norm, MisE* out) {
+__device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n, float r, float norm, bool merges,
+                        MisE* out) {
   double pb = e[0].oprob, pb_prev = 0.0, u = 0.0;
   F3 thr = {1, 1, 1};
   float prob = 1.0f;
@@ -250,7 +258,7 @@ __device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n
       double fe = cos_term(S, cam, pe);
       fe /= (double)d * d;
       fe *= origin_pdf(S, rev_to(v, pe), pe);
-      double se = u + (k >= 2 && rnd(pe) ? merge_area(pb_prev, pe, r, norm) : 0.0);
+      double se = u + (merges && k >= 2 && rnd(pe) ? merge_area(pb_prev, pe, r, norm) : 0.0);
       m.sea = (float)(fe * se / pb);
     }
     m.thr = thr;
@@ -283,7 +291,7 @@ __device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n
       }
       double un = u * g;
       if (rnd(v) && rnd(pe)) un += pb_prev;
-      if (k >= 2 && rnd(pe)) un += merge_area(g * pb_prev * (rnd(v) ? 1.0 : opf), pe, r, norm);
+      if (merges && k >= 2 && rnd(pe)) un += merge_area(g * pb_prev * (rnd(v) ? 1.0 : opf), pe, r, norm);
       u = un;
     }
     pb_prev = pb;
@@ -328,8 +336,8 @@ __device__ __forceinline__ void join(const DevScene& S, const CamDev& cam, const
 // joined path from the two subpaths' records. Returns false where the reference drops
 // the path (zero colour or probability); col / prob / wt as the reference's.
 __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, const PV* Lm, const PV& Lp, const PV& Ep,
-                          const PV* pe, const MisL& ml, const MisE& me, bool merged, float r, float norm, F3& col,
-                          float& prob, float& wt) {
+                          const PV* pe, const MisL& ml, const MisE& me, bool merged, bool bpt, float r, float norm,
+                          F3& col, float& prob, float& wt) {
   const float D = fmaxf(length(Ep.o - Lp.o), 1e-5f);
   const float cosL = cos_term(S, cam, Lp), cosE = cos_term(S, cam, Ep);
   const PV rE = pe ? rev_to(Ep, *pe) : Ep;  // link(ci+1, ci+2); for t = 1 only its origin is read
@@ -354,8 +362,8 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
   // every term over pf[ci] pb[ci+1]
   const float g = 1.0f / (D * D);
   const float C = rl ? 1.0f : 0.0f;  // connection at ci
-  float M = 0.0f;                     // merge at ci (needs an eye vertex after E)
-  if (pe) {
+  float M = 0.0f;                     // merge at ci (needs an eye vertex after E; none without merging)
+  if (pe && !bpt) {
     M = (rl ? dpf : 1.0f) * opf * cosE * g * (RX_PI * r * r) * norm;
     if (Ep.inside != kNone && Ep.contact == kNone) M *= 4.0f / 3.0f * r;
   }
@@ -368,7 +376,7 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
     if (rnd(*pe)) sum += pf1 * me.pbr;                      // connection at ci+1
     sum += pf1 * dir_pdf(S, cam, Lp, rE, false) * me.sea;
   }
-  if (!pe && !Lm) sum += pb0 / L.oprob;  // two-vertex path: mustUsePT adds pb[0] (pf[0] = originProb of L)
+  if (!pe && !Lm && !bpt) sum += pb0 / L.oprob;  // two-vertex path: VCM's mustUsePT adds pb[0] (pf[0] = originProb of L)
   const float res = (merged ? M : C) / sum;
   wt = res >= 0.0f ? res : 0.0f;
   return true;
@@ -386,9 +394,9 @@ __global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, floa
     PV start = emit_ray(S, P.cam, rng, h);
     float4* out = lv + 4 * ((size_t)p * P.maxv);
     bool emitter_seen = false;  // photons stop at the first emitter after the origin
-    int n = sample_path(S, P.cam, start, h, P.max_depth, rng, [&](int i, const PV& v) {
+    int n = sample_path(S, P.cam, start, h, P.max_depth, true, rng, [&](int i, const PV& v) {
       store_pv(out + 4 * i, v);
-      if (i == 0 || emitter_seen) return;
+      if (P.bpt || i == 0 || emitter_seen) return;  // no photons without merging
       if (is_emissive(S, v.contact)) {
         emitter_seen = true;
         return;
@@ -411,7 +419,7 @@ __global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, floa
 __global__ void __launch_bounds__(128) k_light_mis(DevScene S, VcmParams P, const float4* lv, const int* llen,
                                                    MisL* lmis) {
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += gridDim.x * blockDim.x)
-    light_mis(S, P.cam, lv + 4 * ((size_t)p * P.maxv), llen[p], P.radius, P.norm, lmis + (size_t)p * P.maxv);
+    light_mis(S, P.cam, lv + 4 * ((size_t)p * P.maxv), llen[p], P.radius, P.norm, !P.bpt, lmis + (size_t)p * P.maxv);
 }
 
 // ---- hash grid ---------------------------------------------------------------------------
@@ -546,10 +554,19 @@ __device__ __forceinline__ bool must_use_pt(const PV* w, int n) {
     if (w[i].flags & kDirRandom) return false;
   return true;
 }
+// BidirectionalPathTracer::mustUsePT (src/BidirectionalPathTracer.cpp:115-122): no two
+// consecutive vertices sampled at random.
+__device__ __forceinline__ bool bpt_must_use_pt(const PV* w, int n) {
+  for (int i = 0; i < n - 1; i++)
+    if ((w[i].flags & kDirRandom) && (w[i + 1].flags & kDirRandom)) return false;
+  return true;
+}
 
 // VCMTracer::connectMergeWeight (src/VCMTracer.cpp:321-428), power 1, double precision
+// With bpt, BidirectionalPathTracer::connectWeight (src/BidirectionalPathTracer.cpp:198-276,
+// exponent 1): no merge techniques and its own mustUsePT.
 __device__ float connect_merge_weight(const DevScene& S, const CamDev& cam, const PV* w, int n, int ci, bool merged,
-                                      float r, float norm) {
+                                      bool bpt, float r, float norm) {
   double pf[2 * kMaxV], pb[2 * kMaxV];
   float dist[2 * kMaxV];
   pf[0] = w[0].oprob;
@@ -585,7 +602,7 @@ __device__ float connect_merge_weight(const DevScene& S, const CamDev& cam, cons
   double sum = 0.0;
   for (int i = 0; i < n - 1; i++) {
     if ((w[i].flags & kDirRandom) && (w[i + 1].flags & kDirRandom)) sum += pf[i] * pb[i + 1];
-    if (i < n - 2 && (w[i + 1].flags & kDirRandom)) {
+    if (!bpt && i < n - 2 && (w[i + 1].flags & kDirRandom)) {
       double p = pf[i] * pb[i + 1];
       if (w[i].flags & kDirRandom) {
         if (i > 0) {
@@ -605,7 +622,7 @@ __device__ float connect_merge_weight(const DevScene& S, const CamDev& cam, cons
       if (merged && ci == i) self = p;
     }
   }
-  if (must_use_pt(w, n)) sum += pb[0];
+  if (bpt ? bpt_must_use_pt(w, n) : must_use_pt(w, n)) sum += pb[0];
   double res = self / sum;
   if (!(res >= 0.0)) return 0.0f;
   return (float)res;
@@ -644,30 +661,32 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
     PV eye[kMaxV];
     Hit3 h;
     PV start = camera_ray(S, P.cam, p, rng, h);
-    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, [&](int i, const PV& v) { eye[i] = v; });
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, !P.bpt, rng, [&](int i, const PV& v) { eye[i] = v; });
     nrays += (unsigned long long)ne;
     for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
     MisE* me = emis + (size_t)p * P.maxv;
-    eye_mis(S, P.cam, eye, ne, r, P.norm, me);
-    // s = 0: the eye path ends on an emitter and no interior vertex was sampled at random
-    // (mustUsePT); its weight is pb[0] / (pb[0] + the two-vertex connection).
+    eye_mis(S, P.cam, eye, ne, r, P.norm, !P.bpt, me);
+    // s = 0: the eye path ends on an emitter and the reference's mustUsePT holds: VCM, no
+    // interior vertex sampled at random (its weight pb[0] / (pb[0] + the two-vertex
+    // connection)); BidirectionalPathTracer, no two consecutive random vertices (then no
+    // connection technique exists and the weight is pb[0] / pb[0]).
     F3 acc = {0, 0, 0};
-    int first_rand = ne;
-    for (int m = 1; m < ne; m++)
-      if (rnd(eye[m])) {
-        first_rand = m;
-        break;
-      }
-    for (int t = 2; t <= ne && first_rand > t - 2; t++) {
+    int first_rand = ne, first_pair = ne;
+    for (int m = ne - 1; m >= 1; m--)
+      if (rnd(eye[m])) first_rand = m;
+    for (int m = ne - 2; m >= 0; m--)
+      if (rnd(eye[m]) && rnd(eye[m + 1])) first_pair = m;
+    for (int t = 2; t <= ne; t++) {
+      if (P.bpt ? first_pair <= t - 2 : first_rand <= t - 2) break;
       const PV& v = eye[t - 1];
       if (!is_emissive(S, v.contact)) continue;
       const MisE m = me[t - 1];
       F3 col = v.c * m.thr;
       float prob = (v.dprob * v.oprob) * m.prob;
       if (!(prob > 0.0f) || !(length(col) > 0.0f)) continue;
-      float wt = m.pb > 0.0 && m.pb < INFINITY ? 1.0f : 0.0f;  // pb[0] / pb[0]
-      if (wt > 0.0f && t == 2 && rnd(v) && rnd(eye[0])) {      // pb[0] / (pb[0] + pf[0] pb[1])
+      float wt = m.pb > 0.0 && m.pb < INFINITY ? 1.0f : 0.0f;      // pb[0] / pb[0]
+      if (!P.bpt && wt > 0.0f && t == 2 && rnd(v) && rnd(eye[0])) {  // pb[0] / (pb[0] + pf[0] pb[1])
         float res = 1.0f / (1.0f + v.oprob * m.pbr);
         wt = res >= 0.0f ? res : 0.0f;
       }
@@ -745,7 +764,7 @@ __global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, cons
       join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, k > 0 ? &pe : nullptr, false, Lp, Ep);
       F3 col;
       float prob, wt;
-      if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, k > 0 ? &pe : nullptr, ml, me, false, r, P.norm,
+      if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, k > 0 ? &pe : nullptr, ml, me, false, P.bpt, r, P.norm,
                      col, prob, wt))
         continue;
       F3 c = col * (wt / prob);
@@ -793,11 +812,11 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
     PV w[2 * kMaxV];
     Hit3 h;
     PV start = camera_ray(S, P.cam, p, rng, h);
-    int ne = sample_path(S, P.cam, start, h, P.max_depth, rng, [&](int i, const PV& v) { eye[i] = v; });
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, !P.bpt, rng, [&](int i, const PV& v) { eye[i] = v; });
     nrays += (unsigned long long)ne;
     for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
-    eye_mis(S, P.cam, eye, ne, r, P.norm, emis + (size_t)p * P.maxv);
+    eye_mis(S, P.cam, eye, ne, r, P.norm, !P.bpt, emis + (size_t)p * P.maxv);
     F3 acc = {0, 0, 0};
     uint32_t lp = p % P.n_light;
     int nl = llen[lp];
@@ -811,7 +830,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
         for (int k = t - 1; k >= 0; k--) w[n++] = eye[k];
         int ci = s - 1;
         if (s == 0 && !is_emissive(S, w[0].contact)) continue;
-        if (s == 0 && !must_use_pt(w, n)) continue;
+        if (s == 0 && !(P.bpt ? bpt_must_use_pt(w, n) : must_use_pt(w, n))) continue;
         if (s > 0) {
           if (s > 1 && is_emissive(S, w[ci].contact)) continue;
           if (is_emissive(S, w[ci + 1].contact)) continue;
@@ -828,7 +847,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
         connect_color_prob(S, P.cam, w, n, ci, false, r, col, prob);
         if (!(prob > 0.0f)) continue;
         if (!(length(col) > 0.0f)) continue;
-        float wt = connect_merge_weight(S, P.cam, w, n, ci, false, r, P.norm);
+        float wt = connect_merge_weight(S, P.cam, w, n, ci, false, P.bpt, r, P.norm);
         F3 c = col * (wt / prob);
         if (!(length(c) > 0.0f)) continue;
         if (t == 1) {  // light tracing: splat onto the pixel the light vertex projects to
@@ -949,7 +968,8 @@ __device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, 
   join(S, P.cam, L, ci > 0 ? &Lm : nullptr, E, &pe, true, Lp, Ep);
   F3 col;
   float prob, wt;
-  if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, &pe, ml, me, true, P.radius, P.norm, col, prob, wt))
+  if (!join_eval(S, P.cam, L, ci > 0 ? &Lm : nullptr, Lp, Ep, &pe, ml, me, true, false, P.radius, P.norm, col, prob,
+                 wt))
     return F3{0, 0, 0};
   return col * (wt / prob) * (1.0f / P.norm);
 }
@@ -1089,7 +1109,7 @@ __global__ void __launch_bounds__(128) k_merge_eval_full(DevScene S, VcmParams P
       float prob;
       connect_color_prob(S, P.cam, w, n, ci, true, r, col, prob);
       if (length(col) == 0.0f || prob == 0.0f) continue;
-      float wt = connect_merge_weight(S, P.cam, w, n, ci, true, r, P.norm);
+      float wt = connect_merge_weight(S, P.cam, w, n, ci, true, false, r, P.norm);
       F3 c = col * (wt / prob) * (1.0f / P.norm);
       if (p != acc_pixel) {
         if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
@@ -1136,9 +1156,10 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   P.max_depth = opt.max_depth;
   P.maxv = opt.max_depth + 3;
   P.n_pixels = cam.width * cam.height;
-  P.n_light = opt.light_paths ? opt.light_paths : P.n_pixels;
+  P.bpt = (opt.flags & kVcmBidirectional) ? 1u : 0u;
+  P.n_light = opt.light_paths && !P.bpt ? opt.light_paths : P.n_pixels;  // BPT: one light path per pixel
   P.norm = (float)P.n_light;
-  const unsigned cap = P.n_light * P.maxv;
+  const unsigned cap = P.bpt ? 1u : P.n_light * P.maxv;  // photon capacity (none without merging)
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
   std::vector<DevBuf> bufs(24);
@@ -1195,19 +1216,21 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     k_vcm_light<<<grid * 4, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
                                      bufs[3].as<int>(), nph, cap, ctr);
     k_light_mis<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[19].as<MisL>());
-    cudaMemsetAsync(bufs[6].p, 0, bufs[6].bytes, s);
-    float cell = 2.0f * radius;
-    k_grid_count<<<grid, 256, 0, s>>>(bufs[2].as<float4>(), nph, cap, cell, buckets - 1, bufs[6].as<unsigned>(),
-                                      bufs[4].as<unsigned>());
-    k_scan_blocks<unsigned><<<nblk, 1024, 0, s>>>(bufs[6].as<unsigned>(), bufs[7].as<unsigned>(),
-                                                    bufs[9].as<unsigned>(), nscan);
-    k_scan_sums<unsigned><<<1, 1024, 0, s>>>(bufs[9].as<unsigned>(), nblk);
-    k_scan_add<unsigned><<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan,
-                                                bufs[8].as<unsigned>());
-    k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap,
-                                        bufs[8].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(),
-                                        bufs[0].as<float4>(), bufs[19].as<MisL>(), P.maxv, bufs[23].as<float4>());
+    const float cell = 2.0f * radius;
     Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(), bufs[23].as<float4>()};
+    if (!P.bpt) {  // the photon grid
+      cudaMemsetAsync(bufs[6].p, 0, bufs[6].bytes, s);
+      k_grid_count<<<grid, 256, 0, s>>>(bufs[2].as<float4>(), nph, cap, cell, buckets - 1, bufs[6].as<unsigned>(),
+                                        bufs[4].as<unsigned>());
+      k_scan_blocks<unsigned><<<nblk, 1024, 0, s>>>(bufs[6].as<unsigned>(), bufs[7].as<unsigned>(),
+                                                      bufs[9].as<unsigned>(), nscan);
+      k_scan_sums<unsigned><<<1, 1024, 0, s>>>(bufs[9].as<unsigned>(), nblk);
+      k_scan_add<unsigned><<<nblk, 1024, 0, s>>>(bufs[7].as<unsigned>(), bufs[9].as<unsigned>(), nscan,
+                                                  bufs[8].as<unsigned>());
+      k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap,
+                                          bufs[8].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(),
+                                          bufs[0].as<float4>(), bufs[19].as<MisL>(), P.maxv, bufs[23].as<float4>());
+    }
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
     unsigned long long* qc = bufs[14].as<unsigned long long>();
     unsigned long long* qo = bufs[15].as<unsigned long long>();
@@ -1247,7 +1270,9 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
                                              bufs[10].as<float>(), ctr + 2);
       }
     }
-    if (full_mis) {  // merging as (query, photon) pair lists: count per query, scan, windows
+    if (P.bpt) {
+      // BidirectionalPathTracer: connections only
+    } else if (full_mis) {  // merging as (query, photon) pair lists: count per query, scan, windows
       k_merge_count<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), G, qc, nq);
       if ((e = scan_total(nq, total)) != cudaSuccess) return e;
       merges += total;

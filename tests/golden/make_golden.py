@@ -181,13 +181,53 @@ def make_vcm_goldens(ref_vcm: str):
         print(f"{path}: {runs} x {iters} iterations, mean {mean.mean(axis=(0, 1))}, {secs:.1f} s", flush=True)
 
 
+# BidirectionalPathTracer goldens: (scene function, max depth, samples per estimate,
+# independent estimates). One reference process per estimate.
+BPT_CASES = {
+    "cornell_bpt": ("cornell_box", 8, 8, 64),
+    "spheres_bpt": ("material_spheres", 8, 8, 48),
+    "medium_bpt": ("medium_scene", 8, 8, 48),
+}
+
+
+def make_bpt_goldens(ref_bpt: str):
+    for case, (scene_fn, depth, spp, runs) in BPT_CASES.items():
+        if not _selected(case):
+            continue
+        sc = render_scene(scene_fn)
+        f = sc.flatten()
+        imgs = []
+        secs = 0.0
+        with tempfile.TemporaryDirectory() as td:
+            cfg = sceneio.write_config(sc, td, "BPT", depth)
+            for run in range(runs):
+                pre = os.path.join(td, f"out{run}")
+                out = subprocess.run([ref_bpt, cfg, str(spp), str(run), pre, "8"], check=True, capture_output=True,
+                                     text=True, cwd=td).stdout.strip().splitlines()[-1].split()
+                secs += float(out[-1])
+                imgs.append(np.fromfile(pre + ".img.f64").reshape(sc.camera.height, sc.camera.width, 3))
+        imgs = np.array(imgs)
+        mean = imgs.mean(axis=0)
+        stderr = imgs.std(axis=0, ddof=1) / np.sqrt(runs)
+        path = os.path.join(HERE, f"render_{case}.npz")
+        np.savez_compressed(path, mean=mean.astype(np.float32), stderr=stderr.astype(np.float32),
+                            runs=np.int64(runs), iterations=np.int64(spp), max_depth=np.int64(depth),
+                            scene=np.array(scene_fn), seconds=np.float64(secs),
+                            geometry_sha256=np.array(geometry_hash(f["verts"], f["tris"])))
+        print(f"{path}: {runs} x {spp} spp, mean {mean.mean(axis=(0, 1))}, {secs:.1f} s", flush=True)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref = args[0] if args else "/root/reference"
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"], check=True)
+    if "--bpt-only" in sys.argv:
+        make_bpt_goldens(os.path.join(ROOT, "oracle", "_ref", "bpt_driver"))
+        return
     if "--vcm-only" not in sys.argv:
         make_render_goldens(os.path.join(ROOT, "oracle", "_ref", "pt_driver"))
     make_vcm_goldens(os.path.join(ROOT, "oracle", "_ref", "vcm_driver"))
+    make_bpt_goldens(os.path.join(ROOT, "oracle", "_ref", "bpt_driver"))
     if "--render-only" in sys.argv or "--vcm-only" in sys.argv:
         return
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "hit_driver")
