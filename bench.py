@@ -278,6 +278,24 @@ def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
+def section_bpt(spp: int = 4, res: int = 512):
+    """BidirectionalPathTracer on the VCM scene (Cornell room + homogeneous-medium sphere)
+    at res^2, depth 16: one eye and one light subpath per pixel per sample."""
+    import renderx_gb300 as rx
+    from renderx_gb300 import scenes
+    sc = scenes.medium_scene(res, res)
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ctx.render_bpt(sc.camera, 1, max_depth=16, seed=1)
+        img, st = ctx.render_bpt(sc.camera, spp, max_depth=16, seed=2)
+    rays = st["rays"] + st["shadow_rays"]
+    return {"workload": f"BidirectionalPathTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, depth 16",
+            "spp": spp, "ms": st["ms"], "ms_per_spp": st["ms"] / spp, "mrays_per_s": rays / (st["ms"] * 1e-3) / 1e6,
+            "samples_per_s": st["paths"] / (st["ms"] * 1e-3), "shadow_rays_per_spp": st["shadow_rays"] // spp,
+            "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
+
+
 def cpu_baseline(f, o, d, budget_s: float = 12.0):
     """Times the oracle (CPU restatement of the reference traversal) on a bounded
     sample of the batch with every host thread."""
@@ -403,6 +421,7 @@ def run_ours(args):
                                 lambda: section_guiding(args.guide_res, args.guide_ref_spp, args.guide_spp)),
                                ("vcm", args.skip_vcm,
                                 lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths)),
+                               ("bpt", args.skip_bpt, lambda: section_bpt()),
                                ("batch", args.skip_batch, lambda: section_batch(args.batch_scenes))):
             if skip:
                 continue
@@ -485,6 +504,7 @@ def main():
     ap.add_argument("--skip-pt", action="store_true")
     ap.add_argument("--skip-mlp", action="store_true")
     ap.add_argument("--skip-guiding", action="store_true")
+    ap.add_argument("--skip-bpt", action="store_true")
     ap.add_argument("--skip-vcm", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64)
@@ -500,7 +520,7 @@ def main():
     args = ap.parse_args()
     globals()["N_RAYS"] = args.rays
     if args.skip_extra:
-        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = True
+        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = args.skip_bpt = True
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -204,7 +204,7 @@ rx_status rx_reftree_serialize(const float* verts_xyz, uint32_t nv, const uint32
 /* What a config file asks for (ConfigManager::load, reference src/ConfigManager.cpp:166-405). */
 typedef struct rx_config_info {
   char renderer[32];       /* <Renderer><type> as written ("PT", "PTtest", "VCM", ...) */
-  int32_t estimator;       /* 0 PathTracer, 1 PathTracerTest, 2 VCMTracer, -1 other */
+  int32_t estimator;       /* 0 PathTracer, 1 PathTracerTest, 2 VCMTracer, 3 BidirectionalPathTracer, -1 other */
   uint32_t max_depth;      /* <maxDepth>, default 20 (MCRenderer) */
   uint32_t spp;            /* <spp>, 0 if absent */
   float radius;            /* <radius> (VCM merge radius), 0 if absent */

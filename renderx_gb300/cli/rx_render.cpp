@@ -5,9 +5,10 @@
 //   rx_render config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N]
 //             [--alpha A] [--seed S] [--guided] [--device D]
 //
-// The renderer type comes from the config (PathTracer / PT, PTtest, VCMTracer / VCM).
-// The reference renders until its <time> budget runs out; here a fixed sample count
-// (--spp, else <spp>, else 16) or VCM iteration count (--iterations, default 8) is used.
+// The renderer type comes from the config (PathTracer / PT, PTtest, VCMTracer / VCM,
+// BidirectionalPathTracer / BPT). The reference renders until its <time> budget runs
+// out; here a fixed sample count (--spp, else <spp>, else 16; PT, PTtest and BPT) or VCM
+// iteration count (--iterations, default 8) is used.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -83,6 +84,12 @@ int main(int argc, char** argv) {
     if (rx_render_vcm(c, &info.camera, &vo, film.data(), &st) != RX_OK) return fail(c, "rendering");
     printf("%s: %u x %u, %u iterations, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
            iters, vo.max_depth, st.ms, (unsigned long long)st.extension_rays, load_s);
+  } else if (info.estimator == 3) {
+    rx_bpt_options bo3 = {spp ? spp : (info.spp ? info.spp : 16u), info.max_depth > 21 ? 21u : info.max_depth, 0, 0,
+                          seed};
+    if (rx_render_bpt(c, &info.camera, &bo3, film.data(), &st) != RX_OK) return fail(c, "rendering");
+    printf("%s: %u x %u, %u spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
+           bo3.iterations, bo3.max_depth, st.ms, (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
   } else {
     fprintf(stderr, "rx_render: renderer type '%s' is not on this library's path\n", info.renderer);
     rx_destroy(c);

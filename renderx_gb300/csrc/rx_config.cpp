@@ -509,6 +509,7 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
   if (type == "PathTracer" || type == "PT") in.estimator = 0;
   if (type == "PTtest") in.estimator = 1;
   if (type == "VCMTracer" || type == "VCM") in.estimator = 2;
+  if (type == "BidirectionalPathTracer" || type == "BPT") in.estimator = 3;
   const char* md = rn ? rn->value("maxDepth") : cfg->value("maxDepth");
   if (md) in.max_depth = (uint32_t)atoi(md);
   const char* spp = rn ? rn->value("spp") : nullptr;

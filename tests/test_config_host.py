@@ -145,3 +145,13 @@ def test_cli_usage():
     assert r.returncode == 2 and "config.xml" in r.stderr
     r = subprocess.run([build.CLI, "x.xml", "--bogus"], capture_output=True, text=True)
     assert r.returncode == 2 and "unknown option" in r.stderr
+
+
+@pytest.mark.parametrize("type_name,code", [("PathTracer", 0), ("PT", 0), ("PTtest", 1), ("VCMTracer", 2), ("VCM", 2),
+                                            ("BidirectionalPathTracer", 3), ("BPT", 3), ("IPT", -1)])
+def test_renderer_type_names(tmp_path, type_name, code):
+    # ConfigManager.cpp:323-354: the <Renderer><type> names and the renderer each selects
+    sc = scenes.cornell_box(8, 8)
+    cfg = sceneio.write_config(sc, str(tmp_path), type_name, 5)
+    _, info = rx.config_read(cfg)
+    assert info["estimator"] == code and info["renderer"] == type_name and info["max_depth"] == 5
