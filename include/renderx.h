@@ -55,6 +55,8 @@ typedef struct rx_object {
   float sigma_s[3], sigma_a[3];   /* homogeneous medium */
   float g;                        /* HG asymmetry */
   float decay[3];                 /* RefractiveMaterial decayColor (per unit length) */
+  float step_size;                /* medium ray-marching step of PhotonMap (SceneVPMObject::stepSize,
+                                     <stepsize>; 0 = the reference's 0.0005) */
 } rx_object;
 
 typedef struct rx_build_options {
@@ -156,13 +158,25 @@ typedef struct rx_bpt_options {
   uint64_t seed;
 } rx_bpt_options;
 
+/* PhotonMap options (reference include/Photonmap.h): progressive photon mapping with
+ * ray marching through media. */
+typedef struct rx_pm_options {
+  uint32_t iterations;     /* progressive iterations (PhotonMap::spp) */
+  uint32_t max_depth;      /* light-path depth (MCRenderer::maxDepth), at most 21 */
+  uint32_t light_paths;    /* photon paths per iteration, 0 = width*height (mPhotonsNum) */
+  uint32_t flags;          /* 0 */
+  float radius;            /* base radius (PhotonMap::setRadius, <radius>) */
+  float alpha;             /* radius exponent, 0 = the reference's 2/3 */
+  uint64_t seed;
+} rx_pm_options;
+
 typedef struct rx_render_stats {
   uint64_t extension_rays; /* closest-hit rays traced (camera + bounce) */
   uint64_t shadow_rays;    /* next-event-estimation visibility rays */
   uint64_t paths;          /* pixel samples */
   float ms;                /* device time of the render (CUDA events) */
   float reserved;
-  uint64_t merges;         /* VCM: (eye vertex, photon) pairs merged */
+  uint64_t merges;         /* VCM: (eye vertex, photon) pairs merged; PhotonMap: photons stored */
 } rx_render_stats;
 
 /* ---- context ------------------------------------------------------------------- */
@@ -204,7 +218,8 @@ rx_status rx_reftree_serialize(const float* verts_xyz, uint32_t nv, const uint32
 /* What a config file asks for (ConfigManager::load, reference src/ConfigManager.cpp:166-405). */
 typedef struct rx_config_info {
   char renderer[32];       /* <Renderer><type> as written ("PT", "PTtest", "VCM", ...) */
-  int32_t estimator;       /* 0 PathTracer, 1 PathTracerTest, 2 VCMTracer, 3 BidirectionalPathTracer, -1 other */
+  int32_t estimator;       /* 0 PathTracer, 1 PathTracerTest, 2 VCMTracer, 3 BidirectionalPathTracer,
+                              4 PhotonMap, -1 other */
   uint32_t max_depth;      /* <maxDepth>, default 20 (MCRenderer) */
   uint32_t spp;            /* <spp>, 0 if absent */
   float radius;            /* <radius> (VCM merge radius), 0 if absent */
@@ -293,6 +308,12 @@ rx_status rx_render_vcm(rx_context* ctx, const rx_camera* cam, const rx_vcm_opti
  * and the vignetting correction. Output as rx_render_vcm. */
 rx_status rx_render_bpt(rx_context* ctx, const rx_camera* cam, const rx_bpt_options* opts, double* film_rgb,
                         rx_render_stats* stats);
+/* Replaces PhotonMap::renderPixels (reference src/Photonmap.cpp:12-138): the running mean
+ * of `iterations` progressive photon-mapping images (surface gather at the first random
+ * eye vertex, ray-marched gather through homogeneous media with each medium's
+ * step_size). Output as rx_render_vcm. */
+rx_status rx_render_pm(rx_context* ctx, const rx_camera* cam, const rx_pm_options* opts, double* film_rgb,
+                       rx_render_stats* stats);
 
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
  * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative

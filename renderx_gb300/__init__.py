@@ -17,8 +17,8 @@ import ctypes
 import numpy as np
 
 from . import _capi
-from ._capi import (RxError, rx_bpt_options, rx_build_options, rx_camera, rx_object, rx_pt_options, rx_render_stats,
-                    rx_vcm_options)
+from ._capi import (RxError, rx_bpt_options, rx_build_options, rx_camera, rx_object, rx_pm_options, rx_pt_options,
+                    rx_render_stats, rx_vcm_options)
 from . import scenes
 
 __all__ = ["Context", "KDTree", "RxError", "reftree_serialize", "scenes", "rays_to_array"]
@@ -256,6 +256,17 @@ class Context:
         self._ck(self._L.rx_render_bpt(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
         return film, dict(rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms)
 
+    def render_pm(self, camera: "scenes.Camera", iterations: int, radius: float, max_depth: int = 8,
+                  light_paths: int = 0, alpha: float = 0.0, seed: int = 1):
+        """PhotonMap renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats);
+        ``alpha`` 0 is the reference's 2/3, ``light_paths`` 0 is width * height."""
+        cam = camera_struct(camera)
+        o = rx_pm_options(iterations, max_depth, light_paths, 0, radius, alpha, seed)
+        film = np.zeros((camera.height, camera.width, 3), np.float64)
+        st = rx_render_stats()
+        self._ck(self._L.rx_render_pm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
+        return film, dict(rays=st.extension_rays, photons=st.merges, paths=st.paths, ms=st.ms)
+
     def set_trace_config(self, variant: int = 3, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
@@ -371,6 +382,7 @@ def objects_from_scene(scene: "scenes.Scene"):
         ro.sigma_a[:] = m.sigma_a
         ro.g = m.g
         ro.decay[:] = m.decay
+        ro.step_size = m.step_size
         objs.append(ro)
         off += len(o.tris)
     return objs

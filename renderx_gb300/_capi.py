@@ -27,7 +27,8 @@ class rx_object(ctypes.Structure):
     _fields_ = [("tri_begin", ctypes.c_uint32), ("tri_count", ctypes.c_uint32), ("material", ctypes.c_uint32),
                 ("has_vertex_normals", ctypes.c_uint32), ("color", ctypes.c_float * 3), ("coeff", ctypes.c_float),
                 ("diffuse_color", ctypes.c_float * 3), ("ior", ctypes.c_float), ("sigma_s", ctypes.c_float * 3),
-                ("sigma_a", ctypes.c_float * 3), ("g", ctypes.c_float), ("decay", ctypes.c_float * 3)]
+                ("sigma_a", ctypes.c_float * 3), ("g", ctypes.c_float), ("decay", ctypes.c_float * 3),
+                ("step_size", ctypes.c_float)]
 
 
 class rx_camera(ctypes.Structure):
@@ -69,6 +70,12 @@ class rx_vcm_options(ctypes.Structure):
 class rx_bpt_options(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+class rx_pm_options(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("light_paths", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("radius", ctypes.c_float), ("alpha", ctypes.c_float),
+                ("seed", ctypes.c_uint64)]
 
 
 class rx_render_stats(ctypes.Structure):
@@ -126,6 +133,7 @@ SIGNATURES = [
     ("rx_render_pt", S, [P, P, P, P, P, P]),
     ("rx_render_vcm", S, [P, P, P, P, P]),
     ("rx_render_bpt", S, [P, P, P, P, P]),
+    ("rx_render_pm", S, [P, P, P, P, P]),
     ("rx_render_pt_batch", S, [P, P, U32, P, P]),
 ]
 

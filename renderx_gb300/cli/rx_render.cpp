@@ -6,9 +6,9 @@
 //             [--alpha A] [--seed S] [--guided] [--device D]
 //
 // The renderer type comes from the config (PathTracer / PT, PTtest, VCMTracer / VCM,
-// BidirectionalPathTracer / BPT). The reference renders until its <time> budget runs
-// out; here a fixed sample count (--spp, else <spp>, else 16; PT, PTtest and BPT) or VCM
-// iteration count (--iterations, default 8) is used.
+// BidirectionalPathTracer / BPT, PhotonMap / PM). The reference renders until its <time>
+// budget runs out; here a fixed sample count (--spp, else <spp>, else 16; PT, PTtest and
+// BPT) or iteration count (--iterations, default 8; VCM and PM) is used.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -90,6 +90,13 @@ int main(int argc, char** argv) {
     if (rx_render_bpt(c, &info.camera, &bo3, film.data(), &st) != RX_OK) return fail(c, "rendering");
     printf("%s: %u x %u, %u spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
            bo3.iterations, bo3.max_depth, st.ms, (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
+  } else if (info.estimator == 4) {
+    float r = info.radius > 0 ? info.radius : 0.01f;
+    rx_pm_options pm = {iters, info.max_depth > 21 ? 21u : info.max_depth, light_paths, 0, r, 0.0f, seed};
+    if (rx_render_pm(c, &info.camera, &pm, film.data(), &st) != RX_OK) return fail(c, "rendering");
+    printf("%s: %u x %u, %u iterations, depth %u: %.1f ms, %llu rays, %llu photons (load + build %.2f s)\n",
+           info.renderer, w, h, iters, pm.max_depth, st.ms, (unsigned long long)st.extension_rays,
+           (unsigned long long)st.merges, load_s);
   } else {
     fprintf(stderr, "rx_render: renderer type '%s' is not on this library's path\n", info.renderer);
     rx_destroy(c);

@@ -294,6 +294,7 @@ rx_status rx_context::build_scene() {
     std::memcpy(d.sigma_a, r.sigma_a, sizeof d.sigma_a);
     d.g = r.g;
     std::memcpy(d.decay, r.decay, sizeof d.decay);
+    d.step_size = r.step_size > 0.0f ? r.step_size : 0.0005f;  // SceneVPMObject.h:64
   }
   for (uint32_t t = 0; t < nt; t++) {
     if (c->objects[c->tri_obj[t]].material != RX_MAT_EMISSIVE) continue;
@@ -461,6 +462,32 @@ rx_status rx_render_bpt(rx_context* c, const rx_camera* cam, const rx_bpt_option
   if ((opts->flags & ~RX_VCM_FULL_PATH_MIS) || opts->reserved) return c->fail(RX_ERR_INVALID, "unknown BPT flags");
   rx_vcm_options v{opts->iterations, opts->max_depth, 0u, opts->flags | rx::kVcmBidirectional, 1.0f, 1.0f, opts->seed};
   return render_bidirectional(c, cam, &v, film_rgb, stats);
+}
+
+rx_status rx_render_pm(rx_context* c, const rx_camera* cam, const rx_pm_options* opts, double* film_rgb,
+                       rx_render_stats* stats) {
+  if (!c) return RX_ERR_INVALID;
+  if (!cam || !opts || !film_rgb) return c->fail(RX_ERR_INVALID, "null argument");
+  if (!c->scene_ready) return c->fail(RX_ERR_STATE, "scene objects not built (rx_scene_set_objects, rx_build_accel)");
+  if (cam->width == 0 || cam->height == 0 || cam->sight_dist == 0) return c->fail(RX_ERR_INVALID, "bad camera");
+  if (opts->iterations == 0) return c->fail(RX_ERR_INVALID, "iterations must be positive");
+  if (opts->max_depth > 21) return c->fail(RX_ERR_INVALID, "max_depth must be at most 21");
+  if (!(opts->radius > 0.0f) || !(opts->alpha >= 0.0f) || opts->flags)
+    return c->fail(RX_ERR_INVALID, "radius must be positive, alpha non-negative, flags 0");
+  if (c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "photon mapping needs an emitter");
+  DeviceGuard g(c->device);
+  size_t np = (size_t)cam->width * cam->height;
+  DevBuf film;
+  rx_status s;
+  if ((s = c->cuda(film.alloc(np * 3 * sizeof(double)), "film")) != RX_OK) return s;
+  cudaMemsetAsync(film.p, 0, film.bytes, c->stream);
+  rx_render_stats st{};
+  if ((s = c->cuda(rx::render_pm(c, *cam, *opts, film.as<double>(), &st, c->stream), "render_pm")) != RX_OK) return s;
+  std::vector<double> h(np * 3);
+  if ((s = c->cuda(cudaMemcpy(h.data(), film.p, film.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
+  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->iterations;
+  if (stats) *stats = st;
+  return RX_OK;
 }
 
 rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {

@@ -387,6 +387,7 @@ bool material(const XNode* nm, rx_object& o, std::string& err) {
     vec(nm, "sigma_a", o.sigma_a);
     num(nm, "inrate", o.ior);
     num(nm, "g", o.g);
+    if (nm->first("stepsize")) num(nm, "stepsize", o.step_size);  // ConfigManager.cpp:69-70
   } else {
     return err = "material type " + t + " is not supported", false;
   }
@@ -510,6 +511,7 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
   if (type == "PTtest") in.estimator = 1;
   if (type == "VCMTracer" || type == "VCM") in.estimator = 2;
   if (type == "BidirectionalPathTracer" || type == "BPT") in.estimator = 3;
+  if (type == "PhotonMap" || type == "PM") in.estimator = 4;
   const char* md = rn ? rn->value("maxDepth") : cfg->value("maxDepth");
   if (md) in.max_depth = (uint32_t)atoi(md);
   const char* spp = rn ? rn->value("spp") : nullptr;

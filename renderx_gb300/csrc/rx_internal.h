@@ -182,4 +182,7 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
 constexpr uint32_t kVcmBidirectional = 1u << 31;
 cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
                        rx_render_stats* stats, cudaStream_t s);
+// PhotonMap (rx_vcm.cu): adds iteration images to `film` (sum).
+cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& opt, double* film,
+                      rx_render_stats* stats, cudaStream_t s);
 }  // namespace rx

@@ -29,6 +29,7 @@ struct DevObject {
   float sigma_s[3], sigma_a[3];
   float g;
   float decay[3];
+  float step_size;  // PhotonMap's ray-marching step in a medium
 };
 
 struct DevScene {

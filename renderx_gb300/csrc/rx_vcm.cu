@@ -1132,10 +1132,247 @@ __global__ void k_vcm_accumulate(VcmParams P, const float* img, double* film) {
   }
 }
 
+// ---- PhotonMap (src/Photonmap.cpp) --------------------------------------------------------
+// Progressive photon mapping with ray marching through media, as PhotonMap::renderPixels
+// runs it (rayMarching is always on there): per iteration W x H light paths deposit
+// photons at their random vertices up to the first emitter (surface photons, OUTVOL, and
+// in-medium photons, INVOL); each eye path (sampleMergePath: eye-path scattering, at most
+// MERGE_LEN bounces, passing straight through media) gathers at its first random surface
+// vertex and, along every segment inside a homogeneous medium, at ray-marching steps of
+// the medium's stepSize, with the kernel 3 (1 - d^2/r^2)^2 / pi over N r^2 (surface) or
+// N r^3 (medium). Photons share the VCM hash grid.
+constexpr int kPmMergeLen = 10;           // MERGE_LEN (Photonmap.cpp:7)
+constexpr int kPmMaxV = kPmMergeLen + 3;  // rays of an eye merge path, with its terminator
+constexpr uint32_t kOutVol = 0u, kInVol = 1u;  // Ray::PhotonType OUTVOL / INVOL
+constexpr int kPmData = 5;                // per photon: the photon ray (4 float4), its power
+__device__ __forceinline__ F3 fdiv(F3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+
+// Light paths and photons (Photonmap.cpp:55-86): the photon at light vertex i carries
+// prod_{k<i} colour_k / directionProb_k / originProb_k x cosine_k x transmittance_k over
+// originProb_i (Photonmap.cpp:229-236), and its ray with the arriving direction.
+__global__ void __launch_bounds__(128) k_pm_light(DevScene S, VcmParams P, float4* ph_pos, float4* ph_data,
+                                                  unsigned* n_photons, unsigned cap, unsigned long long* rays) {
+  uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long nr = 0;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_light; p += stride) {
+    Rng rng(P.seed, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+    Hit3 h;
+    PV start = emit_ray(S, P.cam, rng, h);
+    PV prev;
+    F3 thr = {1, 1, 1};
+    bool stop = false;
+    int n = sample_path(S, P.cam, start, h, P.max_depth, true, rng, [&](int i, const PV& v) {
+      if (i > 0) {
+        thr = thr * fdiv(fdiv(prev.c, prev.dprob), prev.oprob);
+        thr = thr * cos_term(S, P.cam, prev);
+        thr = thr * decay_of(S, prev.inside, length(prev.o - v.o));
+        if (!stop && is_emissive(S, v.contact)) stop = true;  // light is not reflective
+        if (!stop && (v.flags & kDirRandom)) {
+          unsigned slot = atomicAdd(n_photons, 1u);
+          if (slot < cap) {
+            const bool in_vol = v.contact == kNone && is_vpm(S, v.inside);
+            ph_pos[slot] = make_float4(v.o.x, v.o.y, v.o.z, __uint_as_float(in_vol ? kInVol : kOutVol));
+            PV ray = v;
+            ray.d = prev.d;
+            store_pv(ph_data + (size_t)kPmData * slot, ray);
+            F3 pw = fdiv(thr, v.oprob);
+            ph_data[(size_t)kPmData * slot + 4] = make_float4(pw.x, pw.y, pw.z, 0.0f);
+          }
+        }
+      }
+      prev = v;
+    });
+    nr += (unsigned long long)n;
+  }
+  if (nr) atomicAdd(rays, nr);
+}
+
+__global__ void k_pm_scatter(const unsigned* key, const float4* pos, const float4* data, const unsigned* n_photons,
+                             unsigned cap, unsigned* cursor, float4* pos_out, float4* data_out) {
+  unsigned n = min(*n_photons, cap);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned slot = atomicAdd(&cursor[key[i]], 1u);
+    pos_out[slot] = pos[i];
+#pragma unroll
+    for (int k = 0; k < kPmData; k++) data_out[(size_t)kPmData * slot + k] = data[(size_t)kPmData * i + k];
+  }
+}
+
+// Bounding boxes of the surface and the medium photons (HashGrid::Build): a query
+// outside its grid's box finds nothing (Hashgrid.h Process). Floats as order-preserving
+// integers for the atomics; box = {min xyz, max xyz} per type.
+__device__ __forceinline__ int ordered(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float unordered(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+__global__ void k_pm_box_init(int* box) {
+  if (threadIdx.x < 12) box[threadIdx.x] = (threadIdx.x % 6) < 3 ? INT_MAX : INT_MIN;
+}
+__global__ void k_pm_box(const float4* pos, const unsigned* n_photons, unsigned cap, int* box) {
+  unsigned n = min(*n_photons, cap);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 q = pos[i];
+    int* b = box + 6 * (int)__float_as_uint(q.w);
+    atomicMin(b + 0, ordered(q.x));
+    atomicMin(b + 1, ordered(q.y));
+    atomicMin(b + 2, ordered(q.z));
+    atomicMax(b + 3, ordered(q.x));
+    atomicMax(b + 4, ordered(q.y));
+    atomicMax(b + 5, ordered(q.z));
+  }
+}
+
+// The density estimate at x of the photons of one type (Photonmap.cpp:211-259), for the
+// out ray `out` (the eye side). Lanes of a warp split the photons when `coop`, else one
+// lane does the whole query.
+__device__ F3 pm_gather(const DevScene& S, const CamDev& cam, const Grid& G, const float4* pdata, const int* box,
+                        F3 x, const PV& out, uint32_t type, float r, float nph, bool coop, int lane) {
+  const int* b = box + 6 * type;
+  if (x.x < unordered(b[0]) || x.y < unordered(b[1]) || x.z < unordered(b[2]) || x.x > unordered(b[3]) ||
+      x.y > unordered(b[4]) || x.z > unordered(b[5]))
+    return F3{0, 0, 0};
+  F3 contrib = {0, 0, 0};
+  const float r2 = r * r;
+  const float norm = type == kInVol ? nph * r * r * r : nph * r * r;
+  merge_buckets(G, x, r, [&](unsigned b0, unsigned b1) {
+    for (unsigned i = b0 + (coop ? (unsigned)lane : 0u); i < b1; i += coop ? 32u : 1u) {
+      const float4 q = G.pos[i];
+      if (__float_as_uint(q.w) != type) continue;
+      const float dist = length(x - f3(q));
+      const float d2 = dist * dist;
+      if (!(d2 <= r2)) continue;
+      const float4* pd = pdata + (size_t)kPmData * i;
+      const PV ray = load_pv(pd);
+      const F3 color = f3(pd[4]) * bsdf_of(S, cam, ray, out);
+      if (lum(color) < 1e-6f) continue;
+      const float sk = fmaxf(0.0f, 1.0f - d2 / r2);
+      const float kernel = 3.0f * sk * sk / RX_PI;
+      contrib = contrib + color * (kernel / norm);
+    }
+  });
+  return contrib;
+}
+
+// One warp per pixel: lane 0 samples the eye merge path into shared memory, then the
+// lanes share the ray-marching steps of each medium segment and the photons of the
+// surface gather.
+__global__ void __launch_bounds__(128) k_pm_eye(DevScene S, VcmParams P, Grid G, const float4* pdata, const int* box,
+                                                float* img, unsigned long long* rays) {
+  __shared__ float4 paths[4][kPmMaxV * 4];
+  const int lane = threadIdx.x & 31;
+  float4* sp = paths[threadIdx.x >> 5];
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  const float r = P.radius;
+  unsigned long long nr = 0;
+  for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < P.n_pixels; p += nw) {
+    Rng rng(P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+    int n = 0;
+    if (lane == 0) {  // PhotonMap::sampleMergePath (Photonmap.cpp:142-187)
+      Hit3 h;
+      PV prev = camera_ray(S, P.cam, p, rng, h);
+      for (int depth = 0;; depth++) {
+        store_pv(sp + 4 * n++, prev);
+        PV next;
+        if (prev.inside != kNone && !is_vpm(S, prev.inside)) {
+          next = scatter_object(S, P.cam, prev.inside, prev, h, false, true, rng);
+        } else if (h.obj != kNone) {
+          PV in = prev;
+          Hit3 hh = h;
+          if (is_vpm(S, h.obj) && prev.contact >= 0 && is_vpm(S, prev.contact)) {  // straight through the medium
+            in.o = prev.o + prev.d * h.dist;
+            hh.dist = 0.0f;
+          }
+          next = scatter_object(S, P.cam, h.obj, in, hh, false, true, rng);
+        } else {
+          store_pv(sp + 4 * n++, pv_term(prev.o));
+          break;
+        }
+        if (length(next.d) < 0.5f) {
+          store_pv(sp + 4 * n++, next);
+          break;
+        }
+        if (depth + 1 > kPmMergeLen) {
+          store_pv(sp + 4 * n++, pv_term(prev.o));
+          break;
+        }
+        PHit t = trace_cond<false>(S, next.o, next.d, INFINITY, next.contact, next.inside);
+        if (t.tid < 0) {
+          store_pv(sp + 4 * n++, next);
+          store_pv(sp + 4 * n++, pv_term(prev.o));
+          break;
+        }
+        h = Hit3{(int)__ldg(&S.tri_obj[t.tid]), t.tid, t.t};
+        prev = next;
+      }
+      nr += (unsigned long long)n;
+    }
+    n = __shfl_sync(0xffffffffu, n, 0);
+    __syncwarp();
+    // PhotonMap::throughputByDensityEstimation (Photonmap.cpp:262-386), rayMarching on
+    F3 Tr = {1, 1, 1}, surf = {0, 0, 0}, vol = {0, 0, 0};
+    for (int i = 1; i < n; i++) {
+      const PV a = load_pv(sp + 4 * (i - 1)), b = load_pv(sp + 4 * i);
+      const float dist = fmaxf(length(a.o - b.o), 1e-5f);
+      if (is_vpm(S, a.inside)) {
+        const float step_size = S.objects[a.inside].step_size;
+        int N = (int)(dist / step_size);
+        if (N == 0) N++;
+        const float step = dist / (float)N;
+        float u = 0.0f;
+        if (lane == 0) u = rng.next();
+        const float offset = step * __shfl_sync(0xffffffffu, u, 0);
+        Tr = Tr * decay_of(S, a.inside, offset);
+        for (int j = lane; j < N; j += 32) {
+          const float t = offset + step * (float)j;
+          PV out = a;
+          out.d = -a.d;
+          out.o = a.o + a.d * t;
+          out.contact = kNone;
+          const F3 c = pm_gather(S, P.cam, G, pdata, box, out.o, out, kInVol, r, P.norm, false, lane);
+          vol = vol + c * (Tr * decay_of(S, a.inside, step * (float)(j + 1))) * step;
+        }
+        Tr = Tr * decay_of(S, a.inside, step * (float)N);
+      } else if (a.inside != kNone) {
+        Tr = Tr * decay_of(S, a.inside, dist);
+      }
+      if (is_emissive(S, b.contact)) {  // the eye path hit a light: its radiance (lane 0's share)
+        surf = lane == 0 ? b.c : F3{0, 0, 0};
+        break;
+      }
+      if (b.contact != kNone && rnd(b)) {
+        if (is_vpm(S, b.contact)) continue;
+        PV out = b;
+        out.d = -a.d;
+        surf = pm_gather(S, P.cam, G, pdata, box, b.o, out, kOutVol, r, P.norm, true, lane);
+        break;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      vol.x += __shfl_xor_sync(0xffffffffu, vol.x, o);
+      vol.y += __shfl_xor_sync(0xffffffffu, vol.y, o);
+      vol.z += __shfl_xor_sync(0xffffffffu, vol.z, o);
+      surf.x += __shfl_xor_sync(0xffffffffu, surf.x, o);
+      surf.y += __shfl_xor_sync(0xffffffffu, surf.y, o);
+      surf.z += __shfl_xor_sync(0xffffffffu, surf.z, o);
+    }
+    if (lane == 0) {
+      const PV e0 = load_pv(sp);
+      F3 color = Tr * surf + vol;
+      color = color * fdiv(fdiv(cos_term(S, P.cam, e0) * e0.c, e0.dprob), e0.oprob);
+      img[3 * p] = color.x;
+      img[3 * p + 1] = color.y;
+      img[3 * p + 2] = color.z;
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && nr) atomicAdd(rays, nr);
+}
+
 // ---- host driver -----------------------------------------------------------------------
-cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
-                       rx_render_stats* stats, cudaStream_t s) {
-  const DevScene& S = c->scene;
+// The camera frame of Camera (src/Camera.cpp): front, right and up from position, focus
+// and up, integer sightDist.
+static VcmParams camera_params(const rx_camera& cam) {
   VcmParams P{};
   auto v3 = [](const float* p) { return F3{p[0], p[1], p[2]}; };
   auto hn = [](F3 a) {
@@ -1152,6 +1389,14 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   P.cam.width = (int)cam.width;
   P.cam.height = (int)cam.height;
   P.focus = foc;
+  P.n_pixels = cam.width * cam.height;
+  return P;
+}
+
+cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
+                       rx_render_stats* stats, cudaStream_t s) {
+  const DevScene& S = c->scene;
+  VcmParams P = camera_params(cam);
   P.seed = opt.seed;
   P.max_depth = opt.max_depth;
   P.maxv = opt.max_depth + 3;
@@ -1330,6 +1575,94 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     stats->extension_rays = h[0] + h[1];
     stats->shadow_rays = h[2];
     stats->merges = merges;
+    stats->paths = (uint64_t)P.n_pixels * opt.iterations;
+    stats->ms = ms;
+  }
+  return cudaSuccess;
+}
+
+// PhotonMap::renderPixels (src/Photonmap.cpp:12-138): per iteration s the radius
+// max(r0 ((s+1)^(alpha-1))^(1/3), EPSILON), light paths and photons, the hash grid over
+// all photons with a box per photon type, the eye pass, and the running mean of the
+// vignetting-corrected images.
+cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& opt, double* film,
+                      rx_render_stats* stats, cudaStream_t s) {
+  const DevScene& S = c->scene;
+  VcmParams P = camera_params(cam);
+  P.seed = opt.seed;
+  P.max_depth = opt.max_depth;
+  P.maxv = opt.max_depth + 3;
+  P.n_light = opt.light_paths ? opt.light_paths : P.n_pixels;  // mPhotonsNum = W * H
+  P.norm = (float)P.n_light;
+  const float alpha = opt.alpha > 0.0f ? opt.alpha : 2.0f / 3.0f;  // mAlpha
+  const unsigned cap = P.n_light * P.maxv;
+  unsigned buckets = 1u << 16;
+  while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
+  const unsigned nscan = buckets + 1, nblk = (nscan + 1023) / 1024;
+  std::vector<DevBuf> bufs(12);
+  cudaError_t e;
+  auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
+  if ((e = al(0, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;            // photon positions (+ type)
+  if ((e = al(1, (size_t)cap * kPmData * sizeof(float4))) != cudaSuccess) return e;  // photon rays, powers
+  if ((e = al(2, (size_t)cap * sizeof(unsigned))) != cudaSuccess) return e;          // bucket keys
+  if ((e = al(3, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;            // positions, bucket order
+  if ((e = al(4, (size_t)cap * kPmData * sizeof(float4))) != cudaSuccess) return e;  // data, bucket order
+  if ((e = al(5, (size_t)nscan * sizeof(unsigned))) != cudaSuccess) return e;        // counts
+  if ((e = al(6, (size_t)nscan * sizeof(unsigned))) != cudaSuccess) return e;        // start
+  if ((e = al(7, (size_t)nscan * sizeof(unsigned))) != cudaSuccess) return e;        // cursor
+  if ((e = al(8, ((size_t)nblk + 2) * sizeof(unsigned))) != cudaSuccess) return e;   // block sums
+  if ((e = al(9, (size_t)P.n_pixels * 3 * sizeof(float))) != cudaSuccess) return e;  // iteration image
+  if ((e = al(10, 16 * sizeof(unsigned long long))) != cudaSuccess) return e;        // counters
+  if ((e = al(11, 12 * sizeof(int))) != cudaSuccess) return e;                       // photon boxes
+  unsigned long long* ctr = bufs[10].as<unsigned long long>();
+  unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
+  cudaMemsetAsync(ctr, 0, 16 * sizeof(unsigned long long), s);
+  const int grid = c->trace_cfg.sms * 4;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  unsigned long long photons = 0;
+  for (uint32_t it = 0; it < opt.iterations; it++) {
+    P.iter = it;
+    P.radius = fmaxf(opt.radius * powf(powf((float)(it + 1), alpha - 1.0f), 1.0f / 3.0f), 1e-5f);
+    cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
+    k_pm_light<<<grid * 4, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<float4>(), nph, cap, ctr);
+    const float cell = 2.0f * P.radius;
+    cudaMemsetAsync(bufs[5].p, 0, bufs[5].bytes, s);
+    k_grid_count<<<grid, 256, 0, s>>>(bufs[0].as<float4>(), nph, cap, cell, buckets - 1, bufs[5].as<unsigned>(),
+                                      bufs[2].as<unsigned>());
+    k_scan_blocks<unsigned><<<nblk, 1024, 0, s>>>(bufs[5].as<unsigned>(), bufs[6].as<unsigned>(),
+                                                    bufs[8].as<unsigned>(), nscan);
+    k_scan_sums<unsigned><<<1, 1024, 0, s>>>(bufs[8].as<unsigned>(), nblk);
+    k_scan_add<unsigned><<<nblk, 1024, 0, s>>>(bufs[6].as<unsigned>(), bufs[8].as<unsigned>(), nscan,
+                                                bufs[7].as<unsigned>());
+    k_pm_scatter<<<grid, 256, 0, s>>>(bufs[2].as<unsigned>(), bufs[0].as<float4>(), bufs[1].as<float4>(), nph, cap,
+                                      bufs[7].as<unsigned>(), bufs[3].as<float4>(), bufs[4].as<float4>());
+    k_pm_box_init<<<1, 32, 0, s>>>(bufs[11].as<int>());
+    k_pm_box<<<grid, 256, 0, s>>>(bufs[0].as<float4>(), nph, cap, bufs[11].as<int>());
+    Grid G{cell, buckets - 1, bufs[6].as<unsigned>(), bufs[3].as<float4>(), nullptr, nullptr};
+    cudaMemsetAsync(bufs[9].p, 0, bufs[9].bytes, s);
+    k_pm_eye<<<grid * 2, 128, 0, s>>>(S, P, G, bufs[4].as<float4>(), bufs[11].as<int>(), bufs[9].as<float>(), ctr + 1);
+    k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[9].as<float>(), film);
+    unsigned np = 0;
+    cudaMemcpyAsync(&np, nph, sizeof np, cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    photons += std::min(np, cap);
+  }
+  cudaEventRecord(e1, s);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (stats) {
+    unsigned long long h[2];
+    cudaMemcpy(h, ctr, sizeof h, cudaMemcpyDeviceToHost);
+    stats->extension_rays = h[0] + h[1];
+    stats->shadow_rays = 0;
+    stats->merges = photons;
     stats->paths = (uint64_t)P.n_pixels * opt.iterations;
     stats->ms = ms;
   }

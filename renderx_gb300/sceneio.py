@@ -60,7 +60,7 @@ def _material_xml(m: scenes.Material) -> str:
         x.append(f"<DiffuseComponent><color>{_vec(m.diffuse_color)}</color></DiffuseComponent>")
     if m.kind == VPM:
         x.append(f"<sigma_s>{_vec(m.sigma_s)}</sigma_s><sigma_a>{_vec(m.sigma_a)}</sigma_a>")
-        x.append(f"<inrate>{m.ior:.9g}</inrate><g>{m.g:.9g}</g>")
+        x.append(f"<inrate>{m.ior:.9g}</inrate><g>{m.g:.9g}</g><stepsize>{m.step_size:.9g}</stepsize>")
     return "<Material>" + "".join(x) + "</Material>"
 
 
@@ -158,6 +158,8 @@ def read_config(path: str) -> tuple[scenes.Scene, dict]:
             m.sigma_a = _read_vec(mn.findtext("sigma_a"))
             m.ior = float(mn.findtext("inrate"))
             m.g = float(mn.findtext("g"))
+            if mn.findtext("stepsize") is not None:
+                m.step_size = float(mn.findtext("stepsize"))
         v, t, n = read_obj(os.path.join(folder, on.findtext("filePath")))
         objs.append(scenes.Obj(on.get("Name", f"obj{len(objs)}"), v, t, m, n))
     cn = root.find("Camera")

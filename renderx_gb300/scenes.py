@@ -41,6 +41,7 @@ class Material:
     sigma_a: tuple = (0.0, 0.0, 0.0)
     g: float = 0.0
     decay: tuple = (1.0, 1.0, 1.0)     # refractive decayColor (per unit length)
+    step_size: float = 0.0005          # medium: PhotonMap ray-marching step (SceneVPMObject::stepSize)
 
 
 @dataclass

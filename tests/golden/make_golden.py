@@ -217,6 +217,50 @@ def make_bpt_goldens(ref_bpt: str):
         print(f"{path}: {runs} x {spp} spp, mean {mean.mean(axis=(0, 1))}, {secs:.1f} s", flush=True)
 
 
+# PhotonMap goldens: (scene function, max depth, iterations per estimate, independent
+# estimates, base radius, medium ray-marching step). One reference process per estimate.
+PM_CASES = {
+    "cornell_pm": ("cornell_box", 8, 8, 64, 0.0963, 0.01),
+    "spheres_pm": ("material_spheres", 8, 8, 48, 0.0963, 0.01),
+    "medium_pm": ("medium_scene", 8, 8, 48, 0.0963, 0.01),
+}
+
+
+def pm_scene(scene_fn: str, step: float):
+    sc = render_scene(scene_fn)
+    for o in sc.objects:
+        if o.material.kind == scenes.VPM:
+            o.material.step_size = step
+    return sc
+
+
+def make_pm_goldens(ref_pm: str):
+    for case, (scene_fn, depth, iters, runs, r0, step) in PM_CASES.items():
+        if not _selected(case):
+            continue
+        sc = pm_scene(scene_fn, step)
+        f = sc.flatten()
+        imgs = []
+        secs = 0.0
+        with tempfile.TemporaryDirectory() as td:
+            cfg = sceneio.write_config(sc, td, "PM", depth, radius=r0)
+            for run in range(runs):
+                pre = os.path.join(td, f"out{run}")
+                out = subprocess.run([ref_pm, cfg, str(iters), str(run), str(r0), pre, "8"], check=True,
+                                     capture_output=True, text=True, cwd=td).stdout.strip().splitlines()[-1].split()
+                secs += float(out[-1])
+                imgs.append(np.fromfile(pre + ".img.f64").reshape(sc.camera.height, sc.camera.width, 3))
+        imgs = np.array(imgs)
+        mean = imgs.mean(axis=0)
+        stderr = imgs.std(axis=0, ddof=1) / np.sqrt(runs)
+        path = os.path.join(HERE, f"render_{case}.npz")
+        np.savez_compressed(path, mean=mean.astype(np.float32), stderr=stderr.astype(np.float32),
+                            runs=np.int64(runs), iterations=np.int64(iters), max_depth=np.int64(depth),
+                            radius=np.float64(r0), step_size=np.float64(step), scene=np.array(scene_fn),
+                            seconds=np.float64(secs), geometry_sha256=np.array(geometry_hash(f["verts"], f["tris"])))
+        print(f"{path}: {runs} x {iters} iterations, mean {mean.mean(axis=(0, 1))}, {secs:.1f} s", flush=True)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref = args[0] if args else "/root/reference"
@@ -224,10 +268,14 @@ def main():
     if "--bpt-only" in sys.argv:
         make_bpt_goldens(os.path.join(ROOT, "oracle", "_ref", "bpt_driver"))
         return
+    if "--pm-only" in sys.argv:
+        make_pm_goldens(os.path.join(ROOT, "oracle", "_ref", "pm_driver"))
+        return
     if "--vcm-only" not in sys.argv:
         make_render_goldens(os.path.join(ROOT, "oracle", "_ref", "pt_driver"))
     make_vcm_goldens(os.path.join(ROOT, "oracle", "_ref", "vcm_driver"))
     make_bpt_goldens(os.path.join(ROOT, "oracle", "_ref", "bpt_driver"))
+    make_pm_goldens(os.path.join(ROOT, "oracle", "_ref", "pm_driver"))
     if "--render-only" in sys.argv or "--vcm-only" in sys.argv:
         return
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "hit_driver")

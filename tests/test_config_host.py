@@ -11,7 +11,7 @@ import pytest
 import renderx_gb300 as rx
 from renderx_gb300 import build, film, scenes, sceneio
 
-FIELDS = ("tri_begin", "tri_count", "material", "has_vertex_normals", "coeff", "ior", "g")
+FIELDS = ("tri_begin", "tri_count", "material", "has_vertex_normals", "coeff", "ior", "g", "step_size")
 VECS = ("color", "diffuse_color", "sigma_s", "sigma_a", "decay")
 
 
@@ -39,6 +39,8 @@ def test_config_round_trip_is_exact(tmp_path, name):
             if k == "coeff" and b.material not in (scenes.GLOSSY, scenes.PHONG):
                 continue
             if k in ("ior", "g") and b.material not in (scenes.REFRACTIVE, scenes.REFLECTIVE, scenes.VPM):
+                continue
+            if k == "step_size" and b.material != scenes.VPM:
                 continue
             assert getattr(a, k) == pytest.approx(getattr(b, k), rel=1e-7), (k, b.material)
         for k in VECS:
@@ -148,7 +150,8 @@ def test_cli_usage():
 
 
 @pytest.mark.parametrize("type_name,code", [("PathTracer", 0), ("PT", 0), ("PTtest", 1), ("VCMTracer", 2), ("VCM", 2),
-                                            ("BidirectionalPathTracer", 3), ("BPT", 3), ("IPT", -1)])
+                                            ("BidirectionalPathTracer", 3), ("BPT", 3), ("PhotonMap", 4), ("PM", 4),
+                                            ("IPT", -1)])
 def test_renderer_type_names(tmp_path, type_name, code):
     # ConfigManager.cpp:323-354: the <Renderer><type> names and the renderer each selects
     sc = scenes.cornell_box(8, 8)
