@@ -296,6 +296,27 @@ def section_bpt(spp: int = 4, res: int = 512):
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
+def section_pm(iters: int = 2, res: int = 512, step: float = 0.01):
+    """PhotonMap on the VCM scene (Cornell room + homogeneous-medium sphere, medium
+    ray-marching step `step`) at res^2, depth 16, W x H photon paths per iteration, base
+    radius 0.0963."""
+    import renderx_gb300 as rx
+    from renderx_gb300 import scenes
+    sc = scenes.medium_scene(res, res)
+    for o in sc.objects:
+        if o.material.kind == scenes.VPM:
+            o.material.step_size = step
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ctx.render_pm(sc.camera, 1, 0.0963, max_depth=16, seed=1)
+        img, st = ctx.render_pm(sc.camera, iters, 0.0963, max_depth=16, seed=2)
+    return {"workload": f"PhotonMap, Cornell room + homogeneous-medium sphere (step {step}), {res}x{res}, depth 16, "
+                        f"{res * res} photon paths/iter, r0 0.0963",
+            "iterations": iters, "ms": st["ms"], "ms_per_iteration": st["ms"] / iters,
+            "photons_per_iteration": st["photons"] // iters, "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
+
+
 def cpu_baseline(f, o, d, budget_s: float = 12.0):
     """Times the oracle (CPU restatement of the reference traversal) on a bounded
     sample of the batch with every host thread."""
@@ -422,6 +443,7 @@ def run_ours(args):
                                ("vcm", args.skip_vcm,
                                 lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths)),
                                ("bpt", args.skip_bpt, lambda: section_bpt()),
+                               ("pm", args.skip_pm, lambda: section_pm()),
                                ("batch", args.skip_batch, lambda: section_batch(args.batch_scenes))):
             if skip:
                 continue
@@ -505,6 +527,7 @@ def main():
     ap.add_argument("--skip-mlp", action="store_true")
     ap.add_argument("--skip-guiding", action="store_true")
     ap.add_argument("--skip-bpt", action="store_true")
+    ap.add_argument("--skip-pm", action="store_true")
     ap.add_argument("--skip-vcm", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64)
@@ -520,7 +543,7 @@ def main():
     args = ap.parse_args()
     globals()["N_RAYS"] = args.rays
     if args.skip_extra:
-        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = args.skip_bpt = True
+        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = args.skip_bpt = args.skip_pm = True
     if args.impl == "reference":
         run_reference(args)
     else:
