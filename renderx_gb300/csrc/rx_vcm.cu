@@ -1211,23 +1211,89 @@ __global__ void k_pm_box_init(int* box) {
 }
 __global__ void k_pm_box(const float4* pos, const unsigned* n_photons, unsigned cap, int* box) {
   unsigned n = min(*n_photons, cap);
+  int m[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) m[k] = (k % 6) < 3 ? INT_MAX : INT_MIN;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 q = pos[i];
-    int* b = box + 6 * (int)__float_as_uint(q.w);
-    atomicMin(b + 0, ordered(q.x));
-    atomicMin(b + 1, ordered(q.y));
-    atomicMin(b + 2, ordered(q.z));
-    atomicMax(b + 3, ordered(q.x));
-    atomicMax(b + 4, ordered(q.y));
-    atomicMax(b + 5, ordered(q.z));
+    const float4 q = pos[i];
+    const int t = __float_as_uint(q.w) == kInVol ? 6 : 0;
+    const int v[3] = {ordered(q.x), ordered(q.y), ordered(q.z)};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {  // per type, unrolled so that m stays in registers
+      if (t == 0) {
+        m[k] = min(m[k], v[k]);
+        m[3 + k] = max(m[3 + k], v[k]);
+      } else {
+        m[6 + k] = min(m[6 + k], v[k]);
+        m[9 + k] = max(m[9 + k], v[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const int w = __shfl_xor_sync(0xffffffffu, m[k], o);
+      m[k] = (k % 6) < 3 ? min(m[k], w) : max(m[k], w);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if ((k % 6) < 3) atomicMin(box + k, m[k]);
+      else atomicMax(box + k, m[k]);
+    }
   }
 }
 
 // The density estimate at x of the photons of one type (Photonmap.cpp:211-259), for the
-// out ray `out` (the eye side). Lanes of a warp split the photons when `coop`, else one
-// lane does the whole query.
+// out ray `out` (the eye side), by the whole warp: lane j hashes the j-th cell the sphere
+// touches (as merge_buckets), equal buckets are walked once (by their lowest lane), and
+// the lanes split each bucket's photons. Every lane returns its partial sum.
 __device__ F3 pm_gather(const DevScene& S, const CamDev& cam, const Grid& G, const float4* pdata, const int* box,
-                        F3 x, const PV& out, uint32_t type, float r, float nph, bool coop, int lane) {
+                        F3 x, const PV& out, uint32_t type, float r, float nph, int lane) {
+  const int* b = box + 6 * type;
+  if (x.x < unordered(b[0]) || x.y < unordered(b[1]) || x.z < unordered(b[2]) || x.x > unordered(b[3]) ||
+      x.y > unordered(b[4]) || x.z > unordered(b[5]))
+    return F3{0, 0, 0};
+  const int x0 = (int)floorf((x.x - r) / G.cell), y0 = (int)floorf((x.y - r) / G.cell);
+  const int z0 = (int)floorf((x.z - r) / G.cell);
+  const int nx = min((int)floorf((x.x + r) / G.cell), x0 + 2) - x0 + 1;
+  const int ny = min((int)floorf((x.y + r) / G.cell), y0 + 2) - y0 + 1;
+  const int nz = min((int)floorf((x.z + r) / G.cell), z0 + 2) - z0 + 1;
+  const bool cell_lane = lane < nx * ny * nz;
+  unsigned bucket = 0xffffffffu, b0 = 0, b1 = 0;
+  if (cell_lane) bucket = cell_hash(x0 + lane / (nz * ny), y0 + (lane / nz) % ny, z0 + lane % nz, G.mask);
+  const unsigned peers = __match_any_sync(0xffffffffu, bucket);
+  const bool leader = cell_lane && (unsigned)(__ffs(peers) - 1) == (unsigned)lane;
+  if (leader) {
+    b0 = G.start[bucket];
+    b1 = G.start[bucket + 1];
+  }
+  F3 contrib = {0, 0, 0};
+  const float r2 = r * r;
+  const float norm = type == kInVol ? nph * r * r * r : nph * r * r;
+  for (unsigned lead = __ballot_sync(0xffffffffu, leader && b1 > b0); lead; lead &= lead - 1) {
+    const int src = __ffs(lead) - 1;
+    const unsigned r0 = __shfl_sync(0xffffffffu, b0, src), r1 = __shfl_sync(0xffffffffu, b1, src);
+    for (unsigned i = r0 + (unsigned)lane; i < r1; i += 32) {
+      const float4 q = G.pos[i];
+      if (__float_as_uint(q.w) != type) continue;
+      const float dist = length(x - f3(q));
+      const float d2 = dist * dist;
+      if (!(d2 <= r2)) continue;
+      const float4* pd = pdata + (size_t)kPmData * i;
+      const PV ray = load_pv(pd);
+      const F3 color = f3(pd[4]) * bsdf_of(S, cam, ray, out);
+      if (lum(color) < 1e-6f) continue;
+      const float sk = fmaxf(0.0f, 1.0f - d2 / r2);
+      const float kernel = 3.0f * sk * sk / RX_PI;
+      contrib = contrib + color * (kernel / norm);
+    }
+  }
+  return contrib;
+}
+
+// The same estimate by one lane alone (the medium gathers, one ray-marching step per
+// lane: their spheres hold few photons each).
+__device__ F3 pm_gather_lane(const DevScene& S, const CamDev& cam, const Grid& G, const float4* pdata, const int* box,
+                             F3 x, const PV& out, uint32_t type, float r, float nph) {
   const int* b = box + 6 * type;
   if (x.x < unordered(b[0]) || x.y < unordered(b[1]) || x.z < unordered(b[2]) || x.x > unordered(b[3]) ||
       x.y > unordered(b[4]) || x.z > unordered(b[5]))
@@ -1236,7 +1302,7 @@ __device__ F3 pm_gather(const DevScene& S, const CamDev& cam, const Grid& G, con
   const float r2 = r * r;
   const float norm = type == kInVol ? nph * r * r * r : nph * r * r;
   merge_buckets(G, x, r, [&](unsigned b0, unsigned b1) {
-    for (unsigned i = b0 + (coop ? (unsigned)lane : 0u); i < b1; i += coop ? 32u : 1u) {
+    for (unsigned i = b0; i < b1; i++) {
       const float4 q = G.pos[i];
       if (__float_as_uint(q.w) != type) continue;
       const float dist = length(x - f3(q));
@@ -1255,8 +1321,8 @@ __device__ F3 pm_gather(const DevScene& S, const CamDev& cam, const Grid& G, con
 }
 
 // One warp per pixel: lane 0 samples the eye merge path into shared memory, then the
-// lanes share the ray-marching steps of each medium segment and the photons of the
-// surface gather.
+// lanes share the ray-marching steps of each medium segment (one gather per lane) and
+// split the photons of the gather at the first random surface vertex.
 __global__ void __launch_bounds__(128) k_pm_eye(DevScene S, VcmParams P, Grid G, const float4* pdata, const int* box,
                                                 float* img, unsigned long long* rays) {
   __shared__ float4 paths[4][kPmMaxV * 4];
@@ -1323,13 +1389,12 @@ __global__ void __launch_bounds__(128) k_pm_eye(DevScene S, VcmParams P, Grid G,
         if (lane == 0) u = rng.next();
         const float offset = step * __shfl_sync(0xffffffffu, u, 0);
         Tr = Tr * decay_of(S, a.inside, offset);
-        for (int j = lane; j < N; j += 32) {
-          const float t = offset + step * (float)j;
+        for (int j = lane; j < N; j += 32) {  // one step per lane; Tr after step j in closed form
           PV out = a;
           out.d = -a.d;
-          out.o = a.o + a.d * t;
+          out.o = a.o + a.d * (offset + step * (float)j);
           out.contact = kNone;
-          const F3 c = pm_gather(S, P.cam, G, pdata, box, out.o, out, kInVol, r, P.norm, false, lane);
+          const F3 c = pm_gather_lane(S, P.cam, G, pdata, box, out.o, out, kInVol, r, P.norm);
           vol = vol + c * (Tr * decay_of(S, a.inside, step * (float)(j + 1))) * step;
         }
         Tr = Tr * decay_of(S, a.inside, step * (float)N);
@@ -1344,7 +1409,7 @@ __global__ void __launch_bounds__(128) k_pm_eye(DevScene S, VcmParams P, Grid G,
         if (is_vpm(S, b.contact)) continue;
         PV out = b;
         out.d = -a.d;
-        surf = pm_gather(S, P.cam, G, pdata, box, b.o, out, kOutVol, r, P.norm, true, lane);
+        surf = pm_gather(S, P.cam, G, pdata, box, b.o, out, kOutVol, r, P.norm, lane);
         break;
       }
     }
