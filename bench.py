@@ -221,13 +221,14 @@ def section_mlp(ctx, peak_tflops):
                          "frac": f_train / peak_tflops, "kernel": "k_guide_train (forward + backward, BF16 tcgen05)"}}
 
 
-def section_batch(n: int = 64):
+def section_batch(n: int = 64, small: bool = False):
     """C3: n seeded sphere-field variants in one wavefront (graph replay, autotuned launch
-    shape) against rendering them one after another."""
+    shape) against rendering them one after another. `small`: the same scenes at 128^2
+    and 4 spp, where no single render fills the GPU."""
     import renderx_gb300 as rx
     from renderx_gb300 import scenes
     t0 = time.perf_counter()
-    variants = scenes.batch_variants(n)
+    variants = scenes.batch_variants(n, resolutions=(128,), spp_range=(4, 4)) if small else scenes.batch_variants(n)
     gen_s = time.perf_counter() - t0
     ctxs = []
     try:
@@ -252,8 +253,9 @@ def section_batch(n: int = 64):
         for c in ctxs:
             c.close()
     rays = st["extension_rays"] + st["shadow_rays"]
-    return {"workload": f"{n} sphere-field variants, {tris} triangles in all (1k-2M each), 128^2-1024^2, "
-                        "4-64 spp, depth 16, 8 with the homogeneous medium",
+    return {"workload": f"{n} sphere-field variants, {tris} triangles in all (1k-2M each), "
+                        + ("128^2, 4 spp" if small else "128^2-1024^2, 4-64 spp")
+                        + ", depth 16, 8 with the homogeneous medium",
             "paths": st["paths"], "ms": st["ms"], "mrays_per_s": rays / st["ms"] / 1e3,
             "samples_per_s": st["paths"] / st["ms"] * 1e3, "chosen_blocks_per_sm": st["blocks_per_sm"],
             "chosen_stack": st["stack"], "one_by_one_ms": seq_ms,
@@ -444,7 +446,8 @@ def run_ours(args):
                                 lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths)),
                                ("bpt", args.skip_bpt, lambda: section_bpt()),
                                ("pm", args.skip_pm, lambda: section_pm()),
-                               ("batch", args.skip_batch, lambda: section_batch(args.batch_scenes))):
+                               ("batch", args.skip_batch, lambda: section_batch(args.batch_scenes)),
+                               ("batch_small", args.skip_batch, lambda: section_batch(args.batch_scenes, True))):
             if skip:
                 continue
             t0 = time.perf_counter()

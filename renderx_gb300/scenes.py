@@ -303,12 +303,13 @@ def guiding_scene(width: int = 1024, height: int = 1024, n_spheres: int = 200, s
                         glossy_exp=(100.0, 1000.0), light_scale=GUIDING_LIGHT_SCALE)
 
 
-def batch_variants(n: int = 64, seed: int = 1, n_medium: int = 8):
+def batch_variants(n: int = 64, seed: int = 1, n_medium: int = 8, resolutions=(128, 256, 512, 1024),
+                   spp_range=(4, 64)):
     """The batching workload: ``n`` seeded variants of the sphere field. Triangle counts
     log-U[1k, 2M] (sphere subdivision 2..5 and sphere count chosen to match),
-    resolution drawn from {128, 256, 512, 1024}^2, spp U{4..64}, depth cap 16, Russian
-    roulette from depth 3; the first ``n_medium`` carry the homogeneous-medium sphere of
-    ``medium_scene``. Returns a list of (Scene, options dict)."""
+    resolution drawn from ``resolutions`` (squared), spp U{spp_range}, depth cap 16,
+    Russian roulette from depth 3; the first ``n_medium`` carry the homogeneous-medium
+    sphere of ``medium_scene``. Returns a list of (Scene, options dict)."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n):
@@ -317,8 +318,8 @@ def batch_variants(n: int = 64, seed: int = 1, n_medium: int = 8):
         while d > 2 and 20 * 4 ** d * 4 > target:
             d -= 1
         ns = int(max(1, min(400, round((target - 36) / (20 * 4 ** d)))))
-        res = int(rng.choice([128, 256, 512, 1024]))
-        spp = int(rng.integers(4, 65))
+        res = int(rng.choice(list(resolutions)))
+        spp = int(rng.integers(spp_range[0], spp_range[1] + 1))
         sc = sphere_field(ns, d, seed=1000 + k, width=res, height=res)
         if k < n_medium:
             med = medium_scene(res, res).objects[-1]

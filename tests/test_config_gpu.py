@@ -49,3 +49,19 @@ def test_cli_renders_config(tmp_path):
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert np.isfinite(film.load_pfm(str(tmp_path / "v.pfm"))).all()
+    # BidirectionalPathTracer and PhotonMap through the same front end, equal to the API's renders
+    for typ, args, fn in (("BPT", ["--spp", "4"], lambda c: c.render_bpt(sc.camera, 4, max_depth=8, seed=1)[0]),
+                          ("PM", ["--iterations", "2"],
+                           lambda c: c.render_pm(sc.camera, 2, 0.05, max_depth=8, seed=1)[0])):
+        d = tmp_path / typ
+        cfg3 = sceneio.write_config(sc, str(d), typ, 8, radius=0.05)
+        r = subprocess.run([build.CLI, cfg3, *args, "--out", str(d / "img.pfm")], capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        img3 = film.load_pfm(str(d / "img.pfm"))
+        with rx.Context(0) as c:
+            c.set_scene(sc)
+            c.build_accel()
+            want = fn(c)
+        assert img3.mean() > 0
+        assert np.allclose(img3, want.astype(np.float32), rtol=2e-3, atol=1e-5), typ
