@@ -124,72 +124,80 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
     }
     if (!__any_sync(FULL, active)) break;
 
-    if (active) {
-      int pl = DONE, pcnt = 0;  // the next leaf to test
-      while (true) {
-        if (cur >= 0) {
-          const float4* np = A.bvh4 + 8 * (size_t)cur;
-          float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-          float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
-          int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
-          const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-          const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-          const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
-          int r[4] = {cr.x, cr.y, cr.z, cr.w}, c[4] = {cc.x, cc.y, cc.z, cc.w};
-          float tn[4];
-          int nh = 0;
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            float a0 = fmaf(lxa[j], inv.x, -ood.x), b0 = fmaf(hxa[j], inv.x, -ood.x);
-            float a1 = fmaf(lya[j], inv.y, -ood.y), b1 = fmaf(hya[j], inv.y, -ood.y);
-            float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
-            float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
-            float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tlimit));
-            bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
-            tn[j] = h ? t0 : INFINITY;
-            nh += h ? 1 : 0;
-          }
-          // sorting network on registers (ties keep child order): near to far
-          auto cs = [&](int a, int b) {
-            if (tn[b] < tn[a]) {
-              float t = tn[a];
-              tn[a] = tn[b];
-              tn[b] = t;
-              int q = r[a];
-              r[a] = r[b];
-              r[b] = q;
-              q = c[a];
-              c[a] = c[b];
-              c[b] = q;
-            }
-          };
-          cs(0, 1);
-          cs(2, 3);
-          cs(0, 2);
-          cs(1, 3);
-          cs(1, 2);
-          if (nh == 0) {
-            cur = pop();
-          } else {
-#pragma unroll
-            for (int k = 3; k >= 1; k--) {  // farthest first, so the nearer pop earlier
-              if (k < nh && sp < kStack4) {
-                stack_ref[sp] = pack(r[k], c[k]);
-                stack_tn[sp] = tn[k];
-                sp++;
-              }
-            }
-            cur = r[0];
-            cnt = c[0];
-          }
-        } else if (cur != DONE) {
-          pl = cur;
-          pcnt = cnt;
-          cur = pop();
-          break;
-        }
-        if (cur == DONE) break;
+    // Traversal steps, warp-uniform: a lane without a leaf to test walks until it finds
+    // one; meanwhile a lane that already holds one keeps walking inner nodes (its leaf
+    // postponed, as in Aila and Laine's speculative traversal), so fewer lanes idle. A
+    // lane stops when it reaches a second leaf. Pruning uses the limit before the
+    // postponed leaf, which only visits more candidates, never fewer.
+    int pl = DONE, pcnt = 0;  // the next leaf to test
+    while (true) {
+      const bool need = active && pl == DONE && cur != DONE;
+      if (!__any_sync(FULL, need)) break;
+      if (!(need || (active && cur >= 0))) continue;
+      if (cur < 0) {  // a leaf (only lanes that need one get here)
+        pl = cur;
+        pcnt = cnt;
+        cur = pop();
+        continue;
       }
+      {
+        const float4* np = A.bvh4 + 8 * (size_t)cur;
+        float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+        float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+        int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
+        const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+        const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+        const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+        int r[4] = {cr.x, cr.y, cr.z, cr.w}, c[4] = {cc.x, cc.y, cc.z, cc.w};
+        float tn[4];
+        int nh = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          float a0 = fmaf(lxa[j], inv.x, -ood.x), b0 = fmaf(hxa[j], inv.x, -ood.x);
+          float a1 = fmaf(lya[j], inv.y, -ood.y), b1 = fmaf(hya[j], inv.y, -ood.y);
+          float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
+          float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
+          float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tlimit));
+          bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
+          tn[j] = h ? t0 : INFINITY;
+          nh += h ? 1 : 0;
+        }
+        // sorting network on registers (ties keep child order): near to far
+        auto cs = [&](int a, int b) {
+          if (tn[b] < tn[a]) {
+            float t = tn[a];
+            tn[a] = tn[b];
+            tn[b] = t;
+            int q = r[a];
+            r[a] = r[b];
+            r[b] = q;
+            q = c[a];
+            c[a] = c[b];
+            c[b] = q;
+          }
+        };
+        cs(0, 1);
+        cs(2, 3);
+        cs(0, 2);
+        cs(1, 3);
+        cs(1, 2);
+        if (nh == 0) {
+          cur = pop();
+        } else {
+#pragma unroll
+          for (int k = 3; k >= 1; k--) {  // farthest first, so the nearer pop earlier
+            if (k < nh && sp < kStack4) {
+              stack_ref[sp] = pack(r[k], c[k]);
+              stack_tn[sp] = tn[k];
+              sp++;
+            }
+          }
+          cur = r[0];
+          cnt = c[0];
+        }
+      }
+    }
+    if (active) {
       if (pl != DONE) {
         int first = ~pl;
         for (int k = 0; k < pcnt; k++) {
