@@ -556,15 +556,17 @@ __global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t 
 // normalisation by the sum.
 //
 // A CTA carries kTrainTiles tiles of 128 samples at once, one warpgroup per tile (thread
-// s of warpgroup g owns sample s of tile g, TMEM lane s of that tile's accumulator).
-// One thread issues every MMA, so the shared weight-gradient accumulators see each
-// tile's contribution in order, and one warpgroup's epilogue overlaps the other tile's
-// MMAs. The 128 x 80 input tile is not kept: it lives in the region of activations 3-4
+// s of warpgroup g owns sample s of tile g, TMEM lane s of that tile's accumulator). The
+// warpgroups run independently (own MMA-issuing thread, mbarrier and named barrier), so
+// one tile's epilogues overlap the other's MMAs; both add into the shared
+// weight-gradient accumulators, zeroed once, which the tensor core updates one MMA at a
+// time. The 128 x 80 input tile is not kept: it lives in the region of activations 3-4
 // during the forward pass and is encoded again from the records for the last weight
 // gradient.
 constexpr int kTrainTiles = 2;
 constexpr uint32_t kTrainTileBytes = 5 * kActBytes;  // A1, A2, A3|A4 (A0 alias), dZ
 constexpr uint32_t kSmTrain2 = kImgBytes + kTrainTiles * kTrainTileBytes;
+constexpr uint32_t kDwCols = 336;  // TMEM columns of the five weight-gradient accumulators
 
 __device__ __forceinline__ void load_record(const float* recs, uint32_t i, float (&q)[9], float (&wi)[3], float& w) {
   const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
@@ -585,8 +587,8 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
   uint32_t first, end;
   train_window(count, n_host, first0, len, step, first, end);
   const uint32_t n = end - first;
-  const uint32_t ngroups = (n + kTile * kTrainTiles - 1) / (kTile * kTrainTiles);
-  if (blockIdx.x >= ngroups) return;
+  const uint32_t ntiles = (n + kTile - 1) / kTile;
+  if (blockIdx.x * kTrainTiles >= ntiles) return;
   if (tid == 0) {
     for (int k = 0; k < kTrainTiles; k++) tc::mbar_init(&bar_mma[k], 1);
     tc::mbar_init(&bar_w, 1);
@@ -600,30 +602,28 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
   const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
   // TMEM columns: per tile one 64-column accumulator (forward, then dA); the shared dW
   const uint32_t t_dw[5] = {T0 + 128, T0 + 208, T0 + 272, T0 + 336, T0 + 400};
-  unsigned char* tile_base[kTrainTiles];
-  for (int k = 0; k < kTrainTiles; k++) tile_base[k] = sm + kImgBytes + k * kTrainTileBytes;
-  // this warpgroup's buffers
-  unsigned char* A1 = tile_base[g];
+  if (g == 0) {  // zero the weight-gradient accumulators (every MMA into them accumulates)
+    const float z[16] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t c0 = 0; c0 < kDwCols; c0 += 16) tc::tmem_st16(T0 + 128 + lane_off + c0, z);
+  }
+  unsigned char* A1 = sm + kImgBytes + (uint32_t)g * kTrainTileBytes;  // this warpgroup's buffers
   unsigned char* A2 = A1 + kActBytes;
   unsigned char* A34 = A1 + 2 * kActBytes;  // A3, A4; A0 (20 KB) aliases it
   unsigned char* dZ = A1 + 4 * kActBytes;
   unsigned char* Al[5] = {A34, A1, A2, A34, A34 + kActBytes};
-  const uint32_t t_acc = T0 + 64u * (uint32_t)g + lane_off;
+  const uint32_t tacc_col = T0 + 64u * (uint32_t)g;
+  const uint32_t t_acc = tacc_col + lane_off;
   const float total = wsum[0], cnt = fmaxf(wsum[1], 1.0f);
   const float wclip = 32.0f * total / cnt;
   const float inv_total = total > 0.0f ? 1.0f / total : 0.0f;
+  tc::tc_fence_before();
   bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0));
+  tc::tc_fence_after();
   uint32_t ph = 0;
-  bool first_group = true;
   float loss = 0.0f;
-  // operand pointers of tile k's layer l (for the issuing thread)
-  auto act = [&](int k, int l) -> unsigned char* {
-    unsigned char* b = tile_base[k];
-    return l == 0 ? b + 2 * kActBytes : l == 1 ? b : l == 2 ? b + kActBytes : l == 3 ? b + 2 * kActBytes
-                                                                                      : b + 3 * kActBytes;
-  };
-  for (uint32_t grp = blockIdx.x; ok && grp < ngroups; grp += gridDim.x) {
-    const uint32_t i = first + (grp * kTrainTiles + g) * kTile + s;
+  for (uint32_t tile = blockIdx.x * kTrainTiles + (uint32_t)g; ok && tile < ntiles;
+       tile += gridDim.x * kTrainTiles) {
+    const uint32_t i = first + tile * kTile + s;
     const bool valid = i < end;
     float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0}, w = 0.0f;
     if (valid) {
@@ -631,76 +631,69 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
       w = fminf(w, wclip) * inv_total;
     }
     encode_row(q, valid, box, Al[0], s);
-    tc_sync();
-    // forward: layer l of every tile, then every warpgroup's epilogue
+    wg_sync(g);
+    // forward
     for (int l = 0; l < 5 && ok; l++) {
-      if (tid == 0) {
-        for (int k = 0; k < kTrainTiles; k++) {
-          issue_fwd(T0 + 64u * k, act(k, l), sm + kSmW + layer_img(l), layer_k(l));
-          tc::mma_commit(&bar_mma[k]);
-        }
+      if (s == 0) {
+        issue_fwd(tacc_col, Al[l], sm + kSmW + layer_img(l), layer_k(l));
+        tc::mma_commit(&bar_mma[g]);
       }
-      ok = tc::mbar_wait(&bar_mma[g], ph);
-      tc::tc_fence_after();
-      if (ok) {
-        if (l < 4) {
-          epi_relu(t_acc, Al[l + 1], s);
-        } else {
-          float raw[48], dz[48];
-          load_raw(t_acc, raw);
-          if (valid && w > 0.0f) {
-            loss += mix_loss_grad(raw, wi, w, dz);
-          } else {
-#pragma unroll
-            for (int k = 0; k < 48; k++) dz[k] = 0.0f;
-          }
-#pragma unroll
-          for (int c0 = 0; c0 < 64; c0 += 8) {
-            float f[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++) f[k] = c0 + k < 48 ? dz[c0 + k] : 0.0f;
-            store_chunk(dZ, tc::core_off(s, c0, kOut), f);
-          }
-        }
-      }
-      ok = __syncthreads_and(ok);
+      ok = wg_and(g, tc::mbar_wait(&bar_mma[g], ph));
       ph ^= 1;
-      tc::fence_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
       tc::tc_fence_after();
+      if (!ok) break;
+      if (l < 4) {
+        epi_relu(t_acc, Al[l + 1], s);
+      } else {
+        float raw[48], dz[48];
+        load_raw(t_acc, raw);
+        if (valid && w > 0.0f) {
+          loss += mix_loss_grad(raw, wi, w, dz);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 48; k++) dz[k] = 0.0f;
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 8) {
+          float f[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) f[k] = c0 + k < 48 ? dz[c0 + k] : 0.0f;
+          store_chunk(dZ, tc::core_off(s, c0, kOut), f);
+        }
+      }
+      wg_sync(g);
     }
-    // backward: dZ holds dZ_{l+1}; dW_l += dZ^T A_l over both tiles; dA_l = dZ W_l
+    // backward: dZ holds dZ_{l+1}; dW_l += dZ^T A_l; dA_l = dZ W_l
     for (int l = 4; l >= 0 && ok; l--) {
       const int K = layer_k(l);
       if (l == 0) {  // the input tile again, into the (now free) activation 3-4 region
         encode_row(q, valid, box, Al[0], s);
-        tc_sync();
+        wg_sync(g);
       }
-      if (tid == 0) {
+      if (s == 0) {
         const uint32_t w0 = tc::smem_u32(sm + kSmW + layer_img(l));
         const uint32_t id_w = tc::idesc_bf16(64, (uint32_t)K, true, true);
         const uint32_t id_a = tc::idesc_bf16(128, (uint32_t)K, false, true);
-        for (int k = 0; k < kTrainTiles; k++) {
-          const uint32_t dz0 = tc::smem_u32(tile_base[k] + 4 * kActBytes), a0 = tc::smem_u32(act(k, l));
-          for (int s0 = 0; s0 < kTile; s0 += 16) {
-            uint64_t ad = tc::sdesc(dz0 + tc::core_off(s0, 0, kOut), (kOut >> 3) * 128u, 128u);
-            uint64_t bd = tc::sdesc(a0 + tc::core_off(s0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
-            tc::mma_bf16(t_dw[l], ad, bd, id_w, (first_group && k == 0 && s0 == 0) ? 0u : 1u);
-          }
-          if (l > 0) {
-            for (int n0 = 0; n0 < kOut; n0 += 16) {
-              uint64_t ad = tc::sdesc(dz0 + tc::core_off(0, n0, kOut), 128u, (kOut >> 3) * 128u);
-              uint64_t bd = tc::sdesc(w0 + tc::core_off(n0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
-              tc::mma_bf16(T0 + 64u * k, ad, bd, id_a, n0 > 0);
-            }
-          }
-          tc::mma_commit(&bar_mma[k]);
+        const uint32_t dz0 = tc::smem_u32(dZ), a0 = tc::smem_u32(Al[l]);
+        for (int s0 = 0; s0 < kTile; s0 += 16) {
+          uint64_t ad = tc::sdesc(dz0 + tc::core_off(s0, 0, kOut), (kOut >> 3) * 128u, 128u);
+          uint64_t bd = tc::sdesc(a0 + tc::core_off(s0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
+          tc::mma_bf16(t_dw[l], ad, bd, id_w, 1u);
         }
+        if (l > 0) {
+          for (int n0 = 0; n0 < kOut; n0 += 16) {
+            uint64_t ad = tc::sdesc(dz0 + tc::core_off(0, n0, kOut), 128u, (kOut >> 3) * 128u);
+            uint64_t bd = tc::sdesc(w0 + tc::core_off(n0, 0, K), (uint32_t)(K >> 3) * 128u, 128u);
+            tc::mma_bf16(tacc_col, ad, bd, id_a, n0 > 0);
+          }
+        }
+        tc::mma_commit(&bar_mma[g]);
       }
-      ok = tc::mbar_wait(&bar_mma[g], ph);
+      ok = wg_and(g, tc::mbar_wait(&bar_mma[g], ph));
+      ph ^= 1;
       tc::tc_fence_after();
-      if (ok && l > 0) {
+      if (!ok) break;
+      if (l > 0) {
 #pragma unroll
         for (int c0 = 0; c0 < kHid; c0 += 16) {
           float v[16];
@@ -720,17 +713,14 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
           store_chunk(dZ, tc::core_off(s, c0 + 8, kHid), b);
         }
       }
-      ok = __syncthreads_and(ok);
-      ph ^= 1;
-      tc::fence_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
-      tc::tc_fence_after();
+      wg_sync(g);
     }
-    first_group = false;
   }
+  tc::tc_fence_before();
+  ok = __syncthreads_and(ok);
+  tc::tc_fence_after();
   // flush the weight-gradient accumulators (warpgroup 0 reads them)
-  if (ok && !first_group && g == 0) {
+  if (ok && g == 0) {
     const int row = m64_row(s);
     for (int l = 0; l < 5; l++) {
       const int K = layer_k(l);
