@@ -140,8 +140,10 @@ def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64):
     # algorithmic bytes: 40 per traced ray, 96 per shade event (path state read + write),
     # 24 per pixel for the FP64 film
     alg = 40 * rays + 96 * st["extension_rays"] + 24 * cam.width * cam.height
+    ref, _, _ = ctx.render_pt(cam, 8 * spp, max_depth=depth, rr_mode=1, seed=5)  # FP64 film, 8x the samples
     return {"workload": f"PathTracer {cam.width}x{cam.height} x {spp} spp, depth {depth}, "
                         "4,096,036 triangles", "ms": st["ms"], "mrays_per_s": rays / s / 1e6,
+            "relmse_vs_high_spp": _relmse(film, ref), "reference": f"the same PathTracer at {8 * spp} spp, FP64 film",
             "samples_per_s": st["paths"] / s, "extension_rays": st["extension_rays"],
             "shadow_rays": st["shadow_rays"], "image_mean": [float(x) for x in film.mean(axis=(0, 1))],
             "roofline": {"bound": "hbm", "achieved": alg / s / 1e9, "peak": peak, "unit": "GB/s",
@@ -273,9 +275,11 @@ def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
         ctx.build_accel()
         ctx.render_vcm(sc.camera, 1, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=1)
         img, st = ctx.render_vcm(sc.camera, iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=2)
+        ref, _ = ctx.render_vcm(sc.camera, 8 * iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=3)
     return {"workload": f"VCMTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, {light_paths} light "
                         "paths/iter, depth 16, r0 0.0963, alpha 0.75", "iterations": iters, "ms": st["ms"],
             "ms_per_iteration": st["ms"] / iters, "rays_per_iteration": st["rays"] // iters,
+            "relmse_vs_high_spp": _relmse(img, ref), "reference": f"the same VCMTracer over {8 * iters} iterations",
             "shadow_rays_per_iteration": st["shadow_rays"] // iters, "merges_per_iteration": st["merges"] // iters,
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
@@ -291,9 +295,11 @@ def section_bpt(spp: int = 4, res: int = 512):
         ctx.build_accel()
         ctx.render_bpt(sc.camera, 1, max_depth=16, seed=1)
         img, st = ctx.render_bpt(sc.camera, spp, max_depth=16, seed=2)
+        ref, _ = ctx.render_bpt(sc.camera, 16 * spp, max_depth=16, seed=3)
     rays = st["rays"] + st["shadow_rays"]
     return {"workload": f"BidirectionalPathTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, depth 16",
             "spp": spp, "ms": st["ms"], "ms_per_spp": st["ms"] / spp, "mrays_per_s": rays / (st["ms"] * 1e-3) / 1e6,
+            "relmse_vs_high_spp": _relmse(img, ref), "reference": f"the same BidirectionalPathTracer at {16 * spp} spp",
             "samples_per_s": st["paths"] / (st["ms"] * 1e-3), "shadow_rays_per_spp": st["shadow_rays"] // spp,
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
@@ -313,10 +319,12 @@ def section_pm(iters: int = 2, res: int = 512, step: float = 0.01):
         ctx.build_accel()
         ctx.render_pm(sc.camera, 1, 0.0963, max_depth=16, seed=1)
         img, st = ctx.render_pm(sc.camera, iters, 0.0963, max_depth=16, seed=2)
+        ref, _ = ctx.render_pm(sc.camera, 8 * iters, 0.0963, max_depth=16, seed=3)
     return {"workload": f"PhotonMap, Cornell room + homogeneous-medium sphere (step {step}), {res}x{res}, depth 16, "
                         f"{res * res} photon paths/iter, r0 0.0963",
             "iterations": iters, "ms": st["ms"], "ms_per_iteration": st["ms"] / iters,
-            "photons_per_iteration": st["photons"] // iters, "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
+            "photons_per_iteration": st["photons"] // iters, "relmse_vs_high_spp": _relmse(img, ref),
+            "reference": f"the same PhotonMap over {8 * iters} iterations", "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
 def cpu_baseline(f, o, d, budget_s: float = 12.0):
