@@ -240,20 +240,21 @@ __device__ void light_mis(const DevScene& S, const CamDev& cam, const float4* lb
   }
 }
 
-// Eye-subpath records for k = 0 .. n-1 (k >= 1 are merge vertices).
-__device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n, float r, float norm, bool merges,
+// Eye-subpath records for k = 0 .. n-1 (k >= 1 are merge vertices); e(k) gives vertex k.
+template <class Get>
+__device__ void eye_mis(const DevScene& S, const CamDev& cam, Get&& e, int n, float r, float norm, bool merges,
                         MisE* out) {
-  double pb = e[0].oprob, pb_prev = 0.0, u = 0.0;
+  double pb = e(0).oprob, pb_prev = 0.0, u = 0.0;
   F3 thr = {1, 1, 1};
   float prob = 1.0f;
   for (int k = 0; k < n; k++) {
-    const PV& v = e[k];
+    const PV v = e(k);
     MisE m;
     m.pb = pb;
     m.pbr = (float)(pb_prev / pb);
     m.sea = 0.0f;
     if (k >= 1) {
-      const PV& pe = e[k - 1];
+      const PV pe = e(k - 1);
       float d = seg_len(v, pe);
       double fe = cos_term(S, cam, pe);
       fe /= (double)d * d;
@@ -266,7 +267,7 @@ __device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n
     out[k] = m;
     if (k + 1 >= n) break;
     // advance to k + 1
-    const PV& up = e[k + 1];
+    const PV up = e(k + 1);
     float d = seg_len(v, up);
     thr = thr * v.c;
     thr = thr * decay_of(S, v.inside, d);
@@ -275,11 +276,11 @@ __device__ void eye_mis(const DevScene& S, const CamDev& cam, const PV* e, int n
     double pbn = pb * cos_term(S, cam, rev_to(up, v));
     pbn /= (double)d * d;
     if (rnd(v)) {
-      pbn *= k > 0 ? dir_pdf(S, cam, e[k - 1], v, false) : dir_pdf(S, cam, v, v, true);
+      pbn *= k > 0 ? dir_pdf(S, cam, e(k - 1), v, false) : dir_pdf(S, cam, v, v, true);
       pbn *= origin_pdf(S, v, up);
     }
     if (k >= 1) {
-      const PV& pe = e[k - 1];
+      const PV pe = e(k - 1);
       float dd = seg_len(v, pe);
       PV rv = rev_to(v, pe);
       double g = cos_term(S, cam, pe);
@@ -650,54 +651,68 @@ __device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
 // the s = 0 technique, and lists which vertices can take part in a connection (sampled
 // at random, not on an emitter past the light's own vertex); the (k, ci) pairs are then
 // evaluated one per lane with their shadow rays (k_conn_eval).
-__global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const float4* lv, const int* llen,
-                                                 float4* ev, int* elen, MisE* emis, uint2* cmask,
-                                                 unsigned long long* ccount, float* img, unsigned long long* rays) {
+__global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, float4* ev, int* elen,
+                                                 unsigned long long* rays) {
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nrays = 0;
-  const float r = P.radius;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += stride) {
     Rng rng(P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
-    PV eye[kMaxV];
     Hit3 h;
     PV start = camera_ray(S, P.cam, p, rng, h);
-    int ne = sample_path(S, P.cam, start, h, P.max_depth, !P.bpt, rng, [&](int i, const PV& v) { eye[i] = v; });
+    float4* out = ev + 4 * ((size_t)p * P.maxv);
+    int ne = sample_path(S, P.cam, start, h, P.max_depth, !P.bpt, rng,
+                         [&](int i, const PV& v) { store_pv(out + 4 * i, v); });
     nrays += (unsigned long long)ne;
-    for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
+  }
+  if (nrays) atomicAdd(rays, nrays);
+}
+
+// Per pixel, from its stored eye subpath: the records, the s = 0 technique (the eye
+// path ends on an emitter and the reference's mustUsePT holds: VCM, no interior vertex
+// sampled at random, weight pb[0] / (pb[0] + the two-vertex connection);
+// BidirectionalPathTracer, no two consecutive random vertices, weight pb[0] / pb[0]),
+// and the lists of eye and light vertices that can take part in a connection.
+__global__ void __launch_bounds__(128) k_eye_post(DevScene S, VcmParams P, const float4* lv, const int* llen,
+                                                  const float4* ev, const int* elen, MisE* emis, uint2* cmask,
+                                                  unsigned long long* ccount, float* img) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += gridDim.x * blockDim.x) {
+    const float4* eb = ev + 4 * ((size_t)p * P.maxv);
+    const int ne = elen[p];
     MisE* me = emis + (size_t)p * P.maxv;
-    eye_mis(S, P.cam, eye, ne, r, P.norm, !P.bpt, me);
-    // s = 0: the eye path ends on an emitter and the reference's mustUsePT holds: VCM, no
-    // interior vertex sampled at random (its weight pb[0] / (pb[0] + the two-vertex
-    // connection)); BidirectionalPathTracer, no two consecutive random vertices (then no
-    // connection technique exists and the weight is pb[0] / pb[0]).
+    eye_mis(S, P.cam, [&](int k) { return load_pv(eb + 4 * k); }, ne, P.radius, P.norm, !P.bpt, me);
     F3 acc = {0, 0, 0};
-    int first_rand = ne, first_pair = ne;
-    for (int m = ne - 1; m >= 1; m--)
-      if (rnd(eye[m])) first_rand = m;
-    for (int m = ne - 2; m >= 0; m--)
-      if (rnd(eye[m]) && rnd(eye[m + 1])) first_pair = m;
-    for (int t = 2; t <= ne; t++) {
-      if (P.bpt ? first_pair <= t - 2 : first_rand <= t - 2) break;
-      const PV& v = eye[t - 1];
-      if (!is_emissive(S, v.contact)) continue;
-      const MisE m = me[t - 1];
-      F3 col = v.c * m.thr;
-      float prob = (v.dprob * v.oprob) * m.prob;
-      if (!(prob > 0.0f) || !(length(col) > 0.0f)) continue;
-      float wt = m.pb > 0.0 && m.pb < INFINITY ? 1.0f : 0.0f;      // pb[0] / pb[0]
-      if (!P.bpt && wt > 0.0f && t == 2 && rnd(v) && rnd(eye[0])) {  // pb[0] / (pb[0] + pf[0] pb[1])
-        float res = 1.0f / (1.0f + v.oprob * m.pbr);
-        wt = res >= 0.0f ? res : 0.0f;
+    uint32_t em = 0;
+    bool rand_interior = false, rand_pair = false, prev_rand = false, first_rand = false, open = true;
+    for (int k = 0; k < ne; k++) {
+      const PV v = load_pv(eb + 4 * k);
+      const bool rv = rnd(v);
+      if (k == 0) first_rand = rv;
+      if (k >= 1) rand_pair |= prev_rand && rv;  // pairs within e[0..k]
+      if (rv && !is_emissive(S, v.contact)) em |= 1u << k;
+      if (k >= 1 && open) {  // s = 0 with t = k + 1 (interior e[1..k-1], pairs within e[0..k])
+        if (P.bpt ? rand_pair : rand_interior) {
+          open = false;
+        } else if (is_emissive(S, v.contact)) {
+          const MisE m = me[k];
+          F3 col = v.c * m.thr;
+          float prob = (v.dprob * v.oprob) * m.prob;
+          if (prob > 0.0f && length(col) > 0.0f) {
+            float wt = m.pb > 0.0 && m.pb < INFINITY ? 1.0f : 0.0f;      // pb[0] / pb[0]
+            if (!P.bpt && wt > 0.0f && k == 1 && rv && first_rand) {  // pb[0] / (pb[0] + pf[0] pb[1])
+              float res = 1.0f / (1.0f + v.oprob * m.pbr);
+              wt = res >= 0.0f ? res : 0.0f;
+            }
+            F3 c = col * (wt / prob);
+            if (length(c) > 0.0f) acc = acc + c;
+          }
+        }
       }
-      F3 c = col * (wt / prob);
-      if (length(c) > 0.0f) acc = acc + c;
+      if (k >= 1) rand_interior |= rv;  // e[k] is interior for every longer path
+      prev_rand = rv;
     }
     img_add(img, (int)p, acc);
-    // connection candidates
-    uint32_t em = 0, lm = 0;
-    for (int k = 0; k < ne; k++)
-      if (rnd(eye[k]) && !is_emissive(S, eye[k].contact)) em |= 1u << k;
+    uint32_t lm = 0;
     const uint32_t lp = p % P.n_light;
     const int nl = llen[lp];
     for (int ci = 0; ci < nl; ci++) {
@@ -709,7 +724,6 @@ __global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, const 
     cmask[p] = make_uint2(em, lm);
     ccount[p] = (unsigned long long)(__popc(em) * __popc(lm));
   }
-  if (nrays) atomicAdd(rays, nrays);
 }
 
 // Pairs [win0, win0 + cap) of the scanned order: pixel and eye vertex (q = p * maxv + k)
@@ -816,7 +830,7 @@ __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, c
     nrays += (unsigned long long)ne;
     for (int k = 0; k < ne; k++) store_pv(ev + 4 * ((size_t)p * P.maxv + k), eye[k]);
     elen[p] = ne;
-    eye_mis(S, P.cam, eye, ne, r, P.norm, !P.bpt, emis + (size_t)p * P.maxv);
+    eye_mis(S, P.cam, [&](int k) { return eye[k]; }, ne, r, P.norm, !P.bpt, emis + (size_t)p * P.maxv);
     F3 acc = {0, 0, 0};
     uint32_t lp = p % P.n_light;
     int nl = llen[lp];
@@ -1567,9 +1581,10 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
       k_vcm_eye_full<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
                                           bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[10].as<float>(), ctr + 1);
     } else {
-      k_vcm_eye<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
-                                     bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[21].as<uint2>(), qc,
-                                     bufs[10].as<float>(), ctr + 1);
+      k_vcm_eye<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), ctr + 1);
+      k_eye_post<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
+                                          bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[21].as<uint2>(), qc,
+                                          bufs[10].as<float>());
       if ((e = scan_total(P.n_pixels, total)) != cudaSuccess) return e;
       for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
         uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
