@@ -115,11 +115,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def rank_rays(rank: int, n: int):
+    """The ray batch of one rank's replica (each rank its own seed)."""
+    from renderx_gb300 import scenes
+    return scenes.hit_rays(n, seed=RAY_SEED + rank)
+
+
 def make_workload(rank: int):
     from renderx_gb300 import scenes
     sc = scenes.sphere_field(N_SPHERES, SUBDIV, seed=SCENE_SEED)
     f = sc.flatten()
-    o, d = scenes.hit_rays(N_RAYS, seed=RAY_SEED + rank)  # N_RAYS may be reset by --rays
+    o, d = rank_rays(rank, N_RAYS)  # N_RAYS may be reset by --rays
     return sc, f, o, d
 
 
@@ -354,6 +360,22 @@ def dist_setup(args):
     return ws, rank, local
 
 
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """The slowest rank's figure (every rank gets it); x itself on one process."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mrays(ws: int, rays_per_rank: int, steps: int, seconds: float) -> float:
+    """Weak scaling: every rank traces its own batch, so the job's throughput is all
+    ranks' rays over the slowest rank's time."""
+    return ws * rays_per_rank * steps / seconds / 1e6
+
+
 def run_reference(args):
     ws, rank, _ = dist_setup(args)
     if rank != 0:
@@ -427,13 +449,9 @@ def run_ours(args):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     kern_ms = ctx.read_trace_timing()  # (steps, 3): walk, visibility check, re-walk
     ctx.set_trace_timing(0)
-    t_ms = sum(step_ms)
-    if dist:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    t_ms = max_over_ranks(sum(step_ms), dist)
     ms_per_step = t_ms / args.steps
-    value = ws * n / (ms_per_step * 1e-3) / 1e6
+    value = whole_job_mrays(ws, n, args.steps, t_ms * 1e-3)
     clocks = clk.summary()
 
     # end to end through the host-buffer C-ABI call, pinned host memory
@@ -484,12 +502,8 @@ def end_to_end(ctx, host_rays, d_tid, args, dist, ws, n):
     for _ in range(args.steps):
         ctx.trace_closest_rays(r_np, t_np, d_np)
     torch.cuda.synchronize()
-    e_s = time.perf_counter() - e0
-    if dist:
-        tt = torch.tensor([e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e_s = float(tt.item())
-    e2e = ws * n * args.steps / e_s / 1e6
+    e_s = max_over_ranks(time.perf_counter() - e0, dist)
+    e2e = whole_job_mrays(ws, n, args.steps, e_s)
     same = bool(np.array_equal(t_np, d_tid.cpu().numpy()))
     return e2e, same
 
