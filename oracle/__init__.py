@@ -3,8 +3,8 @@
 CPU restatement of the reference's light-transport path (reference src/KDTree.cpp,
 src/PathTracer.cpp and the material code), compiled from ``oracle/*.cpp`` into
 ``oracle/liboracle.so``. Only ``tests/``, ``__graft_entry__.smoke()`` and
-``bench.py``'s CPU-baseline leg may import this package; it is the checker, never the
-thing measured or shipped.
+``bench.py``'s CPU-baseline leg may import this package; it checks results and times
+the CPU baseline, and is never the thing measured or shipped.
 
 Parity pins: ``tests/test_oracle_golden.py`` checks this restatement against golden
 fixtures produced by the reference's own code compiled from its sources
