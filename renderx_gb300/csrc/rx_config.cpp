@@ -5,10 +5,11 @@
 //
 // Covered: <Config> with <Scene><path/><name/><camera/></Scene>, <Renderer> (<type>,
 // <maxDepth>, <spp>, <radius>), <time>, <savePath>; scene files with <Object Name>
-// (<filePath>, optional <transform>, a <Material> inline or referenced by <path>/<name>)
-// and <Camera Name>; materials Diffuse, Glossy, Phong, Refractive, Reflective,
-// Emissive, VPM. Not covered (RX_ERR_UNSUPPORTED): <GroupObject>, textures, bump maps,
-// GridVolume, ParallelLight.
+// (<filePath>, optional <transform>, a <Material> inline or referenced by <path>/<name>),
+// <GroupObject> (one OBJ split into named shapes by its "g" lines, unitized, with the
+// group's <transform>; its <Object Name> children pick the shapes) and <Camera Name>;
+// materials Diffuse, Glossy, Phong, Refractive, Reflective, Emissive, VPM (<stepsize>).
+// Not covered (RX_ERR_UNSUPPORTED): textures, bump maps, GridVolume, ParallelLight.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -243,6 +244,43 @@ struct Mesh {
   std::vector<uint32_t> f;         // triangles
 };
 
+// Indexed mesh from parsed OBJ data: corners whose normal index differs from an
+// earlier corner's at the same position get their own vertex.
+bool finish_mesh(const std::vector<float>& pos, const std::vector<float>& nrm, const std::vector<int>& corner_v,
+                 const std::vector<int>& corner_n, const std::string& path, Mesh& m, std::string& err) {
+  const int nv = (int)pos.size() / 3, nn = (int)nrm.size() / 3;
+  bool has_n = nn > 0;
+  for (size_t i = 0; i < corner_v.size() && has_n; i++) has_n = corner_n[i] >= 0 && corner_n[i] < nn;
+  m.v = pos;
+  if (has_n) m.n.assign(pos.size(), 0.0f);
+  std::vector<int> vnorm(nv, -1);
+  std::unordered_map<uint64_t, uint32_t> split;
+  for (size_t i = 0; i < corner_v.size(); i++) {
+    int a = corner_v[i];
+    if (a < 0 || a >= nv) return err = "face index out of range in " + path, false;
+    uint32_t idx = (uint32_t)a;
+    if (has_n) {
+      int b = corner_n[i];
+      if (vnorm[a] < 0 || vnorm[a] == b) {
+        vnorm[a] = b;
+        for (int q = 0; q < 3; q++) m.n[3 * a + q] = nrm[3 * b + q];
+      } else {  // the same position with another normal: its own vertex
+        uint64_t key = ((uint64_t)a << 32) | (uint32_t)b;
+        auto it = split.find(key);
+        if (it == split.end()) {
+          idx = (uint32_t)(m.v.size() / 3);
+          for (int q = 0; q < 3; q++) m.v.push_back(pos[3 * a + q]), m.n.push_back(nrm[3 * b + q]);
+          split[key] = idx;
+        } else {
+          idx = it->second;
+        }
+      }
+    }
+    m.f.push_back(idx);
+  }
+  return true;
+}
+
 // SimpleShape::loadShape for .obj (v / vn / f with v, v//n, v/t/n, quads split (0,1,2),
 // (0,2,3); normals normalised on load) and .shp (int count, floats, int count, uints).
 // Corners whose normal index differs from the vertex index get their own vertex.
@@ -305,35 +343,89 @@ bool load_mesh(const std::string& path, Mesh& m, std::string& err) {
         }
     }
   }
-  const int nv = (int)pos.size() / 3, nn = (int)nrm.size() / 3;
-  bool has_n = nn > 0;
-  for (size_t i = 0; i < corner_v.size() && has_n; i++) has_n = corner_n[i] >= 0 && corner_n[i] < nn;
-  m.v = pos;
-  if (has_n) m.n.assign(pos.size(), 0.0f);
-  std::vector<int> vnorm(nv, -1);
-  std::unordered_map<uint64_t, uint32_t> split;
-  for (size_t i = 0; i < corner_v.size(); i++) {
-    int a = corner_v[i];
-    if (a < 0 || a >= nv) return err = "face index out of range in " + path, false;
-    uint32_t idx = (uint32_t)a;
-    if (has_n) {
-      int b = corner_n[i];
-      if (vnorm[a] < 0 || vnorm[a] == b) {
-        vnorm[a] = b;
-        for (int q = 0; q < 3; q++) m.n[3 * a + q] = nrm[3 * b + q];
-      } else {  // the same position with another normal: its own vertex
-        uint64_t key = ((uint64_t)a << 32) | (uint32_t)b;
-        auto it = split.find(key);
-        if (it == split.end()) {
-          idx = (uint32_t)(m.v.size() / 3);
-          for (int q = 0; q < 3; q++) m.v.push_back(pos[3 * a + q]), m.n.push_back(nrm[3 * b + q]);
-          split[key] = idx;
-        } else {
-          idx = it->second;
-        }
+  return finish_mesh(pos, nrm, corner_v, corner_n, path, m, err);
+}
+
+// SimpleShape::loadShape(path, true, &shapes) for a <GroupObject> (src/SimpleShape.cpp:
+// 44-313): every "g name" line starts a shape that takes the vertices, normals and
+// triangles that follow it (indices relative to where it starts; quads stay with the
+// file only, as there); then every shape is unitized by the whole file's bounding box
+// (centre to the origin, largest extent to 2: SimpleShape::unitize, applied as the
+// transposed matrix it returns). Shapes by name.
+bool load_group(const std::string& path, std::unordered_map<std::string, Mesh>& out, std::string& err) {
+  std::string text;
+  if (!read_file(path, text)) return err = "cannot read " + path, false;
+  struct Part {
+    std::string name;
+    std::vector<float> pos, nrm;
+    std::vector<int> cv, cn;
+  };
+  std::vector<Part> parts;
+  std::vector<float> all;  // every vertex of the file (the unitize box)
+  int v_base = 0, n_base = 0, nv_all = 0, nn_all = 0;
+  const char* p = text.c_str();
+  while (*p) {
+    const char* eol = strchr(p, '\n');
+    std::string line(p, eol ? eol : p + strlen(p));
+    p = eol ? eol + 1 : p + strlen(p);
+    char tag[8] = {0};
+    int off = 0;
+    if (sscanf(line.c_str(), "%7s%n", tag, &off) != 1 || tag[0] == '#') continue;
+    const char* rest = line.c_str() + off;
+    if (!strcmp(tag, "g")) {
+      char name[256] = {0};
+      sscanf(rest, "%255s", name);
+      parts.push_back(Part{name, {}, {}, {}, {}});
+      v_base = nv_all;
+      n_base = nn_all;
+    } else if (!strcmp(tag, "v") || !strcmp(tag, "vn")) {
+      float x, y, z;
+      if (sscanf(rest, "%f %f %f", &x, &y, &z) != 3) continue;
+      if (tag[1] == 'n') {
+        float l = std::sqrt(x * x + y * y + z * z);
+        if (l > 0) x /= l, y /= l, z /= l;
+        nn_all++;
+        if (!parts.empty()) parts.back().nrm.insert(parts.back().nrm.end(), {x, y, z});
+      } else {
+        nv_all++;
+        all.insert(all.end(), {x, y, z});
+        if (!parts.empty()) parts.back().pos.insert(parts.back().pos.end(), {x, y, z});
+      }
+    } else if (!strcmp(tag, "f") && !parts.empty()) {
+      int vi[4], ni[4], k = 0;
+      char tok[64];
+      int used = 0;
+      while (k < 4 && sscanf(rest, "%63s%n", tok, &used) == 1) {
+        rest += used;
+        int a = 0, b = 0, c = 0;
+        ni[k] = -1;
+        if (sscanf(tok, "%d/%d/%d", &a, &b, &c) == 3) vi[k] = a - 1, ni[k] = c - 1;
+        else if (sscanf(tok, "%d//%d", &a, &c) == 2) vi[k] = a - 1, ni[k] = c - 1;
+        else if (sscanf(tok, "%d", &a) == 1) vi[k] = a - 1;
+        else break;
+        k++;
+      }
+      if (k != 3) continue;  // quads are not split into the shapes (loadShape: "not dealt with")
+      for (int q = 0; q < 3; q++) {
+        parts.back().cv.push_back(vi[q] - v_base);
+        parts.back().cn.push_back(ni[q] < 0 ? -1 : ni[q] - n_base);
       }
     }
-    m.f.push_back(idx);
+  }
+  if (all.empty()) return err = "no vertices in " + path, false;
+  float lo[3] = {all[0], all[1], all[2]}, hi[3] = {all[0], all[1], all[2]};
+  for (size_t i = 0; i < all.size(); i += 3)
+    for (int q = 0; q < 3; q++) lo[q] = std::min(lo[q], all[i + q]), hi[q] = std::max(hi[q], all[i + q]);
+  float len = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+  const float sc = 2 / len, neg = -2 / len;
+  float tr[3];
+  for (int q = 0; q < 3; q++) tr[q] = neg * ((lo[q] + hi[q]) / 2);
+  for (Part& part : parts) {
+    for (size_t i = 0; i < part.pos.size(); i += 3)
+      for (int q = 0; q < 3; q++) part.pos[i + q] = sc * part.pos[i + q] + tr[q];
+    Mesh m;
+    if (!finish_mesh(part.pos, part.nrm, part.cv, part.cn, path, m, err)) return false;
+    out[part.name] = std::move(m);
   }
   return true;
 }
@@ -430,13 +522,11 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
   }
   if (!scene) scene = Loader::find(cd->roots, "Scene", scene_name);
   if (!scene) return err = "scene not found", RX_ERR_INVALID;
-  if (scene->first("GroupObject")) return err = "<GroupObject> is not supported", RX_ERR_UNSUPPORTED;
-
-  for (auto& k : scene->kids) {
-    if (k->tag != "Object") continue;
+  // one scene object: material from <Material> (a <path>/<name> reference into another
+  // file or this scene, else inline), mesh, optional transform (ConfigManager.cpp:166-246)
+  auto resolve = [&](const XNode* k, rx_object& o) -> rx_status {
     const XNode* mref = k->first("Material");
     if (!mref) return err = "object without <Material>", RX_ERR_INVALID;
-    // material: <path>/<name> reference (another file or this scene), else inline
     const XNode* nm = nullptr;
     std::string mpath = mref->value("path") ? mref->value("path") : scene_path;
     std::string mname = mref->value("name") ? mref->value("name") : "";
@@ -446,15 +536,13 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
       if (!nm && mref->first("name")) nm = Loader::find(scene->kids, "Material", mname);
     }
     if (!nm) nm = mref;
-    rx_object o{};
-    if (!material(nm, o, err)) return RX_ERR_UNSUPPORTED;
-    const char* fp = k->value("filePath");
-    if (!fp) return err = "object without <filePath>", RX_ERR_INVALID;
-    Mesh m;
-    if (!load_mesh(L.resolve(fp), m, err)) return RX_ERR_INVALID;
+    o = rx_object{};
+    return material(nm, o, err) ? RX_OK : RX_ERR_UNSUPPORTED;
+  };
+  auto add_object = [&](rx_object o, const Mesh& m, const char* xform) -> rx_status {
     float M[4][4];
-    bool xf = k->first("transform") != nullptr;
-    if (xf && !read_matrix(k->value("transform"), M)) return err = "bad <transform>", RX_ERR_INVALID;
+    bool xf = xform != nullptr;
+    if (xf && !read_matrix(xform, M)) return err = "bad <transform>", RX_ERR_INVALID;
     uint32_t base = (uint32_t)(H.verts.size() / 3);
     for (size_t i = 0; i < m.v.size(); i += 3) {
       float x = m.v[i], y = m.v[i + 1], z = m.v[i + 2];
@@ -490,6 +578,38 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
       H.tri_local.push_back(t);
     }
     H.objs.push_back(o);
+    return RX_OK;
+  };
+  // <GroupObject>s first (ConfigManager.cpp:193-224): one OBJ split into named shapes, each
+  // <Object Name=...> inside taking its shape with the group's transform
+  for (auto& g : scene->kids) {
+    if (g->tag != "GroupObject") continue;
+    const char* fp = g->value("filePath");
+    if (!fp) return err = "<GroupObject> without <filePath>", RX_ERR_INVALID;
+    std::unordered_map<std::string, Mesh> shapes;
+    if (!load_group(L.resolve(fp), shapes, err)) return RX_ERR_INVALID;
+    const char* xform = g->first("transform") ? g->value("transform") : nullptr;
+    for (auto& k : g->kids) {
+      if (k->tag != "Object") continue;
+      rx_object o;
+      rx_status st = resolve(k.get(), o);
+      if (st != RX_OK) return st;
+      const char* nm = k->attr("Name");
+      auto it = nm ? shapes.find(nm) : shapes.end();
+      if (it == shapes.end()) return err = std::string("group shape ") + (nm ? nm : "?") + " not in " + fp, RX_ERR_INVALID;
+      if ((st = add_object(o, it->second, xform)) != RX_OK) return st;
+    }
+  }
+  for (auto& k : scene->kids) {
+    if (k->tag != "Object") continue;
+    rx_object o;
+    rx_status st = resolve(k.get(), o);
+    if (st != RX_OK) return st;
+    const char* fp = k->value("filePath");
+    if (!fp) return err = "object without <filePath>", RX_ERR_INVALID;
+    Mesh m;
+    if (!load_mesh(L.resolve(fp), m, err)) return RX_ERR_INVALID;
+    if ((st = add_object(o, m, k->first("transform") ? k->value("transform") : nullptr)) != RX_OK) return st;
   }
   if (H.objs.empty()) return err = "scene has no objects", RX_ERR_INVALID;
   const XNode* cam = Loader::find(scene->kids, "Camera", sc->value("camera"));

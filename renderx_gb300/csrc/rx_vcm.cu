@@ -1172,7 +1172,7 @@ __global__ void __launch_bounds__(128) k_pm_light(DevScene S, VcmParams P, float
     Rng rng(P.seed, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
     Hit3 h;
     PV start = emit_ray(S, P.cam, rng, h);
-    PV prev;
+    PV prev = start;
     F3 thr = {1, 1, 1};
     bool stop = false;
     int n = sample_path(S, P.cam, start, h, P.max_depth, true, rng, [&](int i, const PV& v) {

@@ -158,3 +158,41 @@ def test_renderer_type_names(tmp_path, type_name, code):
     cfg = sceneio.write_config(sc, str(tmp_path), type_name, 5)
     _, info = rx.config_read(cfg)
     assert info["estimator"] == code and info["renderer"] == type_name and info["max_depth"] == 5
+
+
+def test_group_object_splits_unitizes_and_transforms(tmp_path):
+    # ConfigManager.cpp:193-224 + SimpleShape::loadShape(path, true, &shapes): "g" lines
+    # start shapes whose indices are the file's minus the vertices before the group; the
+    # whole file is unitized (centre 0, largest extent 2); quads stay with the file; the
+    # group's transform applies to every shape
+    _write(tmp_path / "grp.obj", "v 9 9 9\n"               # before any group: counts for the box only
+                                 "g left\nv 0 0 0\nv 2 0 0\nv 0 2 0\nf 2 3 4\n"
+                                 "g right\nv 2 2 0\nv 4 2 0\nv 2 4 0\nv 4 4 0\nf 5 6 7\nf 5 6 8 7\n")
+    _write(tmp_path / "scene.xml",
+           "<Scene Name=\"s\">\n"
+           "  <GroupObject><filePath>grp.obj</filePath>"
+           "<transform>[1, 0, 0, 10][0, 1, 0, 0][0, 0, 1, 0][0, 0, 0, 1]</transform>"
+           "<Object Name=\"right\"><Material><type>Diffuse</type><color>(0.5, 0.5, 0.5)</color></Material></Object>"
+           "<Object Name=\"left\"><Material><type>Emissive</type><color>(1, 1, 1)</color></Material></Object>"
+           "</GroupObject>\n"
+           "  <Object Name=\"t\"><filePath>tri.obj</filePath><Material><type>Diffuse</type></Material></Object>\n"
+           "  <Camera Name=\"c\"><width>4</width><height>4</height><sightDist>5</sightDist><focus>(0,0,0)</focus>"
+           "<position>(0,0,1)</position><up>(0,1,0)</up></Camera>\n</Scene>\n")
+    _write(tmp_path / "tri.obj", "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    _write(tmp_path / "config.xml", "<Config><Scene><path>scene.xml</path><name>s</name><camera>c</camera></Scene>"
+                                    "<Renderer><type>PT</type></Renderer></Config>\n")
+    a, info = rx.config_read(str(tmp_path / "config.xml"))
+    o = a["objects"]
+    assert [x.material for x in o] == [scenes.DIFFUSE, scenes.EMISSIVE, scenes.DIFFUSE]  # group first, in order
+    assert [x.tri_count for x in o] == [1, 1, 1]  # the quad of "right" is not in the shape
+    # file box: (0,0,0)-(9,9,9): centre 4.5, largest extent 9 -> scale 2/9
+    s, c = np.float32(2) / np.float32(9), np.float32(4.5)
+    t = np.float32(-2) / np.float32(9) * c
+
+    def unit(v):
+        return np.array([s * np.float32(x) + t for x in v], np.float32) + np.array([10, 0, 0], np.float32)
+    right = a["verts"][a["tris"][o[0].tri_begin]]
+    left = a["verts"][a["tris"][o[1].tri_begin]]
+    assert np.allclose(right, [unit(v) for v in ([2, 2, 0], [4, 2, 0], [2, 4, 0])], atol=1e-6)
+    assert np.allclose(left, [unit(v) for v in ([0, 0, 0], [2, 0, 0], [0, 2, 0])], atol=1e-6)
+    assert info["num_triangles"] == 3
