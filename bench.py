@@ -527,7 +527,7 @@ def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_m
                 "gpu_launches": 3 * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                             "kernel": "k_trace_persistent4 (closest-hit walk, 4-wide BVH)", "kernel_ms": walk_ms,
+                             "kernel": "k_trace_persistent4<16> (closest-hit walk, 4-wide BVH, shared-memory short stack)", "kernel_ms": walk_ms,
                              "algorithmic_bytes_per_launch": bytes_alg},
                 "kernel_ms_mean": {"walk": walk_ms,
                                    "visibility_check": float(kern_ms[:, 1].mean()) if len(kern_ms) else None,

@@ -130,7 +130,9 @@ typedef struct rx_batch_options {
   uint32_t autotune;       /* 1: time the launch-shape candidates on the first passes */
   uint32_t reserved;
   int32_t chosen_blocks_per_sm;  /* out: extend / shade blocks per SM used */
-  int32_t chosen_stack;          /* out: traversal stack depth used */
+  int32_t chosen_stack;          /* out: walk used: 4 = 4-wide BVH, 5 = 4-wide BVH with a
+                                    shared-memory short stack, 32 / 64 = binary BVH with
+                                    that stack depth */
 } rx_batch_options;
 
 /* Vertex connection and merging options (VCMTracer, reference include/VCMTracer.h). */
@@ -317,8 +319,9 @@ rx_status rx_render_pm(rx_context* ctx, const rx_camera* cam, const rx_pm_option
 
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
  * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative
- * leaf postponing, 3 = persistent over the 4-wide BVH (the default; falls back to 1
- * when that tree is too deep for its stack); blocks of 128 threads, blocks_per_sm per
+ * leaf postponing, 3 = persistent over the 4-wide BVH, 4 = 3 with the first 16 entries
+ * of each walk's stack in shared memory (the default); 3 and 4 fall back to 1 when the
+ * 4-wide tree is too deep for their stack. Blocks of 128 threads, blocks_per_sm per
  * SM. No reference counterpart (launch tuning). */
 rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_per_sm);
 /* Closest-hit options (no reference counterpart): check_mode = how each walk's winner

@@ -267,7 +267,7 @@ class Context:
         self._ck(self._L.rx_render_pm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
         return film, dict(rays=st.extension_rays, photons=st.merges, paths=st.paths, ms=st.ms)
 
-    def set_trace_config(self, variant: int = 3, blocks_per_sm: int = 12):
+    def set_trace_config(self, variant: int = 4, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
     def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18, walk_stack: int = 0):

@@ -623,8 +623,8 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
 
 rx_status rx_trace_set_config(rx_context* c, int32_t variant, int32_t blocks_per_sm) {
   if (!c) return RX_ERR_INVALID;
-  if (variant < 0 || variant > 3 || blocks_per_sm < 1 || blocks_per_sm > 32)
-    return c->fail(RX_ERR_INVALID, "variant must be 0..3 and blocks_per_sm 1..32");
+  if (variant < 0 || variant > 4 || blocks_per_sm < 1 || blocks_per_sm > 32)
+    return c->fail(RX_ERR_INVALID, "variant must be 0..4 and blocks_per_sm 1..32");
   c->trace_cfg.variant = variant;
   c->trace_cfg.blocks_per_sm = blocks_per_sm;
   return RX_OK;

@@ -15,10 +15,11 @@ namespace rx {
 struct GuideState;
 void guide_free(GuideState* g);
 
-// Closest-hit launch shape: variant 0 = one thread per ray, 1 = persistent warps
-// refilling finished lanes; blocks_per_sm x sms blocks of 128 threads.
+// Closest-hit launch shape: variant 0 = one thread per ray, 1-2 = persistent warps
+// refilling finished lanes (binary BVH), 3 = the same over the 4-wide BVH, 4 = 3 with the
+// first 16 stack entries in shared memory; blocks_per_sm x sms blocks of 128 threads.
 struct TraceConfig {
-  int variant = 3;
+  int variant = 4;
   int blocks_per_sm = 12;
   int sms = 152;
   int pt_blocks_per_sm = 8;  // wavefront extend / shade kernels
@@ -28,8 +29,9 @@ struct TraceConfig {
 };
 
 // Launch shape of the wavefront's extend / shade kernels: blocks of 128 threads per SM
-// and the walk: 4 = the 4-wide BVH, 32 or 64 = the binary BVH with that many stack
-// entries (must exceed the BVH depth).
+// and the walk: 4 = the 4-wide BVH, 5 = the same with the first 16 stack entries in
+// shared memory, 32 or 64 = the binary BVH with that many stack entries (must exceed
+// the BVH depth).
 struct PtShape {
   int blocks_per_sm = 8;
   int stack = 64;

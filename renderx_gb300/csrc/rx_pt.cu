@@ -536,7 +536,8 @@ void enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
 
 void enqueue_pass_shape(const Wave& W, const PtShape& sh, int sms, cudaStream_t s) {
   int grid = sms * sh.blocks_per_sm;
-  if (sh.stack == kWalk4) enqueue_pass<kWalk4>(W, grid, s);
+  if (sh.stack == kWalk4S) enqueue_pass<kWalk4S>(W, grid, s);
+  else if (sh.stack == kWalk4) enqueue_pass<kWalk4>(W, grid, s);
   else if (sh.stack == 32) enqueue_pass<32>(W, grid, s);
   else enqueue_pass<kStackDepth>(W, grid, s);
 }
@@ -617,12 +618,12 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   }
 
   // launch shapes: the context's default, or candidates timed on the first passes
-  PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4 : (max_bvh_depth < 32 ? 32 : kStackDepth)};
+  PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4S : (max_bvh_depth < 32 ? 32 : kStackDepth)};
   std::vector<PtShape> cands;
   if (run.autotune && !guided) {
     for (int bps : {4, 8, 16})
-      for (int st : {kWalk4, 32, kStackDepth})
-        if (st == kWalk4 ? wide_ok : st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
+      for (int st : {kWalk4S, kWalk4, 32, kStackDepth})
+        if (st == kWalk4 || st == kWalk4S ? wide_ok : st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
     if (npasses < cands.size() + 2) cands.clear();
   }
 
@@ -688,7 +689,9 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       unsigned *cc = W.cnt, *cn = W.cnt + 1;
       for (uint32_t d = 0; d < W.loops; d++) {
         const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
-        if (best.stack == kWalk4)
+        if (best.stack == kWalk4S)
+          k_extend<kWalk4S><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
+        else if (best.stack == kWalk4)
           k_extend<kWalk4><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
         else if (best.stack == 32)
           k_extend<32><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
@@ -697,7 +700,9 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
         if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, sms, s)) != cudaSuccess)
           return e;
         k_zero<<<1, 1, 0, s>>>(cn);
-        if (best.stack == kWalk4)
+        if (best.stack == kWalk4S)
+          k_shade<kWalk4S><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
+        else if (best.stack == kWalk4)
           k_shade<kWalk4><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
         else if (best.stack == 32)
           k_shade<32><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);

@@ -233,7 +233,9 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
 // 128-byte node, nearest hit child next, the others stacked far to near with their entry
 // distance so that popped subtrees beyond the current best are skipped. The stack holds
 // at most 3 entries per level: callers use it only when 3 * bvh4_depth + 1 <= 64.
-constexpr int kWalk4 = 4;  // walk selector: the 4-wide BVH
+constexpr int kWalk4 = 4;   // walk selector: the 4-wide BVH
+constexpr int kWalk4S = 5;  // the 4-wide BVH, first kShortStack stack entries in shared memory
+constexpr int kShortStack = 16;
 // The cnt triangles of the 4-wide tree's leaf at slot `first` (Moller-Trumbore, the
 // NoSelfIntersectionCondition when cond): lowers best to the nearest legal hit; with ANY,
 // returns true at the first one.
@@ -270,17 +272,24 @@ __device__ __forceinline__ bool leaf_test(const DevScene& S, int first, int cnt,
   return false;
 }
 
-template <bool ANY>
+// SH > 0: the first SH stack entries of each thread sit in shared memory, one column
+// per thread (callers are kernels of at most kShortCols threads per block).
+constexpr int kShortCols = 128;
+template <bool ANY, int SH = 0>
 __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
   const DevAccel& A = S.accel;
+  constexpr int kSHN = SH > 0 ? SH : 1;
+  __shared__ int s_ref[kSHN][kShortCols];
+  __shared__ float s_tn[kSHN][kShortCols];
+  const int tx = threadIdx.x;
   F3 inv = {fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(1e30f, d.x),
             fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(1e30f, d.y),
             fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(1e30f, d.z)};
   F3 ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
   PHit best{-1, tmax};
   constexpr int kS = 64;
-  int stack_ref[kS];
-  float stack_tn[kS];
+  int stack_ref[kS - SH];
+  float stack_tn[kS - SH];
   int sp = 0, cur = 0, cnt = 0;
   const bool cond = !(contact == -1 && inside == -1);
   while (true) {
@@ -328,8 +337,14 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
 #pragma unroll
         for (int k = 3; k >= 1; k--)
           if (k < nh && sp < kS) {
-            stack_ref[sp] = r[k] < 0 ? ~((~r[k]) << 3 | (c[k] - 1)) : r[k];
-            stack_tn[sp] = tn[k];
+            const int e = r[k] < 0 ? ~((~r[k]) << 3 | (c[k] - 1)) : r[k];
+            if (SH > 0 && sp < SH) {
+              s_ref[sp][tx] = e;
+              s_tn[sp][tx] = tn[k];
+            } else {
+              stack_ref[sp - SH] = e;
+              stack_tn[sp - SH] = tn[k];
+            }
             sp++;
           }
         cur = r[0];
@@ -342,8 +357,9 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
     bool found = false;
     while (sp > 0) {
       sp--;
-      if (stack_tn[sp] <= best.t) {
-        int rr = stack_ref[sp];
+      const bool sh = SH > 0 && sp < SH;
+      if ((sh ? s_tn[sp][tx] : stack_tn[sp - SH]) <= best.t) {
+        int rr = sh ? s_ref[sp][tx] : stack_ref[sp - SH];
         if (rr < 0) {
           int packed = ~rr;
           cur = ~(packed >> 3);
@@ -360,11 +376,13 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
   return best;
 }
 
-// Closest / any legal hit with the walk WALK selects: kWalk4 = the 4-wide BVH, else the
-// binary BVH with a stack of WALK entries.
+// Closest / any legal hit with the walk WALK selects: kWalk4 = the 4-wide BVH, kWalk4S =
+// the same with its first kShortStack stack entries in shared memory, else the binary
+// BVH with a stack of WALK entries.
 template <bool ANY, int WALK>
 __device__ __forceinline__ PHit trace_walk(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
-  if constexpr (WALK == kWalk4) return trace_cond4<ANY>(S, o, d, tmax, contact, inside);
+  if constexpr (WALK == kWalk4) return trace_cond4<ANY, 0>(S, o, d, tmax, contact, inside);
+  else if constexpr (WALK == kWalk4S) return trace_cond4<ANY, kShortStack>(S, o, d, tmax, contact, inside);
   else return trace_cond<ANY, WALK>(S, o, d, tmax, contact, inside);
 }
 

@@ -57,6 +57,9 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
 // The persistent walk over the 4-wide BVH: one node visit tests four child boxes
 // (128-byte node, one cache line), visits the nearest hit child next and stacks the
 // others far to near; pruning, leaf tests and refills as k_trace_persistent.
+// kShort > 0: the first kShort entries of each thread's stack sit in shared memory
+// (one column per thread, conflict-free), deeper entries in local memory.
+template <int kShort>
 __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
                                                            const uint32_t* __restrict__ order,
                                                            int32_t* __restrict__ out_tid,
@@ -66,22 +69,26 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int DONE = INT_MIN;
   constexpr int kStack4 = 64;  // at most 3 entries per level of a BVH4 shallower than 21 levels
-  const int lane = threadIdx.x & 31;
+  constexpr int kShortN = kShort > 0 ? kShort : 1;
+  __shared__ int s_ref[kShortN][128];
+  __shared__ float s_tn[kShortN][128];
+  const int lane = threadIdx.x & 31, tx = threadIdx.x;
   unsigned long long* cursor = counters + 4;
   bool active = false, exhausted = false;
   uint32_t ray = 0;
   F3 o{}, d{}, inv{}, ood{};
   float tlimit = INFINITY;
   HitResult best{-1, -1.0f, 0u, 0u, false};
-  int stack_ref[kStack4];
-  float stack_tn[kStack4];
+  int stack_ref[kStack4 - kShort];
+  float stack_tn[kStack4 - kShort];
   int sp = 0, cur = DONE, cnt = 0;
 
   auto pop = [&]() {
     while (sp > 0) {
       sp--;
-      if (stack_tn[sp] <= tlimit) {
-        int r = stack_ref[sp];
+      const bool sh = kShort > 0 && sp < kShort;
+      if ((sh ? s_tn[sp][tx] : stack_tn[sp - kShort]) <= tlimit) {
+        int r = sh ? s_ref[sp][tx] : stack_ref[sp - kShort];
         if (r < 0) {
           int packed = ~r;
           cnt = (packed & 7) + 1;
@@ -187,8 +194,13 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
 #pragma unroll
           for (int k = 3; k >= 1; k--) {  // farthest first, so the nearer pop earlier
             if (k < nh && sp < kStack4) {
-              stack_ref[sp] = pack(r[k], c[k]);
-              stack_tn[sp] = tn[k];
+              if (kShort > 0 && sp < kShort) {
+                s_ref[sp][tx] = pack(r[k], c[k]);
+                s_tn[sp][tx] = tn[k];
+              } else {
+                stack_ref[sp - kShort] = pack(r[k], c[k]);
+                stack_tn[sp - kShort] = tn[k];
+              }
               sp++;
             }
           }
@@ -565,8 +577,11 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     blocks = blocks < need ? blocks : need;
     // the walk's stack lives in local memory: the shallower one when the BVH allows
     const bool shallow = cfg.walk_stack != 64 && A.bvh_depth < 32;
-    if (cfg.variant == 3 && A.bvh4 && 3 * A.bvh4_depth + 1 <= 64)  // the 4-wide walk's stack bound
-      k_trace_persistent4<<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+    const bool walk4 = A.bvh4 && 3 * A.bvh4_depth + 1 <= 64;  // the 4-wide walk's stack bound
+    if (cfg.variant == 4 && walk4)
+      k_trace_persistent4<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+    else if (cfg.variant == 3 && walk4)
+      k_trace_persistent4<0><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
     else if (cfg.variant == 1 && shallow)
       k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
     else if (cfg.variant == 1)
