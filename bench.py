@@ -53,7 +53,7 @@ WORKLOAD = "hit_batch_2^24_rays_cornell+200_icospheres_4096036_tris"
 
 # DRAM bytes (read + write) of one walk-kernel launch over the 2^24-ray batch, from a
 # one-pass ncu capture of this workload (profiles/k_trace_persistent4_hit2e24.md)
-TRAFFIC_BYTES_PER_RAY = (7063220224 + 1839674368) / (1 << 24)
+TRAFFIC_BYTES_PER_RAY = (6416909056 + 1577210624) / (1 << 24)
 
 
 def load_tflops():

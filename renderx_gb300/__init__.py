@@ -270,6 +270,10 @@ class Context:
     def set_trace_config(self, variant: int = 4, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
+    def set_trace_staging(self, chunk_rays: int = 0):
+        """Rays per staged chunk of the host-buffer call (0 = default 2^23)."""
+        self._ck(self._L.rx_trace_set_staging(self.h, int(chunk_rays)))
+
     def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18, walk_stack: int = 0):
         """Visibility check of each winner (1 = thread per ray, 0 = warp per ray), the
         batch size from which rays are binned before the walk (0 = never) and the walk

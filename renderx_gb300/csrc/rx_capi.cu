@@ -57,7 +57,7 @@ void rx_destroy(rx_context* c) {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
     for (DevBuf* b : {&c->d_bvh, &c->d_bvh4, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
-                      &c->d_anc_range, &c->d_anc_nodes, &c->d_slot_n, &c->d_tri_v, &c->d_tri_n, &c->d_tri_obj,
+                      &c->d_anc_range, &c->d_anc_nodes, &c->d_anc_box, &c->d_slot_n, &c->d_tri_v, &c->d_tri_n, &c->d_tri_obj,
                       &c->d_objects, &c->d_light_cdf, &c->d_light_tri,
                       &c->d_counters, &c->d_queue})
       b->release();
@@ -186,6 +186,12 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
     for (int32_t nd = leaf_node[l]; nd >= 0; nd = c->ref.nodes[nd].parent) anc_nodes.push_back(nd);
     anc_range[2 * l + 1] = (uint32_t)anc_nodes.size();
   }
+  // the same root paths as boxes, contiguous per leaf (one dependent load fewer)
+  std::vector<float4> anc_box(2 * anc_nodes.size());
+  for (size_t k = 0; k < anc_nodes.size(); k++) {
+    anc_box[2 * k] = refn[2 * (size_t)anc_nodes[k]];
+    anc_box[2 * k + 1] = refn[2 * (size_t)anc_nodes[k] + 1];
+  }
   rx_status s;
   if ((s = upload(c, c->d_bvh, nodes.data(), nodes.size() * sizeof(float4), "upload BVH")) != RX_OK) return s;
   rx::collapse_bvh4(c->bvh, c->bvh4);
@@ -202,6 +208,8 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
     return s;
   if ((s = upload(c, c->d_anc_nodes, anc_nodes.data(), anc_nodes.size() * 4, "upload ancestor lists")) != RX_OK)
     return s;
+  if ((s = upload(c, c->d_anc_box, anc_box.data(), anc_box.size() * sizeof(float4), "upload ancestor boxes")) != RX_OK)
+    return s;
   rx::DevAccel& A = c->accel;
   A.bvh = c->d_bvh.as<float4>();
   A.tris = c->d_tris.as<float4>();
@@ -211,6 +219,7 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.ref_tris = c->d_ref_tris.as<float4>();
   A.anc_range = c->d_anc_range.as<uint32_t>();
   A.anc_nodes = c->d_anc_nodes.as<int32_t>();
+  A.anc_box = c->d_anc_box.as<float4>();
   A.num_nodes = (uint32_t)c->bvh.nodes.size();
   A.num_tris = nt;
   A.num_ref_nodes = (uint32_t)c->ref.nodes.size();
@@ -576,20 +585,26 @@ rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, 
                  "trace_reforder launch");
 }
 
-// Host buffers. The rays go to the device in chunks of up to kWholeBatch that alternate
+// Host buffers. The rays go to the device in chunks of up to stage_rays that alternate
 // between two copy/compute streams, so one chunk's copies overlap the other chunk's
-// kernels (2^23 rays per chunk: large enough for binning and the persistent walk; for a
-// 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for one whole-batch
-// copy, trace and copy back).
-static constexpr size_t kWholeBatch = (size_t)1 << 23;
+// kernels (2^23 rays per chunk by default: large enough for binning and the persistent
+// walk; for a 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for
+// one whole-batch copy, trace and copy back).
+rx_status rx_trace_set_staging(rx_context* c, uint32_t chunk_rays) {
+  if (!c) return RX_ERR_INVALID;
+  if (chunk_rays != 0 && chunk_rays < (1u << 16)) return c->fail(RX_ERR_INVALID, "chunk_rays: 0 or at least 65536");
+  c->stage_rays = chunk_rays ? chunk_rays : (size_t)1 << 23;
+  return RX_OK;
+}
+
 rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist) {
   if (!c) return RX_ERR_INVALID;
   if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
   if (n == 0) return RX_OK;
   if (!rays || !out_tid || !out_dist) return c->fail(RX_ERR_INVALID, "null buffer");
   DeviceGuard g(c->device);
-  const size_t chunk = std::min<size_t>(n, kWholeBatch);
-  const int nring = n > kWholeBatch ? 2 : 1;
+  const size_t chunk = std::min<size_t>(n, c->stage_rays);
+  const int nring = n > chunk ? 2 : 1;
   if (c->ring_chunk < chunk || (nring == 2 && !c->ring_rays[1].p)) {
     for (int k = 0; k < nring; k++) {
       rx_status s;

@@ -26,6 +26,7 @@ struct DevAccel {
   const float4* ref_tris;          // 3 float4 per triangle in reference DFS order (v*.w unused but v0.w = id)
   const uint32_t* anc_range;       // 2 per leaf: [begin, end) into anc_nodes
   const int32_t* anc_nodes;        // per leaf, its root path (leaf first) as node ids
+  const float4* anc_box;           // the same entries as 2 float4 each: that node's ref box
   uint32_t num_nodes, num_tris, num_ref_nodes, num_ref_leaves;
   float prune_rel;                 // pruning margin: t_limit = best + prune_rel*(1+best)
   float lo[3], hi[3];              // scene bounds (ray binning)

@@ -127,7 +127,7 @@ struct rx_context {
   bool accel_ready = false;
   rx::Bvh4 bvh4;
   rx::DevBuf d_bvh4;
-  rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes;
+  rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes, d_anc_box;
   rx::DevScene scene{};
   bool scene_ready = false;
   rx::DevBuf d_slot_n, d_tri_v, d_tri_n, d_tri_obj, d_objects, d_light_cdf, d_light_tri;
@@ -136,6 +136,7 @@ struct rx_context {
   // staging ring for host-buffer calls
   rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
   size_t ring_chunk = 0;
+  size_t stage_rays = (size_t)1 << 23;  // rays per staged chunk (rx_trace_set_staging)
   // per-kernel timing of device-buffer closest-hit calls (rx_trace_set_timing)
   std::vector<cudaEvent_t> timing_ev;  // 4 per recorded call
   size_t timing_used = 0;

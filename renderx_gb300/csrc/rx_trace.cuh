@@ -33,19 +33,16 @@ __device__ __forceinline__ bool ref_visible(const DevAccel& A, uint32_t leaf, F3
                                             unsigned* n_exact) {
   uint32_t b = __ldg(&A.anc_range[2 * leaf]), e = __ldg(&A.anc_range[2 * leaf + 1]);
   for (uint32_t k = b; k < e; k += 4) {
-    int nd[4];
     float4 lo[4], hi[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) nd[j] = (k + j < e) ? __ldg(&A.anc_nodes[k + j]) : -1;
-#pragma unroll
     for (int j = 0; j < 4; j++) {
-      int q = nd[j] < 0 ? 0 : nd[j];
-      lo[j] = __ldg(&A.ref[2 * q]);
-      hi[j] = __ldg(&A.ref[2 * q + 1]);
+      const uint32_t q = k + j < e ? k + j : k;
+      lo[j] = __ldg(&A.anc_box[2 * (size_t)q]);
+      hi[j] = __ldg(&A.anc_box[2 * (size_t)q + 1]);
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      if (nd[j] < 0) continue;
+      if (k + j >= e) continue;
       if (zero_dir || !box_clear_pass(f3(lo[j]), f3(hi[j]), o, d, inv)) {
         (*n_exact)++;
         if (!box_exact(f3(lo[j]), f3(hi[j]), o, d)) return false;
