@@ -16,7 +16,8 @@ Secondary sections of the same JSON line (each skippable):
   pt      : wavefront PathTracer on the same scene, 1024^2 x 64 spp, depth 16, Russian
             roulette from depth 3: Mrays/s (extension + shadow rays), samples/s.
   guiding : the glossy workload (60% glossy spheres, exponent log-U[100,1000], light of
-            1% of the ceiling): plain vs guided PathTracer at equal samples, relMSE
+            1% of the ceiling): plain vs guided PathTracer at equal samples and at equal
+            wall time (rx_pt_options.time_budget_s), relMSE
             against a high-sample FP64 render, relMSE x time (lower is better).
   mlp     : the guiding network's tensor-core kernels alone: training step on 2^18
             records and inference on 2^20 queries, TFLOP/s against the BF16 peak.
@@ -157,7 +158,9 @@ def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64):
 
 
 def section_guiding(res: int, ref_spp: int, spp: int):
-    """C4 glossy workload at res^2: plain vs guided PathTracer at equal samples.
+    """C4 glossy workload at res^2: plain vs guided PathTracer at equal samples, then at
+    equal time (both under a wall-time budget equal to the plain render's time, sample
+    count uncapped).
 
     The reference image is a guided render of ref_spp samples (an unbiased estimator
     with a fraction of plain sampling's variance, so the reference's own noise barely
@@ -181,7 +184,18 @@ def section_guiding(res: int, ref_spp: int, spp: int):
         ctx.guide_init(seed=1, **gopt)
         guided, _, sg = ctx.render_pt(sc.camera, spp, max_depth=16, rr_mode=1, seed=6, guided=True,
                                       paths_per_pass=ppp)
+        budget = sp["ms"] * 1e-3
+        plain_t, _, spt = ctx.render_pt(sc.camera, 1 << 16, max_depth=16, rr_mode=1, seed=7, paths_per_pass=ppp,
+                                        time_budget_s=budget)
+        ctx.guide_init(seed=2, **gopt)
+        guided_t, _, sgt = ctx.render_pt(sc.camera, 1 << 16, max_depth=16, rr_mode=1, seed=8, guided=True,
+                                         paths_per_pass=ppp, time_budget_s=budget)
     rp, rg = _relmse(plain, ref), _relmse(guided, ref)
+    rpt, rgt = _relmse(plain_t, ref), _relmse(guided_t, ref)
+    out["equal_time"] = {"budget_s": budget,
+                         "plain": {"ms": spt["ms"], "spp": spt["paths"] / (res * res), "relmse": rpt},
+                         "guided": {"ms": sgt["ms"], "spp": sgt["paths"] / (res * res), "relmse": rgt},
+                         "relmse_ratio": rgt / rpt}
     out.update({"guide_options": dict(gopt, paths_per_pass=ppp, bsdf_fraction=0.5),
                 "plain": {"ms": sp["ms"], "relmse": rp, "relmse_x_s": rp * sp["ms"] * 1e-3},
                 "guided": {"ms": sg["ms"], "relmse": rg, "relmse_x_s": rg * sg["ms"] * 1e-3},

@@ -95,6 +95,14 @@ typedef struct rx_pt_options {
   uint64_t seed;
   uint32_t paths_per_pass; /* wavefront size, 0 = 2^22 */
   uint32_t flags;          /* RX_PT_GUIDED or 0 */
+  float time_budget_s;     /* > 0: stop after the pass during which this much wall time
+                              has passed (whole passes, spp the cap); paths run in
+                              sample-major order, each pixel's mean divides by its own
+                              sample count (stats.paths = paths done). rx_render_pt only:
+                              0 in batch items. The equal-time comparisons of
+                              MCRenderer's per-iteration timer (reference
+                              include/MCRenderer.h:60, src/PathTracer.cpp:9,22). */
+  uint32_t reserved;
 } rx_pt_options;
 
 /* rx_pt_options.flags: sample directions at diffuse / glossy / Phong vertices by
@@ -144,6 +152,11 @@ typedef struct rx_vcm_options {
   float radius;            /* initial merge radius (VCMTracer::mergeRadius, <radius> in XML) */
   float alpha;             /* radius shrink: r *= ((s+alpha)/(s+1))^(1/3) (reference default 0.6667) */
   uint64_t seed;
+  float time_budget_s;     /* > 0: stop after the iteration during which this much wall time
+                              has passed (VCMTracer.cpp:142, the <time> runtime), iterations
+                              the cap; the mean is over the iterations done (stats.paths =
+                              pixels x iterations done) */
+  uint32_t reserved;       /* 0 */
 } rx_vcm_options;
 /* Evaluate each merge's colour and MIS weight with the reference's loops over the whole
  * joined path (VCMTracer::connectColorProb / connectMergeWeight, O(path length) per
@@ -156,7 +169,8 @@ typedef struct rx_bpt_options {
   uint32_t iterations;     /* samples per pixel (BidirectionalPathTracer::spp) */
   uint32_t max_depth;      /* MCRenderer::maxDepth, at most 21 */
   uint32_t flags;          /* RX_VCM_FULL_PATH_MIS or 0 */
-  uint32_t reserved;       /* 0 */
+  float time_budget_s;     /* > 0: stop after the iteration during which this much wall time
+                              has passed (BidirectionalPathTracer.cpp:114), as rx_vcm_options */
   uint64_t seed;
 } rx_bpt_options;
 
@@ -170,6 +184,9 @@ typedef struct rx_pm_options {
   float radius;            /* base radius (PhotonMap::setRadius, <radius>) */
   float alpha;             /* radius exponent, 0 = the reference's 2/3 */
   uint64_t seed;
+  float time_budget_s;     /* > 0: stop after the iteration during which this much wall time
+                              has passed, as rx_vcm_options */
+  uint32_t reserved;       /* 0 */
 } rx_pm_options;
 
 typedef struct rx_render_stats {

@@ -198,12 +198,17 @@ class Context:
 
     # -- rendering -------------------------------------------------------------------
     def render_pt(self, camera: "scenes.Camera", spp: int, max_depth: int = 8, nee: bool = False, rr_mode: int = 0,
-                  seed: int = 1, paths_per_pass: int = 0, want_sq: bool = False, guided: bool = False):
+                  seed: int = 1, paths_per_pass: int = 0, want_sq: bool = False, guided: bool = False,
+                  time_budget_s: float = 0.0):
         """PathTracer (nee=False) or PathTracerTest (nee=True) renderPixels for ``spp``
         samples: returns (mean (H,W,3) float64, mean of squares or None, stats dict).
-        guided: one-sample MIS with the guiding network (guide_init first; PathTracer only)."""
+        guided: one-sample MIS with the guiding network (guide_init first; PathTracer only).
+        time_budget_s > 0: stop after the pass during which that much wall time passed
+        (spp is then the cap; stats["paths"] = pixel samples done, each pixel's mean over
+        its own samples)."""
         cam = camera_struct(camera)
-        o = rx_pt_options(spp, max_depth, rr_mode, int(bool(nee)), seed, paths_per_pass, 1 if guided else 0)
+        o = rx_pt_options(spp, max_depth, rr_mode, int(bool(nee)), seed, paths_per_pass, 1 if guided else 0,
+                          float(time_budget_s), 0)
         h, w = camera.height, camera.width
         film = np.zeros((h, w, 3), np.float64)
         sq = np.zeros((h, w, 3), np.float64) if want_sq else None
@@ -232,12 +237,16 @@ class Context:
                            blocks_per_sm=bo.chosen_blocks_per_sm, stack=bo.chosen_stack)
 
     def render_vcm(self, camera: "scenes.Camera", iterations: int, radius: float, alpha: float = 0.6667,
-                   max_depth: int = 8, light_paths: int = 0, seed: int = 1, full_path_mis: bool = False):
+                   max_depth: int = 8, light_paths: int = 0, seed: int = 1, full_path_mis: bool = False,
+                   time_budget_s: float = 0.0):
         """VCMTracer renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats).
         ``full_path_mis`` evaluates merges with the reference's whole-path loops
-        (RX_VCM_FULL_PATH_MIS) instead of the per-subpath records."""
+        (RX_VCM_FULL_PATH_MIS) instead of the per-subpath records. ``time_budget_s`` > 0
+        stops after the iteration during which that much wall time passed (the mean is
+        over the iterations done: stats["paths"] / pixels)."""
         cam = camera_struct(camera)
-        o = rx_vcm_options(iterations, max_depth, light_paths, 1 if full_path_mis else 0, radius, alpha, seed)
+        o = rx_vcm_options(iterations, max_depth, light_paths, 1 if full_path_mis else 0, radius, alpha, seed,
+                           float(time_budget_s), 0)
         film = np.zeros((camera.height, camera.width, 3), np.float64)
         st = rx_render_stats()
         self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
@@ -245,23 +254,25 @@ class Context:
                           ms=st.ms)
 
     def render_bpt(self, camera: "scenes.Camera", iterations: int, max_depth: int = 8, seed: int = 1,
-                   full_path_mis: bool = False):
+                   full_path_mis: bool = False, time_budget_s: float = 0.0):
         """BidirectionalPathTracer renderPixels for ``iterations`` samples per pixel:
         returns (mean (H,W,3) float64, stats). ``full_path_mis`` evaluates connections with
-        the reference's whole-path loops (RX_VCM_FULL_PATH_MIS)."""
+        the reference's whole-path loops (RX_VCM_FULL_PATH_MIS). ``time_budget_s`` as
+        render_vcm."""
         cam = camera_struct(camera)
-        o = rx_bpt_options(iterations, max_depth, 1 if full_path_mis else 0, 0, seed)
+        o = rx_bpt_options(iterations, max_depth, 1 if full_path_mis else 0, float(time_budget_s), seed)
         film = np.zeros((camera.height, camera.width, 3), np.float64)
         st = rx_render_stats()
         self._ck(self._L.rx_render_bpt(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
         return film, dict(rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms)
 
     def render_pm(self, camera: "scenes.Camera", iterations: int, radius: float, max_depth: int = 8,
-                  light_paths: int = 0, alpha: float = 0.0, seed: int = 1):
+                  light_paths: int = 0, alpha: float = 0.0, seed: int = 1, time_budget_s: float = 0.0):
         """PhotonMap renderPixels for ``iterations``: returns (mean (H,W,3) float64, stats);
-        ``alpha`` 0 is the reference's 2/3, ``light_paths`` 0 is width * height."""
+        ``alpha`` 0 is the reference's 2/3, ``light_paths`` 0 is width * height;
+        ``time_budget_s`` as render_vcm."""
         cam = camera_struct(camera)
-        o = rx_pm_options(iterations, max_depth, light_paths, 0, radius, alpha, seed)
+        o = rx_pm_options(iterations, max_depth, light_paths, 0, radius, alpha, seed, float(time_budget_s), 0)
         film = np.zeros((camera.height, camera.width, 3), np.float64)
         st = rx_render_stats()
         self._ck(self._L.rx_render_pm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))

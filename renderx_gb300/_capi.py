@@ -40,7 +40,7 @@ class rx_camera(ctypes.Structure):
 class rx_pt_options(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("rr_mode", ctypes.c_uint32),
                 ("nee", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("paths_per_pass", ctypes.c_uint32),
-                ("flags", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("time_budget_s", ctypes.c_float), ("reserved", ctypes.c_uint32)]
 
 
 class rx_config_info(ctypes.Structure):
@@ -64,18 +64,18 @@ class rx_batch_options(ctypes.Structure):
 class rx_vcm_options(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("light_paths", ctypes.c_uint32),
                 ("flags", ctypes.c_uint32), ("radius", ctypes.c_float), ("alpha", ctypes.c_float),
-                ("seed", ctypes.c_uint64)]
+                ("seed", ctypes.c_uint64), ("time_budget_s", ctypes.c_float), ("reserved", ctypes.c_uint32)]
 
 
 class rx_bpt_options(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("flags", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+                ("time_budget_s", ctypes.c_float), ("seed", ctypes.c_uint64)]
 
 
 class rx_pm_options(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("light_paths", ctypes.c_uint32),
                 ("flags", ctypes.c_uint32), ("radius", ctypes.c_float), ("alpha", ctypes.c_float),
-                ("seed", ctypes.c_uint64)]
+                ("seed", ctypes.c_uint64), ("time_budget_s", ctypes.c_float), ("reserved", ctypes.c_uint32)]
 
 
 class rx_render_stats(ctypes.Structure):

@@ -3,12 +3,14 @@
 // src/Renderer.cpp:47-126, src/ConfigManager.cpp:166-405), through the C ABI.
 //
 //   rx_render config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N]
-//             [--alpha A] [--seed S] [--guided] [--device D]
+//             [--alpha A] [--seed S] [--guided] [--time SECONDS] [--device D]
 //
 // The renderer type comes from the config (PathTracer / PT, PTtest, VCMTracer / VCM,
-// BidirectionalPathTracer / BPT, PhotonMap / PM). The reference renders until its <time>
-// budget runs out; here a fixed sample count (--spp, else <spp>, else 16; PT, PTtest and
-// BPT) or iteration count (--iterations, default 8; VCM and PM) is used.
+// BidirectionalPathTracer / BPT, PhotonMap / PM). As the reference, the render stops
+// after the pass or iteration during which its time budget ran out (--time, else the
+// config's <time> hours and minutes); the sample count (--spp, else <spp>, else 16 --
+// 65,536 under a time budget; PT, PTtest and BPT) or iteration count (--iterations, else
+// 8 -- 65,536 under a time budget; VCM and PM) caps it.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -28,12 +30,13 @@ int main(int argc, char** argv) {
   if (argc < 2 || !strcmp(argv[1], "-h") || !strcmp(argv[1], "--help")) {
     fprintf(stderr,
             "usage: %s config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N] [--alpha A]\n"
-            "       [--seed S] [--guided] [--device D]\n",
+            "       [--seed S] [--guided] [--time SECONDS] [--device D]\n",
             argv[0]);
     return 2;
   }
   std::string cfg = argv[1], out;
-  uint32_t spp = 0, iters = 8, light_paths = 0;
+  uint32_t spp = 0, iters = 0, light_paths = 0;
+  double time_s = 0;
   float alpha = 0.6667f;
   uint64_t seed = 1;
   int device = 0;
@@ -49,6 +52,7 @@ int main(int argc, char** argv) {
     else if (a == "--seed") seed = strtoull(next(), nullptr, 10);
     else if (a == "--device") device = atoi(next());
     else if (a == "--guided") guided = true;
+    else if (a == "--time") time_s = atof(next());
     else {
       fprintf(stderr, "rx_render: unknown option %s\n", a.c_str());
       return 2;
@@ -66,9 +70,13 @@ int main(int argc, char** argv) {
   const uint32_t w = info.camera.width, h = info.camera.height;
   std::vector<double> film(3 * (size_t)w * h);
   rx_render_stats st{};
+  if (time_s <= 0) time_s = info.runtime_s;
+  const float budget = time_s > 0 ? (float)time_s : 0.0f;
+  const uint32_t uncapped = 1u << 16;  // the cap under a time budget when none is given
+  if (!spp) spp = info.spp ? info.spp : (budget > 0 ? uncapped : 16u);
+  if (!iters) iters = budget > 0 ? uncapped : 8u;
   if (info.estimator == 0 || info.estimator == 1) {
-    rx_pt_options po = {spp ? spp : (info.spp ? info.spp : 16u), info.max_depth, 0, (uint32_t)info.estimator, seed,
-                        0, 0};
+    rx_pt_options po = {spp, info.max_depth, 0, (uint32_t)info.estimator, seed, 0, 0, budget, 0};
     if (guided) {
       if (info.estimator != 0) return fail(c, "--guided applies to PathTracer");
       rx_guide_options go = {5e-3f, 0.5f, 1u << 18, 4, 16, 1, seed};
@@ -76,27 +84,29 @@ int main(int argc, char** argv) {
       po.flags = RX_PT_GUIDED;
     }
     if (rx_render_pt(c, &info.camera, &po, film.data(), nullptr, &st) != RX_OK) return fail(c, "rendering");
-    printf("%s: %u x %u, %u spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h, po.spp,
-           po.max_depth, st.ms, (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
+    printf("%s: %u x %u, %.2f spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
+           (double)st.paths / ((double)w * h), po.max_depth, st.ms,
+           (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
   } else if (info.estimator == 2) {
     float r = info.radius > 0 ? info.radius : 0.01f;
-    rx_vcm_options vo = {iters, info.max_depth > 21 ? 21u : info.max_depth, light_paths, 0, r, alpha, seed};
+    rx_vcm_options vo = {iters, info.max_depth > 21 ? 21u : info.max_depth, light_paths, 0, r, alpha, seed, budget, 0};
     if (rx_render_vcm(c, &info.camera, &vo, film.data(), &st) != RX_OK) return fail(c, "rendering");
-    printf("%s: %u x %u, %u iterations, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
-           iters, vo.max_depth, st.ms, (unsigned long long)st.extension_rays, load_s);
+    printf("%s: %u x %u, %llu iterations, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w,
+           h, (unsigned long long)(st.paths / ((uint64_t)w * h)), vo.max_depth, st.ms,
+           (unsigned long long)st.extension_rays, load_s);
   } else if (info.estimator == 3) {
-    rx_bpt_options bo3 = {spp ? spp : (info.spp ? info.spp : 16u), info.max_depth > 21 ? 21u : info.max_depth, 0, 0,
-                          seed};
+    rx_bpt_options bo3 = {spp, info.max_depth > 21 ? 21u : info.max_depth, 0, budget, seed};
     if (rx_render_bpt(c, &info.camera, &bo3, film.data(), &st) != RX_OK) return fail(c, "rendering");
-    printf("%s: %u x %u, %u spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
-           bo3.iterations, bo3.max_depth, st.ms, (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
+    printf("%s: %u x %u, %llu spp, depth %u: %.1f ms, %llu rays (load + build %.2f s)\n", info.renderer, w, h,
+           (unsigned long long)(st.paths / ((uint64_t)w * h)), bo3.max_depth, st.ms,
+           (unsigned long long)(st.extension_rays + st.shadow_rays), load_s);
   } else if (info.estimator == 4) {
     float r = info.radius > 0 ? info.radius : 0.01f;
-    rx_pm_options pm = {iters, info.max_depth > 21 ? 21u : info.max_depth, light_paths, 0, r, 0.0f, seed};
+    rx_pm_options pm = {iters, info.max_depth > 21 ? 21u : info.max_depth, light_paths, 0, r, 0.0f, seed, budget, 0};
     if (rx_render_pm(c, &info.camera, &pm, film.data(), &st) != RX_OK) return fail(c, "rendering");
-    printf("%s: %u x %u, %u iterations, depth %u: %.1f ms, %llu rays, %llu photons (load + build %.2f s)\n",
-           info.renderer, w, h, iters, pm.max_depth, st.ms, (unsigned long long)st.extension_rays,
-           (unsigned long long)st.merges, load_s);
+    printf("%s: %u x %u, %llu iterations, depth %u: %.1f ms, %llu rays, %llu photons (load + build %.2f s)\n",
+           info.renderer, w, h, (unsigned long long)(st.paths / ((uint64_t)w * h)), pm.max_depth, st.ms,
+           (unsigned long long)st.extension_rays, (unsigned long long)st.merges, load_s);
   } else {
     fprintf(stderr, "rx_render: renderer type '%s' is not on this library's path\n", info.renderer);
     rx_destroy(c);

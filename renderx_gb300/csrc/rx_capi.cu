@@ -355,6 +355,7 @@ rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options*
   if (opts->max_depth > 1000) return c->fail(RX_ERR_INVALID, "max_depth too large");
   if (opts->nee && c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
   if (opts->flags & ~RX_PT_GUIDED) return c->fail(RX_ERR_INVALID, "unknown flags");
+  if (!(opts->time_budget_s >= 0.0f)) return c->fail(RX_ERR_INVALID, "time_budget_s must be >= 0");
   if (opts->flags & RX_PT_GUIDED) {
     if (opts->nee) return c->fail(RX_ERR_INVALID, "guiding applies to PathTracer (nee = 0)");
     if (!rx::guide_ready(c->guide)) return c->fail(RX_ERR_STATE, "guided rendering needs rx_guide_init");
@@ -371,12 +372,16 @@ rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options*
   if ((s = c->cuda(rx::render_pt(c, *cam, *opts, sum.as<double>(), film_sq ? sq.as<double>() : nullptr, &st, c->stream),
                    "render_pt")) != RX_OK)
     return s;
+  // paths run sample-major: with st.paths done, pixel q holds done / np samples, one
+  // more when q < done % np (every pixel holds spp when the render completed)
+  const uint64_t done = st.paths;
+  auto count = [&](size_t q) { return (double)(done / np + (q < done % np ? 1 : 0)); };
   std::vector<double> h(np * 3);
   if ((s = c->cuda(cudaMemcpy(h.data(), sum.p, sum.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
-  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->spp;
+  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = count(k / 3) > 0 ? h[k] / count(k / 3) : 0.0;
   if (film_sq) {
     if ((s = c->cuda(cudaMemcpy(h.data(), sq.p, sq.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
-    for (size_t k = 0; k < h.size(); k++) film_sq[k] = h[k] / opts->spp;
+    for (size_t k = 0; k < h.size(); k++) film_sq[k] = count(k / 3) > 0 ? h[k] / count(k / 3) : 0.0;
   }
   if (stats) *stats = st;
   return RX_OK;
@@ -397,6 +402,7 @@ rx_status rx_render_pt_batch(rx_context* c, const rx_batch_item* items, uint32_t
     const rx_camera& cam = it.camera;
     if (cam.width == 0 || cam.height == 0 || cam.sight_dist == 0) return c->fail(RX_ERR_INVALID, "bad camera");
     if (it.options.spp == 0 || it.options.max_depth > 1000) return c->fail(RX_ERR_INVALID, "bad spp or max_depth");
+    if (it.options.time_budget_s != 0.0f) return c->fail(RX_ERR_INVALID, "time_budget_s applies to rx_render_pt only");
     if (it.options.nee && it.scene->scene.num_lights == 0)
       return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
     jobs[k] = rx::PtJob{it.scene, cam, it.options, pixels};
@@ -441,6 +447,7 @@ static rx_status render_bidirectional(rx_context* c, const rx_camera* cam, const
   if (opts->iterations == 0) return c->fail(RX_ERR_INVALID, "iterations must be positive");
   if (opts->max_depth > 21) return c->fail(RX_ERR_INVALID, "max_depth must be at most 21");
   if (!(opts->radius > 0.0f) || !(opts->alpha > 0.0f)) return c->fail(RX_ERR_INVALID, "radius and alpha must be positive");
+  if (!(opts->time_budget_s >= 0.0f) || opts->reserved) return c->fail(RX_ERR_INVALID, "time_budget_s >= 0, reserved 0");
   if (c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "vertex connection and merging needs an emitter");
   DeviceGuard g(c->device);
   size_t np = (size_t)cam->width * cam->height;
@@ -452,7 +459,8 @@ static rx_status render_bidirectional(rx_context* c, const rx_camera* cam, const
   if ((s = c->cuda(rx::render_vcm(c, *cam, *opts, film.as<double>(), &st, c->stream), "render_vcm")) != RX_OK) return s;
   std::vector<double> h(np * 3);
   if ((s = c->cuda(cudaMemcpy(h.data(), film.p, film.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
-  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->iterations;
+  const double iters = (double)(st.paths / np);  // iterations done (fewer under a time budget)
+  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / iters;
   if (stats) *stats = st;
   return RX_OK;
 }
@@ -468,8 +476,10 @@ rx_status rx_render_bpt(rx_context* c, const rx_camera* cam, const rx_bpt_option
                         rx_render_stats* stats) {
   if (!c) return RX_ERR_INVALID;
   if (!opts) return c->fail(RX_ERR_INVALID, "null argument");
-  if ((opts->flags & ~RX_VCM_FULL_PATH_MIS) || opts->reserved) return c->fail(RX_ERR_INVALID, "unknown BPT flags");
-  rx_vcm_options v{opts->iterations, opts->max_depth, 0u, opts->flags | rx::kVcmBidirectional, 1.0f, 1.0f, opts->seed};
+  if (opts->flags & ~RX_VCM_FULL_PATH_MIS) return c->fail(RX_ERR_INVALID, "unknown BPT flags");
+  rx_vcm_options v{opts->iterations, opts->max_depth, 0u,        opts->flags | rx::kVcmBidirectional,
+                   1.0f,             1.0f,            opts->seed, opts->time_budget_s,
+                   0u};
   return render_bidirectional(c, cam, &v, film_rgb, stats);
 }
 
@@ -483,6 +493,7 @@ rx_status rx_render_pm(rx_context* c, const rx_camera* cam, const rx_pm_options*
   if (opts->max_depth > 21) return c->fail(RX_ERR_INVALID, "max_depth must be at most 21");
   if (!(opts->radius > 0.0f) || !(opts->alpha >= 0.0f) || opts->flags)
     return c->fail(RX_ERR_INVALID, "radius must be positive, alpha non-negative, flags 0");
+  if (!(opts->time_budget_s >= 0.0f) || opts->reserved) return c->fail(RX_ERR_INVALID, "time_budget_s >= 0, reserved 0");
   if (c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "photon mapping needs an emitter");
   DeviceGuard g(c->device);
   size_t np = (size_t)cam->width * cam->height;
@@ -494,7 +505,8 @@ rx_status rx_render_pm(rx_context* c, const rx_camera* cam, const rx_pm_options*
   if ((s = c->cuda(rx::render_pm(c, *cam, *opts, film.as<double>(), &st, c->stream), "render_pm")) != RX_OK) return s;
   std::vector<double> h(np * 3);
   if ((s = c->cuda(cudaMemcpy(h.data(), film.p, film.bytes, cudaMemcpyDeviceToHost), "film copy")) != RX_OK) return s;
-  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / opts->iterations;
+  const double iters = (double)(st.paths / np);  // iterations done (fewer under a time budget)
+  for (size_t k = 0; k < h.size(); k++) film_rgb[k] = h[k] / iters;
   if (stats) *stats = st;
   return RX_OK;
 }

@@ -172,6 +172,8 @@ struct PtRun {
   bool autotune = false;        // time launch shapes on the first passes
   bool bin = false;             // bin bounce rays by origin cell and direction before each extend
                                 // (measured slower for path tracing: off)
+  double time_budget_s = 0;     // > 0: stop launching passes once this much wall time has
+                                // passed (checked as each pass is queued, one pass in flight)
 };
 // Renders all jobs in one wavefront into device films (sum, optional sum of squares).
 cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun& run, double* film_sum,

@@ -9,6 +9,7 @@
 // with an inline shadow ray, Russian roulette) with queue compaction by warp ballot +
 // one atomic per warp. Film accumulation is FP64.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <vector>
 
@@ -632,6 +633,19 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   uint64_t pass = 0;
+  // time budget: after queueing pass p, wait for pass p - 1 and stop if the wall time is
+  // spent (pass p still completes)
+  const auto t_start = std::chrono::steady_clock::now();
+  cudaEvent_t pass_ev[2] = {nullptr, nullptr};
+  if (run.time_budget_s > 0)
+    for (auto& ev : pass_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  auto budget_spent = [&](uint64_t p) -> bool {
+    if (run.time_budget_s <= 0) return false;
+    cudaEventRecord(pass_ev[p & 1], s);
+    if (p == 0) return false;
+    cudaEventSynchronize(pass_ev[(p - 1) & 1]);
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= run.time_budget_s;
+  };
   if (!cands.empty()) {
     float best_t = INFINITY;
     cudaEvent_t t0, t1;
@@ -663,12 +677,18 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
         cudaGraphDestroy(graph);
         return e;
       }
-      for (; pass < npasses && e == cudaSuccess; pass++) e = cudaGraphLaunch(exec, s);
+      while (pass < npasses && e == cudaSuccess) {
+        e = cudaGraphLaunch(exec, s);
+        if (budget_spent(pass++)) break;
+      }
       cudaGraphExecDestroy(exec);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) return e;
     } else {
-      for (; pass < npasses; pass++) enqueue_pass_shape(W, best, sms, s);
+      while (pass < npasses) {
+        enqueue_pass_shape(W, best, sms, s);
+        if (budget_spent(pass++)) break;
+      }
     }
   } else {
     const int grid = sms * best.blocks_per_sm;
@@ -718,6 +738,10 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
           return e;
       }
       k_advance<<<1, 1, 0, s>>>(W.ps);
+      if (budget_spent(pass)) {
+        pass++;
+        break;
+      }
     }
   }
   cudaEventRecord(e1, s);
@@ -728,12 +752,14 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  for (auto ev : pass_ev)
+    if (ev) cudaEventDestroy(ev);
   if (stats) {
     unsigned long long h[2];
     cudaMemcpy(h, W.ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0];
     stats->shadow_rays = h[1];
-    stats->paths = total;
+    stats->paths = std::min<uint64_t>(total, pass * (uint64_t)per_pass);
     stats->ms = ms;
   }
   return cudaSuccess;
@@ -746,6 +772,7 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
   run.paths_per_pass = opt.paths_per_pass;
   run.guided = (opt.flags & RX_PT_GUIDED) != 0;
   run.use_graph = true;
+  run.time_budget_s = opt.time_budget_s > 0 ? opt.time_budget_s : 0;
   return render_pt_jobs(c, &job, 1, run, film_sum, film_sq, stats, nullptr, s);
 }
 

@@ -22,6 +22,7 @@
 // as eye paths, the connection weight without merge techniques, and its own rule for
 // the pure path-tracing technique (VcmParams::bpt).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -1532,6 +1533,8 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   unsigned long long merges = 0;
   unsigned nscan = buckets + 1;
   unsigned nblk = (nscan + 1023) / 1024;
+  const auto t_start = std::chrono::steady_clock::now();
+  uint32_t done = 0;
   for (uint32_t it = 0; it < opt.iterations; it++) {
     radius *= powf(((float)it + opt.alpha) / ((float)it + 1.0f), 1.0f / 3.0f);  // VCMTracer.cpp:29-30
     P.radius = radius;
@@ -1641,6 +1644,12 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
       }
     }
     k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
+    done = it + 1;
+    if (opt.time_budget_s > 0) {  // the reference's runtime check after each iteration
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+      if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= opt.time_budget_s)
+        break;
+    }
   }
   cudaEventRecord(e1, s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -1655,7 +1664,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     stats->extension_rays = h[0] + h[1];
     stats->shadow_rays = h[2];
     stats->merges = merges;
-    stats->paths = (uint64_t)P.n_pixels * opt.iterations;
+    stats->paths = (uint64_t)P.n_pixels * done;
     stats->ms = ms;
   }
   return cudaSuccess;
@@ -1703,6 +1712,8 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   unsigned long long photons = 0;
+  const auto t_start = std::chrono::steady_clock::now();
+  uint32_t done = 0;
   for (uint32_t it = 0; it < opt.iterations; it++) {
     P.iter = it;
     P.radius = fmaxf(opt.radius * powf(powf((float)(it + 1), alpha - 1.0f), 1.0f / 3.0f), 1e-5f);
@@ -1729,6 +1740,10 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
     cudaMemcpyAsync(&np, nph, sizeof np, cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     photons += std::min(np, cap);
+    done = it + 1;
+    if (opt.time_budget_s > 0 &&
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= opt.time_budget_s)
+      break;
   }
   cudaEventRecord(e1, s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -1743,7 +1758,7 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
     stats->extension_rays = h[0] + h[1];
     stats->shadow_rays = 0;
     stats->merges = photons;
-    stats->paths = (uint64_t)P.n_pixels * opt.iterations;
+    stats->paths = (uint64_t)P.n_pixels * done;
     stats->ms = ms;
   }
   return cudaSuccess;
