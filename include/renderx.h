@@ -269,6 +269,19 @@ rx_status rx_scene_load_config(rx_context* ctx, const char* config_path, rx_conf
  * values, rows from the top, written as a little-endian PFM with rows from the bottom. */
 rx_status rx_write_pfm(const char* path, uint32_t width, uint32_t height, const double* rgb);
 
+/* Time-stamped convergence snapshots (MCRenderer::showCurrentResult with time and
+ * iteration, reference src/MCRenderer.cpp:465-490, called every timeStep seconds from
+ * the renderers' loops, e.g. src/PathTracer.cpp:75-82). With every_s > 0 and fn set,
+ * the next rx_render_pt (single scene), rx_render_vcm, rx_render_bpt and rx_render_pm
+ * calls invoke fn after the pass or iteration during which the elapsed wall time
+ * reached each next multiple of every_s: elapsed_s, samples = samples per pixel (path
+ * tracing: paths done / pixels) or iterations done, and the running mean so far as
+ * width*height*3 RGB values, rows from the top, valid during the call. The render
+ * waits for the device before each snapshot. every_s = 0 or fn = NULL turns them off. */
+typedef void (*rx_snapshot_fn)(void* user, double elapsed_s, double samples, const double* film_rgb, uint32_t width,
+                               uint32_t height);
+rx_status rx_set_snapshots(rx_context* ctx, double every_s, rx_snapshot_fn fn, void* user);
+
 /* ---- closest hit --------------------------------------------------------------- */
 /* KDTree::intersect(ray, triangleID, NULL) (reference include/KDTree.h:50,
  * src/KDTree.cpp:408-412) over a batch, host buffers: out_tid[i] = global triangle id

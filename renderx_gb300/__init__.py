@@ -281,6 +281,22 @@ class Context:
     def set_trace_config(self, variant: int = 4, blocks_per_sm: int = 12):
         self._ck(self._L.rx_trace_set_config(self.h, variant, blocks_per_sm))
 
+    def set_snapshots(self, every_s: float, fn=None):
+        """Convergence snapshots of the following renders (rx_set_snapshots): fn(elapsed_s,
+        samples, mean (H,W,3) float64 copy) after the pass or iteration during which the
+        elapsed wall time reached each next multiple of every_s; every_s = 0 or fn None
+        turns them off."""
+        if fn is None or every_s <= 0:
+            self._snap_cb = None
+            self._ck(self._L.rx_set_snapshots(self.h, 0.0, _capi.SNAPSHOT_FN(), None))
+            return
+
+        def cb(_user, elapsed, samples, film, w, h):
+            fn(elapsed, samples, np.ctypeslib.as_array(film, shape=(h * w * 3,)).reshape(h, w, 3).copy())
+
+        self._snap_cb = _capi.SNAPSHOT_FN(cb)  # kept alive while the library may call it
+        self._ck(self._L.rx_set_snapshots(self.h, float(every_s), self._snap_cb, None))
+
     def set_trace_staging(self, chunk_rays: int = 0):
         """Rays per staged chunk of the host-buffer call (0 = default 2^23)."""
         self._ck(self._L.rx_trace_set_staging(self.h, int(chunk_rays)))

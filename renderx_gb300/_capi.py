@@ -98,6 +98,8 @@ _LIB = None
 
 # (name, restype, argtypes) of every exported entry point of include/renderx.h
 P, U32, I32, S = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int
+# rx_snapshot_fn(user, elapsed_s, samples, film_rgb, width, height)
+SNAPSHOT_FN = ctypes.CFUNCTYPE(None, P, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double), U32, U32)
 SIGNATURES = [
     ("rx_create", S, [ctypes.POINTER(P), S]),
     ("rx_destroy", None, [P]),
@@ -113,6 +115,7 @@ SIGNATURES = [
     ("rx_host_scene_arrays", S, [P, P, P, P, P, P, P, P, P, P]),
     ("rx_scene_load_config", S, [P, ctypes.c_char_p, P]),
     ("rx_write_pfm", S, [ctypes.c_char_p, U32, U32, P]),
+    ("rx_set_snapshots", S, [P, ctypes.c_double, SNAPSHOT_FN, P]),
     ("rx_trace_closest", S, [P, P, U32, P, P]),
     ("rx_trace_closest_device", S, [P, P, U32, P, P, P]),
     ("rx_trace_closest_noalloc", S, [P, P, U32, P, P, P]),

@@ -3,14 +3,19 @@
 // src/Renderer.cpp:47-126, src/ConfigManager.cpp:166-405), through the C ABI.
 //
 //   rx_render config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N]
-//             [--alpha A] [--seed S] [--guided] [--time SECONDS] [--device D]
+//             [--alpha A] [--seed S] [--guided] [--time SECONDS] [--snapshot-every SECONDS]
+//             [--device D]
 //
 // The renderer type comes from the config (PathTracer / PT, PTtest, VCMTracer / VCM,
 // BidirectionalPathTracer / BPT, PhotonMap / PM). As the reference, the render stops
 // after the pass or iteration during which its time budget ran out (--time, else the
 // config's <time> hours and minutes); the sample count (--spp, else <spp>, else 16 --
 // 65,536 under a time budget; PT, PTtest and BPT) or iteration count (--iterations, else
-// 8 -- 65,536 under a time budget; VCM and PM) caps it.
+// 8 -- 65,536 under a time budget; VCM and PM) caps it. Convergence snapshots go to
+// <out stem>_time_<seconds>_iter_<s>.pfm every --snapshot-every seconds (default: the
+// reference's 300 s timeStep under a time budget, else none; s = samples or iterations
+// done - 1, the reference's loop index), the names MCRenderer::showCurrentResult writes
+// (reference src/MCRenderer.cpp:465-490) and cmp/compare.cpp's calcRMSEs parses.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -19,6 +24,17 @@
 #include <vector>
 
 #include "renderx.h"
+
+struct SnapshotFiles {
+  std::string stem;
+};
+
+static void write_snapshot(void* user, double elapsed_s, double samples, const double* rgb, uint32_t w, uint32_t h) {
+  const SnapshotFiles* f = static_cast<const SnapshotFiles*>(user);
+  char name[1024];
+  snprintf(name, sizeof name, "%s_time_%u_iter_%d.pfm", f->stem.c_str(), (unsigned)elapsed_s, (int)samples - 1);
+  if (rx_write_pfm(name, w, h, rgb) == RX_OK) printf("snapshot %s\n", name);
+}
 
 static int fail(rx_context* c, const char* what) {
   fprintf(stderr, "rx_render: %s: %s\n", what, c ? rx_last_error(c) : "");
@@ -30,13 +46,13 @@ int main(int argc, char** argv) {
   if (argc < 2 || !strcmp(argv[1], "-h") || !strcmp(argv[1], "--help")) {
     fprintf(stderr,
             "usage: %s config.xml [--out image.pfm] [--spp N] [--iterations N] [--light-paths N] [--alpha A]\n"
-            "       [--seed S] [--guided] [--time SECONDS] [--device D]\n",
+            "       [--seed S] [--guided] [--time SECONDS] [--snapshot-every SECONDS] [--device D]\n",
             argv[0]);
     return 2;
   }
   std::string cfg = argv[1], out;
   uint32_t spp = 0, iters = 0, light_paths = 0;
-  double time_s = 0;
+  double time_s = 0, snap_s = -1;
   float alpha = 0.6667f;
   uint64_t seed = 1;
   int device = 0;
@@ -53,6 +69,7 @@ int main(int argc, char** argv) {
     else if (a == "--device") device = atoi(next());
     else if (a == "--guided") guided = true;
     else if (a == "--time") time_s = atof(next());
+    else if (a == "--snapshot-every") snap_s = atof(next());
     else {
       fprintf(stderr, "rx_render: unknown option %s\n", a.c_str());
       return 2;
@@ -75,6 +92,10 @@ int main(int argc, char** argv) {
   const uint32_t uncapped = 1u << 16;  // the cap under a time budget when none is given
   if (!spp) spp = info.spp ? info.spp : (budget > 0 ? uncapped : 16u);
   if (!iters) iters = budget > 0 ? uncapped : 8u;
+  if (snap_s < 0) snap_s = budget > 0 ? 300.0 : 0.0;  // MCRenderer: timeStep = lastTime = 300
+  SnapshotFiles snap_files{out.substr(0, out.rfind('.') == std::string::npos ? out.size() : out.rfind('.'))};
+  if (snap_s > 0 && rx_set_snapshots(c, snap_s, write_snapshot, &snap_files) != RX_OK)
+    return fail(c, "snapshots");
   if (info.estimator == 0 || info.estimator == 1) {
     rx_pt_options po = {spp, info.max_depth, 0, (uint32_t)info.estimator, seed, 0, 0, budget, 0};
     if (guided) {

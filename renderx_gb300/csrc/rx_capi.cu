@@ -602,6 +602,15 @@ rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, 
 // kernels (2^23 rays per chunk by default: large enough for binning and the persistent
 // walk; for a 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for
 // one whole-batch copy, trace and copy back).
+rx_status rx_set_snapshots(rx_context* c, double every_s, rx_snapshot_fn fn, void* user) {
+  if (!c) return RX_ERR_INVALID;
+  if (!(every_s >= 0.0)) return c->fail(RX_ERR_INVALID, "every_s must be >= 0");
+  c->snap_every = fn ? every_s : 0.0;
+  c->snap_fn = every_s > 0 ? fn : nullptr;
+  c->snap_user = user;
+  return RX_OK;
+}
+
 rx_status rx_trace_set_staging(rx_context* c, uint32_t chunk_rays) {
   if (!c) return RX_ERR_INVALID;
   if (chunk_rays != 0 && chunk_rays < (1u << 16)) return c->fail(RX_ERR_INVALID, "chunk_rays: 0 or at least 65536");

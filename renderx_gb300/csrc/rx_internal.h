@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -143,6 +144,10 @@ struct rx_context {
   bool timing_on = false;
   // learned guiding (rx_guide.cu)
   rx::GuideState* guide = nullptr;
+  // convergence snapshots (rx_set_snapshots)
+  double snap_every = 0;
+  rx_snapshot_fn snap_fn = nullptr;
+  void* snap_user = nullptr;
 
   rx_status build_scene();
   rx_status fail(rx_status s, const std::string& m) {
@@ -157,6 +162,38 @@ struct rx_context {
 };
 
 namespace rx {
+// Convergence snapshots of one render (rx_set_snapshots): `due` after each pass or
+// iteration; `take` waits for the stream, copies the device film sum and hands the mean
+// (sum / count(pixel)) to the context's callback.
+struct Snapshots {
+  const rx_context* c;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  double next;
+  std::vector<double> sum, mean;
+  explicit Snapshots(const rx_context* ctx) : c(ctx), next(ctx->snap_every) {}
+  bool on() const { return c->snap_fn && c->snap_every > 0; }
+  double elapsed() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+  bool due() const { return on() && elapsed() >= next; }
+  template <class Count>
+  cudaError_t take(const double* film_sum, uint32_t w, uint32_t h, double samples, Count&& count, cudaStream_t s) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    const size_t np = (size_t)w * h;
+    sum.resize(3 * np);
+    mean.resize(3 * np);
+    if ((e = cudaMemcpy(sum.data(), film_sum, 3 * np * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return e;
+    for (size_t k = 0; k < 3 * np; k++) {
+      const double n = count(k / 3);
+      mean[k] = n > 0 ? sum[k] / n : 0.0;
+    }
+    const double t = elapsed();
+    c->snap_fn(c->snap_user, t, samples, mean.data(), w, h);
+    while (next <= t) next += c->snap_every;
+    return cudaSuccess;
+  }
+};
+
 // One scene of a path-traced render: a context with a built scene, its camera and options,
 // and the offset (pixels) of its image in the shared film.
 struct PtJob {

@@ -646,6 +646,20 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     cudaEventSynchronize(pass_ev[(p - 1) & 1]);
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= run.time_budget_s;
   };
+  // after queueing pass p: a due convergence snapshot (the film through pass p; one
+  // scene only), then the budget; true = stop (e holds an error, if any)
+  Snapshots snaps(c);
+  const bool snap_on = nj == 1 && snaps.on();
+  auto after_pass = [&](uint64_t p) -> bool {
+    if (snap_on && snaps.due()) {
+      const uint64_t done = std::min<uint64_t>(total, (p + 1) * (uint64_t)per_pass);
+      const uint64_t npx = recs[0].P.pixels;
+      e = snaps.take(film_sum, jobs[0].cam.width, jobs[0].cam.height, (double)done / (double)npx,
+                     [&](size_t q) { return (double)(done / npx + (q < done % npx ? 1 : 0)); }, s);
+      if (e != cudaSuccess) return true;
+    }
+    return budget_spent(p);
+  };
   if (!cands.empty()) {
     float best_t = INFINITY;
     cudaEvent_t t0, t1;
@@ -679,7 +693,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       }
       while (pass < npasses && e == cudaSuccess) {
         e = cudaGraphLaunch(exec, s);
-        if (budget_spent(pass++)) break;
+        if (e == cudaSuccess && after_pass(pass++)) break;
       }
       cudaGraphExecDestroy(exec);
       cudaGraphDestroy(graph);
@@ -687,8 +701,9 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     } else {
       while (pass < npasses) {
         enqueue_pass_shape(W, best, sms, s);
-        if (budget_spent(pass++)) break;
+        if (after_pass(pass++)) break;
       }
+      if (e != cudaSuccess) return e;
     }
   } else {
     const int grid = sms * best.blocks_per_sm;
@@ -738,11 +753,12 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
           return e;
       }
       k_advance<<<1, 1, 0, s>>>(W.ps);
-      if (budget_spent(pass)) {
+      if (after_pass(pass)) {
         pass++;
         break;
       }
     }
+    if (e != cudaSuccess) return e;
   }
   cudaEventRecord(e1, s);
   e = cudaGetLastError();

@@ -1535,6 +1535,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   unsigned nblk = (nscan + 1023) / 1024;
   const auto t_start = std::chrono::steady_clock::now();
   uint32_t done = 0;
+  Snapshots snaps(c);
   for (uint32_t it = 0; it < opt.iterations; it++) {
     radius *= powf(((float)it + opt.alpha) / ((float)it + 1.0f), 1.0f / 3.0f);  // VCMTracer.cpp:29-30
     P.radius = radius;
@@ -1645,6 +1646,10 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     }
     k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
     done = it + 1;
+    if (snaps.due()) {
+      const double n = done;
+      if ((e = snaps.take(film, cam.width, cam.height, n, [&](size_t) { return n; }, s)) != cudaSuccess) return e;
+    }
     if (opt.time_budget_s > 0) {  // the reference's runtime check after each iteration
       if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
       if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= opt.time_budget_s)
@@ -1714,6 +1719,7 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
   unsigned long long photons = 0;
   const auto t_start = std::chrono::steady_clock::now();
   uint32_t done = 0;
+  Snapshots snaps(c);
   for (uint32_t it = 0; it < opt.iterations; it++) {
     P.iter = it;
     P.radius = fmaxf(opt.radius * powf(powf((float)(it + 1), alpha - 1.0f), 1.0f / 3.0f), 1e-5f);
@@ -1741,6 +1747,10 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     photons += std::min(np, cap);
     done = it + 1;
+    if (snaps.due()) {
+      const double n = done;
+      if ((e = snaps.take(film, cam.width, cam.height, n, [&](size_t) { return n; }, s)) != cudaSuccess) return e;
+    }
     if (opt.time_budget_s > 0 &&
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= opt.time_budget_s)
       break;

@@ -9,9 +9,16 @@
   the squared RGB distance (without the [0,4] clamp of visualizeUtils.h's reader).
 * ``relmse`` — mean over pixels and channels of (I-R)^2 / (R^2 + 1e-2).
 * ``save_png`` — 8-bit tone-mapped preview (gamma 2.2), no third-party imaging.
+* ``convergence`` / ``write_convergence`` / ``load_mask`` — cmp/compare.cpp's
+  calcRMSEs (:242-331): every ``*_time_<t>_iter_<s>.pfm`` snapshot (the names
+  MCRenderer::showCurrentResult writes, src/MCRenderer.cpp:465-490) against a reference
+  image, optionally inside a mask (whitespace-separated 0/1 per pixel, rows from the
+  bottom), sorted by time and written as ``time rmse`` lines.
 """
 from __future__ import annotations
 
+import glob
+import os
 import struct
 import zlib
 
@@ -63,3 +70,45 @@ def save_png(path: str, film: np.ndarray, exposure: float = 1.0):
     with open(path, "wb") as f:
         f.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
                 + chunk(b"IDAT", zlib.compress(raw, 9)) + chunk(b"IEND", b""))
+
+
+def snapshot_stamp(name: str):
+    """(time, iter) of a snapshot file name, or None: the tokens between '_' and '.'
+    that follow "time" and "iter" (compare.cpp's parser)."""
+    time = it = None
+    toks = name.replace(".", "_").split("_")
+    for a, b in zip(toks, toks[1:]):
+        if a == "time" and b.lstrip("-").isdigit():
+            time = int(b)
+        if a == "iter" and b.lstrip("-").isdigit():
+            it = int(b)
+    return None if time is None or it is None else (time, it)
+
+
+def load_mask(path: str, width: int, height: int) -> np.ndarray:
+    """compare.cpp's mask file: width*height integers, rows from the bottom; True = 1."""
+    vals = np.array(open(path).read().split(), np.int64)[: width * height]
+    return (vals.reshape(height, width) == 1)[::-1]
+
+
+def convergence(paths, ref: np.ndarray, mask: np.ndarray | None = None):
+    """[(time, iter, rmse, relmse)] of the stamped snapshots among ``paths`` (a list of
+    files or one directory), sorted by time."""
+    if isinstance(paths, str):
+        paths = sorted(glob.glob(os.path.join(paths, "*.pfm")))
+    rows = []
+    for p in paths:
+        st = snapshot_stamp(os.path.basename(p))
+        if st is None:
+            continue
+        img = load_pfm(p)
+        rows.append((st[0], st[1], rmse(img, ref, mask), relmse(img, ref)))
+    rows.sort(key=lambda r: r[0])
+    return rows
+
+
+def write_convergence(path: str, rows):
+    """compare.cpp's output: one "time rmse" line per snapshot."""
+    with open(path, "w") as f:
+        for t, _, e, _ in rows:
+            f.write(f"{t} {e:.8f}\n")

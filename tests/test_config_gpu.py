@@ -65,3 +65,18 @@ def test_cli_renders_config(tmp_path):
             want = fn(c)
         assert img3.mean() > 0
         assert np.allclose(img3, want.astype(np.float32), rtol=2e-3, atol=1e-5), typ
+
+
+def test_cli_writes_time_stamped_snapshots(tmp_path):
+    # MCRenderer::showCurrentResult's names <stem>_time_<t>_iter_<s>.pfm, read back by
+    # the convergence tooling; the last snapshot is the final image
+    sc = scenes.cornell_box(32, 32)
+    cfg = sceneio.write_config(sc, str(tmp_path), "PT", 8)
+    build.build()
+    out = str(tmp_path / "img.pfm")
+    r = subprocess.run([build.CLI, cfg, "--spp", "3", "--snapshot-every", "0.000001", "--out", out],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rows = film.convergence(str(tmp_path), film.load_pfm(out))
+    assert sorted(it for _, it, _, _ in rows)[-1] == 2
+    assert rows[-1][2] < 1e-6  # the last snapshot holds all three samples

@@ -76,3 +76,33 @@ def test_budget_rejects_negative_values():
             c.render_bpt(sc.camera, 2, time_budget_s=-1.0)
         with pytest.raises(rx.RxError):
             c.render_pm(sc.camera, 2, 0.1, time_budget_s=-1.0)
+
+
+def test_snapshots_hand_over_the_running_mean():
+    # MCRenderer::showCurrentResult(pixelColors, &time, &iter) every timeStep seconds:
+    # with a step far below one pass, one snapshot per pass / iteration, each equal to
+    # the fixed-count render of that many samples
+    sc = scenes.cornell_box(32, 32)
+    n = 32 * 32
+    got = []
+    with _ctx(sc) as c:
+        c.set_snapshots(1e-9, lambda t, s, img: got.append((t, s, img)))
+        c.render_pt(sc.camera, 3, max_depth=8, seed=5, paths_per_pass=n)
+        pt = list(got)
+        got.clear()
+        c.render_vcm(sc.camera, 3, 0.1, max_depth=8, seed=3)
+        vcm = list(got)
+        c.set_snapshots(0)
+        got.clear()
+        c.render_pt(sc.camera, 2, max_depth=8, seed=5, paths_per_pass=n)
+        assert not got
+        refs = [c.render_pt(sc.camera, k, max_depth=8, seed=5, paths_per_pass=n)[0] for k in (1, 2, 3)]
+        vrefs = [c.render_vcm(sc.camera, k, 0.1, max_depth=8, seed=3)[0] for k in (1, 2, 3)]
+    assert [s for _, s, _ in pt] == [1.0, 2.0, 3.0] and [s for _, s, _ in vcm] == [1.0, 2.0, 3.0]
+    for snaps in (pt, vcm):
+        ts = [t for t, _, _ in snaps]
+        assert ts == sorted(ts) and ts[0] > 0
+    for (_, _, img), ref in zip(pt, refs):
+        assert np.allclose(img, ref, rtol=1e-9, atol=1e-12)
+    for (_, _, img), ref in zip(vcm, vrefs):
+        np.testing.assert_allclose(img, ref, rtol=1e-5, atol=1e-6 * ref.max())
