@@ -14,8 +14,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
 #include <memory>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -301,45 +304,81 @@ bool load_mesh(const std::string& path, Mesh& m, std::string& err) {
   if (!read_file(path, text)) return err = "cannot read " + path, false;
   std::vector<float> pos, nrm;
   std::vector<int> corner_v, corner_n;
+  pos.reserve(text.size() / 12);
+  corner_v.reserve(text.size() / 8);
+  corner_n.reserve(text.size() / 8);
   const char* p = text.c_str();
-  while (*p) {
-    const char* eol = strchr(p, '\n');
-    std::string line(p, eol ? eol : p + strlen(p));
-    p = eol ? eol + 1 : p + strlen(p);
-    char tag[8] = {0};
-    int off = 0;
-    if (sscanf(line.c_str(), "%7s%n", tag, &off) != 1 || tag[0] == '#') continue;
-    const char* rest = line.c_str() + off;
-    if (!strcmp(tag, "v") || !strcmp(tag, "vn")) {
-      float x, y, z;
-      if (sscanf(rest, "%f %f %f", &x, &y, &z) != 3) continue;
-      if (tag[1] == 'n') {
-        float l = std::sqrt(x * x + y * y + z * z);
-        if (l > 0) x /= l, y /= l, z /= l;
-        nrm.insert(nrm.end(), {x, y, z});
-      } else {
-        pos.insert(pos.end(), {x, y, z});
+  const char* const end = p + text.size();
+  auto space = [](char ch) { return ch == ' ' || ch == '\t' || ch == '\r' || ch == '\v' || ch == '\f'; };
+  while (p < end) {
+    const char* eol = static_cast<const char*>(memchr(p, '\n', (size_t)(end - p)));
+    if (!eol) eol = end;
+    // the line's first token (the tag), as sscanf's %s
+    const char* t = p;
+    while (t < eol && space(*t)) t++;
+    const char* te = t;
+    while (te < eol && !space(*te)) te++;
+    const size_t tl = (size_t)(te - t);
+    const char* rest = te;
+    p = eol + 1;
+    if (tl == 0 || *t == '#') continue;
+    // numbers as strtof / strtol read them (what sscanf's %f / %d convert with); the
+    // text is NUL-terminated, so a number never reads past the buffer, and one that
+    // runs into the next line means the line held too few
+    if ((tl == 1 && t[0] == 'v') || (tl == 2 && t[0] == 'v' && t[1] == 'n')) {
+      float x[3];
+      int k = 0;
+      for (; k < 3; k++) {
+        char* ne;
+        x[k] = strtof(rest, &ne);
+        if (ne == rest || ne > eol) break;
+        rest = ne;
       }
-    } else if (!strcmp(tag, "f")) {
+      if (k != 3) continue;
+      if (tl == 2) {
+        float l = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        if (l > 0) x[0] /= l, x[1] /= l, x[2] /= l;
+        nrm.insert(nrm.end(), {x[0], x[1], x[2]});
+      } else {
+        pos.insert(pos.end(), {x[0], x[1], x[2]});
+      }
+    } else if (tl == 1 && t[0] == 'f') {
+      // corners "a", "a/b", "a/b/c", "a//c": a/b/c and a//c carry a normal, the rest
+      // only a position (the sscanf forms %d/%d/%d, %d//%d, %d tried in that order)
       int vi[4], ni[4], k = 0;
-      char tok[64];
-      int used = 0;
-      while (k < 4 && sscanf(rest, "%63s%n", tok, &used) == 1) {
-        rest += used;
-        int a = 0, b = 0, c = 0;
-        ni[k] = -1;
-        if (sscanf(tok, "%d/%d/%d", &a, &b, &c) == 3) vi[k] = a - 1, ni[k] = c - 1;
-        else if (sscanf(tok, "%d//%d", &a, &c) == 2) vi[k] = a - 1, ni[k] = c - 1;
-        else if (sscanf(tok, "%d", &a) == 1) vi[k] = a - 1;
-        else break;
+      while (k < 4) {
+        while (rest < eol && space(*rest)) rest++;
+        if (rest >= eol) break;
+        const char* tok_end = rest;
+        while (tok_end < eol && !space(*tok_end)) tok_end++;
+        char* ne;
+        long a = strtol(rest, &ne, 10);
+        if (ne == rest || ne > tok_end) break;
+        const char* q = ne;
+        long c = 0;
+        bool has_c = false;
+        if (q + 1 < tok_end && q[0] == '/' && q[1] == '/') {
+          c = strtol(q + 2, &ne, 10);
+          has_c = ne != q + 2 && ne <= tok_end && !space(q[2]);
+        } else if (q < tok_end && q[0] == '/') {
+          strtol(q + 1, &ne, 10);
+          if (ne != q + 1 && ne < tok_end && !space(q[1]) && ne[0] == '/') {
+            const char* r = ne + 1;
+            c = strtol(r, &ne, 10);
+            has_c = ne != r && ne <= tok_end && !space(*r);
+          }
+        }
+        vi[k] = (int)a - 1;
+        ni[k] = has_c ? (int)c - 1 : -1;
         k++;
+        rest = tok_end;
       }
       if (k < 3) continue;
       int tri[2][3] = {{0, 1, 2}, {0, 2, 3}};
-      for (int t = 0; t < (k == 4 ? 2 : 1); t++)
+      for (int f = 0; f < (k == 4 ? 2 : 1); f++)
         for (int q = 0; q < 3; q++) {
-          corner_v.push_back(vi[tri[t][q]]);
-          corner_n.push_back(ni[tri[t][q]]);
+          corner_v.push_back(vi[tri[f][q]]);
+          corner_n.push_back(ni[tri[f][q]]);
         }
     }
   }
@@ -600,16 +639,37 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
       if ((st = add_object(o, it->second, xform)) != RX_OK) return st;
     }
   }
-  for (auto& k : scene->kids) {
-    if (k->tag != "Object") continue;
+  // the <Object> meshes are read by a pool of threads, then added in document order
+  // (errors as a sequential reader meets them: an object's material before its mesh)
+  std::vector<const XNode*> objs;
+  for (auto& k : scene->kids)
+    if (k->tag == "Object") objs.push_back(k.get());
+  std::vector<Mesh> meshes(objs.size());
+  std::vector<std::string> mesh_err(objs.size());
+  std::vector<char> mesh_ok(objs.size(), 0);
+  {
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+      for (size_t i; (i = next.fetch_add(1)) < objs.size();) {
+        const char* fp = objs[i]->value("filePath");
+        if (fp) mesh_ok[i] = load_mesh(L.resolve(fp), meshes[i], mesh_err[i]);
+      }
+    };
+    const size_t nt = std::min<size_t>(objs.size(), std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+  }
+  for (size_t i = 0; i < objs.size(); i++) {
+    const XNode* k = objs[i];
     rx_object o;
-    rx_status st = resolve(k.get(), o);
+    rx_status st = resolve(k, o);
     if (st != RX_OK) return st;
-    const char* fp = k->value("filePath");
-    if (!fp) return err = "object without <filePath>", RX_ERR_INVALID;
-    Mesh m;
-    if (!load_mesh(L.resolve(fp), m, err)) return RX_ERR_INVALID;
-    if ((st = add_object(o, m, k->first("transform") ? k->value("transform") : nullptr)) != RX_OK) return st;
+    if (!k->value("filePath")) return err = "object without <filePath>", RX_ERR_INVALID;
+    if (!mesh_ok[i]) return err = mesh_err[i], RX_ERR_INVALID;
+    if ((st = add_object(o, meshes[i], k->first("transform") ? k->value("transform") : nullptr)) != RX_OK) return st;
+    meshes[i] = Mesh();  // release as we go
   }
   if (H.objs.empty()) return err = "scene has no objects", RX_ERR_INVALID;
   const XNode* cam = Loader::find(scene->kids, "Camera", sc->value("camera"));

@@ -101,6 +101,39 @@ def test_quads_texcoords_transform_and_material_reference(tmp_path):
     assert info["runtime_s"] == 3720 and info["save_path"] == "out.pfm"
 
 
+def _one_object(tmp_path, obj_text):
+    _write(tmp_path / "m.obj", obj_text)
+    _write(tmp_path / "scene.xml",
+           "<Scene Name=\"s\"><Object Name=\"m\"><filePath>m.obj</filePath><Material><type>Diffuse</type>"
+           "</Material></Object><Camera Name=\"c\"><width>4</width><height>4</height><sightDist>5</sightDist>"
+           "<focus>(0,0,0)</focus><position>(0,0,1)</position><up>(0,1,0)</up></Camera></Scene>\n")
+    _write(tmp_path / "config.xml", "<Config><Scene><path>scene.xml</path><name>s</name><camera>c</camera></Scene>"
+                                    "<Renderer><type>PT</type></Renderer></Config>\n")
+    return rx.config_read(str(tmp_path / "config.xml"))[0]
+
+
+def test_obj_line_forms_as_sscanf_reads_them(tmp_path):
+    # SimpleShape::loadShape reads lines with sscanf: a "v" needs three numbers on its own
+    # line (signs, tabs and CR allowed), corners "a", "a/b", "a/" carry no normal, at most
+    # four corners per face (a quad splits into (0,1,2), (0,2,3)), unknown tags are skipped
+    a = _one_object(tmp_path, "# c\nv 0 0 0\nv\t1 0 0\r\nv +0 1e0 0\nv 0 0\n1\nv 1 1 0\nvt 0 0\n"
+                              "usemtl x\nf 1 2 3\nf 1/9 2/ 4\r\nf 1 2 4 3 2\nf 1 2\n")
+    assert a["verts"].tolist() == [[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]]
+    assert a["tris"].tolist() == [[0, 1, 2], [0, 1, 3], [0, 1, 3], [0, 3, 2]]
+    assert a["objects"][0].has_vertex_normals == 0
+
+
+def test_obj_normals_split_shared_positions(tmp_path):
+    # a/b/c and a//c carry normal c (normalised); a position met again with another
+    # normal becomes its own vertex
+    a = _one_object(tmp_path, "v 0 0 0\nv 1 0 0\nv 0 1 0\nv 1 1 0\nvn 0 0 2\nvn 0 0 -1\n"
+                              "f 1/5/1 2/1/1 3/1/1\nf 1//2 2//2 4//2\n")
+    assert a["tris"].tolist() == [[0, 1, 2], [4, 5, 3]]
+    assert a["verts"].tolist() == [[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [0, 0, 0], [1, 0, 0]]
+    assert a["normals"].tolist() == [[0, 0, 1]] * 3 + [[0, 0, -1]] * 3
+    assert a["objects"][0].has_vertex_normals == 1
+
+
 def test_shp_mesh(tmp_path):
     v = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32)
     f = np.array([0, 1, 2], np.uint32)
