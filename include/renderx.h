@@ -102,7 +102,7 @@ typedef struct rx_pt_options {
                               0 in batch items. The equal-time comparisons of
                               MCRenderer's per-iteration timer (reference
                               include/MCRenderer.h:60, src/PathTracer.cpp:9,22). */
-  uint32_t reserved;
+  uint32_t reserved;       /* 0 */
 } rx_pt_options;
 
 /* rx_pt_options.flags: sample directions at diffuse / glossy / Phong vertices by

@@ -355,7 +355,7 @@ rx_status rx_render_pt(rx_context* c, const rx_camera* cam, const rx_pt_options*
   if (opts->max_depth > 1000) return c->fail(RX_ERR_INVALID, "max_depth too large");
   if (opts->nee && c->scene.num_lights == 0) return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
   if (opts->flags & ~RX_PT_GUIDED) return c->fail(RX_ERR_INVALID, "unknown flags");
-  if (!(opts->time_budget_s >= 0.0f)) return c->fail(RX_ERR_INVALID, "time_budget_s must be >= 0");
+  if (!(opts->time_budget_s >= 0.0f) || opts->reserved) return c->fail(RX_ERR_INVALID, "time_budget_s >= 0, reserved 0");
   if (opts->flags & RX_PT_GUIDED) {
     if (opts->nee) return c->fail(RX_ERR_INVALID, "guiding applies to PathTracer (nee = 0)");
     if (!rx::guide_ready(c->guide)) return c->fail(RX_ERR_STATE, "guided rendering needs rx_guide_init");
@@ -402,7 +402,8 @@ rx_status rx_render_pt_batch(rx_context* c, const rx_batch_item* items, uint32_t
     const rx_camera& cam = it.camera;
     if (cam.width == 0 || cam.height == 0 || cam.sight_dist == 0) return c->fail(RX_ERR_INVALID, "bad camera");
     if (it.options.spp == 0 || it.options.max_depth > 1000) return c->fail(RX_ERR_INVALID, "bad spp or max_depth");
-    if (it.options.time_budget_s != 0.0f) return c->fail(RX_ERR_INVALID, "time_budget_s applies to rx_render_pt only");
+    if (it.options.time_budget_s != 0.0f || it.options.reserved)
+      return c->fail(RX_ERR_INVALID, "time_budget_s applies to rx_render_pt only; reserved 0");
     if (it.options.nee && it.scene->scene.num_lights == 0)
       return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
     jobs[k] = rx::PtJob{it.scene, cam, it.options, pixels};
