@@ -598,11 +598,6 @@ rx_status rx_trace_closest_reforder_device(rx_context* c, const rx_ray* d_rays, 
                  "trace_reforder launch");
 }
 
-// Host buffers. The rays go to the device in chunks of up to stage_rays that alternate
-// between two copy/compute streams, so one chunk's copies overlap the other chunk's
-// kernels (2^23 rays per chunk by default: large enough for binning and the persistent
-// walk; for a 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for
-// one whole-batch copy, trace and copy back).
 rx_status rx_set_snapshots(rx_context* c, double every_s, rx_snapshot_fn fn, void* user) {
   if (!c) return RX_ERR_INVALID;
   if (!(every_s >= 0.0)) return c->fail(RX_ERR_INVALID, "every_s must be >= 0");
@@ -619,6 +614,11 @@ rx_status rx_trace_set_staging(rx_context* c, uint32_t chunk_rays) {
   return RX_OK;
 }
 
+// Host buffers. The rays go to the device in chunks of up to stage_rays that alternate
+// between two copy/compute streams, so one chunk's copies overlap the other chunk's
+// kernels (2^23 rays per chunk by default: large enough for binning and the persistent
+// walk; for a 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for
+// one whole-batch copy, trace and copy back).
 rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist) {
   if (!c) return RX_ERR_INVALID;
   if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
