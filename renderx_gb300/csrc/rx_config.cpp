@@ -16,6 +16,7 @@
 #include <cstring>
 #include <algorithm>
 #include <atomic>
+#include <exception>
 #include <memory>
 #include <string>
 #include <thread>
@@ -652,12 +653,23 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
     auto work = [&]() {
       for (size_t i; (i = next.fetch_add(1)) < objs.size();) {
         const char* fp = objs[i]->value("filePath");
-        if (fp) mesh_ok[i] = load_mesh(L.resolve(fp), meshes[i], mesh_err[i]);
+        try {
+          if (fp) mesh_ok[i] = load_mesh(L.resolve(fp), meshes[i], mesh_err[i]);
+        } catch (const std::exception&) {  // no exception leaves a worker (or the C ABI)
+          mesh_ok[i] = 0;
+          mesh_err[i] = "out of host memory reading " + std::string(fp);
+        }
       }
     };
     const size_t nt = std::min<size_t>(objs.size(), std::max(1u, std::thread::hardware_concurrency()));
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+    for (size_t t = 1; t < nt; t++) {
+      try {
+        pool.emplace_back(work);
+      } catch (const std::exception&) {
+        break;  // fewer threads: the calling thread reads the rest
+      }
+    }
     work();
     for (auto& th : pool) th.join();
   }
