@@ -53,7 +53,7 @@ WORKLOAD = "hit_batch_2^24_rays_cornell+200_icospheres_4096036_tris"
 
 
 # DRAM bytes (read + write) of one walk-kernel launch over the 2^24-ray batch, from a
-# one-pass ncu capture of this workload (profiles/k_trace_persistent4_hit2e24.md)
+# one-pass ncu capture of this workload
 TRAFFIC_BYTES_PER_RAY = (6416909056 + 1577210624) / (1 << 24)
 
 
@@ -347,24 +347,39 @@ def section_pm(iters: int = 2, res: int = 512, step: float = 0.01):
             "reference": f"the same PhotonMap over {8 * iters} iterations", "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
-def cpu_baseline(f, o, d, budget_s: float = 12.0):
-    """Times the oracle (CPU restatement of the reference traversal) on a bounded
-    sample of the batch with every host thread."""
+CPU_SAMPLE = 1 << 12  # rays of the fixed CPU subsample: every (N_RAYS / 4096)-th ray of the batch
+
+
+def cpu_sample(o, d):
+    """The fixed subsample both CPU legs time: 2^12 rays spread evenly over the batch
+    (indices 0, s, 2s, ... with s = N_RAYS / 2^12)."""
+    idx = np.arange(CPU_SAMPLE, dtype=np.int64) * max(1, len(o) // CPU_SAMPLE)
+    return idx, o[idx], d[idx]
+
+
+def cpu_trace_timed(T, o, d, threads):
+    """Seconds the oracle takes for these rays with `threads` host threads."""
+    t0 = time.perf_counter()
+    T.trace(o, d, threads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(f, o, d, parts: int = 1):
+    """Times the oracle (CPU restatement of the reference traversal, every host thread)
+    on the fixed 2^12-ray subsample of the batch, split into `parts` consecutive slices
+    timed one after another; the rate is the subsample's rays over the summed time."""
     import oracle
     T = oracle.RefTree(f["verts"], f["tris"])
     threads = os.cpu_count() or 1
-    n = 64
-    t0 = time.perf_counter()
-    T.trace(o[:n], d[:n], threads=threads)
-    dt = time.perf_counter() - t0
-    m = int(max(n, min(1 << 14, n * budget_s / max(dt, 1e-3))))
-    m = max(threads, (m // threads) * threads)
-    t0 = time.perf_counter()
-    T.trace(o[n:n + m], d[n:n + m], threads=threads)
-    dt = time.perf_counter() - t0
-    return {"value": m / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{m} rays of the 2^24 batch (rays {n}..{n + m - 1}), oracle restatement of "
-                      f"KDTree::intersect, {threads} threads, {dt:.1f} s"}
+    idx, so, sd = cpu_sample(o, d)
+    cpu_trace_timed(T, o[1:65], d[1:65], threads)  # warm-up: threads up, tree in cache
+    bounds = np.linspace(0, len(idx), parts + 1).astype(int)
+    secs = [cpu_trace_timed(T, so[a:b], sd[a:b], threads) for a, b in zip(bounds[:-1], bounds[1:])]
+    dt = sum(secs)
+    return {"value": len(idx) / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(idx)} rays of the 2^24 batch (every {idx[1] - idx[0]}-th ray), oracle restatement of "
+                      f"KDTree::intersect, {threads} threads, {dt:.1f} s",
+            "slice_s": [round(x, 3) for x in secs]}
 
 
 def dist_setup(args):
@@ -391,22 +406,33 @@ def whole_job_mrays(ws: int, rays_per_rank: int, steps: int, seconds: float) -> 
 
 
 def run_reference(args):
+    """The reference arm: the reference's closest-hit traversal on the host cores (the
+    oracle restatement of KDTree::intersect; the reference's own sources are not on the
+    GPU machine). Warm-up steps trace 64 rays each; the K timed steps trace consecutive
+    slices of the fixed 2^12-ray subsample, so the run covers exactly the rays the
+    cpu_baseline leg of the other arm times; the value is those rays over the summed
+    step time."""
     ws, rank, _ = dist_setup(args)
     if rank != 0:
         return
+    import oracle
     _, f, o, d = make_workload(0)
-    times = []
-    cb = None
-    for s in range(args.warmup + args.steps):
-        cb = cpu_baseline(f, o, d, budget_s=max(2.0, 20.0 / max(1, args.steps)))
-        if s >= args.warmup:
-            times.append(cb["value"])
-    v = statistics.median(times)
-    cb["value"] = v
+    T = oracle.RefTree(f["verts"], f["tris"])
+    threads = os.cpu_count() or 1
+    for s in range(args.warmup):
+        cpu_trace_timed(T, o[1 + 64 * s:65 + 64 * s], d[1 + 64 * s:65 + 64 * s], threads)
+    idx, so, sd = cpu_sample(o, d)
+    bounds = np.linspace(0, len(idx), args.steps + 1).astype(int)
+    secs = [cpu_trace_timed(T, so[a:b], sd[a:b], threads) for a, b in zip(bounds[:-1], bounds[1:])]
+    v = len(idx) / sum(secs) / 1e6
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"{len(idx)} rays of the 2^24 batch (every {idx[1] - idx[0]}-th ray) in {args.steps} "
+                    f"slices, oracle restatement of KDTree::intersect, {threads} threads, {sum(secs):.1f} s"}
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": N_RAYS / (v * 1e6) * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": sum(secs) / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "rays": N_RAYS, "triangles": 4096036, "sample": cb["sample"]},
+            "config": {"workload": WORKLOAD, "rays": N_RAYS, "triangles": 4096036, "sample": cb["sample"],
+                       "rays_per_step": int(len(idx) // args.steps)},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

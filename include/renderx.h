@@ -217,13 +217,13 @@ rx_status rx_scene_set_geometry(rx_context* ctx, const float* verts_xyz, uint32_
                                 const float* vnormals_xyz);
 /* Materials per object (reference ConfigManager.cpp:25-164 generateSceneObject). */
 rx_status rx_scene_set_objects(rx_context* ctx, const rx_object* objs, uint32_t nobj);
-/* KDTree::build (reference src/KDTree.cpp:303-319, include/KDTree.h:54): builds the
+/* KDTree::build (reference src/KDTree.cpp:230-246, include/KDTree.h:54): builds the
  * reference-order tree (tie ranks, visibility boxes) and the device BVH, uploads both. */
 rx_status rx_build_accel(rx_context* ctx, const rx_build_options* opts);
 /* Tree statistics: [0] BVH nodes, [1] BVH depth, [2] reference nodes,
  * [3] reference depth, [4] triangles, [5] reference leaves. */
 rx_status rx_accel_stats(rx_context* ctx, int64_t out[8]);
-/* KDTree::serializeForGPU (reference include/KDTree.h:56, src/KDTree.cpp:419-456) of
+/* KDTree::serializeForGPU (reference include/KDTree.h:56, src/KDTree.cpp:346-382) of
  * the reference-order tree this library builds, host only (no device, no context).
  * nodes12: 12 floats per node (parent, rightChild, leafStart, leafEnd, min.xyz, 0,
  * max.xyz, 0); leaf_tid: triangle id per leaf slot. Pass NULL outputs to query
@@ -284,7 +284,7 @@ rx_status rx_set_snapshots(rx_context* ctx, double every_s, rx_snapshot_fn fn, v
 
 /* ---- closest hit --------------------------------------------------------------- */
 /* KDTree::intersect(ray, triangleID, NULL) (reference include/KDTree.h:50,
- * src/KDTree.cpp:408-412) over a batch, host buffers: out_tid[i] = global triangle id
+ * src/KDTree.cpp:335-339) over a batch, host buffers: out_tid[i] = global triangle id
  * or -1, out_dist[i] = hit distance or -1. Up to 2^24 rays are copied and traced as one
  * batch; larger inputs are pipelined in chunks of 2^24 over two streams. */
 rx_status rx_trace_closest(rx_context* ctx, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist);
@@ -302,7 +302,9 @@ rx_status rx_trace_closest_device(rx_context* ctx, const rx_ray* d_rays, uint32_
  * device looks up the array's device address with that device current; make that
  * first call before any stream capture. All calls share the one array: calls whose
  * work overlaps on the GPU (other streams, other contexts on the device) race on it
- * and must be serialised by the caller. Requires a built accelerator. */
+ * and must be serialised by the caller. The array's address is that of the device's
+ * primary context, valid until cudaDeviceReset. Calls are not counted in
+ * rx_trace_counters. Requires a built accelerator. */
 rx_status rx_trace_closest_noalloc(rx_context* ctx, const rx_ray* d_rays, uint32_t n, int32_t* d_tid,
                                    float* d_dist, void* stream);
 /* Same semantics, without the BVH: walks every triangle the reference tree lets the

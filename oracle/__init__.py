@@ -48,6 +48,7 @@ def lib():
         L.rxo_tree_max_depth.argtypes = [P]
         L.rxo_tree_serialize.argtypes = [P, P, P]
         L.rxo_trace.argtypes = [P, P, ctypes.c_uint32, P, P, ctypes.c_int]
+        L.rxo_trace_unboxed.argtypes = [P, P, ctypes.c_uint32, P, P, ctypes.c_int]
         L.rxo_box_test.restype = ctypes.c_float
         L.rxo_box_test.argtypes = [P, P, P, P]
         L.rxo_num_threads.restype = ctypes.c_int
@@ -93,12 +94,21 @@ class RefTree:
 
     def trace(self, origins: np.ndarray, dirs: np.ndarray, threads: int = 0):
         """Closest hit per ray: (tid int32 with -1 on miss, dist float32)."""
+        return self._run(lib().rxo_trace, origins, dirs, threads)
+
+    def trace_unboxed(self, origins: np.ndarray, dirs: np.ndarray, threads: int = 0):
+        """Closest hit over every triangle, the tree's box tests ignored (same tie
+        order). Rays where this differs from trace() are those whose closest triangle
+        the reference's box tests hide."""
+        return self._run(lib().rxo_trace_unboxed, origins, dirs, threads)
+
+    def _run(self, fn, origins, dirs, threads):
         r = np.ascontiguousarray(np.concatenate([np.asarray(origins, np.float32).reshape(-1, 3),
                                                  np.asarray(dirs, np.float32).reshape(-1, 3)], 1))
         n = len(r)
         tid = np.empty(n, np.int32)
         dist = np.empty(n, np.float32)
-        lib().rxo_trace(self.h, _p(r), n, _p(tid), _p(dist), threads)
+        fn(self.h, _p(r), n, _p(tid), _p(dist), threads)
         return tid, dist
 
 

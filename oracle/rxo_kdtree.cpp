@@ -58,16 +58,16 @@ struct Node {
 struct rxo_tree {
   std::vector<V3> verts;
   std::vector<uint32_t> tris;  // 3 per triangle
-  std::vector<Node> nodes;     // DFS pre-order, left child first (KDTree.cpp:419-450)
+  std::vector<Node> nodes;     // DFS pre-order, left child first (KDTree.cpp:346-377)
   std::vector<uint32_t> tri_order;  // leaf triangle ids, leaves in DFS order
   int max_depth = 0;
 };
 
 namespace {
 
-// KDTree::splitBest, KDTree.cpp:202-301. Split policy:
+// KDTree::splitBest, KDTree.cpp:129-228. Split policy:
 //  0 = the reference as compiled with GCC/libstdc++: `abs(ratio-0.5)` at
-//      KDTree.cpp:264 binds to int abs(int), truncates both sides to 0 and 9, so the
+//      KDTree.cpp:191 binds to int abs(int), truncates both sides to 0 and 9, so the
 //      first axis (x) is always kept;
 //  1 = the intended behaviour (libc++/MSVC bind abs(double)): the axis whose
 //      left-count ratio is closest to 0.5, first axis on ties.
@@ -80,7 +80,7 @@ struct Builder {
   std::vector<float> coords;
 
   void bounds(const std::vector<uint32_t>& idx, Node& n) {
-    // KDTree.cpp:212-226: start from the first triangle's first vertex
+    // KDTree.cpp:139-153: start from the first triangle's first vertex
     V3 p0 = T->verts[T->tris[3 * idx[0]]];
     float mn[3] = {p0.x, p0.y, p0.z}, mx[3] = {p0.x, p0.y, p0.z};
     for (uint32_t t : idx)
@@ -107,7 +107,7 @@ struct Builder {
     if (!leaf) {
       int ndims = policy == 0 ? 1 : 3;  // policy 0 never keeps axes 1, 2
       for (int dim = 0; dim < ndims; dim++) {
-        // unique vertex indices of the node (unordered_set at KDTree.cpp:215-225)
+        // unique vertex indices of the node (unordered_set at KDTree.cpp:142-152)
         cur++;
         coords.clear();
         for (uint32_t t : idx)
@@ -117,7 +117,7 @@ struct Builder {
           }
         size_t mid = coords.size() >> 1;
         std::nth_element(coords.begin(), coords.begin() + mid, coords.end());
-        float split = coords[mid];  // KDTree.cpp:240-244
+        float split = coords[mid];  // KDTree.cpp:167-171
         unsigned left = 0;
         for (uint32_t t : idx) {
           unsigned mask = 0;
@@ -130,7 +130,7 @@ struct Builder {
         else better = std::fabs(ratio - 0.5) < std::fabs(best_ratio - 0.5);
         if (better) { best_ratio = ratio; best_dim = dim; best_split = split; }
       }
-      if (best_ratio == 0 || best_ratio == 1) leaf = true;  // KDTree.cpp:272-276
+      if (best_ratio == 0 || best_ratio == 1) leaf = true;  // KDTree.cpp:199-203
     }
     if (leaf) {
       n.tri_begin = (uint32_t)T->tri_order.size();
@@ -139,7 +139,7 @@ struct Builder {
       T->nodes[id] = n;
       return id;
     }
-    // KDTree.cpp:281-297: right gets triangles with no vertex <= split, in order
+    // KDTree.cpp:208-224: right gets triangles with no vertex <= split, in order
     std::vector<uint32_t> L, R;
     L.reserve(idx.size());
     for (uint32_t t : idx) {
@@ -157,7 +157,7 @@ struct Builder {
   }
 };
 
-// KDTree::Node::BoundingBox::intersect, KDTree.cpp:107-125. Faces in the order of the
+// KDTree::Node::BoundingBox::intersect, KDTree.cpp:34-52. Faces in the order of the
 // box's float layout (min.xyz then max.xyz); no epsilon.
 float box_test(const Node& n, V3 o, V3 d) {
   const float b[6] = {n.mn[0], n.mn[1], n.mn[2], n.mx[0], n.mx[1], n.mx[2]};
@@ -178,7 +178,7 @@ float box_test(const Node& n, V3 o, V3 d) {
   return minDist;
 }
 
-// KDTree::intersect(ray, triangle), KDTree.cpp:340-366 (no condition).
+// KDTree::intersect(ray, triangle), KDTree.cpp:267-293 (no condition).
 float tri_test(const rxo_tree* T, uint32_t t, V3 o, V3 d) {
   V3 vs[3];
   for (int i = 0; i < 3; i++) vs[i] = T->verts[T->tris[3 * t + i]];
@@ -199,7 +199,7 @@ float tri_test(const rxo_tree* T, uint32_t t, V3 o, V3 d) {
   return orthoDist / dd;
 }
 
-// KDTree::intersect(ray, node), KDTree.cpp:368-406: both children always visited;
+// KDTree::intersect(ray, node), KDTree.cpp:295-333: both children always visited;
 // equal distances keep the right child; in a leaf the first strictly closer wins.
 float node_isect(const rxo_tree* T, int ni, V3 o, V3 d, unsigned& tid) {
   const Node& n = T->nodes[ni];
@@ -248,7 +248,7 @@ uint32_t rxo_tree_num_nodes(const rxo_tree* T) { return (uint32_t)T->nodes.size(
 uint32_t rxo_tree_num_leaf_tris(const rxo_tree* T) { return (uint32_t)T->tri_order.size(); }
 int rxo_tree_max_depth(const rxo_tree* T) { return T->max_depth; }
 
-// Same content as KDTree::serializeForGPU (KDTree.cpp:419-456): per node 12 floats
+// Same content as KDTree::serializeForGPU (KDTree.cpp:346-382): per node 12 floats
 // (parent, rightChild, leafStart, leafEnd, min.xyz, 0, max.xyz, 0) and, per leaf
 // triangle, its id, in DFS order.
 void rxo_tree_serialize(const rxo_tree* T, float* nodes12, float* leaf_tid) {
@@ -268,7 +268,7 @@ void rxo_tree_serialize(const rxo_tree* T, float* nodes12, float* leaf_tid) {
 }
 
 // Closest hit for n rays (rays6: origin xyz, direction xyz), the public
-// KDTree::intersect(ray, tid, NULL) of KDTree.cpp:408-412. tid = -1 on a miss.
+// KDTree::intersect(ray, tid, NULL) of KDTree.cpp:335-339. tid = -1 on a miss.
 void rxo_trace(const rxo_tree* T, const float* rays6, uint32_t n, int32_t* tid, float* dist, int nthreads) {
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -281,6 +281,38 @@ void rxo_trace(const rxo_tree* T, const float* rays6, uint32_t n, int32_t* tid, 
     float r = node_isect(T, 0, o, d, t);
     dist[i] = r;
     tid[i] = r >= 0 ? (int32_t)t : -1;
+  }
+}
+
+// Closest hit over every triangle that passes the triangle test, ignoring the tree's
+// box tests: candidates ordered by (distance, later leaf first, earlier leaf slot
+// first), the order in which the reference's traversal (KDTree.cpp:295-333) would
+// pick them if every box passed. Where this differs from rxo_trace, the reference's
+// box tests hide the closest triangle from the ray.
+void rxo_trace_unboxed(const rxo_tree* T, const float* rays6, uint32_t n, int32_t* tid, float* dist, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+  for (long i = 0; i < (long)n; i++) {
+    V3 o = {rays6[6 * i], rays6[6 * i + 1], rays6[6 * i + 2]};
+    V3 d = {rays6[6 * i + 3], rays6[6 * i + 4], rays6[6 * i + 5]};
+    float best = -1;
+    int32_t bt = -1;
+    for (size_t ni = 0; ni < T->nodes.size(); ni++) {  // DFS pre-order: leaves in DFS order
+      const Node& nd = T->nodes[ni];
+      if (nd.left >= 0) continue;
+      float lbest = -1;
+      int32_t lt = -1;
+      for (uint32_t k = nd.tri_begin; k < nd.tri_end; k++) {
+        uint32_t tt = T->tri_order[k];
+        float r = tri_test(T, tt, o, d);
+        if (r >= 0 && (r < lbest || lbest < 0)) { lbest = r; lt = (int32_t)tt; }
+      }
+      if (lbest >= 0 && (best < 0 || lbest <= best)) { best = lbest; bt = lt; }  // ties: later leaf
+    }
+    dist[i] = best;
+    tid[i] = bt;
   }
 }
 

@@ -1,12 +1,12 @@
 // Host-side acceleration structures for the closest-hit path.
 //
 // Two trees are built over the same triangles:
-//  * RefOrder: the reference's own triangle tree (reference src/KDTree.cpp:202-319,
+//  * RefOrder: the reference's own triangle tree (reference src/KDTree.cpp:129-246,
 //    splitBest + build), rebuilt exactly. It is never traversed on the GPU; it
 //    supplies (a) the rank that breaks equal-distance ties the way the reference's
-//    recursive traversal does (KDTree.cpp:368-406: right child wins ties, first
+//    recursive traversal does (KDTree.cpp:295-333: right child wins ties, first
 //    triangle in a leaf wins) and (b) the node boxes whose reference box test
-//    (KDTree.cpp:107-125, no epsilon) decides whether the reference can see a
+//    (KDTree.cpp:34-52, no epsilon) decides whether the reference can see a
 //    triangle at all.
 //  * Bvh: a binned-SAH bounding volume hierarchy with padded boxes, the structure the
 //    GPU actually walks.
@@ -32,7 +32,7 @@ struct RefOrder {
   int max_depth = 0;
 };
 
-// policy 0: the reference as compiled by GCC/libstdc++ (KDTree.cpp:264 `abs` binds to
+// policy 0: the reference as compiled by GCC/libstdc++ (KDTree.cpp:191 `abs` binds to
 // int abs, the x axis is always kept); policy 1: best-ratio axis (libc++/MSVC builds).
 bool build_ref_order(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt, int policy,
                      int threads, RefOrder& out);

@@ -1,5 +1,5 @@
 // Host builders for the closest-hit path: the reference-order tree (exact rebuild of
-// reference src/KDTree.cpp:202-319) and the binned-SAH BVH the GPU walks.
+// reference src/KDTree.cpp:129-246) and the binned-SAH BVH the GPU walks.
 #include "rx_accel.h"
 
 #include <algorithm>
@@ -37,13 +37,13 @@ class RefBuilder {
  public:
   RefBuilder(const RefCtx& c, uint32_t nv) : c_(c), stamp_(nv, 0) {}
 
-  // Splits ``idx`` per KDTree::splitBest (KDTree.cpp:202-301). Returns true and fills
+  // Splits ``idx`` per KDTree::splitBest (KDTree.cpp:129-228). Returns true and fills
   // L, R when the node splits; false for a leaf. Always fills the node box.
   bool split(const std::vector<uint32_t>& idx, float mn[3], float mx[3], std::vector<uint32_t>& L,
              std::vector<uint32_t>& R) {
     const float* V = c_.v;
     const uint32_t* T = c_.t;
-    // box from the first triangle's first vertex, then all vertices (KDTree.cpp:212-226)
+    // box from the first triangle's first vertex, then all vertices (KDTree.cpp:139-153)
     const float* p0 = V + 3 * (size_t)T[3 * (size_t)idx[0]];
     for (int a = 0; a < 3; a++) mn[a] = mx[a] = p0[a];
     for (uint32_t tr : idx)

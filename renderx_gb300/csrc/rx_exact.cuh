@@ -2,8 +2,8 @@
 // single-precision operation per reference operation, round-to-nearest, never fused:
 //  * vector ops of nvVector.h:491-527 (cross; dot accumulated from 0; normalize by
 //    the correctly rounded sqrt of the accumulated square norm),
-//  * the ray/triangle test of KDTree.cpp:340-366,
-//  * the node box test of KDTree.cpp:107-125.
+//  * the ray/triangle test of KDTree.cpp:267-293,
+//  * the node box test of KDTree.cpp:34-52.
 // __f*_rn intrinsics are never contracted into FMAs, so the results match the
 // reference built with -ffp-contract=off on the host bit for bit.
 #pragma once
@@ -40,7 +40,7 @@ __device__ __forceinline__ F3 xnormalize(F3 v) {
   return v;
 }
 
-// KDTree::intersect(ray, triangle) without a condition (KDTree.cpp:340-366). Returns
+// KDTree::intersect(ray, triangle) without a condition (KDTree.cpp:267-293). Returns
 // true when the reference accepts the triangle (distance >= 0; NaN never passes the
 // caller's `dist >= 0`), and the distance.
 __device__ __forceinline__ bool tri_exact(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float& t) {
@@ -62,7 +62,7 @@ __device__ __forceinline__ bool tri_exact(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float
   return true;
 }
 
-// KDTree::Node::BoundingBox::intersect (KDTree.cpp:107-125) reduced to pass/fail:
+// KDTree::Node::BoundingBox::intersect (KDTree.cpp:34-52) reduced to pass/fail:
 // some face at non-negative distance whose intersection point lies within the other
 // two slabs, inclusive, no epsilon. Faces are skipped when the direction component is
 // exactly zero.

@@ -105,6 +105,32 @@ struct DevBuf {
   T* as() const { return static_cast<T*>(p); }
 };
 
+// A CUDA event, destroyed with its owner (null until created).
+struct Event {
+  cudaEvent_t e = nullptr;
+  Event() = default;
+  Event(const Event&) = delete;
+  Event& operator=(const Event&) = delete;
+  ~Event() {
+    if (e) cudaEventDestroy(e);
+  }
+  cudaError_t create(unsigned flags = cudaEventDefault) { return cudaEventCreateWithFlags(&e, flags); }
+  operator cudaEvent_t() const { return e; }
+};
+
+// A captured CUDA graph and its executable, destroyed with their owner.
+struct Graph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t x = nullptr;
+  Graph() = default;
+  Graph(const Graph&) = delete;
+  Graph& operator=(const Graph&) = delete;
+  ~Graph() {
+    if (x) cudaGraphExecDestroy(x);
+    if (g) cudaGraphDestroy(g);
+  }
+};
+
 }  // namespace rx
 
 struct rx_context {

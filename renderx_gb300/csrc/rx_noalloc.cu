@@ -10,7 +10,8 @@
 //   hit_leaf  : one uint32 per ray (each winner's reference leaf)
 //   queue     : one uint32 per ray (rays re-walked exactly)
 // for at most kNoAllocMaxRays rays per call, 8 MiB + 64 B. Every GPU that loads the
-// library holds the array until the process exits.
+// library holds the array until the process exits. Each call clears the counters (a
+// memset, no allocation); they are not added to the context's trace statistics.
 #include <mutex>
 
 #include "rx_internal.h"
@@ -25,6 +26,8 @@ static __device__ __align__(256) unsigned char g_trace_scratch[kScratchBytes];
 
 // Device address of g_trace_scratch per device: host code only holds a stand-in for
 // the array, so the address is looked up once per device with that device current.
+// The address belongs to the device's primary context (the one the CUDA runtime
+// uses); it stays valid until that context is destroyed (cudaDeviceReset).
 std::mutex g_mu;
 constexpr int kMaxDevices = 64;
 void* g_addr[kMaxDevices] = {};
@@ -54,19 +57,20 @@ extern "C" rx_status rx_trace_closest_noalloc(rx_context* c, const rx_ray* d_ray
                                        " rays exceed the limit of 1048576 rays per call");
   if (!d_rays || !d_tid || !d_dist) return c->fail(RX_ERR_INVALID, "null buffer");
   if (reinterpret_cast<uintptr_t>(d_rays) % 16) return c->fail(RX_ERR_INVALID, "rays must be 16-byte aligned");
-  int prev = -1;
-  cudaGetDevice(&prev);
-  if (prev != c->device) cudaSetDevice(c->device);
+  rx::DeviceGuard guard(c->device);
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e == cudaSuccess && cur != c->device) e = cudaErrorInvalidDevice;  // the switch did not take
+  if (e != cudaSuccess) return c->cuda(e, "trace_closest_noalloc: select the context's device");
   void* base = nullptr;
-  cudaError_t e = scratch_address(c->device, &base);
-  if (e == cudaSuccess) {
-    auto* counters = static_cast<unsigned long long*>(base);
-    auto* queue = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + kCounterBytes);
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-    // the launcher clears the queue length and the batch cursor before its kernels
+  if ((e = scratch_address(c->device, &base)) != cudaSuccess) return c->cuda(e, "trace_closest_noalloc: scratch address");
+  auto* counters = static_cast<unsigned long long*>(base);
+  auto* queue = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + kCounterBytes);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  // counters start at zero on every call (the previous call's values stay in the array)
+  e = cudaMemsetAsync(counters, 0, kCounterBytes, st);
+  if (e == cudaSuccess)
     e = rx::launch_trace_closest(c->accel, d_rays, n, d_tid, d_dist, queue, counters, c->trace_cfg, st, nullptr,
                                  false);
-  }
-  if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
   return c->cuda(e, "trace_closest_noalloc");
 }

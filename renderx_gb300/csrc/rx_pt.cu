@@ -628,17 +628,17 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     if (npasses < cands.size() + 2) cands.clear();
   }
 
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  Event e0, e1;
+  if ((e = e0.create()) != cudaSuccess || (e = e1.create()) != cudaSuccess) return e;
   cudaEventRecord(e0, s);
   uint64_t pass = 0;
   // time budget: after queueing pass p, wait for pass p - 1 and stop if the wall time is
   // spent (pass p still completes)
   const auto t_start = std::chrono::steady_clock::now();
-  cudaEvent_t pass_ev[2] = {nullptr, nullptr};
+  Event pass_ev[2];
   if (run.time_budget_s > 0)
-    for (auto& ev : pass_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (auto& ev : pass_ev)
+      if ((e = ev.create(cudaEventDisableTiming)) != cudaSuccess) return e;
   auto budget_spent = [&](uint64_t p) -> bool {
     if (run.time_budget_s <= 0) return false;
     cudaEventRecord(pass_ev[p & 1], s);
@@ -662,9 +662,8 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   };
   if (!cands.empty()) {
     float best_t = INFINITY;
-    cudaEvent_t t0, t1;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
+    Event t0, t1;
+    if ((e = t0.create()) != cudaSuccess || (e = t1.create()) != cudaSuccess) return e;
     for (const PtShape& sh : cands) {
       cudaEventRecord(t0, s);
       enqueue_pass_shape(W, sh, sms, s);
@@ -675,28 +674,20 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       if (ms < best_t) best_t = ms, best = sh;
       pass++;
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
   }
   if (chosen) *chosen = best;
 
   if (!guided) {
     if (run.use_graph && npasses - pass >= 2) {
-      cudaGraph_t graph;
-      cudaGraphExec_t exec;
+      Graph graph;
       if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
       enqueue_pass_shape(W, best, sms, s);
-      if ((e = cudaStreamEndCapture(s, &graph)) != cudaSuccess) return e;
-      if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        return e;
-      }
+      if ((e = cudaStreamEndCapture(s, &graph.g)) != cudaSuccess) return e;
+      if ((e = cudaGraphInstantiate(&graph.x, graph.g, 0)) != cudaSuccess) return e;
       while (pass < npasses && e == cudaSuccess) {
-        e = cudaGraphLaunch(exec, s);
+        e = cudaGraphLaunch(graph.x, s);
         if (e == cudaSuccess && after_pass(pass++)) break;
       }
-      cudaGraphExecDestroy(exec);
-      cudaGraphDestroy(graph);
       if (e != cudaSuccess) return e;
     } else {
       while (pass < npasses) {
@@ -766,10 +757,6 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  for (auto ev : pass_ev)
-    if (ev) cudaEventDestroy(ev);
   if (stats) {
     unsigned long long h[2];
     cudaMemcpy(h, W.ctr, sizeof h, cudaMemcpyDeviceToHost);

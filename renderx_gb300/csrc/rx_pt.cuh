@@ -124,7 +124,7 @@ __device__ __forceinline__ F3 world_normal(const TriGeom& g, bool has_normals, F
 
 // ---- self-intersection condition + closest hit ---------------------------------------
 // NoSelfIntersectionCondition::legal (src/NoSelfIntersectionCondition.cpp:12-27),
-// evaluated on every candidate before the closest one is chosen (KDTree.cpp:363):
+// evaluated on every candidate before the closest one is chosen (KDTree.cpp:290):
 // the sign of the direction against the candidate's shading normal decides.
 __device__ __forceinline__ bool legal_hit(int contact, int inside, int obj, float dn) {
   bool in = dn <= 0.0f, out = dn >= 0.0f;

@@ -10,7 +10,7 @@ namespace rx {
 // tests decided by the exact test, [2]: rays re-walked (cumulative), [3]: errors
 constexpr uint32_t kNoLeaf = 0xffffffffu;
 
-// Reference visibility of each ray's winner (KDTree.cpp:107-125 on every box of the
+// Reference visibility of each ray's winner (KDTree.cpp:34-52 on every box of the
 // winner's root path), one warp per ray and one root-path box per lane; the boxes of
 // the reference tree are few and stay in cache. Rays whose winner the reference cannot
 // see go to the eager queue.
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(128) k_trace_eager(DevAccel A, const rx_ray* _
   if (n_exact) atomicAdd(&counters[1], (unsigned long long)n_exact);
 }
 
-// The reference's own walk (KDTree.cpp:368-406) on the reference tree: every node whose
+// The reference's own walk (KDTree.cpp:295-333) on the reference tree: every node whose
 // box passes is entered, both children, no pruning; ties resolved exactly as there.
 // ref node layout: a = (min.xyz, parent), b = (max.xyz, right child or ~leaf index).
 __global__ void __launch_bounds__(128) k_trace_reforder(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,

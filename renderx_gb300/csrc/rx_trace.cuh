@@ -1,6 +1,6 @@
 // Closest-hit traversal with the reference's answer, bit for bit.
 //
-// The reference (KDTree::intersect, reference src/KDTree.cpp:368-412) returns, over
+// The reference (KDTree::intersect, reference src/KDTree.cpp:295-339) returns, over
 // the triangles it can see, the smallest distance; among equal distances the one in
 // the latest leaf of its DFS order (the right child wins ties) and, within a leaf, the
 // first. A triangle is visible when it passes the ray/triangle test and every node
@@ -27,7 +27,7 @@ __device__ __forceinline__ F3 safe_inv(F3 d) {
 }
 
 // Reference visibility of a triangle in reference leaf `leaf`: every box on the root
-// path passes KDTree.cpp:107-125. The root path comes from the per-leaf ancestor list,
+// path passes KDTree.cpp:34-52. The root path comes from the per-leaf ancestor list,
 // read four boxes at a time so the loads are independent.
 __device__ __forceinline__ bool ref_visible(const DevAccel& A, uint32_t leaf, F3 o, F3 d, F3 inv, bool zero_dir,
                                             unsigned* n_exact) {

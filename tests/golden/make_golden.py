@@ -263,7 +263,8 @@ def make_pm_goldens(ref_pm: str):
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else (os.environ.get("RENDERX_REFERENCE") or
+                                os.path.join(os.path.dirname(ROOT), "reference"))
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"], check=True)
     if "--bpt-only" in sys.argv:
         make_bpt_goldens(os.path.join(ROOT, "oracle", "_ref", "bpt_driver"))
