@@ -134,7 +134,66 @@ def _relmse(img, ref):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64):
+class Oracle:
+    """An FP64-film render of plain BSDF-sampling PathTracer with many samples: the
+    reference image every rendering section states its relMSE against. `var` is its
+    per-pixel variance of the mean (from the mean of squares); relmse() also reports
+    the relMSE with the oracle's own expected noise contribution removed (the image and
+    the oracle are independent, so E[(I - R)^2] = E[(I - mu)^2] + var_R)."""
+
+    def __init__(self, ctx, camera, spp, max_depth, rr_mode, seed=99, paths_per_pass=1 << 22):
+        m, sq, st = ctx.render_pt(camera, spp, max_depth=max_depth, rr_mode=rr_mode, seed=seed, want_sq=True,
+                                  paths_per_pass=paths_per_pass)
+        self.mean, self.spp, self.ms = m, spp, st["ms"]
+        self.var = np.maximum(sq - m * m, 0.0) / (spp - 1)
+        self.desc = f"plain PathTracer, {spp} spp, FP64 film, RR mode {rr_mode}, depth {max_depth}"
+
+    def noise(self) -> float:
+        return float(np.mean(self.var / (self.mean ** 2 + 1e-2)))
+
+    def relmse(self, img) -> dict:
+        raw = _relmse(img, self.mean)
+        return {"relmse": raw, "relmse_minus_oracle_noise": raw - self.noise()}
+
+
+def section_c0(peak):
+    """C0: the 36-triangle Cornell box, plain PathTracer at 256^2 x 16 spp, depth 8,
+    Russian roulette from depth 3; the reference's CPU PathTracer restated (the oracle)
+    renders the same frame on every host core."""
+    import oracle
+    import renderx_gb300 as rx
+    from renderx_gb300 import scenes
+    sc = scenes.cornell_box(256, 256)
+    spp, depth = 16, 8
+    with rx.Context(0) as ctx:
+        ctx.set_scene(sc)
+        ctx.build_accel()
+        ctx.render_pt(sc.camera, 1, max_depth=depth, rr_mode=1, seed=3)  # warm-up
+        runs = [ctx.render_pt(sc.camera, spp, max_depth=depth, rr_mode=1, seed=4 + k) for k in range(5)]
+        film, _, st = runs[-1]
+        ms = float(np.median([r[2]["ms"] for r in runs]))
+        orc = Oracle(ctx, sc.camera, 65536, depth, 1)
+    rays = st["extension_rays"] + st["shadow_rays"]
+    alg = 40 * rays + 96 * st["extension_rays"] + 24 * sc.camera.width * sc.camera.height
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cimg, _, crays = oracle.RefPathTracer(sc).render(sc.camera, spp, max_depth=depth, rr_mode=1, seed=5,
+                                                     threads=threads)
+    cs = time.perf_counter() - t0
+    return {"workload": f"PathTracer, Cornell box (36 triangles) {sc.camera.width}x{sc.camera.height} x {spp} spp, "
+                        f"depth {depth}, RR from depth 3", "ms": ms, "mrays_per_s": rays / ms / 1e3,
+            "samples_per_s": st["paths"] / ms * 1e3, "extension_rays": st["extension_rays"],
+            "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(film).items()},
+            "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": peak, "unit": "GB/s",
+                         "frac": alg / ms / 1e6 / peak},
+            "cpu_baseline": {"value": crays / cs / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "samples_per_s": sc.camera.width * sc.camera.height * spp / cs, "seconds": cs,
+                             "relmse_vs_oracle": orc.relmse(cimg)["relmse"],
+                             "sample": "the whole frame (256x256 x 16 spp), oracle restatement of PathTracer "
+                                       "over the reference's KDTree"}}
+
+
+def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64, cpu_tree=None):
     """C1: plain wavefront PathTracer at 1024^2 x 64 spp, depth 16, RR from depth 3."""
     from dataclasses import replace
     depth = 16
@@ -147,59 +206,106 @@ def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64):
     # algorithmic bytes: 40 per traced ray, 96 per shade event (path state read + write),
     # 24 per pixel for the FP64 film
     alg = 40 * rays + 96 * st["extension_rays"] + 24 * cam.width * cam.height
-    ref, _, _ = ctx.render_pt(cam, 8 * spp, max_depth=depth, rr_mode=1, seed=5)  # FP64 film, 8x the samples
-    return {"workload": f"PathTracer {cam.width}x{cam.height} x {spp} spp, depth {depth}, "
-                        "4,096,036 triangles", "ms": st["ms"], "mrays_per_s": rays / s / 1e6,
-            "relmse_vs_high_spp": _relmse(film, ref), "reference": f"the same PathTracer at {8 * spp} spp, FP64 film",
-            "samples_per_s": st["paths"] / s, "extension_rays": st["extension_rays"],
-            "shadow_rays": st["shadow_rays"], "image_mean": [float(x) for x in film.mean(axis=(0, 1))],
-            "roofline": {"bound": "hbm", "achieved": alg / s / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / s / 1e9 / peak}}
+    orc = Oracle(ctx, cam, 8 * spp, depth, 1, seed=5)
+    out = {"workload": f"PathTracer {cam.width}x{cam.height} x {spp} spp, depth {depth}, "
+                       "4,096,036 triangles", "ms": st["ms"], "mrays_per_s": rays / s / 1e6,
+           "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(film).items()},
+           "samples_per_s": st["paths"] / s, "extension_rays": st["extension_rays"],
+           "shadow_rays": st["shadow_rays"], "image_mean": [float(x) for x in film.mean(axis=(0, 1))],
+           "roofline": {"bound": "hbm", "achieved": alg / s / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": alg / s / 1e9 / peak}}
+    if cpu_tree is not None:  # the reference's CPU PathTracer (restated) on a crop of the same frame
+        import oracle
+        threads = os.cpu_count() or 1
+        crop = (cam.width // 2 - 8, cam.height // 2 - 8, 16, 16)
+        t0 = time.perf_counter()
+        _, _, crays = oracle.RefPathTracer(sc, tree=cpu_tree).render(cam, 1, max_depth=depth, rr_mode=1, seed=6,
+                                                                     crop=crop, threads=threads)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": crays / cs / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                               "samples_per_s": 256 / cs, "seconds": cs,
+                               "sample": "16x16 pixels at the image centre x 1 spp (the reference's unpruned "
+                                         "KDTree walk over 4.1M triangles manages a few hundred rays/s), oracle "
+                                         "restatement of PathTracer"}
+    return out
 
 
 def section_guiding(res: int, ref_spp: int, spp: int):
-    """C4 glossy workload at res^2: plain vs guided PathTracer at equal samples, then at
-    equal time (both under a wall-time budget equal to the plain render's time, sample
-    count uncapped).
+    """C4: the glossy workload at res^2 (4.1M triangles, 60% glossy spheres with exponent
+    log-U[100,1000], light of 1% of the ceiling, depth 16, RR from depth 3), plain BSDF
+    sampling against the batched + guided form, both through rx_render_pt_batch (passes
+    replayed as CUDA graphs, launch shape autotuned on the first passes); the guided item
+    trains its network during its own first passes (training and inference time
+    included). Every image is scored against the plain FP64 oracle (relMSE, and relMSE
+    with the oracle's own noise removed).
 
-    The reference image is a guided render of ref_spp samples (an unbiased estimator
-    with a fraction of plain sampling's variance, so the reference's own noise barely
-    enters either relMSE). Guided renders train during their own first passes; their
-    time includes inference and training."""
+    Time to relMSE 1e-3: both estimators are unbiased, so relMSE falls as 1 / samples;
+    from each render at `spp` samples, the samples needed for 1e-3 follow, and the time is
+    the guided render's fixed training cost plus its per-sample time (from two guided
+    renders of different sample counts), the plain render's per-sample time alone. The
+    guided estimate is then checked by rendering that many samples. Equal time: both
+    single-scene renders under one wall-time budget (the plain render's time)."""
     import renderx_gb300 as rx
     from renderx_gb300 import scenes
     sc = scenes.guiding_scene(res, res, 200, 5, seed=1)
-    out = {"workload": f"glossy guiding workload {res}x{res}, 4,096,036 triangles, depth 16, RR from depth 3",
-           "reference": f"guided PathTracer, {ref_spp} spp", "spp": spp}
+    depth = 16
     gopt = dict(learning_rate=5e-3, batch=1 << 18, warmup_passes=1, train_passes=4, steps_per_pass=16)
     ppp = 1 << 21
+    target = 1e-3
+    out = {"workload": f"glossy guiding workload {res}x{res}, 4,096,036 triangles, depth {depth}, RR from depth 3",
+           "spp": spp, "guide_options": dict(gopt, paths_per_pass=ppp, bsdf_fraction=0.5), "target_relmse": target}
     with rx.Context(0) as ctx:
         ctx.set_scene(sc)
         ctx.build_accel()
-        ctx.guide_init(seed=11, **gopt)
-        ref, _, st = ctx.render_pt(sc.camera, ref_spp, max_depth=16, rr_mode=1, seed=1, guided=True,
-                                   paths_per_pass=ppp)
-        out["reference_ms"] = st["ms"]
-        plain, _, sp = ctx.render_pt(sc.camera, spp, max_depth=16, rr_mode=1, seed=5)
-        ctx.guide_init(seed=1, **gopt)
-        guided, _, sg = ctx.render_pt(sc.camera, spp, max_depth=16, rr_mode=1, seed=6, guided=True,
-                                      paths_per_pass=ppp)
+        t0 = time.perf_counter()
+        orc = Oracle(ctx, sc.camera, ref_spp, depth, 1, seed=1, paths_per_pass=1 << 22)
+        out["oracle"] = orc.desc
+        out["oracle_ms"] = orc.ms
+        out["oracle_noise_relmse"] = orc.noise()
+
+        def batch(n, guided, seed):
+            if guided:
+                ctx.guide_init(seed=seed, **gopt)
+            films, st = ctx.render_pt_batch([(ctx, sc.camera, dict(spp=n, max_depth=depth, rr_mode=1, seed=seed,
+                                                                   guided=guided))],
+                                            paths_per_pass=ppp, use_graph=True, autotune=True)
+            return films[0], st
+
+        batch(16, False, 90)  # warm-up
+        plain, sp = batch(spp, False, 5)
+        guided, sg = batch(spp, True, 6)
+        guided2, sg2 = batch(2 * spp, True, 7)
+        rp, rg = orc.relmse(plain), orc.relmse(guided)
+        # samples and time for relMSE 1e-3 (noise-corrected relMSE x samples is constant)
+        n_p = spp * rp["relmse_minus_oracle_noise"] / target
+        n_g = spp * rg["relmse_minus_oracle_noise"] / target
+        per_p = sp["ms"] / spp
+        per_g = (sg2["ms"] - sg["ms"]) / spp  # guided per-sample time; the rest is training
+        fixed_g = sg["ms"] - per_g * spp
+        t_p, t_g = n_p * per_p, fixed_g + n_g * per_g
+        out["plain"] = {"ms": sp["ms"], **rp, "chosen_stack": sp["stack"], "chosen_blocks_per_sm": sp["blocks_per_sm"]}
+        out["guided"] = {"ms": sg["ms"], **rg, "ms_2x_spp": sg2["ms"], **{k + "_2x_spp": v for k, v in
+                                                                          orc.relmse(guided2).items()},
+                         "chosen_stack": sg["stack"], "chosen_blocks_per_sm": sg["blocks_per_sm"]}
+        out["to_target"] = {"plain_spp": n_p, "plain_ms": t_p, "guided_spp": n_g, "guided_ms": t_g,
+                            "guided_fixed_ms": fixed_g, "time_ratio": t_g / t_p}
+        # check: the guided render at the samples predicted for the target
+        ng = int(max(1, round(n_g)))
+        gchk, sgc = batch(ng, True, 8)
+        out["to_target"]["guided_check"] = {"spp": ng, "ms": sgc["ms"], **orc.relmse(gchk)}
+        # equal time: one wall-time budget for both single-scene renders
         budget = sp["ms"] * 1e-3
-        plain_t, _, spt = ctx.render_pt(sc.camera, 1 << 16, max_depth=16, rr_mode=1, seed=7, paths_per_pass=ppp,
+        plain_t, _, spt = ctx.render_pt(sc.camera, 1 << 16, max_depth=depth, rr_mode=1, seed=9, paths_per_pass=ppp,
                                         time_budget_s=budget)
-        ctx.guide_init(seed=2, **gopt)
-        guided_t, _, sgt = ctx.render_pt(sc.camera, 1 << 16, max_depth=16, rr_mode=1, seed=8, guided=True,
+        ctx.guide_init(seed=10, **gopt)
+        guided_t, _, sgt = ctx.render_pt(sc.camera, 1 << 16, max_depth=depth, rr_mode=1, seed=11, guided=True,
                                          paths_per_pass=ppp, time_budget_s=budget)
-    rp, rg = _relmse(plain, ref), _relmse(guided, ref)
-    rpt, rgt = _relmse(plain_t, ref), _relmse(guided_t, ref)
-    out["equal_time"] = {"budget_s": budget,
-                         "plain": {"ms": spt["ms"], "spp": spt["paths"] / (res * res), "relmse": rpt},
-                         "guided": {"ms": sgt["ms"], "spp": sgt["paths"] / (res * res), "relmse": rgt},
-                         "relmse_ratio": rgt / rpt}
-    out.update({"guide_options": dict(gopt, paths_per_pass=ppp, bsdf_fraction=0.5),
-                "plain": {"ms": sp["ms"], "relmse": rp, "relmse_x_s": rp * sp["ms"] * 1e-3},
-                "guided": {"ms": sg["ms"], "relmse": rg, "relmse_x_s": rg * sg["ms"] * 1e-3},
-                "time_to_equal_relmse_ratio": (rg * sg["ms"]) / (rp * sp["ms"])})
+        ept, egt = orc.relmse(plain_t), orc.relmse(guided_t)
+        out["equal_time"] = {"budget_s": budget,
+                             "plain": {"ms": spt["ms"], "spp": spt["paths"] / (res * res), **ept},
+                             "guided": {"ms": sgt["ms"], "spp": sgt["paths"] / (res * res), **egt},
+                             "relmse_ratio": egt["relmse_minus_oracle_noise"] / ept["relmse_minus_oracle_noise"]}
+        out["section_s"] = round(time.perf_counter() - t0, 1)
     return out
 
 
@@ -285,8 +391,25 @@ def section_batch(n: int = 64, small: bool = False):
             "scene_generation_s": round(gen_s, 1), "accel_build_s": round(build_s, 1)}
 
 
-def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
-    """C2: VCMTracer, medium scene at 512^2, 2^20 light paths per iteration."""
+_MEDIUM_ORACLE = {}
+
+
+def medium_oracle(ctx, sc, res: int):
+    """The plain FP64 PathTracer oracle of the medium scene at res^2 (computed once)."""
+    if res not in _MEDIUM_ORACLE:
+        _MEDIUM_ORACLE[res] = Oracle(ctx, sc.camera, 4096, 16, 0, seed=77)
+    return _MEDIUM_ORACLE[res]
+
+
+def section_vcm(peak, iters: int = 32, res: int = 512, light_paths: int = 1 << 20):
+    """C2: VCMTracer, medium scene at 512^2, 2^20 light paths per iteration, 32
+    iterations, r0 = 0.0963, alpha = 0.75, depth 16. relMSE against the plain FP64
+    oracle (VCM's merging is biased at any finite radius: in the medium the reference's
+    VCMTracer sits a few percent above its path tracers, which the relMSE includes) and
+    against the same VCMTracer at 4x the iterations. Roofline of the merge gather (the
+    grid walk and pair evaluation): algorithmic bytes = 80 per query (the eye vertex, 16,
+    and 8 cell heads, 64) + 48 per merged photon + 48 per stored light vertex, over the
+    gather's device time."""
     import renderx_gb300 as rx
     from renderx_gb300 import scenes
     sc = scenes.medium_scene(res, res)
@@ -295,12 +418,25 @@ def section_vcm(iters: int = 2, res: int = 512, light_paths: int = 1 << 20):
         ctx.build_accel()
         ctx.render_vcm(sc.camera, 1, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=1)
         img, st = ctx.render_vcm(sc.camera, iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=2)
-        ref, _ = ctx.render_vcm(sc.camera, 8 * iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=3)
+        ref, _ = ctx.render_vcm(sc.camera, 4 * iters, 0.0963, 0.75, max_depth=16, light_paths=light_paths, seed=3)
+        orc = medium_oracle(ctx, sc, res)
+    alg = 80 * st["merge_queries"] + 48 * st["merges"] + 48 * st["photons"]
+    gbs = alg / (st["merge_ms"] * 1e-3) / 1e9 if st["merge_ms"] > 0 else None
     return {"workload": f"VCMTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, {light_paths} light "
-                        "paths/iter, depth 16, r0 0.0963, alpha 0.75", "iterations": iters, "ms": st["ms"],
-            "ms_per_iteration": st["ms"] / iters, "rays_per_iteration": st["rays"] // iters,
-            "relmse_vs_high_spp": _relmse(img, ref), "reference": f"the same VCMTracer over {8 * iters} iterations",
+                        f"paths/iter, {iters} iterations, depth 16, r0 0.0963, alpha 0.75", "iterations": iters,
+            "ms": st["ms"], "ms_per_iteration": st["ms"] / iters, "rays_per_iteration": st["rays"] // iters,
+            "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(img).items()},
+            "relmse_vs_4x_iterations": _relmse(img, ref),
             "shadow_rays_per_iteration": st["shadow_rays"] // iters, "merges_per_iteration": st["merges"] // iters,
+            "merge_queries_per_iteration": st["merge_queries"] // iters,
+            "photons_per_iteration": st["photons"] // iters, "merge_gather_ms_per_iteration": st["merge_ms"] / iters,
+            "roofline": None if gbs is None else {
+                "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                "kernel": "k_merge_walk + k_merge_eval (merge gather)",
+                "algorithmic_bytes_per_iteration": alg // iters},
+            "cpu_baseline": None,
+            "cpu_baseline_note": "not measured on the GPU machine: the reference's VCMTracer runs only from its own "
+                                 "sources, which are not there, and the oracle restates its PathTracer, not VCM",
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
@@ -315,11 +451,11 @@ def section_bpt(spp: int = 4, res: int = 512):
         ctx.build_accel()
         ctx.render_bpt(sc.camera, 1, max_depth=16, seed=1)
         img, st = ctx.render_bpt(sc.camera, spp, max_depth=16, seed=2)
-        ref, _ = ctx.render_bpt(sc.camera, 16 * spp, max_depth=16, seed=3)
+        orc = medium_oracle(ctx, sc, res)
     rays = st["rays"] + st["shadow_rays"]
     return {"workload": f"BidirectionalPathTracer, Cornell room + homogeneous-medium sphere, {res}x{res}, depth 16",
             "spp": spp, "ms": st["ms"], "ms_per_spp": st["ms"] / spp, "mrays_per_s": rays / (st["ms"] * 1e-3) / 1e6,
-            "relmse_vs_high_spp": _relmse(img, ref), "reference": f"the same BidirectionalPathTracer at {16 * spp} spp",
+            "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(img).items()},
             "samples_per_s": st["paths"] / (st["ms"] * 1e-3), "shadow_rays_per_spp": st["shadow_rays"] // spp,
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
@@ -340,11 +476,13 @@ def section_pm(iters: int = 2, res: int = 512, step: float = 0.01):
         ctx.render_pm(sc.camera, 1, 0.0963, max_depth=16, seed=1)
         img, st = ctx.render_pm(sc.camera, iters, 0.0963, max_depth=16, seed=2)
         ref, _ = ctx.render_pm(sc.camera, 8 * iters, 0.0963, max_depth=16, seed=3)
+        orc = medium_oracle(ctx, sc, res)
     return {"workload": f"PhotonMap, Cornell room + homogeneous-medium sphere (step {step}), {res}x{res}, depth 16, "
                         f"{res * res} photon paths/iter, r0 0.0963",
             "iterations": iters, "ms": st["ms"], "ms_per_iteration": st["ms"] / iters,
-            "photons_per_iteration": st["photons"] // iters, "relmse_vs_high_spp": _relmse(img, ref),
-            "reference": f"the same PhotonMap over {8 * iters} iterations", "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
+            "photons_per_iteration": st["photons"] // iters, "relmse_vs_8x_iterations": _relmse(img, ref),
+            "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(img).items()},
+            "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
 
 
 CPU_SAMPLE = 1 << 12  # rays of the fixed CPU subsample: every (N_RAYS / 4096)-th ray of the batch
@@ -364,12 +502,12 @@ def cpu_trace_timed(T, o, d, threads):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(f, o, d, parts: int = 1):
+def cpu_baseline(f, o, d, parts: int = 1, tree=None):
     """Times the oracle (CPU restatement of the reference traversal, every host thread)
     on the fixed 2^12-ray subsample of the batch, split into `parts` consecutive slices
     timed one after another; the rate is the subsample's rays over the summed time."""
     import oracle
-    T = oracle.RefTree(f["verts"], f["tris"])
+    T = tree if tree is not None else oracle.RefTree(f["verts"], f["tris"])
     threads = os.cpu_count() or 1
     idx, so, sd = cpu_sample(o, d)
     cpu_trace_timed(T, o[1:65], d[1:65], threads)  # warm-up: threads up, tree in cache
@@ -501,15 +639,21 @@ def run_ours(args):
         e2e, same = end_to_end(ctx, host_rays, d_tid, args, dist, ws, n)
 
     extra = {}
+    cpu_tree = None
     if rank == 0:
         peak, _ = load_peaks()
         tf = load_tflops()
-        for name, skip, fn in (("pt", args.skip_pt, lambda: section_pt(ctx, sc, peak, args.pt_res, args.pt_spp)),
+        if not args.skip_cpu_baseline:
+            import oracle
+            cpu_tree = oracle.RefTree(f["verts"], f["tris"])  # the reference tree of the hit-batch scene
+        for name, skip, fn in (("c0", args.skip_c0, lambda: section_c0(peak)),
+                               ("pt", args.skip_pt,
+                                lambda: section_pt(ctx, sc, peak, args.pt_res, args.pt_spp, cpu_tree)),
                                ("mlp", args.skip_mlp, lambda: section_mlp(ctx, tf)),
                                ("guiding", args.skip_guiding,
                                 lambda: section_guiding(args.guide_res, args.guide_ref_spp, args.guide_spp)),
                                ("vcm", args.skip_vcm,
-                                lambda: section_vcm(args.vcm_iters, args.vcm_res, args.vcm_light_paths)),
+                                lambda: section_vcm(peak, args.vcm_iters, args.vcm_res, args.vcm_light_paths)),
                                ("bpt", args.skip_bpt, lambda: section_bpt()),
                                ("pm", args.skip_pm, lambda: section_pm()),
                                ("batch", args.skip_batch, lambda: section_batch(args.batch_scenes)),
@@ -522,7 +666,8 @@ def run_ours(args):
             except Exception as ex:  # a failing section is reported, not hidden
                 extra[name] = {"error": f"{type(ex).__name__}: {ex}"}
             extra[name]["wall_s"] = round(time.perf_counter() - t0, 2)
-        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms, extra)
+        emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms, extra,
+             cpu_tree)
     ctx.close()
     if dist:
         dist.destroy_process_group()
@@ -548,7 +693,8 @@ def end_to_end(ctx, host_rays, d_tid, args, dist, ws, n):
     return e2e, same
 
 
-def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms, extra):
+def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_ms, wall, f, o, d, kern_ms, extra,
+         cpu_tree=None):
     if True:
         peak, peak_kind = load_peaks()
         bytes_alg = 40 * n + 48 * st["triangles"] + 64 * st["bvh_nodes"]
@@ -575,7 +721,7 @@ def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_m
                 "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms], "wall_s": wall}
         line.update(extra)
         if not args.skip_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(f, o, d)
+            line["cpu_baseline"] = cpu_baseline(f, o, d, tree=cpu_tree)
         print(json.dumps(line), flush=True)
 
 
@@ -588,6 +734,7 @@ def main():
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="batch size (profiler captures use a smaller one)")
+    ap.add_argument("--skip-c0", action="store_true")
     ap.add_argument("--skip-pt", action="store_true")
     ap.add_argument("--skip-mlp", action="store_true")
     ap.add_argument("--skip-guiding", action="store_true")
@@ -597,18 +744,19 @@ def main():
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--skip-extra", action="store_true", help="skip every secondary section")
-    ap.add_argument("--guide-res", type=int, default=256)
+    ap.add_argument("--guide-res", type=int, default=1024)
     ap.add_argument("--guide-ref-spp", type=int, default=4096)
-    ap.add_argument("--guide-spp", type=int, default=512)
+    ap.add_argument("--guide-spp", type=int, default=256)
     ap.add_argument("--pt-res", type=int, default=1024, help="path-tracing section resolution (profiling: smaller)")
     ap.add_argument("--pt-spp", type=int, default=64)
     ap.add_argument("--vcm-res", type=int, default=512)
     ap.add_argument("--vcm-light-paths", type=int, default=1 << 20)
-    ap.add_argument("--vcm-iters", type=int, default=2)
+    ap.add_argument("--vcm-iters", type=int, default=32)
     args = ap.parse_args()
     globals()["N_RAYS"] = args.rays
     if args.skip_extra:
-        args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = args.skip_bpt = args.skip_pm = True
+        args.skip_c0 = args.skip_pt = args.skip_mlp = args.skip_guiding = args.skip_vcm = args.skip_batch = True
+        args.skip_bpt = args.skip_pm = True
     if args.impl == "reference":
         run_reference(args)
     else:

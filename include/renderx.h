@@ -128,7 +128,9 @@ typedef struct rx_guide_options {
 typedef struct rx_batch_item {
   rx_context* scene;       /* context holding the scene (objects set, accelerator built) */
   rx_camera camera;
-  rx_pt_options options;   /* spp, max_depth, rr_mode, nee, seed; paths_per_pass and flags unused */
+  rx_pt_options options;   /* spp, max_depth, rr_mode, nee, seed, flags (RX_PT_GUIDED: guided
+                              by the scene context's network, rx_guide_init); paths_per_pass
+                              unused, time_budget_s 0 */
   double* film_rgb;        /* host output: width*height*3 per-pixel means, rows from the top */
 } rx_batch_item;
 
@@ -194,8 +196,10 @@ typedef struct rx_render_stats {
   uint64_t shadow_rays;    /* next-event-estimation visibility rays */
   uint64_t paths;          /* pixel samples */
   float ms;                /* device time of the render (CUDA events) */
-  float reserved;
+  float merge_ms;          /* VCM: device time of the merge gather (grid walk + pair evaluation) */
   uint64_t merges;         /* VCM: (eye vertex, photon) pairs merged; PhotonMap: photons stored */
+  uint64_t merge_queries;  /* VCM: eye vertices that queried the photon grid */
+  uint64_t photons;        /* VCM, PhotonMap: photons stored in the grids, all iterations */
 } rx_render_stats;
 
 /* ---- context ------------------------------------------------------------------- */
@@ -325,7 +329,14 @@ rx_status rx_render_pt(rx_context* ctx, const rx_camera* cam, const rx_pt_option
  * scene per Renderer): every item's paths share the pass queues; paths of uneven
  * length compact away per bounce. Each item's image equals what rx_render_pt gives for
  * the same options (up to the summation order of the FP64 film). ctx supplies the
- * stream and device; every item's scene must live on the same device. */
+ * stream and device; every item's scene must live on the same device.
+ * Guided items (RX_PT_GUIDED) each use the network of their scene's context (items
+ * sharing a context share it) with that context's guide options; all networks warm up,
+ * train and guide on the same schedule of passes, because every pass then takes an equal
+ * share of each item's samples (each item's image is still unbiased; with guided items
+ * the pass order, and so the random numbers, differ from rx_render_pt's). Inference runs
+ * grouped: the live paths sorted by network, each network's rows through its own weights;
+ * each network trains on its own scene's records. */
 rx_status rx_render_pt_batch(rx_context* ctx, const rx_batch_item* items, uint32_t n, rx_batch_options* opts,
                              rx_render_stats* stats);
 

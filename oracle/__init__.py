@@ -1,8 +1,10 @@
 """ORACLE — test infrastructure only.
 
-CPU restatement of the reference's light-transport path (reference src/KDTree.cpp,
-src/PathTracer.cpp and the material code), compiled from ``oracle/*.cpp`` into
-``oracle/liboracle.so``. Only ``tests/``, ``__graft_entry__.smoke()`` and
+CPU restatement of the reference's light-transport path, compiled from
+``oracle/*.cpp`` into ``oracle/liboracle.so``: the triangle KDTree (reference
+src/KDTree.cpp; ``RefTree``) and the PathTracer estimator with the surface materials
+(src/PathTracer.cpp, src/MCRenderer.cpp, the material code; ``RefPathTracer``). The
+guiding network's FP64 restatement is ``oracle.guide_mlp``. Only ``tests/``, ``__graft_entry__.smoke()`` and
 ``bench.py``'s CPU-baseline leg may import this package; it checks results and times
 the CPU baseline, and is never the thing measured or shipped.
 
@@ -52,6 +54,10 @@ def lib():
         L.rxo_box_test.restype = ctypes.c_float
         L.rxo_box_test.argtypes = [P, P, P, P]
         L.rxo_num_threads.restype = ctypes.c_int
+        L.rxo_pt_render.restype = ctypes.c_uint64
+        L.rxo_pt_render.argtypes = [P, P, P, P, ctypes.c_uint32, P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint64, ctypes.c_int, P, P]
         _LIB = L
     return _LIB
 
@@ -110,6 +116,57 @@ class RefTree:
         dist = np.empty(n, np.float32)
         fn(self.h, _p(r), n, _p(tid), _p(dist), threads)
         return tid, dist
+
+
+class _PtObject(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("color", ctypes.c_float * 3), ("coeff", ctypes.c_float),
+                ("diffuse_color", ctypes.c_float * 3), ("ior", ctypes.c_float), ("decay", ctypes.c_float * 3),
+                ("has_normals", ctypes.c_uint32)]
+
+
+class _PtCamera(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("sight_dist", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("position", ctypes.c_float * 3), ("focus", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3)]
+
+
+class RefPathTracer:
+    """The reference's PathTracer restated on the CPU (rxo_pt.cpp) over the reference's
+    own tree and traversal: surface materials, objects that neither overlap nor nest."""
+
+    def __init__(self, scene, policy: int = SPLIT_GCC, tree: "RefTree | None" = None):
+        f = scene.flatten()
+        self.tree = tree if tree is not None else RefTree(f["verts"], f["tris"], policy)
+        self._tri_obj = np.ascontiguousarray(f["tri_obj"], np.uint32)
+        self._normals = np.ascontiguousarray(f["normals"], np.float32)
+        objs = (_PtObject * len(scene.objects))()
+        for k, o in enumerate(scene.objects):
+            m = o.material
+            objs[k].kind = m.kind
+            objs[k].color[:] = m.color
+            objs[k].coeff = m.coeff
+            objs[k].diffuse_color[:] = m.diffuse_color
+            objs[k].ior = -1.0 if m.kind == 5 else m.ior
+            objs[k].decay[:] = m.decay
+            objs[k].has_normals = int(f["has_normals"][k])
+        self._objs = objs
+
+    def render(self, camera, spp: int, max_depth: int = 8, rr_mode: int = 0, seed: int = 1, crop=None,
+               threads: int = 0, want_sq: bool = False):
+        """Per-pixel mean over spp samples of the crop (x0, y0, w, h) (default the whole
+        image) as (h, w, 3) float64, the mean of squares (want_sq) or None, and the
+        number of closest-hit queries traced."""
+        x0, y0, w, h = crop if crop is not None else (0, 0, camera.width, camera.height)
+        cam = _PtCamera(camera.width, camera.height, camera.sight_dist, 0)
+        cam.position[:] = camera.position
+        cam.focus[:] = camera.focus
+        cam.up[:] = camera.up
+        s = np.zeros((h, w, 3), np.float64)
+        q = np.zeros((h, w, 3), np.float64) if want_sq else None
+        rays = lib().rxo_pt_render(self.tree.h, _p(self._tri_obj), _p(self._normals), ctypes.byref(self._objs),
+                                   len(self._objs), ctypes.byref(cam), x0, y0, w, h, spp, max_depth, rr_mode, seed,
+                                   threads, _p(s), None if q is None else _p(q))
+        return s / spp, (q / spp if q is not None else None), int(rays)
 
 
 def box_test(mn, mx, o, d) -> float:

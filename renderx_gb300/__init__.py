@@ -219,7 +219,9 @@ class Context:
 
     def render_pt_batch(self, items, paths_per_pass: int = 0, use_graph: bool = True, autotune: bool = False):
         """Renders several scenes in one wavefront. items: list of (Context, Camera,
-        dict(spp, max_depth, rr_mode, nee, seed)). Returns (list of (H,W,3) means, stats)."""
+        dict(spp, max_depth, rr_mode, nee, seed, guided)); guided items use their
+        context's network (guide_init on that context). Returns (list of (H,W,3) means,
+        stats)."""
         arr = (_capi.rx_batch_item * len(items))()
         films = []
         for k, (ctx, cam, o) in enumerate(items):
@@ -228,7 +230,8 @@ class Context:
             arr[k].scene = ctx.h
             arr[k].camera = camera_struct(cam)
             arr[k].options = rx_pt_options(o.get("spp", 16), o.get("max_depth", 8), o.get("rr_mode", 0),
-                                           int(bool(o.get("nee", False))), o.get("seed", 1), 0, 0)
+                                           int(bool(o.get("nee", False))), o.get("seed", 1), 0,
+                                           1 if o.get("guided", False) else 0)
             arr[k].film_rgb = film.ctypes.data
         bo = _capi.rx_batch_options(paths_per_pass, int(use_graph), int(autotune), 0, 0, 0)
         st = rx_render_stats()
@@ -251,7 +254,7 @@ class Context:
         st = rx_render_stats()
         self._ck(self._L.rx_render_vcm(self.h, ctypes.byref(cam), ctypes.byref(o), _capi.ptr(film), ctypes.byref(st)))
         return film, dict(rays=st.extension_rays, shadow_rays=st.shadow_rays, merges=st.merges, paths=st.paths,
-                          ms=st.ms)
+                          ms=st.ms, merge_ms=st.merge_ms, merge_queries=st.merge_queries, photons=st.photons)
 
     def render_bpt(self, camera: "scenes.Camera", iterations: int, max_depth: int = 8, seed: int = 1,
                    full_path_mis: bool = False, time_budget_s: float = 0.0):

@@ -80,7 +80,8 @@ class rx_pm_options(ctypes.Structure):
 
 class rx_render_stats(ctypes.Structure):
     _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64), ("paths", ctypes.c_uint64),
-                ("ms", ctypes.c_float), ("reserved", ctypes.c_float), ("merges", ctypes.c_uint64)]
+                ("ms", ctypes.c_float), ("merge_ms", ctypes.c_float), ("merges", ctypes.c_uint64),
+                ("merge_queries", ctypes.c_uint64), ("photons", ctypes.c_uint64)]
 
 
 class rx_guide_options(ctypes.Structure):

@@ -406,9 +406,12 @@ rx_status rx_render_pt_batch(rx_context* c, const rx_batch_item* items, uint32_t
       return c->fail(RX_ERR_INVALID, "time_budget_s applies to rx_render_pt only; reserved 0");
     if (it.options.nee && it.scene->scene.num_lights == 0)
       return c->fail(RX_ERR_INVALID, "light sampling needs an emissive object");
-    if (it.options.flags & RX_PT_GUIDED)
-      return c->fail(RX_ERR_UNSUPPORTED, "guided rendering of batches is not supported (rx_render_pt only)");
-    if (it.options.flags) return c->fail(RX_ERR_INVALID, "unknown flags");
+    if (it.options.flags & ~RX_PT_GUIDED) return c->fail(RX_ERR_INVALID, "unknown flags");
+    if (it.options.flags & RX_PT_GUIDED) {
+      if (it.options.nee) return c->fail(RX_ERR_INVALID, "guiding applies to PathTracer (nee = 0)");
+      if (!rx::guide_ready(it.scene->guide))
+        return c->fail(RX_ERR_STATE, "guided batch item needs rx_guide_init on its scene's context");
+    }
     jobs[k] = rx::PtJob{it.scene, cam, it.options, pixels};
     pixels += (uint64_t)cam.width * cam.height;
   }

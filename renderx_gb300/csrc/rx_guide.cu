@@ -16,6 +16,7 @@
 // radiance) / (sampling density) of sample s. The training kernel runs forward and
 // backward per tile and accumulates every layer's weight gradient in tensor memory
 // across all tiles a CTA processes; one flush per CTA adds them to the FP32 gradient.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -346,9 +347,9 @@ struct RecordIO {
   struct Pre {
     float4 a, b, c;
   };
-  __device__ Pre prefetch(uint32_t i, uint32_t n) const {
+  __device__ Pre prefetch(uint32_t i, bool valid) const {
     Pre p{};
-    if (i < n) {
+    if (valid) {
       const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * kRec);
       p.a = r[0];
       p.b = r[1];
@@ -356,11 +357,11 @@ struct RecordIO {
     }
     return p;
   }
-  __device__ bool finish(const Pre& p, uint32_t i, uint32_t n, float (&q)[9], float (&wi)[3]) const {
+  __device__ bool finish(const Pre& p, uint32_t, bool valid, float (&q)[9], float (&wi)[3]) const {
     q[0] = p.a.x; q[1] = p.a.y; q[2] = p.a.z; q[3] = p.a.w; q[4] = p.b.x; q[5] = p.b.y; q[6] = p.b.z; q[7] = p.b.w;
     q[8] = p.c.x;
     wi[0] = p.c.y; wi[1] = p.c.z; wi[2] = p.c.w;
-    return i < n;
+    return valid;
   }
   __device__ void store(uint32_t i, const float (&raw)[48], const float (&wi)[3]) const {
     if (raw_out) {
@@ -373,9 +374,10 @@ struct RecordIO {
 };
 
 // Queries from the wavefront: the hit point of each live path, if its surface is guided
-// (diffuse, glossy or Phong, seen from the front, the path not inside an object).
+// (diffuse, glossy or Phong, seen from the front, the path not inside an object). The
+// path's scene is scenes[info.w >> 16].
 struct PathIO {
-  DevScene S;
+  const DevScene* scenes;
   PathSoA P;
   const int2* hit;
   float* lobes;
@@ -384,10 +386,10 @@ struct PathIO {
     int4 inf;
     float4 o, d;
   };
-  __device__ Pre prefetch(uint32_t i, uint32_t n) const {
+  __device__ Pre prefetch(uint32_t i, bool valid) const {
     Pre p;
     p.h = make_int2(-1, 0);
-    if (i < n) {
+    if (valid) {
       p.h = hit[i];
       p.inf = P.info[i];
       p.o = P.o[i];
@@ -395,9 +397,10 @@ struct PathIO {
     }
     return p;
   }
-  __device__ bool finish(const Pre& p, uint32_t i, uint32_t n, float (&q)[9], float (&wi)[3]) const {
+  __device__ bool finish(const Pre& p, uint32_t i, bool valid, float (&q)[9], float (&wi)[3]) const {
     wi[0] = wi[1] = wi[2] = 0.0f;
-    if (i >= n) return false;
+    if (!valid) return false;
+    const DevScene& S = scenes[(uint32_t)p.inf.w >> 16];
     bool ok = p.h.x >= 0 && p.inf.z < 0;
     int obj = ok ? (int)__ldg(&S.tri_obj[p.h.x]) : -1;
     if (ok) {
@@ -446,45 +449,106 @@ __device__ __forceinline__ bool wg_and(int g, bool v) {
   return r != 0;
 }
 
+// Network k of a grouped launch: the segment of seg[0..nnet] holding row r.
+__device__ __forceinline__ int seg_of(const uint32_t* seg, int nnet, uint32_t r) {
+  int lo = 0, hi = nnet - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&seg[mid]) <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Persistent inference: kInferTiles warpgroups per CTA share the weight image and each
 // runs its own 128-sample tiles through the five layers (its own input / activation
 // buffers, TMEM columns 64 g .. 64 g + 63, mbarrier, and MMA-issuing thread), so several
 // tiles' MMA -> epilogue chains interleave on the SM. The next tile's inputs are loaded
-// while the current one runs.
-template <class IO>
+// while the current one runs. A CTA's step covers kInferTiles consecutive tiles (tile
+// 4 st + g for warpgroup g).
+//
+// GROUPED: rows[r] (or -1 for padding) name the queries, and network k owns rows
+// [seg[k], seg[k + 1]) (multiples of kGroupRows, so a step's four tiles share one
+// network). When a step's network differs from the staged one, the CTA waits until every
+// warpgroup is done with the old weights and stages the new ones (bulk copy, 43 KB).
+// Steps run in increasing row order per CTA, so a CTA stages each network at most once.
+// Every warpgroup runs the same number of steps; a failed wait skips the remaining work
+// instead of leaving the loop, so the CTA-wide barriers stay matched.
+template <class IO, bool GROUPED>
 __global__ void __launch_bounds__(128 * kInferTiles, 1)
-    k_guide_infer(IO io, const unsigned* count, uint32_t n_host, const unsigned char* img, Box box, int* status) {
+    k_guide_infer(IO io, const unsigned* count, uint32_t n_host, const NetDev* nets, int nnet, const int* rows,
+                  const uint32_t* seg, const uint32_t* pass) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar_mma[kInferTiles], bar_w;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, s = tid & 127;
-  const uint32_t n = count ? *count : n_host;
-  const uint32_t ntiles = (n + kTile - 1) / kTile;
-  if (blockIdx.x * kInferTiles >= ntiles) return;
+  uint32_t n = 0, nsteps;
+  if constexpr (GROUPED) {
+    nsteps = __ldg(&seg[nnet]) / kGroupRows;
+  } else {
+    if (pass && *pass < nets[0].warmup) return;
+    n = count ? *count : n_host;
+    nsteps = (n + kGroupRows - 1) / kGroupRows;
+  }
+  if (blockIdx.x >= nsteps) return;
   if (tid == 0) {
     for (int k = 0; k < kInferTiles; k++) tc::mbar_init(&bar_mma[k], 1);
     tc::mbar_init(&bar_w, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
-  if (tid == 0) load_weights(sm, img, &bar_w);
+  int net = GROUPED ? seg_of(seg, nnet, blockIdx.x * kGroupRows) : 0;
+  if (tid == 0) load_weights(sm, nets[net].img, &bar_w);
   if (warp == 0) tc::tmem_alloc(&tmem_base, 64 * kInferTiles);
   tc_sync();
   const uint32_t tcol = tmem_base + 64u * (uint32_t)g;
   const uint32_t tacc = tcol + ((uint32_t)((warp & 3) * 32) << 16);
   bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0));
+  uint32_t wph = 1;
+  Box box = nets[net].box;
   uint32_t ph = 0;
   unsigned char* A0 = sm + kImgBytes + (uint32_t)g * kInferTileBytes;
   unsigned char* A1 = A0 + 128 * kIn * 2;
-  const uint32_t tstride = gridDim.x * kInferTiles;
-  uint32_t tile = blockIdx.x * kInferTiles + (uint32_t)g;
-  typename IO::Pre pre = io.prefetch(tile * kTile + s, tile < ntiles ? n : 0u);
-  for (; ok && tile < ntiles; tile += tstride) {
-    const uint32_t i = tile * kTile + s;
+  // the query of row r: its index and whether it exists
+  auto query = [&](uint32_t r, uint32_t& i) -> bool {
+    if constexpr (GROUPED) {
+      if (r >= nsteps * kGroupRows) return false;
+      int q = __ldg(&rows[r]);
+      i = (uint32_t)q;
+      return q >= 0;
+    } else {
+      i = r;
+      return r < n;
+    }
+  };
+  uint32_t st = blockIdx.x;
+  uint32_t qi = 0;
+  bool qv = query((st * kInferTiles + (uint32_t)g) * kTile + (uint32_t)s, qi);
+  typename IO::Pre pre = io.prefetch(qi, qv);
+  for (; st < nsteps; st += gridDim.x) {
+    if constexpr (GROUPED) {
+      const int j = seg_of(seg, nnet, st * kGroupRows);  // the same for the whole CTA
+      if (j != net) {
+        tc::tc_fence_before();
+        ok = __syncthreads_and(ok);  // every warpgroup's MMAs on the old weights are complete
+        tc::tc_fence_after();
+        if (ok && tid == 0) load_weights(sm, nets[j].img, &bar_w);
+        if (ok) ok = __syncthreads_and(tc::mbar_wait(&bar_w, wph));
+        wph ^= 1;
+        net = j;
+        box = nets[j].box;
+      }
+    } else {
+      if (!ok) break;
+    }
+    const uint32_t tile = st * kInferTiles + (uint32_t)g;
+    const uint32_t i = qi;
     float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0};
-    const bool valid = io.finish(pre, i, n, q, wi);
-    const uint32_t next = tile + tstride;
-    pre = io.prefetch(next * kTile + s, next < ntiles ? n : 0u);
+    const bool valid = io.finish(pre, i, qv, q, wi);
+    qv = query(((st + gridDim.x) * kInferTiles + (uint32_t)g) * kTile + (uint32_t)s, qi);
+    pre = io.prefetch(qi, qv);
+    if (!GROUPED && tile * kTile >= n) continue;  // this warpgroup's tile is past the end
+    if (!ok) continue;
     encode_row(q, valid, box, A0, s);
     wg_sync(g);
     float raw[48];
@@ -505,38 +569,56 @@ __global__ void __launch_bounds__(128 * kInferTiles, 1)
     }
     if (ok && valid) io.store(i, raw, wi);
   }
-  if (!ok && s == 0) atomicExch(status, 1);
+  if (!ok && s == 0) atomicExch(nets[net].status, 1);
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem_base, 64 * kInferTiles);
 }
 
-// ---- training --------------------------------------------------------------------------
+// ---- training ----------------------------------------------------------------------
 // The records a training step reads: with step >= 0, the step-th window of `len` records
-// of the live count (device count clipped to n_host, wrapping); else [first, first + len)
-// clipped to n_host.
-__device__ __forceinline__ void train_window(const unsigned* count, uint32_t n_host, uint32_t first, uint32_t len,
-                                             int step, uint32_t& lo, uint32_t& hi) {
-  uint32_t n = count ? min(*count, n_host) : n_host;
+// of the live count (device count clipped to cap, wrapping); else the first `len`
+// records (clipped to cap).
+__device__ __forceinline__ void train_window(const RecSeg& R, int step, uint32_t& lo, uint32_t& hi) {
+  uint32_t n = R.count ? min(*R.count, R.cap) : R.cap;
   if (step >= 0) {
-    uint32_t L = min(len, n);
-    lo = n > len ? (uint32_t)(((uint64_t)step * len) % (n - len + 1)) : 0u;
+    uint32_t L = min(R.len, n);
+    lo = n > R.len ? (uint32_t)(((uint64_t)step * R.len) % (n - R.len + 1)) : 0u;
     hi = lo + L;
   } else {
-    lo = min(first, n);
-    hi = min(first + len, n);
+    lo = 0;
+    hi = min(R.len, n);
   }
 }
 
-// Sum of record weights and number of records (for the loss normalisation).
-__global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t n_host, uint32_t first,
-                             uint32_t len, int step, float* out) {
+// Whether a network takes training step `step` of the render pass *pass (pass null:
+// outside a render, always): inside its training passes and its steps per pass.
+__device__ __forceinline__ bool net_trains(const NetDev& N, const uint32_t* pass, int step) {
+  return !pass || (*pass < N.train && (uint32_t)step < N.steps_per_pass);
+}
+
+// Clears each training network's step scratch (weight sum, count, loss).
+__global__ void k_net_clear(const NetDev* nets, int nnet, const uint32_t* pass, int step) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nnet && net_trains(nets[j], pass, step)) {
+    nets[j].scratch[0] = 0.0f;
+    nets[j].scratch[1] = 0.0f;
+    nets[j].scratch[2] = 0.0f;
+  }
+}
+
+// Sum of record weights and number of records per network (the loss normalisation);
+// blocks [j * per, (j + 1) * per) serve network j.
+__global__ void k_weight_sum(const NetDev* nets, const RecSeg* segs, int per, int step, const uint32_t* pass) {
+  const int j = blockIdx.x / per;
+  if (!net_trains(nets[j], pass, step)) return;
+  const RecSeg R = segs[j];
   uint32_t lo, end;
-  train_window(count, n_host, first, len, step, lo, end);
+  train_window(R, step, lo, end);
   float acc = 0.0f;
   unsigned c = 0;
-  for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
-    acc += recs[(size_t)i * kRec + 12];
+  for (uint32_t i = lo + (blockIdx.x % per) * blockDim.x + threadIdx.x; i < end; i += per * blockDim.x) {
+    acc += R.recs[(size_t)i * kRec + 12];
     c++;
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -544,16 +626,16 @@ __global__ void k_weight_sum(const float* recs, const unsigned* count, uint32_t 
     c += __shfl_xor_sync(0xffffffffu, c, o);
   }
   if ((threadIdx.x & 31) == 0 && c) {
-    atomicAdd(out, acc);
-    atomicAdd(out + 1, (float)c);
+    atomicAdd(nets[j].scratch, acc);
+    atomicAdd(nets[j].scratch + 1, (float)c);
   }
 }
 
 // Gradient of the batch loss over the records a window selects (train_window): forward
 // and backward per tile, weight gradients accumulated in tensor memory across all tiles
-// a CTA processes, flushed once per CTA into `grad` (FP32, row-major per layer).
-// wsum = {sum w, count}; weights are clipped at 32 x their batch mean before
-// normalisation by the sum.
+// a CTA processes, flushed once per CTA into the network's FP32 gradient. The network's
+// scratch holds {sum w, count}; weights are clipped at 32 x their batch mean before
+// normalisation by the sum. CTAs [j * per, (j + 1) * per) train network j.
 //
 // A CTA carries kTrainTiles tiles of 128 samples at once, one warpgroup per tile (thread
 // s of warpgroup g owns sample s of tile g, TMEM lane s of that tile's accumulator). The
@@ -577,25 +659,31 @@ __device__ __forceinline__ void load_record(const float* recs, uint32_t i, float
 }
 
 __global__ void __launch_bounds__(128 * kTrainTiles, 1)
-    k_guide_train(const float* recs, const unsigned* count, uint32_t n_host, uint32_t first0, uint32_t len, int step,
-                  const unsigned char* img, Box box, const float* wsum, float* grad, float* loss_sum, int* status) {
+    k_guide_train(const NetDev* nets, const RecSeg* segs, int per, int step, const uint32_t* pass) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t bar_mma[kTrainTiles], bar_w;
   __shared__ uint32_t tmem_base;
   __shared__ float red[4 * kTrainTiles];
   const int tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, s = tid & 127;
+  const int j = blockIdx.x / per, part = blockIdx.x % per;
+  const NetDev& N = nets[j];
+  if (!net_trains(N, pass, step)) return;
+  const RecSeg R = segs[j];
+  const float* recs = R.recs;
+  const Box box = N.box;
+  float* grad = N.grad;
   uint32_t first, end;
-  train_window(count, n_host, first0, len, step, first, end);
+  train_window(R, step, first, end);
   const uint32_t n = end - first;
   const uint32_t ntiles = (n + kTile - 1) / kTile;
-  if (blockIdx.x * kTrainTiles >= ntiles) return;
+  if ((uint32_t)part * kTrainTiles >= ntiles) return;
   if (tid == 0) {
     for (int k = 0; k < kTrainTiles; k++) tc::mbar_init(&bar_mma[k], 1);
     tc::mbar_init(&bar_w, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
-  if (tid == 0) load_weights(sm, img, &bar_w);
+  if (tid == 0) load_weights(sm, N.img, &bar_w);
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   tc_sync();
   const uint32_t T0 = tmem_base;
@@ -613,7 +701,7 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
   unsigned char* Al[5] = {A34, A1, A2, A34, A34 + kActBytes};
   const uint32_t tacc_col = T0 + 64u * (uint32_t)g;
   const uint32_t t_acc = tacc_col + lane_off;
-  const float total = wsum[0], cnt = fmaxf(wsum[1], 1.0f);
+  const float total = N.scratch[0], cnt = fmaxf(N.scratch[1], 1.0f);
   const float wclip = 32.0f * total / cnt;
   const float inv_total = total > 0.0f ? 1.0f / total : 0.0f;
   tc::tc_fence_before();
@@ -621,8 +709,8 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
   tc::tc_fence_after();
   uint32_t ph = 0;
   float loss = 0.0f;
-  for (uint32_t tile = blockIdx.x * kTrainTiles + (uint32_t)g; ok && tile < ntiles;
-       tile += gridDim.x * kTrainTiles) {
+  for (uint32_t tile = (uint32_t)part * kTrainTiles + (uint32_t)g; ok && tile < ntiles;
+       tile += (uint32_t)per * kTrainTiles) {
     const uint32_t i = first + tile * kTile + s;
     const bool valid = i < end;
     float q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, wi[3] = {0, 0, 0}, w = 0.0f;
@@ -735,13 +823,13 @@ __global__ void __launch_bounds__(128 * kTrainTiles, 1)
   }
   for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
   if ((tid & 31) == 0) red[warp] = loss;
-  if (!ok && tid == 0) atomicExch(status, 1);
+  if (!ok && tid == 0) atomicExch(N.status, 1);
   tc::tc_fence_before();
   __syncthreads();
   if (tid == 0) {
     float t = 0.0f;
     for (int k = 0; k < 4 * kTrainTiles; k++) t += red[k];
-    atomicAdd(loss_sum, t);
+    atomicAdd(N.scratch + 2, t);
   }
   if (warp == 0) tc::tmem_dealloc(T0, 512);
 }
@@ -759,20 +847,30 @@ __global__ void k_make_image(const float* w, unsigned char* img) {
   if (i < kParams) image_store(img, i, w[i]);
 }
 
-// Adam (bias-corrected), then the BF16 image; clears the gradient.
-__global__ void k_adam(float* w, float* m, float* v, float* g, unsigned char* img, float lr, float b1, float b2,
-                       float eps, float c1, float c2) {
+// Adam (bias-corrected with the network's step count), then the BF16 image; clears the
+// gradient. blockIdx.y = network.
+__global__ void k_adam(const NetDev* nets, const uint32_t* pass, int step, float b1, float b2, float eps) {
+  const NetDev& N = nets[blockIdx.y];
+  if (!net_trains(N, pass, step)) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kParams) return;
-  float gi = g[i];
-  g[i] = 0.0f;
-  float mi = b1 * m[i] + (1.0f - b1) * gi;
-  float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
-  m[i] = mi;
-  v[i] = vi;
-  float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
-  w[i] = wi;
-  image_store(img, i, wi);
+  const float t = (float)(*N.step + 1u);
+  const float c1 = 1.0f / (1.0f - powf(b1, t)), c2 = 1.0f / (1.0f - powf(b2, t));
+  float gi = N.grad[i];
+  N.grad[i] = 0.0f;
+  float mi = b1 * N.m[i] + (1.0f - b1) * gi;
+  float vi = b2 * N.v[i] + (1.0f - b2) * gi * gi;
+  N.m[i] = mi;
+  N.v[i] = vi;
+  float wi = N.params[i] - N.lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  N.params[i] = wi;
+  image_store(const_cast<unsigned char*>(N.img), i, wi);
+}
+
+// Counts the Adam step of every training network (after k_adam read the old count).
+__global__ void k_net_step(const NetDev* nets, int nnet, const uint32_t* pass, int step) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nnet && net_trains(nets[j], pass, step)) *nets[j].step += 1u;
 }
 
 }  // namespace rx
@@ -815,18 +913,36 @@ namespace rx {
 struct GuideState {
   rx_guide_options opt{};
   guide::Box box{};
-  DevBuf params, m, v, grad, img, scratch, status;  // scratch: {sum w, count, loss}
-  uint32_t step = 0;
+  // params, Adam moments, gradient, BF16 image; scratch {sum w, count, loss}; status;
+  // step count; device copies of this network's NetDev and of the record segment the
+  // single-network entry points train on
+  DevBuf params, m, v, grad, img, scratch, status, step, dnet, dseg;
   int sms = 152;
   bool ready = false;
 };
 
 void guide_free(GuideState* g) { delete g; }
 bool guide_ready(const GuideState* g) { return g && g->ready; }
-float guide_bsdf_fraction(const GuideState* g) { return g->opt.bsdf_fraction; }
-uint32_t guide_train_passes(const GuideState* g) { return g->opt.train_passes; }
-uint32_t guide_steps_per_pass(const GuideState* g) { return g->opt.steps_per_pass; }
-uint32_t guide_warmup_passes(const GuideState* g) { return g->opt.warmup_passes; }
+
+NetDev guide_net(const GuideState* g) {
+  NetDev N{};
+  N.img = g->img.as<unsigned char>();
+  N.params = g->params.as<float>();
+  N.m = g->m.as<float>();
+  N.v = g->v.as<float>();
+  N.grad = g->grad.as<float>();
+  N.scratch = g->scratch.as<float>();
+  N.status = g->status.as<int>();
+  N.step = g->step.as<uint32_t>();
+  N.box = g->box;
+  N.lr = g->opt.learning_rate;
+  N.frac = g->opt.bsdf_fraction;
+  N.batch = g->opt.batch;
+  N.warmup = g->opt.warmup_passes;
+  N.train = g->opt.train_passes;
+  N.steps_per_pass = g->opt.steps_per_pass;
+  return N;
+}
 
 // Opts the network kernels into their shared-memory sizes, once per device.
 static void set_kernel_smem() {
@@ -834,51 +950,66 @@ static void set_kernel_smem() {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && (done_mask >> dev) & 1) return;
-  cudaFuncSetAttribute(k_guide_infer<RecordIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
-  cudaFuncSetAttribute(k_guide_infer<PathIO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
+  cudaFuncSetAttribute(k_guide_infer<RecordIO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
+  cudaFuncSetAttribute(k_guide_infer<PathIO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
+  cudaFuncSetAttribute(k_guide_infer<PathIO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmInfer);
   cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTrain2);
   if (dev < 64) done_mask |= 1ull << dev;
 }
 
-cudaError_t guide_infer_paths(GuideState* g, const DevScene& S, const PathSoA& P, const unsigned* count,
-                              const int2* hit, float* lobes, int grid, cudaStream_t s) {
+void guide_prepare() { set_kernel_smem(); }
+
+cudaError_t guide_infer_wave(const NetDev* nets, int nnet, const DevScene* scenes, const PathSoA& P,
+                             const unsigned* count, const int2* hit, float* lobes, const int* rows,
+                             const uint32_t* seg, const uint32_t* pass, int sms, cudaStream_t s) {
   set_kernel_smem();
-  PathIO io{S, P, hit, lobes};
-  k_guide_infer<PathIO><<<grid, 128 * kInferTiles, kSmInfer, s>>>(io, count, 0, g->img.as<unsigned char>(), g->box,
-                                                                   g->status.as<int>());
+  PathIO io{scenes, P, hit, lobes};
+  if (rows)
+    k_guide_infer<PathIO, true><<<sms, 128 * kInferTiles, kSmInfer, s>>>(io, nullptr, 0, nets, nnet, rows, seg, pass);
+  else
+    k_guide_infer<PathIO, false><<<sms, 128 * kInferTiles, kSmInfer, s>>>(io, count, 0, nets, 1, nullptr, nullptr,
+                                                                           pass);
   return cudaGetLastError();
 }
 
-// One Adam step (or, without update, the gradient alone) on the records a window
-// selects (train_window).
-static cudaError_t train_step(GuideState* g, const float* recs, const unsigned* count, uint32_t n, uint32_t first,
-                              uint32_t len, int step, cudaStream_t s, bool update) {
+// CTAs per network of a training launch: enough for its batch, and together about one
+// per SM.
+static int train_ctas_per_net(uint32_t batch, int nnet, int sms) {
+  int need = (int)((batch + kTile * kTrainTiles - 1) / (kTile * kTrainTiles));
+  return std::max(1, std::min(need, (sms + nnet - 1) / nnet));
+}
+
+// One training step of every network (gradient, and with `update` Adam and the step
+// count) on the window `step` of its records (step < 0: the first len records).
+static cudaError_t train_nets_step(const NetDev* nets, const RecSeg* segs, int nnet, int per, int step,
+                                   const uint32_t* pass, bool update, int sms, cudaStream_t s) {
   set_kernel_smem();
-  float* sc = g->scratch.as<float>();
-  cudaMemsetAsync(sc, 0, 3 * sizeof(float), s);
-  k_weight_sum<<<g->sms * 4, 256, 0, s>>>(recs, count, n, first, len, step, sc);
-  uint32_t groups = (std::min(len, n) + kTile * kTrainTiles - 1) / (kTile * kTrainTiles);
-  uint32_t grid = std::min<uint32_t>(groups, (uint32_t)g->sms);
-  if (grid == 0) return cudaGetLastError();
-  k_guide_train<<<grid, 128 * kTrainTiles, kSmTrain2, s>>>(recs, count, n, first, len, step, g->img.as<unsigned char>(), g->box, sc,
-                                            g->grad.as<float>(), sc + 2, g->status.as<int>());
+  k_net_clear<<<(nnet + 127) / 128, 128, 0, s>>>(nets, nnet, pass, step);
+  const int wper = std::max(1, std::min(4 * sms / nnet, 64));
+  k_weight_sum<<<nnet * wper, 256, 0, s>>>(nets, segs, wper, step, pass);
+  k_guide_train<<<nnet * per, 128 * kTrainTiles, kSmTrain2, s>>>(nets, segs, per, step, pass);
   if (update) {
-    g->step++;
-    const float b1 = 0.9f, b2 = 0.999f;
-    float c1 = 1.0f / (1.0f - powf(b1, (float)g->step)), c2 = 1.0f / (1.0f - powf(b2, (float)g->step));
-    k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(g->params.as<float>(), g->m.as<float>(), g->v.as<float>(),
-                                                 g->grad.as<float>(), g->img.as<unsigned char>(),
-                                                 g->opt.learning_rate, b1, b2, 1e-8f, c1, c2);
+    k_adam<<<dim3((kParams + 255) / 256, nnet), 256, 0, s>>>(nets, pass, step, 0.9f, 0.999f, 1e-8f);
+    k_net_step<<<(nnet + 127) / 128, 128, 0, s>>>(nets, nnet, pass, step);
   }
   return cudaGetLastError();
 }
 
-cudaError_t guide_train_records(GuideState* g, const float* recs, const unsigned* count, uint32_t n_max, int steps,
-                                cudaStream_t s) {
+cudaError_t guide_train_nets(const NetDev* nets, const RecSeg* segs, int nnet, int steps, uint32_t batch_max,
+                             const uint32_t* pass, int sms, cudaStream_t s) {
+  const int per = train_ctas_per_net(batch_max, nnet, sms);
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < steps && e == cudaSuccess; k++)
-    e = train_step(g, recs, count, n_max, 0, g->opt.batch, k, s, true);
+  for (int k = 0; k < steps && e == cudaSuccess; k++) e = train_nets_step(nets, segs, nnet, per, k, pass, true, sms, s);
   return e;
+}
+
+// One step of this network alone on n device records (the single-network entry points).
+static cudaError_t train_step(GuideState* g, const float* recs, uint32_t n, cudaStream_t s, bool update) {
+  RecSeg R{recs, nullptr, n, n};
+  cudaError_t e = cudaMemcpyAsync(g->dseg.p, &R, sizeof R, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  const int per = train_ctas_per_net(n, 1, g->sms);
+  return train_nets_step(g->dnet.as<NetDev>(), g->dseg.as<RecSeg>(), 1, per, -1, nullptr, update, g->sms, s);
 }
 
 }  // namespace rx
@@ -927,6 +1058,9 @@ extern "C" rx_status rx_guide_init(rx_context* c, const rx_guide_options* opt, c
   if (s == RX_OK) s = c->cuda(g->img.alloc(rx::guide::kImgBytes), "allocate guide image");
   if (s == RX_OK) s = c->cuda(g->scratch.alloc(64), "allocate guide scratch");
   if (s == RX_OK) s = c->cuda(g->status.alloc(16), "allocate guide status");
+  if (s == RX_OK) s = c->cuda(g->step.alloc(16), "allocate guide step count");
+  if (s == RX_OK) s = c->cuda(g->dnet.alloc(sizeof(rx::guide::NetDev)), "allocate guide view");
+  if (s == RX_OK) s = c->cuda(g->dseg.alloc(sizeof(rx::guide::RecSeg)), "allocate guide records view");
   if (s != RX_OK) {
     delete g;
     return s;
@@ -948,6 +1082,9 @@ extern "C" rx_status rx_guide_init(rx_context* c, const rx_guide_options* opt, c
   for (DevBuf* b : {&g->m, &g->v, &g->grad}) cudaMemset(b->p, 0, pb);
   cudaMemset(g->img.p, 0, rx::guide::kImgBytes);
   cudaMemset(g->status.p, 0, 16);
+  cudaMemset(g->step.p, 0, 16);
+  const rx::guide::NetDev view = rx::guide_net(g);
+  cudaMemcpy(g->dnet.p, &view, sizeof view, cudaMemcpyHostToDevice);
   rx::k_make_image<<<(rx::guide::kParams + 255) / 256, 256, 0, c->stream>>>(g->params.as<float>(),
                                                                              g->img.as<unsigned char>());
   s = c->cuda(cudaStreamSynchronize(c->stream), "guide init");
@@ -978,9 +1115,10 @@ extern "C" rx_status rx_guide_set_params(rx_context* c, const float* params) {
   DeviceGuard dg(c->device);
   rx::GuideState* g = c->guide;
   const size_t pb = rx::guide::kParams * sizeof(float);
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide sync")) != RX_OK) return s;
   cudaMemcpy(g->params.p, params, pb, cudaMemcpyHostToDevice);
   for (DevBuf* b : {&g->m, &g->v, &g->grad}) cudaMemset(b->p, 0, pb);
-  g->step = 0;
+  cudaMemset(g->step.p, 0, 16);
   rx::k_make_image<<<(rx::guide::kParams + 255) / 256, 256, 0, c->stream>>>(g->params.as<float>(),
                                                                              g->img.as<unsigned char>());
   return c->cuda(cudaStreamSynchronize(c->stream), "set guide parameters");
@@ -1010,10 +1148,9 @@ extern "C" rx_status rx_guide_eval(rx_context* c, const float* recs, uint32_t n,
   cudaMemcpy(dr.p, recs, (size_t)n * rx::guide::kRec * 4, cudaMemcpyHostToDevice);
   rx::set_kernel_smem();
   rx::RecordIO io{dr.as<float>(), draw.as<float>(), dp.as<float>()};
-  uint32_t tiles = (n + rx::guide::kTile - 1) / rx::guide::kTile;
-  uint32_t grid = std::min<uint32_t>((tiles + rx::kInferTiles - 1) / rx::kInferTiles, (uint32_t)g->sms);
-  rx::k_guide_infer<rx::RecordIO><<<grid, 128 * rx::kInferTiles, rx::kSmInfer, c->stream>>>(
-      io, nullptr, n, g->img.as<unsigned char>(), g->box, g->status.as<int>());
+  uint32_t grid = std::min<uint32_t>((n + rx::guide::kGroupRows - 1) / rx::guide::kGroupRows, (uint32_t)g->sms);
+  rx::k_guide_infer<rx::RecordIO, false><<<grid, 128 * rx::kInferTiles, rx::kSmInfer, c->stream>>>(
+      io, nullptr, n, g->dnet.as<rx::guide::NetDev>(), 1, nullptr, nullptr, nullptr);
   if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide eval")) != RX_OK) return s;
   if ((s = guide_status(c)) != RX_OK) return s;
   if (raw40) cudaMemcpy(raw40, draw.p, (size_t)n * rx::guide::kOutUsed * 4, cudaMemcpyDeviceToHost);
@@ -1032,11 +1169,10 @@ extern "C" rx_status rx_guide_eval_device(rx_context* c, const float* d_recs, ui
   rx::GuideState* g = c->guide;
   rx::set_kernel_smem();
   rx::RecordIO io{d_recs, d_raw40, d_pdf};
-  uint32_t tiles = (n + rx::guide::kTile - 1) / rx::guide::kTile;
-  uint32_t grid = std::min<uint32_t>((tiles + rx::kInferTiles - 1) / rx::kInferTiles, (uint32_t)g->sms);
+  uint32_t grid = std::min<uint32_t>((n + rx::guide::kGroupRows - 1) / rx::guide::kGroupRows, (uint32_t)g->sms);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  rx::k_guide_infer<rx::RecordIO><<<grid, 128 * rx::kInferTiles, rx::kSmInfer, st>>>(
-      io, nullptr, n, g->img.as<unsigned char>(), g->box, g->status.as<int>());
+  rx::k_guide_infer<rx::RecordIO, false><<<grid, 128 * rx::kInferTiles, rx::kSmInfer, st>>>(
+      io, nullptr, n, g->dnet.as<rx::guide::NetDev>(), 1, nullptr, nullptr, nullptr);
   return c->cuda(cudaGetLastError(), "guide eval");
 }
 
@@ -1050,7 +1186,7 @@ extern "C" rx_status rx_guide_gradient(rx_context* c, const float* recs, uint32_
   if ((s = c->cuda(dr.alloc((size_t)n * rx::guide::kRec * 4), "alloc")) != RX_OK) return s;
   cudaMemcpy(dr.p, recs, (size_t)n * rx::guide::kRec * 4, cudaMemcpyHostToDevice);
   cudaMemsetAsync(g->grad.p, 0, rx::guide::kParams * 4, c->stream);
-  cudaError_t e = rx::train_step(g, dr.as<float>(), nullptr, n, 0, n, -1, c->stream, false);
+  cudaError_t e = rx::train_step(g, dr.as<float>(), n, c->stream, false);
   if ((s = c->cuda(e, "guide gradient")) != RX_OK) return s;
   if ((s = c->cuda(cudaStreamSynchronize(c->stream), "guide gradient")) != RX_OK) return s;
   if ((s = guide_status(c)) != RX_OK) return s;
@@ -1067,7 +1203,7 @@ extern "C" rx_status rx_guide_train_step(rx_context* c, const float* d_recs, uin
   if (reinterpret_cast<uintptr_t>(d_recs) % 16) return c->fail(RX_ERR_INVALID, "records must be 16-byte aligned");
   DeviceGuard dg(c->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  cudaError_t e = rx::train_step(c->guide, d_recs, nullptr, n, 0, n, -1, st, true);
+  cudaError_t e = rx::train_step(c->guide, d_recs, n, st, true);
   if ((s = c->cuda(e, "guide train step")) != RX_OK) return s;
   if (loss) {
     if ((s = c->cuda(cudaStreamSynchronize(st), "guide train step")) != RX_OK) return s;

@@ -69,25 +69,64 @@ __device__ __forceinline__ F3 mix_sample(const float* L, float u0, float u1, flo
   return to_world(f, F3{sn * cp, c, sn * sp});
 }
 
+// One network as the kernels see it: its parameters, optimiser state and render
+// schedule. A render of several scenes carries one network per guided scene; the
+// grouped kernels take an array of these.
+struct NetDev {
+  const unsigned char* img;  // BF16 weight image (core-matrix layout)
+  float *params, *m, *v, *grad;
+  float* scratch;            // {sum of record weights, record count, loss} of the current step
+  int* status;               // set when a bounded tensor-core wait gave up
+  uint32_t* step;            // Adam steps taken
+  guide::Box box;            // position-encoding box
+  float lr;                  // Adam step size
+  float frac;                // one-sample MIS: probability of sampling the BSDF
+  uint32_t batch;            // records per Adam step
+  uint32_t warmup;           // render passes before the first guided pass
+  uint32_t train;            // render passes whose samples train the network
+  uint32_t steps_per_pass;   // Adam steps after each training pass
+};
+
+// The records one network trains on: `cap` slots at `recs` (guide::kRec floats each),
+// the live count at *count (device; null: all cap), `len` records per step.
+struct RecSeg {
+  const float* recs;
+  const unsigned* count;
+  uint32_t cap, len;
+};
+
+// Rows of a grouped inference: each network's rows are a segment padded to a multiple of
+// kGroupRows (one inference CTA's four tiles), so a CTA's tiles share one network.
+constexpr uint32_t kGroupRows = 4 * kTile;
+
 }  // namespace guide
 
 // Host-side state of a context's guiding network (rx_guide.cu).
 struct GuideState;
 void guide_free(GuideState* g);
-
-// Launches the inference kernel over the `n` live paths of a wavefront: for each path
-// whose hit is a guided surface, writes its mixture (guide::kLobeStride floats) to `lobes`.
-cudaError_t guide_infer_paths(GuideState* g, const DevScene& S, const PathSoA& P, const unsigned* count,
-                              const int2* hit, float* lobes, int grid, cudaStream_t s);
-// `steps` Adam steps on the record buffer whose live count (at most n_max) is device-
-// resident: step k trains on a window of `batch` records picked on the device, so no
-// host synchronisation is needed.
-cudaError_t guide_train_records(GuideState* g, const float* recs, const unsigned* count, uint32_t n_max,
-                                int steps, cudaStream_t s);
 bool guide_ready(const GuideState* g);
-float guide_bsdf_fraction(const GuideState* g);
-uint32_t guide_train_passes(const GuideState* g);
-uint32_t guide_steps_per_pass(const GuideState* g);
-uint32_t guide_warmup_passes(const GuideState* g);
+// The network's device view with its options (pointers into the state's buffers).
+guide::NetDev guide_net(const GuideState* g);
+// Sets the network kernels' shared-memory limits on the current device (call before
+// capturing their launches in a graph).
+void guide_prepare();
+
+// Launches the inference kernel over a wavefront's live paths: for each path whose hit is
+// a guided surface, writes its mixture (guide::kLobeStride floats) to `lobes`, else
+// lobes[i * kLobeStride] = -1. scenes: the paths' scenes (index info.w >> 16).
+// Ungrouped (rows null): one network (nets[0]) over queue entries 0..*count-1.
+// Grouped: rows[r] = queue entry or -1 over segments seg[0..nnet] (multiples of
+// kGroupRows), network k over rows [seg[k], seg[k + 1]). A network whose warm-up is not
+// over at pass *pass (device) is skipped.
+cudaError_t guide_infer_wave(const guide::NetDev* nets, int nnet, const DevScene* scenes, const PathSoA& P,
+                             const unsigned* count, const int2* hit, float* lobes, const int* rows,
+                             const uint32_t* seg, const uint32_t* pass, int sms, cudaStream_t s);
+// Adam steps of every network on its own records: step k of a pass trains network j on
+// the k-th window of its records (picked on the device); a network trains only while
+// *pass < its train passes (pass null: always). Every launch size is fixed on the host, so
+// the steps can be captured in a CUDA graph.
+// batch_max: the largest `len` of the segments (sizes the launch).
+cudaError_t guide_train_nets(const guide::NetDev* nets, const guide::RecSeg* segs, int nnet, int steps,
+                             uint32_t batch_max, const uint32_t* pass, int sms, cudaStream_t s);
 
 }  // namespace rx

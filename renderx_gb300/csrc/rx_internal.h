@@ -230,7 +230,6 @@ struct PtJob {
 };
 struct PtRun {
   uint32_t paths_per_pass = 0;  // 0 = 2^22
-  bool guided = false;          // one scene only
   bool use_graph = true;        // replay a captured pass
   bool autotune = false;        // time launch shapes on the first passes
   bool bin = false;             // bin bounce rays by origin cell and direction before each extend

@@ -37,15 +37,30 @@ struct PtParams {
 struct SceneRec {
   DevScene S;
   PtParams P;
-  uint64_t path_begin;  // first global path index of the scene
+  uint64_t path_begin;  // concatenated passes: first global path index of the scene
   uint64_t film_base;   // first pixel of the scene in the shared film
+  uint64_t paths;       // pixels x spp
+  uint32_t per_pass;    // interleaved passes: paths of this scene in each pass
+  int32_t net;          // guiding network of the scene (index into the render's networks), -1: none
 };
 
-// Pass cursor in device memory, so that one captured pass replays unchanged.
+// Pass cursor in device memory, so that one captured pass replays unchanged. Two
+// layouts of the paths over passes: concatenated (pass p takes global paths
+// [p per_pass, (p + 1) per_pass) of the scenes' paths laid end to end) and interleaved
+// (pass p takes paths [p q_k, (p + 1) q_k) of every scene k, q_k = SceneRec::per_pass,
+// so every scene advances through its samples at the same pace: guided renders, whose
+// networks warm up, train and guide on a schedule of passes).
 struct PassState {
-  uint64_t base, total;
+  uint64_t base, total;  // concatenated: first global path of the pass, all paths
   uint32_t per_pass, npaths;
+  uint32_t pass;         // passes done (the guiding schedule reads it)
+  uint32_t interleaved;
 };
+
+// A path's id: its index within its scene (the random-number key) and, in the top 24
+// bits, its slot in the pass's generation order (training records refer to it).
+constexpr int kLocalShift = 40;
+constexpr uint64_t kPidMask = (1ull << kLocalShift) - 1;
 
 __device__ __forceinline__ int scene_of(const SceneRec* R, int nr, uint64_t g) {
   int lo = 0, hi = nr - 1;
@@ -65,16 +80,76 @@ __device__ __forceinline__ F3 camera_dir(const CamDev& c, float xp, float yp) {
   return normalize(c.front * c.sight + c.right * x + c.up * y);
 }
 
-__global__ void k_generate(const SceneRec* R, int nr, PassState* ps, PathSoA S, unsigned* count) {
+// Interleaved passes: paths of scene r in pass p.
+__host__ __device__ __forceinline__ uint32_t pass_share(const SceneRec& r, uint32_t p) {
+  const uint64_t start = (uint64_t)p * r.per_pass;
+  if (start >= r.paths) return 0u;
+  const uint64_t left = r.paths - start;
+  return left < r.per_pass ? (uint32_t)left : r.per_pass;
+}
+
+// Interleaved passes: offsets off[0..nr] of each scene's paths in the generation order
+// of the current pass (one block).
+__global__ void __launch_bounds__(256) k_layout(const SceneRec* R, int nr, const PassState* ps, uint32_t* off) {
+  __shared__ uint32_t part[256];
+  const uint32_t p = ps->pass;
+  const int per = (nr + 255) / 256, k0 = threadIdx.x * per, k1 = min(nr, k0 + per);
+  uint32_t sum = 0;
+  for (int k = k0; k < k1; k++) {
+    sum += pass_share(R[k], p);
+  }
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {  // inclusive scan of the per-thread sums
+    uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t acc = part[threadIdx.x] - sum;
+  for (int k = k0; k < k1; k++) {
+    off[k] = acc;
+    acc += pass_share(R[k], p);
+  }
+  if (threadIdx.x == 255) off[nr] = part[255];
+}
+
+// Scene k with off[k] <= i < off[k + 1].
+__device__ __forceinline__ int scene_at(const uint32_t* off, int nr, uint32_t i) {
+  int lo = 0, hi = nr - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_generate(const SceneRec* R, int nr, PassState* ps, const uint32_t* off, PathSoA S,
+                           unsigned* count) {
+  uint32_t np;
+  const bool inter = ps->interleaved != 0;
+  if (inter) {
+    np = off[nr];
+  } else {
+    const uint64_t left = ps->base < ps->total ? ps->total - ps->base : 0;
+    np = (uint32_t)(left < ps->per_pass ? left : ps->per_pass);
+  }
   const uint64_t base = ps->base;
-  const uint64_t left = base < ps->total ? ps->total - base : 0;
-  const uint32_t np = (uint32_t)(left < ps->per_pass ? left : ps->per_pass);
+  const uint32_t pass = ps->pass;
   uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
-    uint64_t g = base + i;
-    int sc = scene_of(R, nr, g);
+    int sc;
+    uint64_t pid;  // path index within its scene (random-number key)
+    if (inter) {
+      sc = scene_at(off, nr, i);
+      pid = (uint64_t)pass * R[sc].per_pass + (i - off[sc]);
+    } else {
+      uint64_t g = base + i;
+      sc = scene_of(R, nr, g);
+      pid = g - R[sc].path_begin;
+    }
     const PtParams& P = R[sc].P;
-    uint64_t pid = g - R[sc].path_begin;  // path index within its scene (random-number key)
     uint32_t pixel = (uint32_t)(pid % P.pixels);
     int x = pixel % P.cam.width, y = pixel / P.cam.width;
     Rng rng(P.seed, pid, 0);
@@ -93,7 +168,7 @@ __global__ void k_generate(const SceneRec* R, int nr, PassState* ps, PathSoA S, 
     S.T[i] = make_float4(w, w, w, 0.0f);
     S.L[i] = make_float4(0, 0, 0, 0);
     S.info[i] = make_int4((int)pixel, kCameraObj, inside, (sc << 16) | (1 << 8));
-    S.id[i] = g;
+    S.id[i] = pid | ((uint64_t)i << kLocalShift);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *count = np;
@@ -186,10 +261,12 @@ __device__ F3 connect_light(const DevScene& SC, const CamDev& cam, const PV& in,
   return f3v(SC.objects[lg.obj].color) * f * (cos_l * cos_s / (pdfa * dist * dist) * mis);
 }
 
-// Guided sampling state of a wavefront (all null / zero when guiding is off).
+// Guided sampling state of a wavefront (all null / zero when guiding is off). A scene's
+// network (SceneRec::net) guides from pass nets[net].warmup on and takes training
+// records while the pass is below nets[net].train.
 struct GuideIO {
+  const guide::NetDev* nets;
   float* lobes;        // per live path: guide::kLobeStride floats, lobes[0] < 0 = not guided
-  float frac;          // one-sample MIS: probability of sampling the BSDF
   float* recs;         // training records (guide::kRec floats) or null
   unsigned* rec_count;
   uint32_t rec_cap;
@@ -288,10 +365,12 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
     int depth = 0;
     bool rec = false;  // a guided vertex whose path continues: a training record
     uint32_t sc = 0;
+    uint32_t local = 0;  // the path's slot in the pass's generation order
     if (i < n) {
       float4 o4 = S.o[i], d4 = S.d[i], T4 = S.T[i], L4 = S.L[i];
       inf = S.info[i];
       pid = S.id[i];
+      local = (uint32_t)(pid >> kLocalShift);
       depth = inf.w & 255;
       bool last_spec = (inf.w >> 8) & 1;
       sc = (uint32_t)inf.w >> 16;
@@ -306,14 +385,18 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
       cur.pixel = inf.x;
       cur.flags = (depth == 0 || !last_spec) ? kDirRandom : 0u;  // the camera ray is RANDOM
       int2 h = hit[i];
-      Rng rng(P.seed, pid - R[sc].path_begin, 16u + 32u * (uint32_t)depth);
+      Rng rng(P.seed, pid & kPidMask, 16u + 32u * (uint32_t)depth);
+      const int net = G.nets ? R[sc].net : -1;
+      const bool training = net >= 0 && G.recs && ps->pass < G.nets[net].train;
       bool done = true;
       if (h.x >= 0) {  // a ray that hits nothing ends the path (samplePathIter's termRay)
         Hit3 hh{(int)__ldg(&SC.tri_obj[h.x]), h.x, __int_as_float(h.y)};
         bool russian = P.rr_mode == 0 || depth >= 3;
-        bool guided = G.lobes && !P.nee && __ldg(&G.lobes[(size_t)i * guide::kLobeStride]) >= 0.0f;
+        bool guided = net >= 0 && G.lobes && !P.nee && ps->pass >= G.nets[net].warmup &&
+                      __ldg(&G.lobes[(size_t)i * guide::kLobeStride]) >= 0.0f;
         if (guided) {
-          nx = scatter_guided(SC, cur, hh, russian, rng, G.lobes + (size_t)i * guide::kLobeStride, G.frac);
+          nx = scatter_guided(SC, cur, hh, russian, rng, G.lobes + (size_t)i * guide::kLobeStride,
+                              G.nets[net].frac);
           leak_kill(SC, P.cam, cur, nx);
         } else {
           nx = scatter_step(SC, P.cam, cur, hh, false, russian, rng);
@@ -334,7 +417,7 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
             // a training sample: a sampled direction at a diffuse / glossy / Phong
             // surface seen from outside any object
             uint32_t m = SC.objects[hh.obj].material;
-            rec = G.recs && cur.inside == kNone && (nx.flags & kDirRandom) && nx.contact == hh.obj &&
+            rec = training && cur.inside == kNone && (nx.flags & kDirRandom) && nx.contact == hh.obj &&
                   (m == kDiffuse || m == kGlossy || m == kPhong);
           }
         } else if (is_emissive(SC, nx.contact)) {
@@ -358,7 +441,7 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
       if (done) {
         if (L.x != 0.0f || L.y != 0.0f || L.z != 0.0f)
           film_add(film_sum, film_sq, (int)(R[sc].film_base + (uint32_t)inf.x), L);
-        if (G.lpath) G.lpath[pid - ps->base] = make_float4(L.x, L.y, L.z, 0.0f);
+        if (training && G.lpath) G.lpath[local] = make_float4(L.x, L.y, L.z, 0.0f);
       } else {
         cont = true;
       }
@@ -379,7 +462,7 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
         r[0] = make_float4(nx.o.x, nx.o.y, nx.o.z, ns.x);
         r[1] = make_float4(ns.y, ns.z, -d4.x, -d4.y);
         r[2] = make_float4(-d4.z, nx.d.x, nx.d.y, nx.d.z);
-        r[3] = make_float4(Tb.x, Tb.y, Tb.z, __uint_as_float((uint32_t)(pid - ps->base)));
+        r[3] = make_float4(Tb.x, Tb.y, Tb.z, __uint_as_float(local));
       }
     }
     // compaction: warp ballot, one atomic per warp
@@ -406,14 +489,40 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
 }
 
 __global__ void k_zero(unsigned* p) { *p = 0; }
-__global__ void k_advance(PassState* ps) { ps->base += ps->per_pass; }
+__global__ void k_advance(PassState* ps) {
+  ps->base += ps->per_pass;
+  ps->pass += 1;
+}
+
+// Whether any network takes training records in this pass.
+__device__ __forceinline__ bool any_training(const guide::NetDev* nets, int nnet, uint32_t pass) {
+  for (int j = 0; j < nnet; j++)
+    if (pass < nets[j].train) return true;
+  return false;
+}
+
+// Start of a pass: clears the raw record count and every network's record count.
+__global__ void k_records_begin(const guide::NetDev* nets, int nnet, const PassState* ps, unsigned* raw_count,
+                                unsigned* net_count) {
+  const uint32_t pass = ps->pass;
+  for (int j = threadIdx.x; j < nnet; j += blockDim.x)
+    if (pass < nets[j].train) net_count[j] = 0;
+  if (threadIdx.x == 0) *raw_count = 0;
+}
 
 // Training samples of a finished pass: each record's weight is the luminance of its
 // path's final radiance over the throughput before the vertex, i.e. (BSDF x cosine x
 // incident radiance) / (sampling density) at the vertex. Records with a positive weight
-// are compacted into `out` (x, n, wo, wi, weight, 0, 0, 0).
-__global__ void k_record_weights(const float* recs, const unsigned* count, uint32_t cap, const float4* lpath,
-                                 float* out, unsigned* out_count) {
+// go to their network's region of `out` (x, n, wo, wi, weight, 0, 0, 0): network j's
+// records at [rbase[j], rbase[j] + rcap[j]), counted in net_count[j] (which may pass
+// rcap[j]: the surplus is dropped). A record's scene is the scene of its path's slot in
+// the pass (off: the interleaved layout's offsets).
+__global__ void k_record_weights(const SceneRec* R, int nr, const uint32_t* off, const PassState* ps,
+                                 const guide::NetDev* nets, int nnet, const float* recs, const unsigned* count,
+                                 uint32_t cap, const float4* lpath, float* out, unsigned* net_count,
+                                 const uint32_t* rbase, const uint32_t* rcap) {
+  const uint32_t pass = ps->pass;
+  if (!any_training(nets, nnet, pass)) return;
   uint32_t n = min(*count, cap);
   const int lane = threadIdx.x & 31;
   uint32_t stride = gridDim.x * blockDim.x;
@@ -422,32 +531,114 @@ __global__ void k_record_weights(const float* recs, const unsigned* count, uint3
     uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
     float4 a{}, b{}, c{}, d{};
     float w = 0.0f;
+    int net = -1;
     if (i < n) {
       const float4* r = reinterpret_cast<const float4*>(recs + (size_t)i * guide::kRec);
       a = r[0];
       b = r[1];
       c = r[2];
       d = r[3];
-      float4 L = lpath[__float_as_uint(d.w)];
+      const uint32_t local = __float_as_uint(d.w);
+      net = R[scene_at(off, nr, local)].net;
+      float4 L = lpath[local];
       F3 q{d.x > 0.0f ? L.x / d.x : 0.0f, d.y > 0.0f ? L.y / d.y : 0.0f, d.z > 0.0f ? L.z / d.z : 0.0f};
       w = lum(q);
       if (!(w < 1e30f)) w = 0.0f;
+      if (net < 0 || pass >= nets[net].train) w = 0.0f;
     }
-    bool keep = w > 0.0f;
-    unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (!m) continue;
-    unsigned base = 0;
-    int leader = __ffs(m) - 1;
-    if (lane == leader) base = atomicAdd(out_count, (unsigned)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
+    const bool keep = w > 0.0f;
+    // lanes that keep a record of the same network share one atomic
+    const unsigned peers = __match_any_sync(0xffffffffu, keep ? net : -1);
     if (keep) {
-      float4* o = reinterpret_cast<float4*>(out + (size_t)(base + __popc(m & ((1u << lane) - 1))) * guide::kRec);
-      o[0] = a;
-      o[1] = b;
-      o[2] = c;
-      o[3] = make_float4(w, 0.0f, 0.0f, 0.0f);
+      const int leader = __ffs(peers) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&net_count[net], (unsigned)__popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      const uint32_t j = base + __popc(peers & ((1u << lane) - 1));
+      if (j < rcap[net]) {
+        float4* o = reinterpret_cast<float4*>(out + (size_t)(rbase[net] + j) * guide::kRec);
+        o[0] = a;
+        o[1] = b;
+        o[2] = c;
+        o[3] = make_float4(w, 0.0f, 0.0f, 0.0f);
+      }
     }
   }
+}
+
+// Grouped inference input: the live paths of scenes whose network guides in this pass,
+// sorted by network into segments padded to guide::kGroupRows rows (a counting sort:
+// count, scan, scatter, pad). ncount / cursor: one counter per network.
+__device__ __forceinline__ int active_net(const SceneRec* R, const guide::NetDev* nets, const int4& inf,
+                                          uint32_t pass) {
+  const int net = R[(uint32_t)inf.w >> 16].net;
+  return net >= 0 && pass >= nets[net].warmup ? net : -1;
+}
+__global__ void k_net_count(const SceneRec* R, const guide::NetDev* nets, const PassState* ps, PathSoA S,
+                            const unsigned* count, unsigned* ncount) {
+  const uint32_t n = *count, pass = ps->pass;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t it = 0; it < iters; it++) {
+    const uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    const int net = i < n ? active_net(R, nets, S.info[i], pass) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, net);
+    if (net >= 0 && lane == __ffs(peers) - 1) atomicAdd(&ncount[net], (unsigned)__popc(peers));
+  }
+}
+// One block: seg[j] = padded offsets of the networks' segments; clears the counters
+// the scatter uses.
+__global__ void __launch_bounds__(256) k_net_scan(int nnet, const unsigned* ncount, uint32_t* seg,
+                                                  unsigned* cursor) {
+  __shared__ uint32_t part[256];
+  const int per = (nnet + 255) / 256, k0 = threadIdx.x * per, k1 = min(nnet, k0 + per);
+  auto padded = [](unsigned c) { return (c + guide::kGroupRows - 1) / guide::kGroupRows * guide::kGroupRows; };
+  uint32_t sum = 0;
+  for (int k = k0; k < k1; k++) sum += padded(ncount[k]);
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t acc = part[threadIdx.x] - sum;
+  for (int k = k0; k < k1; k++) {
+    seg[k] = acc;
+    cursor[k] = 0;
+    acc += padded(ncount[k]);
+  }
+  if (threadIdx.x == 255) seg[nnet] = part[255];
+}
+__global__ void k_net_scatter(const SceneRec* R, const guide::NetDev* nets, const PassState* ps, PathSoA S,
+                              const unsigned* count, const uint32_t* seg, unsigned* cursor, int* rows) {
+  const uint32_t n = *count, pass = ps->pass;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t it = 0; it < iters; it++) {
+    const uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    const int net = i < n ? active_net(R, nets, S.info[i], pass) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, net);
+    if (net >= 0) {
+      const int leader = __ffs(peers) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&cursor[net], (unsigned)__popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      rows[seg[net] + base + __popc(peers & ((1u << lane) - 1))] = (int)i;
+    }
+  }
+}
+// Padding rows of each segment (after its ncount[j] live rows) are -1; then the count is
+// cleared for the next sort (block j owns network j).
+__global__ void k_net_pad(int nnet, unsigned* ncount, const uint32_t* seg, int* rows) {
+  const int j = blockIdx.x;
+  if (j >= nnet) return;
+  for (uint32_t r = seg[j] + ncount[j] + threadIdx.x; r < seg[j + 1]; r += blockDim.x) rows[r] = -1;
+  __syncthreads();
+  if (threadIdx.x == 0) ncount[j] = 0;
 }
 
 // -------------------------------------------------------------------------------------
@@ -500,10 +691,29 @@ struct Wave {
   PathSoA A, B;
   int2* hit;
   unsigned long long* ctr;  // [0] extension rays, [1] shadow rays
-  unsigned* cnt;            // [0], [1] queue lengths, [2] records, [3] weighted records
+  unsigned* cnt;            // [0], [1] queue lengths, [2] raw training records
   double *film, *sq;
   uint32_t loops;           // bounce stages per pass (max depth cap + 1)
   uint32_t *keys, *order, *hist;  // ray binning of bounce rays (null: off)
+  uint32_t* off;            // interleaved passes: each scene's offset in the pass (null: concatenated)
+  int sms;
+  // guiding (nets null: off)
+  const guide::NetDev* nets;
+  int nnet;
+  const DevScene* scenes;   // the scenes' geometry, for the inference kernel
+  float* lobes;             // mixture per live path
+  float* recs;              // raw training records (null: no network trains)
+  uint32_t rec_cap;
+  float4* lpath;            // each pass slot's final radiance
+  float* train;             // records by network (weights computed)
+  unsigned* net_count;      // per network: records in its region
+  const uint32_t *rbase, *rcap;
+  const guide::RecSeg* segs;
+  int steps;                // Adam steps per training pass (the most any network takes)
+  uint32_t batch_max;
+  unsigned *ncount, *cursor;  // grouped inference sort (nnet > 1)
+  uint32_t* seg;
+  int* rows;
 };
 
 // Bins the queue's rays (bounces after the camera rays) and returns the visiting order.
@@ -516,31 +726,56 @@ const uint32_t* enqueue_binning(const Wave& W, PathSoA cur, const unsigned* cc, 
   return W.order;
 }
 
-// One pass: generate, `loops` x (extend, clear the next queue, shade), advance the cursor.
-// Everything is a kernel on `s` with device-resident counts, so the pass can be captured
-// into a CUDA graph once and replayed.
+// The guiding mixtures of the live paths whose scene's network guides in this pass: one
+// network over the queue, or several over the queue sorted by network.
+cudaError_t enqueue_infer(const Wave& W, const PathSoA& cur, const unsigned* cc, int grid, cudaStream_t s) {
+  const uint32_t* pass = &W.ps->pass;
+  if (W.nr == 1)  // one scene, one network: the queue as it is
+    return guide_infer_wave(W.nets, 1, W.scenes, cur, cc, W.hit, W.lobes, nullptr, nullptr, pass, W.sms, s);
+  k_net_count<<<grid, 256, 0, s>>>(W.R, W.nets, W.ps, cur, cc, W.ncount);
+  k_net_scan<<<1, 256, 0, s>>>(W.nnet, W.ncount, W.seg, W.cursor);
+  k_net_scatter<<<grid, 256, 0, s>>>(W.R, W.nets, W.ps, cur, cc, W.seg, W.cursor, W.rows);
+  k_net_pad<<<W.nnet, 128, 0, s>>>(W.nnet, W.ncount, W.seg, W.rows);
+  return guide_infer_wave(W.nets, W.nnet, W.scenes, cur, cc, W.hit, W.lobes, W.rows, W.seg, pass, W.sms, s);
+}
+
+// One pass: (layout), generate, `loops` x (extend, guiding inference, clear the next
+// queue, shade), (training), advance the cursor. Everything is a kernel on `s` with
+// device-resident counts and schedule, so the pass can be captured into a CUDA graph
+// once and replayed.
 template <int STACK>
-void enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
-  k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.A, W.cnt);
+cudaError_t enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (W.off) k_layout<<<1, 256, 0, s>>>(W.R, W.nr, W.ps, W.off);
+  if (W.recs) k_records_begin<<<1, 256, 0, s>>>(W.nets, W.nnet, W.ps, W.cnt + 2, W.net_count);
+  k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.off, W.A, W.cnt);
+  const GuideIO G{W.nets, W.lobes, W.recs, W.cnt + 2, W.rec_cap, W.lpath};
   PathSoA cur = W.A, nxt = W.B;
   unsigned *cc = W.cnt, *cn = W.cnt + 1;
   for (uint32_t d = 0; d < W.loops; d++) {
     const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
     k_extend<STACK><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
+    if (W.nets && e == cudaSuccess) e = enqueue_infer(W, cur, cc, grid, s);
     k_zero<<<1, 1, 0, s>>>(cn);
-    k_shade<STACK><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, GuideIO{});
+    k_shade<STACK><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, G);
     std::swap(cur, nxt);
     std::swap(cc, cn);
   }
+  if (W.recs) {
+    k_record_weights<<<grid, 128, 0, s>>>(W.R, W.nr, W.off, W.ps, W.nets, W.nnet, W.recs, W.cnt + 2, W.rec_cap,
+                                          W.lpath, W.train, W.net_count, W.rbase, W.rcap);
+    if (e == cudaSuccess) e = guide_train_nets(W.nets, W.segs, W.nnet, W.steps, W.batch_max, &W.ps->pass, W.sms, s);
+  }
   k_advance<<<1, 1, 0, s>>>(W.ps);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
-void enqueue_pass_shape(const Wave& W, const PtShape& sh, int sms, cudaStream_t s) {
+cudaError_t enqueue_pass_shape(const Wave& W, const PtShape& sh, int sms, cudaStream_t s) {
   int grid = sms * sh.blocks_per_sm;
-  if (sh.stack == kWalk4S) enqueue_pass<kWalk4S>(W, grid, s);
-  else if (sh.stack == kWalk4) enqueue_pass<kWalk4>(W, grid, s);
-  else if (sh.stack == 32) enqueue_pass<32>(W, grid, s);
-  else enqueue_pass<kStackDepth>(W, grid, s);
+  if (sh.stack == kWalk4S) return enqueue_pass<kWalk4S>(W, grid, s);
+  if (sh.stack == kWalk4) return enqueue_pass<kWalk4>(W, grid, s);
+  if (sh.stack == 32) return enqueue_pass<32>(W, grid, s);
+  return enqueue_pass<kStackDepth>(W, grid, s);
 }
 
 }  // namespace
@@ -551,21 +786,47 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   uint64_t total = 0;
   uint32_t max_depth = 0, max_bvh_depth = 0;
   bool wide_ok = true;  // every scene's 4-wide BVH fits the 4-wide walk's stack
+  // guiding: one network per distinct guiding state among the guided jobs
+  std::vector<const GuideState*> net_state;
   for (int k = 0; k < nj; k++) {
     recs[k].S = jobs[k].ctx->scene;
     recs[k].P = make_pt_params(jobs[k].ctx, jobs[k].cam, jobs[k].opt);
     recs[k].path_begin = total;
     recs[k].film_base = jobs[k].film_base;
-    total += (uint64_t)recs[k].P.pixels * jobs[k].opt.spp;
+    recs[k].paths = (uint64_t)recs[k].P.pixels * jobs[k].opt.spp;
+    recs[k].net = -1;
+    if (recs[k].paths >= (1ull << kLocalShift)) return cudaErrorInvalidValue;  // path ids keep 40 bits
+    total += recs[k].paths;
     max_depth = std::max(max_depth, jobs[k].opt.max_depth);
     max_bvh_depth = std::max<uint32_t>(max_bvh_depth, (uint32_t)jobs[k].ctx->bvh.max_depth);
     const DevAccel& A = jobs[k].ctx->scene.accel;
     wide_ok = wide_ok && A.bvh4 && 3 * A.bvh4_depth + 1 <= 64;
+    if ((jobs[k].opt.flags & RX_PT_GUIDED) && !jobs[k].opt.nee && guide_ready(jobs[k].ctx->guide)) {
+      const GuideState* g = jobs[k].ctx->guide;
+      auto it = std::find(net_state.begin(), net_state.end(), g);
+      recs[k].net = (int)(it - net_state.begin());
+      if (it == net_state.end()) net_state.push_back(g);
+    }
   }
+  const int nnet = (int)net_state.size();
+  const bool guided = nnet > 0;
+  // a pass slot index keeps 24 bits of the path id; interleaved passes add up to one slot
+  // per scene to the pass size
+  const uint32_t max_slots = (1u << 24) - (uint32_t)nj;
   uint32_t per_pass = run.paths_per_pass ? run.paths_per_pass : (1u << 22);
-  per_pass = (uint32_t)std::min<uint64_t>(per_pass, total);
+  per_pass = (uint32_t)std::min<uint64_t>(std::min<uint32_t>(per_pass, max_slots - (uint32_t)nj), total);
   if (per_pass == 0) return cudaSuccess;
   const uint64_t npasses = (total + per_pass - 1) / per_pass;
+  // guided renders interleave the scenes: every pass takes its share of each scene
+  uint32_t slots = per_pass;
+  if (guided) {
+    uint64_t sum = 0;
+    for (auto& r : recs) {
+      r.per_pass = (uint32_t)((r.paths + npasses - 1) / npasses);
+      sum += r.per_pass;
+    }
+    slots = (uint32_t)sum;
+  }
   const int sms = c->trace_cfg.sms;
 
   std::vector<DevBuf> bufs;
@@ -575,53 +836,94 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     if ((e = bufs.back().alloc(bytes)) != cudaSuccess) return nullptr;
     return bufs.back().p;
   };
+  auto upload = [&](const void* src, size_t bytes) -> void* {
+    void* p = alloc(bytes);
+    if (p && (e = cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) return nullptr;
+    return p;
+  };
   Wave W{};
   W.nr = nj;
   W.loops = max_depth + 1;
   W.film = film_sum;
   W.sq = film_sq;
-  void* pR = alloc(sizeof(SceneRec) * nj);
-  if (!pR) return e;
-  W.R = static_cast<const SceneRec*>(pR);
-  cudaMemcpyAsync(pR, recs.data(), sizeof(SceneRec) * nj, cudaMemcpyHostToDevice, s);
-  if (!(W.ps = static_cast<PassState*>(alloc(sizeof(PassState))))) return e;
-  PassState ps0{0, total, per_pass, 0};
-  cudaMemcpyAsync(W.ps, &ps0, sizeof ps0, cudaMemcpyHostToDevice, s);
-  if ((e = alloc_soa(W.A, bufs, per_pass)) != cudaSuccess) return e;
-  if ((e = alloc_soa(W.B, bufs, per_pass)) != cudaSuccess) return e;
-  if (!(W.hit = static_cast<int2*>(alloc(per_pass * sizeof(int2))))) return e;
+  W.sms = sms;
+  if (!(W.R = static_cast<const SceneRec*>(upload(recs.data(), sizeof(SceneRec) * nj)))) return e;
+  PassState ps0{0, total, per_pass, 0, 0, guided ? 1u : 0u};
+  if (!(W.ps = static_cast<PassState*>(upload(&ps0, sizeof ps0)))) return e;
+  if ((e = alloc_soa(W.A, bufs, slots)) != cudaSuccess) return e;
+  if ((e = alloc_soa(W.B, bufs, slots)) != cudaSuccess) return e;
+  if (!(W.hit = static_cast<int2*>(alloc(slots * sizeof(int2))))) return e;
   if (!(W.ctr = static_cast<unsigned long long*>(alloc(64 * sizeof(unsigned long long))))) return e;
   W.cnt = reinterpret_cast<unsigned*>(W.ctr + 8);
   cudaMemsetAsync(W.ctr, 0, 64 * sizeof(unsigned long long), s);
-  if (run.bin && per_pass >= c->trace_cfg.bin_min && c->trace_cfg.bin_min) {
-    if (!(W.keys = static_cast<uint32_t*>(alloc((size_t)per_pass * 4)))) return e;
-    if (!(W.order = static_cast<uint32_t*>(alloc((size_t)per_pass * 4)))) return e;
+  if (run.bin && slots >= c->trace_cfg.bin_min && c->trace_cfg.bin_min) {
+    if (!(W.keys = static_cast<uint32_t*>(alloc((size_t)slots * 4)))) return e;
+    if (!(W.order = static_cast<uint32_t*>(alloc((size_t)slots * 4)))) return e;
     if (!(W.hist = static_cast<uint32_t*>(alloc((size_t)kRayBins * 4 + 4096)))) return e;
   }
 
-  // guiding (one scene): mixture per live path, training records, per-path radiance
-  const bool guided = run.guided && nj == 1 && guide_ready(c->guide) && !jobs[0].opt.nee;
-  GuideIO G{};
-  float* train = nullptr;
-  unsigned* rcnt = W.cnt + 2;
-  uint32_t cap = 0;
   if (guided) {
-    cap = (uint32_t)std::min<uint64_t>((uint64_t)per_pass * 4, 1u << 22);
-    if (!(G.lobes = static_cast<float*>(alloc((size_t)per_pass * guide::kLobeStride * sizeof(float))))) return e;
-    G.frac = guide_bsdf_fraction(c->guide);
-    if (guide_train_passes(c->guide) > 0) {
-      if (!(G.recs = static_cast<float*>(alloc((size_t)cap * guide::kRec * sizeof(float))))) return e;
-      if (!(train = static_cast<float*>(alloc((size_t)cap * guide::kRec * sizeof(float))))) return e;
-      if (!(G.lpath = static_cast<float4*>(alloc((size_t)per_pass * sizeof(float4))))) return e;
-      G.rec_count = rcnt;
-      G.rec_cap = cap;
+    if (!(W.off = static_cast<uint32_t*>(alloc((size_t)(nj + 1) * 4)))) return e;
+    std::vector<guide::NetDev> nets(nnet);
+    int steps = 0;
+    uint32_t batch_max = 0;
+    bool any_train = false;
+    for (int j = 0; j < nnet; j++) {
+      nets[j] = guide_net(net_state[j]);
+      steps = std::max<int>(steps, (int)nets[j].steps_per_pass);
+      batch_max = std::max(batch_max, nets[j].batch);
+      any_train = any_train || (nets[j].train > 0 && nets[j].steps_per_pass > 0);
     }
+    W.nnet = nnet;
+    if (!(W.nets = static_cast<const guide::NetDev*>(upload(nets.data(), sizeof(guide::NetDev) * nnet)))) return e;
+    std::vector<DevScene> sc(nj);
+    for (int k = 0; k < nj; k++) sc[k] = recs[k].S;
+    if (!(W.scenes = static_cast<const DevScene*>(upload(sc.data(), sizeof(DevScene) * nj)))) return e;
+    if (!(W.lobes = static_cast<float*>(alloc((size_t)slots * guide::kLobeStride * sizeof(float))))) return e;
+    if (nnet > 1) {
+      if (!(W.ncount = static_cast<unsigned*>(alloc((size_t)nnet * 4)))) return e;
+      if (!(W.cursor = static_cast<unsigned*>(alloc((size_t)nnet * 4)))) return e;
+      if (!(W.seg = static_cast<uint32_t*>(alloc((size_t)(nnet + 1) * 4)))) return e;
+      if (!(W.rows = static_cast<int*>(alloc(((size_t)slots + (size_t)nnet * guide::kGroupRows) * 4)))) return e;
+      cudaMemsetAsync(W.ncount, 0, (size_t)nnet * 4, s);
+    }
+    if (any_train) {
+      // raw records, then each network's region of the weighted records, sized by its
+      // share of the pass's paths
+      const uint32_t cap = (uint32_t)std::min<uint64_t>((uint64_t)slots * 4, 1u << 22);
+      W.rec_cap = cap;
+      if (!(W.recs = static_cast<float*>(alloc((size_t)cap * guide::kRec * sizeof(float))))) return e;
+      if (!(W.train = static_cast<float*>(alloc((size_t)cap * guide::kRec * sizeof(float))))) return e;
+      if (!(W.lpath = static_cast<float4*>(alloc((size_t)slots * sizeof(float4))))) return e;
+      if (!(W.net_count = static_cast<unsigned*>(alloc((size_t)nnet * 4)))) return e;
+      std::vector<uint64_t> share(nnet, 0);
+      for (auto& r : recs)
+        if (r.net >= 0) share[r.net] += r.per_pass;
+      uint64_t all = 0;
+      for (uint64_t v : share) all += v;
+      std::vector<uint32_t> rbase(nnet), rcap(nnet);
+      std::vector<guide::RecSeg> segs(nnet);
+      uint32_t acc = 0;
+      for (int j = 0; j < nnet; j++) {
+        rbase[j] = acc;
+        rcap[j] = (uint32_t)((uint64_t)cap * share[j] / std::max<uint64_t>(all, 1));
+        acc += rcap[j];
+        segs[j] = guide::RecSeg{W.train + (size_t)rbase[j] * guide::kRec, W.net_count + j, rcap[j], nets[j].batch};
+      }
+      if (!(W.rbase = static_cast<const uint32_t*>(upload(rbase.data(), (size_t)nnet * 4)))) return e;
+      if (!(W.rcap = static_cast<const uint32_t*>(upload(rcap.data(), (size_t)nnet * 4)))) return e;
+      if (!(W.segs = static_cast<const guide::RecSeg*>(upload(segs.data(), sizeof(guide::RecSeg) * nnet)))) return e;
+      W.steps = steps;
+      W.batch_max = batch_max;
+      cudaMemsetAsync(W.net_count, 0, (size_t)nnet * 4, s);
+    }
+    guide_prepare();  // kernel attributes set before any capture
   }
 
   // launch shapes: the context's default, or candidates timed on the first passes
   PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4S : (max_bvh_depth < 32 ? 32 : kStackDepth)};
   std::vector<PtShape> cands;
-  if (run.autotune && !guided) {
+  if (run.autotune) {
     for (int bps : {4, 8, 16})
       for (int st : {kWalk4S, kWalk4, 32, kStackDepth})
         if (st == kWalk4 || st == kWalk4S ? wide_ok : st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
@@ -632,6 +934,13 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   if ((e = e0.create()) != cudaSuccess || (e = e1.create()) != cudaSuccess) return e;
   cudaEventRecord(e0, s);
   uint64_t pass = 0;
+  // paths finished after `p` passes
+  auto paths_done = [&](uint64_t p) -> uint64_t {
+    if (!guided) return std::min<uint64_t>(total, p * (uint64_t)per_pass);
+    uint64_t d = 0;
+    for (auto& r : recs) d += std::min<uint64_t>(r.paths, p * (uint64_t)r.per_pass);
+    return d;
+  };
   // time budget: after queueing pass p, wait for pass p - 1 and stop if the wall time is
   // spent (pass p still completes)
   const auto t_start = std::chrono::steady_clock::now();
@@ -652,7 +961,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   const bool snap_on = nj == 1 && snaps.on();
   auto after_pass = [&](uint64_t p) -> bool {
     if (snap_on && snaps.due()) {
-      const uint64_t done = std::min<uint64_t>(total, (p + 1) * (uint64_t)per_pass);
+      const uint64_t done = paths_done(p + 1);
       const uint64_t npx = recs[0].P.pixels;
       e = snaps.take(film_sum, jobs[0].cam.width, jobs[0].cam.height, (double)done / (double)npx,
                      [&](size_t q) { return (double)(done / npx + (q < done % npx ? 1 : 0)); }, s);
@@ -666,7 +975,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     if ((e = t0.create()) != cudaSuccess || (e = t1.create()) != cudaSuccess) return e;
     for (const PtShape& sh : cands) {
       cudaEventRecord(t0, s);
-      enqueue_pass_shape(W, sh, sms, s);
+      if ((e = enqueue_pass_shape(W, sh, sms, s)) != cudaSuccess) return e;
       cudaEventRecord(t1, s);
       if ((e = cudaEventSynchronize(t1)) != cudaSuccess) return e;
       float ms = 0;
@@ -677,77 +986,23 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   }
   if (chosen) *chosen = best;
 
-  if (!guided) {
-    if (run.use_graph && npasses - pass >= 2) {
-      Graph graph;
-      if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-      enqueue_pass_shape(W, best, sms, s);
-      if ((e = cudaStreamEndCapture(s, &graph.g)) != cudaSuccess) return e;
-      if ((e = cudaGraphInstantiate(&graph.x, graph.g, 0)) != cudaSuccess) return e;
-      while (pass < npasses && e == cudaSuccess) {
-        e = cudaGraphLaunch(graph.x, s);
-        if (e == cudaSuccess && after_pass(pass++)) break;
-      }
-      if (e != cudaSuccess) return e;
-    } else {
-      while (pass < npasses) {
-        enqueue_pass_shape(W, best, sms, s);
-        if (after_pass(pass++)) break;
-      }
-      if (e != cudaSuccess) return e;
+  if (run.use_graph && npasses - pass >= 2) {
+    Graph graph;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+    cudaError_t eq = enqueue_pass_shape(W, best, sms, s);
+    e = cudaStreamEndCapture(s, &graph.g);
+    if (eq != cudaSuccess) return eq;
+    if (e != cudaSuccess) return e;
+    if ((e = cudaGraphInstantiate(&graph.x, graph.g, 0)) != cudaSuccess) return e;
+    while (pass < npasses && e == cudaSuccess) {
+      e = cudaGraphLaunch(graph.x, s);
+      if (e == cudaSuccess && after_pass(pass++)) break;
     }
+    if (e != cudaSuccess) return e;
   } else {
-    const int grid = sms * best.blocks_per_sm;
-    for (; pass < npasses; pass++) {
-      const bool training = G.recs && pass < guide_train_passes(c->guide);
-      const bool use_guide = pass >= guide_warmup_passes(c->guide);
-      GuideIO Gp = G;
-      if (!use_guide) Gp.lobes = nullptr;
-      if (!training) {
-        Gp.recs = nullptr;
-        Gp.lpath = nullptr;
-      } else {
-        cudaMemsetAsync(rcnt, 0, 2 * sizeof(unsigned), s);
-        cudaMemsetAsync(G.lpath, 0, (size_t)per_pass * sizeof(float4), s);
-      }
-      k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.A, W.cnt);
-      PathSoA cur = W.A, nxt = W.B;
-      unsigned *cc = W.cnt, *cn = W.cnt + 1;
-      for (uint32_t d = 0; d < W.loops; d++) {
-        const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
-        if (best.stack == kWalk4S)
-          k_extend<kWalk4S><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
-        else if (best.stack == kWalk4)
-          k_extend<kWalk4><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
-        else if (best.stack == 32)
-          k_extend<32><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
-        else
-          k_extend<kStackDepth><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
-        if (use_guide && (e = guide_infer_paths(c->guide, recs[0].S, cur, cc, W.hit, G.lobes, sms, s)) != cudaSuccess)
-          return e;
-        k_zero<<<1, 1, 0, s>>>(cn);
-        if (best.stack == kWalk4S)
-          k_shade<kWalk4S><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
-        else if (best.stack == kWalk4)
-          k_shade<kWalk4><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
-        else if (best.stack == 32)
-          k_shade<32><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
-        else
-          k_shade<kStackDepth><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, Gp);
-        std::swap(cur, nxt);
-        std::swap(cc, cn);
-      }
-      if (training) {
-        k_record_weights<<<grid, 128, 0, s>>>(G.recs, rcnt, cap, G.lpath, train, rcnt + 1);
-        if ((e = guide_train_records(c->guide, train, rcnt + 1, cap, (int)guide_steps_per_pass(c->guide), s)) !=
-            cudaSuccess)
-          return e;
-      }
-      k_advance<<<1, 1, 0, s>>>(W.ps);
-      if (after_pass(pass)) {
-        pass++;
-        break;
-      }
+    while (pass < npasses) {
+      if ((e = enqueue_pass_shape(W, best, sms, s)) != cudaSuccess) return e;
+      if (after_pass(pass++)) break;
     }
     if (e != cudaSuccess) return e;
   }
@@ -762,7 +1017,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     cudaMemcpy(h, W.ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0];
     stats->shadow_rays = h[1];
-    stats->paths = std::min<uint64_t>(total, pass * (uint64_t)per_pass);
+    stats->paths = paths_done(pass);
     stats->ms = ms;
   }
   return cudaSuccess;
@@ -773,7 +1028,6 @@ cudaError_t render_pt(rx_context* c, const rx_camera& cam, const rx_pt_options& 
   PtJob job{c, cam, opt, 0};
   PtRun run{};
   run.paths_per_pass = opt.paths_per_pass;
-  run.guided = (opt.flags & RX_PT_GUIDED) != 0;
   run.use_graph = true;
   run.time_budget_s = opt.time_budget_s > 0 ? opt.time_budget_s : 0;
   return render_pt_jobs(c, &job, 1, run, film_sum, film_sq, stats, nullptr, s);

@@ -997,8 +997,10 @@ __device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, 
 // `cap` are counted, not written (the host then grows the list or splits the range).
 __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, const float4* ev, const int* elen,
                                                     Grid G, uint32_t p0, uint32_t p1, unsigned long long cap,
-                                                    uint32_t* pair_q, int* pair_ref, unsigned long long* npairs) {
+                                                    uint32_t* pair_q, int* pair_ref, unsigned long long* npairs,
+                                                    unsigned long long* nqueries) {
   const int lane = threadIdx.x & 31;
+  unsigned long long queries = 0;  // merge vertices this warp queried (counted by lane 0)
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   const float r = P.radius;
@@ -1011,6 +1013,7 @@ __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, con
       if (!(__float_as_uint(t4.w) & kDirRandom)) continue;
       const F3 x = f3(o4);
       const uint32_t q = p * P.maxv + (uint32_t)k;
+      queries++;
       // the cells the sphere touches (as merge_buckets), one per lane; equal buckets are
       // walked once, by the lowest lane that holds them
       const int x0 = (int)floorf((x.x - r) / G.cell), y0 = (int)floorf((x.y - r) / G.cell);
@@ -1065,6 +1068,7 @@ __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, con
       }
     }
   }
+  if (lane == 0 && queries) atomicAdd(nqueries, queries);
 }
 
 // One merge pair per lane, kRun consecutive pairs per thread (pairs of one query are
@@ -1473,6 +1477,12 @@ static VcmParams camera_params(const rx_camera& cam) {
   return P;
 }
 
+// Photons stored in this iteration's grid (the stored count, clipped to the capacity),
+// added to a running total.
+__global__ void k_count_photons(const unsigned* nph, unsigned cap, unsigned long long* total) {
+  *total += (unsigned long long)min(*nph, cap);
+}
+
 cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options& opt, double* film,
                        rx_render_stats* stats, cudaStream_t s) {
   const DevScene& S = c->scene;
@@ -1525,12 +1535,13 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
   cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
   int grid = c->trace_cfg.sms * 4;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  Event e0, e1, m0, m1;  // render; merge gather of an iteration (with stats)
+  if ((e = e0.create()) != cudaSuccess || (e = e1.create()) != cudaSuccess) return e;
+  if (stats && ((e = m0.create()) != cudaSuccess || (e = m1.create()) != cudaSuccess)) return e;
   cudaEventRecord(e0, s);
   float radius = opt.radius;
-  unsigned long long merges = 0;
+  unsigned long long merges = 0, queries = 0;
+  float merge_ms = 0;
   unsigned nscan = buckets + 1;
   unsigned nblk = (nscan + 1023) / 1024;
   const auto t_start = std::chrono::steady_clock::now();
@@ -1558,6 +1569,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
       k_grid_scatter<<<grid, 256, 0, s>>>(bufs[4].as<unsigned>(), bufs[2].as<float4>(), bufs[3].as<int>(), nph, cap,
                                           bufs[8].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(),
                                           bufs[0].as<float4>(), bufs[19].as<MisL>(), P.maxv, bufs[23].as<float4>());
+      k_count_photons<<<1, 1, 0, s>>>(nph, cap, ctr + 6);
     }
     cudaMemsetAsync(bufs[10].p, 0, bufs[10].bytes, s);
     unsigned long long* qc = bufs[14].as<unsigned long long>();
@@ -1614,15 +1626,17 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
                                                    bufs[10].as<float>());
       }
     } else {  // one walk appending pairs, then one pair per lane
+      if (m0) cudaEventRecord(m0, s);
       for (uint32_t p0 = 0; p0 < P.n_pixels;) {
         const uint32_t p1 = (uint32_t)std::min<uint64_t>(P.n_pixels, (uint64_t)p0 + pix_chunk);
-        unsigned long long* np_dev = ctr + 4;
-        cudaMemsetAsync(np_dev, 0, sizeof(unsigned long long), s);
+        unsigned long long* np_dev = ctr + 4;  // [4] pairs, [5] queries of this pixel range
+        cudaMemsetAsync(np_dev, 0, 2 * sizeof(unsigned long long), s);
         k_merge_walk<<<grid * 2, 256, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), G, p0, p1, pair_alloc,
-                                              bufs[17].as<uint32_t>(), bufs[18].as<int>(), np_dev);
-        unsigned long long np = 0;
-        cudaMemcpyAsync(&np, np_dev, sizeof np, cudaMemcpyDeviceToHost, s);
+                                              bufs[17].as<uint32_t>(), bufs[18].as<int>(), np_dev, np_dev + 1);
+        unsigned long long pq[2] = {0, 0};
+        cudaMemcpyAsync(pq, np_dev, sizeof pq, cudaMemcpyDeviceToHost, s);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        unsigned long long np = pq[0];
         if (np > pair_alloc) {  // grow the pair list, or split the pixel range once it is at its cap
           if (pair_alloc < kMergeCap) {
             pair_alloc = (uint32_t)std::min<unsigned long long>(kMergeCap, np + np / 4);
@@ -1637,11 +1651,19 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
           np = pair_alloc;  // one pixel beyond the cap: its first kMergeCap pairs
         }
         merges += np;
+        queries += pq[1];
         if (np)
           k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[20].as<MisE>(), bufs[23].as<float4>(),
                                                 bufs[17].as<uint32_t>(), bufs[18].as<int>(), (uint32_t)np,
                                                 bufs[10].as<float>());
         p0 = p1;
+      }
+      if (m1) {  // device time of this iteration's merge gather (walk + pair evaluation)
+        cudaEventRecord(m1, s);
+        if ((e = cudaEventSynchronize(m1)) != cudaSuccess) return e;
+        float mms = 0;
+        cudaEventElapsedTime(&mms, m0, m1);
+        merge_ms += mms;
       }
     }
     k_vcm_accumulate<<<grid, 256, 0, s>>>(P, bufs[10].as<float>(), film);
@@ -1661,16 +1683,17 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (stats) {
-    unsigned long long h[4];
+    unsigned long long h[8];
     cudaMemcpy(h, ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0] + h[1];
     stats->shadow_rays = h[2];
     stats->merges = merges;
     stats->paths = (uint64_t)P.n_pixels * done;
     stats->ms = ms;
+    stats->merge_ms = merge_ms;
+    stats->merge_queries = queries;
+    stats->photons = h[6];
   }
   return cudaSuccess;
 }
@@ -1712,9 +1735,8 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
   unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
   cudaMemsetAsync(ctr, 0, 16 * sizeof(unsigned long long), s);
   const int grid = c->trace_cfg.sms * 4;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  Event e0, e1;
+  if ((e = e0.create()) != cudaSuccess || (e = e1.create()) != cudaSuccess) return e;
   cudaEventRecord(e0, s);
   unsigned long long photons = 0;
   const auto t_start = std::chrono::steady_clock::now();
@@ -1760,14 +1782,13 @@ cudaError_t render_pm(rx_context* c, const rx_camera& cam, const rx_pm_options& 
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (stats) {
     unsigned long long h[2];
     cudaMemcpy(h, ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0] + h[1];
     stats->shadow_rays = 0;
     stats->merges = photons;
+    stats->photons = photons;
     stats->paths = (uint64_t)P.n_pixels * done;
     stats->ms = ms;
   }
