@@ -710,7 +710,9 @@ def emit(args, ws, n, ms_per_step, value, clocks, build_s, st, e2e, same, step_m
                            "parallelism": f"replicas x{ws}", "accel_build_s": round(build_s, 2)},
                 "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                                                  "d2h_bytes_per_step": n * 8, "matches_device_path": same},
-                "gpu_launches": 3 * args.steps,
+                # our kernels per call: binning (keys, three scan kernels, scatter) when the
+                # batch is at least the binning threshold, then walk, visibility check, re-walk
+                "gpu_launches": (8 if n >= (1 << 18) else 3) * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                              "kernel": "k_trace_persistent4<16> (closest-hit walk, 4-wide BVH, shared-memory short stack)", "kernel_ms": walk_ms,

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <exception>
 #include <memory>
@@ -536,9 +537,10 @@ struct rx_host_scene {
 };
 
 namespace {
-void set_err(char* dst, size_t len, const std::string& m) {
-  if (dst && len) snprintf(dst, len, "%s", m.c_str());
+void set_err(char* dst, size_t len, const char* m) {
+  if (dst && len) snprintf(dst, len, "%s", m);
 }
+void set_err(char* dst, size_t len, const std::string& m) { set_err(dst, len, m.c_str()); }
 
 rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info& in, std::string& err) {
   Loader L;
@@ -648,16 +650,31 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
   std::vector<Mesh> meshes(objs.size());
   std::vector<std::string> mesh_err(objs.size());
   std::vector<char> mesh_ok(objs.size(), 0);
+  // a worker that meets an exception records it here without allocating (no exception
+  // leaves a worker thread); the message is built on the calling thread afterwards
+  enum : char { kNoExc = 0, kOutOfMemory = 1, kOtherExc = 2 };
+  std::vector<char> mesh_exc(objs.size(), kNoExc);
+  std::vector<std::array<char, 160>> mesh_what(objs.size());
   {
     std::atomic<size_t> next{0};
-    auto work = [&]() {
+    auto work = [&]() noexcept {
       for (size_t i; (i = next.fetch_add(1)) < objs.size();) {
         const char* fp = objs[i]->value("filePath");
         try {
           if (fp) mesh_ok[i] = load_mesh(L.resolve(fp), meshes[i], mesh_err[i]);
-        } catch (const std::exception&) {  // no exception leaves a worker (or the C ABI)
+        } catch (const std::bad_alloc&) {
           mesh_ok[i] = 0;
-          mesh_err[i] = "out of host memory reading " + std::string(fp);
+          mesh_exc[i] = kOutOfMemory;
+        } catch (const std::exception& ex) {
+          mesh_ok[i] = 0;
+          mesh_exc[i] = kOtherExc;
+          std::strncpy(mesh_what[i].data(), ex.what(), mesh_what[i].size() - 1);
+          mesh_what[i].back() = 0;
+        } catch (...) {
+          mesh_ok[i] = 0;
+          mesh_exc[i] = kOtherExc;
+          std::strncpy(mesh_what[i].data(), "unknown exception", mesh_what[i].size() - 1);
+          mesh_what[i].back() = 0;
         }
       }
     };
@@ -679,6 +696,9 @@ rx_status read_config(const char* config_path, rx_host_scene& H, rx_config_info&
     rx_status st = resolve(k, o);
     if (st != RX_OK) return st;
     if (!k->value("filePath")) return err = "object without <filePath>", RX_ERR_INVALID;
+    if (mesh_exc[i] == kOutOfMemory) return err = "out of host memory reading " + std::string(k->value("filePath")), RX_ERR_OOM;
+    if (mesh_exc[i] == kOtherExc)
+      return err = "error reading " + std::string(k->value("filePath")) + ": " + mesh_what[i].data(), RX_ERR_INVALID;
     if (!mesh_ok[i]) return err = mesh_err[i], RX_ERR_INVALID;
     if ((st = add_object(o, meshes[i], k->first("transform") ? k->value("transform") : nullptr)) != RX_OK) return st;
     meshes[i] = Mesh();  // release as we go
@@ -727,16 +747,25 @@ extern "C" rx_status rx_config_read(const char* config_path, rx_host_scene** out
                                     size_t err_len) {
   if (!config_path || !out) return set_err(err, err_len, "null argument"), RX_ERR_INVALID;
   *out = nullptr;
-  auto* H = new rx_host_scene();
+  std::unique_ptr<rx_host_scene> H;
   rx_config_info in{};
   std::string e;
-  rx_status s = read_config(config_path, *H, in, e);
+  rx_status s;
+  try {  // no exception crosses the C ABI
+    H.reset(new rx_host_scene());
+    s = read_config(config_path, *H, in, e);
+  } catch (const std::bad_alloc&) {
+    set_err(err, err_len, "out of host memory");
+    return RX_ERR_OOM;
+  } catch (const std::exception& ex) {
+    set_err(err, err_len, ex.what());
+    return RX_ERR_INVALID;
+  }
   if (s != RX_OK) {
-    delete H;
     set_err(err, err_len, e);
     return s;
   }
-  *out = H;
+  *out = H.release();
   if (info) *info = in;
   return RX_OK;
 }
@@ -766,7 +795,14 @@ extern "C" rx_status rx_scene_load_config(rx_context* c, const char* config_path
   rx_host_scene H;
   rx_config_info in{};
   std::string err;
-  rx_status s = read_config(config_path, H, in, err);
+  rx_status s;
+  try {  // no exception crosses the C ABI
+    s = read_config(config_path, H, in, err);
+  } catch (const std::bad_alloc&) {
+    return c->fail(RX_ERR_OOM, "out of host memory reading the config");
+  } catch (const std::exception& ex) {
+    return c->fail(RX_ERR_INVALID, ex.what());
+  }
   if (s != RX_OK) return c->fail(s, err);
   s = rx_scene_set_geometry(c, H.verts.data(), (uint32_t)(H.verts.size() / 3), H.tris.data(),
                             (uint32_t)(H.tris.size() / 3), H.tri_obj.data(), H.tri_local.data(),

@@ -39,9 +39,10 @@ struct PtShape {
 };
 
 // Scratch of a closest-hit launch over n rays (rx_trace.cu): winner leaves, re-walk
-// queue, and the ray binning's keys, permutation and bin counters.
+// queue, and the ray binning's keys (then the walk's ids by slot), permutation, the
+// walk's distances by slot, and bin counters.
 constexpr uint32_t kRayBins = 1u << 18;
-inline size_t trace_scratch_bytes(size_t n) { return n * 16 + (size_t)kRayBins * 4 + 4096; }
+inline size_t trace_scratch_bytes(size_t n) { return n * 20 + (size_t)kRayBins * 4 + 4096; }
 // Launchers (rx_trace.cu). `queue`: trace_scratch_bytes(n) bytes, or 8 n bytes when
 // `bin` is false. bin: reorder rays by origin cell and direction before the walk (for
 // large batches). `ev` (optional): four events recorded before the walk kernel, after

@@ -65,6 +65,8 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
                                                            int32_t* __restrict__ out_tid,
                                                            float* __restrict__ out_dist,
                                                            uint32_t* __restrict__ hit_leaf,
+                                                           int32_t* __restrict__ slot_tid,
+                                                           float* __restrict__ slot_dist,
                                                            unsigned long long* __restrict__ counters) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int DONE = INT_MIN;
@@ -75,7 +77,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
   const int lane = threadIdx.x & 31, tx = threadIdx.x;
   unsigned long long* cursor = counters + 4;
   bool active = false, exhausted = false;
-  uint32_t ray = 0;
+  uint32_t ray = 0, slot = 0;
   F3 o{}, d{}, inv{}, ood{};
   float tlimit = INFINITY;
   HitResult best{-1, -1.0f, 0u, 0u, false};
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
       if (!active && !exhausted) {
         unsigned long long r = base + __popc(want & ((1u << lane) - 1));
         if (r < n) {
+          slot = (uint32_t)r;
           ray = order ? __ldg(&order[r]) : (uint32_t)r;
           const float4* rp = reinterpret_cast<const float4*>(rays + ray);
           float4 ro = __ldg(rp), rd = __ldg(rp + 1);
@@ -231,9 +234,15 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
     }
 
     if (active && cur == DONE) {
-      out_tid[ray] = best.hit ? best.tid : -1;
-      out_dist[ray] = best.hit ? best.t : -1.0f;
-      hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+      if (slot_tid) {  // by binned slot (coalesced); the check scatters them to ray order
+        slot_tid[slot] = best.hit ? best.tid : -1;
+        slot_dist[slot] = best.hit ? best.t : -1.0f;
+        hit_leaf[slot] = best.hit ? best.leaf : kNoLeaf;
+      } else {
+        out_tid[ray] = best.hit ? best.tid : -1;
+        out_dist[ray] = best.hit ? best.t : -1.0f;
+        hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+      }
       active = false;
     }
   }
@@ -245,6 +254,10 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
 __global__ void __launch_bounds__(128) k_check_visible_thread(DevAccel A, const rx_ray* __restrict__ rays,
                                                               uint32_t n, const uint32_t* __restrict__ order,
                                                               const uint32_t* __restrict__ hit_leaf,
+                                                              const int32_t* __restrict__ slot_tid,
+                                                              const float* __restrict__ slot_dist,
+                                                              int32_t* __restrict__ out_tid,
+                                                              float* __restrict__ out_dist,
                                                               uint32_t* __restrict__ eager_queue,
                                                               unsigned long long* __restrict__ counters) {
   constexpr unsigned FULL = 0xffffffffu;
@@ -257,7 +270,13 @@ __global__ void __launch_bounds__(128) k_check_visible_thread(DevAccel A, const 
     uint32_t i = j < n && order ? __ldg(&order[j]) : j;  // binned order: a warp checks nearby leaves
     bool fail = false;
     if (j < n) {
-      uint32_t leaf = __ldg(&hit_leaf[i]);
+      // slot_tid: the walk left its answers by binned slot; this is where they reach ray
+      // order (a rejected winner is re-walked after, overwriting them)
+      uint32_t leaf = __ldg(&hit_leaf[slot_tid ? j : i]);
+      if (slot_tid) {
+        out_tid[i] = __ldg(&slot_tid[j]);
+        out_dist[i] = __ldg(&slot_dist[j]);
+      }
       if (leaf != kNoLeaf) {
         const float4* rp = reinterpret_cast<const float4*>(rays + i);
         F3 o = f3(__ldg(rp)), d = f3(__ldg(rp + 1));
@@ -320,13 +339,15 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
                                                           int32_t* __restrict__ out_tid,
                                                           float* __restrict__ out_dist,
                                                           uint32_t* __restrict__ hit_leaf,
+                                                           int32_t* __restrict__ slot_tid,
+                                                           float* __restrict__ slot_dist,
                                                           unsigned long long* __restrict__ counters) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int DONE = INT_MIN;
   const int lane = threadIdx.x & 31;
   unsigned long long* cursor = counters + 4;
   bool active = false, exhausted = false;
-  uint32_t ray = 0;
+  uint32_t ray = 0, slot = 0;
   F3 o{}, d{}, inv{}, ood{};
   float tlimit = INFINITY;
   HitResult best{-1, -1.0f, 0u, 0u, false};
@@ -361,6 +382,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
       if (!active && !exhausted) {
         unsigned long long r = base + __popc(want & ((1u << lane) - 1));
         if (r < n) {
+          slot = (uint32_t)r;
           ray = order ? __ldg(&order[r]) : (uint32_t)r;
           const float4* rp = reinterpret_cast<const float4*>(rays + ray);
           float4 ro = __ldg(rp), rd = __ldg(rp + 1);
@@ -450,9 +472,15 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
     }
 
     if (active && cur == DONE) {
-      out_tid[ray] = best.hit ? best.tid : -1;
-      out_dist[ray] = best.hit ? best.t : -1.0f;
-      hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+      if (slot_tid) {  // by binned slot (coalesced); the check scatters them to ray order
+        slot_tid[slot] = best.hit ? best.tid : -1;
+        slot_dist[slot] = best.hit ? best.t : -1.0f;
+        hit_leaf[slot] = best.hit ? best.leaf : kNoLeaf;
+      } else {
+        out_tid[ray] = best.hit ? best.tid : -1;
+        out_dist[ray] = best.hit ? best.t : -1.0f;
+        hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+      }
       active = false;
     }
   }
@@ -558,15 +586,21 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
   uint32_t* eager = queue + n;  // then up to n queued rays
   if (cfg.variant != 0) cudaMemsetAsync(counters + 4, 0, sizeof(unsigned long long), s);  // batch cursor
   const uint32_t* order = nullptr;
+  int32_t* slot_tid = nullptr;
+  float* slot_dist = nullptr;
   if (bin && cfg.variant != 0 && cfg.bin_min && n >= cfg.bin_min) {
     uint32_t* keys = queue + 2 * (size_t)n;
     uint32_t* perm = queue + 3 * (size_t)n;
-    uint32_t* hist = queue + 4 * (size_t)n;
+    uint32_t* hist = queue + 5 * (size_t)n;
     cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), s);
     k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist);
     scan_bins(hist, hist + kRayBins, s);
     k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, nullptr, hist, perm);
     order = perm;
+    if (cfg.check_thread) {  // the walk writes by slot: ids into the keys (no longer needed), distances after perm
+      slot_tid = reinterpret_cast<int32_t*>(keys);
+      slot_dist = reinterpret_cast<float*>(queue + 4 * (size_t)n);
+    }
   }
   if (ev) cudaEventRecord(ev[0], s);
   if (cfg.variant == 0) {
@@ -579,21 +613,22 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     const bool shallow = cfg.walk_stack != 64 && A.bvh_depth < 32;
     const bool walk4 = A.bvh4 && 3 * A.bvh4_depth + 1 <= 64;  // the 4-wide walk's stack bound
     if (cfg.variant == 4 && walk4)
-      k_trace_persistent4<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent4<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
     else if (cfg.variant == 3 && walk4)
-      k_trace_persistent4<0><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent4<0><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
     else if (cfg.variant == 1 && shallow)
-      k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
     else if (cfg.variant == 1)
-      k_trace_persistent<false, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent<false, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
     else if (shallow)
-      k_trace_persistent<true, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent<true, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
     else
-      k_trace_persistent<true, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, counters);
+      k_trace_persistent<true, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
   }
   if (ev) cudaEventRecord(ev[1], s);
   if (cfg.check_thread)
-    k_check_visible_thread<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, order, hit_leaf, eager, counters);
+    k_check_visible_thread<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, order, hit_leaf, slot_tid, slot_dist, tid, dist,
+                                                        eager, counters);
   else
     k_check_visible<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, hit_leaf, eager, counters);
   if (ev) cudaEventRecord(ev[2], s);
