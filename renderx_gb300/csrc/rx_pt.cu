@@ -439,7 +439,12 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
         }
       }
       if (done) {
-        if (L.x != 0.0f || L.y != 0.0f || L.z != 0.0f)
+        // a sample that is not finite is dropped: it comes from a direction the 24-bit
+        // generator draws with probability density zero (a cosine lobe's pole at
+        // u = 0), where the reference's arithmetic divides by zero; one such sample
+        // would poison a pixel's FP64 sum at very high sample counts
+        const bool finite = isfinite(L.x) && isfinite(L.y) && isfinite(L.z);
+        if (finite && (L.x != 0.0f || L.y != 0.0f || L.z != 0.0f))
           film_add(film_sum, film_sq, (int)(R[sc].film_base + (uint32_t)inf.x), L);
         if (training && G.lpath) G.lpath[local] = make_float4(L.x, L.y, L.z, 0.0f);
       } else {

@@ -1,16 +1,17 @@
 // Vertex connection and merging: the reference's VCMTracer (src/VCMTracer.cpp:6-639).
 //
 // Per iteration (VCMTracer.cpp:25-142):
-//  1. k_vcm_light: one light subpath per light path (emission sample + the bounce loop
-//     of MCRenderer::samplePathIter, with light-path scattering), its vertices stored;
-//     every non-specular vertex after the first that is not on an emitter becomes a
-//     photon (VCMTracer.cpp:64-95).
+//  1. Light subpaths (emission sample + the bounce loop of MCRenderer::samplePathIter,
+//     with light-path scattering) as a wavefront, one launch per bounce over the live
+//     subpaths (k_sub_begin / k_sub_step), their vertices stored; every non-specular
+//     vertex after the first that is not on an emitter becomes a photon
+//     (VCMTracer.cpp:64-95).
 //  2. A sort-by-cell hash grid over the photons (cell = 2 r, SmallVCM's spatial hash
 //     (x*73856093)^(y*19349663)^(z*83492791)): count per bucket, exclusive scan,
 //     scatter (the counting-sort build of include/Hashgrid.h:21-91); it replaces the
 //     per-iteration PointKDTree (include/PointKDTree.h), queried with the same strict
 //     |p-x| < r test over the (up to) 8 cells the sphere touches.
-//  3. k_vcm_eye: per pixel, the eye subpath (sampled with light-path scattering, as
+//  3. Per pixel, the eye subpath (the same wavefront, with light-path scattering, as
 //     VCMTracer.cpp:107 does), then colorByMergingPaths (:566-636) and
 //     colorByConnectingPaths (:430-562) with the full-path MIS of connectMergeWeight
 //     (:321-428, double precision) and light-tracing splats through
@@ -385,6 +386,8 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
 }
 
 // ---- light subpaths + photons ----------------------------------------------------------
+// One light subpath per thread (the whole-path check mode, RX_VCM_FULL_PATH_MIS; the
+// default samples them as a wavefront, k_sub_begin / k_sub_step below).
 __global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen,
                                                    float4* photon_pos, int* photon_ref, unsigned* n_photons,
                                                    unsigned photon_cap, unsigned long long* rays) {
@@ -412,6 +415,145 @@ __global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, floa
     });
     nr += (unsigned long long)n;
     llen[p] = n;
+  }
+  if (nr) atomicAdd(rays, nr);
+}
+
+// ---- subpaths as a wavefront -------------------------------------------------------------
+// The bounce loop of sample_path split into launches, one per depth: each launch takes
+// the live subpaths of a queue, scatters and traces one step for each, stores the new
+// vertex and compacts the survivors into the next queue (warp ballot, one atomic per
+// warp), so a warp's lanes stay busy until the queue drains instead of idling while one
+// long subpath finishes. Between launches a subpath is its index, its random-number
+// counter, its vertex count, its depth and its last hit; its last vertex is read back
+// from the vertex store. The random numbers, and so the subpaths, are sample_path's.
+struct SubQ {
+  uint32_t p, k;     // subpath index, random-number counter
+  int n;             // vertices stored
+  uint32_t depth;    // bounce depth; bit 31: an emitter was met after the origin (photons stop)
+  int obj, tri;      // the last ray's hit
+  float dist;
+  uint32_t pad;
+};
+constexpr uint32_t kSeenEmitter = 1u << 31;
+
+// Where a subpath's vertices go: the vertex store, and for VCM light subpaths the photons
+// (random vertices after the origin, up to the first emitter: k_vcm_light's rule).
+struct SubSink {
+  float4* verts;
+  int* len;
+  bool photons;
+  float4* photon_pos;
+  int* photon_ref;
+  unsigned* n_photons;
+  unsigned photon_cap;
+  __device__ void put(const DevScene& S, const VcmParams& P, uint32_t p, int i, const PV& v, bool& seen) const {
+    store_pv(verts + 4 * ((size_t)p * P.maxv + i), v);
+    if (!photons || i == 0 || seen) return;
+    if (is_emissive(S, v.contact)) {
+      seen = true;
+      return;
+    }
+    if (!(v.flags & kDirRandom)) return;
+    unsigned slot = atomicAdd(n_photons, 1u);
+    if (slot < photon_cap) {
+      photon_pos[slot] = make_float4(v.o.x, v.o.y, v.o.z, 0.0f);
+      photon_ref[slot] = (int)(p * P.maxv + i);
+    }
+  }
+};
+
+// Appends the lanes with `live` to queue q (count *qn): warp ballot, one atomic per warp.
+__device__ __forceinline__ void sub_push(bool live, const SubQ& s, SubQ* q, unsigned* qn) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(0xffffffffu, live);
+  if (!m) return;
+  unsigned base = 0;
+  const int leader = __ffs(m) - 1;
+  if (lane == leader) base = atomicAdd(qn, (unsigned)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (live) q[base + __popc(m & ((1u << lane) - 1))] = s;
+}
+
+// The subpaths' first rays: light subpaths from emit_ray (k_vcm_light's stream), eye
+// subpaths from camera_ray (k_vcm_eye_full's); the first vertex stored, live ones queued.
+template <bool LIGHT>
+__global__ void __launch_bounds__(128) k_sub_begin(DevScene S, VcmParams P, SubSink out, SubQ* q, unsigned* qn,
+                                                   unsigned long long* rays) {
+  const uint32_t n = LIGHT ? P.n_light : P.n_pixels;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  unsigned long long nr = 0;
+  for (uint32_t it = 0; it < iters; it++) {
+    const uint32_t p = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = false;
+    SubQ st{};
+    if (p < n) {
+      Rng rng(LIGHT ? P.seed : P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+      Hit3 h;
+      PV start = LIGHT ? emit_ray(S, P.cam, rng, h) : camera_ray(S, P.cam, p, rng, h);
+      bool seen = false;
+      out.put(S, P, p, 0, start, seen);
+      if (start.inside == kNone && h.obj == kNone) {  // nothing to scatter from: the terminating ray
+        out.put(S, P, p, 1, pv_term(start.o), seen);
+        out.len[p] = 2;
+        nr += 2;
+      } else {
+        live = true;
+        st = SubQ{p, rng.k, 1, seen ? kSeenEmitter : 0u, h.obj, h.tri, h.dist, 0u};
+      }
+    }
+    sub_push(live, st, q, qn);
+  }
+  if (nr) atomicAdd(rays, nr);
+}
+
+// One bounce of every queued subpath (sample_path's loop body after its first put):
+// scatter from the last vertex, end on a killed ray or the depth cap, trace the new ray,
+// end on a miss, else store it and queue the subpath for the next launch. `light`: the
+// isLightPath argument of the scattering.
+template <bool LIGHT>
+__global__ void __launch_bounds__(128) k_sub_step(DevScene S, VcmParams P, SubSink out, bool light_scatter,
+                                                  const SubQ* qin, const unsigned* qin_n, SubQ* qout, unsigned* qout_n,
+                                                  unsigned long long* rays) {
+  const uint32_t n = *qin_n;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (n + stride - 1) / stride;
+  unsigned long long nr = 0;
+  for (uint32_t it = 0; it < iters; it++) {
+    const uint32_t j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = false;
+    SubQ st{};
+    if (j < n) {
+      st = qin[j];
+      const uint32_t p = st.p;
+      Rng rng(LIGHT ? P.seed : P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, st.k);
+      const PV prev = load_pv(out.verts + 4 * ((size_t)p * P.maxv + st.n - 1));
+      bool seen = (st.depth & kSeenEmitter) != 0;
+      const uint32_t depth = st.depth & ~kSeenEmitter;
+      int m = st.n;
+      PV next = scatter_step(S, P.cam, prev, Hit3{st.obj, st.tri, st.dist}, light_scatter, true, rng);
+      if (length(next.d) < 0.5f) {
+        out.put(S, P, p, m++, next, seen);
+      } else if (depth + 1 > P.max_depth) {
+        out.put(S, P, p, m++, pv_term(prev.o), seen);
+      } else {
+        PHit hh = trace_cond<false>(S, next.o, next.d, INFINITY, next.contact, next.inside);
+        out.put(S, P, p, m++, next, seen);
+        if (hh.tid < 0) {
+          out.put(S, P, p, m++, pv_term(prev.o), seen);
+        } else {
+          live = true;
+          st = SubQ{p, rng.k, m, (depth + 1) | (seen ? kSeenEmitter : 0u), (int)__ldg(&S.tri_obj[hh.tid]), hh.tid,
+                    hh.t, 0u};
+        }
+      }
+      if (!live) {
+        out.len[p] = m;
+        nr += (unsigned long long)m;
+      }
+    }
+    sub_push(live, st, qout, qout_n);
   }
   if (nr) atomicAdd(rays, nr);
 }
@@ -648,26 +790,11 @@ __device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
 // ---- eye subpaths and connections as a wavefront -----------------------------------------
 // colorByConnectingPaths (VCMTracer.cpp:430-562) joins every light vertex ci of the
 // pixel's light path with every eye vertex k (s = ci + 1, t = k + 1), plus the pure
-// eye path (s = 0). k_vcm_eye samples and stores the eye subpath and its records, adds
-// the s = 0 technique, and lists which vertices can take part in a connection (sampled
+// eye path (s = 0). The subpath wavefront samples and stores the eye subpath; k_eye_post
+// builds its records, adds the s = 0 technique, and lists which vertices can take part
+// in a connection (sampled
 // at random, not on an emitter past the light's own vertex); the (k, ci) pairs are then
 // evaluated one per lane with their shadow rays (k_conn_eval).
-__global__ void __launch_bounds__(128) k_vcm_eye(DevScene S, VcmParams P, float4* ev, int* elen,
-                                                 unsigned long long* rays) {
-  uint32_t stride = gridDim.x * blockDim.x;
-  unsigned long long nrays = 0;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n_pixels; p += stride) {
-    Rng rng(P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
-    Hit3 h;
-    PV start = camera_ray(S, P.cam, p, rng, h);
-    float4* out = ev + 4 * ((size_t)p * P.maxv);
-    int ne = sample_path(S, P.cam, start, h, P.max_depth, !P.bpt, rng,
-                         [&](int i, const PV& v) { store_pv(out + 4 * i, v); });
-    nrays += (unsigned long long)ne;
-    elen[p] = ne;
-  }
-  if (nrays) atomicAdd(rays, nrays);
-}
 
 // Per pixel, from its stored eye subpath: the records, the s = 0 technique (the eye
 // path ends on an emitter and the reference's mustUsePT holds: VCM, no interior vertex
@@ -814,7 +941,9 @@ __global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, cons
 
 // Per pixel: the eye subpath and colorByConnectingPaths by the reference's loops over each
 // whole joined path, a shadow ray per connection in the same thread. Kept as the check of
-// k_vcm_eye + k_conn_eval (RX_VCM_FULL_PATH_MIS).
+// the eye wavefront + k_eye_post + k_conn_eval (RX_VCM_FULL_PATH_MIS, which also samples
+// the light subpaths one per thread, k_vcm_light: the same random numbers, so the same
+// subpaths as the wavefronts).
 __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, const float4* lv, const int* llen,
                                                  float4* ev, int* elen, MisE* emis, float* img,
                                                  unsigned long long* rays) {
@@ -1147,7 +1276,10 @@ __global__ void k_vcm_accumulate(VcmParams P, const float* img, double* film) {
     int x = p % P.cam.width, y = p / P.cam.width;
     F3 dc = cam_dir(P.cam, x + 0.5f, y + 0.5f);
     float v = fabsf(dot(dc, P.cam.front));
-    for (int c = 0; c < 3; c++) film[3 * p + c] += (double)(img[3 * p + c] / v);
+    for (int c = 0; c < 3; c++) {
+      const double a = (double)(img[3 * p + c] / v);
+      if (isfinite(a)) film[3 * p + c] += a;  // a non-finite value (a zero-density sample) is dropped
+    }
   }
 }
 
@@ -1497,9 +1629,13 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.bpt ? 1u : P.n_light * P.maxv;  // photon capacity (none without merging)
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(24);
+  std::vector<DevBuf> bufs(27);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
+  const size_t nsub = std::max(P.n_light, P.n_pixels);
+  if ((e = al(24, nsub * sizeof(SubQ))) != cudaSuccess) return e;  // subpath queues (wavefront)
+  if ((e = al(25, nsub * sizeof(SubQ))) != cudaSuccess) return e;
+  if ((e = al(26, 16)) != cudaSuccess) return e;                      // their lengths
   if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
   if ((e = al(1, (size_t)P.n_light * sizeof(int))) != cudaSuccess) return e;
   if ((e = al(2, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;                      // photon positions
@@ -1552,8 +1688,33 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     P.radius = radius;
     P.iter = it;
     cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
-    k_vcm_light<<<grid * 4, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
-                                     bufs[3].as<int>(), nph, cap, ctr);
+    // the subpaths as a wavefront (the whole-path check mode keeps one thread per subpath)
+    auto subpaths = [&](bool light_side) {
+      const SubSink out = light_side ? SubSink{bufs[0].as<float4>(), bufs[1].as<int>(), !P.bpt, bufs[2].as<float4>(),
+                                               bufs[3].as<int>(), nph, cap}
+                                     : SubSink{bufs[12].as<float4>(), bufs[13].as<int>(), false, nullptr, nullptr,
+                                               nullptr, 0u};
+      SubQ* q[2] = {bufs[24].as<SubQ>(), bufs[25].as<SubQ>()};
+      unsigned* qn = bufs[26].as<unsigned>();
+      unsigned long long* rc = ctr + (light_side ? 0 : 1);
+      cudaMemsetAsync(qn, 0, 2 * sizeof(unsigned), s);
+      if (light_side) k_sub_begin<true><<<grid * 4, 128, 0, s>>>(S, P, out, q[0], qn, rc);
+      else k_sub_begin<false><<<grid * 4, 128, 0, s>>>(S, P, out, q[0], qn, rc);
+      const bool light_scatter = light_side || !P.bpt;  // VCM samples eye paths with light-path scattering
+      for (uint32_t d = 0; d <= P.max_depth; d++) {
+        const int a = d & 1, b = a ^ 1;
+        cudaMemsetAsync(qn + b, 0, sizeof(unsigned), s);
+        if (light_side)
+          k_sub_step<true><<<grid * 4, 128, 0, s>>>(S, P, out, light_scatter, q[a], qn + a, q[b], qn + b, rc);
+        else
+          k_sub_step<false><<<grid * 4, 128, 0, s>>>(S, P, out, light_scatter, q[a], qn + a, q[b], qn + b, rc);
+      }
+    };
+    if (full_mis)
+      k_vcm_light<<<grid * 4, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
+                                       bufs[3].as<int>(), nph, cap, ctr);
+    else
+      subpaths(true);
     k_light_mis<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[19].as<MisL>());
     const float cell = 2.0f * radius;
     Grid G{cell, buckets - 1, bufs[7].as<unsigned>(), bufs[22].as<float4>(), bufs[5].as<int>(), bufs[23].as<float4>()};
@@ -1597,7 +1758,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
       k_vcm_eye_full<<<grid, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
                                           bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[10].as<float>(), ctr + 1);
     } else {
-      k_vcm_eye<<<grid * 4, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), ctr + 1);
+      subpaths(false);
       k_eye_post<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[12].as<float4>(),
                                           bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[21].as<uint2>(), qc,
                                           bufs[10].as<float>());
