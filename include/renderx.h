@@ -137,8 +137,11 @@ typedef struct rx_batch_item {
 typedef struct rx_batch_options {
   uint32_t paths_per_pass; /* wavefront size shared by all scenes, 0 = 2^22 */
   uint32_t use_graph;      /* 1: capture one pass as a CUDA graph and replay it */
-  uint32_t autotune;       /* 1: time the launch-shape candidates on the first passes */
-  uint32_t reserved;
+  uint32_t autotune;       /* 1: time candidates on the first passes, two passes each (their
+                              samples count): the launch shapes at paths_per_pass, then the
+                              pass sizes 2^20..2^23 with the best shape. Autotuned and guided
+                              batches take an equal share of every item in each pass. */
+  uint32_t chosen_paths_per_pass;  /* out: paths per pass of the remaining passes */
   int32_t chosen_blocks_per_sm;  /* out: extend / shade blocks per SM used */
   int32_t chosen_stack;          /* out: walk used: 4 = 4-wide BVH, 5 = 4-wide BVH with a
                                     shared-memory short stack, 32 / 64 = binary BVH with

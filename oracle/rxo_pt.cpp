@@ -180,6 +180,15 @@ PRay scatter_diffuse(const Scene& S, int obj, V3 col, const PRay& in, bool russi
   }
   out.d = to_world(frame_from(n), hemi_cos(1.0f, rng));
   float p = maxc(col);
+  if (!(dot(n, out.d) >= kCosTermMin)) {
+    // a direction at the hemisphere's rim (u = 0 exactly, probability 2^-24 here, zero
+    // for the continuous sampler): its density falls below the cosine clamp, so the
+    // weight would blow up; the path ends (as the library's sampler does)
+    out.d = {0, 0, 0};
+    out.color = {0, 0, 0};
+    out.dprob = 1;
+    return out;
+  }
   if (rng.next() < p || !russian) {
     bool front = dot(n, in.d) <= 0 && dot(n, out.d) >= 0;
     out.color = front ? mul(col, 1.0f / kPi) : V3{0, 0, 0};

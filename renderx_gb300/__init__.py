@@ -237,7 +237,8 @@ class Context:
         st = rx_render_stats()
         self._ck(self._L.rx_render_pt_batch(self.h, arr, len(items), ctypes.byref(bo), ctypes.byref(st)))
         return films, dict(extension_rays=st.extension_rays, shadow_rays=st.shadow_rays, paths=st.paths, ms=st.ms,
-                           blocks_per_sm=bo.chosen_blocks_per_sm, stack=bo.chosen_stack)
+                           blocks_per_sm=bo.chosen_blocks_per_sm, stack=bo.chosen_stack,
+                           paths_per_pass=bo.chosen_paths_per_pass)
 
     def render_vcm(self, camera: "scenes.Camera", iterations: int, radius: float, alpha: float = 0.6667,
                    max_depth: int = 8, light_paths: int = 0, seed: int = 1, full_path_mis: bool = False,

@@ -57,7 +57,7 @@ class rx_batch_item(ctypes.Structure):
 
 class rx_batch_options(ctypes.Structure):
     _fields_ = [("paths_per_pass", ctypes.c_uint32), ("use_graph", ctypes.c_uint32), ("autotune", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32), ("chosen_blocks_per_sm", ctypes.c_int32),
+                ("chosen_paths_per_pass", ctypes.c_uint32), ("chosen_blocks_per_sm", ctypes.c_int32),
                 ("chosen_stack", ctypes.c_int32)]
 
 

@@ -439,6 +439,7 @@ rx_status rx_render_pt_batch(rx_context* c, const rx_batch_item* items, uint32_t
   if (opts) {
     opts->chosen_blocks_per_sm = shape.blocks_per_sm;
     opts->chosen_stack = shape.stack;
+    opts->chosen_paths_per_pass = shape.paths_per_pass;
   }
   if (stats) *stats = st;
   return RX_OK;

@@ -917,6 +917,7 @@ struct GuideState {
   // step count; device copies of this network's NetDev and of the record segment the
   // single-network entry points train on
   DevBuf params, m, v, grad, img, scratch, status, step, dnet, dseg;
+  RecSeg seg_uploaded{};  // what dseg holds (uploaded again only when it changes)
   int sms = 152;
   bool ready = false;
 };
@@ -1005,9 +1006,12 @@ cudaError_t guide_train_nets(const NetDev* nets, const RecSeg* segs, int nnet, i
 
 // One step of this network alone on n device records (the single-network entry points).
 static cudaError_t train_step(GuideState* g, const float* recs, uint32_t n, cudaStream_t s, bool update) {
-  RecSeg R{recs, nullptr, n, n};
-  cudaError_t e = cudaMemcpyAsync(g->dseg.p, &R, sizeof R, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return e;
+  const RecSeg R{recs, nullptr, n, n};
+  if (std::memcmp(&R, &g->seg_uploaded, sizeof R) != 0) {
+    cudaError_t e = cudaMemcpyAsync(g->dseg.p, &R, sizeof R, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    g->seg_uploaded = R;
+  }
   const int per = train_ctas_per_net(n, 1, g->sms);
   return train_nets_step(g->dnet.as<NetDev>(), g->dseg.as<RecSeg>(), 1, per, -1, nullptr, update, g->sms, s);
 }

@@ -32,17 +32,18 @@ struct TraceConfig {
 // Launch shape of the wavefront's extend / shade kernels: blocks of 128 threads per SM
 // and the walk: 4 = the 4-wide BVH, 5 = the same with the first 16 stack entries in
 // shared memory, 32 or 64 = the binary BVH with that many stack entries (must exceed
-// the BVH depth).
+// the BVH depth); and the paths per pass.
 struct PtShape {
   int blocks_per_sm = 8;
   int stack = 64;
+  uint32_t paths_per_pass = 0;  // paths per pass (the queue size)
 };
 
 // Scratch of a closest-hit launch over n rays (rx_trace.cu): winner leaves, re-walk
-// queue, and the ray binning's keys (then the walk's ids by slot), permutation, the
-// walk's distances by slot, and bin counters.
+// queue, the ray binning's keys and permutation, the walk's answers by binned slot
+// (16 bytes a ray, 16-byte aligned), and bin counters.
 constexpr uint32_t kRayBins = 1u << 18;
-inline size_t trace_scratch_bytes(size_t n) { return n * 20 + (size_t)kRayBins * 4 + 4096; }
+inline size_t trace_scratch_bytes(size_t n) { return n * 32 + (size_t)kRayBins * 4 + 4096; }
 // Launchers (rx_trace.cu). `queue`: trace_scratch_bytes(n) bytes, or 8 n bytes when
 // `bin` is false. bin: reorder rays by origin cell and direction before the walk (for
 // large batches). `ev` (optional): four events recorded before the walk kernel, after

@@ -91,6 +91,9 @@ __device__ __forceinline__ F3 hg_sample(float g, F3 d, float e1, float e2) {
   return to_world(f, F3{st * cp, ct, st * sp});
 }
 
+// COS_TERM_MIN (reference include/macros.h:9): the floor of Ray::getCosineTerm.
+constexpr float kCosMin = 1e-6f;
+
 // Ray::getContactNormal: the contact object's normal at the ray origin; the camera's is
 // its viewing direction (Camera::getWorldNormal).
 __device__ __forceinline__ F3 contact_normal(const DevScene& S, const CamDev& cam, const PV& r, bool flat = false) {
@@ -104,7 +107,7 @@ __device__ __forceinline__ float cos_term(const DevScene& S, const CamDev& cam, 
   float d = 1.0f;
   bool has_cos = r.contact == kCameraObj || (r.contact >= 0 && !is_vpm(S, r.contact));
   if (has_cos && length(r.d) > 0.5f) d = fabsf(dot(contact_normal(S, cam, r), r.d));
-  return fmaxf(d, 1e-6f);
+  return fmaxf(d, kCosMin);
 }
 // Ray::getRadianceDecay: the inside object's transmittance over `dist`
 __device__ __forceinline__ F3 decay_of(const DevScene& S, int inside, float dist) {
@@ -448,6 +451,16 @@ static __device__ PV scatter_material(const DevScene& S, const CamDev& cam, int 
     o.d = to_world(f, hemi_cos(1.0f, r1, r2));
     float p = maxc(c);
     o.flags = kDirRandom;
+    if (!(dot(n, o.d) >= kCosMin)) {
+      // a direction at the hemisphere's rim (u = 0 exactly: probability 2^-24 for a
+      // 24-bit generator, zero for the continuous sampler): its density cos / pi falls
+      // below the cosine clamp of Ray::getCosineTerm (COS_TERM_MIN), so the reference's
+      // weight (BSDF x clamped cosine / density) would blow up; the path ends instead
+      o.d = {0, 0, 0};
+      o.c = {0, 0, 0};
+      o.dprob = 1.0f;
+      return o;
+    }
     if (rng.next() < p || !russian) {
       o.c = (dot(n, in.d) <= 0.0f && dot(n, o.d) >= 0.0f) ? c * (1.0f / RX_PI) : F3{0, 0, 0};
       float pdf = cos_lobe_pdf(n, o.d, 1.0f);

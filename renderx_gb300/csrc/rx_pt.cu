@@ -40,21 +40,30 @@ struct SceneRec {
   uint64_t path_begin;  // concatenated passes: first global path index of the scene
   uint64_t film_base;   // first pixel of the scene in the shared film
   uint64_t paths;       // pixels x spp
-  uint32_t per_pass;    // interleaved passes: paths of this scene in each pass
   int32_t net;          // guiding network of the scene (index into the render's networks), -1: none
 };
 
 // Pass cursor in device memory, so that one captured pass replays unchanged. Two
 // layouts of the paths over passes: concatenated (pass p takes global paths
 // [p per_pass, (p + 1) per_pass) of the scenes' paths laid end to end) and interleaved
-// (pass p takes paths [p q_k, (p + 1) q_k) of every scene k, q_k = SceneRec::per_pass,
-// so every scene advances through its samples at the same pace: guided renders, whose
-// networks warm up, train and guide on a schedule of passes).
+// (each pass takes the next quota[k] paths of every scene k, quota[k] proportional to
+// the scene's paths, so every scene advances through its samples at the same pace and
+// every pass holds the same mix: guided renders, whose networks warm up, train and
+// guide on a schedule of passes, and autotuned ones, whose candidates are timed on
+// consecutive passes). Interleaved passes keep each scene's cursor (paths taken) in
+// device memory; the quotas can change between passes (the queue-size candidates).
 struct PassState {
   uint64_t base, total;  // concatenated: first global path of the pass, all paths
   uint32_t per_pass, npaths;
   uint32_t pass;         // passes done (the guiding schedule reads it)
   uint32_t interleaved;
+};
+
+// Interleaved layout: per scene, the paths taken so far and the quota of each pass.
+struct Layout {
+  uint32_t* off;        // the current pass's offset of each scene's paths (nr + 1)
+  uint64_t* taken;      // paths of each scene taken by earlier passes
+  const uint32_t* quota;  // paths of each scene per pass
 };
 
 // A path's id: its index within its scene (the random-number key) and, in the top 24
@@ -80,24 +89,20 @@ __device__ __forceinline__ F3 camera_dir(const CamDev& c, float xp, float yp) {
   return normalize(c.front * c.sight + c.right * x + c.up * y);
 }
 
-// Interleaved passes: paths of scene r in pass p.
-__host__ __device__ __forceinline__ uint32_t pass_share(const SceneRec& r, uint32_t p) {
-  const uint64_t start = (uint64_t)p * r.per_pass;
-  if (start >= r.paths) return 0u;
-  const uint64_t left = r.paths - start;
-  return left < r.per_pass ? (uint32_t)left : r.per_pass;
+// Interleaved passes: the share of scene k in the current pass.
+__host__ __device__ __forceinline__ uint32_t pass_share(uint64_t paths, uint64_t taken, uint32_t quota) {
+  if (taken >= paths) return 0u;
+  const uint64_t left = paths - taken;
+  return left < quota ? (uint32_t)left : quota;
 }
 
 // Interleaved passes: offsets off[0..nr] of each scene's paths in the generation order
 // of the current pass (one block).
-__global__ void __launch_bounds__(256) k_layout(const SceneRec* R, int nr, const PassState* ps, uint32_t* off) {
+__global__ void __launch_bounds__(256) k_layout(const SceneRec* R, int nr, Layout L) {
   __shared__ uint32_t part[256];
-  const uint32_t p = ps->pass;
   const int per = (nr + 255) / 256, k0 = threadIdx.x * per, k1 = min(nr, k0 + per);
   uint32_t sum = 0;
-  for (int k = k0; k < k1; k++) {
-    sum += pass_share(R[k], p);
-  }
+  for (int k = k0; k < k1; k++) sum += pass_share(R[k].paths, L.taken[k], L.quota[k]);
   part[threadIdx.x] = sum;
   __syncthreads();
   for (int o = 1; o < 256; o <<= 1) {  // inclusive scan of the per-thread sums
@@ -108,10 +113,15 @@ __global__ void __launch_bounds__(256) k_layout(const SceneRec* R, int nr, const
   }
   uint32_t acc = part[threadIdx.x] - sum;
   for (int k = k0; k < k1; k++) {
-    off[k] = acc;
-    acc += pass_share(R[k], p);
+    L.off[k] = acc;
+    acc += pass_share(R[k].paths, L.taken[k], L.quota[k]);
   }
-  if (threadIdx.x == 255) off[nr] = part[255];
+  if (threadIdx.x == 255) L.off[nr] = part[255];
+}
+
+// End of an interleaved pass: each scene's cursor moves past its share (one block).
+__global__ void k_layout_advance(int nr, Layout L) {
+  for (int k = threadIdx.x; k < nr; k += blockDim.x) L.taken[k] += L.off[k + 1] - L.off[k];
 }
 
 // Scene k with off[k] <= i < off[k + 1].
@@ -125,25 +135,23 @@ __device__ __forceinline__ int scene_at(const uint32_t* off, int nr, uint32_t i)
   return lo;
 }
 
-__global__ void k_generate(const SceneRec* R, int nr, PassState* ps, const uint32_t* off, PathSoA S,
-                           unsigned* count) {
+__global__ void k_generate(const SceneRec* R, int nr, PassState* ps, Layout L, PathSoA S, unsigned* count) {
   uint32_t np;
   const bool inter = ps->interleaved != 0;
   if (inter) {
-    np = off[nr];
+    np = L.off[nr];
   } else {
     const uint64_t left = ps->base < ps->total ? ps->total - ps->base : 0;
     np = (uint32_t)(left < ps->per_pass ? left : ps->per_pass);
   }
   const uint64_t base = ps->base;
-  const uint32_t pass = ps->pass;
   uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += stride) {
     int sc;
     uint64_t pid;  // path index within its scene (random-number key)
     if (inter) {
-      sc = scene_at(off, nr, i);
-      pid = (uint64_t)pass * R[sc].per_pass + (i - off[sc]);
+      sc = scene_at(L.off, nr, i);
+      pid = L.taken[sc] + (i - L.off[sc]);
     } else {
       uint64_t g = base + i;
       sc = scene_of(R, nr, g);
@@ -310,8 +318,10 @@ static __device__ PV scatter_guided(const DevScene& S, const PV& in, Hit3 h, boo
       return o;  // d = 0, c = 0: the path ends
     }
     float pdf = frac * cos_lobe_pdf(n, w, 1.0f) + (1.0f - frac) * guide::mix_pdf(G, w);
-    bool front = dot(n, in.d) <= 0.0f && dot(n, w) >= 0.0f;
-    if (!front || !(pdf > 0.0f)) return o;  // no contribution: end
+    // no contribution below the surface; at its rim (cosine under the clamp of
+    // Ray::getCosineTerm) the path ends as in the plain diffuse scatter
+    bool front = dot(n, in.d) <= 0.0f && dot(n, w) >= kCosMin;
+    if (!front || !(pdf > 0.0f)) return o;  // end
     o.d = w;
     o.c = c * (1.0f / RX_PI);
     o.dprob = (russian ? p : 1.0f) * pdf;
@@ -700,7 +710,7 @@ struct Wave {
   double *film, *sq;
   uint32_t loops;           // bounce stages per pass (max depth cap + 1)
   uint32_t *keys, *order, *hist;  // ray binning of bounce rays (null: off)
-  uint32_t* off;            // interleaved passes: each scene's offset in the pass (null: concatenated)
+  Layout L;                 // interleaved passes (L.off null: concatenated)
   int sms;
   // guiding (nets null: off)
   const guide::NetDev* nets;
@@ -751,9 +761,9 @@ cudaError_t enqueue_infer(const Wave& W, const PathSoA& cur, const unsigned* cc,
 template <int STACK>
 cudaError_t enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
-  if (W.off) k_layout<<<1, 256, 0, s>>>(W.R, W.nr, W.ps, W.off);
+  if (W.L.off) k_layout<<<1, 256, 0, s>>>(W.R, W.nr, W.L);
   if (W.recs) k_records_begin<<<1, 256, 0, s>>>(W.nets, W.nnet, W.ps, W.cnt + 2, W.net_count);
-  k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.off, W.A, W.cnt);
+  k_generate<<<grid, 256, 0, s>>>(W.R, W.nr, W.ps, W.L, W.A, W.cnt);
   const GuideIO G{W.nets, W.lobes, W.recs, W.cnt + 2, W.rec_cap, W.lpath};
   PathSoA cur = W.A, nxt = W.B;
   unsigned *cc = W.cnt, *cn = W.cnt + 1;
@@ -767,10 +777,11 @@ cudaError_t enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
     std::swap(cc, cn);
   }
   if (W.recs) {
-    k_record_weights<<<grid, 128, 0, s>>>(W.R, W.nr, W.off, W.ps, W.nets, W.nnet, W.recs, W.cnt + 2, W.rec_cap,
+    k_record_weights<<<grid, 128, 0, s>>>(W.R, W.nr, W.L.off, W.ps, W.nets, W.nnet, W.recs, W.cnt + 2, W.rec_cap,
                                           W.lpath, W.train, W.net_count, W.rbase, W.rcap);
     if (e == cudaSuccess) e = guide_train_nets(W.nets, W.segs, W.nnet, W.steps, W.batch_max, &W.ps->pass, W.sms, s);
   }
+  if (W.L.off) k_layout_advance<<<1, 256, 0, s>>>(W.nr, W.L);
   k_advance<<<1, 1, 0, s>>>(W.ps);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
@@ -822,16 +833,37 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   per_pass = (uint32_t)std::min<uint64_t>(std::min<uint32_t>(per_pass, max_slots - (uint32_t)nj), total);
   if (per_pass == 0) return cudaSuccess;
   const uint64_t npasses = (total + per_pass - 1) / per_pass;
-  // guided renders interleave the scenes: every pass takes its share of each scene
-  uint32_t slots = per_pass;
-  if (guided) {
-    uint64_t sum = 0;
-    for (auto& r : recs) {
-      r.per_pass = (uint32_t)((r.paths + npasses - 1) / npasses);
-      sum += r.per_pass;
+  // interleaved passes for guided renders (one schedule for all networks) and autotuned
+  // ones (candidates timed on passes of the same mix)
+  const bool inter = guided || run.autotune;
+  // per-scene quotas of a pass of about `size` paths: guided and untuned renders divide
+  // every scene over the same number of passes; the queue-size candidates take their
+  // share of `size` in proportion to the scenes' paths
+  auto quotas = [&](uint32_t size, bool same_passes) {
+    std::vector<uint32_t> q(nj);
+    const uint64_t np = (total + size - 1) / size;
+    for (int k = 0; k < nj; k++) {
+      uint64_t v = same_passes ? (recs[k].paths + np - 1) / np
+                               : (uint64_t)(((unsigned __int128)recs[k].paths * size + total - 1) / total);
+      q[k] = (uint32_t)std::max<uint64_t>(recs[k].paths ? 1 : 0, std::min<uint64_t>(v, max_slots));
     }
-    slots = (uint32_t)sum;
-  }
+    return q;
+  };
+  auto qsum = [](const std::vector<uint32_t>& q) {
+    uint64_t s = 0;
+    for (uint32_t v : q) s += v;
+    return s;
+  };
+  const std::vector<uint32_t> q_default = quotas(per_pass, true);
+  // queue-size candidates (untuned: the given size only)
+  std::vector<uint32_t> sizes;
+  if (run.autotune && !guided)
+    for (uint32_t c : {1u << 20, 1u << 21, 1u << 22, 1u << 23})
+      if (c <= max_slots - (uint32_t)nj && (uint64_t)c * 8 <= total) sizes.push_back(c);
+  uint64_t slots64 = inter ? qsum(q_default) : per_pass;
+  for (uint32_t c : sizes) slots64 = std::max<uint64_t>(slots64, qsum(quotas(c, false)));
+  if (slots64 > max_slots) return cudaErrorInvalidValue;
+  const uint32_t slots = (uint32_t)slots64;
   const int sms = c->trace_cfg.sms;
 
   std::vector<DevBuf> bufs;
@@ -853,8 +885,16 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   W.sq = film_sq;
   W.sms = sms;
   if (!(W.R = static_cast<const SceneRec*>(upload(recs.data(), sizeof(SceneRec) * nj)))) return e;
-  PassState ps0{0, total, per_pass, 0, 0, guided ? 1u : 0u};
+  PassState ps0{0, total, per_pass, 0, 0, inter ? 1u : 0u};
   if (!(W.ps = static_cast<PassState*>(upload(&ps0, sizeof ps0)))) return e;
+  uint32_t* d_quota = nullptr;
+  if (inter) {
+    if (!(W.L.off = static_cast<uint32_t*>(alloc((size_t)(nj + 1) * 4)))) return e;
+    if (!(W.L.taken = static_cast<uint64_t*>(alloc((size_t)nj * 8)))) return e;
+    if (!(d_quota = static_cast<uint32_t*>(upload(q_default.data(), (size_t)nj * 4)))) return e;
+    W.L.quota = d_quota;
+    cudaMemsetAsync(W.L.taken, 0, (size_t)nj * 8, s);
+  }
   if ((e = alloc_soa(W.A, bufs, slots)) != cudaSuccess) return e;
   if ((e = alloc_soa(W.B, bufs, slots)) != cudaSuccess) return e;
   if (!(W.hit = static_cast<int2*>(alloc(slots * sizeof(int2))))) return e;
@@ -868,7 +908,6 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   }
 
   if (guided) {
-    if (!(W.off = static_cast<uint32_t*>(alloc((size_t)(nj + 1) * 4)))) return e;
     std::vector<guide::NetDev> nets(nnet);
     int steps = 0;
     uint32_t batch_max = 0;
@@ -902,8 +941,8 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
       if (!(W.lpath = static_cast<float4*>(alloc((size_t)slots * sizeof(float4))))) return e;
       if (!(W.net_count = static_cast<unsigned*>(alloc((size_t)nnet * 4)))) return e;
       std::vector<uint64_t> share(nnet, 0);
-      for (auto& r : recs)
-        if (r.net >= 0) share[r.net] += r.per_pass;
+      for (int k = 0; k < nj; k++)
+        if (recs[k].net >= 0) share[recs[k].net] += q_default[k];
       uint64_t all = 0;
       for (uint64_t v : share) all += v;
       std::vector<uint32_t> rbase(nnet), rcap(nnet);
@@ -927,24 +966,42 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
 
   // launch shapes: the context's default, or candidates timed on the first passes
   PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4S : (max_bvh_depth < 32 ? 32 : kStackDepth)};
+  best.paths_per_pass = per_pass;
   std::vector<PtShape> cands;
   if (run.autotune) {
     for (int bps : {4, 8, 16})
       for (int st : {kWalk4S, kWalk4, 32, kStackDepth})
-        if (st == kWalk4 || st == kWalk4S ? wide_ok : st > (int)max_bvh_depth) cands.push_back(PtShape{bps, st});
-    if (npasses < cands.size() + 2) cands.clear();
+        if (st == kWalk4 || st == kWalk4S ? wide_ok : st > (int)max_bvh_depth)
+          cands.push_back(PtShape{bps, st, per_pass});
+    if (npasses < 2 * cands.size() + 2) cands.clear();
   }
 
   Event e0, e1;
   if ((e = e0.create()) != cudaSuccess || (e = e1.create()) != cudaSuccess) return e;
   cudaEventRecord(e0, s);
   uint64_t pass = 0;
-  // paths finished after `p` passes
-  auto paths_done = [&](uint64_t p) -> uint64_t {
-    if (!guided) return std::min<uint64_t>(total, p * (uint64_t)per_pass);
-    uint64_t d = 0;
-    for (auto& r : recs) d += std::min<uint64_t>(r.paths, p * (uint64_t)r.per_pass);
-    return d;
+  // paths taken so far: per scene (interleaved passes, mirroring the device cursors) or
+  // in all (concatenated)
+  std::vector<uint64_t> taken(nj, 0);
+  std::vector<uint32_t> q_now = q_default;
+  uint64_t done_all = 0;
+  auto account = [&]() -> uint64_t {  // one more pass: the paths it took
+    uint64_t n = 0;
+    if (inter) {
+      for (int k = 0; k < nj; k++) {
+        const uint32_t sh = pass_share(recs[k].paths, taken[k], q_now[k]);
+        taken[k] += sh;
+        n += sh;
+      }
+    } else {
+      n = std::min<uint64_t>(per_pass, total - done_all);
+    }
+    done_all += n;
+    return n;
+  };
+  auto set_quota = [&](const std::vector<uint32_t>& q) -> cudaError_t {
+    q_now = q;
+    return cudaMemcpyAsync(d_quota, q_now.data(), (size_t)nj * 4, cudaMemcpyHostToDevice, s);
   };
   // time budget: after queueing pass p, wait for pass p - 1 and stop if the wall time is
   // spent (pass p still completes)
@@ -966,7 +1023,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   const bool snap_on = nj == 1 && snaps.on();
   auto after_pass = [&](uint64_t p) -> bool {
     if (snap_on && snaps.due()) {
-      const uint64_t done = paths_done(p + 1);
+      const uint64_t done = done_all;
       const uint64_t npx = recs[0].P.pixels;
       e = snaps.take(film_sum, jobs[0].cam.width, jobs[0].cam.height, (double)done / (double)npx,
                      [&](size_t q) { return (double)(done / npx + (q < done % npx ? 1 : 0)); }, s);
@@ -974,24 +1031,59 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     }
     return budget_spent(p);
   };
+  // candidates, each timed over two passes (ms per path); first the launch shapes at the
+  // given pass size, then the pass sizes with the best shape
   if (!cands.empty()) {
-    float best_t = INFINITY;
     Event t0, t1;
     if ((e = t0.create()) != cudaSuccess || (e = t1.create()) != cudaSuccess) return e;
-    for (const PtShape& sh : cands) {
+    auto time_passes = [&](const PtShape& sh, double& ms_per_path) -> cudaError_t {
       cudaEventRecord(t0, s);
-      if ((e = enqueue_pass_shape(W, sh, sms, s)) != cudaSuccess) return e;
+      uint64_t n = 0;
+      for (int r = 0; r < 2; r++) {
+        cudaError_t err = enqueue_pass_shape(W, sh, sms, s);
+        if (err != cudaSuccess) return err;
+        n += account();
+        pass++;
+      }
       cudaEventRecord(t1, s);
-      if ((e = cudaEventSynchronize(t1)) != cudaSuccess) return e;
+      cudaError_t err = cudaEventSynchronize(t1);
+      if (err != cudaSuccess) return err;
       float ms = 0;
       cudaEventElapsedTime(&ms, t0, t1);
-      if (ms < best_t) best_t = ms, best = sh;
-      pass++;
+      ms_per_path = n ? ms / (double)n : INFINITY;
+      return cudaSuccess;
+    };
+    double best_t = INFINITY;
+    for (const PtShape& sh : cands) {
+      double tp;
+      if ((e = time_passes(sh, tp)) != cudaSuccess) return e;
+      if (tp < best_t) best_t = tp, best = sh;
+    }
+    // pass sizes, when their passes fit in what is left of the render
+    uint64_t need = 0;
+    for (uint32_t sz : sizes) need += 2 * qsum(quotas(sz, false));
+    if (!sizes.empty() && done_all + need <= total) {
+      best_t = INFINITY;
+      PtShape bs = best;
+      std::vector<uint32_t> best_q = q_now;
+      for (uint32_t sz : sizes) {
+        const std::vector<uint32_t> q = quotas(sz, false);
+        if ((e = set_quota(q)) != cudaSuccess) return e;
+        PtShape sh = best;
+        sh.paths_per_pass = (uint32_t)qsum(q);
+        double tp;
+        if ((e = time_passes(sh, tp)) != cudaSuccess) return e;
+        if (tp < best_t) best_t = tp, bs = sh, best_q = q;
+      }
+      best = bs;
+      if ((e = set_quota(best_q)) != cudaSuccess) return e;
     }
   }
   if (chosen) *chosen = best;
 
-  if (run.use_graph && npasses - pass >= 2) {
+  // the remaining passes: one captured pass replayed, or enqueued one by one
+  auto left = [&]() { return done_all < total; };
+  if (run.use_graph && left()) {
     Graph graph;
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
     cudaError_t eq = enqueue_pass_shape(W, best, sms, s);
@@ -999,14 +1091,16 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     if (eq != cudaSuccess) return eq;
     if (e != cudaSuccess) return e;
     if ((e = cudaGraphInstantiate(&graph.x, graph.g, 0)) != cudaSuccess) return e;
-    while (pass < npasses && e == cudaSuccess) {
+    while (left() && e == cudaSuccess) {
       e = cudaGraphLaunch(graph.x, s);
+      account();
       if (e == cudaSuccess && after_pass(pass++)) break;
     }
     if (e != cudaSuccess) return e;
   } else {
-    while (pass < npasses) {
+    while (left()) {
       if ((e = enqueue_pass_shape(W, best, sms, s)) != cudaSuccess) return e;
+      account();
       if (after_pass(pass++)) break;
     }
     if (e != cudaSuccess) return e;
@@ -1022,7 +1116,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     cudaMemcpy(h, W.ctr, sizeof h, cudaMemcpyDeviceToHost);
     stats->extension_rays = h[0];
     stats->shadow_rays = h[1];
-    stats->paths = paths_done(pass);
+    stats->paths = done_all;
     stats->ms = ms;
   }
   return cudaSuccess;

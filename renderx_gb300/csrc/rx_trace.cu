@@ -65,8 +65,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
                                                            int32_t* __restrict__ out_tid,
                                                            float* __restrict__ out_dist,
                                                            uint32_t* __restrict__ hit_leaf,
-                                                           int32_t* __restrict__ slot_tid,
-                                                           float* __restrict__ slot_dist,
+                                                           int4* __restrict__ slot_rec,
                                                            unsigned long long* __restrict__ counters) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int DONE = INT_MIN;
@@ -234,10 +233,9 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
     }
 
     if (active && cur == DONE) {
-      if (slot_tid) {  // by binned slot (coalesced); the check scatters them to ray order
-        slot_tid[slot] = best.hit ? best.tid : -1;
-        slot_dist[slot] = best.hit ? best.t : -1.0f;
-        hit_leaf[slot] = best.hit ? best.leaf : kNoLeaf;
+      if (slot_rec) {  // one 16-byte record by binned slot; the check scatters it to ray order
+        slot_rec[slot] = make_int4(best.hit ? best.tid : -1, __float_as_int(best.hit ? best.t : -1.0f),
+                                   (int)(best.hit ? best.leaf : kNoLeaf), 0);
       } else {
         out_tid[ray] = best.hit ? best.tid : -1;
         out_dist[ray] = best.hit ? best.t : -1.0f;
@@ -254,8 +252,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
 __global__ void __launch_bounds__(128) k_check_visible_thread(DevAccel A, const rx_ray* __restrict__ rays,
                                                               uint32_t n, const uint32_t* __restrict__ order,
                                                               const uint32_t* __restrict__ hit_leaf,
-                                                              const int32_t* __restrict__ slot_tid,
-                                                              const float* __restrict__ slot_dist,
+                                                              const int4* __restrict__ slot_rec,
                                                               int32_t* __restrict__ out_tid,
                                                               float* __restrict__ out_dist,
                                                               uint32_t* __restrict__ eager_queue,
@@ -270,12 +267,16 @@ __global__ void __launch_bounds__(128) k_check_visible_thread(DevAccel A, const 
     uint32_t i = j < n && order ? __ldg(&order[j]) : j;  // binned order: a warp checks nearby leaves
     bool fail = false;
     if (j < n) {
-      // slot_tid: the walk left its answers by binned slot; this is where they reach ray
-      // order (a rejected winner is re-walked after, overwriting them)
-      uint32_t leaf = __ldg(&hit_leaf[slot_tid ? j : i]);
-      if (slot_tid) {
-        out_tid[i] = __ldg(&slot_tid[j]);
-        out_dist[i] = __ldg(&slot_dist[j]);
+      // slot_rec: the walk left its answer by binned slot; this is where it reaches ray
+      // order (a rejected winner is re-walked after, overwriting it)
+      uint32_t leaf;
+      if (slot_rec) {
+        const int4 rec = __ldg(slot_rec + j);
+        out_tid[i] = rec.x;
+        out_dist[i] = __int_as_float(rec.y);
+        leaf = (uint32_t)rec.z;
+      } else {
+        leaf = __ldg(&hit_leaf[i]);
       }
       if (leaf != kNoLeaf) {
         const float4* rp = reinterpret_cast<const float4*>(rays + i);
@@ -339,8 +340,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
                                                           int32_t* __restrict__ out_tid,
                                                           float* __restrict__ out_dist,
                                                           uint32_t* __restrict__ hit_leaf,
-                                                           int32_t* __restrict__ slot_tid,
-                                                           float* __restrict__ slot_dist,
+                                                           int4* __restrict__ slot_rec,
                                                           unsigned long long* __restrict__ counters) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int DONE = INT_MIN;
@@ -472,10 +472,9 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
     }
 
     if (active && cur == DONE) {
-      if (slot_tid) {  // by binned slot (coalesced); the check scatters them to ray order
-        slot_tid[slot] = best.hit ? best.tid : -1;
-        slot_dist[slot] = best.hit ? best.t : -1.0f;
-        hit_leaf[slot] = best.hit ? best.leaf : kNoLeaf;
+      if (slot_rec) {  // one 16-byte record by binned slot; the check scatters it to ray order
+        slot_rec[slot] = make_int4(best.hit ? best.tid : -1, __float_as_int(best.hit ? best.t : -1.0f),
+                                   (int)(best.hit ? best.leaf : kNoLeaf), 0);
       } else {
         out_tid[ray] = best.hit ? best.tid : -1;
         out_dist[ray] = best.hit ? best.t : -1.0f;
@@ -586,21 +585,18 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
   uint32_t* eager = queue + n;  // then up to n queued rays
   if (cfg.variant != 0) cudaMemsetAsync(counters + 4, 0, sizeof(unsigned long long), s);  // batch cursor
   const uint32_t* order = nullptr;
-  int32_t* slot_tid = nullptr;
-  float* slot_dist = nullptr;
+  int4* slot_rec = nullptr;
   if (bin && cfg.variant != 0 && cfg.bin_min && n >= cfg.bin_min) {
     uint32_t* keys = queue + 2 * (size_t)n;
     uint32_t* perm = queue + 3 * (size_t)n;
-    uint32_t* hist = queue + 5 * (size_t)n;
+    uint32_t* hist = queue + 8 * (size_t)n;
     cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), s);
     k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist);
     scan_bins(hist, hist + kRayBins, s);
     k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, nullptr, hist, perm);
     order = perm;
-    if (cfg.check_thread) {  // the walk writes by slot: ids into the keys (no longer needed), distances after perm
-      slot_tid = reinterpret_cast<int32_t*>(keys);
-      slot_dist = reinterpret_cast<float*>(queue + 4 * (size_t)n);
-    }
+    if (cfg.check_thread)  // the walk writes its answers by slot: 16-byte records after perm
+      slot_rec = reinterpret_cast<int4*>(queue + 4 * (size_t)n);
   }
   if (ev) cudaEventRecord(ev[0], s);
   if (cfg.variant == 0) {
@@ -613,22 +609,22 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     const bool shallow = cfg.walk_stack != 64 && A.bvh_depth < 32;
     const bool walk4 = A.bvh4 && 3 * A.bvh4_depth + 1 <= 64;  // the 4-wide walk's stack bound
     if (cfg.variant == 4 && walk4)
-      k_trace_persistent4<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
+      k_trace_persistent4<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
     else if (cfg.variant == 3 && walk4)
-      k_trace_persistent4<0><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
+      k_trace_persistent4<0><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
     else if (cfg.variant == 1 && shallow)
-      k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
+      k_trace_persistent<false, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
     else if (cfg.variant == 1)
-      k_trace_persistent<false, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
+      k_trace_persistent<false, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
     else if (shallow)
-      k_trace_persistent<true, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
+      k_trace_persistent<true, 32><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
     else
-      k_trace_persistent<true, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_tid, slot_dist, counters);
+      k_trace_persistent<true, kStack><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
   }
   if (ev) cudaEventRecord(ev[1], s);
   if (cfg.check_thread)
-    k_check_visible_thread<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, order, hit_leaf, slot_tid, slot_dist, tid, dist,
-                                                        eager, counters);
+    k_check_visible_thread<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, order, hit_leaf, slot_rec, tid, dist, eager,
+                                                        counters);
   else
     k_check_visible<<<cfg.sms * 16, 128, 0, s>>>(A, rays, n, hit_leaf, eager, counters);
   if (ev) cudaEventRecord(ev[2], s);

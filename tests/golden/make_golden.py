@@ -178,8 +178,14 @@ def make_vcm_goldens(ref_vcm: str):
         imgs = np.array(imgs)
         mean = imgs.mean(axis=0)
         stderr = imgs.std(axis=0, ddof=1) / np.sqrt(runs)
+        # standard errors of 4x4-block means from the runs themselves (merging correlates
+        # neighbouring pixels, so they are not the per-pixel errors combined)
+        h, w, _ = mean.shape
+        blocks = imgs.reshape(runs, h // 4, 4, w // 4, 4, 3).mean(axis=(2, 4))
+        block_stderr = blocks.std(axis=0, ddof=1) / np.sqrt(runs)
         path = os.path.join(HERE, f"render_{case}.npz")
         np.savez_compressed(path, mean=mean.astype(np.float32), stderr=stderr.astype(np.float32),
+                            block_stderr=block_stderr.astype(np.float32),
                             runs=np.int64(runs), iterations=np.int64(iters), max_depth=np.int64(depth),
                             radius=np.float64(r0), alpha=np.float64(alpha), scene=np.array(scene_fn),
                             seconds=np.float64(secs), geometry_sha256=np.array(geometry_hash(f["verts"], f["tris"])))

@@ -32,7 +32,7 @@ def test_batch_equals_single_scene_renders(use_graph, autotune):
         singles = [c.render_pt(sc.camera, o["spp"], max_depth=o["max_depth"], nee=o["nee"], rr_mode=o["rr_mode"],
                                seed=o["seed"], paths_per_pass=1 << 13)[0] for c, (sc, o) in zip(ctxs, items)]
         films, st = ctxs[0].render_pt_batch([(c, sc.camera, o) for c, (sc, o) in zip(ctxs, items)],
-                                            paths_per_pass=1 << 13, use_graph=use_graph, autotune=autotune)
+                                            paths_per_pass=1 << 12, use_graph=use_graph, autotune=autotune)
     finally:
         for c in ctxs:
             c.close()
@@ -42,6 +42,37 @@ def test_batch_equals_single_scene_renders(use_graph, autotune):
         assert a.mean() > 0
     assert st["paths"] == sum(sc.camera.width * sc.camera.height * o["spp"] for sc, o in items)
     assert st["blocks_per_sm"] in (4, 8, 16) and st["stack"] in (4, 5, 32, 64)
+
+
+def test_autotuned_batch_picks_a_pass_size_and_equals_single_scene_renders():
+    """Autotuning times the launch shapes and then the pass sizes 2^20..2^23 (two passes
+    each, on interleaved passes that hold the same mix of every scene); the chosen size
+    is reported, and every image still equals its single-scene render up to the FP64
+    summation order (the random numbers depend on each scene's own path indices only)."""
+    items = [(scenes.cornell_box(128, 128), dict(spp=512, max_depth=8, rr_mode=1, seed=31)),
+             (scenes.material_spheres(128, 128), dict(spp=512, max_depth=8, rr_mode=1, seed=32)),
+             (scenes.medium_scene(128, 128), dict(spp=512, max_depth=8, rr_mode=1, seed=33)),
+             (scenes.cornell_box(128, 128), dict(spp=512, max_depth=8, rr_mode=0, nee=True, seed=34))]
+    ctxs = []
+    try:
+        for sc, _ in items:
+            c = rx.Context(0)
+            c.set_scene(sc)
+            c.build_accel()
+            ctxs.append(c)
+        singles = [c.render_pt(sc.camera, o["spp"], max_depth=o["max_depth"], nee=o.get("nee", False),
+                               rr_mode=o["rr_mode"], seed=o["seed"])[0] for c, (sc, o) in zip(ctxs, items)]
+        films, st = ctxs[0].render_pt_batch([(c, sc.camera, o) for c, (sc, o) in zip(ctxs, items)],
+                                            paths_per_pass=1 << 18, autotune=True)
+    finally:
+        for c in ctxs:
+            c.close()
+    total = sum(sc.camera.width * sc.camera.height * o["spp"] for sc, o in items)
+    assert st["paths"] == total
+    assert st["paths_per_pass"] in [sum(-(-128 * 128 * 512 * sz // total) for _ in items)
+                                    for sz in (1 << 20, 1 << 21, 1 << 22)], st["paths_per_pass"]
+    for a, b in zip(films, singles):
+        assert np.allclose(a, b, rtol=1e-9, atol=1e-12), np.abs(a - b).max()
 
 
 def test_batch_rejects_bad_input():

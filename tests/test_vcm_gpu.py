@@ -63,13 +63,15 @@ def _check_against_golden(z, imgs):
     bad = np.abs(mean - ref) > 3 * sig + 1e-4
     assert bad.mean() <= 0.02, f"{bad.mean():.4f} of channels beyond 3 sigma (max z {zz.max():.1f})"
     assert (zz > 8).sum() == 0, f"channels beyond 8 sigma: {(zz > 8).sum()}"
-    # 4x4 blocks: the GPU side's block error from the runs themselves (merging correlates
-    # neighbouring pixels, so a block error built from per-pixel errors as if they were
-    # independent would be too small); the golden's from its per-pixel errors
+    # 4x4 blocks: block errors from the runs themselves on both sides where the golden
+    # stores them (merging correlates neighbouring pixels, so a block error built from
+    # per-pixel errors as if they were independent would be too small)
     h, w, _ = mean.shape
     per_run = imgs.reshape(runs, h // 4, 4, w // 4, 4, 3).mean(axis=(2, 4))
     bm, bs = per_run.mean(axis=0), per_run.std(axis=0, ddof=1) / np.sqrt(runs)
     rm, rs = _blocks(ref, rse)
+    if "block_stderr" in z:
+        rs = z["block_stderr"].astype(np.float64)
     bsig = np.sqrt(bs ** 2 + rs ** 2)
     bz = np.abs(bm - rm) / (bsig + 1e-12)
     bfrac = (np.abs(bm - rm) > 3 * bsig + 1e-4).mean()
