@@ -151,9 +151,16 @@ class Oracle:
     def noise(self) -> float:
         return float(np.mean(self.var / (self.mean ** 2 + 1e-2)))
 
-    def relmse(self, img) -> dict:
+    def relmse(self, img, spp=None) -> dict:
+        """relMSE of `img` against the oracle. spp: `img` is the same estimator (plain
+        PathTracer, same depth and roulette) at spp samples, so an unbiased image is
+        expected at the noise of both: the oracle's per-sample variance over spp, plus
+        the oracle's own (`relmse_expected_if_unbiased`)."""
         raw = _relmse(img, self.mean)
-        return {"relmse": raw, "relmse_minus_oracle_noise": raw - self.noise()}
+        out = {"relmse": raw, "relmse_minus_oracle_noise": raw - self.noise()}
+        if spp:
+            out["relmse_expected_if_unbiased"] = self.noise() * (self.spp / spp + 1.0)
+        return out
 
 
 def section_c0(peak):
@@ -183,12 +190,13 @@ def section_c0(peak):
     return {"workload": f"PathTracer, Cornell box (36 triangles) {sc.camera.width}x{sc.camera.height} x {spp} spp, "
                         f"depth {depth}, RR from depth 3", "ms": ms, "mrays_per_s": rays / ms / 1e3,
             "samples_per_s": st["paths"] / ms * 1e3, "extension_rays": st["extension_rays"],
-            "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(film).items()},
+            "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(film, spp).items()},
             "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": peak, "unit": "GB/s",
                          "frac": alg / ms / 1e6 / peak},
             "cpu_baseline": {"value": crays / cs / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "samples_per_s": sc.camera.width * sc.camera.height * spp / cs, "seconds": cs,
-                             "relmse_vs_oracle": orc.relmse(cimg)["relmse"],
+                             **{k + "_vs_oracle": v for k, v in orc.relmse(cimg, spp).items()
+                                if k != "relmse_minus_oracle_noise"},
                              "sample": "the whole frame (256x256 x 16 spp), oracle restatement of PathTracer "
                                        "over the reference's KDTree"}}
 
@@ -209,7 +217,7 @@ def section_pt(ctx, sc, peak, res: int = 1024, spp: int = 64, cpu_tree=None):
     orc = Oracle(ctx, cam, 8 * spp, depth, 1, seed=5)
     out = {"workload": f"PathTracer {cam.width}x{cam.height} x {spp} spp, depth {depth}, "
                        "4,096,036 triangles", "ms": st["ms"], "mrays_per_s": rays / s / 1e6,
-           "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(film).items()},
+           "oracle": orc.desc, **{k + "_vs_oracle": v for k, v in orc.relmse(film, spp).items()},
            "samples_per_s": st["paths"] / s, "extension_rays": st["extension_rays"],
            "shadow_rays": st["shadow_rays"], "image_mean": [float(x) for x in film.mean(axis=(0, 1))],
            "roofline": {"bound": "hbm", "achieved": alg / s / 1e9, "peak": peak, "unit": "GB/s",

@@ -139,8 +139,10 @@ typedef struct rx_batch_options {
   uint32_t use_graph;      /* 1: capture one pass as a CUDA graph and replay it */
   uint32_t autotune;       /* 1: time candidates on the first passes, two passes each (their
                               samples count): the launch shapes at paths_per_pass, then the
-                              pass sizes 2^20..2^23 with the best shape. Autotuned and guided
-                              batches take an equal share of every item in each pass. */
+                              pass sizes 2^20..2^23 with the best shape. Guided batches take an
+                              equal share of every item in each pass; autotuned ones do so in
+                              the tuning passes only, then take the items one after another
+                              (a pass then touches one or two scenes' trees). */
   uint32_t chosen_paths_per_pass;  /* out: paths per pass of the remaining passes */
   int32_t chosen_blocks_per_sm;  /* out: extend / shade blocks per SM used */
   int32_t chosen_stack;          /* out: walk used: 4 = 4-wide BVH, 5 = 4-wide BVH with a
@@ -228,7 +230,8 @@ rx_status rx_scene_set_objects(rx_context* ctx, const rx_object* objs, uint32_t 
  * reference-order tree (tie ranks, visibility boxes) and the device BVH, uploads both. */
 rx_status rx_build_accel(rx_context* ctx, const rx_build_options* opts);
 /* Tree statistics: [0] BVH nodes, [1] BVH depth, [2] reference nodes,
- * [3] reference depth, [4] triangles, [5] reference leaves. */
+ * [3] reference depth, [4] triangles, [5] reference leaves, [6] 4-wide BVH depth,
+ * [7] 8-wide BVH depth. */
 rx_status rx_accel_stats(rx_context* ctx, int64_t out[8]);
 /* KDTree::serializeForGPU (reference include/KDTree.h:56, src/KDTree.cpp:346-382) of
  * the reference-order tree this library builds, host only (no device, no context).
@@ -366,9 +369,11 @@ rx_status rx_render_pm(rx_context* ctx, const rx_camera* cam, const rx_pm_option
 /* Closest-hit launch shape (what the autotuner picks): variant 0 = one thread per
  * ray, 1 = persistent warps that refill finished lanes, 2 = the same with speculative
  * leaf postponing, 3 = persistent over the 4-wide BVH, 4 = 3 with the first 16 entries
- * of each walk's stack in shared memory (the default); 3 and 4 fall back to 1 when the
- * 4-wide tree is too deep for their stack. Blocks of 128 threads, blocks_per_sm per
- * SM. No reference counterpart (launch tuning). */
+ * of each walk's stack in shared memory (the default), 5 = 4 over the 8-wide BVH
+ * (256-byte nodes, half the levels). 4 and 5 take the other wide tree when theirs is
+ * too deep for its stack (4-wide: 21 levels, 8-wide: 11); 3 to 5 fall back to 2 when no
+ * wide tree fits. Blocks of 128 threads, blocks_per_sm per SM. No reference
+ * counterpart (launch tuning). */
 rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_per_sm);
 /* Closest-hit options (no reference counterpart): check_mode = how each walk's winner
  * is checked for reference visibility, 1 = one thread per ray (default), 0 = one warp

@@ -170,7 +170,8 @@ class Context:
         out = np.zeros(8, np.int64)
         self._ck(self._L.rx_accel_stats(self.h, _capi.ptr(out)))
         return dict(bvh_nodes=int(out[0]), bvh_depth=int(out[1]), ref_nodes=int(out[2]), ref_depth=int(out[3]),
-                    triangles=int(out[4]), ref_leaves=int(out[5]))
+                    triangles=int(out[4]), ref_leaves=int(out[5]), bvh4_depth=int(out[6]),
+                    bvh8_depth=int(out[7]))
 
     # -- closest hit -----------------------------------------------------------------
     def trace_closest(self, origins, dirs):

@@ -66,5 +66,8 @@ struct Bvh4 {
   size_t num_nodes() const { return data.size() / 32; }
 };
 void collapse_bvh4(const Bvh& b2, Bvh4& out);
+// The same with up to eight children per node: 16 float4 = 256 B per node (lo.x, hi.x,
+// lo.y, hi.y, lo.z, hi.z of the eight children, then refs and leaf counts).
+void collapse_bvh8(const Bvh& b2, Bvh4& out);
 
 }  // namespace rx

@@ -534,11 +534,15 @@ void children_of(const BvhNodeHost& n, Child4 (&c)[2]) {
   c[1].ref = n.child[1];
   c[1].count = n.count[1];
 }
+// One node of a W-wide BVH from binary node n2: its children opened largest surface area
+// first until W of them; node layout: per axis the W lower then the W upper child bounds,
+// then W refs and W leaf counts (8 W floats).
+template <int W>
 int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
   Child4 two[2];
   children_of(b2.nodes[n2], two);
   std::vector<Child4> kids = {two[0], two[1]};
-  while (kids.size() < 4) {
+  while (kids.size() < (size_t)W) {
     int best = -1;
     float area = -1.0f;
     for (size_t i = 0; i < kids.size(); i++)
@@ -549,27 +553,28 @@ int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
     kids[best] = sub[0];
     kids.push_back(sub[1]);
   }
-  const int32_t me = (int32_t)out.num_nodes();
-  out.data.resize(out.data.size() + 32, 0.0f);
+  constexpr int kF = 8 * W;  // floats per node
+  const int32_t me = (int32_t)(out.data.size() / kF);
+  out.data.resize(out.data.size() + kF, 0.0f);
   out.max_depth = std::max(out.max_depth, depth);
-  int32_t refs[4], counts[4];
-  for (int j = 0; j < 4; j++) {
+  int32_t refs[W], counts[W];
+  for (int j = 0; j < W; j++) {
     refs[j] = kBvh4Empty;
     counts[j] = 0;
   }
   for (size_t j = 0; j < kids.size(); j++) {
-    refs[j] = kids[j].ref >= 0 ? collapse(b2, kids[j].ref, depth + 1, out) : kids[j].ref;
+    refs[j] = kids[j].ref >= 0 ? collapse<W>(b2, kids[j].ref, depth + 1, out) : kids[j].ref;
     counts[j] = kids[j].count;
   }
-  float* f = out.data.data() + 32 * (size_t)me;  // after the recursion: data may have moved
-  for (int j = 0; j < 4; j++) {
+  float* f = out.data.data() + kF * (size_t)me;  // after the recursion: data may have moved
+  for (int j = 0; j < W; j++) {
     bool has = j < (int)kids.size();
     for (int k = 0; k < 3; k++) {
-      f[8 * k + j] = has ? kids[j].lo[k] : 0.0f;
-      f[8 * k + 4 + j] = has ? kids[j].hi[k] : 0.0f;
+      f[2 * W * k + j] = has ? kids[j].lo[k] : 0.0f;
+      f[2 * W * k + W + j] = has ? kids[j].hi[k] : 0.0f;
     }
-    std::memcpy(&f[24 + j], &refs[j], 4);
-    std::memcpy(&f[28 + j], &counts[j], 4);
+    std::memcpy(&f[6 * W + j], &refs[j], 4);
+    std::memcpy(&f[7 * W + j], &counts[j], 4);
   }
   return me;
 }
@@ -578,7 +583,13 @@ int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
 void collapse_bvh4(const Bvh& b2, Bvh4& out) {
   out.data.clear();
   out.max_depth = 0;
-  if (!b2.nodes.empty()) collapse(b2, 0, 0, out);
+  if (!b2.nodes.empty()) collapse<4>(b2, 0, 0, out);
+}
+
+void collapse_bvh8(const Bvh& b2, Bvh4& out) {
+  out.data.clear();
+  out.max_depth = 0;
+  if (!b2.nodes.empty()) collapse<8>(b2, 0, 0, out);
 }
 
 }  // namespace rx

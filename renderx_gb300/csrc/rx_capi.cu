@@ -56,7 +56,7 @@ void rx_destroy(rx_context* c) {
   {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf* b : {&c->d_bvh, &c->d_bvh4, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
+    for (DevBuf* b : {&c->d_bvh, &c->d_bvh4, &c->d_bvh8, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
                       &c->d_anc_range, &c->d_anc_nodes, &c->d_anc_box, &c->d_slot_n, &c->d_tri_v, &c->d_tri_n, &c->d_tri_obj,
                       &c->d_objects, &c->d_light_cdf, &c->d_light_tri,
                       &c->d_counters, &c->d_queue})
@@ -197,6 +197,9 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   rx::collapse_bvh4(c->bvh, c->bvh4);
   if ((s = upload(c, c->d_bvh4, c->bvh4.data.data(), c->bvh4.data.size() * sizeof(float), "upload BVH4")) != RX_OK)
     return s;
+  rx::collapse_bvh8(c->bvh, c->bvh8);
+  if ((s = upload(c, c->d_bvh8, c->bvh8.data.data(), c->bvh8.data.size() * sizeof(float), "upload BVH8")) != RX_OK)
+    return s;
   if ((s = upload(c, c->d_tris, slots.data(), slots.size() * sizeof(float4), "upload triangles")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref, refn.data(), refn.size() * sizeof(float4), "upload reference nodes")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref_leaf_node, leaf_node.data(), leaf_node.size() * 4, "upload leaf map")) != RX_OK) return s;
@@ -228,6 +231,8 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   A.bvh_depth = (uint32_t)c->bvh.max_depth;
   A.bvh4 = c->d_bvh4.as<float4>();
   A.bvh4_depth = (uint32_t)c->bvh4.max_depth;
+  A.bvh8 = c->d_bvh8.as<float4>();
+  A.bvh8_depth = (uint32_t)c->bvh8.max_depth;
   for (int k = 0; k < 3; k++) {
     const rx::BvhNodeHost& r = c->bvh.nodes[0];
     A.lo[k] = std::min(r.c0lo[k], r.c1lo[k]);
@@ -528,6 +533,8 @@ rx_status rx_accel_stats(rx_context* c, int64_t out[8]) {
   out[3] = c->ref.max_depth;
   out[4] = (int64_t)(c->tris.size() / 3);
   out[5] = (int64_t)c->ref.leaf_node.size();
+  out[6] = c->bvh4.max_depth;
+  out[7] = c->bvh8.max_depth;
   return RX_OK;
 }
 
@@ -666,8 +673,8 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
 
 rx_status rx_trace_set_config(rx_context* c, int32_t variant, int32_t blocks_per_sm) {
   if (!c) return RX_ERR_INVALID;
-  if (variant < 0 || variant > 4 || blocks_per_sm < 1 || blocks_per_sm > 32)
-    return c->fail(RX_ERR_INVALID, "variant must be 0..4 and blocks_per_sm 1..32");
+  if (variant < 0 || variant > 5 || blocks_per_sm < 1 || blocks_per_sm > 32)
+    return c->fail(RX_ERR_INVALID, "variant must be 0..5 and blocks_per_sm 1..32");
   c->trace_cfg.variant = variant;
   c->trace_cfg.blocks_per_sm = blocks_per_sm;
   return RX_OK;

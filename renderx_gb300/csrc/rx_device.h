@@ -33,6 +33,8 @@ struct DevAccel {
   uint32_t bvh_depth;              // deepest BVH level (the walk's stack must exceed it)
   const float4* bvh4;              // 4-wide BVH, 8 float4 per node (rx_accel.h), or null
   uint32_t bvh4_depth;
+  const float4* bvh8;              // 8-wide BVH, 16 float4 per node (rx_accel.h), or null
+  uint32_t bvh8_depth;
 };
 
 }  // namespace rx

@@ -154,8 +154,8 @@ struct rx_context {
   rx::DevAccel accel{};
   rx::TraceConfig trace_cfg;
   bool accel_ready = false;
-  rx::Bvh4 bvh4;
-  rx::DevBuf d_bvh4;
+  rx::Bvh4 bvh4, bvh8;
+  rx::DevBuf d_bvh4, d_bvh8;
   rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes, d_anc_box;
   rx::DevScene scene{};
   bool scene_ready = false;

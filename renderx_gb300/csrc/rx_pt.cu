@@ -38,6 +38,8 @@ struct SceneRec {
   DevScene S;
   PtParams P;
   uint64_t path_begin;  // concatenated passes: first global path index of the scene
+  uint64_t pid_first;   // concatenated passes: the scene's first path id (0, or the paths
+                        // that interleaved tuning passes took before)
   uint64_t film_base;   // first pixel of the scene in the shared film
   uint64_t paths;       // pixels x spp
   int32_t net;          // guiding network of the scene (index into the render's networks), -1: none
@@ -155,7 +157,7 @@ __global__ void k_generate(const SceneRec* R, int nr, PassState* ps, Layout L, P
     } else {
       uint64_t g = base + i;
       sc = scene_of(R, nr, g);
-      pid = g - R[sc].path_begin;
+      pid = R[sc].pid_first + (g - R[sc].path_begin);
     }
     const PtParams& P = R[sc].P;
     uint32_t pixel = (uint32_t)(pid % P.pixels);
@@ -808,6 +810,7 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     recs[k].S = jobs[k].ctx->scene;
     recs[k].P = make_pt_params(jobs[k].ctx, jobs[k].cam, jobs[k].opt);
     recs[k].path_begin = total;
+    recs[k].pid_first = 0;
     recs[k].film_base = jobs[k].film_base;
     recs[k].paths = (uint64_t)recs[k].P.pixels * jobs[k].opt.spp;
     recs[k].net = -1;
@@ -834,8 +837,9 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   if (per_pass == 0) return cudaSuccess;
   const uint64_t npasses = (total + per_pass - 1) / per_pass;
   // interleaved passes for guided renders (one schedule for all networks) and autotuned
-  // ones (candidates timed on passes of the same mix)
-  const bool inter = guided || run.autotune;
+  // ones (candidates timed on passes of the same mix; the passes after the tuning go
+  // back to the concatenated layout)
+  bool inter = guided || run.autotune;
   // per-scene quotas of a pass of about `size` paths: guided and untuned renders divide
   // every scene over the same number of passes; the queue-size candidates take their
   // share of `size` in proportion to the scenes' paths
@@ -1080,6 +1084,27 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     }
   }
   if (chosen) *chosen = best;
+  // Autotuned, unguided: the remaining passes take the scenes one after another again.
+  // An interleaved pass touches every scene's tree and triangles (for a large batch far
+  // more than L2 holds); a concatenated pass touches one or two scenes. Each scene
+  // continues after the paths the tuning passes took from it.
+  PassState ps_rest{};
+  if (inter && !guided) {
+    uint64_t begin = 0;
+    for (int k = 0; k < nj; k++) {
+      recs[k].pid_first = taken[k];
+      recs[k].path_begin = begin;
+      begin += recs[k].paths - taken[k];
+    }
+    per_pass = std::min<uint32_t>(best.paths_per_pass, slots);  // the path arrays hold `slots`
+    ps_rest = PassState{0, begin, per_pass, 0, (uint32_t)pass, 0u};
+    if ((e = cudaMemcpyAsync(const_cast<SceneRec*>(W.R), recs.data(), sizeof(SceneRec) * nj, cudaMemcpyHostToDevice,
+                             s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(W.ps, &ps_rest, sizeof ps_rest, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return e;
+    W.L = Layout{};
+    inter = false;
+  }
 
   // the remaining passes: one captured pass replayed, or enqueued one by one
   auto left = [&]() { return done_all < total; };

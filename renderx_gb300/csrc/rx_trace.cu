@@ -54,22 +54,20 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
   if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
 }
 
-// The persistent walk over the 4-wide BVH: one node visit tests four child boxes
-// (128-byte node, one cache line), visits the nearest hit child next and stacks the
-// others far to near; pruning, leaf tests and refills as k_trace_persistent.
-// kShort > 0: the first kShort entries of each thread's stack sit in shared memory
-// (one column per thread, conflict-free), deeper entries in local memory.
-template <int kShort>
-__global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
-                                                           const uint32_t* __restrict__ order,
-                                                           int32_t* __restrict__ out_tid,
-                                                           float* __restrict__ out_dist,
-                                                           uint32_t* __restrict__ hit_leaf,
-                                                           int4* __restrict__ slot_rec,
-                                                           unsigned long long* __restrict__ counters) {
+// The persistent walk over a W-wide BVH (W = 4: 128-byte nodes, one cache line; W = 8:
+// 256-byte nodes, half the levels): one node visit tests W child boxes, visits the
+// nearest hit child next and stacks the others far to near; pruning, leaf tests and
+// refills as k_trace_persistent. kShort > 0: the first kShort entries of each thread's
+// stack sit in shared memory (one column per thread, conflict-free), deeper entries in
+// local memory. kStack bounds the stack: (W - 1) entries per level below the root.
+template <int W, int kShort, int kStack>
+__device__ __forceinline__ void walk_wide(const DevAccel& A, const float4* __restrict__ nodes,
+                                          const rx_ray* __restrict__ rays, uint32_t n,
+                                          const uint32_t* __restrict__ order, int32_t* __restrict__ out_tid,
+                                          float* __restrict__ out_dist, uint32_t* __restrict__ hit_leaf,
+                                          int4* __restrict__ slot_rec, unsigned long long* __restrict__ counters) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int DONE = INT_MIN;
-  constexpr int kStack4 = 64;  // at most 3 entries per level of a BVH4 shallower than 21 levels
   constexpr int kShortN = kShort > 0 ? kShort : 1;
   __shared__ int s_ref[kShortN][128];
   __shared__ float s_tn[kShortN][128];
@@ -80,8 +78,8 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
   F3 o{}, d{}, inv{}, ood{};
   float tlimit = INFINITY;
   HitResult best{-1, -1.0f, 0u, 0u, false};
-  int stack_ref[kStack4 - kShort];
-  float stack_tn[kStack4 - kShort];
+  int stack_ref[kStack - kShort];
+  float stack_tn[kStack - kShort];
   int sp = 0, cur = DONE, cnt = 0;
 
   auto pop = [&]() {
@@ -150,21 +148,32 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
         continue;
       }
       {
-        const float4* np = A.bvh4 + 8 * (size_t)cur;
-        float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-        float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
-        int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
-        const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-        const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-        const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
-        int r[4] = {cr.x, cr.y, cr.z, cr.w}, c[4] = {cc.x, cc.y, cc.z, cc.w};
-        float tn[4];
+        const float4* np = nodes + 2 * W * (size_t)cur;
+        float lo[3][W], hi[3][W];
+        int r[W], c[W];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+#pragma unroll
+          for (int q = 0; q < W / 4; q++) {
+            float4 l = __ldg(np + 2 * (W / 4) * k + q), h = __ldg(np + 2 * (W / 4) * k + W / 4 + q);
+            lo[k][4 * q] = l.x, lo[k][4 * q + 1] = l.y, lo[k][4 * q + 2] = l.z, lo[k][4 * q + 3] = l.w;
+            hi[k][4 * q] = h.x, hi[k][4 * q + 1] = h.y, hi[k][4 * q + 2] = h.z, hi[k][4 * q + 3] = h.w;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < W / 4; q++) {
+          int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6 * (W / 4) + q));
+          int4 cc = __ldg(reinterpret_cast<const int4*>(np + 7 * (W / 4) + q));
+          r[4 * q] = cr.x, r[4 * q + 1] = cr.y, r[4 * q + 2] = cr.z, r[4 * q + 3] = cr.w;
+          c[4 * q] = cc.x, c[4 * q + 1] = cc.y, c[4 * q + 2] = cc.z, c[4 * q + 3] = cc.w;
+        }
+        float tn[W];
         int nh = 0;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          float a0 = fmaf(lxa[j], inv.x, -ood.x), b0 = fmaf(hxa[j], inv.x, -ood.x);
-          float a1 = fmaf(lya[j], inv.y, -ood.y), b1 = fmaf(hya[j], inv.y, -ood.y);
-          float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
+        for (int j = 0; j < W; j++) {
+          float a0 = fmaf(lo[0][j], inv.x, -ood.x), b0 = fmaf(hi[0][j], inv.x, -ood.x);
+          float a1 = fmaf(lo[1][j], inv.y, -ood.y), b1 = fmaf(hi[1][j], inv.y, -ood.y);
+          float a2 = fmaf(lo[2][j], inv.z, -ood.z), b2 = fmaf(hi[2][j], inv.z, -ood.z);
           float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
           float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tlimit));
           bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
@@ -185,17 +194,22 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
             c[b] = q;
           }
         };
-        cs(0, 1);
-        cs(2, 3);
-        cs(0, 2);
-        cs(1, 3);
-        cs(1, 2);
+        if constexpr (W == 4) {
+          cs(0, 1), cs(2, 3), cs(0, 2), cs(1, 3), cs(1, 2);
+        } else {  // Batcher's odd-even merge sort of eight (19 exchanges)
+          cs(0, 1), cs(2, 3), cs(4, 5), cs(6, 7);
+          cs(0, 2), cs(1, 3), cs(4, 6), cs(5, 7);
+          cs(1, 2), cs(5, 6);
+          cs(0, 4), cs(1, 5), cs(2, 6), cs(3, 7);
+          cs(2, 4), cs(3, 5);
+          cs(1, 2), cs(3, 4), cs(5, 6);
+        }
         if (nh == 0) {
           cur = pop();
         } else {
 #pragma unroll
-          for (int k = 3; k >= 1; k--) {  // farthest first, so the nearer pop earlier
-            if (k < nh && sp < kStack4) {
+          for (int k = W - 1; k >= 1; k--) {  // farthest first, so the nearer pop earlier
+            if (k < nh && sp < kStack) {
               if (kShort > 0 && sp < kShort) {
                 s_ref[sp][tx] = pack(r[k], c[k]);
                 s_tn[sp][tx] = tn[k];
@@ -244,6 +258,32 @@ __global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_
       active = false;
     }
   }
+}
+
+// 4-wide walk: 128-byte nodes; at most 3 stack entries per level of a tree shallower
+// than 22 levels.
+template <int kShort>
+__global__ void __launch_bounds__(128) k_trace_persistent4(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                           const uint32_t* __restrict__ order,
+                                                           int32_t* __restrict__ out_tid,
+                                                           float* __restrict__ out_dist,
+                                                           uint32_t* __restrict__ hit_leaf,
+                                                           int4* __restrict__ slot_rec,
+                                                           unsigned long long* __restrict__ counters) {
+  walk_wide<4, kShort, 64>(A, A.bvh4, rays, n, order, out_tid, out_dist, hit_leaf, slot_rec, counters);
+}
+
+// 8-wide walk: 256-byte nodes; at most 7 stack entries per level of a tree shallower
+// than 12 levels.
+template <int kShort>
+__global__ void __launch_bounds__(128) k_trace_persistent8(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n,
+                                                           const uint32_t* __restrict__ order,
+                                                           int32_t* __restrict__ out_tid,
+                                                           float* __restrict__ out_dist,
+                                                           uint32_t* __restrict__ hit_leaf,
+                                                           int4* __restrict__ slot_rec,
+                                                           unsigned long long* __restrict__ counters) {
+  walk_wide<8, kShort, 80>(A, A.bvh8, rays, n, order, out_tid, out_dist, hit_leaf, slot_rec, counters);
 }
 
 // The same check with one thread per ray: each thread walks its winner's ancestor list
@@ -608,7 +648,10 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     // the walk's stack lives in local memory: the shallower one when the BVH allows
     const bool shallow = cfg.walk_stack != 64 && A.bvh_depth < 32;
     const bool walk4 = A.bvh4 && 3 * A.bvh4_depth + 1 <= 64;  // the 4-wide walk's stack bound
-    if (cfg.variant == 4 && walk4)
+    const bool walk8 = A.bvh8 && 7 * A.bvh8_depth + 1 <= 80;  // the 8-wide walk's
+    if ((cfg.variant == 5 && walk8) || (cfg.variant == 4 && !walk4 && walk8))
+      k_trace_persistent8<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
+    else if ((cfg.variant == 4 || cfg.variant == 5) && walk4)
       k_trace_persistent4<16><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);
     else if (cfg.variant == 3 && walk4)
       k_trace_persistent4<0><<<blocks, 128, 0, s>>>(A, rays, n, order, tid, dist, hit_leaf, slot_rec, counters);

@@ -46,9 +46,11 @@ def test_batch_equals_single_scene_renders(use_graph, autotune):
 
 def test_autotuned_batch_picks_a_pass_size_and_equals_single_scene_renders():
     """Autotuning times the launch shapes and then the pass sizes 2^20..2^23 (two passes
-    each, on interleaved passes that hold the same mix of every scene); the chosen size
-    is reported, and every image still equals its single-scene render up to the FP64
-    summation order (the random numbers depend on each scene's own path indices only)."""
+    each, on interleaved passes that hold the same mix of every scene); the remaining
+    passes take the scenes one after another, each continuing after the paths the
+    tuning took from it. The chosen size is reported, and every image still equals its
+    single-scene render up to the FP64 summation order (the random numbers depend on
+    each scene's own path indices only)."""
     items = [(scenes.cornell_box(128, 128), dict(spp=512, max_depth=8, rr_mode=1, seed=31)),
              (scenes.material_spheres(128, 128), dict(spp=512, max_depth=8, rr_mode=1, seed=32)),
              (scenes.medium_scene(128, 128), dict(spp=512, max_depth=8, rr_mode=1, seed=33)),

@@ -18,7 +18,7 @@ def _bits_equal(a, b):
 
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("leaf_size", [1, 4, 8])
-@pytest.mark.parametrize("variant", [0, 1, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 3, 4, 5])
 @pytest.mark.parametrize("check", [0, 1])
 def test_hits_match_reference_golden(name, leaf_size, variant, check):
     z = load(name)
@@ -126,7 +126,7 @@ def test_full_size_batch_matches_oracle_sample_and_reference_walk():
         ctx.trace_closest_device(rays, n, tid2, dist2)
         torch.cuda.synchronize()
         assert torch.equal(tid, tid2) and torch.equal(dist.view(torch.int32), dist2.view(torch.int32))
-        for variant in (0, 1, 3):  # every walk variant returns the same answers on the whole batch
+        for variant in (0, 1, 3, 5):  # every walk variant returns the same answers on the whole batch
             ctx.set_trace_config(variant, 12)
             ctx.trace_closest_device(rays, n, tid2, dist2)
             torch.cuda.synchronize()

@@ -41,7 +41,7 @@ def _compare(ctx, torch, o, d):
     return got_t.cpu().numpy()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 3, 4, 5])
 @pytest.mark.parametrize("check", [0, 1])
 def test_noalloc_matches_allocating_entry_point_on_two_calls(variant, check):
     torch = pytest.importorskip("torch")
