@@ -61,9 +61,12 @@ void rx_destroy(rx_context* c) {
                       &c->d_objects, &c->d_light_cdf, &c->d_light_tri,
                       &c->d_counters, &c->d_queue})
       b->release();
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < 2; k++) {
       for (DevBuf* b : {&c->ring_rays[k], &c->ring_tid[k], &c->ring_dist[k], &c->ring_queue[k], &c->ring_counters[k]})
         b->release();
+      for (cudaEvent_t& e : c->ring_ev[k])
+        if (e) cudaEventDestroy(e);
+    }
     for (cudaEvent_t e : c->timing_ev) cudaEventDestroy(e);
     rx::guide_free(c->guide);
     c->guide = nullptr;
@@ -627,11 +630,13 @@ rx_status rx_trace_set_staging(rx_context* c, uint32_t chunk_rays) {
   return RX_OK;
 }
 
-// Host buffers. The rays go to the device in chunks of up to stage_rays that alternate
-// between two copy/compute streams, so one chunk's copies overlap the other chunk's
-// kernels (2^23 rays per chunk by default: large enough for binning and the persistent
-// walk; for a 2^24-ray batch this measured 1,130 end-to-end Mrays/s against 1,033 for
-// one whole-batch copy, trace and copy back).
+// Host buffers. The rays go to the device in chunks through a two-slot ring and three
+// streams: copies in on one, the closest-hit launches on the context's stream, the
+// results back on the third, ordered per slot by events, so the copies of one chunk
+// overlap the kernels of another while the kernels themselves run one chunk at a time
+// (two walks sharing the SMs slowed each other). The chunks ramp up (a quarter, a half,
+// then stage_rays: 2^23 by default, large enough for binning and the persistent walk)
+// so that the first copy, the one no kernel hides, is short.
 rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist) {
   if (!c) return RX_ERR_INVALID;
   if (!c->accel_ready) return c->fail(RX_ERR_STATE, "accelerator not built");
@@ -639,7 +644,14 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
   if (!rays || !out_tid || !out_dist) return c->fail(RX_ERR_INVALID, "null buffer");
   DeviceGuard g(c->device);
   const size_t chunk = std::min<size_t>(n, c->stage_rays);
-  const int nring = n > chunk ? 2 : 1;
+  std::vector<size_t> sizes;  // the chunk schedule
+  for (size_t b = 0, sz = std::max<size_t>(chunk / 4, std::min<size_t>(chunk, (size_t)1 << 16)); b < n;) {
+    const size_t m = std::min(sz, (size_t)n - b);
+    sizes.push_back(m);
+    b += m;
+    sz = std::min(chunk, 2 * sz);
+  }
+  const int nring = sizes.size() > 1 ? 2 : 1;
   if (c->ring_chunk < chunk || (nring == 2 && !c->ring_rays[1].p)) {
     for (int k = 0; k < nring; k++) {
       rx_status s;
@@ -652,19 +664,41 @@ rx_status rx_trace_closest(rx_context* c, const rx_ray* rays, uint32_t n, int32_
     }
     c->ring_chunk = chunk;
   }
-  for (size_t b = 0, k = 0; b < n; b += chunk, k = (k + 1) % nring) {
-    size_t m = std::min<size_t>(chunk, n - b);
-    cudaStream_t st = c->copy_stream[k];
-    cudaMemcpyAsync(c->ring_rays[k].p, rays + b, m * sizeof(rx_ray), cudaMemcpyHostToDevice, st);
+  for (int k = 0; k < 2; k++)
+    for (cudaEvent_t& e : c->ring_ev[k]) {
+      rx_status s;
+      if (!e && (s = c->cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "staging events")) != RX_OK)
+        return s;
+    }
+  cudaStream_t in = c->copy_stream[0], run = c->stream, out = c->copy_stream[1];
+  size_t b = 0;
+  for (size_t i = 0; i < sizes.size(); i++) {
+    const int k = (int)(i % nring);
+    const size_t m = sizes[i];
+    cudaEvent_t* ev = c->ring_ev[k];  // [0] copied in, [1] traced, [2] copied out
+    if (i >= (size_t)nring) cudaStreamWaitEvent(in, ev[1], 0);  // the slot's previous rays are traced
+    cudaMemcpyAsync(c->ring_rays[k].p, rays + b, m * sizeof(rx_ray), cudaMemcpyHostToDevice, in);
+    cudaEventRecord(ev[0], in);
+    cudaStreamWaitEvent(run, ev[0], 0);
+    if (i >= (size_t)nring) cudaStreamWaitEvent(run, ev[2], 0);  // the slot's previous results are copied out
     cudaError_t e = rx::launch_trace_closest(c->accel, c->ring_rays[k].as<rx_ray>(), (uint32_t)m,
                                              c->ring_tid[k].as<int32_t>(), c->ring_dist[k].as<float>(),
                                              c->ring_queue[k].as<uint32_t>(),
-                                             c->ring_counters[k].as<unsigned long long>(), c->trace_cfg, st);
-    if (e != cudaSuccess) return c->cuda(e, "trace_closest launch");
-    cudaMemcpyAsync(out_tid + b, c->ring_tid[k].p, m * 4, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(out_dist + b, c->ring_dist[k].p, m * 4, cudaMemcpyDeviceToHost, st);
+                                             c->ring_counters[k].as<unsigned long long>(), c->trace_cfg, run);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(in);
+      cudaStreamSynchronize(run);
+      cudaStreamSynchronize(out);
+      return c->cuda(e, "trace_closest launch");
+    }
+    cudaEventRecord(ev[1], run);
+    cudaStreamWaitEvent(out, ev[1], 0);
+    cudaMemcpyAsync(out_tid + b, c->ring_tid[k].p, m * 4, cudaMemcpyDeviceToHost, out);
+    cudaMemcpyAsync(out_dist + b, c->ring_dist[k].p, m * 4, cudaMemcpyDeviceToHost, out);
+    cudaEventRecord(ev[2], out);
+    b += m;
   }
-  for (auto s : c->copy_stream) {
+  for (cudaStream_t s : {in, run, out}) {
     rx_status r = c->cuda(cudaStreamSynchronize(s), "trace_closest");
     if (r != RX_OK) return r;
   }

@@ -164,6 +164,7 @@ struct rx_context {
   rx::DevBuf d_queue;        // closest-hit scratch (winner leaves + eager queue)
   // staging ring for host-buffer calls
   rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
+  cudaEvent_t ring_ev[2][3] = {};  // per slot: rays copied in, traced, results copied out
   size_t ring_chunk = 0;
   size_t stage_rays = (size_t)1 << 23;  // rays per staged chunk (rx_trace_set_staging)
   // per-kernel timing of device-buffer closest-hit calls (rx_trace_set_timing)

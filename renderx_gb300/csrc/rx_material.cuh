@@ -588,8 +588,8 @@ static __device__ PV scatter_step(const DevScene& S, const CamDev& cam, const PV
 
 // SceneObject::emit(isUniformOrigin = true, isUniformDir = false) through
 // Scene::SurfaceSampler (src/SceneObject.cpp:233-314, src/Scene.cpp:91-98): an emitter
-// triangle by area, a uniform point, a cosine direction; then its first hit.
-static __device__ PV emit_ray(const DevScene& S, const CamDev& cam, Rng& rng, Hit3& hit) {
+// triangle by area, a uniform point, a cosine direction (the ray, not yet traced).
+static __device__ PV emit_start(const DevScene& S, const CamDev& cam, Rng& rng) {
   float ru = rng.next() * S.light_area;
   int lo = 0, hi = (int)S.num_lights - 1;
   while (lo < hi) {
@@ -615,8 +615,19 @@ static __device__ PV emit_ray(const DevScene& S, const CamDev& cam, Rng& rng, Hi
   r.c = is_emissive(S, r.contact) ? bsdf_of(S, cam, r, r) : F3{1, 1, 1};
   r.dprob = cos_lobe_pdf(n, r.d, 1.0f);
   r.flags = kDirRandom | kOrgRandom;
+  return r;
+}
+
+// The first hit of an emitted ray (a hit at distance 0 counts as none).
+__device__ __forceinline__ Hit3 emit_hit(const DevScene& S, const PV& r) {
   PHit h = trace_cond<false>(S, r.o, r.d, INFINITY, r.contact, r.inside);
-  hit = (h.tid >= 0 && h.t > 0.0f) ? Hit3{(int)__ldg(&S.tri_obj[h.tid]), h.tid, h.t} : Hit3{kNone, -1, -1.0f};
+  return (h.tid >= 0 && h.t > 0.0f) ? Hit3{(int)__ldg(&S.tri_obj[h.tid]), h.tid, h.t} : Hit3{kNone, -1, -1.0f};
+}
+
+// emit_start and its first hit.
+static __device__ PV emit_ray(const DevScene& S, const CamDev& cam, Rng& rng, Hit3& hit) {
+  PV r = emit_start(S, cam, rng);
+  hit = emit_hit(S, r);
   return r;
 }
 

@@ -2,8 +2,8 @@
 //
 // Per iteration (VCMTracer.cpp:25-142):
 //  1. Light subpaths (emission sample + the bounce loop of MCRenderer::samplePathIter,
-//     with light-path scattering) as a wavefront, one launch per bounce over the live
-//     subpaths (k_sub_begin / k_sub_step), their vertices stored; every non-specular
+//     with light-path scattering) on persistent warps that take the next subpath when
+//     one ends (k_sub_run), their vertices stored; every non-specular
 //     vertex after the first that is not on an emitter becomes a photon
 //     (VCMTracer.cpp:64-95).
 //  2. A sort-by-cell hash grid over the photons (cell = 2 r, SmallVCM's spatial hash
@@ -11,7 +11,7 @@
 //     scatter (the counting-sort build of include/Hashgrid.h:21-91); it replaces the
 //     per-iteration PointKDTree (include/PointKDTree.h), queried with the same strict
 //     |p-x| < r test over the (up to) 8 cells the sphere touches.
-//  3. Per pixel, the eye subpath (the same wavefront, with light-path scattering, as
+//  3. Per pixel, the eye subpath (the same kernel, with light-path scattering, as
 //     VCMTracer.cpp:107 does), then colorByMergingPaths (:566-636) and
 //     colorByConnectingPaths (:430-562) with the full-path MIS of connectMergeWeight
 //     (:321-428, double precision) and light-tracing splats through
@@ -55,8 +55,8 @@ __device__ __forceinline__ F3 cam_dir(const CamDev& c, float xp, float yp) {
   return normalize(c.front * c.sight + c.right * x + c.up * y);
 }
 
-// Camera::generateRay + generateRayBase (src/Camera.cpp:4-47)
-__device__ PV camera_ray(const DevScene& S, const CamDev& c, uint32_t pixel, Rng& rng, Hit3& hit) {
+// Camera::generateRay + generateRayBase (src/Camera.cpp:4-47): the ray, not yet traced.
+__device__ PV camera_start(const DevScene& S, const CamDev& c, uint32_t pixel, Rng& rng) {
   int x = pixel % c.width, y = pixel / c.width;
   float jx = rng.next(), jy = rng.next();
   PV r = pv_term(c.pos);
@@ -65,9 +65,20 @@ __device__ PV camera_ray(const DevScene& S, const CamDev& c, uint32_t pixel, Rng
   r.contact = kCameraObj;
   r.flags = kDirRandom;
   r.pixel = (int)pixel;
-  PHit h = trace_cond<false>(S, r.o, r.d, INFINITY, kNone, kNone);
-  hit = h.tid >= 0 ? Hit3{(int)__ldg(&S.tri_obj[h.tid]), h.tid, h.t} : Hit3{kNone, -1, -1.0f};
   r.inside = find_inside(S, r.o, r.d, kNone);
+  return r;
+}
+
+// The first hit of a camera ray (no condition: the camera is no surface).
+__device__ __forceinline__ Hit3 camera_hit(const DevScene& S, const PV& r) {
+  PHit h = trace_cond<false>(S, r.o, r.d, INFINITY, kNone, kNone);
+  return h.tid >= 0 ? Hit3{(int)__ldg(&S.tri_obj[h.tid]), h.tid, h.t} : Hit3{kNone, -1, -1.0f};
+}
+
+// camera_start and its first hit.
+__device__ PV camera_ray(const DevScene& S, const CamDev& c, uint32_t pixel, Rng& rng, Hit3& hit) {
+  PV r = camera_start(S, c, pixel, rng);
+  hit = camera_hit(S, r);
   return r;
 }
 
@@ -387,7 +398,7 @@ __device__ bool join_eval(const DevScene& S, const CamDev& cam, const PV& L, con
 
 // ---- light subpaths + photons ----------------------------------------------------------
 // One light subpath per thread (the whole-path check mode, RX_VCM_FULL_PATH_MIS; the
-// default samples them as a wavefront, k_sub_begin / k_sub_step below).
+// default samples them on persistent warps, k_sub_run below).
 __global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, float4* lv, int* llen,
                                                    float4* photon_pos, int* photon_ref, unsigned* n_photons,
                                                    unsigned photon_cap, unsigned long long* rays) {
@@ -419,24 +430,15 @@ __global__ void __launch_bounds__(128) k_vcm_light(DevScene S, VcmParams P, floa
   if (nr) atomicAdd(rays, nr);
 }
 
-// ---- subpaths as a wavefront -------------------------------------------------------------
-// The bounce loop of sample_path split into launches, one per depth: each launch takes
-// the live subpaths of a queue, scatters and traces one step for each, stores the new
-// vertex and compacts the survivors into the next queue (warp ballot, one atomic per
-// warp), so a warp's lanes stay busy until the queue drains instead of idling while one
-// long subpath finishes. Between launches a subpath is its index, its random-number
-// counter, its vertex count, its depth and its last hit; its last vertex is read back
-// from the vertex store. The random numbers, and so the subpaths, are sample_path's.
-struct SubQ {
-  uint32_t p, k;     // subpath index, random-number counter
-  int n;             // vertices stored
-  uint32_t depth;    // bounce depth; bit 31: an emitter was met after the origin (photons stop)
-  int obj, tri;      // the last ray's hit
-  float dist;
-  uint32_t pad;
-};
-constexpr uint32_t kSeenEmitter = 1u << 31;
-
+// ---- subpaths on persistent warps --------------------------------------------------------
+// The bounce loop of sample_path with the subpaths spread over persistent warps: a lane
+// whose subpath has ended takes the next one from a counter (one atomic per warp and
+// refill), so a warp's lanes stay busy until every subpath is sampled, and one slow
+// bounce holds only its own lane (a ray that finds no legal hit walks most of the tree)
+// instead of the whole GPU at every depth, as it would with one launch per depth. Every
+// iteration of the loop traces one ray per busy lane: a new subpath's first ray, or the
+// ray the lane's last scatter made; then the lane stores the vertex, scatters again or
+// ends. The random numbers, and so the subpaths, are sample_path's.
 // Where a subpath's vertices go: the vertex store, and for VCM light subpaths the photons
 // (random vertices after the origin, up to the first emitter: k_vcm_light's rule).
 struct SubSink {
@@ -463,97 +465,88 @@ struct SubSink {
   }
 };
 
-// Appends the lanes with `live` to queue q (count *qn): warp ballot, one atomic per warp.
-__device__ __forceinline__ void sub_push(bool live, const SubQ& s, SubQ* q, unsigned* qn) {
-  const int lane = threadIdx.x & 31;
-  const unsigned m = __ballot_sync(0xffffffffu, live);
-  if (!m) return;
-  unsigned base = 0;
-  const int leader = __ffs(m) - 1;
-  if (lane == leader) base = atomicAdd(qn, (unsigned)__popc(m));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (live) q[base + __popc(m & ((1u << lane) - 1))] = s;
-}
-
-// The subpaths' first rays: light subpaths from emit_ray (k_vcm_light's stream), eye
-// subpaths from camera_ray (k_vcm_eye_full's); the first vertex stored, live ones queued.
+// Light subpaths from emit_start (k_vcm_light's stream) or eye subpaths from
+// camera_start (k_vcm_eye_full's), each subpath's vertices in the store; `light`: the
+// isLightPath argument of the scattering. cursor: subpaths handed out (zero at launch).
 template <bool LIGHT>
-__global__ void __launch_bounds__(128) k_sub_begin(DevScene S, VcmParams P, SubSink out, SubQ* q, unsigned* qn,
-                                                   unsigned long long* rays) {
+__global__ void __launch_bounds__(128) k_sub_run(DevScene S, VcmParams P, SubSink out, bool light_scatter,
+                                                 unsigned* cursor, unsigned long long* rays) {
+  constexpr unsigned FULL = 0xffffffffu;
   const uint32_t n = LIGHT ? P.n_light : P.n_pixels;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t iters = (n + stride - 1) / stride;
+  const int lane = threadIdx.x & 31;
+  bool active = false, exhausted = false, first = false, seen = false;
+  uint32_t p = 0, depth = 0;
+  int m = 0;
+  Rng rng(0, 0, 0);
+  PV prev, next;  // the last stored vertex; the vertex whose ray is traced next
   unsigned long long nr = 0;
-  for (uint32_t it = 0; it < iters; it++) {
-    const uint32_t p = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = false;
-    SubQ st{};
-    if (p < n) {
-      Rng rng(LIGHT ? P.seed : P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
-      Hit3 h;
-      PV start = LIGHT ? emit_ray(S, P.cam, rng, h) : camera_ray(S, P.cam, p, rng, h);
-      bool seen = false;
-      out.put(S, P, p, 0, start, seen);
-      if (start.inside == kNone && h.obj == kNone) {  // nothing to scatter from: the terminating ray
-        out.put(S, P, p, 1, pv_term(start.o), seen);
-        out.len[p] = 2;
-        nr += 2;
-      } else {
-        live = true;
-        st = SubQ{p, rng.k, 1, seen ? kSeenEmitter : 0u, h.obj, h.tri, h.dist, 0u};
-      }
-    }
-    sub_push(live, st, q, qn);
-  }
-  if (nr) atomicAdd(rays, nr);
-}
-
-// One bounce of every queued subpath (sample_path's loop body after its first put):
-// scatter from the last vertex, end on a killed ray or the depth cap, trace the new ray,
-// end on a miss, else store it and queue the subpath for the next launch. `light`: the
-// isLightPath argument of the scattering.
-template <bool LIGHT>
-__global__ void __launch_bounds__(128) k_sub_step(DevScene S, VcmParams P, SubSink out, bool light_scatter,
-                                                  const SubQ* qin, const unsigned* qin_n, SubQ* qout, unsigned* qout_n,
-                                                  unsigned long long* rays) {
-  const uint32_t n = *qin_n;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t iters = (n + stride - 1) / stride;
-  unsigned long long nr = 0;
-  for (uint32_t it = 0; it < iters; it++) {
-    const uint32_t j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = false;
-    SubQ st{};
-    if (j < n) {
-      st = qin[j];
-      const uint32_t p = st.p;
-      Rng rng(LIGHT ? P.seed : P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, st.k);
-      const PV prev = load_pv(out.verts + 4 * ((size_t)p * P.maxv + st.n - 1));
-      bool seen = (st.depth & kSeenEmitter) != 0;
-      const uint32_t depth = st.depth & ~kSeenEmitter;
-      int m = st.n;
-      PV next = scatter_step(S, P.cam, prev, Hit3{st.obj, st.tri, st.dist}, light_scatter, true, rng);
-      if (length(next.d) < 0.5f) {
-        out.put(S, P, p, m++, next, seen);
-      } else if (depth + 1 > P.max_depth) {
-        out.put(S, P, p, m++, pv_term(prev.o), seen);
-      } else {
-        PHit hh = trace_cond<false>(S, next.o, next.d, INFINITY, next.contact, next.inside);
-        out.put(S, P, p, m++, next, seen);
-        if (hh.tid < 0) {
-          out.put(S, P, p, m++, pv_term(prev.o), seen);
+  while (true) {
+    const unsigned want = __ballot_sync(FULL, !active && !exhausted);
+    if (want) {
+      const int leader = __ffs(want) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(cursor, (unsigned)__popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if (!active && !exhausted) {
+        const unsigned r = base + (unsigned)__popc(want & ((1u << lane) - 1));
+        if (r < n) {
+          p = r;
+          rng = Rng(LIGHT ? P.seed : P.seed ^ 0x5bd1e995ull, ((uint64_t)P.iter << 33) | (uint64_t)p, 0);
+          next = LIGHT ? emit_start(S, P.cam, rng) : camera_start(S, P.cam, p, rng);
+          seen = false;
+          m = 0;
+          out.put(S, P, p, m++, next, seen);
+          depth = 0;
+          first = true;
+          active = true;
         } else {
-          live = true;
-          st = SubQ{p, rng.k, m, (depth + 1) | (seen ? kSeenEmitter : 0u), (int)__ldg(&S.tri_obj[hh.tid]), hh.tid,
-                    hh.t, 0u};
+          exhausted = true;
         }
       }
-      if (!live) {
-        out.len[p] = m;
-        nr += (unsigned long long)m;
+    }
+    if (!__any_sync(FULL, active)) break;
+    if (!active) continue;
+    // the one trace of this iteration
+    Hit3 h;
+    if (first) {
+      h = LIGHT ? emit_hit(S, next) : camera_hit(S, next);
+    } else {
+      const PHit hh = trace_cond<false>(S, next.o, next.d, INFINITY, next.contact, next.inside);
+      h = hh.tid >= 0 ? Hit3{(int)__ldg(&S.tri_obj[hh.tid]), hh.tid, hh.t} : Hit3{kNone, -1, -1.0f};
+    }
+    bool end = false;
+    if (first) {  // the subpath's origin is stored; nothing to scatter from ends it
+      if (next.inside == kNone && h.obj == kNone) {
+        out.put(S, P, p, m++, pv_term(next.o), seen);
+        end = true;
+      }
+      prev = next;
+      first = false;
+    } else {
+      out.put(S, P, p, m++, next, seen);
+      if (h.obj == kNone) {
+        out.put(S, P, p, m++, pv_term(prev.o), seen);
+        end = true;
+      } else {
+        prev = next;
+        depth++;
       }
     }
-    sub_push(live, st, qout, qout_n);
+    if (!end) {  // scatter from the last vertex: the next ray, or the end of the subpath
+      next = scatter_step(S, P.cam, prev, h, light_scatter, true, rng);
+      if (length(next.d) < 0.5f) {
+        out.put(S, P, p, m++, next, seen);
+        end = true;
+      } else if (depth + 1 > P.max_depth) {
+        out.put(S, P, p, m++, pv_term(prev.o), seen);
+        end = true;
+      }
+    }
+    if (end) {
+      out.len[p] = m;
+      nr += (unsigned long long)m;
+      active = false;
+    }
   }
   if (nr) atomicAdd(rays, nr);
 }
@@ -787,10 +780,10 @@ __device__ __forceinline__ void img_add(float* img, int pixel, F3 c) {
   atomicAdd(img + 3 * pixel + 2, c.z);
 }
 
-// ---- eye subpaths and connections as a wavefront -----------------------------------------
+// ---- eye subpaths and connections ---------------------------------------------------------
 // colorByConnectingPaths (VCMTracer.cpp:430-562) joins every light vertex ci of the
 // pixel's light path with every eye vertex k (s = ci + 1, t = k + 1), plus the pure
-// eye path (s = 0). The subpath wavefront samples and stores the eye subpath; k_eye_post
+// eye path (s = 0). k_sub_run samples and stores the eye subpath; k_eye_post
 // builds its records, adds the s = 0 technique, and lists which vertices can take part
 // in a connection (sampled
 // at random, not on an emitter past the light's own vertex); the (k, ci) pairs are then
@@ -941,9 +934,9 @@ __global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, cons
 
 // Per pixel: the eye subpath and colorByConnectingPaths by the reference's loops over each
 // whole joined path, a shadow ray per connection in the same thread. Kept as the check of
-// the eye wavefront + k_eye_post + k_conn_eval (RX_VCM_FULL_PATH_MIS, which also samples
-// the light subpaths one per thread, k_vcm_light: the same random numbers, so the same
-// subpaths as the wavefronts).
+// k_sub_run + k_eye_post + k_conn_eval (RX_VCM_FULL_PATH_MIS, which also samples the
+// light subpaths one per thread, k_vcm_light: the same random numbers, so the same
+// subpaths as k_sub_run).
 __global__ void __launch_bounds__(128) k_vcm_eye_full(DevScene S, VcmParams P, const float4* lv, const int* llen,
                                                  float4* ev, int* elen, MisE* emis, float* img,
                                                  unsigned long long* rays) {
@@ -1118,31 +1111,83 @@ __device__ __forceinline__ F3 merge_pair(const DevScene& S, const VcmParams& P, 
   return col * (wt / prob) * (1.0f / P.norm);
 }
 
-// Merge pairs (colorByMergingPaths, VCMTracer.cpp:566-636), one warp per pixel of
-// [p0, p1): for each merge vertex of the pixel's eye path (ei >= 1, sampled at random,
-// up to the first emitter) the warp walks the grid cells the sphere touches, 128 sorted
-// photons per step (coalesced positions, the strict |p - x| < r test), and appends the
-// photons inside as (query, photon slot in bucket order) pairs with one atomic per step. Pairs past
-// `cap` are counted, not written (the host then grows the list or splits the range).
-__global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, const float4* ev, const int* elen,
-                                                    Grid G, uint32_t p0, uint32_t p1, unsigned long long cap,
-                                                    uint32_t* pair_q, int* pair_ref, unsigned long long* npairs,
-                                                    unsigned long long* nqueries) {
+// The iteration's merge queries in spatial order. A query is an eye vertex that merges
+// (colorByMergingPaths, VCMTracer.cpp:566-636: vertex ei >= 1 of the pixel's eye path,
+// sampled at random, before the first emitter); its key is the Morton code of its
+// position on a 64^3 grid over the scene bounds, so that the counting sort by key
+// (k_ray_scatter) puts queries that gather the same photons next to each other.
+__device__ __forceinline__ uint32_t spread6(uint32_t v) {  // 6 bits -> every third bit
+  uint32_t r = 0;
+#pragma unroll
+  for (int b = 0; b < 6; b++) r |= ((v >> b) & 1u) << (3 * b);
+  return r;
+}
+__global__ void __launch_bounds__(128) k_merge_queries(DevScene S, VcmParams P, const float4* ev, const int* elen,
+                                                       uint32_t* qlist, uint32_t* qkey, uint32_t* hist,
+                                                       unsigned* count) {
+  constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  unsigned long long queries = 0;  // merge vertices this warp queried (counted by lane 0)
+  const unsigned lt = (1u << lane) - 1u;
+  const DevAccel& A = S.accel;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t iters = (P.n_pixels + stride - 1) / stride;
+  for (uint32_t it = 0; it < iters; it++) {
+    const uint32_t p = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    const int ne = p < P.n_pixels ? elen[p] : 0;
+    int nmax = ne;
+    for (int s2 = 16; s2 > 0; s2 >>= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, s2));
+    bool stop = false;
+    for (int k = 1; k < nmax; k++) {
+      bool valid = false;
+      F3 x{};
+      if (k < ne && !stop) {
+        const float4* eb = ev + 4 * ((size_t)p * P.maxv + k);
+        const float4 o4 = eb[0], t4 = eb[3];
+        if (is_emissive(S, __float_as_int(t4.x))) stop = true;  // the merge loop stops at the first emitter
+        else if (__float_as_uint(t4.w) & kDirRandom) valid = true, x = f3(o4);
+      }
+      const unsigned m = __ballot_sync(FULL, valid);
+      if (!m) continue;
+      const int leader = __ffs(m) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (valid) {
+        const float xs[3] = {x.x, x.y, x.z};
+        uint32_t key = 0;
+#pragma unroll
+        for (int a2 = 0; a2 < 3; a2++) {
+          const float u = (xs[a2] - A.lo[a2]) / fmaxf(A.hi[a2] - A.lo[a2], 1e-20f) * 64.0f;
+          key |= spread6((uint32_t)fminf(fmaxf(u, 0.0f), 63.0f)) << a2;
+        }
+        const unsigned slot = base + __popc(m & lt);
+        qlist[slot] = p * P.maxv + (uint32_t)k;
+        qkey[slot] = key;
+        atomicAdd(&hist[key], 1u);
+      }
+    }
+  }
+}
+
+// Merge pairs (colorByMergingPaths, VCMTracer.cpp:566-636), one warp per query of the
+// spatially sorted list, positions [j0, j1): the 32 lanes hash the cells the sphere
+// touches, and the warp walks each distinct bucket 128 sorted photons per step
+// (coalesced positions, the strict |p - x| < r test), appending the photons inside as
+// (query, photon slot in bucket order) pairs with one atomic per step. Pairs past `cap`
+// are counted, not written (the host then grows the list or splits the range). Queries
+// taken in spatial order make the pairs that follow one another gather the same photons.
+__global__ void __launch_bounds__(256) k_merge_walk(VcmParams P, const float4* ev, Grid G, const uint32_t* qlist,
+                                                    const uint32_t* order, uint32_t j0, uint32_t j1,
+                                                    unsigned long long cap, uint32_t* pair_q, int* pair_ref,
+                                                    unsigned long long* npairs) {
+  const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   const float r = P.radius;
-  for (uint32_t p = p0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < p1; p += nw) {
-    const float4* eb = ev + 4 * ((size_t)p * P.maxv);
-    const int ne = elen[p];
-    for (int k = 1; k < ne; k++) {
-      const float4 o4 = eb[4 * k], t4 = eb[4 * k + 3];
-      if (is_emissive(S, __float_as_int(t4.x))) break;  // the reference's merge loop stops at the first emitter
-      if (!(__float_as_uint(t4.w) & kDirRandom)) continue;
-      const F3 x = f3(o4);
-      const uint32_t q = p * P.maxv + (uint32_t)k;
-      queries++;
+  for (uint32_t j = j0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); j < j1; j += nw) {
+    {
+      const uint32_t q = __ldg(&qlist[__ldg(&order[j])]);
+      const F3 x = f3(ev[4 * (size_t)q]);  // vertex q % maxv of pixel q / maxv
       // the cells the sphere touches (as merge_buckets), one per lane; equal buckets are
       // walked once, by the lowest lane that holds them
       const int x0 = (int)floorf((x.x - r) / G.cell), y0 = (int)floorf((x.y - r) / G.cell);
@@ -1197,7 +1242,6 @@ __global__ void __launch_bounds__(256) k_merge_walk(DevScene S, VcmParams P, con
       }
     }
   }
-  if (lane == 0 && queries) atomicAdd(nqueries, queries);
 }
 
 // One merge pair per lane, kRun consecutive pairs per thread (pairs of one query are
@@ -1629,13 +1673,10 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.bpt ? 1u : P.n_light * P.maxv;  // photon capacity (none without merging)
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(27);
+  std::vector<DevBuf> bufs(32);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
-  const size_t nsub = std::max(P.n_light, P.n_pixels);
-  if ((e = al(24, nsub * sizeof(SubQ))) != cudaSuccess) return e;  // subpath queues (wavefront)
-  if ((e = al(25, nsub * sizeof(SubQ))) != cudaSuccess) return e;
-  if ((e = al(26, 16)) != cudaSuccess) return e;                      // their lengths
+  if ((e = al(26, 16)) != cudaSuccess) return e;  // subpath cursors
   if ((e = al(0, (size_t)P.n_light * P.maxv * 4 * sizeof(float4))) != cudaSuccess) return e;  // light vertices
   if ((e = al(1, (size_t)P.n_light * sizeof(int))) != cudaSuccess) return e;
   if ((e = al(2, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;                      // photon positions
@@ -1660,9 +1701,16 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   if ((e = al(21, (size_t)P.n_pixels * sizeof(uint2))) != cudaSuccess) return e;                // connection masks
   if ((e = al(22, (size_t)cap * sizeof(float4))) != cudaSuccess) return e;                      // sorted photon positions
   if ((e = al(23, (size_t)cap * kJoin * sizeof(float4))) != cudaSuccess) return e;              // photon join data
+  if (!P.bpt) {  // merge queries in spatial order: list, keys, sorted order, key counts, count
+    if ((e = al(27, (size_t)nq * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = al(28, (size_t)nq * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = al(29, (size_t)nq * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = al(30, ((size_t)kRayBins + 1024) * sizeof(uint32_t))) != cudaSuccess) return e;
+    if ((e = al(31, 16)) != cudaSuccess) return e;
+  }
   const bool full_mis = (opt.flags & RX_VCM_FULL_PATH_MIS) != 0;
   constexpr uint32_t kMergeCap = 1u << 30;  // merge pairs per evaluation (8 GB of pair list)
-  uint32_t pix_chunk = P.n_pixels;           // pixels per merge walk
+  uint32_t q_chunk = nq;                     // sorted queries per merge walk
   const uint32_t pair_cap = 1u << 27;  // pairs per evaluation window
   uint32_t pair_alloc = 1u << 20;      // grows with demand up to pair_cap
   if ((e = al(17, (size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
@@ -1671,6 +1719,14 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
   cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
   int grid = c->trace_cfg.sms * 4;
+  int sub_grid[2] = {0, 0};  // resident blocks of k_sub_run<false>, <true>
+  {
+    int per = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sub_run<false>, 128, 0)) != cudaSuccess) return e;
+    sub_grid[0] = c->trace_cfg.sms * std::max(per, 1);
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sub_run<true>, 128, 0)) != cudaSuccess) return e;
+    sub_grid[1] = c->trace_cfg.sms * std::max(per, 1);
+  }
   Event e0, e1, m0, m1;  // render; merge gather of an iteration (with stats)
   if ((e = e0.create()) != cudaSuccess || (e = e1.create()) != cudaSuccess) return e;
   if (stats && ((e = m0.create()) != cudaSuccess || (e = m1.create()) != cudaSuccess)) return e;
@@ -1688,27 +1744,19 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
     P.radius = radius;
     P.iter = it;
     cudaMemsetAsync(nph, 0, sizeof(unsigned), s);
-    // the subpaths as a wavefront (the whole-path check mode keeps one thread per subpath)
+    cudaMemsetAsync(bufs[26].p, 0, bufs[26].bytes, s);  // subpath cursors
+    // the subpaths on persistent warps (the whole-path check mode keeps one thread per
+    // subpath): one launch per side, as many blocks as stay resident
     auto subpaths = [&](bool light_side) {
       const SubSink out = light_side ? SubSink{bufs[0].as<float4>(), bufs[1].as<int>(), !P.bpt, bufs[2].as<float4>(),
                                                bufs[3].as<int>(), nph, cap}
                                      : SubSink{bufs[12].as<float4>(), bufs[13].as<int>(), false, nullptr, nullptr,
                                                nullptr, 0u};
-      SubQ* q[2] = {bufs[24].as<SubQ>(), bufs[25].as<SubQ>()};
-      unsigned* qn = bufs[26].as<unsigned>();
+      unsigned* cursor = bufs[26].as<unsigned>() + (light_side ? 0 : 1);
       unsigned long long* rc = ctr + (light_side ? 0 : 1);
-      cudaMemsetAsync(qn, 0, 2 * sizeof(unsigned), s);
-      if (light_side) k_sub_begin<true><<<grid * 4, 128, 0, s>>>(S, P, out, q[0], qn, rc);
-      else k_sub_begin<false><<<grid * 4, 128, 0, s>>>(S, P, out, q[0], qn, rc);
       const bool light_scatter = light_side || !P.bpt;  // VCM samples eye paths with light-path scattering
-      for (uint32_t d = 0; d <= P.max_depth; d++) {
-        const int a = d & 1, b = a ^ 1;
-        cudaMemsetAsync(qn + b, 0, sizeof(unsigned), s);
-        if (light_side)
-          k_sub_step<true><<<grid * 4, 128, 0, s>>>(S, P, out, light_scatter, q[a], qn + a, q[b], qn + b, rc);
-        else
-          k_sub_step<false><<<grid * 4, 128, 0, s>>>(S, P, out, light_scatter, q[a], qn + a, q[b], qn + b, rc);
-      }
+      if (light_side) k_sub_run<true><<<sub_grid[1], 128, 0, s>>>(S, P, out, light_scatter, cursor, rc);
+      else k_sub_run<false><<<sub_grid[0], 128, 0, s>>>(S, P, out, light_scatter, cursor, rc);
     };
     if (full_mis)
       k_vcm_light<<<grid * 4, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[1].as<int>(), bufs[2].as<float4>(),
@@ -1786,38 +1834,50 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
                                                    bufs[17].as<uint32_t>(), bufs[18].as<int>(), np,
                                                    bufs[10].as<float>());
       }
-    } else {  // one walk appending pairs, then one pair per lane
+    } else {  // the queries in spatial order, one walk appending pairs, then one pair per lane
       if (m0) cudaEventRecord(m0, s);
-      for (uint32_t p0 = 0; p0 < P.n_pixels;) {
-        const uint32_t p1 = (uint32_t)std::min<uint64_t>(P.n_pixels, (uint64_t)p0 + pix_chunk);
-        unsigned long long* np_dev = ctr + 4;  // [4] pairs, [5] queries of this pixel range
-        cudaMemsetAsync(np_dev, 0, 2 * sizeof(unsigned long long), s);
-        k_merge_walk<<<grid * 2, 256, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), G, p0, p1, pair_alloc,
-                                              bufs[17].as<uint32_t>(), bufs[18].as<int>(), np_dev, np_dev + 1);
-        unsigned long long pq[2] = {0, 0};
-        cudaMemcpyAsync(pq, np_dev, sizeof pq, cudaMemcpyDeviceToHost, s);
+      uint32_t* qlist = bufs[27].as<uint32_t>();
+      uint32_t* qkey = bufs[28].as<uint32_t>();
+      uint32_t* qorder = bufs[29].as<uint32_t>();
+      uint32_t* qhist = bufs[30].as<uint32_t>();
+      unsigned* qcount = bufs[31].as<unsigned>();
+      cudaMemsetAsync(qcount, 0, sizeof(unsigned), s);
+      cudaMemsetAsync(qhist, 0, (size_t)kRayBins * sizeof(uint32_t), s);
+      k_merge_queries<<<grid, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[13].as<int>(), qlist, qkey, qhist, qcount);
+      scan_bins(qhist, qhist + kRayBins, s);
+      k_ray_scatter<<<grid * 2, 256, 0, s>>>(qkey, 0, qcount, qhist, qorder);
+      unsigned nqv = 0;
+      cudaMemcpyAsync(&nqv, qcount, sizeof nqv, cudaMemcpyDeviceToHost, s);
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+      queries += nqv;
+      for (uint32_t j0 = 0; j0 < nqv;) {
+        const uint32_t j1 = (uint32_t)std::min<uint64_t>(nqv, (uint64_t)j0 + q_chunk);
+        unsigned long long* np_dev = ctr + 4;  // [4] pairs of this query range
+        cudaMemsetAsync(np_dev, 0, sizeof(unsigned long long), s);
+        k_merge_walk<<<grid * 2, 256, 0, s>>>(P, bufs[12].as<float4>(), G, qlist, qorder, j0, j1, pair_alloc,
+                                              bufs[17].as<uint32_t>(), bufs[18].as<int>(), np_dev);
+        unsigned long long np = 0;
+        cudaMemcpyAsync(&np, np_dev, sizeof np, cudaMemcpyDeviceToHost, s);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-        unsigned long long np = pq[0];
-        if (np > pair_alloc) {  // grow the pair list, or split the pixel range once it is at its cap
+        if (np > pair_alloc) {  // grow the pair list, or split the query range once it is at its cap
           if (pair_alloc < kMergeCap) {
             pair_alloc = (uint32_t)std::min<unsigned long long>(kMergeCap, np + np / 4);
             if ((e = bufs[17].alloc((size_t)pair_alloc * sizeof(uint32_t))) != cudaSuccess) return e;
             if ((e = bufs[18].alloc((size_t)pair_alloc * sizeof(int))) != cudaSuccess) return e;
             continue;
           }
-          if (p1 - p0 > 1) {
-            pix_chunk = (p1 - p0) / 2;
+          if (j1 - j0 > 1) {
+            q_chunk = (j1 - j0) / 2;
             continue;
           }
-          np = pair_alloc;  // one pixel beyond the cap: its first kMergeCap pairs
+          np = pair_alloc;  // one query beyond the cap: its first kMergeCap pairs
         }
         merges += np;
-        queries += pq[1];
         if (np)
           k_merge_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[12].as<float4>(), bufs[20].as<MisE>(), bufs[23].as<float4>(),
                                                 bufs[17].as<uint32_t>(), bufs[18].as<int>(), (uint32_t)np,
                                                 bufs[10].as<float>());
-        p0 = p1;
+        j0 = j1;
       }
       if (m1) {  // device time of this iteration's merge gather (walk + pair evaluation)
         cudaEventRecord(m1, s);

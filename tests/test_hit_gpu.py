@@ -100,6 +100,32 @@ def test_invalid_inputs_raise():
             ctx.set_geometry(v, np.array([[0, 1, 2]], np.uint32))
 
 
+@pytest.mark.parametrize("stage,n", [(1 << 16, 5 * (1 << 16) + 77), (1 << 20, 3 * (1 << 20) + 12345)])
+def test_host_buffer_ring_matches_device_path(stage, n):
+    """The host-buffer call stages the rays through a two-slot ring on three streams
+    (copies in, kernels, copies out, ordered by events) in chunks that ramp up to the
+    staging size: equal chunks of 2^16 (five and a ragged tail, each slot reused), and
+    2^18, 2^19, 2^20, 2^20 plus a tail. Every answer equals the device-buffer call's."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.sphere_field(20, 3, seed=2)
+    f = sc.flatten()
+    o, d = scenes.hit_rays(n, seed=11)
+    with rx.Context(0) as ctx:
+        ctx.set_geometry(f["verts"], f["tris"])
+        ctx.build_accel()
+        rays = torch.from_numpy(rx.rays_to_array(o, d)).cuda()
+        tid = torch.empty(n, dtype=torch.int32, device="cuda")
+        dist = torch.empty(n, dtype=torch.float32, device="cuda")
+        ctx.trace_closest_device(rays, n, tid, dist)
+        torch.cuda.synchronize()
+        ctx.set_trace_staging(stage)
+        for _ in range(2):  # twice: the second call reuses the ring and its events
+            ht, hd = ctx.trace_closest(o, d)
+            assert np.array_equal(ht, tid.cpu().numpy())
+            assert _bits_equal(hd, dist.cpu().numpy())
+        assert ctx.counters()["errors"] == 0
+
+
 @pytest.mark.slow
 def test_full_size_batch_matches_oracle_sample_and_reference_walk():
     """4,096,036 triangles, 2^24 rays: the whole batch through the fast path; a sample
