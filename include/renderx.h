@@ -146,8 +146,9 @@ typedef struct rx_batch_options {
   uint32_t chosen_paths_per_pass;  /* out: paths per pass of the remaining passes */
   int32_t chosen_blocks_per_sm;  /* out: extend / shade blocks per SM used */
   int32_t chosen_stack;          /* out: walk used: 4 = 4-wide BVH, 5 = 4-wide BVH with a
-                                    shared-memory short stack, 32 / 64 = binary BVH with
-                                    that stack depth */
+                                    shared-memory short stack, 6 = 5 on persistent warps
+                                    that refill finished lanes (the default), 32 / 64 =
+                                    binary BVH with that stack depth */
 } rx_batch_options;
 
 /* Vertex connection and merging options (VCMTracer, reference include/VCMTracer.h). */
@@ -435,6 +436,11 @@ rx_status rx_guide_train_step(rx_context* ctx, const float* d_recs, uint32_t n, 
  * 16..128, both in steps of 16. */
 rx_status rx_diag_umma_gemm(rx_context* ctx, uint32_t M, uint32_t N, uint32_t K, int32_t a_mn, int32_t b_mn,
                             const uint16_t* a_bf16, const uint16_t* b_bf16, float* d_out);
+/* Tensor-core issue rate (no reference counterpart): `count` back-to-back BF16 MMAs of
+ * M = 128, K = 16 and N = 64, 128 or 256 (the guiding network's layers are N = 64) issued
+ * by one thread of one CTA; returns SM clock cycles per MMA to the last issue and to the
+ * completion of all (the second launch of two). count 1..4096. */
+rx_status rx_diag_umma_rate(rx_context* ctx, uint32_t N, uint32_t count, double* issue_clk, double* done_clk);
 
 #ifdef __cplusplus
 }

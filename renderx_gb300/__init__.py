@@ -337,6 +337,14 @@ class Context:
                                            _capi.ptr(out)))
         return out
 
+    def diag_umma_rate(self, n: int, count: int = 256) -> tuple:
+        """Tensor-core issue rate: SM clock cycles per back-to-back BF16 MMA of
+        M = 128, K = 16 and N = n (64, 128 or 256) from one thread, (to the last issue, to
+        completion)."""
+        issue, done = ctypes.c_double(), ctypes.c_double()
+        self._ck(self._L.rx_diag_umma_rate(self.h, int(n), int(count), ctypes.byref(issue), ctypes.byref(done)))
+        return issue.value, done.value
+
     # ---- learned guiding ---------------------------------------------------------
     def guide_init(self, learning_rate: float = 5e-3, bsdf_fraction: float = 0.5, batch: int = 1 << 18,
                    train_passes: int = 4, steps_per_pass: int = 4, warmup_passes: int = 0, seed: int = 1, box=None):

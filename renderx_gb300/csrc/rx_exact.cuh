@@ -17,6 +17,26 @@ struct F3 {
 };
 
 __device__ __forceinline__ F3 f3(float4 v) { return {v.x, v.y, v.z}; }
+
+// Not parity arithmetic: the BVH walks' slab tests (their boxes only pick candidates).
+// Three-input float minimum and maximum (one instruction each on sm_100 and later; the
+// same values as two fminf / fmaxf, NaN operands aside, which the walk never forms).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+// The slab tests' inverse direction: finite and never zero (+-1e30 for components
+// within 1e-30 of zero).
+__device__ __forceinline__ F3 safe_inv(F3 d) {
+  auto iv = [](float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysignf(1e30f, x); };
+  return {iv(d.x), iv(d.y), iv(d.z)};
+}
 __device__ __forceinline__ float comp(F3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 
 __device__ __forceinline__ F3 xsub(F3 a, F3 b) {

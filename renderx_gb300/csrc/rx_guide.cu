@@ -103,6 +103,50 @@ __global__ void __launch_bounds__(128) k_diag_umma(const uint16_t* A, const uint
   if (warp == 0) tc::tmem_dealloc(tbase, 128);
 }
 
+// Back-to-back tcgen05.mma issue from one thread: `count` MMAs of M = 128, K = 16 and the
+// given N (BF16, FP32 accumulation, operands in shared memory), timed with the SM clock
+// from the first issue to the last issue and to the completion of all. Shared memory
+// holds A (128 x 64) and B (256 x 64) BF16 tiles; each MMA reads one K = 16 slice.
+constexpr uint32_t kRateSmem = (128 + 256) * 64 * 2;
+__global__ void __launch_bounds__(128, 1) k_diag_umma_rate(uint32_t N, uint32_t count, unsigned long long* clk,
+                                                           int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tbase;
+  for (uint32_t i = threadIdx.x; i < kRateSmem / 16; i += blockDim.x)
+    reinterpret_cast<uint4*>(sm)[i] = make_uint4(0x3f803f80u, 0u, 0x3f803f80u, 0u);  // 1.0 / 0.0 pairs
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&tbase, 256);
+  tc::fence_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (threadIdx.x == 0) {
+    const uint32_t id = tc::idesc_bf16(128, N, false, false);
+    const uint32_t a0 = tc::smem_u32(sm), b0 = tc::smem_u32(sm + 128 * 64 * 2);
+    const uint32_t sbo = 8u * 128u;  // K = 64: the next 8 rows
+    const long long t0 = clock64();
+    for (uint32_t m = 0; m < count; m++) {
+      const uint32_t k0 = 16u * (m & 3u);
+      tc::mma_bf16(tbase, tc::sdesc(a0 + tc::core_off(0, k0, 64), 128u, sbo),
+                   tc::sdesc(b0 + tc::core_off(0, k0, 64), 128u, sbo), id, m > 0);
+    }
+    const long long t1 = clock64();
+    tc::mma_commit(&bar);
+    const bool ok = tc::mbar_wait(&bar, 0);
+    const long long t2 = clock64();
+    clk[0] = (unsigned long long)(t1 - t0);
+    clk[1] = (unsigned long long)(t2 - t0);
+    if (!ok) *status = 1;
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tbase, 256);
+}
+
 // =======================================================================================
 // Network kernels
 // =======================================================================================
@@ -902,6 +946,32 @@ extern "C" rx_status rx_diag_umma_gemm(rx_context* c, uint32_t M, uint32_t N, ui
   cudaMemcpy(&st, ds.p, 4, cudaMemcpyDeviceToHost);
   cudaMemcpy(d_out, dd.p, (size_t)128 * N * 4, cudaMemcpyDeviceToHost);
   if (st) return c->fail(RX_ERR_TIMEOUT, "tensor-core MMA did not complete");
+  return RX_OK;
+}
+
+extern "C" rx_status rx_diag_umma_rate(rx_context* c, uint32_t N, uint32_t count, double* issue_clk,
+                                       double* done_clk) {
+  if (!c) return RX_ERR_INVALID;
+  if (!issue_clk || !done_clk) return c->fail(RX_ERR_INVALID, "null output");
+  if ((N != 64 && N != 128 && N != 256) || count == 0 || count > 4096)
+    return c->fail(RX_ERR_INVALID, "N must be 64, 128 or 256 and count 1..4096");
+  DeviceGuard g(c->device);
+  DevBuf dc, ds;
+  rx_status s;
+  if ((s = c->cuda(dc.alloc(2 * sizeof(unsigned long long)), "alloc")) != RX_OK) return s;
+  if ((s = c->cuda(ds.alloc(4), "alloc")) != RX_OK) return s;
+  cudaMemset(ds.p, 0, 4);
+  cudaFuncSetAttribute(rx::k_diag_umma_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rx::kRateSmem);
+  for (int rep = 0; rep < 2; rep++)  // the first launch warms the instruction cache
+    rx::k_diag_umma_rate<<<1, 128, rx::kRateSmem, c->stream>>>(N, count, dc.as<unsigned long long>(), ds.as<int>());
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "umma rate")) != RX_OK) return s;
+  unsigned long long h[2] = {0, 0};
+  int st = 0;
+  cudaMemcpy(h, dc.p, sizeof h, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&st, ds.p, 4, cudaMemcpyDeviceToHost);
+  if (st) return c->fail(RX_ERR_TIMEOUT, "tensor-core MMA did not complete");
+  *issue_clk = (double)h[0] / count;
+  *done_clk = (double)h[1] / count;
   return RX_OK;
 }
 

@@ -17,6 +17,7 @@
 #include "rx_guide.h"
 #include "rx_internal.h"
 #include "rx_material.cuh"
+#include "rx_walk.cuh"
 #include "rx_wavefront.h"
 
 namespace rx {
@@ -186,6 +187,55 @@ __global__ void k_generate(const SceneRec* R, int nr, PassState* ps, Layout L, P
   }
 }
 
+// The extension rays' lanes for walk_persistent (kWalk4P): path `order[r]` (binned
+// order) or r of the queue, its scene's 4-wide BVH, the closest legal hit
+// (NoSelfIntersectionCondition through leaf_test, as trace_cond4); the answer to hit[].
+struct ExtendLane {
+  const SceneRec* R;
+  PathSoA S;
+  uint32_t n;
+  const uint32_t* __restrict__ order;
+  int2* hit;
+  const DevScene* sc = nullptr;
+  uint32_t i = 0;
+  int contact = kNone, inside = kNone;
+  bool cond = false;
+  PHit best{-1, INFINITY};
+
+  __device__ bool begin(uint32_t r, F3& o, F3& d) {
+    if (r >= n) return false;
+    i = order ? __ldg(&order[r]) : r;
+    const float4 o4 = S.o[i], d4 = S.d[i];
+    const int4 inf = S.info[i];
+    const bool camera = (inf.w & 255) == 0;  // the camera ray's first query has no condition
+    sc = &R[(uint32_t)inf.w >> 16].S;
+    contact = camera ? kNone : inf.y;
+    inside = camera ? kNone : inf.z;
+    cond = !(contact == kNone && inside == kNone);
+    best = PHit{-1, INFINITY};
+    o = f3(o4);
+    d = f3(d4);
+    return true;
+  }
+  __device__ const float4* nodes() const { return sc->accel.bvh4; }
+  __device__ float limit() const { return best.t; }
+  __device__ void leaf(int first, int count, F3 o, F3 d) {
+    leaf_test<false>(*sc, first, count, o, d, cond, contact, inside, best);
+  }
+  __device__ void end() { hit[i] = make_int2(best.tid, __float_as_int(best.t)); }
+};
+
+// Closest legal hit of each live path's ray on persistent warps (kWalk4P): the same
+// answers as k_extend<kWalk4S>, with lanes refilled from `cursor` (zero at launch)
+// instead of each thread walking its share of the queue to the end.
+__global__ void __launch_bounds__(128, 8) k_extend_p(const SceneRec* R, PathSoA S, const unsigned* count,
+                                                     const uint32_t* __restrict__ order, int2* hit,
+                                                     unsigned long long* rays, unsigned long long* cursor) {
+  const uint32_t n = *count;
+  ExtendLane L{R, S, n, order, hit};
+  walk_persistent<4, kShortStack, 64>(L, cursor);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
+}
 // Bin keys of the live paths' next rays (counting sort input; rx_bin.cuh).
 __global__ void k_path_keys(const SceneRec* R, PathSoA S, const unsigned* count, uint32_t* keys, uint32_t* hist) {
   uint32_t n = *count;
@@ -505,7 +555,13 @@ __global__ void __launch_bounds__(128) k_shade(const SceneRec* R, const PassStat
   if (lane == 0 && shadows) atomicAdd(shadow_rays, (unsigned long long)shadows);
 }
 
-__global__ void k_zero(unsigned* p) { *p = 0; }
+// The next queue's length, and the extension walk's refill cursor for the next bounce
+// (kWalk4P: every k_extend_p launch of a pass is followed by this one, so the cursor is
+// zero when the next starts).
+__global__ void k_zero(unsigned* p, unsigned long long* cursor) {
+  *p = 0;
+  *cursor = 0ull;
+}
 __global__ void k_advance(PassState* ps) {
   ps->base += ps->per_pass;
   ps->pass += 1;
@@ -700,6 +756,10 @@ PtParams make_pt_params(const rx_context* c, const rx_camera& cam, const rx_pt_o
 
 namespace {
 
+// W.ctr slot of the persistent extension walk's refill cursor (slots 0 and 1 count rays,
+// 8 onwards hold the unsigned queue counts).
+constexpr int kExtendCursor = 40;
+
 // Device buffers of one wavefront render.
 struct Wave {
   const SceneRec* R;
@@ -771,9 +831,12 @@ cudaError_t enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
   unsigned *cc = W.cnt, *cn = W.cnt + 1;
   for (uint32_t d = 0; d < W.loops; d++) {
     const uint32_t* order = d > 0 ? enqueue_binning(W, cur, cc, grid, s) : nullptr;
-    k_extend<STACK><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
+    if constexpr (STACK == kWalk4P)  // persistent: the blocks that stay resident (8 per SM)
+      k_extend_p<<<W.sms * 8, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr, W.ctr + kExtendCursor);
+    else
+      k_extend<STACK><<<grid, 128, 0, s>>>(W.R, cur, cc, order, W.hit, W.ctr);
     if (W.nets && e == cudaSuccess) e = enqueue_infer(W, cur, cc, grid, s);
-    k_zero<<<1, 1, 0, s>>>(cn);
+    k_zero<<<1, 1, 0, s>>>(cn, W.ctr + kExtendCursor);
     k_shade<STACK><<<grid, 128, 0, s>>>(W.R, W.ps, cur, cc, W.hit, nxt, cn, W.film, W.sq, W.ctr + 1, G);
     std::swap(cur, nxt);
     std::swap(cc, cn);
@@ -790,6 +853,7 @@ cudaError_t enqueue_pass(const Wave& W, int grid, cudaStream_t s) {
 
 cudaError_t enqueue_pass_shape(const Wave& W, const PtShape& sh, int sms, cudaStream_t s) {
   int grid = sms * sh.blocks_per_sm;
+  if (sh.stack == kWalk4P) return enqueue_pass<kWalk4P>(W, grid, s);
   if (sh.stack == kWalk4S) return enqueue_pass<kWalk4S>(W, grid, s);
   if (sh.stack == kWalk4) return enqueue_pass<kWalk4>(W, grid, s);
   if (sh.stack == 32) return enqueue_pass<32>(W, grid, s);
@@ -969,13 +1033,13 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   }
 
   // launch shapes: the context's default, or candidates timed on the first passes
-  PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4S : (max_bvh_depth < 32 ? 32 : kStackDepth)};
+  PtShape best{c->trace_cfg.pt_blocks_per_sm, wide_ok ? kWalk4P : (max_bvh_depth < 32 ? 32 : kStackDepth)};
   best.paths_per_pass = per_pass;
   std::vector<PtShape> cands;
   if (run.autotune) {
     for (int bps : {4, 8, 16})
-      for (int st : {kWalk4S, kWalk4, 32, kStackDepth})
-        if (st == kWalk4 || st == kWalk4S ? wide_ok : st > (int)max_bvh_depth)
+      for (int st : {kWalk4P, kWalk4S, kWalk4, 32, kStackDepth})
+        if (st == kWalk4 || st == kWalk4S || st == kWalk4P ? wide_ok : st > (int)max_bvh_depth)
           cands.push_back(PtShape{bps, st, per_pass});
     if (npasses < 2 * cands.size() + 2) cands.clear();
   }

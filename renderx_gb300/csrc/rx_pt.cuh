@@ -161,13 +161,13 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
       float a0 = fmaf(n0.x, inv.x, -ood.x), b0 = fmaf(n0.y, inv.x, -ood.x);
       float a1 = fmaf(n0.z, inv.y, -ood.y), b1 = fmaf(n0.w, inv.y, -ood.y);
       float a2 = fmaf(n2.x, inv.z, -ood.z), b2 = fmaf(n2.y, inv.z, -ood.z);
-      float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
-      float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), best.t));
+      float tn0 = fmaxf(max3f(fminf(a0, b0), fminf(a1, b1), fminf(a2, b2)), 0.0f);
+      float tf0 = fminf(min3f(fmaxf(a0, b0), fmaxf(a1, b1), fmaxf(a2, b2)), best.t);
       float c0 = fmaf(n1.x, inv.x, -ood.x), d0 = fmaf(n1.y, inv.x, -ood.x);
       float c1 = fmaf(n1.z, inv.y, -ood.y), d1 = fmaf(n1.w, inv.y, -ood.y);
       float c2 = fmaf(n2.z, inv.z, -ood.z), d2 = fmaf(n2.w, inv.z, -ood.z);
-      float tn1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), 0.0f));
-      float tf1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), best.t));
+      float tn1 = fmaxf(max3f(fminf(c0, d0), fminf(c1, d1), fminf(c2, d2)), 0.0f);
+      float tf1 = fminf(min3f(fmaxf(c0, d0), fmaxf(c1, d1), fmaxf(c2, d2)), best.t);
       bool h0 = tn0 <= tf0 * 1.0000005f, h1 = tn1 <= tf1 * 1.0000005f;
       if (h0 && h1) {
         bool first0 = tn0 <= tn1;
@@ -235,6 +235,7 @@ __device__ __forceinline__ PHit trace_cond(const DevScene& S, F3 o, F3 d, float 
 // at most 3 entries per level: callers use it only when 3 * bvh4_depth + 1 <= 64.
 constexpr int kWalk4 = 4;   // walk selector: the 4-wide BVH
 constexpr int kWalk4S = 5;  // the 4-wide BVH, first kShortStack stack entries in shared memory
+constexpr int kWalk4P = 6;  // kWalk4S on persistent warps that refill finished lanes (extension rays)
 constexpr int kShortStack = 16;
 // The cnt triangles of the 4-wide tree's leaf at slot `first` (Moller-Trumbore, the
 // NoSelfIntersectionCondition when cond): lowers best to the nearest legal hit; with ANY,
@@ -286,6 +287,10 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
             fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(1e30f, d.y),
             fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(1e30f, d.z)};
   F3 ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
+  // the near plane of each axis: the lower bound where the inverse direction is positive
+  // (it is never zero), else the upper one; fma(x, inv, -ood) is monotonic in x, so the
+  // near plane gives the smaller slab value, as ordering both with min / max would
+  const int ox = inv.x < 0.0f ? 1 : 0, oy = inv.y < 0.0f ? 1 : 0, oz = inv.z < 0.0f ? 1 : 0;
   PHit best{-1, tmax};
   constexpr int kS = 64;
   int stack_ref[kS - SH];
@@ -295,8 +300,8 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
   while (true) {
     if (cur >= 0) {
       const float4* np = A.bvh4 + 8 * (size_t)cur;
-      float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-      float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+      float4 lx = __ldg(np + ox), hx = __ldg(np + 1 - ox), ly = __ldg(np + 2 + oy), hy = __ldg(np + 3 - oy);
+      float4 lz = __ldg(np + 4 + oz), hz = __ldg(np + 5 - oz);  // near (l) and far (h) planes
       int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
       const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
       const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
@@ -309,8 +314,8 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
         float a0 = fmaf(lxa[j], inv.x, -ood.x), b0 = fmaf(hxa[j], inv.x, -ood.x);
         float a1 = fmaf(lya[j], inv.y, -ood.y), b1 = fmaf(hya[j], inv.y, -ood.y);
         float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
-        float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
-        float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), best.t));
+        float t0 = fmaxf(max3f(a0, a1, a2), 0.0f);
+        float t1 = fminf(min3f(b0, b1, b2), best.t);
         bool h = r[j] != 0x7fffffff && t0 <= t1 * 1.0000005f;
         tn[j] = h ? t0 : INFINITY;
         nh += h ? 1 : 0;
@@ -382,7 +387,8 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
 template <bool ANY, int WALK>
 __device__ __forceinline__ PHit trace_walk(const DevScene& S, F3 o, F3 d, float tmax, int contact, int inside) {
   if constexpr (WALK == kWalk4) return trace_cond4<ANY, 0>(S, o, d, tmax, contact, inside);
-  else if constexpr (WALK == kWalk4S) return trace_cond4<ANY, kShortStack>(S, o, d, tmax, contact, inside);
+  else if constexpr (WALK == kWalk4S || WALK == kWalk4P)
+    return trace_cond4<ANY, kShortStack>(S, o, d, tmax, contact, inside);
   else return trace_cond<ANY, WALK>(S, o, d, tmax, contact, inside);
 }
 

@@ -3,6 +3,7 @@
 #include "rx_bin.cuh"
 #include "rx_trace.cuh"
 #include "rx_accel.h"
+#include "rx_walk.cuh"
 
 namespace rx {
 
@@ -54,210 +55,71 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
   if (lane == 0 && sum) atomicAdd(&counters[1], (unsigned long long)sum);
 }
 
-// The persistent walk over a W-wide BVH (W = 4: 128-byte nodes, one cache line; W = 8:
-// 256-byte nodes, half the levels): one node visit tests W child boxes, visits the
-// nearest hit child next and stacks the others far to near; pruning, leaf tests and
-// refills as k_trace_persistent. kShort > 0: the first kShort entries of each thread's
-// stack sit in shared memory (one column per thread, conflict-free), deeper entries in
-// local memory. kStack bounds the stack: (W - 1) entries per level below the root.
+// The closest-hit batch's lanes for walk_persistent: ray `order[r]` (binned order) or r,
+// the reference's exact triangle test and tie rule (closest distance, then the larger
+// reference leaf, then the earlier position), pruning at best + prune_rel (1 + best); the
+// answer goes to the slot record (binned order; the check scatters it) or to the outputs.
+struct HitLane {
+  const DevAccel& A;
+  const rx_ray* __restrict__ rays;
+  uint32_t n;
+  const uint32_t* __restrict__ order;
+  int32_t* __restrict__ out_tid;
+  float* __restrict__ out_dist;
+  uint32_t* __restrict__ hit_leaf;
+  int4* __restrict__ slot_rec;
+  const float4* bvh;
+  uint32_t ray = 0, slot = 0;
+  float tlimit = INFINITY;
+  HitResult best{-1, -1.0f, 0u, 0u, false};
+
+  __device__ bool begin(uint32_t r, F3& o, F3& d) {
+    if (r >= n) return false;
+    slot = r;
+    ray = order ? __ldg(&order[r]) : r;
+    const float4* rp = reinterpret_cast<const float4*>(rays + ray);
+    o = f3(__ldg(rp));
+    d = f3(__ldg(rp + 1));
+    tlimit = INFINITY;
+    best = {-1, -1.0f, 0u, 0u, false};
+    return true;
+  }
+  __device__ const float4* nodes() const { return bvh; }
+  __device__ float limit() const { return tlimit; }
+  __device__ void leaf(int first, int count, F3 o, F3 d) {
+    for (int k = 0; k < count; k++) {
+      const float4* tp = A.tris + 3 * (size_t)(first + k);
+      float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+      float t;
+      if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
+        uint32_t lf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
+        if (!best.hit || t < best.t || (t == best.t && (lf > best.leaf || (lf == best.leaf && pos < best.pos)))) {
+          best = {__float_as_int(v0.w), t, lf, pos, true};
+          tlimit = t + A.prune_rel * (1.0f + t);
+        }
+      }
+    }
+  }
+  __device__ void end() {
+    if (slot_rec) {  // one 16-byte record by binned slot; the check scatters it to ray order
+      slot_rec[slot] = make_int4(best.hit ? best.tid : -1, __float_as_int(best.hit ? best.t : -1.0f),
+                                 (int)(best.hit ? best.leaf : kNoLeaf), 0);
+    } else {
+      out_tid[ray] = best.hit ? best.tid : -1;
+      out_dist[ray] = best.hit ? best.t : -1.0f;
+      hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
+    }
+  }
+};
+
 template <int W, int kShort, int kStack>
 __device__ __forceinline__ void walk_wide(const DevAccel& A, const float4* __restrict__ nodes,
                                           const rx_ray* __restrict__ rays, uint32_t n,
                                           const uint32_t* __restrict__ order, int32_t* __restrict__ out_tid,
                                           float* __restrict__ out_dist, uint32_t* __restrict__ hit_leaf,
                                           int4* __restrict__ slot_rec, unsigned long long* __restrict__ counters) {
-  constexpr unsigned FULL = 0xffffffffu;
-  constexpr int DONE = INT_MIN;
-  constexpr int kShortN = kShort > 0 ? kShort : 1;
-  __shared__ int s_ref[kShortN][128];
-  __shared__ float s_tn[kShortN][128];
-  const int lane = threadIdx.x & 31, tx = threadIdx.x;
-  unsigned long long* cursor = counters + 4;
-  bool active = false, exhausted = false;
-  uint32_t ray = 0, slot = 0;
-  F3 o{}, d{}, inv{}, ood{};
-  float tlimit = INFINITY;
-  HitResult best{-1, -1.0f, 0u, 0u, false};
-  int stack_ref[kStack - kShort];
-  float stack_tn[kStack - kShort];
-  int sp = 0, cur = DONE, cnt = 0;
-
-  auto pop = [&]() {
-    while (sp > 0) {
-      sp--;
-      const bool sh = kShort > 0 && sp < kShort;
-      if ((sh ? s_tn[sp][tx] : stack_tn[sp - kShort]) <= tlimit) {
-        int r = sh ? s_ref[sp][tx] : stack_ref[sp - kShort];
-        if (r < 0) {
-          int packed = ~r;
-          cnt = (packed & 7) + 1;
-          return ~(packed >> 3);
-        }
-        return r;
-      }
-    }
-    return DONE;
-  };
-  auto pack = [](int ref, int count) { return ref < 0 ? ~((~ref) << 3 | (count - 1)) : ref; };
-
-  while (true) {
-    unsigned want = __ballot_sync(FULL, !active && !exhausted);
-    if (want) {
-      int leader = __ffs(want) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(cursor, (unsigned long long)__popc(want));
-      base = __shfl_sync(FULL, base, leader);
-      if (!active && !exhausted) {
-        unsigned long long r = base + __popc(want & ((1u << lane) - 1));
-        if (r < n) {
-          slot = (uint32_t)r;
-          ray = order ? __ldg(&order[r]) : (uint32_t)r;
-          const float4* rp = reinterpret_cast<const float4*>(rays + ray);
-          float4 ro = __ldg(rp), rd = __ldg(rp + 1);
-          o = f3(ro);
-          d = f3(rd);
-          inv = safe_inv(d);
-          ood = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
-          tlimit = INFINITY;
-          best = {-1, -1.0f, 0u, 0u, false};
-          sp = 0;
-          cur = 0;
-          cnt = 0;
-          active = true;
-        } else {
-          exhausted = true;
-        }
-      }
-    }
-    if (!__any_sync(FULL, active)) break;
-
-    // Traversal steps, warp-uniform: a lane without a leaf to test walks until it finds
-    // one; meanwhile a lane that already holds one keeps walking inner nodes (its leaf
-    // postponed, as in Aila and Laine's speculative traversal), so fewer lanes idle. A
-    // lane stops when it reaches a second leaf. Pruning uses the limit before the
-    // postponed leaf, which only visits more candidates, never fewer.
-    int pl = DONE, pcnt = 0;  // the next leaf to test
-    while (true) {
-      const bool need = active && pl == DONE && cur != DONE;
-      if (!__any_sync(FULL, need)) break;
-      if (!(need || (active && cur >= 0))) continue;
-      if (cur < 0) {  // a leaf (only lanes that need one get here)
-        pl = cur;
-        pcnt = cnt;
-        cur = pop();
-        continue;
-      }
-      {
-        const float4* np = nodes + 2 * W * (size_t)cur;
-        float lo[3][W], hi[3][W];
-        int r[W], c[W];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-#pragma unroll
-          for (int q = 0; q < W / 4; q++) {
-            float4 l = __ldg(np + 2 * (W / 4) * k + q), h = __ldg(np + 2 * (W / 4) * k + W / 4 + q);
-            lo[k][4 * q] = l.x, lo[k][4 * q + 1] = l.y, lo[k][4 * q + 2] = l.z, lo[k][4 * q + 3] = l.w;
-            hi[k][4 * q] = h.x, hi[k][4 * q + 1] = h.y, hi[k][4 * q + 2] = h.z, hi[k][4 * q + 3] = h.w;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < W / 4; q++) {
-          int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6 * (W / 4) + q));
-          int4 cc = __ldg(reinterpret_cast<const int4*>(np + 7 * (W / 4) + q));
-          r[4 * q] = cr.x, r[4 * q + 1] = cr.y, r[4 * q + 2] = cr.z, r[4 * q + 3] = cr.w;
-          c[4 * q] = cc.x, c[4 * q + 1] = cc.y, c[4 * q + 2] = cc.z, c[4 * q + 3] = cc.w;
-        }
-        float tn[W];
-        int nh = 0;
-#pragma unroll
-        for (int j = 0; j < W; j++) {
-          float a0 = fmaf(lo[0][j], inv.x, -ood.x), b0 = fmaf(hi[0][j], inv.x, -ood.x);
-          float a1 = fmaf(lo[1][j], inv.y, -ood.y), b1 = fmaf(hi[1][j], inv.y, -ood.y);
-          float a2 = fmaf(lo[2][j], inv.z, -ood.z), b2 = fmaf(hi[2][j], inv.z, -ood.z);
-          float t0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), 0.0f));
-          float t1 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tlimit));
-          bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
-          tn[j] = h ? t0 : INFINITY;
-          nh += h ? 1 : 0;
-        }
-        // sorting network on registers (ties keep child order): near to far
-        auto cs = [&](int a, int b) {
-          if (tn[b] < tn[a]) {
-            float t = tn[a];
-            tn[a] = tn[b];
-            tn[b] = t;
-            int q = r[a];
-            r[a] = r[b];
-            r[b] = q;
-            q = c[a];
-            c[a] = c[b];
-            c[b] = q;
-          }
-        };
-        if constexpr (W == 4) {
-          cs(0, 1), cs(2, 3), cs(0, 2), cs(1, 3), cs(1, 2);
-        } else {  // Batcher's odd-even merge sort of eight (19 exchanges)
-          cs(0, 1), cs(2, 3), cs(4, 5), cs(6, 7);
-          cs(0, 2), cs(1, 3), cs(4, 6), cs(5, 7);
-          cs(1, 2), cs(5, 6);
-          cs(0, 4), cs(1, 5), cs(2, 6), cs(3, 7);
-          cs(2, 4), cs(3, 5);
-          cs(1, 2), cs(3, 4), cs(5, 6);
-        }
-        if (nh == 0) {
-          cur = pop();
-        } else {
-#pragma unroll
-          for (int k = W - 1; k >= 1; k--) {  // farthest first, so the nearer pop earlier
-            if (k < nh && sp < kStack) {
-              if (kShort > 0 && sp < kShort) {
-                s_ref[sp][tx] = pack(r[k], c[k]);
-                s_tn[sp][tx] = tn[k];
-              } else {
-                stack_ref[sp - kShort] = pack(r[k], c[k]);
-                stack_tn[sp - kShort] = tn[k];
-              }
-              sp++;
-            }
-          }
-          cur = r[0];
-          cnt = c[0];
-        }
-      }
-    }
-    if (active) {
-      if (pl != DONE) {
-        int first = ~pl;
-        for (int k = 0; k < pcnt; k++) {
-          const float4* tp = A.tris + 3 * (size_t)(first + k);
-          float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-          float t;
-          if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
-            uint32_t leaf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
-            if (!best.hit || t < best.t ||
-                (t == best.t && (leaf > best.leaf || (leaf == best.leaf && pos < best.pos)))) {
-              best = {__float_as_int(v0.w), t, leaf, pos, true};
-              tlimit = t + A.prune_rel * (1.0f + t);
-            }
-          }
-        }
-        // (the next node was popped under the limit before this leaf's test: a looser
-        // limit only visits more candidates, never fewer)
-      }
-    }
-
-    if (active && cur == DONE) {
-      if (slot_rec) {  // one 16-byte record by binned slot; the check scatters it to ray order
-        slot_rec[slot] = make_int4(best.hit ? best.tid : -1, __float_as_int(best.hit ? best.t : -1.0f),
-                                   (int)(best.hit ? best.leaf : kNoLeaf), 0);
-      } else {
-        out_tid[ray] = best.hit ? best.tid : -1;
-        out_dist[ray] = best.hit ? best.t : -1.0f;
-        hit_leaf[ray] = best.hit ? best.leaf : kNoLeaf;
-      }
-      active = false;
-    }
-  }
+  HitLane L{A, rays, n, order, out_tid, out_dist, hit_leaf, slot_rec, nodes};
+  walk_persistent<W, kShort, kStack>(L, counters + 4);
 }
 
 // 4-wide walk: 128-byte nodes; at most 3 stack entries per level of a tree shallower

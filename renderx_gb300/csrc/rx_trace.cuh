@@ -21,10 +21,6 @@ namespace rx {
 
 constexpr int kStack = kStackDepth;
 
-__device__ __forceinline__ F3 safe_inv(F3 d) {
-  auto iv = [](float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysignf(1e30f, x); };
-  return {iv(d.x), iv(d.y), iv(d.z)};
-}
 
 // Reference visibility of a triangle in reference leaf `leaf`: every box on the root
 // path passes KDTree.cpp:34-52. The root path comes from the per-leaf ancestor list,

@@ -198,3 +198,16 @@ def test_guiding_gain_on_glossy_workload():
     e_guided = _relmse(guided, ref) * sg["ms"]
     print(f"relMSE x ms: plain {e_plain:.4g} ({sp['ms']:.1f} ms), guided {e_guided:.4g} ({sg['ms']:.1f} ms)")
     assert e_guided < 0.6 * e_plain, (e_guided, e_plain)
+
+
+def test_tensor_core_issue_rate_is_measured():
+    """rx_diag_umma_rate: back-to-back BF16 MMAs (M = 128, K = 16) from one thread. The
+    cycles per MMA grow with N and stay within the tensor core's bounds: an MMA of
+    N = 256 (524,288 multiply-adds) cannot take less than 64 cycles on a core of at most
+    8,192 multiply-adds per cycle, and none of the shapes takes 2,000."""
+    with rx.Context(0) as ctx:
+        rates = {n: ctx.diag_umma_rate(n, 256) for n in (64, 128, 256)}
+    for n, (issue, done) in rates.items():
+        assert 0 < issue <= done < 2000, (n, issue, done)
+    assert rates[64][1] <= rates[256][1] and rates[256][1] >= 64
+
