@@ -162,7 +162,7 @@ class Context:
         self.set_objects(objects_from_scene(scene))
         return f
 
-    def build_accel(self, split_policy: int = SPLIT_GCC, leaf_size: int = 4, host_threads: int = 0):
+    def build_accel(self, split_policy: int = SPLIT_GCC, leaf_size: int = 0, host_threads: int = 0):
         o = rx_build_options(split_policy, leaf_size, host_threads, 0)
         self._ck(self._L.rx_build_accel(self.h, ctypes.byref(o)))
 

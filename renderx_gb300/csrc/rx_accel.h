@@ -57,9 +57,20 @@ bool build_bvh(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t n
 // 4-wide BVH collapsed from the binary one: each node holds up to four children (inner
 // nodes or leaves of the binary tree), found by repeatedly opening the child with the
 // largest surface area. Node layout on the device: 8 float4 = 128 B (lo.x, hi.x, lo.y,
-// hi.y, lo.z, hi.z of the four children, then child refs and leaf counts; an empty
-// child slot has ref kBvh4Empty).
+// hi.y, lo.z, hi.z of the four children, then the four child refs, then four spare
+// words, zero). A child ref is an inner node's index (>= 0), a leaf packed with its
+// triangle count as ~(first_slot << 3 | (count - 1)) (negative; counts 1..8, slots below
+// 2^28: the walks' stack entries use the same packing, so refs are pushed as they are),
+// or kBvh4Empty for an empty slot.
 constexpr int32_t kBvh4Empty = 0x7fffffff;
+#ifdef __CUDACC__
+#define RX_HD __host__ __device__
+#else
+#define RX_HD
+#endif
+RX_HD inline int32_t pack_leaf(int32_t first_slot, int32_t count) { return ~((first_slot << 3) | (count - 1)); }
+RX_HD inline int32_t leaf_first(int32_t packed) { return (~packed) >> 3; }
+RX_HD inline int32_t leaf_count(int32_t packed) { return ((~packed) & 7) + 1; }
 struct Bvh4 {
   std::vector<float> data;  // 32 floats per node
   int max_depth = 0;
@@ -67,7 +78,7 @@ struct Bvh4 {
 };
 void collapse_bvh4(const Bvh& b2, Bvh4& out);
 // The same with up to eight children per node: 16 float4 = 256 B per node (lo.x, hi.x,
-// lo.y, hi.y, lo.z, hi.z of the eight children, then refs and leaf counts).
+// lo.y, hi.y, lo.z, hi.z of the eight children, then eight packed refs, eight spare).
 void collapse_bvh8(const Bvh& b2, Bvh4& out);
 
 }  // namespace rx

@@ -557,15 +557,10 @@ int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
   const int32_t me = (int32_t)(out.data.size() / kF);
   out.data.resize(out.data.size() + kF, 0.0f);
   out.max_depth = std::max(out.max_depth, depth);
-  int32_t refs[W], counts[W];
-  for (int j = 0; j < W; j++) {
-    refs[j] = kBvh4Empty;
-    counts[j] = 0;
-  }
-  for (size_t j = 0; j < kids.size(); j++) {
-    refs[j] = kids[j].ref >= 0 ? collapse<W>(b2, kids[j].ref, depth + 1, out) : kids[j].ref;
-    counts[j] = kids[j].count;
-  }
+  int32_t refs[W];
+  for (int j = 0; j < W; j++) refs[j] = kBvh4Empty;
+  for (size_t j = 0; j < kids.size(); j++)  // inner node index, or the leaf packed with its count
+    refs[j] = kids[j].ref >= 0 ? collapse<W>(b2, kids[j].ref, depth + 1, out) : pack_leaf(~kids[j].ref, kids[j].count);
   float* f = out.data.data() + kF * (size_t)me;  // after the recursion: data may have moved
   for (int j = 0; j < W; j++) {
     bool has = j < (int)kids.size();
@@ -573,8 +568,7 @@ int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
       f[2 * W * k + j] = has ? kids[j].lo[k] : 0.0f;
       f[2 * W * k + W + j] = has ? kids[j].hi[k] : 0.0f;
     }
-    std::memcpy(&f[6 * W + j], &refs[j], 4);
-    std::memcpy(&f[7 * W + j], &counts[j], 4);
+    std::memcpy(&f[6 * W + j], &refs[j], 4);  // f[7 W + j]: spare, zero
   }
   return me;
 }

@@ -112,12 +112,13 @@ rx_status rx_scene_set_objects(rx_context* c, const rx_object* objs, uint32_t no
 rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   if (!c) return RX_ERR_INVALID;
   if (c->tris.empty()) return c->fail(RX_ERR_STATE, "no geometry");
-  rx_build_options o{0, 4, 0, 0};
+  rx_build_options o{0, 0, 0, 0};
   if (opts) o = *opts;
   if (o.split_policy != 0 && o.split_policy != 1) return c->fail(RX_ERR_INVALID, "split_policy must be 0 or 1");
-  if (o.leaf_size <= 0) o.leaf_size = 4;
+  if (o.leaf_size <= 0) o.leaf_size = 3;
   if (o.leaf_size > 8) return c->fail(RX_ERR_INVALID, "leaf_size must be 1..8");
   uint32_t nv = (uint32_t)(c->verts.size() / 3), nt = (uint32_t)(c->tris.size() / 3);
+  if (nt >= (1u << 28)) return c->fail(RX_ERR_UNSUPPORTED, "at most 2^28 - 1 triangles (packed leaf refs)");
   if (!rx::build_ref_order(c->verts.data(), nv, c->tris.data(), nt, o.split_policy, o.host_threads, c->ref))
     return c->fail(RX_ERR_INVALID, "reference-order build failed");
   if (!rx::build_bvh(c->verts.data(), nv, c->tris.data(), nt, o.leaf_size, o.host_threads, c->bvh))

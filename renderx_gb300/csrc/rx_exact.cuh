@@ -112,25 +112,23 @@ __device__ __forceinline__ int box_clear_pass(F3 mn, F3 mx, F3 o, F3 d, F3 inv) 
   float t0x = __fmul_rn(__fsub_rn(mn.x, o.x), inv.x), t1x = __fmul_rn(__fsub_rn(mx.x, o.x), inv.x);
   float t0y = __fmul_rn(__fsub_rn(mn.y, o.y), inv.y), t1y = __fmul_rn(__fsub_rn(mx.y, o.y), inv.y);
   float t0z = __fmul_rn(__fsub_rn(mn.z, o.z), inv.z), t1z = __fmul_rn(__fsub_rn(mx.z, o.z), inv.z);
-  float tn[3] = {fminf(t0x, t1x), fminf(t0y, t1y), fminf(t0z, t1z)};
-  float tf[3] = {fmaxf(t0x, t1x), fmaxf(t0y, t1y), fmaxf(t0z, t1z)};
-  int ae = tn[0] >= tn[1] ? (tn[0] >= tn[2] ? 0 : 2) : (tn[1] >= tn[2] ? 1 : 2);
-  int ax = tf[0] <= tf[1] ? (tf[0] <= tf[2] ? 0 : 2) : (tf[1] <= tf[2] ? 1 : 2);
+  const float nx = fminf(t0x, t1x), ny = fminf(t0y, t1y), nz = fminf(t0z, t1z);
+  const float fx = fmaxf(t0x, t1x), fy = fmaxf(t0y, t1y), fz = fmaxf(t0z, t1z);
+  const float te = max3f(nx, ny, nz), tx = min3f(fx, fy, fz);  // entry and exit faces
 #pragma unroll
   for (int f = 0; f < 2; f++) {
-    int a = f == 0 ? ae : ax;
-    float t = f == 0 ? tn[a] : tf[a];
+    const float t = f == 0 ? te : tx;
     if (!(t >= 0.0f)) continue;
-    bool ok = true;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      if (k == a) continue;
-      float ok_ = comp(o, k), td = t * comp(d, k);
-      float p = ok_ + td;
-      float delta = 4e-6f * (1.0f + fabsf(ok_) + fabsf(td));
-      ok &= (p >= comp(mn, k) + delta) && (p <= comp(mx, k) - delta);
-    }
-    if (ok) return 1;
+    // the face's axis (any axis that attains t: each is a face the ray meets at t), then
+    // the point on it inside the other two slabs with the margin, all three axes at once
+    const int a = f == 0 ? (nx == t ? 0 : (ny == t ? 1 : 2)) : (fx == t ? 0 : (fy == t ? 1 : 2));
+    const float tdx = t * d.x, tdy = t * d.y, tdz = t * d.z;
+    const float px = o.x + tdx, py = o.y + tdy, pz = o.z + tdz;
+    const float dx = 4e-6f * (1.0f + fabsf(o.x) + fabsf(tdx)), dy = 4e-6f * (1.0f + fabsf(o.y) + fabsf(tdy));
+    const float dz = 4e-6f * (1.0f + fabsf(o.z) + fabsf(tdz));
+    const bool inx = (px >= mn.x + dx) && (px <= mx.x - dx), iny = (py >= mn.y + dy) && (py <= mx.y - dy);
+    const bool inz = (pz >= mn.z + dz) && (pz <= mx.z - dz);
+    if ((inx || a == 0) && (iny || a == 1) && (inz || a == 2)) return 1;
   }
   return 0;
 }

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "rx_accel.h"
 #include "rx_exact.cuh"
 #include "rx_scene.h"
 
@@ -295,18 +296,18 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
   constexpr int kS = 64;
   int stack_ref[kS - SH];
   float stack_tn[kS - SH];
-  int sp = 0, cur = 0, cnt = 0;
+  int sp = 0, cur = 0;  // an inner node or a packed leaf (rx_accel.h)
   const bool cond = !(contact == -1 && inside == -1);
   while (true) {
     if (cur >= 0) {
       const float4* np = A.bvh4 + 8 * (size_t)cur;
       float4 lx = __ldg(np + ox), hx = __ldg(np + 1 - ox), ly = __ldg(np + 2 + oy), hy = __ldg(np + 3 - oy);
       float4 lz = __ldg(np + 4 + oz), hz = __ldg(np + 5 - oz);  // near (l) and far (h) planes
-      int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6)), cc = __ldg(reinterpret_cast<const int4*>(np + 7));
+      int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6));
       const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
       const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
       const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
-      int r[4] = {cr.x, cr.y, cr.z, cr.w}, c[4] = {cc.x, cc.y, cc.z, cc.w};
+      int r[4] = {cr.x, cr.y, cr.z, cr.w};
       float tn[4];
       int nh = 0;
 #pragma unroll
@@ -316,7 +317,7 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
         float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
         float t0 = fmaxf(max3f(a0, a1, a2), 0.0f);
         float t1 = fminf(min3f(b0, b1, b2), best.t);
-        bool h = r[j] != 0x7fffffff && t0 <= t1 * 1.0000005f;
+        bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
         tn[j] = h ? t0 : INFINITY;
         nh += h ? 1 : 0;
       }
@@ -328,9 +329,6 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
           int q = r[a];
           r[a] = r[b];
           r[b] = q;
-          q = c[a];
-          c[a] = c[b];
-          c[b] = q;
         }
       };
       cs(0, 1);
@@ -342,21 +340,19 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
 #pragma unroll
         for (int k = 3; k >= 1; k--)
           if (k < nh && sp < kS) {
-            const int e = r[k] < 0 ? ~((~r[k]) << 3 | (c[k] - 1)) : r[k];
-            if (SH > 0 && sp < SH) {
-              s_ref[sp][tx] = e;
+            if (SH > 0 && sp < SH) {  // packed refs go on the stack as they are
+              s_ref[sp][tx] = r[k];
               s_tn[sp][tx] = tn[k];
             } else {
-              stack_ref[sp - SH] = e;
+              stack_ref[sp - SH] = r[k];
               stack_tn[sp - SH] = tn[k];
             }
             sp++;
           }
         cur = r[0];
-        cnt = c[0];
         continue;
       }
-    } else if (leaf_test<ANY>(S, ~cur, cnt, o, d, cond, contact, inside, best)) {
+    } else if (leaf_test<ANY>(S, leaf_first(cur), leaf_count(cur), o, d, cond, contact, inside, best)) {
       return best;
     }
     bool found = false;
@@ -364,14 +360,7 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
       sp--;
       const bool sh = SH > 0 && sp < SH;
       if ((sh ? s_tn[sp][tx] : stack_tn[sp - SH]) <= best.t) {
-        int rr = sh ? s_ref[sp][tx] : stack_ref[sp - SH];
-        if (rr < 0) {
-          int packed = ~rr;
-          cur = ~(packed >> 3);
-          cnt = (packed & 7) + 1;
-        } else {
-          cur = rr;
-        }
+        cur = sh ? s_ref[sp][tx] : stack_ref[sp - SH];
         found = true;
         break;
       }

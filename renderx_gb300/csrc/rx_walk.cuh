@@ -3,7 +3,9 @@
 // path tracer's extension rays (rx_pt.cu). Warps stay resident and refill lanes whose
 // ray has finished from a cursor (one atomic per warp and refill), so a warp never idles
 // behind its longest ray. One node visit tests W child boxes, visits the nearest hit
-// child next and stacks the others far to near with their entry distances.
+// child next and stacks the others far to near with their entry distances. Child refs
+// come packed from the node (a leaf's first triangle and count in one word, rx_accel.h)
+// and go on the stack as they are; a leaf is unpacked when its triangles are tested.
 //
 // Traversal steps are warp-uniform: a lane without a leaf to test walks until it finds
 // one; meanwhile a lane that already holds one keeps walking inner nodes (its leaf
@@ -27,11 +29,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "rx_accel.h"
 #include "rx_exact.cuh"
 
 namespace rx {
-
-constexpr int kWideEmpty = 0x7fffffff;  // child slot without a child (rx_accel.h kBvh4Empty)
 
 template <int W, int kShort, int kStack, class Lane>
 __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cursor) {
@@ -46,26 +47,17 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
   int near_bits = 0;  // bit k: the near plane of axis k is the upper bound
   int stack_ref[kStack - kShort];
   float stack_tn[kStack - kShort];
-  int sp = 0, cur = DONE, cnt = 0;
+  int sp = 0, cur = DONE;  // cur: an inner node, a packed leaf, or DONE
 
   auto pop = [&]() {
     const float lim = L.limit();
     while (sp > 0) {
       sp--;
       const bool sh = kShort > 0 && sp < kShort;
-      if ((sh ? s_tn[sp][tx] : stack_tn[sp - kShort]) <= lim) {
-        int r = sh ? s_ref[sp][tx] : stack_ref[sp - kShort];
-        if (r < 0) {
-          int packed = ~r;
-          cnt = (packed & 7) + 1;
-          return ~(packed >> 3);
-        }
-        return r;
-      }
+      if ((sh ? s_tn[sp][tx] : stack_tn[sp - kShort]) <= lim) return sh ? s_ref[sp][tx] : stack_ref[sp - kShort];
     }
     return DONE;
   };
-  auto pack = [](int ref, int count) { return ref < 0 ? ~((~ref) << 3 | (count - 1)) : ref; };
 
   while (true) {
     const unsigned want = __ballot_sync(FULL, !active && !exhausted);
@@ -84,7 +76,6 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
           near_bits = (inv.x < 0.0f ? 1 : 0) | (inv.y < 0.0f ? 2 : 0) | (inv.z < 0.0f ? 4 : 0);
           sp = 0;
           cur = 0;
-          cnt = 0;
           active = true;
         } else {
           exhausted = true;
@@ -93,20 +84,19 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
     }
     if (!__any_sync(FULL, active)) break;
 
-    int pl = DONE, pcnt = 0;  // the next leaf to test
+    int pl = DONE;  // the next leaf to test (packed)
     while (true) {
       const bool need = active && pl == DONE && cur != DONE;
       if (!__any_sync(FULL, need)) break;
       if (!(need || (active && cur >= 0))) continue;
       if (cur < 0) {  // a leaf (only lanes that need one get here)
         pl = cur;
-        pcnt = cnt;
         cur = pop();
         continue;
       }
       const float4* np = L.nodes() + 2 * W * (size_t)cur;
       float nr[3][W], fr[3][W];  // each child's near and far plane per axis
-      int r[W], c[W];
+      int r[W];
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         const int nb = (near_bits >> k) & 1, on = (W / 4) * nb, of = (W / 4) * (1 - nb);
@@ -120,9 +110,7 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
 #pragma unroll
       for (int q = 0; q < W / 4; q++) {
         int4 cr = __ldg(reinterpret_cast<const int4*>(np + 6 * (W / 4) + q));
-        int4 cc = __ldg(reinterpret_cast<const int4*>(np + 7 * (W / 4) + q));
         r[4 * q] = cr.x, r[4 * q + 1] = cr.y, r[4 * q + 2] = cr.z, r[4 * q + 3] = cr.w;
-        c[4 * q] = cc.x, c[4 * q + 1] = cc.y, c[4 * q + 2] = cc.z, c[4 * q + 3] = cc.w;
       }
       const float lim = L.limit();
       float tn[W];
@@ -136,7 +124,7 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
         float a2 = fmaf(nr[2][j], inv.z, -ood.z), b2 = fmaf(fr[2][j], inv.z, -ood.z);
         float t0 = fmaxf(max3f(a0, a1, a2), 0.0f);
         float t1 = fminf(min3f(b0, b1, b2), lim);
-        bool h = r[j] != kWideEmpty && t0 <= t1 * 1.0000005f;
+        bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
         tn[j] = h ? t0 : INFINITY;
         nh += h ? 1 : 0;
       }
@@ -149,9 +137,6 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
           int q = r[a];
           r[a] = r[b];
           r[b] = q;
-          q = c[a];
-          c[a] = c[b];
-          c[b] = q;
         }
       };
       if constexpr (W == 4) {
@@ -171,22 +156,21 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
         for (int k = W - 1; k >= 1; k--) {  // farthest first, so the nearer pop earlier
           if (k < nh && sp < kStack) {
             if (kShort > 0 && sp < kShort) {
-              s_ref[sp][tx] = pack(r[k], c[k]);
+              s_ref[sp][tx] = r[k];
               s_tn[sp][tx] = tn[k];
             } else {
-              stack_ref[sp - kShort] = pack(r[k], c[k]);
+              stack_ref[sp - kShort] = r[k];
               stack_tn[sp - kShort] = tn[k];
             }
             sp++;
           }
         }
         cur = r[0];
-        cnt = c[0];
       }
     }
     // (the next node was popped under the limit before this leaf's test: a looser limit
     // only visits more candidates, never fewer)
-    if (active && pl != DONE) L.leaf(~pl, pcnt, o, d);
+    if (active && pl != DONE) L.leaf(leaf_first(pl), leaf_count(pl), o, d);
     if (active && cur == DONE) {
       L.end();
       active = false;

@@ -17,7 +17,7 @@ def _bits_equal(a, b):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("leaf_size", [1, 4, 8])
+@pytest.mark.parametrize("leaf_size", [1, 3, 4, 8])
 @pytest.mark.parametrize("variant", [0, 1, 3, 4, 5])
 @pytest.mark.parametrize("check", [0, 1])
 def test_hits_match_reference_golden(name, leaf_size, variant, check):
