@@ -398,7 +398,7 @@ def section_batch(n: int = 64, small: bool = False):
                         + ", depth 16, 8 with the homogeneous medium",
             "paths": st["paths"], "ms": st["ms"], "mrays_per_s": rays / st["ms"] / 1e3,
             "samples_per_s": st["paths"] / st["ms"] * 1e3, "chosen_blocks_per_sm": st["blocks_per_sm"],
-            "chosen_stack": st["stack"], "one_by_one_ms": seq_ms,
+            "chosen_stack": st["stack"], "chosen_paths_per_pass": st["paths_per_pass"], "one_by_one_ms": seq_ms,
             "one_by_one_mrays_per_s": seq_rays / seq_ms / 1e3, "speedup_vs_one_by_one": seq_ms / st["ms"],
             "scene_generation_s": round(gen_s, 1), "accel_build_s": round(build_s, 1)}
 

@@ -141,8 +141,10 @@ typedef struct rx_batch_options {
   uint32_t paths_per_pass; /* wavefront size shared by all scenes, 0 = 2^22 */
   uint32_t use_graph;      /* 1: capture one pass as a CUDA graph and replay it */
   uint32_t autotune;       /* 1: time candidates on the first passes, two passes each (their
-                              samples count): the launch shapes at paths_per_pass, then the
-                              pass sizes 2^20..2^23 with the best shape. Guided batches take an
+                              samples count): the launch shapes at paths_per_pass (the
+                              4-wide short-stack walks, 6 and 5, when every scene's 4-wide
+                              tree fits, else the binary walks; 4, 8 or 16 shading blocks
+                              per SM), then the pass sizes 2^20..2^23 with the best shape. Guided batches take an
                               equal share of every item in each pass; autotuned ones do so in
                               the tuning passes only, then take the items one after another
                               (a pass then touches one or two scenes' trees). */

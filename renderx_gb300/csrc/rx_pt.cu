@@ -1037,9 +1037,12 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
   best.paths_per_pass = per_pass;
   std::vector<PtShape> cands;
   if (run.autotune) {
+    // the walks that can win: the two 4-wide short-stack walks when every scene's 4-wide
+    // tree fits (the binary walks and the all-local stack never did: each timing pass of
+    // a candidate renders real samples at that candidate's speed), else the binary walks
     for (int bps : {4, 8, 16})
-      for (int st : {kWalk4P, kWalk4S, kWalk4, 32, kStackDepth})
-        if (st == kWalk4 || st == kWalk4S || st == kWalk4P ? wide_ok : st > (int)max_bvh_depth)
+      for (int st : {kWalk4P, kWalk4S, 32, kStackDepth})
+        if (st == kWalk4S || st == kWalk4P ? wide_ok : !wide_ok && st > (int)max_bvh_depth)
           cands.push_back(PtShape{bps, st, per_pass});
     if (npasses < 2 * cands.size() + 2) cands.clear();
   }
