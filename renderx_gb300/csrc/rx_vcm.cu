@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "rx_bin.cuh"
+#include "rx_walk.cuh"
 #include "rx_internal.h"
 #include "rx_material.cuh"
 
@@ -867,21 +868,29 @@ __global__ void k_conn_fill(VcmParams P, const uint2* cmask, const unsigned long
   }
 }
 
-// One connection per lane (runs of kConnRun per thread, accumulated per pixel): the
-// joined path's colour, probability and MIS weight from the records, then the shadow
-// ray (testVisibility) for the contributions that are not zero.
+// A connection's shadow ray (testVisibility) and what it adds when nothing blocks it:
+// origin and length, direction and contact object, colour and inside object, pixel.
+struct ShadowQ {
+  float4 o_len;
+  float4 d_contact;
+  float4 col_inside;
+  int4 pixel;
+};
+
+// One connection per lane (runs of kConnRun per thread): the joined path's colour,
+// probability and MIS weight from the records; a contribution that is not zero queues its
+// shadow ray (testVisibility) in `sq` (one slot per connection at most), and the shadow
+// kernel that follows adds it to its pixel when nothing blocks it.
 constexpr int kConnRun = 4;
 __global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, const float4* lv, const float4* ev,
                                                    const MisL* lmis, const MisE* emis, const uint32_t* pair_q,
                                                    const int* pair_c, uint32_t npairs, float* img,
-                                                   unsigned long long* rays) {
+                                                   unsigned long long* rays, ShadowQ* sq, unsigned* sq_n) {
   const float r = P.radius;
   uint32_t stride = gridDim.x * blockDim.x;
   unsigned long long nrays = 0;
   for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kConnRun; base < npairs;
        base += stride * kConnRun) {
-    F3 acc = {0, 0, 0};
-    int acc_pixel = -1;
     for (uint32_t j = base; j < base + kConnRun && j < npairs; j++) {
       uint32_t q = pair_q[j];
       int ci = pair_c[j];
@@ -906,8 +915,7 @@ __global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, cons
       if (!(length(c) > 0.0f)) continue;
       float len = length(Ep.o - Lp.o);
       nrays++;
-      PHit sh = trace_cond<true>(S, Ep.o, Ep.d, len - 1e-5f, Ep.contact, Ep.inside);  // testVisibility
-      if (sh.tid >= 0) continue;
+      int target = p;
       if (k == 0) {  // light tracing: splat onto the pixel the light vertex projects to
         F3 dir = normalize(Lp.o - Ep.o);
         float ca = fabsf(dot(P.cam.front, dir));
@@ -917,19 +925,79 @@ __global__ void __launch_bounds__(128) k_conn_eval(DevScene S, VcmParams P, cons
         float px, py;
         trans_to_pixel(P.cam, Lp.o, px, py);
         int ix = (int)px, iy = (int)py;
-        if (ix >= 0 && ix < P.cam.width && iy >= 0 && iy < P.cam.height) img_add(img, iy * P.cam.width + ix, c);
-        continue;
+        target = ix >= 0 && ix < P.cam.width && iy >= 0 && iy < P.cam.height ? iy * P.cam.width + ix : -1;
       }
-      if (p != acc_pixel) {
-        if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
-        acc = {0, 0, 0};
-        acc_pixel = p;
-      }
-      acc = acc + c;
+      if (target < 0) continue;
+      // queue the shadow ray (testVisibility): the lanes here take their slots with one
+      // atomic
+      const unsigned m = __activemask();
+      const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+      unsigned slot = 0;
+      if (lane == leader) slot = atomicAdd(sq_n, (unsigned)__popc(m));
+      slot = __shfl_sync(m, slot, leader) + __popc(m & ((1u << lane) - 1));
+      sq[slot] = ShadowQ{make_float4(Ep.o.x, Ep.o.y, Ep.o.z, len - 1e-5f),
+                         make_float4(Ep.d.x, Ep.d.y, Ep.d.z, __int_as_float(Ep.contact)),
+                         make_float4(c.x, c.y, c.z, __int_as_float(Ep.inside)), make_int4(target, 0, 0, 0)};
     }
-    if (acc_pixel >= 0) img_add(img, acc_pixel, acc);
   }
   if (nrays) atomicAdd(rays, nrays);
+}
+
+// The queued shadow rays on persistent warps over the scene's 4-wide BVH (rx_walk.cuh):
+// any legal hit shorter than the connection (NoSelfIntersectionCondition, as trace_cond)
+// blocks it; an unblocked connection adds its colour to its pixel.
+struct ShadowLane {
+  const DevScene& S;
+  const ShadowQ* __restrict__ q;
+  uint32_t n;
+  float* img;
+  int contact = kNone, inside = kNone, target = 0;
+  bool cond = false, blocked = false;
+  float lim = 0.0f;
+  F3 col{};
+
+  __device__ bool begin(uint32_t r, F3& o, F3& d) {
+    if (r >= n) return false;
+    const ShadowQ e = q[r];
+    o = F3{e.o_len.x, e.o_len.y, e.o_len.z};
+    d = F3{e.d_contact.x, e.d_contact.y, e.d_contact.z};
+    lim = e.o_len.w;
+    contact = __float_as_int(e.d_contact.w);
+    inside = __float_as_int(e.col_inside.w);
+    col = F3{e.col_inside.x, e.col_inside.y, e.col_inside.z};
+    target = e.pixel.x;
+    cond = !(contact == kNone && inside == kNone);
+    blocked = false;
+    return true;
+  }
+  __device__ const float4* nodes() const { return S.accel.bvh4; }
+  __device__ float limit() const { return lim; }
+  __device__ void leaf(int first, int count, F3 o, F3 d) {
+    PHit b{-1, lim};
+    if (leaf_test<true>(S, first, count, o, d, cond, contact, inside, b)) {
+      blocked = true;
+      lim = -INFINITY;  // every remaining box and stack entry is pruned
+    }
+  }
+  __device__ void end() {
+    if (!blocked) img_add(img, target, col);
+  }
+};
+__global__ void __launch_bounds__(128, 8) k_shadow_wide(DevScene S, const ShadowQ* q, const unsigned* qn, float* img,
+                                                        unsigned long long* cursor) {
+  ShadowLane L{S, q, *qn, img};
+  walk_persistent<4, kShortStack, 64>(L, cursor);
+}
+// The same, one thread per queued ray over the binary BVH (when the 4-wide tree is too
+// deep for the persistent walk's stack).
+__global__ void __launch_bounds__(128) k_shadow_thread(DevScene S, const ShadowQ* q, const unsigned* qn, float* img) {
+  const uint32_t n = *qn;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const ShadowQ e = q[i];
+    PHit sh = trace_cond<true>(S, F3{e.o_len.x, e.o_len.y, e.o_len.z}, F3{e.d_contact.x, e.d_contact.y, e.d_contact.z},
+                               e.o_len.w, __float_as_int(e.d_contact.w), __float_as_int(e.col_inside.w));
+    if (sh.tid < 0) img_add(img, e.pixel.x, F3{e.col_inside.x, e.col_inside.y, e.col_inside.z});
+  }
 }
 
 // Per pixel: the eye subpath and colorByConnectingPaths by the reference's loops over each
@@ -1673,7 +1741,7 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   const unsigned cap = P.bpt ? 1u : P.n_light * P.maxv;  // photon capacity (none without merging)
   unsigned buckets = 1u << 16;
   while (buckets < cap && buckets < (1u << 26)) buckets <<= 1;
-  std::vector<DevBuf> bufs(32);
+  std::vector<DevBuf> bufs(33);
   cudaError_t e;
   auto al = [&](int k, size_t bytes) { return bufs[k].alloc(bytes); };
   if ((e = al(26, 16)) != cudaSuccess) return e;  // subpath cursors
@@ -1719,6 +1787,8 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
   unsigned* nph = reinterpret_cast<unsigned*>(ctr + 8);
   cudaMemsetAsync(ctr, 0, 64 * sizeof(unsigned long long), s);
   int grid = c->trace_cfg.sms * 4;
+  // shadow rays on the persistent 4-wide walk when the tree fits its stack
+  const bool wide_shadow = c->d_bvh4.p && 3 * c->bvh4.max_depth + 1 <= 64;
   int sub_grid[2] = {0, 0};  // resident blocks of k_sub_run<false>, <true>
   {
     int per = 0;
@@ -1811,13 +1881,26 @@ cudaError_t render_vcm(rx_context* c, const rx_camera& cam, const rx_vcm_options
                                           bufs[13].as<int>(), bufs[20].as<MisE>(), bufs[21].as<uint2>(), qc,
                                           bufs[10].as<float>());
       if ((e = scan_total(P.n_pixels, total)) != cudaSuccess) return e;
+      // the shadow-ray queue: at most one ray per connection of a window
+      const size_t sq_bytes = (size_t)std::min<unsigned long long>(pair_alloc, std::max(total, 1ull)) * sizeof(ShadowQ);
+      if (bufs[32].bytes < sq_bytes && (e = bufs[32].alloc(sq_bytes)) != cudaSuccess) return e;
+      unsigned* sq_n = reinterpret_cast<unsigned*>(ctr + 13);
+      unsigned long long* sq_cursor = ctr + 12;
       for (unsigned long long w0 = 0; w0 < total; w0 += pair_alloc) {
         uint32_t np = (uint32_t)std::min<unsigned long long>(pair_alloc, total - w0);
         k_conn_fill<<<grid * 4, 128, 0, s>>>(P, bufs[21].as<uint2>(), qo, w0, pair_alloc, bufs[17].as<uint32_t>(),
                                              bufs[18].as<int>());
+        cudaMemsetAsync(sq_n, 0, sizeof(unsigned), s);
         k_conn_eval<<<grid * 2, 128, 0, s>>>(S, P, bufs[0].as<float4>(), bufs[12].as<float4>(), bufs[19].as<MisL>(),
                                              bufs[20].as<MisE>(), bufs[17].as<uint32_t>(), bufs[18].as<int>(), np,
-                                             bufs[10].as<float>(), ctr + 2);
+                                             bufs[10].as<float>(), ctr + 2, bufs[32].as<ShadowQ>(), sq_n);
+        if (wide_shadow) {  // persistent: the blocks that stay resident (8 per SM)
+          cudaMemsetAsync(sq_cursor, 0, sizeof(unsigned long long), s);
+          k_shadow_wide<<<c->trace_cfg.sms * 8, 128, 0, s>>>(S, bufs[32].as<ShadowQ>(), sq_n, bufs[10].as<float>(),
+                                                            sq_cursor);
+        } else {
+          k_shadow_thread<<<grid * 2, 128, 0, s>>>(S, bufs[32].as<ShadowQ>(), sq_n, bufs[10].as<float>());
+        }
       }
     }
     if (P.bpt) {
