@@ -1173,9 +1173,12 @@ cudaError_t render_pt_jobs(rx_context* c, const PtJob* jobs, int nj, const PtRun
     inter = false;
   }
 
-  // the remaining passes: one captured pass replayed, or enqueued one by one
+  // the remaining passes: one captured pass replayed, or enqueued one by one (a single
+  // remaining pass is enqueued: capturing and instantiating a graph to replay it once
+  // costs more than its launches, and the GPU would wait for the instantiation)
   auto left = [&]() { return done_all < total; };
-  if (run.use_graph && left()) {
+  const bool several = total - done_all > (uint64_t)per_pass;
+  if (run.use_graph && left() && several) {
     Graph graph;
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
     cudaError_t eq = enqueue_pass_shape(W, best, sms, s);
