@@ -58,7 +58,8 @@ bool build_bvh(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t n
 // nodes or leaves of the binary tree), found by repeatedly opening the child with the
 // largest surface area. Node layout on the device: 8 float4 = 128 B (lo.x, hi.x, lo.y,
 // hi.y, lo.z, hi.z of the four children, then the four child refs, then four spare
-// words, zero). A child ref is an inner node's index (>= 0), a leaf packed with its
+// words, zero; an empty child slot has the inverted box lo = +inf, hi = -inf, which every
+// slab test rejects, and ref kBvh4Empty). A child ref is an inner node's index (>= 0), a leaf packed with its
 // triangle count as ~(first_slot << 3 | (count - 1)) (negative; counts 1..8, slots below
 // 2^28: the walks' stack entries use the same packing, so refs are pushed as they are),
 // or kBvh4Empty for an empty slot.

@@ -564,9 +564,9 @@ int32_t collapse(const Bvh& b2, int32_t n2, int depth, Bvh4& out) {
   float* f = out.data.data() + kF * (size_t)me;  // after the recursion: data may have moved
   for (int j = 0; j < W; j++) {
     bool has = j < (int)kids.size();
-    for (int k = 0; k < 3; k++) {
-      f[2 * W * k + j] = has ? kids[j].lo[k] : 0.0f;
-      f[2 * W * k + W + j] = has ? kids[j].hi[k] : 0.0f;
+    for (int k = 0; k < 3; k++) {  // an empty slot is an inverted box: no ray enters it
+      f[2 * W * k + j] = has ? kids[j].lo[k] : INFINITY;
+      f[2 * W * k + W + j] = has ? kids[j].hi[k] : -INFINITY;
     }
     std::memcpy(&f[6 * W + j], &refs[j], 4);  // f[7 W + j]: spare, zero
   }

@@ -317,7 +317,7 @@ __device__ __forceinline__ PHit trace_cond4(const DevScene& S, F3 o, F3 d, float
         float a2 = fmaf(lza[j], inv.z, -ood.z), b2 = fmaf(hza[j], inv.z, -ood.z);
         float t0 = fmaxf(max3f(a0, a1, a2), 0.0f);
         float t1 = fminf(min3f(b0, b1, b2), best.t);
-        bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
+        bool h = t0 <= t1 * 1.0000005f;  // an empty slot's inverted box gives t0 = +inf, t1 = -inf
         tn[j] = h ? t0 : INFINITY;
         nh += h ? 1 : 0;
       }

@@ -124,7 +124,7 @@ __device__ __forceinline__ void walk_persistent(Lane& L, unsigned long long* cur
         float a2 = fmaf(nr[2][j], inv.z, -ood.z), b2 = fmaf(fr[2][j], inv.z, -ood.z);
         float t0 = fmaxf(max3f(a0, a1, a2), 0.0f);
         float t1 = fminf(min3f(b0, b1, b2), lim);
-        bool h = r[j] != kBvh4Empty && t0 <= t1 * 1.0000005f;
+        bool h = t0 <= t1 * 1.0000005f;  // an empty slot's inverted box gives t0 = +inf, t1 = -inf
         tn[j] = h ? t0 : INFINITY;
         nh += h ? 1 : 0;
       }
