@@ -1,11 +1,16 @@
 // The persistent walk over a W-wide BVH (W = 4: 128-byte nodes, one cache line; W = 8:
-// 256-byte nodes, half the levels), shared by the closest-hit batch (rx_trace.cu) and the
-// path tracer's extension rays (rx_pt.cu). Warps stay resident and refill lanes whose
+// 256-byte nodes, half the levels), shared by the closest-hit batch (rx_trace.cu), the
+// path tracer's extension rays (rx_pt.cu) and the connections' shadow rays (rx_vcm.cu,
+// any hit). Warps stay resident and refill lanes whose
 // ray has finished from a cursor (one atomic per warp and refill), so a warp never idles
 // behind its longest ray. One node visit tests W child boxes, visits the nearest hit
 // child next and stacks the others far to near with their entry distances. Child refs
 // come packed from the node (a leaf's first triangle and count in one word, rx_accel.h)
 // and go on the stack as they are; a leaf is unpacked when its triangles are tested.
+// Each axis's near plane is picked once per ray by the sign of its inverse direction and
+// loaded as such, so the slab values need no ordering; an empty child slot holds an
+// inverted box that the slab test rejects by itself. An any-hit policy ends its ray by
+// returning a limit below every entry distance.
 //
 // Traversal steps are warp-uniform: a lane without a leaf to test walks until it finds
 // one; meanwhile a lane that already holds one keeps walking inner nodes (its leaf
