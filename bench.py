@@ -446,10 +446,25 @@ def section_vcm(peak, iters: int = 32, res: int = 512, light_paths: int = 1 << 2
                 "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                 "kernel": "k_merge_walk + k_merge_eval (merge gather)",
                 "algorithmic_bytes_per_iteration": alg // iters},
-            "cpu_baseline": None,
-            "cpu_baseline_note": "not measured on the GPU machine: the reference's VCMTracer runs only from its own "
-                                 "sources, which are not there, and the oracle restates its PathTracer, not VCM",
+            "cpu_baseline": vcm_cpu_reference(),
             "image_mean": [float(x) for x in img.mean(axis=(0, 1))]}
+
+
+def vcm_cpu_reference():
+    """The reference's own VCMTracer on the same scene at 512^2, as recorded by
+    tests/golden/make_cpu_reference_timing.py on the build machine: its sources are not on
+    the GPU machine, so it cannot be timed beside the GPU run, and the oracle restates
+    PathTracer, not VCM. The reference traces width x height light paths per iteration."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "cpu_reference_vcm_512.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        rec = json.load(fh)
+    return {"value": rec["ms_per_iteration"], "unit": "ms per iteration", "cores": rec["threads"],
+            "kind": "reference", "measured_on": rec["machine"],
+            "sample": f"{rec['iterations']} iterations of {rec['implementation']}, {rec['workload']}, "
+                      f"{rec['light_paths_per_iteration']} light paths per iteration",
+            "recorded_by": "tests/golden/make_cpu_reference_timing.py"}
 
 
 def section_bpt(spp: int = 4, res: int = 512):

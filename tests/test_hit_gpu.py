@@ -135,7 +135,7 @@ def test_full_size_batch_matches_oracle_sample_and_reference_walk():
     passes, in the reference's order, with no BVH, no pruning and no visibility check, so
     it costs nearly a brute-force test per ray; only the exact box and triangle
     arithmetic, pinned to the goldens, is shared); the whole batch twice for determinism, through every walk
-    variant, and once more from host buffers (two chunks over two streams)."""
+    variant and check mode, and once more from host buffers (staged chunks)."""
     torch = pytest.importorskip("torch")
     sc = scenes.sphere_field(200, 5, seed=1)
     f = sc.flatten()
@@ -158,6 +158,11 @@ def test_full_size_batch_matches_oracle_sample_and_reference_walk():
             torch.cuda.synchronize()
             assert torch.equal(tid, tid2) and torch.equal(dist.view(torch.int32), dist2.view(torch.int32)), variant
         ctx.set_trace_config(4, 12)
+        ctx.set_trace_options(0)  # the warp-per-ray check: the same answers as thread per ray
+        ctx.trace_closest_device(rays, n, tid2, dist2)
+        torch.cuda.synchronize()
+        assert torch.equal(tid, tid2) and torch.equal(dist.view(torch.int32), dist2.view(torch.int32))
+        ctx.set_trace_options(1)
         m = 1 << 18
         tr = torch.empty(m, dtype=torch.int32, device="cuda")
         dr = torch.empty(m, dtype=torch.float32, device="cuda")
