@@ -389,9 +389,11 @@ rx_status rx_trace_set_config(rx_context* ctx, int32_t variant, int32_t blocks_p
  * BVH is shallower than 32 levels, else 64 (default 0); 64 = always 64. Answers depend
  * on none of them. */
 rx_status rx_trace_set_options(rx_context* ctx, int32_t check_mode, uint32_t bin_min, int32_t walk_stack);
-/* Host-buffer rx_trace_closest: rays per staged chunk; chunks alternate between two
- * streams so one chunk's copies overlap the other's walk. 0 = the default (2^23),
- * otherwise at least 65,536. Answers do not depend on it. No reference counterpart. */
+/* Host-buffer rx_trace_closest: rays per staged chunk; chunks rotate through three
+ * device slots, each with its own kernel stream, so one chunk's copies overlap other
+ * chunks' kernels and the next chunk's walk fills the tail of the last. 0 = the default
+ * (2^22), otherwise at least 65,536. Answers do not depend on it. No reference
+ * counterpart. */
 rx_status rx_trace_set_staging(rx_context* ctx, uint32_t chunk_rays);
 /* Per-kernel device timing of rx_trace_closest_device calls: the next max_calls calls
  * record CUDA events around their three kernels (walk, reference-visibility check,

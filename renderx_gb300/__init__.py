@@ -303,7 +303,7 @@ class Context:
         self._ck(self._L.rx_set_snapshots(self.h, float(every_s), self._snap_cb, None))
 
     def set_trace_staging(self, chunk_rays: int = 0):
-        """Rays per staged chunk of the host-buffer call (0 = default 2^23)."""
+        """Rays per staged chunk of the host-buffer call (0 = default 2^22)."""
         self._ck(self._L.rx_trace_set_staging(self.h, int(chunk_rays)))
 
     def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18, walk_stack: int = 0):

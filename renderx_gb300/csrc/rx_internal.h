@@ -163,10 +163,12 @@ struct rx_context {
   rx::DevBuf d_counters;     // 4 x u64 diagnostics + per-slot queue lengths
   rx::DevBuf d_queue;        // closest-hit scratch (winner leaves + eager queue)
   // staging ring for host-buffer calls
-  rx::DevBuf ring_rays[2], ring_tid[2], ring_dist[2], ring_queue[2], ring_counters[2];
-  cudaEvent_t ring_ev[2][3] = {};  // per slot: rays copied in, traced, results copied out
+  static constexpr int kRing = 3;  // staging slots of the host-buffer trace
+  rx::DevBuf ring_rays[kRing], ring_tid[kRing], ring_dist[kRing], ring_queue[kRing], ring_counters[kRing];
+  cudaEvent_t ring_ev[kRing][3] = {};       // per slot: rays copied in, traced, results copied out
+  cudaStream_t ring_stream[kRing] = {};     // per slot: the kernels of its chunks
   size_t ring_chunk = 0;
-  size_t stage_rays = (size_t)1 << 23;  // rays per staged chunk (rx_trace_set_staging)
+  size_t stage_rays = (size_t)1 << 22;  // rays per staged chunk (rx_trace_set_staging)
   // per-kernel timing of device-buffer closest-hit calls (rx_trace_set_timing)
   std::vector<cudaEvent_t> timing_ev;  // 4 per recorded call
   size_t timing_used = 0;

@@ -102,10 +102,11 @@ def test_invalid_inputs_raise():
 
 @pytest.mark.parametrize("stage,n", [(1 << 16, 5 * (1 << 16) + 77), (1 << 20, 3 * (1 << 20) + 12345)])
 def test_host_buffer_ring_matches_device_path(stage, n):
-    """The host-buffer call stages the rays through a two-slot ring on three streams
-    (copies in, kernels, copies out, ordered by events) in chunks that ramp up to the
-    staging size: equal chunks of 2^16 (five and a ragged tail, each slot reused), and
-    2^18, 2^19, 2^20, 2^20 plus a tail. Every answer equals the device-buffer call's."""
+    """The host-buffer call stages the rays through a three-slot ring (copies in on one
+    stream, each slot's kernels on their own, copies out on another, ordered by events)
+    in chunks that ramp up to the staging size: equal chunks of 2^16 (five and a ragged
+    tail, each slot reused), and 2^18, 2^19, 2^20, 2^20 plus a tail. Every answer equals
+    the device-buffer call's."""
     torch = pytest.importorskip("torch")
     sc = scenes.sphere_field(20, 3, seed=2)
     f = sc.flatten()
