@@ -395,6 +395,14 @@ rx_status rx_trace_set_options(rx_context* ctx, int32_t check_mode, uint32_t bin
  * (2^22), otherwise at least 65,536. Answers do not depend on it. No reference
  * counterpart. */
 rx_status rx_trace_set_staging(rx_context* ctx, uint32_t chunk_rays);
+/* Closest-hit ray binning key (no reference counterpart; launch tuning): rays are sorted
+ * by the Morton code of their origin's cell on a 2^cell_bits per axis grid over the
+ * scene bounds (cell_bits 3..5), then by a direction bin: dir_map 0 = each component
+ * quantised to 2^dir_bits levels (dir_bits 1..3, cell_bits + dir_bits <= 7); 1 = the
+ * octahedral map of the direction on a 2^dir_bits square grid in Morton order (dir_bits
+ * 1..6, 3 cell_bits + 2 dir_bits <= 21). Default 4, 4, 1 (16^3 cells x 16^2 directions).
+ * Answers do not depend on it. */
+rx_status rx_trace_set_binning(rx_context* ctx, int32_t cell_bits, int32_t dir_bits, int32_t dir_map);
 /* Per-kernel device timing of rx_trace_closest_device calls: the next max_calls calls
  * record CUDA events around their three kernels (walk, reference-visibility check,
  * re-walk of rejected winners); 0 turns timing off. No reference counterpart

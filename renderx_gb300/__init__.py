@@ -306,6 +306,12 @@ class Context:
         """Rays per staged chunk of the host-buffer call (0 = default 2^22)."""
         self._ck(self._L.rx_trace_set_staging(self.h, int(chunk_rays)))
 
+    def set_trace_binning(self, cell_bits: int = 4, dir_bits: int = 4, dir_map: int = 1):
+        """Binning key of the closest-hit batch: 2^cell_bits origin cells per axis, then a
+        direction bin: 2^dir_bits levels per component (dir_map 0) or a 2^dir_bits square
+        grid over the octahedral map (dir_map 1)."""
+        self._ck(self._L.rx_trace_set_binning(self.h, int(cell_bits), int(dir_bits), int(dir_map)))
+
     def set_trace_options(self, check_mode: int = 1, bin_min: int = 1 << 18, walk_stack: int = 0):
         """Visibility check of each winner (1 = thread per ray, 0 = warp per ray), the
         batch size from which rays are binned before the walk (0 = never) and the walk

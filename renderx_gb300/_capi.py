@@ -126,6 +126,7 @@ SIGNATURES = [
     ("rx_trace_set_timing", S, [P, I32]),
     ("rx_trace_set_options", S, [P, I32, U32, I32]),
     ("rx_trace_set_staging", S, [P, U32]),
+    ("rx_trace_set_binning", S, [P, I32, I32, I32]),
     ("rx_diag_umma_gemm", S, [P, U32, U32, U32, I32, I32, P, P, P]),
     ("rx_diag_umma_rate", S, [P, U32, U32, P, P]),
     ("rx_guide_init", S, [P, P, P]),

@@ -625,6 +625,20 @@ rx_status rx_set_snapshots(rx_context* c, double every_s, rx_snapshot_fn fn, voi
   return RX_OK;
 }
 
+rx_status rx_trace_set_binning(rx_context* c, int32_t cell_bits, int32_t dir_bits, int32_t dir_map) {
+  if (!c) return RX_ERR_INVALID;
+  const bool ok = cell_bits >= 3 && cell_bits <= 5 && dir_bits >= 1 &&
+                  (dir_map == 0 ? dir_bits <= 3 && 3 * (cell_bits + dir_bits) <= 21
+                                : dir_map == 1 && dir_bits <= 6 && 3 * cell_bits + 2 * dir_bits <= 21);
+  if (!ok)
+    return c->fail(RX_ERR_INVALID, "binning: cell_bits 3..5; dir_map 0: dir_bits 1..3, cell_bits + dir_bits <= 7; "
+                                   "dir_map 1: dir_bits 1..6, 3 cell_bits + 2 dir_bits <= 21");
+  c->trace_cfg.bin_cell_bits = cell_bits;
+  c->trace_cfg.bin_dir_bits = dir_bits;
+  c->trace_cfg.bin_dir_map = dir_map;
+  return RX_OK;
+}
+
 rx_status rx_trace_set_staging(rx_context* c, uint32_t chunk_rays) {
   if (!c) return RX_ERR_INVALID;
   if (chunk_rays != 0 && chunk_rays < (1u << 16)) return c->fail(RX_ERR_INVALID, "chunk_rays: 0 or at least 65536");

@@ -26,6 +26,9 @@ struct TraceConfig {
   int pt_blocks_per_sm = 8;  // wavefront extend / shade kernels
   int check_thread = 1;      // reference-visibility check: 1 = thread per ray, 0 = warp per ray
   uint32_t bin_min = 1u << 18;  // bin rays before the walk from this batch size on (0 = never)
+  int bin_cell_bits = 4;        // binning key: 2^bits origin cells per axis (Morton order)
+  int bin_dir_bits = 4;         // and 2^bits direction levels per octahedral coordinate (or axis)
+  int bin_dir_map = 1;          // 1: octahedral map (2^20 bins); 0: direction components
   int walk_stack = 0;           // walk stack entries: 0 = 32 when the BVH is shallower, else 64
 };
 
@@ -42,8 +45,11 @@ struct PtShape {
 // Scratch of a closest-hit launch over n rays (rx_trace.cu): winner leaves, re-walk
 // queue, the ray binning's keys and permutation, the walk's answers by binned slot
 // (16 bytes a ray, 16-byte aligned), and bin counters.
-constexpr uint32_t kRayBins = 1u << 18;
-inline size_t trace_scratch_bytes(size_t n) { return n * 32 + (size_t)kRayBins * 4 + 4096; }
+constexpr uint32_t kRayBins = 1u << 18;     // the default key's bins (16^3 cells x 4^3 directions)
+constexpr uint32_t kRayBinsMax = 1u << 21;  // the finest key rx_trace_set_binning allows
+inline size_t trace_scratch_bytes(size_t n) {
+  return n * 32 + (size_t)(kRayBinsMax + kRayBinsMax / 1024) * 4 + 4096;
+}
 // Launchers (rx_trace.cu). `queue`: trace_scratch_bytes(n) bytes, or 8 n bytes when
 // `bin` is false. bin: reorder rays by origin cell and direction before the walk (for
 // large batches). `ev` (optional): four events recorded before the walk kernel, after

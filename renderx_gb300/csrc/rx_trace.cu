@@ -464,10 +464,10 @@ __global__ void __launch_bounds__(128) k_trace_reforder(DevAccel A, const rx_ray
 
 // ---- ray binning (rx_bin.cuh): counting sort by (origin cell, direction bin) --------
 __global__ void k_ray_keys(DevAccel A, const rx_ray* __restrict__ rays, uint32_t n, uint32_t* __restrict__ keys,
-                           uint32_t* __restrict__ hist) {
+                           uint32_t* __restrict__ hist, int cbits, int dbits, int dir_map) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4* rp = reinterpret_cast<const float4*>(rays + i);
-    uint32_t k = ray_key(A.lo, A.hi, __ldg(rp), __ldg(rp + 1));
+    uint32_t k = ray_key(A.lo, A.hi, __ldg(rp), __ldg(rp + 1), cbits, dbits, dir_map);
     keys[i] = k;
     atomicAdd(&hist[k], 1u);
   }
@@ -494,9 +494,11 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
     uint32_t* keys = queue + 2 * (size_t)n;
     uint32_t* perm = queue + 3 * (size_t)n;
     uint32_t* hist = queue + 8 * (size_t)n;
-    cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), s);
-    k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist);
-    scan_bins(hist, hist + kRayBins, s);
+    const uint32_t bins = 1u << (3 * cfg.bin_cell_bits + (cfg.bin_dir_map ? 2 : 3) * cfg.bin_dir_bits);
+    cudaMemsetAsync(hist, 0, bins * sizeof(uint32_t), s);  // at most kRayBinsMax
+    k_ray_keys<<<cfg.sms * 8, 256, 0, s>>>(A, rays, n, keys, hist, cfg.bin_cell_bits, cfg.bin_dir_bits,
+                                           cfg.bin_dir_map);
+    scan_bins(hist, hist + kRayBinsMax, s, bins);
     k_ray_scatter<<<cfg.sms * 8, 256, 0, s>>>(keys, n, nullptr, hist, perm);
     order = perm;
     if (cfg.check_thread)  // the walk writes its answers by slot: 16-byte records after perm

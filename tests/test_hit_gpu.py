@@ -98,6 +98,25 @@ def test_invalid_inputs_raise():
         v[0, 0] = np.nan
         with pytest.raises(rx.RxError):
             ctx.set_geometry(v, np.array([[0, 1, 2]], np.uint32))
+        for key in ((2, 2, 0), (6, 1, 0), (4, 4, 0), (5, 3, 0), (4, 5, 1), (3, 7, 1), (4, 2, 2)):  # out of range
+            with pytest.raises(rx.RxError):
+                ctx.set_trace_binning(*key)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("key", [(3, 1, 0), (3, 3, 0), (5, 2, 0), (4, 3, 0), (4, 4, 1), (3, 6, 1), (5, 1, 1)])
+def test_binning_key_does_not_change_answers(name, key):
+    """Every binning key the options allow orders the rays differently and returns the
+    reference's answers bit for bit (the golden batches, binned from 64 rays on)."""
+    z = load(name)
+    with rx.Context(0) as ctx:
+        ctx.set_trace_options(1, 64, 0)
+        ctx.set_trace_binning(*key)
+        ctx.set_geometry(z["verts"], z["tris"])
+        ctx.build_accel()
+        tid, dist = ctx.trace_closest(z["origins"], z["dirs"])
+    assert np.array_equal(tid, z["tid"])
+    assert _bits_equal(dist, z["dist"])
 
 
 @pytest.mark.parametrize("stage,n", [(1 << 16, 5 * (1 << 16) + 77), (1 << 20, 3 * (1 << 20) + 12345)])
