@@ -58,7 +58,7 @@ WORKLOAD = "hit_batch_2^24_rays_cornell+200_icospheres_4096036_tris"
 
 # DRAM bytes (read + write) of one walk-kernel launch over the 2^24-ray batch, from a
 # one-pass ncu capture of this workload
-TRAFFIC_BYTES_PER_RAY = (4324112640 + 289060096) / (1 << 24)
+TRAFFIC_BYTES_PER_RAY = (4315510528 + 288115456) / (1 << 24)
 
 
 def load_tflops():
