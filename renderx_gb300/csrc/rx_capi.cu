@@ -56,7 +56,7 @@ void rx_destroy(rx_context* c) {
   {
     DeviceGuard g(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf* b : {&c->d_bvh, &c->d_bvh4, &c->d_bvh8, &c->d_tris, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
+    for (DevBuf* b : {&c->d_bvh, &c->d_bvh4, &c->d_bvh8, &c->d_tris, &c->d_tri_nrm, &c->d_ref, &c->d_ref_leaf_node, &c->d_ref_leaf_range, &c->d_ref_tris,
                       &c->d_anc_range, &c->d_anc_nodes, &c->d_anc_box, &c->d_slot_n, &c->d_tri_v, &c->d_tri_n, &c->d_tri_obj,
                       &c->d_objects, &c->d_light_cdf, &c->d_light_tri,
                       &c->d_counters, &c->d_queue})
@@ -206,6 +206,15 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   if ((s = upload(c, c->d_bvh8, c->bvh8.data.data(), c->bvh8.data.size() * sizeof(float), "upload BVH8")) != RX_OK)
     return s;
   if ((s = upload(c, c->d_tris, slots.data(), slots.size() * sizeof(float4), "upload triangles")) != RX_OK) return s;
+  const uint32_t nslots = (uint32_t)(slots.size() / 3);
+  if ((s = c->cuda(c->d_tri_nrm.alloc((size_t)std::max<uint32_t>(nslots, 1) * sizeof(float4)), "triangle normals")) !=
+      RX_OK)
+    return s;
+  if ((s = c->cuda(rx::launch_slot_normals(c->d_tris.as<float4>(), nslots, c->d_tri_nrm.as<float4>(), c->stream),
+                   "triangle normals")) != RX_OK)
+    return s;
+  // traces may follow on any stream
+  if ((s = c->cuda(cudaStreamSynchronize(c->stream), "triangle normals")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref, refn.data(), refn.size() * sizeof(float4), "upload reference nodes")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref_leaf_node, leaf_node.data(), leaf_node.size() * 4, "upload leaf map")) != RX_OK) return s;
   if ((s = upload(c, c->d_ref_leaf_range, leaf_range.data(), leaf_range.size() * 4, "upload leaf ranges")) != RX_OK)
@@ -221,6 +230,7 @@ rx_status rx_build_accel(rx_context* c, const rx_build_options* opts) {
   rx::DevAccel& A = c->accel;
   A.bvh = c->d_bvh.as<float4>();
   A.tris = c->d_tris.as<float4>();
+  A.tri_nrm = c->d_tri_nrm.as<float4>();
   A.ref = c->d_ref.as<float4>();
   A.ref_leaf_node = c->d_ref_leaf_node.as<int32_t>();
   A.ref_leaf_range = c->d_ref_leaf_range.as<uint32_t>();

@@ -20,6 +20,7 @@ constexpr int kStackDepth = 64;
 struct DevAccel {
   const float4* bvh;
   const float4* tris;
+  const float4* tri_nrm;  // per triangle slot: xnormalize(xcross(v1 - v0, v2 - v1)) (k_slot_normals)
   const float4* ref;
   const int32_t* ref_leaf_node;
   const uint32_t* ref_leaf_range;  // 2 per leaf: [begin, end) in reference DFS order

@@ -63,7 +63,11 @@ __device__ __forceinline__ F3 xnormalize(F3 v) {
 // KDTree::intersect(ray, triangle) without a condition (KDTree.cpp:267-293). Returns
 // true when the reference accepts the triangle (distance >= 0; NaN never passes the
 // caller's `dist >= 0`), and the distance.
-__device__ __forceinline__ bool tri_exact(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float& t) {
+// `normal(l0, l1)` gives the triangle's unit normal, xnormalize(xcross(l0, l1)): formed
+// here, or read from the triangle's slot, where the same functions formed it once
+// (k_slot_normals) with the same bits.
+template <class Normal>
+__device__ __forceinline__ bool tri_exact_with(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float& t, Normal normal) {
   F3 l0 = xsub(v1, v0), l1 = xsub(v2, v1), l2 = xsub(v0, v2);
   F3 r0 = xsub(v0, o), r1 = xsub(v1, o), r2 = xsub(v2, o);
   float s0 = xdot(d, xcross(l0, r0));
@@ -72,7 +76,7 @@ __device__ __forceinline__ bool tri_exact(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float
   bool pos = (s0 >= 0.0f) & (s1 >= 0.0f) & (s2 >= 0.0f);
   bool neg = (s0 <= 0.0f) & (s1 <= 0.0f) & (s2 <= 0.0f);
   if (!(pos | neg)) return false;
-  F3 n = xnormalize(xcross(l0, l1));
+  F3 n = normal(l0, l1);
   float od = xdot(n, r2);
   float dd = xdot(n, d);
   if (dd == 0.0f) return false;
@@ -80,6 +84,14 @@ __device__ __forceinline__ bool tri_exact(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float
   if (!(q >= 0.0f)) return false;
   t = q;
   return true;
+}
+__device__ __forceinline__ bool tri_exact(F3 v0, F3 v1, F3 v2, F3 o, F3 d, float& t) {
+  return tri_exact_with(v0, v1, v2, o, d, t, [](F3 l0, F3 l1) { return xnormalize(xcross(l0, l1)); });
+}
+// The same test with the unit normal read from the triangle's slot (loaded only for
+// rays that pass the edge tests).
+__device__ __forceinline__ bool tri_exact_n(F3 v0, F3 v1, F3 v2, const float4* nrm, F3 o, F3 d, float& t) {
+  return tri_exact_with(v0, v1, v2, o, d, t, [nrm](F3, F3) { return f3(__ldg(nrm)); });
 }
 
 // KDTree::Node::BoundingBox::intersect (KDTree.cpp:34-52) reduced to pass/fail:

@@ -57,6 +57,8 @@ inline size_t trace_scratch_bytes(size_t n) {
 cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                  uint32_t* queue, unsigned long long* counters, const TraceConfig& cfg,
                                  cudaStream_t s, const cudaEvent_t* ev = nullptr, bool bin = true);
+// The unit normal of each of the BVH's triangle slots (3 float4 each), for tri_exact_n.
+cudaError_t launch_slot_normals(const float4* tris, uint32_t nslots, float4* nrm, cudaStream_t s);
 cudaError_t launch_trace_reforder(const DevAccel& A, const rx_ray* rays, uint32_t n, int32_t* tid, float* dist,
                                   unsigned long long* counters, cudaStream_t s);
 
@@ -162,7 +164,7 @@ struct rx_context {
   bool accel_ready = false;
   rx::Bvh4 bvh4, bvh8;
   rx::DevBuf d_bvh4, d_bvh8;
-  rx::DevBuf d_bvh, d_tris, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes, d_anc_box;
+  rx::DevBuf d_bvh, d_tris, d_tri_nrm, d_ref, d_ref_leaf_node, d_ref_leaf_range, d_ref_tris, d_anc_range, d_anc_nodes, d_anc_box;
   rx::DevScene scene{};
   bool scene_ready = false;
   rx::DevBuf d_slot_n, d_tri_v, d_tri_n, d_tri_obj, d_objects, d_light_cdf, d_light_tri;

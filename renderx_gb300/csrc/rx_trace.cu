@@ -91,7 +91,7 @@ struct HitLane {
       const float4* tp = A.tris + 3 * (size_t)(first + k);
       float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
       float t;
-      if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
+      if (tri_exact_n(f3(v0), f3(v1), f3(v2), A.tri_nrm + first + k, o, d, t)) {
         uint32_t lf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
         if (!best.hit || t < best.t || (t == best.t && (lf > best.leaf || (lf == best.leaf && pos < best.pos)))) {
           best = {__float_as_int(v0.w), t, lf, pos, true};
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevAccel A, const rx_r
           const float4* tp = A.tris + 3 * (size_t)(first + k);
           float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
           float t;
-          if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
+          if (tri_exact_n(f3(v0), f3(v1), f3(v2), A.tri_nrm + first + k, o, d, t)) {
             uint32_t leaf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
             if (!best.hit || t < best.t ||
                 (t == best.t && (leaf > best.leaf || (leaf == best.leaf && pos < best.pos)))) {
@@ -539,6 +539,23 @@ cudaError_t launch_trace_closest(const DevAccel& A, const rx_ray* rays, uint32_t
   if (ev) cudaEventRecord(ev[2], s);
   k_trace_eager<<<cfg.sms, 128, 0, s>>>(A, rays, tid, dist, eager, counters);
   if (ev) cudaEventRecord(ev[3], s);
+  return cudaGetLastError();
+}
+
+// The triangle test's unit normal per slot, by the test's own functions (so the bits
+// are those the test would form: IEEE operations, never contracted).
+__global__ void k_slot_normals(const float4* __restrict__ tris, uint32_t nslots, float4* __restrict__ nrm) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nslots; i += gridDim.x * blockDim.x) {
+    const float4* tp = tris + 3 * (size_t)i;
+    const F3 v0 = f3(tp[0]), v1 = f3(tp[1]), v2 = f3(tp[2]);
+    const F3 n = xnormalize(xcross(xsub(v1, v0), xsub(v2, v1)));
+    nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
+  }
+}
+
+cudaError_t launch_slot_normals(const float4* tris, uint32_t nslots, float4* nrm, cudaStream_t s) {
+  if (nslots == 0) return cudaSuccess;
+  k_slot_normals<<<(nslots + 255) / 256 < 4096 ? (nslots + 255) / 256 : 4096, 256, 0, s>>>(tris, nslots, nrm);
   return cudaGetLastError();
 }
 

@@ -112,7 +112,7 @@ __device__ __forceinline__ HitResult trace_ref_exact(const DevAccel& A, F3 o, F3
         const float4* tp = A.tris + 3 * (size_t)(first + k);
         float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
         float t;
-        if (tri_exact(f3(v0), f3(v1), f3(v2), o, d, t)) {
+        if (tri_exact_n(f3(v0), f3(v1), f3(v2), A.tri_nrm + first + k, o, d, t)) {
           uint32_t leaf = __float_as_uint(v1.w), pos = __float_as_uint(v2.w);
           bool better = !best.hit || t < best.t || (t == best.t && (leaf > best.leaf || (leaf == best.leaf && pos < best.pos)));
           if (EAGER && better) better = ref_visible(A, leaf, o, d, inv, zero_dir, n_exact);
