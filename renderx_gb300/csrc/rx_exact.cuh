@@ -115,12 +115,24 @@ __device__ __forceinline__ bool box_exact(F3 mn, F3 mx, F3 o, F3 d) {
   return false;
 }
 
+// The margins of box_clear_pass for one ray: per axis 4e-6 (1 + |o|) and 4e-6 |d|, so
+// that the margin at distance t, 4e-6 (1 + |o| + t |d|), is one fused multiply-add (its
+// rounding moves it by about 1e-7 of itself; the margin is four times the bound it must
+// exceed).
+struct ClearMargins {
+  F3 mo, md;
+};
+__device__ __forceinline__ ClearMargins clear_margins(F3 o, F3 d) {
+  return {{4e-6f * (1.0f + fabsf(o.x)), 4e-6f * (1.0f + fabsf(o.y)), 4e-6f * (1.0f + fabsf(o.z))},
+          {4e-6f * fabsf(d.x), 4e-6f * fabsf(d.y), 4e-6f * fabsf(d.z)}};
+}
+
 // Decides the reference box test cheaply when the answer is clear: the ray's entry
 // (or exit) face point lies inside that face with a margin that exceeds the
 // reference's rounding error (< 8 ulp of |o|+|t d| per coordinate); the sign of the
 // face distance is exact because both sides form fl(b - o) and divide by d's sign.
 // Returns 1 = passes, 0 = undecided (caller runs box_exact).
-__device__ __forceinline__ int box_clear_pass(F3 mn, F3 mx, F3 o, F3 d, F3 inv) {
+__device__ __forceinline__ int box_clear_pass(F3 mn, F3 mx, F3 o, F3 d, F3 inv, const ClearMargins& m) {
   float t0x = __fmul_rn(__fsub_rn(mn.x, o.x), inv.x), t1x = __fmul_rn(__fsub_rn(mx.x, o.x), inv.x);
   float t0y = __fmul_rn(__fsub_rn(mn.y, o.y), inv.y), t1y = __fmul_rn(__fsub_rn(mx.y, o.y), inv.y);
   float t0z = __fmul_rn(__fsub_rn(mn.z, o.z), inv.z), t1z = __fmul_rn(__fsub_rn(mx.z, o.z), inv.z);
@@ -134,10 +146,8 @@ __device__ __forceinline__ int box_clear_pass(F3 mn, F3 mx, F3 o, F3 d, F3 inv) 
     // the face's axis (any axis that attains t: each is a face the ray meets at t), then
     // the point on it inside the other two slabs with the margin, all three axes at once
     const int a = f == 0 ? (nx == t ? 0 : (ny == t ? 1 : 2)) : (fx == t ? 0 : (fy == t ? 1 : 2));
-    const float tdx = t * d.x, tdy = t * d.y, tdz = t * d.z;
-    const float px = o.x + tdx, py = o.y + tdy, pz = o.z + tdz;
-    const float dx = 4e-6f * (1.0f + fabsf(o.x) + fabsf(tdx)), dy = 4e-6f * (1.0f + fabsf(o.y) + fabsf(tdy));
-    const float dz = 4e-6f * (1.0f + fabsf(o.z) + fabsf(tdz));
+    const float px = o.x + t * d.x, py = o.y + t * d.y, pz = o.z + t * d.z;
+    const float dx = fmaf(t, m.md.x, m.mo.x), dy = fmaf(t, m.md.y, m.mo.y), dz = fmaf(t, m.md.z, m.mo.z);
     const bool inx = (px >= mn.x + dx) && (px <= mx.x - dx), iny = (py >= mn.y + dy) && (py <= mx.y - dy);
     const bool inz = (pz >= mn.z + dz) && (pz <= mx.z - dz);
     if ((inx || a == 0) && (iny || a == 1) && (inz || a == 2)) return 1;

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
     const float4* rp = reinterpret_cast<const float4*>(rays + i);
     F3 o = f3(__ldg(rp)), d = f3(__ldg(rp + 1));
     F3 inv = safe_inv(d);
+    const ClearMargins mg = clear_margins(o, d);
     bool zd = (d.x == 0.0f) | (d.y == 0.0f) | (d.z == 0.0f);
     uint32_t b = __ldg(&A.anc_range[2 * leaf]), e = __ldg(&A.anc_range[2 * leaf + 1]);
     bool ok = true;
@@ -38,7 +39,7 @@ __global__ void __launch_bounds__(128) k_check_visible(DevAccel A, const rx_ray*
       if (k < e) {
         int node = __ldg(&A.anc_nodes[k]);
         float4 lo = __ldg(&A.ref[2 * node]), hi = __ldg(&A.ref[2 * node + 1]);
-        if (zd || !box_clear_pass(f3(lo), f3(hi), o, d, inv)) {
+        if (zd || !box_clear_pass(f3(lo), f3(hi), o, d, inv, mg)) {
           n_exact++;
           pass = box_exact(f3(lo), f3(hi), o, d);
         }

@@ -28,6 +28,7 @@ constexpr int kStack = kStackDepth;
 __device__ __forceinline__ bool ref_visible(const DevAccel& A, uint32_t leaf, F3 o, F3 d, F3 inv, bool zero_dir,
                                             unsigned* n_exact) {
   uint32_t b = __ldg(&A.anc_range[2 * leaf]), e = __ldg(&A.anc_range[2 * leaf + 1]);
+  const ClearMargins mg = clear_margins(o, d);
   for (uint32_t k = b; k < e; k += 4) {
     float4 lo[4], hi[4];
 #pragma unroll
@@ -39,7 +40,7 @@ __device__ __forceinline__ bool ref_visible(const DevAccel& A, uint32_t leaf, F3
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       if (k + j >= e) continue;
-      if (zero_dir || !box_clear_pass(f3(lo[j]), f3(hi[j]), o, d, inv)) {
+      if (zero_dir || !box_clear_pass(f3(lo[j]), f3(hi[j]), o, d, inv, mg)) {
         (*n_exact)++;
         if (!box_exact(f3(lo[j]), f3(hi[j]), o, d)) return false;
       }
