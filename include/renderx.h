@@ -301,8 +301,11 @@ rx_status rx_set_snapshots(rx_context* ctx, double every_s, rx_snapshot_fn fn, v
 /* ---- closest hit --------------------------------------------------------------- */
 /* KDTree::intersect(ray, triangleID, NULL) (reference include/KDTree.h:50,
  * src/KDTree.cpp:335-339) over a batch, host buffers: out_tid[i] = global triangle id
- * or -1, out_dist[i] = hit distance or -1. Up to 2^24 rays are copied and traced as one
- * batch; larger inputs are pipelined in chunks of 2^24 over two streams. */
+ * or -1, out_dist[i] = hit distance or -1. The rays go to the device in chunks that ramp
+ * up to rx_trace_set_staging's size (2^22 by default) through three device slots: the
+ * copies in and out overlap other chunks' kernels, and each slot's kernels run on a
+ * stream of their own. Returns when the answers are in host memory (page-locked host
+ * buffers give the full copy rate). */
 rx_status rx_trace_closest(rx_context* ctx, const rx_ray* rays, uint32_t n, int32_t* out_tid, float* out_dist);
 /* Same on device buffers (no copies), enqueued on `stream` (a cudaStream_t, NULL for
  * the context's stream). */
